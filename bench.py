@@ -1,0 +1,274 @@
+"""Benchmark: particle-steps/s of the superellipsoid timestep on one GB300.
+
+A step is one full timestep (collider gate and pass when triggered, narrowphase + contact
+law, force reduction, integration) of a seeded synthetic assembly already resident in HBM.
+Prints one JSON line.  ``--impl reference`` times the CPU restatement of the reference (the
+oracle, OpenMP over all host cores) on the same workload instead.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s on 1 GB300, mixed/batched vs plain FP64 at stated force error"
+UNIT = "particle-steps/s"
+
+# HBM bytes one launch of the contact kernel must move (each item once): per body the
+# state it gathers (pos 24, ori 32, vel 24, angVel 24, shape 48, info 16, bounds 48) and per
+# table entry the history it reads (ids+flags 12, angle 16, depth 8, normal 24, shear 24,
+# phys 24) and the fields it writes (flags 4, depth 8, angle 16, normal 24, contact point 24,
+# shear 24, normal force 24, force 24).
+BYTES_PER_BODY = 216
+BYTES_PER_PAIR = 108 + 148
+
+
+def workload_spec(name, seed):
+    from sudodem_gb300 import assemblies
+    if name == "sq200k_walled":
+        # 200,000 superellipsoids with the size distribution of the plain-vs-mixed config
+        # (half-axes U[0.8,1.2] mm, eps1/eps2 U[0.3,1.8]) deposited in a walled box.
+        return assemblies.deposition_box(200_000, seed=seed, eps_range=(0.3, 1.8))
+    if name == "sq1k_config0":
+        return assemblies.config0(seed=seed)
+    if name.startswith("sq") and name.endswith("_walled"):
+        n = int(float(name[2:-7].replace("k", "e3").replace("m", "e6")))
+        return assemblies.deposition_box(n, seed=seed, eps_range=(0.3, 1.8))
+    raise SystemExit(f"unknown workload {name}")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1])); mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names[1:], parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic_per_pair():
+    """dram bytes per table entry of one k_contacts launch from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_contacts_sq200k.txt")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        if ln.startswith("dram_bytes_per_entry:"):
+            return float(ln.split(":")[1])
+    return None
+
+
+def cpu_baseline(spec, budget_s=20.0, threads=None):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import OracleScene
+    threads = threads or os.cpu_count()
+    o = OracleScene.from_spec(spec, threads=threads)
+    o.step(1)
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        o.step(1)
+        n += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or n >= 50:
+            break
+    np_ = spec.n_particles
+    return {"value": np_ * n / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"CPU oracle, {n} timesteps of the same {np_}-particle assembly after 1 warm-up step, "
+                      f"{threads} OpenMP threads, {el:.1f} s"}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    import torch
+    rank = int(os.environ["RANK"])
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
+    dist.init_process_group("nccl")
+    return rank, ws, dist
+
+
+def run_reference(args):
+    rank, ws, dist = dist_setup()
+    if rank != 0:
+        return
+    spec = workload_spec(args.workload, args.seed)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import OracleScene
+    threads = os.cpu_count()
+    o = OracleScene.from_spec(spec, threads=threads)
+    o.step(max(1, min(args.warmup, 3)))
+    budget = 120.0
+    t0 = time.perf_counter()
+    n = 0
+    while n < args.steps:
+        o.step(1)
+        n += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    v = spec.n_particles * n / el
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": n, "warmup": args.warmup,
+            "ms_per_step": 1e3 * el / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "particles": spec.n_particles, "precision": "fp64"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{n} timesteps of the full workload (time budget {budget:.0f} s)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    rank, ws, dist = dist_setup()
+    from sudodem_gb300 import Engine
+    spec = workload_spec(args.workload, args.seed + rank)
+    eng = Engine(device=0, precision=args.precision, contacts_per_body=args.contacts_per_body)
+    eng.load(spec)
+    npart = spec.n_particles
+    eng.step(args.warmup)
+    eng.sync()
+    # timed region: K graph-replayed timesteps, CUDA events on the engine stream
+    l0 = eng.launch_count()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    if dist:
+        dist.barrier()
+    clocks.start()
+    ms = eng.time_steps(args.steps)
+    rep = eng.sync()
+    clk = clocks.stop()
+    launches = eng.launch_count() - l0
+    if dist:
+        import torch
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * npart * args.steps / (ms / 1e3)
+    nentries = len(eng.interactions(True))
+    # per-stage device times from eager launches (events on the engine stream)
+    eng.set_use_graph(False)
+    k2 = 3
+    eng.step(k2)
+    st = eng.stage_times()
+    eng.sync()
+    eng.set_use_graph(True)
+    contacts_ms = st[1] / k2
+    peak, peak_kind = measured_peaks()
+    alg_bytes = BYTES_PER_BODY * spec.n_bodies + BYTES_PER_PAIR * nentries
+    achieved = alg_bytes / (contacts_ms / 1e3) / 1e9
+    tpp = profiled_traffic_per_pair()
+    roofline = {"bound": "hbm", "kernel": "k_contacts", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": (tpp * nentries) if tpp else None,
+                "algorithmic_bytes": alg_bytes, "launch_ms": contacts_ms,
+                "stage_ms_per_step": {"collider": st[0] / k2, "contacts": st[1] / k2, "integrate": st[2] / k2},
+                "note": "FP64-issue bound on GB300 (transcendental-heavy LM narrowphase); HBM fraction stated for the contact kernel"}
+    # end to end through the C ABI with pinned host buffers
+    import torch
+    kin = eng.kinematics()
+    hin = torch.empty((spec.n_bodies, 16), dtype=torch.float64, pin_memory=True)
+    hout = torch.empty((spec.n_bodies, 16), dtype=torch.float64, pin_memory=True)
+    hin.numpy()[:] = kin
+    e2e_steps = max(3, min(args.steps, 20))
+    ems = eng.time_e2e(e2e_steps, hin.data_ptr(), hout.data_ptr())
+    e2e = {"value": npart * e2e_steps / (ems / 1e3) * ws, "unit": UNIT,
+           "h2d_bytes_per_step": 128 * spec.n_bodies, "d2h_bytes_per_step": 128 * spec.n_bodies}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(spec, budget_s=args.cpu_budget)
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+                "data": "synthetic",
+                "config": {"workload": args.workload, "particles": npart, "bodies": spec.n_bodies,
+                           "table_entries": nentries, "precision": args.precision, "parallelism": "replicas",
+                           "l2": f"inputs larger than L2: contact table {nentries} entries x >= 256 B"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
+                "report": rep}
+        print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="sq200k_walled")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--contacts-per-body", type=int, default=16)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

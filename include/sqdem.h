@@ -1,0 +1,182 @@
+/* sqdem.h — C ABI of libsqdem_gpu.so, the GB300 (sm_103a) engine for SudoDEM3D's
+ * superellipsoid per-timestep path.
+ *
+ * One context = one GPU scene (bodies, materials, contact table, collider state) living
+ * in device memory.  A call to sqdem_step() advances it by whole timesteps with the same
+ * engine sequence a SudoDEM3D script builds with
+ *
+ *   O.engines = [ForceResetter(),
+ *                InsertionSortCollider([Bo1_Superquadrics_Aabb(), Bo1_Wall_Aabb()], verletDist=...),
+ *                InteractionLoop([Ig2_Wall_Superquadrics_SuperquadricsGeom(),
+ *                                 Ig2_Superquadrics_Superquadrics_SuperquadricsGeom()],
+ *                                [Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys()],
+ *                                [SuperquadricsLaw()]),
+ *                NewtonIntegrator(damping=..., gravity=..., isSuperquadrics=1)]
+ *
+ * Conventions: plain pointers and sizes, no exceptions across the ABI, every call returns
+ * an sqdem_status; host buffers are owned by the caller, device buffers by the library.
+ * Body ids are the reference's Body::id (walls and particles share one id space).
+ *
+ * Reference interfaces replaced (paths relative to the SudoDEM repository root):
+ *   Scene::moveToNextTimeStep                 SudoDEM3D/core/Scene.cpp:70-138
+ *   Engine::action (the four engines above)   SudoDEM3D/core/Engine.hpp:33-34
+ *   BoundFunctor::go / IGeomFunctor::go /
+ *   IPhysFunctor::go / LawFunctor::go         SudoDEM3D/pkg/common/Dispatching.hpp:19-71
+ *   O.bodies / O.interactions / O.forces      SudoDEM3D/py/wrapper/sudodemWrapper.cpp:937-987
+ */
+#ifndef SQDEM_H
+#define SQDEM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sqdem_ctx sqdem_ctx;
+
+typedef enum {
+  SQDEM_OK = 0,
+  SQDEM_ERR_ARG = 1,      /* bad argument (size, pointer, range) */
+  SQDEM_ERR_CUDA = 2,     /* a CUDA runtime call failed; see sqdem_last_error */
+  SQDEM_ERR_CAPACITY = 3, /* contact table / candidate buffer overflow; state not advanced past it */
+  SQDEM_ERR_STATE = 4,    /* call out of order (e.g. step before bodies are set) */
+  SQDEM_ERR_NUMERIC = 5   /* NaN depth met (the reference calls exit(1), Superquadrics.cpp:1352) */
+} sqdem_status;
+
+/* Body kinds. */
+enum { SQDEM_SUPERQUADRIC = 0, SQDEM_WALL = 1 };
+
+/* Arithmetic form of the narrowphase. */
+enum { SQDEM_FP64 = 0, SQDEM_MIXED = 1 };
+
+typedef struct {
+  int device;              /* CUDA device ordinal */
+  int precision;           /* SQDEM_FP64 or SQDEM_MIXED */
+  int contacts_per_body;   /* contact-table capacity per particle (0 -> 16) */
+  int use_graph;           /* capture the timestep in a CUDA graph (1) or launch eagerly (0) */
+} sqdem_config;
+
+/* Engine attributes, named as in the reference:
+ *   NewtonIntegrator.{damping,gravity,isSuperquadrics,exactAsphericalRot}  NewtonIntegrator.hpp:70-89
+ *   InsertionSortCollider.{verletDist,targetInterv,minSweepDistFactor,sortAxis}
+ *                                                       InsertionSortCollider.hpp:212-222
+ *   Scene.dt                                            core/Scene.hpp */
+typedef struct {
+  double dt;
+  double gravity[3];
+  double damping;
+  double verletDist;
+  int targetInterv;
+  double minSweepDistFactor;
+  int sortAxis;
+  int isSuperquadrics;
+  int exactAsphericalRot;
+} sqdem_params;
+
+/* Per-step error words read back by sqdem_sync (the reference logs NaN normals/forces to
+ * SuperquadricsLaw_err.log, Superquadrics_Ig2.cpp:2165-2188, Superquadrics.cpp:1324-1350). */
+typedef struct {
+  long long nan_normals;      /* NaN contact normals met by the narrowphase */
+  long long nan_forces;       /* NaN forces zeroed by the contact law */
+  long long lm_calls;         /* Levenberg-Marquardt solves */
+  long long lm_iterations;    /* summed LM iterations */
+  long long lm_maxiter;       /* solves that hit itmax (stop code 3) */
+  long long overflow;         /* contact-table or candidate-buffer overflows */
+  long long collider_runs;    /* collider passes executed */
+  long long steps;            /* timesteps executed */
+} sqdem_report;
+
+/* Record layouts shared with the CPU oracle (doubles per record). */
+#define SQDEM_BODY_STRIDE 37
+/* pos3 ori4(w,x,y,z) vel3 angVel3 angMom3 force3 torque3 bmin3 bmax3 refPos3
+   sweepLength lastUpdateIter mass inertia3 */
+#define SQDEM_INTR_STRIDE 44
+/* id1 id2 isReal hasGeom depth contactAngle2 contactPoint3 normal3 shearInc3 point1_3 point2_3
+   isShearNew kn ks tanphi normalForce3 shearForce3 twist3 orthonormal3 relVn3 relVs3 */
+#define SQDEM_SCALARS 9
+/* iter maxVelocitySq fastestBodyMaxDist strideActive newtonFound verletDist numReinit colliderRuns
+   sortedBoundsValid (0: the next collider pass is a full sort, InsertionSortCollider.cpp:213-222) */
+
+/* Create a context on cfg->device.  Replaces building a Scene (core/Scene.hpp). */
+sqdem_status sqdem_create(sqdem_ctx** out, const sqdem_config* cfg);
+void sqdem_destroy(sqdem_ctx* ctx);
+/* Last error text of this context (static storage valid until the next call). */
+const char* sqdem_last_error(sqdem_ctx* ctx);
+
+/* Materials, SuperquadricsMat{Kn,Ks,frictionAngle,betan,betas,density}
+ * (pkg/dem/Superquadrics.hpp:247-264).  Index i is the material id used below. */
+sqdem_status sqdem_set_materials(sqdem_ctx* ctx, int n, const double* Kn, const double* Ks,
+                                 const double* frictionAngle, const double* betan,
+                                 const double* betas, const double* density);
+
+/* All bodies in reference id order.  kind[i] is SQDEM_SUPERQUADRIC or SQDEM_WALL.
+ * shape5 = (rx,ry,rz,eps1,eps2) for superquadrics (ignored for walls); wall = (axis,sense)
+ * (ignored for particles); state = SQDEM_BODY_STRIDE doubles per body (force/torque and bound
+ * columns are ignored: bounds start unset, as after NewSuperquadrics_rot2 and utils.wall,
+ * py/_superquadrics_utils.cpp:354-380, py/utils.py:311-327).  Mass and inertia are taken
+ * from the state columns; sqdem_shape_props gives the reference's values. */
+sqdem_status sqdem_set_bodies(sqdem_ctx* ctx, int n, const int* kind, const double* shape5,
+                              const int* wall_axis_sense, const int* mat, const int* isSphere,
+                              const double* state);
+sqdem_status sqdem_set_params(sqdem_ctx* ctx, const sqdem_params* p);
+
+/* Advance nsteps timesteps (asynchronous on the context stream). */
+sqdem_status sqdem_step(sqdem_ctx* ctx, int nsteps);
+/* Wait for the stream, read and clear the error words.  report may be NULL. */
+sqdem_status sqdem_sync(sqdem_ctx* ctx, sqdem_report* report);
+
+/* Body state in the SQDEM_BODY_STRIDE layout (O.bodies[i].state, O.forces). */
+sqdem_status sqdem_get_body_state(sqdem_ctx* ctx, double* out);
+/* Overwrite dynamic and bound state from the same layout (mass/inertia/force columns ignored). */
+sqdem_status sqdem_put_body_state(sqdem_ctx* ctx, const double* in);
+/* Same as get/put but only positions, orientations, velocities, angular velocities and
+ * angular momenta (16 doubles per body), for streaming state to and from the host. */
+sqdem_status sqdem_get_kinematics(sqdem_ctx* ctx, double* out16);
+sqdem_status sqdem_put_kinematics(sqdem_ctx* ctx, const double* in16);
+
+/* Interactions (O.interactions): count, then records in the SQDEM_INTR_STRIDE layout.
+ * include_potential = 0 returns only real interactions (geom and phys present). */
+sqdem_status sqdem_num_interactions(sqdem_ctx* ctx, int include_potential, long* n);
+sqdem_status sqdem_get_interactions(sqdem_ctx* ctx, int include_potential, double* out, long cap, long* n);
+/* Replace the contact table (history included) from records. */
+sqdem_status sqdem_put_interactions(sqdem_ctx* ctx, long n, const double* in);
+
+sqdem_status sqdem_get_scalars(sqdem_ctx* ctx, double* out9);
+sqdem_status sqdem_put_scalars(sqdem_ctx* ctx, const double* in9);
+
+/* Record the full contact geometry (point1/2, shearInc, twist/orthonormal axes, relative
+ * velocities of SuperquadricsGeom, Superquadrics.hpp:175-208) every step.  Off by default:
+ * the step then writes only the history the next step needs. */
+sqdem_status sqdem_set_record_full(sqdem_ctx* ctx, int on);
+
+/* Per-stage device time of the last sqdem_step call in milliseconds (cudaEvent pairs on the
+ * context stream; only when the context was created with use_graph == 0):
+ * out[0] collider gate+passes, out[1] contacts (narrowphase+law), out[2] integrator+reductions. */
+sqdem_status sqdem_stage_times(sqdem_ctx* ctx, double* out3);
+
+/* Replay the timestep as a CUDA graph (on = 1, default) or launch its kernels one by one with
+ * per-stage event timing readable through sqdem_stage_times (on = 0). */
+sqdem_status sqdem_set_use_graph(sqdem_ctx* ctx, int on);
+
+/* Timing entry points (cudaEvents on the context stream).
+ * sqdem_time_steps: nsteps timesteps, device milliseconds in *ms.
+ * sqdem_time_e2e:   nsteps x (upload 16 doubles/body from in16, one timestep, download to out16),
+ *                   the end-to-end path of a host caller; use pinned host buffers.
+ * sqdem_time_contacts: one launch of the narrowphase+law kernel, averaged over nrep launches. */
+sqdem_status sqdem_time_steps(sqdem_ctx* ctx, int nsteps, double* ms);
+sqdem_status sqdem_time_e2e(sqdem_ctx* ctx, int nsteps, const double* in16, double* out16, double* ms);
+sqdem_status sqdem_time_contacts(sqdem_ctx* ctx, int nrep, double* ms);
+
+/* Superquadrics::Initial (pkg/dem/Superquadrics.cpp:47-93): volume, geometric inertia (3),
+ * bounding radius r_max, for unit density.  Host-only helper. */
+sqdem_status sqdem_shape_props(double rx, double ry, double rz, double eps1, double eps2, double* out5);
+
+/* Number of kernel launches issued by the last sqdem_step call. */
+long long sqdem_launch_count(sqdem_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

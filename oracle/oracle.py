@@ -1,0 +1,197 @@
+"""ctypes wrapper of the CPU oracle (oracle/sqdem_oracle.cpp).
+
+Test infrastructure only: imported by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline.  Parity of the oracle against the reference is unpinned (the reference cannot be
+built here and ships no golden data for this path); see the header of sqdem_oracle.cpp.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "libsqdem_oracle.so")
+BODY_STRIDE = 37
+INTR_STRIDE = 44
+
+_lib = None
+
+
+def build(force=False):
+    src = os.path.join(HERE, "sqdem_oracle.cpp")
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-B" if force else "-s", "-C", HERE], check=True)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    build()
+    L = C.CDLL(LIB)
+    d, i, l, v = C.c_double, C.c_int, C.c_long, C.c_void_p
+    dp = C.POINTER(d)
+    sig = {
+        "sqo_create": (v, []), "sqo_destroy": (None, [v]), "sqo_set_threads": (None, [v, i]),
+        "sqo_add_material": (i, [v, d, d, d, d, d, d]),
+        "sqo_add_wall": (i, [v, dp, i, i, i]),
+        "sqo_add_sq": (i, [v, d, d, d, d, d, i, dp, i, dp]),
+        "sqo_set_params": (None, [v, d, dp, d, d, i, d, i]),
+        "sqo_step": (None, [v, i]), "sqo_collide": (i, [v]), "sqo_last_step_collided": (i, [v]),
+        "sqo_iter": (l, [v]), "sqo_num_bodies": (i, [v]), "sqo_num_interactions": (l, [v]),
+        "sqo_stats": (None, [v, C.POINTER(l)]), "sqo_max_velocity_sq": (d, [v]),
+        "sqo_get_bodies": (None, [v, dp]), "sqo_set_bodies": (None, [v, dp]),
+        "sqo_get_interactions": (None, [v, dp]), "sqo_set_interactions": (None, [v, l, dp]),
+        "sqo_get_scalars": (None, [v, dp]), "sqo_set_scalars": (None, [v, dp]),
+        "sqo_rebuild_sorted_bounds": (None, [v]),
+        "sqo_pair_geom": (i, [v, i, i, i, dp, dp]),
+        "sqo_shape_props": (None, [d, d, d, d, d, dp]),
+        "sqo_surface": (None, [d, d, d, d, d, d, d, dp]),
+        "sqo_normal": (None, [d, d, d, d, d, d, d, dp]),
+        "sqo_normal2phi": (None, [d, d, d, d, d, dp, dp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def shape_props(rx, ry, rz, e1, e2):
+    out = np.zeros(5)
+    lib().sqo_shape_props(rx, ry, rz, e1, e2, _dp(out))
+    return out
+
+
+def surface(shape5, ph0, ph1):
+    out = np.zeros(3)
+    lib().sqo_surface(*[float(x) for x in shape5], ph0, ph1, _dp(out))
+    return out
+
+
+def normal(shape5, ph0, ph1):
+    out = np.zeros(3)
+    lib().sqo_normal(*[float(x) for x in shape5], ph0, ph1, _dp(out))
+    return out
+
+
+def normal2phi(shape5, n):
+    out = np.zeros(2)
+    n = np.ascontiguousarray(n, dtype=np.float64)
+    lib().sqo_normal2phi(*[float(x) for x in shape5], _dp(n), _dp(out))
+    return out
+
+
+class OracleScene:
+    """A reference-semantics scene on the CPU."""
+
+    def __init__(self, threads=1):
+        self.L = lib()
+        self.h = self.L.sqo_create()
+        self.L.sqo_set_threads(self.h, threads)
+
+    def close(self):
+        if self.h:
+            self.L.sqo_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @classmethod
+    def from_spec(cls, spec, threads=1):
+        o = cls(threads)
+        m = spec.materials
+        for k in range(len(m["Kn"])):
+            o.L.sqo_add_material(o.h, m["Kn"][k], m["Ks"][k], m["frictionAngle"][k], m["betan"][k], m["betas"][k],
+                                 m["density"][k])
+        for i in range(spec.n_bodies):
+            st = spec.state[i]
+            pos = np.ascontiguousarray(st[0:3])
+            if spec.kind[i] == 1:
+                o.L.sqo_add_wall(o.h, _dp(pos), int(spec.wall_axis_sense[i, 0]), int(spec.wall_axis_sense[i, 1]),
+                                 int(spec.mat[i]))
+            else:
+                q = np.ascontiguousarray(st[3:7])
+                s = spec.shape5[i]
+                o.L.sqo_add_sq(o.h, s[0], s[1], s[2], s[3], s[4], int(spec.mat[i]), _dp(q), int(spec.isSphere[i]),
+                               _dp(pos))
+        p = spec.params
+        g = np.ascontiguousarray(p["gravity"], dtype=np.float64)
+        o.L.sqo_set_params(o.h, p["dt"], _dp(g), p["damping"], p["verletDist"], int(p["targetInterv"]),
+                           p["minSweepDistFactor"], int(p["sortAxis"]))
+        o.n = spec.n_bodies
+        # velocities from the spec (the factory leaves them zero)
+        if np.any(spec.state[:, 7:16] != 0):
+            b = o.bodies()
+            b[:, 7:16] = spec.state[:, 7:16]
+            o.set_bodies(b)
+        return o
+
+    def step(self, n=1):
+        self.L.sqo_step(self.h, int(n))
+
+    def collide(self):
+        return self.L.sqo_collide(self.h)
+
+    def last_step_collided(self):
+        return bool(self.L.sqo_last_step_collided(self.h))
+
+    @property
+    def iter(self):
+        return self.L.sqo_iter(self.h)
+
+    def bodies(self):
+        n = self.L.sqo_num_bodies(self.h)
+        out = np.zeros((n, BODY_STRIDE))
+        self.L.sqo_get_bodies(self.h, _dp(out))
+        return out
+
+    def set_bodies(self, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        self.L.sqo_set_bodies(self.h, _dp(b))
+
+    def interactions(self):
+        n = self.L.sqo_num_interactions(self.h)
+        out = np.zeros((max(n, 1), INTR_STRIDE))
+        if n:
+            self.L.sqo_get_interactions(self.h, _dp(out))
+        return out[:n]
+
+    def set_interactions(self, recs):
+        recs = np.ascontiguousarray(recs, dtype=np.float64).reshape(-1, INTR_STRIDE)
+        self.L.sqo_set_interactions(self.h, len(recs), _dp(recs))
+
+    def scalars(self):
+        out = np.zeros(9)
+        self.L.sqo_get_scalars(self.h, _dp(out))
+        return out
+
+    def set_scalars(self, s):
+        s = np.ascontiguousarray(s, dtype=np.float64)
+        self.L.sqo_set_scalars(self.h, _dp(s))
+
+    def rebuild_sorted_bounds(self):
+        self.L.sqo_rebuild_sorted_bounds(self.h)
+
+    def stats(self):
+        out = (C.c_long * 5)()
+        self.L.sqo_stats(self.h, out)
+        return dict(zip(("lm_calls", "lm_iterations", "dis_calls", "restarts", "nan_normals"), list(out)))
+
+    def pair_geom(self, ia, ib, prior=None):
+        out = np.zeros(15)
+        pr = np.zeros(4) if prior is None else np.ascontiguousarray(prior, dtype=np.float64)
+        it = self.L.sqo_pair_geom(self.h, ia, ib, 1 if prior is None else 0, _dp(pr), _dp(out))
+        return {"depth": out[0], "normal": out[1:4], "contactPoint": out[4:7], "point1": out[7:10],
+                "point2": out[10:13], "contactAngle": out[13:15], "lm_iterations": it}

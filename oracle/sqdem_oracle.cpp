@@ -1,0 +1,1187 @@
+// SudoDEM3D superellipsoid per-timestep path — CPU ORACLE (test infrastructure only).
+//
+// This file is a C++17/FP64 restatement of the reference's hot path, written to
+// check the GPU engine.  It is never shipped or called by the product path: only
+// tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm load
+// it.  Each function cites the reference file:line it follows (paths are relative
+// to the SudoDEM repository root).
+//
+// Parity status: the reference itself cannot be compiled here (Boost.Python and a
+// prebuilt third-party tree are required by SudoDEM3D/lib/base/Math.hpp:10,57-72 and
+// SudoDEM3D/CMakeLists.txt:6,73), and the reference ships no test, golden vector or
+// fixture for this path.  Parity of this restatement against the reference is
+// therefore UNPINNED; it is anchored on (a) operation-for-operation restatement of
+// the cited lines, (b) Eigen 3.3.5's evaluation order (vendored in
+// SudoDEM3D/lib/Eigen: unrolled tree reductions, Core/Redux.h:91-122; coefficient
+// products, Core/ProductEvaluators.h:550-553; Quaternion.h:475-485,536-568), and
+// (c) known-answer tests built with the reference's own PositionPB construction
+// (py/_superquadrics_utils.cpp:109-131).
+//
+// Build: -O2 -ffp-contract=off (the reference builds with -O2 and no FMA on x86-64,
+// SudoDEM3D/CMakeLists.txt:64); -fopenmp for the multi-threaded baseline.
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <cfloat>
+#include <vector>
+#include <unordered_map>
+#include <algorithm>
+#include <limits>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace sqo {
+
+typedef double Real;
+static const Real NaN = std::numeric_limits<Real>::quiet_NaN();
+static const Real Inf = std::numeric_limits<Real>::infinity();
+
+// ---------------------------------------------------------------------------
+// Small linear algebra with Eigen 3.3.5 evaluation order.
+// Reductions of length 3 unroll as a0 + (a1 + a2), length 4 as (a0+a1)+(a2+a3)
+// (lib/Eigen/src/Core/Redux.h:91-105).
+struct V3 {
+  Real v[3];
+  V3() { v[0] = v[1] = v[2] = 0; }
+  V3(Real a, Real b, Real c) { v[0] = a; v[1] = b; v[2] = c; }
+  Real& operator[](int i) { return v[i]; }
+  Real operator[](int i) const { return v[i]; }
+};
+static inline V3 operator+(const V3& a, const V3& b) { return V3(a[0] + b[0], a[1] + b[1], a[2] + b[2]); }
+static inline V3 operator-(const V3& a, const V3& b) { return V3(a[0] - b[0], a[1] - b[1], a[2] - b[2]); }
+static inline V3 operator-(const V3& a) { return V3(-a[0], -a[1], -a[2]); }
+static inline V3 operator*(Real s, const V3& a) { return V3(s * a[0], s * a[1], s * a[2]); }
+static inline V3 operator*(const V3& a, Real s) { return V3(a[0] * s, a[1] * s, a[2] * s); }
+static inline Real dot(const V3& a, const V3& b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
+static inline Real sqnorm(const V3& a) { return a[0] * a[0] + (a[1] * a[1] + a[2] * a[2]); }
+static inline Real norm(const V3& a) { return std::sqrt(sqnorm(a)); }
+// Geometry/OrthoMethods.h:34-48
+static inline V3 cross(const V3& a, const V3& b) {
+  return V3(a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]);
+}
+// Core/Dot.h:145-151 (normalize divides by sqrt of the squared norm when positive)
+static inline void normalize(V3& a) {
+  Real z = sqnorm(a);
+  if (z > 0) { Real n = std::sqrt(z); a[0] /= n; a[1] /= n; a[2] /= n; }
+}
+struct M3 { Real m[9]; };
+// Coefficient-based 3x3*3 product: row(i).col.sum() with the tree reduction.
+static inline V3 mul(const M3& M, const V3& x) {
+  return V3(M.m[0] * x[0] + (M.m[1] * x[1] + M.m[2] * x[2]),
+            M.m[3] * x[0] + (M.m[4] * x[1] + M.m[5] * x[2]),
+            M.m[6] * x[0] + (M.m[7] * x[1] + M.m[8] * x[2]));
+}
+struct Quat { Real w, x, y, z; };
+// Geometry/Quaternion.h:536-568
+static inline M3 toRot(const Quat& q) {
+  const Real tx = 2.0 * q.x, ty = 2.0 * q.y, tz = 2.0 * q.z;
+  const Real twx = tx * q.w, twy = ty * q.w, twz = tz * q.w;
+  const Real txx = tx * q.x, txy = ty * q.x, txz = tz * q.x;
+  const Real tyy = ty * q.y, tyz = tz * q.y, tzz = tz * q.z;
+  M3 r;
+  r.m[0] = 1.0 - (tyy + tzz); r.m[1] = txy - twz;         r.m[2] = txz + twy;
+  r.m[3] = txy + twz;         r.m[4] = 1.0 - (txx + tzz); r.m[5] = tyz - twx;
+  r.m[6] = txz - twy;         r.m[7] = tyz + twx;         r.m[8] = 1.0 - (txx + tyy);
+  return r;
+}
+static inline Quat conj(const Quat& q) { return Quat{q.w, -q.x, -q.y, -q.z}; }
+// Quaternion coefficients are stored (x,y,z,w); squaredNorm = (x²+y²)+(z²+w²).
+static inline void qnormalize(Quat& q) {
+  Real z = (q.x * q.x + q.y * q.y) + (q.z * q.z + q.w * q.w);
+  if (z > 0) { Real n = std::sqrt(z); q.x /= n; q.y /= n; q.z /= n; q.w /= n; }
+}
+// Geometry/Quaternion.h:475-485 (_transformVector)
+static inline V3 qrotate(const Quat& q, const V3& v) {
+  V3 qv(q.x, q.y, q.z);
+  V3 uv = cross(qv, v);
+  uv = uv + uv;
+  V3 c = cross(qv, uv);
+  return V3((v[0] + q.w * uv[0]) + c[0], (v[1] + q.w * uv[1]) + c[1], (v[2] + q.w * uv[2]) + c[2]);
+}
+
+// lib/base/Math.hpp:186 (Sign(0) == 0)
+static inline Real Sign(Real f) { if (f < 0) return -1; if (f > 0) return 1; return 0; }
+
+// lib/base/Math.hpp:192-212: Lanczos log-gamma (Numerical Recipes 3rd ed., Sect. 6.1)
+// and Beta(z,w) = exp(lnG(z)+lnG(w)-lnG(z+w)).  The 14 coefficients are the published
+// NR3 table, which the reference uses as-is; mass and inertia depend on them.
+static double gammln(const double xx) {
+  static const double cof[14] = {57.1562356658629235, -59.5979603554754912, 14.1360979747417471,
+                                 -0.491913816097620199, .339946499848118887e-4, .465236289270485756e-4,
+                                 -.983744753048795646e-4, .158088703224912494e-3, -.210264441724104883e-3,
+                                 .217439618115212643e-3, -.164318106536763890e-3, .844182239838527433e-4,
+                                 -.261908384015814087e-4, .368991826595316234e-5};
+  double x, tmp, y, ser;
+  y = x = xx;
+  tmp = x + 5.24218750000000000;
+  tmp = (x + 0.5) * std::log(tmp) - tmp;
+  ser = 0.999999999999997092;
+  for (int j = 0; j < 14; j++) ser += cof[j] / ++y;
+  return tmp + std::log(2.5066282746310005 * ser / x);
+}
+static double betaf(const double z, const double w) { return std::exp(gammln(z) + gammln(w) - gammln(z + w)); }
+
+// ---------------------------------------------------------------------------
+// Superquadric shape (pkg/dem/Superquadrics.hpp:48-166, Superquadrics.cpp:29-120,269-307)
+struct SQ {
+  Real rx, ry, rz, eps1, eps2, r_max;
+  bool isSphere;
+  Real volume;
+  V3 inertia;   // geometric (unit density)
+  M3 loc, glob; // rot_mat2local / rot_mat2global cached on the shape
+};
+
+// Superquadrics.cpp:47-93 (Initial)
+static void sqInitial(SQ& s) {
+  s.r_max = (s.rx > s.ry) ? s.rx : s.ry;
+  s.r_max = s.r_max > s.rz ? s.r_max : s.rz;
+  if ((s.eps1 < 1.0) || (s.eps2 < 1.0)) s.r_max *= std::pow(2.0, 0.5);
+  double a = s.rx * s.ry * s.rz * s.eps1 * s.eps2;
+  double beta1 = betaf(1.5 * s.eps1, 0.5 * s.eps1) * betaf(0.5 * s.eps2, 2. * s.eps2 + 1);
+  double beta2 = betaf(0.5 * s.eps1, 0.5 * s.eps1 + 1) * betaf(1.5 * s.eps2, s.eps2 + 1);
+  s.volume = 2. * a * betaf(s.eps1 * 0.5, s.eps1 * 0.5) * betaf(s.eps2 * 0.5 + 1, s.eps2);
+  s.inertia[0] = 0.5 * a * (std::pow(s.ry, 2.) * beta1 + 4. * std::pow(s.rz, 2.) * beta2);
+  s.inertia[1] = 0.5 * a * (std::pow(s.rx, 2.) * beta1 + 4. * std::pow(s.rz, 2.) * beta2);
+  s.inertia[2] = 0.5 * a * (std::pow(s.rx, 2.) + std::pow(s.ry, 2.)) * beta1;
+}
+
+// Superquadrics.cpp:103-108
+static bool sqIsInside(const SQ& s, V3 p) {
+  p = mul(s.loc, p);
+  return 1 > std::pow(std::pow(std::fabs(p[0] / s.rx), 2.0 / s.eps1) + std::pow(std::fabs(p[1] / s.ry), 2.0 / s.eps1),
+                      s.eps1 / s.eps2) + std::pow(std::fabs(p[2] / s.rz), 2.0 / s.eps2);
+}
+// Superquadrics.cpp:110-120 (local surface point from the two surface angles)
+static inline V3 sqSurface(const SQ& s, Real ph0, Real ph1) {
+  V3 r;
+  r[0] = Sign(std::cos(ph0)) * s.rx * std::pow(std::fabs(std::cos(ph0)), s.eps1) * std::pow(std::fabs(std::cos(ph1)), s.eps2);
+  r[1] = Sign(std::sin(ph0)) * s.ry * std::pow(std::fabs(std::sin(ph0)), s.eps1) * std::pow(std::fabs(std::cos(ph1)), s.eps2);
+  r[2] = Sign(std::sin(ph1)) * s.rz * std::pow(std::fabs(std::sin(ph1)), s.eps2);
+  return r;
+}
+// Superquadrics.cpp:269-307 (surface angles of the point whose outward normal is n, local frame)
+static inline void sqNormal2Phi(const SQ& s, const V3& n, Real& ph0, Real& ph1) {
+  ph0 = std::atan2(Sign(n[1]) * std::pow(std::fabs(s.ry * n[1]), 1 / (2. - s.eps1)),
+                   Sign(n[0]) * std::pow(std::fabs(s.rx * n[0]), 1 / (2. - s.eps1)));
+  ph1 = std::atan2(Sign(n[2]) * std::pow(std::fabs(s.rz * n[2] * std::pow(std::fabs(std::cos(ph0)), 2. - s.eps1)), 1 / (2. - s.eps2)),
+                   std::pow(std::fabs(s.rx * n[0]), 1 / (2. - s.eps2)));
+}
+// Superquadrics.cpp:258-266 (local, unnormalised outward normal at angles phi)
+static inline V3 sqNormal(const SQ& s, Real ph0, Real ph1) {
+  V3 n;
+  n[0] = Sign(std::cos(ph0)) / s.rx * std::pow(std::fabs(std::cos(ph0)), 2. - s.eps1) * std::pow(std::fabs(std::cos(ph1)), 2. - s.eps2);
+  n[1] = Sign(std::sin(ph0)) / s.ry * std::pow(std::fabs(std::sin(ph0)), 2. - s.eps1) * std::pow(std::fabs(std::cos(ph1)), 2. - s.eps2);
+  n[2] = Sign(std::sin(ph1)) / s.rz * std::pow(std::fabs(std::sin(ph1)), 2. - s.eps2);
+  return n;
+}
+
+// ---------------------------------------------------------------------------
+// Scene data
+enum { KIND_SQ = 0, KIND_WALL = 1 };
+static const unsigned DOF_ALL = 63u;
+
+struct Mat { Real Kn, Ks, frictionAngle, betan, betas, density; };
+
+struct Body {
+  int kind;
+  int axis, sense;    // Wall (pkg/common/Wall.hpp:11-13)
+  SQ sq;
+  int mat;
+  V3 pos; Quat ori; V3 vel, angVel, angMom; Real mass; V3 inertia;
+  unsigned blockedDOFs; bool isDamped; bool aspherical;
+  int groupMask;
+  // Bound (core/Bound.hpp:24-31)
+  bool hasBound; V3 bmin, bmax, refPos; Real sweepLength; long lastUpdateIter;
+};
+
+// SuperquadricsGeom (Superquadrics.hpp:175-208)
+struct Geom {
+  Real PenetrationDepth; Real contactAngle[2];
+  V3 contactPoint, shearInc, relativeVn, relativeVs, normal, twist_axis, orthonormal_axis, point1, point2;
+  bool isShearNew;
+};
+// SuperquadricsPhys : FrictPhys (Superquadrics.hpp:303-321, FrictPhys.hpp:15-25)
+struct Phys { Real kn, ks, tanphi, betan, betas; V3 normalForce, shearForce; };
+
+struct Interaction {
+  int id1, id2;
+  bool hasGeom, hasPhys;
+  bool geomFunctorSet;  // functorCache.geom (core/Interaction.hpp:35-43)
+  bool geomExists;      // functorCache.geomExists
+  Geom g; Phys p;
+  long iterBorn; long linIx; int cellDist[3];
+};
+
+// InsertionSortCollider::Bounds (InsertionSortCollider.hpp:90-109)
+struct Bounds {
+  Real coord; int id; int period; bool hasBB; bool isMin;
+  bool operator<(const Bounds& b) const { if (id == b.id && coord == b.coord) return isMin; return coord < b.coord; }
+  bool operator>(const Bounds& b) const { if (id == b.id && coord == b.coord) return !isMin; return coord > b.coord; }
+};
+
+struct Stats { long lmCalls, lmIters, disCalls, restarts, nanNormals; };
+
+struct Scene {
+  std::vector<Body> bodies;
+  std::vector<Mat> mats;
+  std::vector<Interaction*> lin;                          // InteractionContainer::linIntrs
+  std::unordered_map<uint64_t, Interaction*> byKey;       // Body::intrs maps
+  Real dt = 1e-5; long iter = 0; Real time = 0;
+  // NewtonIntegrator attributes (NewtonIntegrator.hpp:70-89)
+  V3 gravity; Real damping = 0.2; int isSuperquadrics = 1; bool exactAsphericalRot = true;
+  Real maxVelocitySq = NaN;
+  // InsertionSortCollider attributes (InsertionSortCollider.hpp:212-222)
+  Real verletDist = -0.5; int targetInterv = 50; Real minSweepDistFactor = 0.1; int sortAxis = 0;
+  Real updatingDispFactor = -1; Real fastestBodyMaxDist = -1; int numReinit = 0; bool doSort = false;
+  bool strideActive = false; bool newtonFound = false; bool interactionsDirty = false;
+  std::vector<Bounds> BB[3];
+  std::vector<Real> minima, maxima;
+  long colliderRuns = 0; bool lastStepCollided = false;
+  // forces (core/ForceContainer.hpp:44-162)
+  int nThreads = 1;
+  std::vector<std::vector<V3>> fbuf, tbuf;
+  std::vector<V3> force, torque;
+  Stats stats{0, 0, 0, 0, 0};
+  std::vector<Stats> tstats;
+  // user hook between InteractionLoop and NewtonIntegrator (boundary controllers)
+  void (*midHook)(void*) = nullptr; void* midHookArg = nullptr;
+};
+
+static inline uint64_t pairKey(int a, int b) {
+  if (a > b) std::swap(a, b);
+  return (uint64_t(uint32_t(a)) << 32) | uint32_t(b);
+}
+static inline int threadNum() {
+#ifdef _OPENMP
+  return omp_get_thread_num();
+#else
+  return 0;
+#endif
+}
+
+// InteractionContainer::insert (core/InteractionContainer.cpp:13-39)
+static bool icInsert(Scene& S, int id1, int id2) {
+  uint64_t k = pairKey(id1, id2);
+  if (S.byKey.count(k)) return false;
+  Interaction* I = new Interaction();
+  std::memset(I, 0, sizeof(Interaction));
+  I->id1 = id1; I->id2 = id2; I->geomExists = true;
+  I->iterBorn = S.iter;
+  I->linIx = (long)S.lin.size();
+  S.lin.push_back(I);
+  S.byKey[k] = I;
+  return true;
+}
+// InteractionContainer::erase (core/InteractionContainer.cpp:54-93): move the last one into the hole
+static void icEraseAt(Scene& S, long linIx) {
+  Interaction* I = S.lin[linIx];
+  S.byKey.erase(pairKey(I->id1, I->id2));
+  long last = (long)S.lin.size() - 1;
+  if (linIx < last) { S.lin[linIx] = S.lin[last]; S.lin[linIx]->linIx = linIx; }
+  S.lin.pop_back();
+  delete I;
+}
+// Interaction::reset (core/Interaction.cpp:19-29)
+static inline void requestErase(Interaction* I) { I->hasGeom = false; I->hasPhys = false; I->geomExists = true; }
+
+// Collider::mayCollide (pkg/common/Collider.cpp:14-27) for standalone bodies with
+// avoidSelfInteractionMask == 0.
+static inline bool mayCollide(const Body& a, const Body& b) { return (a.groupMask & b.groupMask) != 0; }
+
+// ---------------------------------------------------------------------------
+// BoundDispatcher::processBody (pkg/common/Dispatching.cpp:30-62) with
+// Bo1_Superquadrics_Aabb::go (Superquadrics.cpp:639-686) and Bo1_Wall_Aabb::go (Wall.cpp:13-21)
+static void processBody(Scene& S, Body& b, Real sweepDist) {
+  if (b.hasBound) {
+    Real& sweepLength = b.sweepLength;
+    if (S.targetInterv >= 0) {
+      V3 disp = b.pos - b.refPos;
+      Real dist = std::max(std::abs(disp[0]), std::max(std::abs(disp[1]), std::abs(disp[2])));
+      if (dist) {
+        Real newLength = dist * S.targetInterv / (S.iter - b.lastUpdateIter);
+        newLength = std::max(0.9 * sweepLength, newLength);
+        sweepLength = std::max(S.minSweepDistFactor * sweepDist, std::min(newLength, sweepDist));
+      } else sweepLength = 0;
+    } else sweepLength = sweepDist;
+  }
+  if (b.kind == KIND_SQ) {
+    Real r = b.sq.r_max;
+    b.bmin = b.pos + V3(-r, -r, -r);
+    b.bmax = b.pos + V3(r, r, r);
+  } else {
+    b.bmin = V3(-Inf, -Inf, -Inf); b.bmin[b.axis] = b.pos[b.axis];
+    b.bmax = V3(Inf, Inf, Inf);    b.bmax[b.axis] = b.pos[b.axis];
+  }
+  if (!b.hasBound) { b.hasBound = true; b.sweepLength = 0; }
+  b.refPos = b.pos;
+  b.lastUpdateIter = S.iter;
+  const Real sl = b.sweepLength;
+  if (sl > 0) {
+    b.bmin = b.bmin - V3(sl, sl, sl);
+    b.bmax = b.bmax + V3(sl, sl, sl);
+  }
+}
+
+// InsertionSortCollider.hpp:166-171
+static inline bool spatialOverlap(const Scene& S, int id1, int id2) {
+  const Real* mn = S.minima.data(); const Real* mx = S.maxima.data();
+  return (mn[3 * id1 + 0] <= mx[3 * id2 + 0]) && (mx[3 * id1 + 0] >= mn[3 * id2 + 0]) &&
+         (mn[3 * id1 + 1] <= mx[3 * id2 + 1]) && (mx[3 * id1 + 1] >= mn[3 * id2 + 1]) &&
+         (mn[3 * id1 + 2] <= mx[3 * id2 + 2]) && (mx[3 * id1 + 2] >= mn[3 * id2 + 2]);
+}
+
+// InsertionSortCollider::handleBoundInversion (InsertionSortCollider.cpp:22-27)
+static void handleBoundInversion(Scene& S, int id1, int id2) {
+  if (spatialOverlap(S, id1, id2) && mayCollide(S.bodies[id1], S.bodies[id2]) && !S.byKey.count(pairKey(id1, id2)))
+    icInsert(S, id1, id2);
+}
+// InsertionSortCollider::insertionSort (InsertionSortCollider.cpp:29-54), serial form
+static void insertionSort(Scene& S, std::vector<Bounds>& v, bool doCollide) {
+  long n = (long)v.size();
+  for (long i = 1; i < n; i++) {
+    const Bounds viInit = v[i]; long j = i - 1;
+    const bool viInitBB = viInit.hasBB, isMin = viInit.isMin;
+    while (j >= 0 && v[j] > viInit) {
+      v[j + 1] = v[j];
+      if (isMin && !v[j].isMin && doCollide && viInitBB && v[j].hasBB && (viInit.id != v[j].id))
+        handleBoundInversion(S, viInit.id, v[j].id);
+      j--;
+    }
+    v[j + 1] = viInit;
+  }
+}
+
+// InsertionSortCollider::isActivated (InsertionSortCollider.cpp:177-189)
+static bool colliderIsActivated(Scene& S) {
+  if (!S.strideActive) return true;
+  if (!S.newtonFound) return true;
+  if (S.fastestBodyMaxDist < 0) { S.fastestBodyMaxDist = 0; return true; }
+  S.fastestBodyMaxDist = S.maxVelocitySq;
+  if (S.fastestBodyMaxDist >= 1 || S.fastestBodyMaxDist == 0) return true;
+  if ((size_t)S.BB[0].size() != 2 * S.bodies.size()) return true;
+  if (S.interactionsDirty) return true;
+  if (S.doSort) { S.doSort = false; return true; }
+  return false;
+}
+
+// InsertionSortCollider::action, non-periodic (InsertionSortCollider.cpp:191-400)
+static void colliderAction(Scene& S) {
+  long nBodies = (long)S.bodies.size();
+  bool doInitSort = false;
+  if (S.doSort) { doInitSort = true; S.doSort = false; }
+  if ((long)S.BB[0].size() != 2 * nBodies) {
+    long BBsize = (long)S.BB[0].size();
+    if (2 * nBodies < BBsize) { for (int i = 0; i < 3; i++) S.BB[i].clear(); BBsize = 0; }
+    if (2 * nBodies - BBsize > 200 || BBsize == 0) doInitSort = true;
+    for (int i = 0; i < 3; i++)
+      for (long id = BBsize / 2; id < nBodies; id++) {
+        S.BB[i].push_back(Bounds{0, (int)id, 0, false, true});
+        S.BB[i].push_back(Bounds{0, (int)id, 0, false, false});
+      }
+  }
+  if (S.minima.size() != (size_t)3 * nBodies) { S.minima.resize(3 * nBodies); S.maxima.resize(3 * nBodies); }
+  if (S.verletDist < 0) S.verletDist = 0;  // no Sphere shapes in this path (:241-252)
+  if (S.interactionsDirty) { doInitSort = true; S.interactionsDirty = false; }
+  // boundDispatcher->action() (Dispatching.cpp:15-28)
+  const Real sweepDist = S.verletDist;
+#pragma omp parallel for num_threads(S.nThreads)
+  for (long id = 0; id < nBodies; id++) processBody(S, S.bodies[id], sweepDist);
+  if (S.verletDist > 0) S.newtonFound = true;
+  if (!S.strideActive && S.verletDist > 0 && S.maxVelocitySq >= 0) S.strideActive = true;
+  // copy bounds (:289-311)
+  for (long i = 0; i < 2 * nBodies; i++)
+    for (int j = 0; j < 3; j++) {
+      Bounds& B = S.BB[j][i];
+      const Body& b = S.bodies[B.id];
+      B.hasBB = b.hasBound;
+      B.coord = b.hasBound ? (B.isMin ? b.bmin[j] : b.bmax[j]) : b.pos[j];
+      if (B.isMin && j == 1 && b.hasBound) {
+        for (int k = 0; k < 3; k++) { S.minima[3 * B.id + k] = b.bmin[k]; S.maxima[3 * B.id + k] = b.bmax[k]; }
+      }
+    }
+  // conditionalyEraseNonReal (InteractionContainer.hpp:104-110; shouldBeErased = !spatialOverlap)
+  for (long linPos = 0; linPos < (long)S.lin.size();) {
+    Interaction* I = S.lin[linPos];
+    bool real = I->hasGeom && I->hasPhys;
+    if (!real && !spatialOverlap(S, I->id1, I->id2)) icEraseAt(S, linPos);
+    else linPos++;
+  }
+  if (!doInitSort) {
+    for (int i = 0; i < 3; i++) insertionSort(S, S.BB[i], true);
+  } else {
+    for (int i = 0; i < 3; i++) std::sort(S.BB[i].begin(), S.BB[i].end());
+    S.numReinit++;
+    std::vector<Bounds>& V = S.BB[S.sortAxis];
+    for (long i = 0; i < 2 * nBodies; i++) {
+      if (!(V[i].isMin && V[i].hasBB)) continue;
+      const int iid = V[i].id;
+      for (long j = i + 1; j < 2 * nBodies && V[j].id != iid; j++) {
+        const int jid = V[j].id;
+        if (!(V[j].isMin && V[j].hasBB)) continue;
+        if (spatialOverlap(S, iid, jid) && mayCollide(S.bodies[iid], S.bodies[jid]))
+          if (!S.byKey.count(pairKey(iid, jid))) icInsert(S, iid, jid);
+      }
+    }
+  }
+  S.colliderRuns++;
+}
+
+// ---------------------------------------------------------------------------
+// Narrowphase between two superellipsoids (pkg/dem/Superquadrics_Ig2.cpp)
+struct PairCtx {
+  const SQ* A; const SQ* B; V3 pos1, pos2;
+  long* disCalls;
+};
+// Disfunction, 9-argument form (Superquadrics_Ig2.cpp:622-687)
+static inline void disfunction(const PairCtx& c, Real pa0, Real pa1, V3& center, V3& p1, V3& p2, bool& stop_flag) {
+  (*c.disCalls)++;
+  V3 contact(std::cos(pa0) * std::cos(pa1), std::sin(pa0) * std::cos(pa1), std::sin(pa1));
+  V3 contact1 = mul(c.A->loc, contact);
+  Real ph0, ph1;
+  sqNormal2Phi(*c.A, contact1, ph0, ph1);
+  p1 = sqSurface(*c.A, ph0, ph1);
+  p1 = mul(c.A->glob, p1) + c.pos1;
+  V3 contact2 = mul(c.B->loc, contact);
+  sqNormal2Phi(*c.B, (-1) * contact2, ph0, ph1);
+  p2 = sqSurface(*c.B, ph0, ph1);
+  p2 = mul(c.B->glob, p2) + c.pos2;
+  V3 d = p2 - p1;
+  center = 0.5 * (p1 + p2);
+  if (dot(contact, d) > 0) stop_flag = true;
+}
+// JacfunctionApp (Superquadrics_Ig2.cpp:1033-1054): forward differences with step paraDelta
+static inline void jacApp(const PairCtx& c, Real pa0, Real pa1, const Real Dp[2], V3& center, V3& p1, V3& p2,
+                          bool& stop_flag, Real J[3][2]) {
+  disfunction(c, pa0, pa1, center, p1, p2, stop_flag);
+  V3 f0 = p2 - p1;
+  disfunction(c, pa0 + Dp[0], pa1, center, p1, p2, stop_flag);
+  V3 f1 = p2 - p1;
+  disfunction(c, pa0, pa1 + Dp[1], center, p1, p2, stop_flag);
+  V3 f2 = p2 - p1;
+  for (int i = 0; i < 3; i++) J[i][0] = (f1[i] - f0[i]) / Dp[0];
+  for (int i = 0; i < 3; i++) J[i][1] = (f2[i] - f0[i]) / Dp[1];
+}
+
+struct LMInfo { int iters; int stop; };
+// lmder2 (Superquadrics_Ig2.cpp:1057-1354) with opts {1.0, 1e-15, 1e-3, 1e-20}
+static void lmder2(const PairCtx& c, Real p[2], int itmax, V3& p1, V3& p2, V3& center, bool& touching, V3& contact,
+                   LMInfo& info) {
+  const Real tau = 1.0, eps1 = 1e-15, eps2 = 1e-3, eps3 = 1e-20;
+  const Real EPSILON = 1e-12, ONE_THIRD = 0.3333333333333334;
+  touching = true;
+  V3 p_f, pDp_f;
+  Real jacTf[2], diag[2];
+  Real jtj[2][2];
+  Real Dp[2] = {1e-7, 1e-7};
+  Real pDp[2];
+  bool stop_flag = false;
+  Real mu = 0, tmp;
+  Real jacTf_inf = 0, p_L2, Dp_L2 = DBL_MAX, dF, dL;
+  Real p_fL2, pDp_fL2;
+  int nu = 2, nu2, stop = 0;
+  int k;
+  disfunction(c, p[0], p[1], center, p1, p2, stop_flag);
+  p_f = p2 - p1;
+  p_fL2 = norm(p_f);
+  if (!std::isfinite(p_fL2)) stop = 7;
+  for (k = 0; k < itmax && !stop; ++k) {
+    if (p_fL2 <= eps3) { stop = 6; break; }
+    if (stop_flag) { stop = 9; touching = false; break; }
+    {
+      contact[0] = std::cos(p[0]) * std::cos(p[1]);
+      contact[1] = std::sin(p[0]) * std::cos(p[1]);
+      contact[2] = std::sin(p[1]);
+      Real angle = dot(p_f, contact) / (norm(p_f) * norm(contact));
+      if (std::fabs(angle) > 0.95) { stop = 8; break; }
+    }
+    Real J[3][2];
+    jacApp(c, p[0], p[1], Dp, center, p1, p2, stop_flag, J);
+    // J^T J and J^T (-f): coefficient products with the 3-term tree reduction
+    jtj[0][0] = J[0][0] * J[0][0] + (J[1][0] * J[1][0] + J[2][0] * J[2][0]);
+    jtj[0][1] = J[0][0] * J[0][1] + (J[1][0] * J[1][1] + J[2][0] * J[2][1]);
+    jtj[1][0] = J[0][1] * J[0][0] + (J[1][1] * J[1][0] + J[2][1] * J[2][0]);
+    jtj[1][1] = J[0][1] * J[0][1] + (J[1][1] * J[1][1] + J[2][1] * J[2][1]);
+    jacTf[0] = J[0][0] * (-1.0 * p_f[0]) + (J[1][0] * (-1.0 * p_f[1]) + J[2][0] * (-1.0 * p_f[2]));
+    jacTf[1] = J[0][1] * (-1.0 * p_f[0]) + (J[1][1] * (-1.0 * p_f[1]) + J[2][1] * (-1.0 * p_f[2]));
+    jacTf_inf = (std::fabs(jacTf[0]) > std::fabs(jacTf[1]) ? std::fabs(jacTf[0]) : std::fabs(jacTf[1]));
+    p_L2 = std::sqrt(p[0] * p[0] + p[1] * p[1]);
+    if (jacTf_inf <= eps1) { Dp_L2 = 0.0; stop = 1; break; }
+    if (k == 0) {
+      tmp = (jtj[0][0] > jtj[1][1] ? jtj[0][0] : jtj[1][1]);
+      mu = tau * tmp;
+    }
+    diag[0] = jtj[0][0]; diag[1] = jtj[1][1];
+    while (1) {
+      jtj[0][0] += mu;
+      jtj[1][1] += mu;
+      double n_a = jtj[0][0] * jtj[1][1] - jtj[0][1] * jtj[0][1];
+      Dp[0] = (jacTf[0] * jtj[1][1] - jacTf[1] * jtj[0][1]) / n_a;
+      Dp[1] = (jacTf[1] * jtj[0][0] - jacTf[0] * jtj[0][1]) / n_a;
+      Dp_L2 = std::sqrt(Dp[0] * Dp[0] + Dp[1] * Dp[1]);
+      if (Dp_L2 < 1e-5) { stop = 2; break; }
+      pDp[0] = p[0] + Dp[0]; pDp[1] = p[1] + Dp[1];
+      if (Dp_L2 >= (p_L2 + eps2) / (EPSILON * EPSILON)) { stop = 4; break; }
+      disfunction(c, pDp[0], pDp[1], center, p1, p2, stop_flag);
+      pDp_f = p2 - p1;
+      pDp_fL2 = norm(pDp_f);
+      if (!std::isfinite(pDp_fL2)) { stop = 7; break; }
+      dL = Dp[0] * (mu * Dp[0] + jacTf[0]) + Dp[1] * (mu * Dp[1] + jacTf[1]);
+      dF = p_fL2 - pDp_fL2;
+      tmp = dF / dL;
+      if (tmp > 0.0) {
+        tmp = 1.0 - std::pow(2 * tmp - 1., 3.);
+        mu = mu * ((tmp >= ONE_THIRD) ? tmp : ONE_THIRD);
+        nu = 2;
+        p[0] = pDp[0]; p[1] = pDp[1];
+        p_f = pDp_f;
+        p_fL2 = pDp_fL2;
+        break;
+      }
+      mu *= nu;
+      nu2 = (int)((unsigned)nu << 1);  // wraps to a non-positive value after 2^30
+      if (nu2 <= nu) { stop = 5; break; }
+      nu = nu2;
+      jtj[0][0] = diag[0]; jtj[1][1] = diag[1];
+    }
+  }
+  if (k >= itmax) stop = 3;
+  info.iters = k; info.stop = stop;
+}
+
+// Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::precompute (Superquadrics.cpp:1030-1050)
+static void precompute(Geom& g, const Body& b1, const Body& b2, Real dt, const V3& currentNormal, bool isNew, const V3& shift2) {
+  if (!isNew) {
+    g.orthonormal_axis = cross(g.normal, currentNormal);
+    Real angle = dt * 0.5 * dot(currentNormal, b1.angVel + b2.angVel);
+    g.twist_axis = angle * currentNormal;
+  } else g.twist_axis = g.orthonormal_axis = V3();
+  g.normal = currentNormal;
+  V3 c1x = g.contactPoint - b1.pos;
+  V3 c2x = (g.contactPoint - b2.pos) - shift2;
+  V3 relVel = (b2.vel + cross(b2.angVel, c2x)) - (b1.vel + cross(b1.angVel, c1x));
+  g.relativeVn = dot(g.normal, relVel) * g.normal;
+  g.relativeVs = relVel - g.relativeVn;
+  g.shearInc = g.relativeVs * dt;
+}
+
+static inline void centerLine(const V3& pos1, const V3& pos2, Real para[2]) {
+  V3 d0 = pos2 - pos1;
+  para[0] = std::atan2(d0[1], d0[0]);
+  para[1] = std::atan(d0[2] / std::sqrt(d0[0] * d0[0] + d0[1] * d0[1]));
+  para[0] += 1e-5; para[1] += 1e-5;
+}
+
+// Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go (Superquadrics_Ig2.cpp:1880-2317)
+static bool ig2SqSq(Scene& S, Interaction* I, const Body& b1, const Body& b2, const V3& shift2, Stats& st) {
+  V3 position1 = b1.pos;
+  V3 position2 = b2.pos + shift2;
+  const SQ* A = &b1.sq; const SQ* B = &b2.sq;
+  bool isNew = !I->hasGeom;
+  Geom& g = I->g;
+  Real para[2] = {1e-5, 1e-5};
+  if (isNew) {
+    std::memset(&g, 0, sizeof(Geom));
+    g.isShearNew = true;
+    I->hasGeom = true;
+    centerLine(position1, position2, para);
+  } else {
+    g.isShearNew = g.PenetrationDepth <= 0;
+    para[0] = g.contactAngle[0]; para[1] = g.contactAngle[1];
+  }
+  V3 contactNormal, center;
+  double pDepth = 0.0;
+  V3 p1, p2;
+  if (A->isSphere && B->isSphere) {
+    V3 dist = position2 - position1;
+    double r_sum = A->r_max + B->r_max;
+    double depth = r_sum - norm(dist);
+    if (depth < 1E-18) { g.PenetrationDepth = 0; g.isShearNew = true; return true; }
+    normalize(dist);
+    p1 = position1 + A->r_max * dist;
+    p2 = position2 - B->r_max * dist;
+    contactNormal = p1 - p2;
+    normalize(contactNormal);
+    g.point1 = p1; g.point2 = p2;
+    g.contactPoint = 0.5 * (p1 + p2);
+    g.PenetrationDepth = depth;
+  } else {
+    double r_sum = A->r_max + B->r_max;
+    if (norm(position1 - position2) > r_sum) { g.PenetrationDepth = 0; g.isShearNew = true; return true; }
+    bool touching = true;
+    PairCtx c{A, B, position1, position2, &st.disCalls};
+    LMInfo info;
+    lmder2(c, para, 50, p1, p2, center, touching, contactNormal, info);
+    st.lmCalls++; st.lmIters += info.iters;
+    if (std::isnan(para[0]) || std::isnan(para[1]) || 7 == info.stop) {
+      if (touching) {
+        centerLine(position1, position2, para);
+        lmder2(c, para, 50, p1, p2, center, touching, contactNormal, info);
+        st.lmCalls++; st.lmIters += info.iters; st.restarts++;
+      }
+    }
+    pDepth = dot(p1 - p2, contactNormal);
+    if (touching) {
+      if (10.0 * norm(p2 - p1) > A->r_max) {
+        if (!(sqIsInside(*A, p2 - position1)) || !(sqIsInside(*B, p1 - position2))) {
+          centerLine(position1, position2, para);
+          lmder2(c, para, 50, p1, p2, center, touching, contactNormal, info);
+          st.lmCalls++; st.lmIters += info.iters; st.restarts++;
+          pDepth = dot(p1 - p2, contactNormal);
+        }
+      }
+    }
+    if (!touching) {
+      g.contactAngle[0] = para[0]; g.contactAngle[1] = para[1];
+      g.PenetrationDepth = 0; g.isShearNew = true;
+      return true;
+    }
+    g.point1 = p1; g.point2 = p2;
+    if (std::isnan(contactNormal[0])) st.nanNormals++;
+    g.contactPoint = center;
+    g.PenetrationDepth = pDepth;
+    normalize(contactNormal);
+  }
+  precompute(g, b1, b2, S.dt, contactNormal, g.isShearNew, shift2);
+  g.normal = contactNormal;
+  g.contactAngle[0] = para[0]; g.contactAngle[1] = para[1];
+  return true;
+}
+
+// Ig2_Wall_Superquadrics_SuperquadricsGeom::go (Superquadrics_Ig2.cpp:2522-2611)
+static bool ig2WallSq(Scene& S, Interaction* I, const Body& w, const Body& b, const V3& shift2) {
+  const int PA = w.axis; const int sense = w.sense;
+  const SQ* B = &b.sq;
+  bool isNew = !I->hasGeom;
+  Geom& g = I->g;
+  if (isNew) {
+    std::memset(&g, 0, sizeof(Geom));
+    g.isShearNew = true;
+    I->hasGeom = true;
+  } else g.isShearNew = g.PenetrationDepth <= 0;
+  V3 normal; normal[PA] = sense;
+  V3 wall_pos = w.pos; V3 B_pos = b.pos;
+  if (B->isSphere) {
+    V3 p1 = B_pos; p1[PA] = wall_pos[PA];
+    V3 point2 = B_pos - normal * B->r_max;
+    double depth = B->r_max - norm(B_pos - p1);
+    if (depth < 0.0) { g.PenetrationDepth = 0; g.isShearNew = true; return true; }
+    g.point1 = p1; g.point2 = point2;
+    g.contactPoint = 0.5 * (point2 + p1);
+    g.PenetrationDepth = depth;
+  } else {
+    Real ph0, ph1;
+    sqNormal2Phi(*B, -mul(B->loc, normal), ph0, ph1);
+    V3 point2 = mul(B->glob, sqSurface(*B, ph0, ph1)) + B_pos;
+    V3 p1 = point2; p1[PA] = wall_pos[PA];
+    V3 d = point2 - p1;
+    if (normal[PA] * d[PA] >= 0.0) { g.PenetrationDepth = 0; g.isShearNew = true; return true; }
+    g.point1 = p1; g.point2 = point2;
+    g.contactPoint = 0.5 * (point2 + p1);
+    g.PenetrationDepth = norm(d);
+  }
+  precompute(g, w, b, S.dt, normal, g.isShearNew, shift2);
+  g.normal = normal;
+  return true;
+}
+
+// Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys::go (Superquadrics.cpp:1086-1116)
+static void ip2(Scene& S, Interaction* I) {
+  if (I->hasPhys) return;
+  const Mat& m1 = S.mats[S.bodies[I->id1].mat];
+  const Mat& m2 = S.mats[S.bodies[I->id2].mat];
+  Phys& p = I->p;
+  std::memset(&p, 0, sizeof(Phys));
+  I->hasPhys = true;
+  if (I->id1 > 5) {
+    Real fa = std::min(m1.frictionAngle, m2.frictionAngle);
+    p.tanphi = std::tan(fa);
+    p.kn = 2.0 * m1.Kn * m2.Kn / (m1.Kn + m2.Kn);
+    p.ks = 2.0 * m1.Ks * m2.Ks / (m1.Ks + m2.Ks);
+  } else {
+    p.tanphi = std::tan(m1.frictionAngle);
+    p.kn = m1.Kn;
+    p.ks = m1.Ks;
+  }
+  p.betan = std::max(m1.betan, m2.betan);
+  p.betas = std::max(m1.betas, m2.betas);
+}
+
+// SuperquadricsGeom::rotate (Superquadrics.cpp:1053-1080)
+static inline V3 rotateShear(const Geom& g, V3 sf) {
+  sf = sf - cross(sf, g.orthonormal_axis);
+  sf = sf - cross(sf, g.twist_axis);
+  sf = sf - dot(g.normal, sf) * g.normal;
+  return sf;
+}
+
+// SuperquadricsLaw::go (Superquadrics.cpp:1181-1363)
+static bool law(Scene& S, Interaction* I, V3* F, V3* T) {
+  if (!I->hasGeom) return true;
+  const Body& A = S.bodies[I->id1];
+  const Body& B = S.bodies[I->id2];
+  Geom& g = I->g; Phys& ph = I->p;
+  V3 ab_min = B.bmin, ab_max = B.bmax;
+  if (A.bmin[0] >= ab_max[0] || ab_min[0] >= A.bmax[0] || A.bmin[1] >= ab_max[1] || ab_min[1] >= A.bmax[1] ||
+      A.bmin[2] >= ab_max[2] || ab_min[2] >= A.bmax[2]) {
+    ph.normalForce = V3(); ph.shearForce = V3();
+    requestErase(I);
+    return false;
+  }
+  if (!(g.PenetrationDepth > 1E-18)) { ph.normalForce = V3(); ph.shearForce = V3(); return true; }
+  V3 normalForce = g.normal * g.PenetrationDepth * ph.kn;
+  V3 shearForce1;
+  bool useDamping = (ph.betan > 1e-5 || ph.betas > 1e-5);
+  Real cs = 0;
+  V3 shearViscous;
+  if (useDamping) {
+    const bool Adyn = A.blockedDOFs != DOF_ALL, Bdyn = B.blockedDOFs != DOF_ALL;
+    Real mbar = (!Adyn && Bdyn) ? B.mass : ((!Bdyn && Adyn) ? A.mass : (A.mass * B.mass / (A.mass + B.mass)));
+    Real Cn_crit = 2. * std::sqrt(mbar * ph.kn);
+    Real Cs_crit = 2. * std::sqrt(mbar * ph.ks);
+    Real cn = Cn_crit * ph.betan;
+    cs = Cs_crit * ph.betas;
+    V3 normalViscous = cn * g.relativeVn;
+    V3 normTemp = normalForce - normalViscous;
+    if (dot(normTemp, g.normal) < 0.0) normalForce = V3();
+    else normalForce = normalForce - normalViscous;
+  }
+  if (g.isShearNew) shearForce1 = V3();
+  else shearForce1 = rotateShear(g, ph.shearForce);
+  shearForce1 = shearForce1 - ph.ks * g.shearInc;
+  Real maxFs = sqnorm(normalForce) * std::pow(ph.tanphi, 2);
+  if (sqnorm(shearForce1) > maxFs) {
+    Real ratio = std::sqrt(maxFs) / norm(shearForce1);
+    shearForce1 = shearForce1 * ratio;
+  } else if (useDamping) {
+    shearViscous = cs * g.relativeVs;
+  }
+  if (std::isnan(shearForce1[0]) || std::isnan(normalForce[0])) { normalForce = V3(); shearForce1 = V3(); }
+  V3 Fv = ((-normalForce) - shearForce1) + shearViscous;
+  F[I->id1] = F[I->id1] + Fv;
+  F[I->id2] = F[I->id2] + (-Fv);
+  T[I->id1] = T[I->id1] + (-cross(A.pos - g.contactPoint, Fv));
+  T[I->id2] = T[I->id2] + cross(B.pos - g.contactPoint, Fv);
+  ph.normalForce = normalForce;
+  ph.shearForce = shearForce1;
+  return true;
+}
+
+// InteractionLoop::action (pkg/common/InteractionLoop.cpp:23-149)
+static void interactionLoop(Scene& S) {
+  const long size = (long)S.lin.size();
+  const int nt = S.nThreads;
+  if ((int)S.fbuf.size() != nt) { S.fbuf.assign(nt, {}); S.tbuf.assign(nt, {}); S.tstats.assign(nt, Stats{0, 0, 0, 0, 0}); }
+  for (int t = 0; t < nt; t++) {
+    S.fbuf[t].assign(S.bodies.size(), V3());
+    S.tbuf[t].assign(S.bodies.size(), V3());
+  }
+#pragma omp parallel for schedule(guided) num_threads(nt)
+  for (long i = 0; i < size; i++) {
+    Interaction* I = S.lin[i];
+    const int tn = threadNum();
+    if (!I->geomExists) continue;
+    bool swap = false;
+    const Body& ba = S.bodies[I->id1];
+    const Body& bb = S.bodies[I->id2];
+    if (!I->geomFunctorSet) {
+      if (ba.kind == KIND_WALL && bb.kind == KIND_WALL) { I->geomExists = false; continue; }
+      I->geomFunctorSet = true;
+      if (ba.kind == KIND_SQ && bb.kind == KIND_WALL) swap = true;  // functor is (Wall, Superquadrics)
+    } else if (ba.kind == KIND_WALL && bb.kind == KIND_WALL) { I->geomExists = false; continue; }
+    if (swap) { std::swap(I->id1, I->id2); for (int k = 0; k < 3; k++) I->cellDist[k] *= -1; }
+    const Body& b1 = S.bodies[I->id1];
+    const Body& b2 = S.bodies[I->id2];
+    V3 shift2;
+    if (b1.kind == KIND_WALL) ig2WallSq(S, I, b1, b2, shift2);
+    else ig2SqSq(S, I, b1, b2, shift2, S.tstats[tn]);
+    ip2(S, I);
+    if (!law(S, I, S.fbuf[tn].data(), S.tbuf[tn].data())) requestErase(I);
+  }
+  for (int t = 0; t < nt; t++) {
+    S.stats.lmCalls += S.tstats[t].lmCalls; S.stats.lmIters += S.tstats[t].lmIters;
+    S.stats.disCalls += S.tstats[t].disCalls; S.stats.restarts += S.tstats[t].restarts;
+    S.stats.nanNormals += S.tstats[t].nanNormals;
+    S.tstats[t] = Stats{0, 0, 0, 0, 0};
+  }
+  // ForceContainer::sync (core/ForceContainer.hpp:134-162): sum thread buffers in thread order
+  const long nb = (long)S.bodies.size();
+  S.force.assign(nb, V3()); S.torque.assign(nb, V3());
+  for (long id = 0; id < nb; id++) {
+    V3 sf, st;
+    for (int t = 0; t < nt; t++) { sf = sf + S.fbuf[t][id]; st = st + S.tbuf[t][id]; }
+    S.force[id] = sf; S.torque[id] = st;
+  }
+}
+
+// NewtonIntegrator (pkg/dem/NewtonIntegrator.cpp)
+// DotQ (:470-477)
+static inline Quat DotQ(const V3& a, const Quat& Q) {
+  Quat d;
+  d.w = (-Q.x * a[0] - Q.y * a[1] - Q.z * a[2]) / 2;
+  d.x = (Q.w * a[0] - Q.z * a[1] + Q.y * a[2]) / 2;
+  d.y = (Q.z * a[0] + Q.w * a[1] - Q.x * a[2]) / 2;
+  d.z = (-Q.y * a[0] + Q.x * a[1] + Q.w * a[2]) / 2;
+  return d;
+}
+// quaternion + and scalar*quaternion on coefficients (lib/base/Math.hpp:172-173)
+static inline Quat qadd(const Quat& a, const Quat& b) { return Quat{a.w + b.w, a.x + b.x, a.y + b.y, a.z + b.z}; }
+static inline Quat qscale(Real f, const Quat& q) { return Quat{q.w * f, q.x * f, q.y * f, q.z * f}; }
+
+// leapfrogAsphericalRotate with A = shape->rot_mat2local (:337-360, :391-429)
+static void leapfrogSqRotate(Scene& S, Body& b, const V3& M) {
+  const Real dt = S.dt;
+  const M3& A = b.sq.loc;
+  const V3 l_n = b.angMom + dt / 2. * M;
+  const V3 l_b_n = mul(A, l_n);
+  V3 w_b_n(l_b_n[0] / b.inertia[0], l_b_n[1] / b.inertia[1], l_b_n[2] / b.inertia[2]);
+  const Quat dotQ_n = DotQ(w_b_n, b.ori);
+  const Quat Q_half = qadd(b.ori, qscale(dt / 2., dotQ_n));
+  b.angMom = b.angMom + dt * M;
+  const V3 l_b_half = mul(A, b.angMom);
+  V3 w_b_half(l_b_half[0] / b.inertia[0], l_b_half[1] / b.inertia[1], l_b_half[2] / b.inertia[2]);
+  const Quat dotQ_half = DotQ(w_b_half, Q_half);
+  b.ori = qadd(b.ori, qscale(dt, dotQ_half));
+  b.angVel = qrotate(b.ori, w_b_half);
+  qnormalize(b.ori);
+  b.sq.loc = toRot(conj(b.ori));
+  b.sq.glob = toRot(b.ori);
+}
+// leapfrogSphericalRotate without move/rot buffers (:319-335)
+static void leapfrogSphericalRotate(Scene& S, Body& b) {
+  Real angle2 = sqnorm(b.angVel);
+  if (angle2 != 0) {
+    Real angle = std::sqrt(angle2);
+    V3 axis(b.angVel[0] / angle, b.angVel[1] / angle, b.angVel[2] / angle);
+    // Quaternionr(AngleAxisr(angle*dt, axis)): w = cos(h), vec = sin(h)*axis
+    Real h = 0.5 * (angle * S.dt);
+    Real s = std::sin(h);
+    Quat q{std::cos(h), s * axis[0], s * axis[1], s * axis[2]};
+    // q * ori (Hamilton product, Eigen Quaternion.h quat_product)
+    Quat o = b.ori;
+    Quat r;
+    r.w = q.w * o.w - q.x * o.x - q.y * o.y - q.z * o.z;
+    r.x = q.w * o.x + q.x * o.w + q.y * o.z - q.z * o.y;
+    r.y = q.w * o.y + q.y * o.w + q.z * o.x - q.x * o.z;
+    r.z = q.w * o.z + q.z * o.w + q.x * o.y - q.y * o.x;
+    b.ori = r;
+  }
+  qnormalize(b.ori);
+}
+
+// NewtonIntegrator::action for non-clump, non-periodic bodies (:99-304)
+static void newtonAction(Scene& S) {
+  const Real dt = S.dt;
+  const long nb = (long)S.bodies.size();
+  S.maxVelocitySq = 0;
+  std::vector<Real> thrMax(S.nThreads, 0.0);
+#pragma omp parallel for num_threads(S.nThreads)
+  for (long id = 0; id < nb; id++) {
+    Body& b = S.bodies[id];
+    V3 f = S.force[id], m = S.torque[id];
+    const bool useAspherical = (S.exactAsphericalRot && b.aspherical && b.blockedDOFs != DOF_ALL);
+    const bool isSphere = (b.kind == KIND_SQ) && b.sq.isSphere;
+    if (b.blockedDOFs != DOF_ALL) {
+      V3 linAccel;
+      if (b.blockedDOFs == 0) linAccel = V3(f[0] / b.mass + S.gravity[0], f[1] / b.mass + S.gravity[1], f[2] / b.mass + S.gravity[2]);
+      else for (int i = 0; i < 3; i++) if (!(b.blockedDOFs & (1u << i))) linAccel[i] += f[i] / b.mass + S.gravity[i];
+      if (b.isDamped)  // cundallDamp2nd (:23-25)
+        for (int i = 0; i < 3; i++) linAccel[i] *= 1 - S.damping * Sign(linAccel[i] * (b.vel[i] + 0.5 * dt * linAccel[i]));
+      b.vel = b.vel + dt * linAccel;
+      if (!useAspherical) {
+        V3 angAccel;
+        if (b.blockedDOFs == 0) angAccel = V3(m[0] / b.inertia[0], m[1] / b.inertia[1], m[2] / b.inertia[2]);
+        else for (int i = 0; i < 3; i++) if (!(b.blockedDOFs & (1u << (i + 3)))) angAccel[i] += m[i] / b.inertia[i];
+        if (b.isDamped)
+          for (int i = 0; i < 3; i++) angAccel[i] *= 1 - S.damping * Sign(angAccel[i] * (b.angVel[i] + 0.5 * dt * angAccel[i]));
+        b.angVel = b.angVel + dt * angAccel;
+      } else {
+        for (int i = 0; i < 3; i++) if (b.blockedDOFs & (1u << (i + 3))) m[i] = 0;
+        if (b.isDamped) {
+          if (S.isSuperquadrics && isSphere) {
+            V3 angAccel;
+            if (b.blockedDOFs == 0) angAccel = V3(m[0] / b.inertia[0], m[1] / b.inertia[1], m[2] / b.inertia[2]);
+            else for (int i = 0; i < 3; i++) if (!(b.blockedDOFs & (1u << (i + 3)))) angAccel[i] += m[i] / b.inertia[i];
+            for (int i = 0; i < 3; i++) angAccel[i] *= 1 - S.damping * Sign(angAccel[i] * (b.angVel[i] + 0.5 * dt * angAccel[i]));
+            b.angVel = b.angVel + dt * angAccel;
+          } else {  // cundallDamp1st on the torque (:19-21)
+            for (int i = 0; i < 3; i++) m[i] *= 1 - S.damping * Sign(m[i] * b.angVel[i]);
+          }
+        }
+      }
+    }
+    if (!useAspherical) leapfrogSphericalRotate(S, b);
+    else if (S.isSuperquadrics) {
+      if (!isSphere) leapfrogSqRotate(S, b, m);
+      else leapfrogSphericalRotate(S, b);
+    }
+    b.pos = b.pos + b.vel * dt;  // leapfrogTranslate (:306-317)
+    // saveMaximaDisplacement (:72-85)
+    if (b.hasBound) {
+      V3 disp = b.pos - b.refPos;
+      Real maxDisp = std::max(std::abs(disp[0]), std::max(std::abs(disp[1]), std::abs(disp[2])));
+      if (!maxDisp || maxDisp < b.sweepLength) maxDisp = 0.5; else maxDisp = 2;
+      Real& t = thrMax[threadNum()];
+      t = std::max(t, maxDisp);
+    }
+  }
+  for (Real t : thrMax) S.maxVelocitySq = std::max(S.maxVelocitySq, t);
+}
+
+// Scene::moveToNextTimeStep (core/Scene.cpp:70-138) for
+// O.engines = [ForceResetter, InsertionSortCollider, InteractionLoop, (hook), NewtonIntegrator]
+static void step(Scene& S) {
+  S.lastStepCollided = false;
+  if (colliderIsActivated(S)) { colliderAction(S); S.lastStepCollided = true; }
+  interactionLoop(S);
+  if (S.midHook) S.midHook(S.midHookArg);
+  newtonAction(S);
+  S.iter++;
+  S.time += S.dt;
+}
+
+}  // namespace sqo
+
+// ===========================================================================
+// C ABI used by tests and the CPU baseline (ctypes)
+using namespace sqo;
+extern "C" {
+
+void* sqo_create(void) { return new Scene(); }
+void sqo_destroy(void* h) {
+  Scene* S = (Scene*)h;
+  for (Interaction* I : S->lin) delete I;
+  delete S;
+}
+void sqo_set_threads(void* h, int n) { ((Scene*)h)->nThreads = n > 0 ? n : 1; }
+
+int sqo_add_material(void* h, double Kn, double Ks, double frictionAngle, double betan, double betas, double density) {
+  Scene* S = (Scene*)h;
+  S->mats.push_back(Mat{Kn, Ks, frictionAngle, betan, betas, density});
+  return (int)S->mats.size() - 1;
+}
+
+// utils.wall (py/utils.py:311-327): fixed, aspherical=False, no bound until the first collider run
+int sqo_add_wall(void* h, const double* pos, int axis, int sense, int mat) {
+  Scene* S = (Scene*)h;
+  Body b; std::memset(&b, 0, sizeof(Body));
+  b.kind = KIND_WALL; b.axis = axis; b.sense = sense; b.mat = mat;
+  b.pos = V3(pos[0], pos[1], pos[2]); b.ori = Quat{1, 0, 0, 0};
+  b.mass = 0; b.blockedDOFs = DOF_ALL; b.isDamped = true; b.aspherical = false; b.groupMask = 1;
+  b.hasBound = false; b.refPos = V3(NaN, NaN, NaN);
+  S->bodies.push_back(b);
+  return (int)S->bodies.size() - 1;
+}
+
+// NewSuperquadrics_rot2 (py/_superquadrics_utils.cpp:354-380) followed by body.state.pos = pos
+int sqo_add_sq(void* h, double rx, double ry, double rz, double e1, double e2, int mat, const double* q_wxyz,
+               int isSphere, const double* pos) {
+  Scene* S = (Scene*)h;
+  Body b; std::memset(&b, 0, sizeof(Body));
+  b.kind = KIND_SQ; b.mat = mat;
+  b.sq.rx = rx; b.sq.ry = ry; b.sq.rz = rz; b.sq.eps1 = e1; b.sq.eps2 = e2; b.sq.isSphere = isSphere != 0;
+  sqInitial(b.sq);
+  const Mat& m = S->mats[mat];
+  b.mass = m.density * b.sq.volume;
+  b.inertia = b.sq.inertia * m.density;
+  Quat o{q_wxyz[0], q_wxyz[1], q_wxyz[2], q_wxyz[3]};
+  qnormalize(o);  // Superquadrics::setOrientation (Superquadrics.hpp:86-91)
+  b.ori = o;
+  b.sq.loc = toRot(conj(o)); b.sq.glob = toRot(o);
+  b.pos = V3(pos[0], pos[1], pos[2]);
+  b.blockedDOFs = 0; b.isDamped = true; b.aspherical = true; b.groupMask = 1;
+  b.hasBound = true; b.refPos = V3(NaN, NaN, NaN); b.sweepLength = 0; b.lastUpdateIter = 0;
+  S->bodies.push_back(b);
+  return (int)S->bodies.size() - 1;
+}
+
+void sqo_set_params(void* h, double dt, const double* gravity, double damping, double verletDist, int targetInterv,
+                    double minSweepDistFactor, int sortAxis) {
+  Scene* S = (Scene*)h;
+  S->dt = dt; S->gravity = V3(gravity[0], gravity[1], gravity[2]); S->damping = damping;
+  S->verletDist = verletDist; S->targetInterv = targetInterv; S->minSweepDistFactor = minSweepDistFactor;
+  S->sortAxis = sortAxis;
+}
+
+void sqo_step(void* h, int n) { Scene* S = (Scene*)h; for (int i = 0; i < n; i++) step(*S); }
+// Run only the collider (if activated) and return whether it ran; for pair-set checks.
+int sqo_collide(void* h) {
+  Scene* S = (Scene*)h;
+  if (colliderIsActivated(*S)) { colliderAction(*S); return 1; }
+  return 0;
+}
+int sqo_last_step_collided(void* h) { return ((Scene*)h)->lastStepCollided ? 1 : 0; }
+long sqo_iter(void* h) { return ((Scene*)h)->iter; }
+int sqo_num_bodies(void* h) { return (int)((Scene*)h)->bodies.size(); }
+long sqo_num_interactions(void* h) { return (long)((Scene*)h)->lin.size(); }
+void sqo_stats(void* h, long* out5) {
+  Stats& s = ((Scene*)h)->stats;
+  out5[0] = s.lmCalls; out5[1] = s.lmIters; out5[2] = s.disCalls; out5[3] = s.restarts; out5[4] = s.nanNormals;
+}
+double sqo_max_velocity_sq(void* h) { return ((Scene*)h)->maxVelocitySq; }
+
+// Body state, 37 doubles per body:
+// pos3 ori4(wxyz) vel3 angVel3 angMom3 force3 torque3 bmin3 bmax3 refPos3 sweepLength lastUpdateIter mass inertia3
+enum { BODY_STRIDE = 37 };
+void sqo_get_bodies(void* h, double* out) {
+  Scene* S = (Scene*)h;
+  for (size_t i = 0; i < S->bodies.size(); i++) {
+    const Body& b = S->bodies[i]; double* o = out + i * BODY_STRIDE;
+    for (int k = 0; k < 3; k++) o[k] = b.pos[k];
+    o[3] = b.ori.w; o[4] = b.ori.x; o[5] = b.ori.y; o[6] = b.ori.z;
+    for (int k = 0; k < 3; k++) { o[7 + k] = b.vel[k]; o[10 + k] = b.angVel[k]; o[13 + k] = b.angMom[k]; }
+    V3 f = i < S->force.size() ? S->force[i] : V3(), t = i < S->torque.size() ? S->torque[i] : V3();
+    for (int k = 0; k < 3; k++) { o[16 + k] = f[k]; o[19 + k] = t[k]; }
+    for (int k = 0; k < 3; k++) { o[22 + k] = b.bmin[k]; o[25 + k] = b.bmax[k]; o[28 + k] = b.refPos[k]; }
+    o[31] = b.sweepLength; o[32] = (double)b.lastUpdateIter; o[33] = b.mass;
+    for (int k = 0; k < 3; k++) o[34 + k] = b.inertia[k];
+  }
+}
+// Overwrite dynamic state (pos, ori, vel, angVel, angMom) and bound state of all bodies
+// from the same 37-double layout; forces/mass/inertia columns are ignored.
+void sqo_set_bodies(void* h, const double* in) {
+  Scene* S = (Scene*)h;
+  for (size_t i = 0; i < S->bodies.size(); i++) {
+    Body& b = S->bodies[i]; const double* o = in + i * BODY_STRIDE;
+    b.pos = V3(o[0], o[1], o[2]);
+    b.ori = Quat{o[3], o[4], o[5], o[6]};
+    b.vel = V3(o[7], o[8], o[9]); b.angVel = V3(o[10], o[11], o[12]); b.angMom = V3(o[13], o[14], o[15]);
+    b.bmin = V3(o[22], o[23], o[24]); b.bmax = V3(o[25], o[26], o[27]); b.refPos = V3(o[28], o[29], o[30]);
+    b.sweepLength = o[31]; b.lastUpdateIter = (long)o[32];
+    if (b.kind == KIND_SQ) { b.sq.loc = toRot(conj(b.ori)); b.sq.glob = toRot(b.ori); }
+  }
+}
+
+// Interaction records, 44 doubles each:
+// id1 id2 real hasGeom depth angle2 contactPoint3 normal3 shearInc3 point1_3 point2_3 isShearNew
+// kn ks tanphi normalForce3 shearForce3 twist3 ortho3 relVn3 relVs3
+enum { INTR_STRIDE = 44 };
+void sqo_get_interactions(void* h, double* out) {
+  Scene* S = (Scene*)h;
+  for (size_t i = 0; i < S->lin.size(); i++) {
+    const Interaction* I = S->lin[i]; double* o = out + i * INTR_STRIDE;
+    const Geom& g = I->g; const Phys& p = I->p;
+    o[0] = I->id1; o[1] = I->id2; o[2] = (I->hasGeom && I->hasPhys) ? 1 : 0; o[3] = I->hasGeom ? 1 : 0;
+    o[4] = g.PenetrationDepth; o[5] = g.contactAngle[0]; o[6] = g.contactAngle[1];
+    for (int k = 0; k < 3; k++) {
+      o[7 + k] = g.contactPoint[k]; o[10 + k] = g.normal[k]; o[13 + k] = g.shearInc[k];
+      o[16 + k] = g.point1[k]; o[19 + k] = g.point2[k];
+    }
+    o[22] = g.isShearNew ? 1 : 0;
+    o[23] = p.kn; o[24] = p.ks; o[25] = p.tanphi;
+    for (int k = 0; k < 3; k++) {
+      o[26 + k] = p.normalForce[k]; o[29 + k] = p.shearForce[k]; o[32 + k] = g.twist_axis[k];
+      o[35 + k] = g.orthonormal_axis[k]; o[38 + k] = g.relativeVn[k]; o[41 + k] = g.relativeVs[k];
+    }
+  }
+}
+// Replace the whole interaction container by the given records (same layout); the
+// functor cache is rebuilt as the InteractionLoop would have left it.
+void sqo_set_interactions(void* h, long n, const double* in) {
+  Scene* S = (Scene*)h;
+  for (Interaction* I : S->lin) delete I;
+  S->lin.clear(); S->byKey.clear();
+  for (long i = 0; i < n; i++) {
+    const double* o = in + i * INTR_STRIDE;
+    int id1 = (int)o[0], id2 = (int)o[1];
+    icInsert(*S, id1, id2);
+    Interaction* I = S->lin.back();
+    I->iterBorn = 0;
+    const Body& a = S->bodies[id1]; const Body& b = S->bodies[id2];
+    I->geomFunctorSet = !(a.kind == KIND_WALL && b.kind == KIND_WALL) && (o[3] != 0 || o[2] != 0);
+    I->geomExists = !(a.kind == KIND_WALL && b.kind == KIND_WALL && I->geomFunctorSet);
+    I->hasGeom = o[3] != 0; I->hasPhys = o[2] != 0;
+    Geom& g = I->g; Phys& p = I->p;
+    g.PenetrationDepth = o[4]; g.contactAngle[0] = o[5]; g.contactAngle[1] = o[6];
+    for (int k = 0; k < 3; k++) {
+      g.contactPoint[k] = o[7 + k]; g.normal[k] = o[10 + k]; g.shearInc[k] = o[13 + k];
+      g.point1[k] = o[16 + k]; g.point2[k] = o[19 + k];
+    }
+    g.isShearNew = o[22] != 0;
+    p.kn = o[23]; p.ks = o[24]; p.tanphi = o[25];
+    for (int k = 0; k < 3; k++) {
+      p.normalForce[k] = o[26 + k]; p.shearForce[k] = o[29 + k]; g.twist_axis[k] = o[32 + k];
+      g.orthonormal_axis[k] = o[35 + k]; g.relativeVn[k] = o[38 + k]; g.relativeVs[k] = o[41 + k];
+    }
+  }
+}
+
+// Collider/integrator scalar state: iter, maxVelocitySq, fastestBodyMaxDist, strideActive,
+// newtonFound, verletDist(current), numReinit, colliderRuns
+void sqo_get_scalars(void* h, double* o) {
+  Scene* S = (Scene*)h;
+  o[0] = (double)S->iter; o[1] = S->maxVelocitySq; o[2] = S->fastestBodyMaxDist; o[3] = S->strideActive;
+  o[4] = S->newtonFound; o[5] = S->verletDist; o[6] = S->numReinit; o[7] = (double)S->colliderRuns;
+  o[8] = S->BB[0].empty() ? 0 : 1;
+}
+void sqo_set_scalars(void* h, const double* o) {
+  Scene* S = (Scene*)h;
+  S->iter = (long)o[0]; S->maxVelocitySq = o[1]; S->fastestBodyMaxDist = o[2]; S->strideActive = o[3] != 0;
+  S->newtonFound = o[4] != 0; S->verletDist = o[5];
+  if (o[8] == 0) for (int j = 0; j < 3; j++) S->BB[j].clear();
+}
+// Rebuild the collider's sorted bound lists from the current body bounds, as the
+// previous collider run would have left them (insertion-sorted, hence sorted by
+// coordinate; equal coordinates keep id order).
+void sqo_rebuild_sorted_bounds(void* h) {
+  Scene* S = (Scene*)h;
+  long nb = (long)S->bodies.size();
+  S->minima.assign(3 * nb, 0); S->maxima.assign(3 * nb, 0);
+  for (int j = 0; j < 3; j++) {
+    S->BB[j].clear();
+    for (long id = 0; id < nb; id++) {
+      const Body& b = S->bodies[id];
+      Bounds lo{b.hasBound ? b.bmin[j] : b.pos[j], (int)id, 0, b.hasBound, true};
+      Bounds hi{b.hasBound ? b.bmax[j] : b.pos[j], (int)id, 0, b.hasBound, false};
+      S->BB[j].push_back(lo); S->BB[j].push_back(hi);
+    }
+    std::stable_sort(S->BB[j].begin(), S->BB[j].end());
+  }
+  for (long id = 0; id < nb; id++)
+    for (int k = 0; k < 3; k++) { S->minima[3 * id + k] = S->bodies[id].bmin[k]; S->maxima[3 * id + k] = S->bodies[id].bmax[k]; }
+}
+
+// Stand-alone narrowphase for known-answer tests: bodies a, b of the scene, optional
+// prior geometry (contactAngle, depth, normal) when isNew == 0.  Writes
+// depth, normal3, contactPoint3, point1_3, point2_3, angle2, touching -> 15 doubles; returns LM stop code.
+int sqo_pair_geom(void* h, int ia, int ib, int isNew, const double* prior4, double* out) {
+  Scene* S = (Scene*)h;
+  Interaction I; std::memset(&I, 0, sizeof(I));
+  I.id1 = ia; I.id2 = ib;
+  if (!isNew) {
+    I.hasGeom = true; I.g.contactAngle[0] = prior4[0]; I.g.contactAngle[1] = prior4[1]; I.g.PenetrationDepth = prior4[2];
+  }
+  Stats st{0, 0, 0, 0, 0};
+  const Body& a = S->bodies[ia]; const Body& b = S->bodies[ib];
+  if (a.kind == KIND_WALL) ig2WallSq(*S, &I, a, b, V3());
+  else ig2SqSq(*S, &I, a, b, V3(), st);
+  const Geom& g = I.g;
+  out[0] = g.PenetrationDepth;
+  for (int k = 0; k < 3; k++) { out[1 + k] = g.normal[k]; out[4 + k] = g.contactPoint[k]; out[7 + k] = g.point1[k]; out[10 + k] = g.point2[k]; }
+  out[13] = g.contactAngle[0]; out[14] = g.contactAngle[1];
+  return (int)st.lmIters;
+}
+
+// Shape properties (Superquadrics::Initial): volume, inertia3 (geometric), r_max
+void sqo_shape_props(double rx, double ry, double rz, double e1, double e2, double* out5) {
+  SQ s; std::memset(&s, 0, sizeof(s));
+  s.rx = rx; s.ry = ry; s.rz = rz; s.eps1 = e1; s.eps2 = e2;
+  sqInitial(s);
+  out5[0] = s.volume; out5[1] = s.inertia[0]; out5[2] = s.inertia[1]; out5[3] = s.inertia[2]; out5[4] = s.r_max;
+}
+// Local surface point / normal / Normal2Phi for known-answer construction
+void sqo_surface(double rx, double ry, double rz, double e1, double e2, double ph0, double ph1, double* out3) {
+  SQ s; std::memset(&s, 0, sizeof(s)); s.rx = rx; s.ry = ry; s.rz = rz; s.eps1 = e1; s.eps2 = e2;
+  V3 p = sqSurface(s, ph0, ph1); out3[0] = p[0]; out3[1] = p[1]; out3[2] = p[2];
+}
+void sqo_normal(double rx, double ry, double rz, double e1, double e2, double ph0, double ph1, double* out3) {
+  SQ s; std::memset(&s, 0, sizeof(s)); s.rx = rx; s.ry = ry; s.rz = rz; s.eps1 = e1; s.eps2 = e2;
+  V3 p = sqNormal(s, ph0, ph1); out3[0] = p[0]; out3[1] = p[1]; out3[2] = p[2];
+}
+void sqo_normal2phi(double rx, double ry, double rz, double e1, double e2, const double* n3, double* out2) {
+  SQ s; std::memset(&s, 0, sizeof(s)); s.rx = rx; s.ry = ry; s.rz = rz; s.eps1 = e1; s.eps2 = e2;
+  sqNormal2Phi(s, V3(n3[0], n3[1], n3[2]), out2[0], out2[1]);
+}
+
+}  // extern "C"

@@ -1,0 +1,272 @@
+"""ctypes binding of libsqdem_gpu.so (the C ABI declared in include/sqdem.h).
+
+There is no CPU fallback: if the library cannot be loaded or no CUDA device is present,
+the constructor raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+BODY_STRIDE = 37
+INTR_STRIDE = 44
+NSCALARS = 9
+
+SQDEM_SUPERQUADRIC = 0
+SQDEM_WALL = 1
+PRECISION = {"fp64": 0, "mixed": 1}
+
+STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_CAPACITY", 4: "ERR_STATE", 5: "ERR_NUMERIC"}
+
+
+class SqdemError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"sqdem {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class _Config(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("contacts_per_body", C.c_int), ("use_graph", C.c_int)]
+
+
+class _Params(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double), ("gravity", C.c_double * 3), ("damping", C.c_double), ("verletDist", C.c_double),
+        ("targetInterv", C.c_int), ("minSweepDistFactor", C.c_double), ("sortAxis", C.c_int),
+        ("isSuperquadrics", C.c_int), ("exactAsphericalRot", C.c_int),
+    ]
+
+
+class _Report(C.Structure):
+    _fields_ = [(n, C.c_longlong) for n in ("nan_normals", "nan_forces", "lm_calls", "lm_iterations", "lm_maxiter",
+                                             "overflow", "collider_runs", "steps")]
+
+
+_LIB = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load_library(build_if_missing=True):
+    """Load libsqdem_gpu.so from the package directory (building it if it is missing)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise OSError(f"{path} is missing; run sudodem_gb300.build.build()")
+        _build.build()
+    lib = C.CDLL(path)
+    P = C.POINTER
+    d, i, l, v = C.c_double, C.c_int, C.c_long, C.c_void_p
+    dp, ip = P(d), P(i)
+    sig = {
+        "sqdem_create": (i, [P(v), P(_Config)]),
+        "sqdem_destroy": (None, [v]),
+        "sqdem_last_error": (C.c_char_p, [v]),
+        "sqdem_set_materials": (i, [v, i, dp, dp, dp, dp, dp, dp]),
+        "sqdem_set_bodies": (i, [v, i, ip, dp, ip, ip, ip, dp]),
+        "sqdem_set_params": (i, [v, P(_Params)]),
+        "sqdem_step": (i, [v, i]),
+        "sqdem_sync": (i, [v, P(_Report)]),
+        "sqdem_get_body_state": (i, [v, dp]),
+        "sqdem_put_body_state": (i, [v, dp]),
+        "sqdem_get_kinematics": (i, [v, dp]),
+        "sqdem_put_kinematics": (i, [v, dp]),
+        "sqdem_num_interactions": (i, [v, i, P(l)]),
+        "sqdem_get_interactions": (i, [v, i, dp, l, P(l)]),
+        "sqdem_put_interactions": (i, [v, l, dp]),
+        "sqdem_get_scalars": (i, [v, dp]),
+        "sqdem_put_scalars": (i, [v, dp]),
+        "sqdem_stage_times": (i, [v, dp]),
+        "sqdem_shape_props": (i, [d, d, d, d, d, dp]),
+        "sqdem_launch_count": (C.c_longlong, [v]),
+        "sqdem_set_record_full": (i, [v, i]),
+        "sqdem_time_steps": (i, [v, i, dp]),
+        "sqdem_time_e2e": (i, [v, i, v, v, dp]),
+        "sqdem_time_contacts": (i, [v, i, dp]),
+        "sqdem_set_use_graph": (i, [v, i]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def exported_symbols():
+    return ["sqdem_create", "sqdem_destroy", "sqdem_last_error", "sqdem_set_materials", "sqdem_set_bodies",
+            "sqdem_set_params", "sqdem_step", "sqdem_sync", "sqdem_get_body_state", "sqdem_put_body_state",
+            "sqdem_get_kinematics", "sqdem_put_kinematics", "sqdem_num_interactions", "sqdem_get_interactions",
+            "sqdem_put_interactions", "sqdem_get_scalars", "sqdem_put_scalars", "sqdem_stage_times",
+            "sqdem_shape_props", "sqdem_launch_count", "sqdem_set_record_full", "sqdem_time_steps",
+            "sqdem_time_e2e", "sqdem_time_contacts", "sqdem_set_use_graph"]
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def shape_props(rx, ry, rz, eps1, eps2):
+    """Superquadrics::Initial: (volume, Ixx, Iyy, Izz, r_max) at unit density."""
+    lib = load_library()
+    out = np.zeros(5)
+    st = lib.sqdem_shape_props(rx, ry, rz, eps1, eps2, _dp(out))
+    if st:
+        raise SqdemError(st, "bad shape parameters")
+    return out
+
+
+class Engine:
+    """One GPU scene behind the C ABI."""
+
+    def __init__(self, device=0, precision="fp64", contacts_per_body=16, use_graph=True):
+        self.lib = load_library()
+        self.h = C.c_void_p()
+        cfg = _Config(device, PRECISION[precision], contacts_per_body, 1 if use_graph else 0)
+        st = self.lib.sqdem_create(C.byref(self.h), C.byref(cfg))
+        if st:
+            msg = self.lib.sqdem_last_error(self.h).decode()
+            self.lib.sqdem_destroy(self.h)
+            self.h = None
+            raise SqdemError(st, msg)
+        self.n = 0
+
+    def _check(self, st):
+        if st:
+            raise SqdemError(st, self.lib.sqdem_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.sqdem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- set-up ---------------------------------------------------------------------------
+    def set_materials(self, Kn, Ks, frictionAngle, betan, betas, density):
+        arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (Kn, Ks, frictionAngle, betan, betas, density)]
+        self._check(self.lib.sqdem_set_materials(self.h, len(arrs[0]), *[_dp(a) for a in arrs]))
+
+    def set_bodies(self, kind, shape5, wall_axis_sense, mat, isSphere, state):
+        kind = np.ascontiguousarray(kind, dtype=np.int32)
+        n = len(kind)
+        shape5 = np.ascontiguousarray(shape5, dtype=np.float64).reshape(n, 5)
+        was = np.ascontiguousarray(wall_axis_sense, dtype=np.int32).reshape(n, 2)
+        mat = np.ascontiguousarray(mat, dtype=np.int32)
+        sph = np.ascontiguousarray(isSphere, dtype=np.int32)
+        state = np.ascontiguousarray(state, dtype=np.float64).reshape(n, BODY_STRIDE)
+        self._check(self.lib.sqdem_set_bodies(self.h, n, _ip(kind), _dp(shape5), _ip(was), _ip(mat), _ip(sph), _dp(state)))
+        self.n = n
+
+    def set_params(self, dt, gravity, damping, verletDist, targetInterv=50, minSweepDistFactor=0.1, sortAxis=0,
+                   isSuperquadrics=1, exactAsphericalRot=1):
+        p = _Params(dt, (C.c_double * 3)(*gravity), damping, verletDist, int(targetInterv), minSweepDistFactor,
+                    int(sortAxis), int(isSuperquadrics), int(exactAsphericalRot))
+        self._check(self.lib.sqdem_set_params(self.h, C.byref(p)))
+
+    def load(self, spec):
+        """Load a scene description (see sudodem_gb300.assemblies.SceneSpec)."""
+        m = spec.materials
+        self.set_materials(m["Kn"], m["Ks"], m["frictionAngle"], m["betan"], m["betas"], m["density"])
+        self.set_params(**spec.params)
+        self.set_bodies(spec.kind, spec.shape5, spec.wall_axis_sense, spec.mat, spec.isSphere, spec.state)
+
+    def set_use_graph(self, on=True):
+        self._check(self.lib.sqdem_set_use_graph(self.h, 1 if on else 0))
+
+    def set_record_full(self, on=True):
+        self._check(self.lib.sqdem_set_record_full(self.h, 1 if on else 0))
+
+    # -- stepping -------------------------------------------------------------------------
+    def step(self, n=1):
+        self._check(self.lib.sqdem_step(self.h, int(n)))
+
+    def sync(self):
+        r = _Report()
+        st = self.lib.sqdem_sync(self.h, C.byref(r))
+        rep = {f: getattr(r, f) for f, _ in _Report._fields_}
+        self._check(st)
+        return rep
+
+    def stage_times(self):
+        out = np.zeros(3)
+        self._check(self.lib.sqdem_stage_times(self.h, _dp(out)))
+        return out
+
+    def time_steps(self, n):
+        """Device milliseconds of n timesteps (events on the engine stream)."""
+        ms = C.c_double()
+        self._check(self.lib.sqdem_time_steps(self.h, int(n), C.byref(ms)))
+        return ms.value
+
+    def time_e2e(self, n, in_ptr, out_ptr):
+        """Device milliseconds of n x (H2D kinematics, step, D2H kinematics); pointers to host
+        buffers of 16 doubles per body (pinned for asynchronous copies)."""
+        ms = C.c_double()
+        self._check(self.lib.sqdem_time_e2e(self.h, int(n), C.c_void_p(in_ptr), C.c_void_p(out_ptr), C.byref(ms)))
+        return ms.value
+
+    def time_contacts(self, nrep=1):
+        ms = C.c_double()
+        self._check(self.lib.sqdem_time_contacts(self.h, int(nrep), C.byref(ms)))
+        return ms.value
+
+    def launch_count(self):
+        return int(self.lib.sqdem_launch_count(self.h))
+
+    # -- state exchange -------------------------------------------------------------------
+    def body_state(self):
+        out = np.zeros((self.n, BODY_STRIDE))
+        self._check(self.lib.sqdem_get_body_state(self.h, _dp(out)))
+        return out
+
+    def put_body_state(self, st):
+        st = np.ascontiguousarray(st, dtype=np.float64).reshape(self.n, BODY_STRIDE)
+        self._check(self.lib.sqdem_put_body_state(self.h, _dp(st)))
+
+    def kinematics(self, out=None):
+        if out is None:
+            out = np.zeros((self.n, 16))
+        self._check(self.lib.sqdem_get_kinematics(self.h, _dp(out)))
+        return out
+
+    def put_kinematics(self, k):
+        k = np.ascontiguousarray(k, dtype=np.float64).reshape(self.n, 16)
+        self._check(self.lib.sqdem_put_kinematics(self.h, _dp(k)))
+
+    def interactions(self, include_potential=True):
+        n = C.c_long()
+        self._check(self.lib.sqdem_num_interactions(self.h, 1 if include_potential else 0, C.byref(n)))
+        out = np.zeros((max(n.value, 1), INTR_STRIDE))
+        got = C.c_long()
+        self._check(self.lib.sqdem_get_interactions(self.h, 1 if include_potential else 0, _dp(out), n.value,
+                                                    C.byref(got)))
+        return out[: got.value]
+
+    def put_interactions(self, recs):
+        recs = np.ascontiguousarray(recs, dtype=np.float64).reshape(-1, INTR_STRIDE)
+        self._check(self.lib.sqdem_put_interactions(self.h, len(recs), _dp(recs)))
+
+    def scalars(self):
+        out = np.zeros(NSCALARS)
+        self._check(self.lib.sqdem_get_scalars(self.h, _dp(out)))
+        return out
+
+    def put_scalars(self, s):
+        s = np.ascontiguousarray(s, dtype=np.float64)
+        self._check(self.lib.sqdem_put_scalars(self.h, _dp(s)))

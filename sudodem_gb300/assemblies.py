@@ -1,0 +1,183 @@
+"""Seeded synthetic superellipsoid assemblies (the inputs of the benchmarks and tests).
+
+Every assembly is a :class:`SceneSpec`: plain numpy arrays in the body order of the
+reference (walls first, ids 0..5, so that the contact-physics wall convention ``id1 <= 5``
+of Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys holds, pkg/dem/Superquadrics.cpp:1100),
+materials and engine parameters.  Bodies are built as NewSuperquadrics_rot2 does
+(py/_superquadrics_utils.cpp:354-380): mass = density * volume, inertia = density * geometric
+inertia, orientation = the given quaternion normalised; walls as utils.wall
+(py/utils.py:311-327): fixed, non-aspherical.
+
+No public dataset is involved; all values come from ``numpy.random.default_rng(seed)``.
+"""
+from dataclasses import dataclass, field
+import math
+
+import numpy as np
+
+from . import _native
+
+BODY_STRIDE = _native.BODY_STRIDE
+
+
+@dataclass
+class SceneSpec:
+    kind: np.ndarray            # (N,) 0 superquadric, 1 wall
+    shape5: np.ndarray          # (N,5) rx ry rz eps1 eps2
+    wall_axis_sense: np.ndarray  # (N,2)
+    mat: np.ndarray             # (N,)
+    isSphere: np.ndarray        # (N,)
+    state: np.ndarray           # (N,37) see include/sqdem.h
+    materials: dict             # Kn Ks frictionAngle betan betas density -> (M,)
+    params: dict                # sqdem_params fields
+    info: dict = field(default_factory=dict)
+
+    @property
+    def n_bodies(self):
+        return len(self.kind)
+
+    @property
+    def n_particles(self):
+        return int(np.sum(self.kind == 0))
+
+
+def _quat_normalize(q):
+    # Eigen's normalize: coefficients (x,y,z,w); squaredNorm = (x²+y²)+(z²+w²); divide by sqrt
+    w, x, y, z = q
+    n2 = (x * x + y * y) + (z * z + w * w)
+    n = math.sqrt(n2)
+    return np.array([w / n, x / n, y / n, z / n])
+
+
+def random_quaternions(rng, n):
+    """Uniform random unit quaternions (w,x,y,z) from normalised 4-D Gaussians."""
+    q = rng.standard_normal((n, 4))
+    return np.array([_quat_normalize(qi) for qi in q])
+
+
+def _builder():
+    return {"kind": [], "shape5": [], "was": [], "mat": [], "sph": [], "state": []}
+
+
+def _add_wall(b, pos, axis, sense, mat=0):
+    st = np.zeros(BODY_STRIDE)
+    st[0:3] = pos
+    st[3] = 1.0
+    st[28:31] = np.nan
+    b["kind"].append(1); b["shape5"].append(np.zeros(5)); b["was"].append((axis, sense))
+    b["mat"].append(mat); b["sph"].append(0); b["state"].append(st)
+
+
+def _add_sq(b, rxyz, eps, q, pos, density, mat=0, isSphere=0, props_cache=None):
+    props = _native.shape_props(rxyz[0], rxyz[1], rxyz[2], eps[0], eps[1])
+    st = np.zeros(BODY_STRIDE)
+    st[0:3] = pos
+    st[3:7] = q
+    st[28:31] = np.nan
+    st[33] = density * props[0]
+    st[34:37] = props[1:4] * density
+    b["kind"].append(0); b["shape5"].append(np.array([*rxyz, *eps], dtype=np.float64)); b["was"].append((0, 0))
+    b["mat"].append(mat); b["sph"].append(isSphere); b["state"].append(st)
+
+
+def _finish(b, materials, params, info):
+    return SceneSpec(
+        kind=np.array(b["kind"], dtype=np.int32),
+        shape5=np.array(b["shape5"], dtype=np.float64).reshape(-1, 5),
+        wall_axis_sense=np.array(b["was"], dtype=np.int32).reshape(-1, 2),
+        mat=np.array(b["mat"], dtype=np.int32),
+        isSphere=np.array(b["sph"], dtype=np.int32),
+        state=np.array(b["state"], dtype=np.float64).reshape(-1, BODY_STRIDE),
+        materials={k: np.asarray(v, dtype=np.float64) for k, v in materials.items()},
+        params=params, info=info)
+
+
+def default_material(kn=1e5, ks_over_kn=0.5, friction=0.5, density=2650.0):
+    return {"Kn": [kn], "Ks": [kn * ks_over_kn], "frictionAngle": [math.atan(friction)], "betan": [0.0],
+            "betas": [0.0], "density": [density]}
+
+
+def critical_dt(spec, factor=0.5):
+    """dt = factor * sqrt(m_min / kn).  The reference has no superquadric critical-dt routine
+    (GlobalStiffnessTimeStepper handles ScGeom only)."""
+    m = spec.state[spec.kind == 0, 33]
+    kn = float(np.max(spec.materials["Kn"]))
+    return factor * math.sqrt(float(np.min(m)) / kn)
+
+
+def walled_lattice(n_particles, seed=0, r_range=(0.8e-3, 1.2e-3), eps_range=(0.5, 1.5), spacing=2.6e-3,
+                   jitter=0.1e-3, per_side=7, box=None, log_radius=False, friction=0.5, kn=1e5, damping=0.3,
+                   verletDist=0.2e-3, lid_height=None, dt_factor=0.5):
+    """Particles on a jittered cubic lattice above the floor of a walled box.
+
+    Six walls are created first: x-, x+, y-, y+, floor (sense +1 into the box) and a lid.
+    """
+    rng = np.random.default_rng(seed)
+    side = box if box is not None else per_side * spacing + 2 * (spacing - 0.0002)
+    if box is None:
+        side = max(side, 20e-3)
+    nx = max(1, int(round((side - spacing) / spacing)))
+    nx = min(nx, per_side) if box is None else nx
+    layers = int(math.ceil(n_particles / (nx * nx)))
+    top = spacing * (layers + 1) + 2e-3
+    lid = lid_height if lid_height is not None else max(10 * top, 0.2)
+    b = _builder()
+    _add_wall(b, [0, 0, 0], 0, +1)
+    _add_wall(b, [side, 0, 0], 0, -1)
+    _add_wall(b, [0, 0, 0], 1, +1)
+    _add_wall(b, [0, side, 0], 1, -1)
+    _add_wall(b, [0, 0, 0], 2, +1)
+    _add_wall(b, [0, 0, lid], 2, -1)
+    x0 = side / 2 - (nx - 1) * spacing / 2
+    z0 = 2.0e-3 if not log_radius else r_range[1] * math.sqrt(2) + 0.3e-3
+    density = 2650.0
+    if log_radius:
+        r = np.exp(rng.uniform(math.log(r_range[0]), math.log(r_range[1]), size=(n_particles, 3)))
+    else:
+        r = rng.uniform(r_range[0], r_range[1], size=(n_particles, 3))
+    eps = rng.uniform(eps_range[0], eps_range[1], size=(n_particles, 2))
+    q = random_quaternions(rng, n_particles)
+    jit = rng.uniform(-jitter, jitter, size=(n_particles, 3))
+    for p in range(n_particles):
+        layer, rem = divmod(p, nx * nx)
+        iy, ix = divmod(rem, nx)
+        pos = np.array([x0 + ix * spacing, x0 + iy * spacing, z0 + layer * spacing]) + jit[p]
+        _add_sq(b, r[p], eps[p], q[p], pos, density)
+    mats = default_material(kn=kn, friction=friction, density=density)
+    params = {"dt": 1.0, "gravity": (0.0, 0.0, -9.81), "damping": damping, "verletDist": verletDist,
+              "targetInterv": 50, "minSweepDistFactor": 0.1, "sortAxis": 0, "isSuperquadrics": 1,
+              "exactAsphericalRot": 1}
+    spec = _finish(b, mats, params, {"box": side, "layers": layers, "seed": seed})
+    spec.params["dt"] = critical_dt(spec, dt_factor)
+    return spec
+
+
+def config0(seed=0, n=1000):
+    """1,000 superellipsoids, half-axes U[0.8,1.2] mm, eps U[0.5,1.5], uniform random
+    orientations, jittered cubic lattice (2.6 mm, +-0.1 mm) 7x7 per layer above the floor of
+    a 20x20 mm walled box; kn=1e5 N/m, ks/kn=0.5, friction 0.5, density 2650, damping 0.3,
+    gravity -9.81, dt = 0.5 critical."""
+    return walled_lattice(n, seed=seed, box=20e-3, per_side=7)
+
+
+def deposition_box(n, seed=0, eps_range=(0.3, 1.8), r_range=(0.8e-3, 1.2e-3), log_radius=False, spacing=2.6e-3):
+    """Large walled deposition scene: a square box sized for ~n^(1/3)^2 particles per layer."""
+    per_side = max(7, int(round(n ** (1.0 / 3.0) * 1.6)))
+    box = per_side * spacing + 2 * (spacing - 0.0002)
+    return walled_lattice(n, seed=seed, box=box, per_side=per_side, eps_range=eps_range, r_range=r_range,
+                          log_radius=log_radius, spacing=spacing)
+
+
+def pair_scene(shapeA, shapeB, posA, posB, qA, qB, kn=1e5, friction=0.5, walls=True):
+    """Two superellipsoids (plus six far-away walls so ids match the wall convention)."""
+    b = _builder()
+    if walls:
+        far = 1.0
+        _add_wall(b, [-far, 0, 0], 0, +1); _add_wall(b, [far, 0, 0], 0, -1)
+        _add_wall(b, [0, -far, 0], 1, +1); _add_wall(b, [0, far, 0], 1, -1)
+        _add_wall(b, [0, 0, -far], 2, +1); _add_wall(b, [0, 0, far], 2, -1)
+    _add_sq(b, shapeA[:3], shapeA[3:5], _quat_normalize(qA), posA, 2650.0)
+    _add_sq(b, shapeB[:3], shapeB[3:5], _quat_normalize(qB), posB, 2650.0)
+    params = {"dt": 1e-6, "gravity": (0.0, 0.0, 0.0), "damping": 0.0, "verletDist": 0.0, "targetInterv": 50,
+              "minSweepDistFactor": 0.1, "sortAxis": 0, "isSuperquadrics": 1, "exactAsphericalRot": 1}
+    return _finish(b, default_material(kn=kn, friction=friction), params, {})

@@ -1,0 +1,223 @@
+// Device arithmetic for the superellipsoid hot path (FP64 form).
+//
+// Every expression keeps the reference's operand order: Eigen 3.3.5 with vectorisation
+// off reduces length-3 sums as a0 + (a1 + a2) (lib/Eigen/src/Core/Redux.h:91-105) and
+// evaluates small matrix-vector products coefficient-wise (Core/ProductEvaluators.h:550).
+// The translation unit that includes this header is compiled with --fmad=false so that
+// a*b+c is not contracted, as in the reference's x86-64 -O2 build.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace sqdem {
+
+struct D3 { double x, y, z; };
+__device__ __forceinline__ D3 d3(double a, double b, double c) { D3 r; r.x = a; r.y = b; r.z = c; return r; }
+__device__ __forceinline__ D3 operator+(D3 a, D3 b) { return d3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ D3 operator-(D3 a, D3 b) { return d3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ D3 operator-(D3 a) { return d3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ D3 operator*(double s, D3 a) { return d3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ D3 operator*(D3 a, double s) { return d3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ double dot(D3 a, D3 b) { return a.x * b.x + (a.y * b.y + a.z * b.z); }
+__device__ __forceinline__ double sqn(D3 a) { return a.x * a.x + (a.y * a.y + a.z * a.z); }
+__device__ __forceinline__ double nrm(D3 a) { return sqrt(sqn(a)); }
+__device__ __forceinline__ D3 cross(D3 a, D3 b) {
+  return d3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ void normalize(D3& a) {
+  double z = sqn(a);
+  if (z > 0) { double n = sqrt(z); a.x /= n; a.y /= n; a.z /= n; }
+}
+__device__ __forceinline__ double sgn(double f) { return f < 0 ? -1.0 : (f > 0 ? 1.0 : 0.0); }
+// std::max / std::min semantics (first argument wins unless the comparison is true),
+// which the reference relies on when a value is NaN (Dispatching.cpp:38-44).
+__device__ __forceinline__ double fmax_ref(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double fmin_ref(double a, double b) { return (b < a) ? b : a; }
+
+// Rotation matrix of a unit quaternion (Eigen Quaternion::toRotationMatrix,
+// Geometry/Quaternion.h:536-568).  The reference caches R (rot_mat2global) and
+// R^T = conj(q).toRotationMatrix() (rot_mat2local) on the shape; both are bit-identical
+// to what is built here from the same quaternion, so only R is kept.
+struct Rot { double m[9]; };
+__device__ __forceinline__ Rot quatToRot(double w, double x, double y, double z) {
+  const double tx = 2.0 * x, ty = 2.0 * y, tz = 2.0 * z;
+  const double twx = tx * w, twy = ty * w, twz = tz * w;
+  const double txx = tx * x, txy = ty * x, txz = tz * x;
+  const double tyy = ty * y, tyz = tz * y, tzz = tz * z;
+  Rot r;
+  r.m[0] = 1.0 - (tyy + tzz); r.m[1] = txy - twz;         r.m[2] = txz + twy;
+  r.m[3] = txy + twz;         r.m[4] = 1.0 - (txx + tzz); r.m[5] = tyz - twx;
+  r.m[6] = txz - twy;         r.m[7] = tyz + twx;         r.m[8] = 1.0 - (txx + tyy);
+  return r;
+}
+// R * v
+__device__ __forceinline__ D3 mulG(const Rot& R, D3 v) {
+  return d3(R.m[0] * v.x + (R.m[1] * v.y + R.m[2] * v.z),
+            R.m[3] * v.x + (R.m[4] * v.y + R.m[5] * v.z),
+            R.m[6] * v.x + (R.m[7] * v.y + R.m[8] * v.z));
+}
+// R^T * v == rot_mat2local * v (same coefficients, same order)
+__device__ __forceinline__ D3 mulL(const Rot& R, D3 v) {
+  return d3(R.m[0] * v.x + (R.m[3] * v.y + R.m[6] * v.z),
+            R.m[1] * v.x + (R.m[4] * v.y + R.m[7] * v.z),
+            R.m[2] * v.x + (R.m[5] * v.y + R.m[8] * v.z));
+}
+
+// Superellipsoid of one body with the exponents it needs per evaluation.
+struct SqShape {
+  double rx, ry, rz, e1, e2, rmax;
+  double a1, a2;       // 2 - eps1, 2 - eps2
+  double i1, i2;       // 1/(2 - eps1), 1/(2 - eps2)
+  Rot R;
+  D3 pos;
+};
+__device__ __forceinline__ void shapeInit(SqShape& s, double rx, double ry, double rz, double e1, double e2,
+                                          double rmax) {
+  s.rx = rx; s.ry = ry; s.rz = rz; s.e1 = e1; s.e2 = e2; s.rmax = rmax;
+  s.a1 = 2. - e1; s.a2 = 2. - e2;
+  s.i1 = 1 / (2. - e1); s.i2 = 1 / (2. - e2);
+}
+
+// Superquadrics::Normal2Phi (pkg/dem/Superquadrics.cpp:269-307), local frame.
+__device__ __forceinline__ void normal2phi(const SqShape& s, D3 n, double& ph0, double& ph1) {
+  ph0 = atan2(sgn(n.y) * pow(fabs(s.ry * n.y), s.i1), sgn(n.x) * pow(fabs(s.rx * n.x), s.i1));
+  ph1 = atan2(sgn(n.z) * pow(fabs(s.rz * n.z * pow(fabs(cos(ph0)), s.a1)), s.i2), pow(fabs(s.rx * n.x), s.i2));
+}
+// Superquadrics::getSurface (Superquadrics.cpp:110-120), local frame.
+__device__ __forceinline__ D3 surface(const SqShape& s, double ph0, double ph1) {
+  double s0, c0, s1, c1;
+  sincos(ph0, &s0, &c0);
+  sincos(ph1, &s1, &c1);
+  const double pc1 = pow(fabs(c1), s.e2);
+  D3 r;
+  r.x = sgn(c0) * s.rx * pow(fabs(c0), s.e1) * pc1;
+  r.y = sgn(s0) * s.ry * pow(fabs(s0), s.e1) * pc1;
+  r.z = sgn(s1) * s.rz * pow(fabs(s1), s.e2);
+  return r;
+}
+// Superquadrics::isInside (Superquadrics.cpp:103-108); p is relative to the centre.
+__device__ __forceinline__ bool isInside(const SqShape& s, D3 p) {
+  p = mulL(s.R, p);
+  return 1 > pow(pow(fabs(p.x / s.rx), 2.0 / s.e1) + pow(fabs(p.y / s.ry), 2.0 / s.e1), s.e1 / s.e2) +
+                 pow(fabs(p.z / s.rz), 2.0 / s.e2);
+}
+
+// Disfunction, 9-argument form (pkg/dem/Superquadrics_Ig2.cpp:622-687).
+__device__ __forceinline__ void disfunction(const SqShape& A, const SqShape& B, double pa0, double pa1, D3& center,
+                                            D3& p1, D3& p2, bool& stop_flag) {
+  double sa0, ca0, sa1, ca1;
+  sincos(pa0, &sa0, &ca0);
+  sincos(pa1, &sa1, &ca1);
+  D3 contact = d3(ca0 * ca1, sa0 * ca1, sa1);
+  double ph0, ph1;
+  normal2phi(A, mulL(A.R, contact), ph0, ph1);
+  p1 = mulG(A.R, surface(A, ph0, ph1)) + A.pos;
+  normal2phi(B, (-1.0) * mulL(B.R, contact), ph0, ph1);
+  p2 = mulG(B.R, surface(B, ph0, ph1)) + B.pos;
+  D3 d = p2 - p1;
+  center = 0.5 * (p1 + p2);
+  if (dot(contact, d) > 0) stop_flag = true;
+}
+
+struct LMOut { int iters; int stop; };
+
+// lmder2 (Superquadrics_Ig2.cpp:1057-1354) with the JacfunctionApp forward-difference
+// Jacobian (:1033-1054) and opts {1.0, 1e-15, 1e-3, 1e-20}.
+__device__ __noinline__ LMOut lmder2(const SqShape& A, const SqShape& B, double p[2], int itmax, D3& p1, D3& p2,
+                                     D3& center, bool& touching, D3& contact) {
+  const double tau = 1.0, eps1 = 1e-15, eps2 = 1e-3, eps3 = 1e-20;
+  const double EPSILON = 1e-12, ONE_THIRD = 0.3333333333333334;
+  touching = true;
+  D3 p_f, pDp_f;
+  double jacTf0, jacTf1, diag0, diag1;
+  double j00, j01, j10, j11;  // J^T J
+  double Dp0 = 1e-7, Dp1 = 1e-7;
+  bool stop_flag = false;
+  double mu = 0, tmp;
+  double jacTf_inf, p_L2, Dp_L2, dF, dL, p_fL2, pDp_fL2;
+  int nu = 2, nu2, stop = 0, k;
+  disfunction(A, B, p[0], p[1], center, p1, p2, stop_flag);
+  p_f = p2 - p1;
+  p_fL2 = nrm(p_f);
+  if (!isfinite(p_fL2)) stop = 7;
+  for (k = 0; k < itmax && !stop; ++k) {
+    if (p_fL2 <= eps3) { stop = 6; break; }
+    if (stop_flag) { stop = 9; touching = false; break; }
+    {
+      double s0, c0, s1, c1;
+      sincos(p[0], &s0, &c0);
+      sincos(p[1], &s1, &c1);
+      contact = d3(c0 * c1, s0 * c1, s1);
+      double angle = dot(p_f, contact) / (nrm(p_f) * nrm(contact));
+      if (fabs(angle) > 0.95) { stop = 8; break; }
+    }
+    D3 f0, f1, f2;
+    disfunction(A, B, p[0], p[1], center, p1, p2, stop_flag);
+    f0 = p2 - p1;
+    disfunction(A, B, p[0] + Dp0, p[1], center, p1, p2, stop_flag);
+    f1 = p2 - p1;
+    disfunction(A, B, p[0], p[1] + Dp1, center, p1, p2, stop_flag);
+    f2 = p2 - p1;
+    const double J00 = (f1.x - f0.x) / Dp0, J10 = (f1.y - f0.y) / Dp0, J20 = (f1.z - f0.z) / Dp0;
+    const double J01 = (f2.x - f0.x) / Dp1, J11 = (f2.y - f0.y) / Dp1, J21 = (f2.z - f0.z) / Dp1;
+    j00 = J00 * J00 + (J10 * J10 + J20 * J20);
+    j01 = J00 * J01 + (J10 * J11 + J20 * J21);
+    j10 = J01 * J00 + (J11 * J10 + J21 * J20);
+    j11 = J01 * J01 + (J11 * J11 + J21 * J21);
+    (void)j10;
+    jacTf0 = J00 * (-1.0 * p_f.x) + (J10 * (-1.0 * p_f.y) + J20 * (-1.0 * p_f.z));
+    jacTf1 = J01 * (-1.0 * p_f.x) + (J11 * (-1.0 * p_f.y) + J21 * (-1.0 * p_f.z));
+    jacTf_inf = (fabs(jacTf0) > fabs(jacTf1) ? fabs(jacTf0) : fabs(jacTf1));
+    p_L2 = sqrt(p[0] * p[0] + p[1] * p[1]);
+    if (jacTf_inf <= eps1) { stop = 1; break; }
+    if (k == 0) {
+      tmp = (j00 > j11 ? j00 : j11);
+      mu = tau * tmp;
+    }
+    diag0 = j00; diag1 = j11;
+    while (1) {
+      j00 += mu;
+      j11 += mu;
+      const double n_a = j00 * j11 - j01 * j01;
+      Dp0 = (jacTf0 * j11 - jacTf1 * j01) / n_a;
+      Dp1 = (jacTf1 * j00 - jacTf0 * j01) / n_a;
+      Dp_L2 = sqrt(Dp0 * Dp0 + Dp1 * Dp1);
+      if (Dp_L2 < 1e-5) { stop = 2; break; }
+      const double q0 = p[0] + Dp0, q1 = p[1] + Dp1;
+      if (Dp_L2 >= (p_L2 + eps2) / (EPSILON * EPSILON)) { stop = 4; break; }
+      disfunction(A, B, q0, q1, center, p1, p2, stop_flag);
+      pDp_f = p2 - p1;
+      pDp_fL2 = nrm(pDp_f);
+      if (!isfinite(pDp_fL2)) { stop = 7; break; }
+      dL = Dp0 * (mu * Dp0 + jacTf0) + Dp1 * (mu * Dp1 + jacTf1);
+      dF = p_fL2 - pDp_fL2;
+      tmp = dF / dL;
+      if (tmp > 0.0) {
+        tmp = 1.0 - pow(2 * tmp - 1., 3.);
+        mu = mu * ((tmp >= ONE_THIRD) ? tmp : ONE_THIRD);
+        nu = 2;
+        p[0] = q0; p[1] = q1;
+        p_f = pDp_f;
+        p_fL2 = pDp_fL2;
+        break;
+      }
+      mu *= nu;
+      nu2 = (int)((unsigned)nu << 1);
+      if (nu2 <= nu) { stop = 5; break; }
+      nu = nu2;
+      j00 = diag0; j11 = diag1;
+    }
+  }
+  if (k >= itmax) stop = 3;
+  LMOut o; o.iters = k; o.stop = stop;
+  return o;
+}
+
+__device__ __forceinline__ void centerLine(D3 pos1, D3 pos2, double para[2]) {
+  D3 d0 = pos2 - pos1;
+  para[0] = atan2(d0.y, d0.x);
+  para[1] = atan(d0.z / sqrt(d0.x * d0.x + d0.y * d0.y));
+  para[0] += 1e-5; para[1] += 1e-5;
+}
+
+}  // namespace sqdem

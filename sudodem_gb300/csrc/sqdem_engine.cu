@@ -1,0 +1,1902 @@
+// libsqdem_gpu.so — GB300 (sm_103a) engine for SudoDEM3D's superellipsoid timestep.
+//
+// One timestep is this kernel sequence on the context stream (captured once in a CUDA
+// graph and replayed):
+//
+//   k_gate          InsertionSortCollider::isActivated   (InsertionSortCollider.cpp:177-189)
+//   collider pass   InsertionSortCollider::action        (InsertionSortCollider.cpp:191-400)
+//     k_bounds        BoundDispatcher::processBody + Bo1_* (Dispatching.cpp:30-62,
+//                     Superquadrics.cpp:639-686, Wall.cpp:13-21)
+//     k_grid_setup / k_cell_count / scan / k_cell_scatter   counting-sort binning on a
+//                     uniform grid whose cell is at least the largest bound extent
+//     k_candidates    overlap tests against the 27 neighbour cells and the walls, then a
+//                     sorted per-body candidate row merged with the body's previous row
+//                     (conditionalyEraseNonReal + insert, InteractionContainer.cpp:13-39)
+//     k_merge         writes the new contact table (rows ordered by partner id), keeping
+//                     contact history for pairs that survive
+//     k_pcount / k_pscatter / k_psort / k_wall_*   incidence lists for the force gather
+//   k_contacts      InteractionLoop body: Ig2_* + Ip2_* + SuperquadricsLaw
+//                   (InteractionLoop.cpp:56-141; Superquadrics_Ig2.cpp:1880-2317,2522-2611;
+//                   Superquadrics.cpp:1030-1116,1181-1363)
+//   k_wall_forces   ForceContainer sum for walls (ForceContainer.hpp:134-162)
+//   k_integrate     ForceContainer sum for particles + NewtonIntegrator::action
+//                   (NewtonIntegrator.cpp:99-304)
+//   k_end           Scene::moveToNextTimeStep epilogue (Scene.cpp:114-115)
+//
+// Collider kernels return at once when k_gate decided the collider does not run this step.
+// Compiled with --fmad=false: FP64 results keep the reference's rounding sequence up to the
+// last-ulp differences between CUDA's and glibc's pow/atan2/sin/cos.
+#include <cuda_runtime.h>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cstdint>
+#include <cmath>
+#include <vector>
+#include <string>
+#include <algorithm>
+#include <limits>
+#include "sq_device.cuh"
+#include "../../include/sqdem.h"
+
+namespace sqdem {
+
+// ---------------------------------------------------------------------------
+// Device-side state
+enum : unsigned {
+  F_GEOM = 1u,        // Interaction::geom present
+  F_PHYS = 2u,        // Interaction::phys present
+  F_SHEARNEW = 4u,    // SuperquadricsGeom::isShearNew
+  F_OWNER_ID1 = 8u,   // the row owner is Interaction::id1 (else the partner is)
+  F_FORCE = 16u,      // the law applied a force this step
+};
+enum { KIND_SQ = 0, KIND_WALL = 1 };
+static const unsigned DOF_ALL = 63u;
+
+struct Params {
+  double dt, g[3], damping, verletDist, minSweepDistFactor, h0;
+  int targetInterv, sortAxis, isSuperquadrics, exactAsphericalRot, recordFull;
+};
+
+enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_NUM };
+
+struct SceneState {
+  long long iter; double time;
+  double maxVelocitySq, fastestBodyMaxDist, verletDistCur;
+  int strideActive, newtonFound, doSort, dirty, bbInit;
+  int runCollider, initSort, newtonRan, maxDispCode;
+  int P, Pnew, nWW, overflowRun;
+  int numReinit; long long colliderRuns;
+  unsigned long long bbLo[3], bbHi[3];   // order-preserving encodings of the bbox of particle bound centres
+  double org[3]; double h; int dim[3]; int nCells;
+  unsigned long long err[E_NUM];
+};
+
+// Contact table, structure of arrays (one set per buffer).
+struct Table {
+  int* owner; int* partner; unsigned* flags;
+  double2* angle; double* depth; double4* normal; double4* shear; double4* nforce;
+  double4* phys;          // kn, ks, tanphi, -
+  double4* F; double4* cp;
+  // full geometry record (written only when Params::recordFull)
+  double4* p1; double4* p2; double4* shearInc; double4* twist; double4* ortho; double4* relVn; double4* relVs;
+};
+
+struct Dev {
+  int N, W, Pcap, Gmax, MAXC, NP;   // NP = particles
+  Params* prm; SceneState* S;
+  // bodies
+  double4 *pos, *ori, *vel, *angVel, *angMom, *inertia, *shpA, *shpB;   // shpA (rx,ry,rz,rmax) shpB (e1,e2,-,-)
+  double* mass; int4* info;  // info: kind, mat, isSphere, wall axis | (sense+1)<<4
+  unsigned* blocked; int* damped; int* aspherical;
+  double4 *bmin, *bmax, *ref, *pmin, *pmax;    // bmin.w sweepLength, bmax.w lastUpdateIter, ref.w hasBound
+  double4 *force, *torque;
+  int* walls;                 // ids of walls
+  double4* mats;              // Kn, Ks, frictionAngle, density
+  double2* matsB;             // betan, betas
+  // tables
+  Table A, B;
+  int* rowStart; int* rowStartNew; int* rowCount;
+  int* cand; int* candCount;
+  int* pCount; int* pStart; int* pFill; int* pList;
+  int* wCount; int* wList;
+  int2* ww;
+  // grid
+  int* bodyCell; int* cellCount; int* cellStart; int* cellFill; int* cellBodies;
+  int* scanTmp;
+  unsigned long long* bbPart;
+};
+
+__device__ __forceinline__ unsigned long long encOrd(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double decOrd(unsigned long long u) {
+  unsigned long long b = (u >> 63) ? (u & 0x7fffffffffffffffull) : ~u;
+  return __longlong_as_double((long long)b);
+}
+__device__ __forceinline__ D3 xyz(double4 v) { return d3(v.x, v.y, v.z); }
+__device__ __forceinline__ double4 dd4(D3 a, double w) { return make_double4(a.x, a.y, a.z, w); }
+__device__ __forceinline__ double comp(double4 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+// ---------------------------------------------------------------------------
+// Exclusive scan over n+1 ints (in[n] treated as 0), three launches, gated.
+static const int SCAN_BS = 1024, SCAN_IPT = 4, SCAN_TILE = SCAN_BS * SCAN_IPT;
+
+__device__ __forceinline__ int blockExclusiveScan(int v, int* sh, int& total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) { int y = __shfl_up_sync(0xffffffffu, x, o); if (lane >= o) x += y; }
+  if (lane == 31) sh[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int s = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) { int y = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += y; }
+    sh[lane] = s;
+  }
+  __syncthreads();
+  total = sh[(blockDim.x >> 5) - 1];
+  int res = x - v + (wid > 0 ? sh[wid - 1] : 0);
+  __syncthreads();
+  return res;
+}
+
+__global__ void k_scan_reduce(const int* __restrict__ in, int n, int* __restrict__ blockSums, const int* gate) {
+  if (gate && !*gate) return;
+  __shared__ int sh[32];
+  int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_IPT;
+  int s = 0;
+  for (int k = 0; k < SCAN_IPT; k++) { int i = base + k; if (i < n) s += in[i]; }
+  int total;
+  blockExclusiveScan(s, sh, total);
+  if (threadIdx.x == 0) blockSums[blockIdx.x] = total;
+}
+__global__ void k_scan_blocks(int* blockSums, int nb, const int* gate) {
+  if (gate && !*gate) return;
+  __shared__ int sh[32];
+  int carry = 0;
+  for (int b0 = 0; b0 < nb; b0 += blockDim.x) {
+    int i = b0 + threadIdx.x;
+    int v = i < nb ? blockSums[i] : 0;
+    int total;
+    int ex = blockExclusiveScan(v, sh, total);
+    if (i < nb) blockSums[i] = ex + carry;
+    carry += total;
+    __syncthreads();
+  }
+}
+// out[i] = sum(in[0..i)) for i in [0, n]; out[n] = total
+__global__ void k_scan_apply(const int* __restrict__ in, int n, const int* __restrict__ blockSums, int* __restrict__ out,
+                             const int* gate) {
+  if (gate && !*gate) return;
+  __shared__ int sh[32];
+  int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_IPT;
+  int v[SCAN_IPT]; int s = 0;
+  for (int k = 0; k < SCAN_IPT; k++) { int i = base + k; v[k] = (i < n) ? in[i] : 0; s += v[k]; }
+  int total;
+  int ex = blockExclusiveScan(s, sh, total) + blockSums[blockIdx.x];
+  for (int k = 0; k < SCAN_IPT; k++) { int i = base + k; if (i <= n) out[i] = ex; ex += v[k]; }
+}
+
+// ---------------------------------------------------------------------------
+// Collider gate: InsertionSortCollider::isActivated (InsertionSortCollider.cpp:177-189)
+// plus the start of action() (:205-252) and the NewtonIntegrator maxVelocitySq readout.
+__global__ void k_gate(Dev d) {
+  SceneState& S = *d.S;
+  if (S.newtonRan) {
+    S.maxVelocitySq = S.maxDispCode == 2 ? 2.0 : (S.maxDispCode == 1 ? 0.5 : 0.0);
+    S.maxDispCode = 0; S.newtonRan = 0;
+  }
+  int run;
+  if (!S.strideActive) run = 1;
+  else if (!S.newtonFound) run = 1;
+  else if (S.fastestBodyMaxDist < 0) { S.fastestBodyMaxDist = 0; run = 1; }
+  else {
+    S.fastestBodyMaxDist = S.maxVelocitySq;
+    if (S.fastestBodyMaxDist >= 1 || S.fastestBodyMaxDist == 0) run = 1;
+    else if (!S.bbInit) run = 1;
+    else if (S.dirty) run = 1;
+    else run = 0;
+  }
+  S.runCollider = run;
+  if (run) {
+    int init = 0;
+    if (S.doSort) { init = 1; S.doSort = 0; }
+    if (!S.bbInit) init = 1;
+    if (S.verletDistCur < 0) S.verletDistCur = 0;
+    if (S.dirty) { init = 1; S.dirty = 0; }
+    S.initSort = init;
+    S.overflowRun = 0;
+    for (int k = 0; k < 3; k++) { S.bbLo[k] = ~0ull; S.bbHi[k] = 0ull; }
+  }
+}
+
+// BoundDispatcher::processBody (Dispatching.cpp:30-62), Bo1_Superquadrics_Aabb::go
+// (Superquadrics.cpp:639-686), Bo1_Wall_Aabb::go (Wall.cpp:13-21).
+__global__ void k_bounds(Dev d) {
+  const SceneState& S = *d.S;
+  if (!S.runCollider) return;
+  const Params& P = *d.prm;
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  double cmin[3] = {INFINITY, INFINITY, INFINITY}, cmax[3] = {-INFINITY, -INFINITY, -INFINITY};
+  if (b < d.N) {
+    const double sweepDist = S.verletDistCur;
+    double4 pos = d.pos[b];
+    double4 mn = d.bmin[b], mx = d.bmax[b], rf = d.ref[b];
+    int4 inf = d.info[b];
+    bool hasBound = rf.w != 0;
+    double sweepLength = mn.w;
+    double lastUpd = mx.w;
+    if (hasBound) {
+      if (P.targetInterv >= 0) {
+        D3 disp = xyz(pos) - xyz(rf);
+        double dist = fmax_ref(fabs(disp.x), fmax_ref(fabs(disp.y), fabs(disp.z)));
+        if (dist != 0) {  // NaN (never bounded) also takes this branch
+          double newLength = dist * P.targetInterv / (double)(S.iter - (long long)lastUpd);
+          newLength = fmax_ref(0.9 * sweepLength, newLength);
+          sweepLength = fmax_ref(P.minSweepDistFactor * sweepDist, fmin_ref(newLength, sweepDist));
+        } else sweepLength = 0;
+      } else sweepLength = sweepDist;
+    }
+    d.pmin[b] = mn; d.pmax[b] = mx;
+    D3 lo, hi;
+    if (inf.x == KIND_SQ) {
+      double r = d.shpA[b].w;
+      lo = xyz(pos) + d3(-r, -r, -r);
+      hi = xyz(pos) + d3(r, r, r);
+    } else {
+      int ax = inf.w & 15;
+      lo = d3(-INFINITY, -INFINITY, -INFINITY); hi = d3(INFINITY, INFINITY, INFINITY);
+      if (ax == 0) { lo.x = hi.x = pos.x; } else if (ax == 1) { lo.y = hi.y = pos.y; } else { lo.z = hi.z = pos.z; }
+    }
+    if (!hasBound) sweepLength = 0;
+    if (sweepLength > 0) {
+      lo = lo - d3(sweepLength, sweepLength, sweepLength);
+      hi = hi + d3(sweepLength, sweepLength, sweepLength);
+    }
+    d.bmin[b] = dd4(lo, sweepLength);
+    d.bmax[b] = dd4(hi, (double)S.iter);
+    d.ref[b] = make_double4(pos.x, pos.y, pos.z, 1.0);
+    if (inf.x == KIND_SQ) {
+      D3 c = 0.5 * (lo + hi);
+      cmin[0] = cmax[0] = c.x; cmin[1] = cmax[1] = c.y; cmin[2] = cmax[2] = c.z;
+    }
+  }
+  // block bbox of particle bound centres -> global atomics on ordered encodings
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    double a = cmin[k], z = cmax[k];
+    for (int o = 16; o > 0; o >>= 1) {
+      a = fmin(a, __shfl_down_sync(0xffffffffu, a, o));
+      z = fmax(z, __shfl_down_sync(0xffffffffu, z, o));
+    }
+    if ((threadIdx.x & 31) == 0 && a <= z) {
+      atomicMin(&d.S->bbLo[k], encOrd(a));
+      atomicMax(&d.S->bbHi[k], encOrd(z));
+    }
+  }
+}
+
+__global__ void k_grid_setup(Dev d) {
+  SceneState& S = *d.S;
+  if (!S.runCollider) return;
+  const Params& P = *d.prm;
+  // post-dispatch stride bookkeeping (InsertionSortCollider.cpp:263-284)
+  if (S.verletDistCur > 0) S.newtonFound = 1;
+  if (!S.strideActive && S.verletDistCur > 0 && S.maxVelocitySq >= 0) S.strideActive = 1;
+  double lo[3], hi[3];
+  bool any = true;
+  for (int k = 0; k < 3; k++) {
+    if (S.bbLo[k] == ~0ull) { any = false; lo[k] = 0; hi[k] = 0; }
+    else { lo[k] = decOrd(S.bbLo[k]); hi[k] = decOrd(S.bbHi[k]); }
+  }
+  if (!any) for (int k = 0; k < 3; k++) { lo[k] = 0; hi[k] = 0; }
+  for (int k = 0; k < 3; k++)
+    if (!isfinite(lo[k]) || !isfinite(hi[k]) || !(hi[k] >= lo[k])) { lo[k] = 0; hi[k] = 0; }
+  double h = P.h0;
+  if (!(h > 0) || !isfinite(h)) h = 1.0;
+  long long cells = 1;
+  int dim[3] = {1, 1, 1};
+  for (int it = 0; it < 4096; it++) {
+    cells = 1;
+    for (int k = 0; k < 3; k++) {
+      double q = floor((hi[k] - lo[k]) / h);
+      long long n = (q >= 0 && q < (double)(1 << 20)) ? (long long)q + 3 : (1ll << 20);
+      dim[k] = (int)n; cells *= n;
+    }
+    if (cells <= d.Gmax) break;
+    h *= 1.25;
+  }
+  if (cells > d.Gmax) { dim[0] = dim[1] = dim[2] = 1; cells = 1; }
+  for (int k = 0; k < 3; k++) { S.org[k] = lo[k] - h; S.dim[k] = dim[k]; }
+  S.h = h;
+  S.nCells = (int)cells;
+}
+
+__global__ void k_zero_cells(Dev d) {
+  if (!d.S->runCollider) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= d.Gmax; i += gridDim.x * blockDim.x) {
+    d.cellCount[i] = 0; d.cellFill[i] = 0;
+  }
+}
+
+// clamped cell coordinate; NaN maps to 0 so that no index leaves [0, dim)
+__device__ __forceinline__ int cellCoord(double c, double org, double h, int dim) {
+  double f = floor((c - org) / h);
+  if (!(f >= 0)) return 0;
+  if (f > (double)(dim - 1)) return dim - 1;
+  return (int)f;
+}
+
+__global__ void k_cell_count(Dev d) {
+  const SceneState& S = *d.S;
+  if (!S.runCollider) return;
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= d.N) return;
+  if (d.info[b].x != KIND_SQ) { d.bodyCell[b] = -1; return; }
+  double4 mn = d.bmin[b], mx = d.bmax[b];
+  int cx = cellCoord(0.5 * (mn.x + mx.x), S.org[0], S.h, S.dim[0]);
+  int cy = cellCoord(0.5 * (mn.y + mx.y), S.org[1], S.h, S.dim[1]);
+  int cz = cellCoord(0.5 * (mn.z + mx.z), S.org[2], S.h, S.dim[2]);
+  int cell = (cz * S.dim[1] + cy) * S.dim[0] + cx;
+  d.bodyCell[b] = cell;
+  atomicAdd(&d.cellCount[cell], 1);
+}
+__global__ void k_cell_scatter(Dev d) {
+  if (!d.S->runCollider) return;
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= d.N) return;
+  int cell = d.bodyCell[b];
+  if (cell < 0) return;
+  int slot = d.cellStart[cell] + atomicAdd(&d.cellFill[cell], 1);
+  d.cellBodies[slot] = b;
+}
+
+// closed overlap test, InsertionSortCollider::spatialOverlap (InsertionSortCollider.hpp:166-171)
+__device__ __forceinline__ bool overlapClosed(double4 amn, double4 amx, double4 bmn, double4 bmx) {
+  return (amn.x <= bmx.x) && (amx.x >= bmn.x) && (amn.y <= bmx.y) && (amx.y >= bmn.y) && (amn.z <= bmx.z) &&
+         (amx.z >= bmn.z);
+}
+
+// Orientation of a pair that enters the container at this collider pass.
+// Returns 1: (i, j) with i = id1; 0: (j, i); -1: the reference's sort would not insert it.
+//  * full sort (first pass, doSort, dirty): the body whose lower bound comes first on
+//    sortAxis is id1 (InsertionSortCollider.cpp:357-376; equal coordinates: lower id);
+//  * incremental insertion sort: axes 0,1,2 in turn; on the first axis where the lower
+//    bound of one body moved below the upper bound of the other since the previous pass,
+//    the body whose lower bound moved is id1 (InsertionSortCollider.cpp:29-54).
+__device__ __forceinline__ int orientNew(const Dev& d, int i, int j, int initSort, int sortAxis) {
+  double4 imn = d.bmin[i], jmn = d.bmin[j];
+  if (initSort) {
+    double a = comp(imn, sortAxis), b = comp(jmn, sortAxis);
+    if (a < b) return 1;
+    if (b < a) return 0;
+    return i < j ? 1 : 0;
+  }
+  double4 imx = d.bmax[i], jmx = d.bmax[j];
+  double4 ipn = d.pmin[i], ipx = d.pmax[i], jpn = d.pmin[j], jpx = d.pmax[j];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    if (comp(jpx, k) < comp(ipn, k) && comp(jmx, k) > comp(imn, k)) return 1;
+    if (comp(ipx, k) < comp(jpn, k) && comp(imx, k) > comp(jmn, k)) return 0;
+  }
+  return -1;
+}
+
+// Candidate row of particle i: partners j>i (particles) and all walls whose bounds overlap
+// i's, sorted by partner id, each tagged with its orientation bit (bit 31).  The union with
+// i's previous row gives the new row length: old entries survive if real or overlapping
+// (conditionalyEraseNonReal), new overlapping pairs are inserted when the sort would insert
+// them.
+__global__ void k_candidates(Dev d) {
+  const SceneState& S = *d.S;
+  if (!S.runCollider) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.N) return;
+  if (d.info[i].x != KIND_SQ) { d.rowCount[i] = 0; d.candCount[i] = 0; return; }
+  const double4 imn = d.bmin[i], imx = d.bmax[i];
+  int* cand = d.cand + (size_t)i * d.MAXC;
+  int n = 0; bool over = false;
+  const int cx = cellCoord(0.5 * (imn.x + imx.x), S.org[0], S.h, S.dim[0]);
+  const int cy = cellCoord(0.5 * (imn.y + imx.y), S.org[1], S.h, S.dim[1]);
+  const int cz = cellCoord(0.5 * (imn.z + imx.z), S.org[2], S.h, S.dim[2]);
+  for (int dz = -1; dz <= 1; dz++) {
+    int z = cz + dz; if (z < 0 || z >= S.dim[2]) continue;
+    for (int dy = -1; dy <= 1; dy++) {
+      int y = cy + dy; if (y < 0 || y >= S.dim[1]) continue;
+      for (int dx = -1; dx <= 1; dx++) {
+        int x = cx + dx; if (x < 0 || x >= S.dim[0]) continue;
+        int cell = (z * S.dim[1] + y) * S.dim[0] + x;
+        int s = d.cellStart[cell], e = d.cellStart[cell + 1];
+        for (int k = s; k < e; k++) {
+          int j = d.cellBodies[k];
+          if (j <= i) continue;
+          if (overlapClosed(imn, imx, d.bmin[j], d.bmax[j])) {
+            if (n < d.MAXC) cand[n++] = j; else over = true;
+          }
+        }
+      }
+    }
+  }
+  for (int w = 0; w < d.W; w++) {
+    int j = d.walls[w];
+    if (overlapClosed(imn, imx, d.bmin[j], d.bmax[j])) {
+      if (n < d.MAXC) cand[n++] = j; else over = true;
+    }
+  }
+  if (over) atomicAdd(&d.S->err[E_OVERFLOW], 1ull);
+  // insertion sort by partner id
+  for (int a = 1; a < n; a++) {
+    int v = cand[a]; int b = a - 1;
+    while (b >= 0 && cand[b] > v) { cand[b + 1] = cand[b]; b--; }
+    cand[b + 1] = v;
+  }
+  // union with the previous row
+  const int os = d.rowStart[i], oe = d.rowStart[i + 1];
+  int o = os, c = 0, cnt = 0, m = 0;
+  while (o < oe || c < n) {
+    int po = o < oe ? d.A.partner[o] : 0x7fffffff;
+    int pc = c < n ? cand[c] : 0x7fffffff;
+    if (po == pc) { cnt++; cand[m++] = pc; o++; c++; }     // survives, history kept
+    else if (po < pc) {                                     // not overlapping any more
+      if ((d.A.flags[o] & (F_GEOM | F_PHYS)) == (F_GEOM | F_PHYS)) cnt++;
+      o++;
+    } else {                                                // new pair
+      int orient;
+      if (d.info[pc].x == KIND_WALL) {
+        orient = S.initSort ? 1 : orientNew(d, i, pc, 0, 0);
+        if (orient >= 0) orient = 0;  // the geometry functor is (Wall, Superquadrics): wall is id1
+      } else orient = orientNew(d, i, pc, S.initSort, d.prm->sortAxis);
+      if (orient >= 0) { cnt++; cand[m++] = pc | (orient ? (int)0x80000000 : 0); }
+      c++;
+    }
+  }
+  d.candCount[i] = m;
+  d.rowCount[i] = cnt;
+}
+
+__global__ void k_check_capacity(Dev d) {
+  SceneState& S = *d.S;
+  if (!S.runCollider) return;
+  int Pn = d.rowStartNew[d.N];
+  S.Pnew = Pn;
+  if (Pn > d.Pcap) { S.overflowRun = 1; atomicAdd(&S.err[E_OVERFLOW], 1ull); }
+}
+
+__device__ __forceinline__ void copyEntry(const Table& s, int a, const Table& t, int b, bool full) {
+  t.owner[b] = s.owner[a]; t.partner[b] = s.partner[a]; t.flags[b] = s.flags[a];
+  t.angle[b] = s.angle[a]; t.depth[b] = s.depth[a]; t.normal[b] = s.normal[a]; t.shear[b] = s.shear[a];
+  t.nforce[b] = s.nforce[a]; t.phys[b] = s.phys[a]; t.F[b] = s.F[a]; t.cp[b] = s.cp[a];
+  if (full) {
+    t.p1[b] = s.p1[a]; t.p2[b] = s.p2[a]; t.shearInc[b] = s.shearInc[a]; t.twist[b] = s.twist[a];
+    t.ortho[b] = s.ortho[a]; t.relVn[b] = s.relVn[a]; t.relVs[b] = s.relVs[a];
+  }
+}
+__device__ __forceinline__ void initEntry(const Table& t, int b, int owner, int partner, bool ownerIsId1, bool full) {
+  const double4 z = make_double4(0, 0, 0, 0);
+  t.owner[b] = owner; t.partner[b] = partner; t.flags[b] = F_SHEARNEW | (ownerIsId1 ? F_OWNER_ID1 : 0u);
+  t.angle[b] = make_double2(0, 0); t.depth[b] = 0; t.normal[b] = z; t.shear[b] = z; t.nforce[b] = z;
+  t.phys[b] = z; t.F[b] = z; t.cp[b] = z;
+  if (full) { t.p1[b] = z; t.p2[b] = z; t.shearInc[b] = z; t.twist[b] = z; t.ortho[b] = z; t.relVn[b] = z; t.relVs[b] = z; }
+}
+
+__global__ void k_merge(Dev d) {
+  const SceneState& S = *d.S;
+  if (!S.runCollider || S.overflowRun) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.N) return;
+  if (d.info[i].x != KIND_SQ) return;
+  const bool full = d.prm->recordFull != 0;
+  const int* cand = d.cand + (size_t)i * d.MAXC;
+  const int n = d.candCount[i];
+  const int os = d.rowStart[i], oe = d.rowStart[i + 1];
+  int out = d.rowStartNew[i];
+  int o = os, c = 0;
+  while (o < oe || c < n) {
+    int po = o < oe ? d.A.partner[o] : 0x7fffffff;
+    int raw = c < n ? cand[c] : 0x7fffffff;
+    int pc = raw & 0x7fffffff;
+    if (po == pc) { copyEntry(d.A, o, d.B, out++, full); o++; c++; }
+    else if (po < pc) {
+      if ((d.A.flags[o] & (F_GEOM | F_PHYS)) == (F_GEOM | F_PHYS)) copyEntry(d.A, o, d.B, out++, full);
+      o++;
+    } else { initEntry(d.B, out++, i, pc, (raw & 0x80000000) != 0, full); c++; }
+  }
+}
+
+__global__ void k_copy_back(Dev d) {
+  const SceneState& S = *d.S;
+  if (!S.runCollider || S.overflowRun) return;
+  const bool full = d.prm->recordFull != 0;
+  const int Pn = S.Pnew;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < Pn; e += gridDim.x * blockDim.x) copyEntry(d.B, e, d.A, e, full);
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b <= d.N; b += gridDim.x * blockDim.x) {
+    d.rowStart[b] = d.rowStartNew[b];
+    if (b < d.N) { d.pCount[b] = 0; d.pFill[b] = 0; }
+  }
+}
+
+__global__ void k_commit(Dev d) {
+  SceneState& S = *d.S;
+  if (!S.runCollider) return;
+  if (!S.overflowRun) S.P = S.Pnew;
+  S.bbInit = 1;
+  if (S.initSort) S.numReinit++;
+  S.colliderRuns++;
+  S.err[E_COLLIDER_RUNS]++;
+  // wall-wall pairs (never real: no geometry functor for (Wall, Wall)), reported only
+  int n = 0;
+  for (int a = 0; a < d.W; a++)
+    for (int b = a + 1; b < d.W; b++) {
+      int ia = d.walls[a], ib = d.walls[b];
+      if (overlapClosed(d.bmin[ia], d.bmax[ia], d.bmin[ib], d.bmax[ib])) d.ww[n++] = make_int2(min(ia, ib), max(ia, ib));
+    }
+  S.nWW = n;
+}
+
+// incidence lists: entries in which a particle is the partner (not the row owner)
+__global__ void k_pcount(Dev d) {
+  const SceneState& S = *d.S;
+  if (!S.runCollider || S.overflowRun) return;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < S.P; e += gridDim.x * blockDim.x) {
+    int p = d.A.partner[e];
+    if (d.info[p].x == KIND_SQ) atomicAdd(&d.pCount[p], 1);
+  }
+}
+__global__ void k_pscatter(Dev d) {
+  const SceneState& S = *d.S;
+  if (!S.runCollider || S.overflowRun) return;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < S.P; e += gridDim.x * blockDim.x) {
+    int p = d.A.partner[e];
+    if (d.info[p].x == KIND_SQ) d.pList[d.pStart[p] + atomicAdd(&d.pFill[p], 1)] = e;
+  }
+}
+// make each partner list ascending in entry index (deterministic summation order)
+__global__ void k_psort(Dev d) {
+  const SceneState& S = *d.S;
+  if (!S.runCollider || S.overflowRun) return;
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= d.N) return;
+  int s = d.pStart[b], e = d.pStart[b + 1];
+  for (int a = s + 1; a < e; a++) {
+    int v = d.pList[a]; int c = a - 1;
+    while (c >= s && d.pList[c] > v) { d.pList[c + 1] = d.pList[c]; c--; }
+    d.pList[c + 1] = v;
+  }
+}
+// per-wall lists by ordered block compaction over the table (one block per wall):
+// k_wall_count writes the list lengths, k_wall_lists the lists in table order.
+__global__ void k_wall_count(Dev d) {
+  const SceneState& S = *d.S;
+  if (!S.runCollider || S.overflowRun) return;
+  __shared__ int sh[32];
+  const int wid = d.walls[blockIdx.x];
+  int cnt = 0;
+  for (int e = threadIdx.x; e < S.P; e += blockDim.x) cnt += (d.A.partner[e] == wid);
+  int total;
+  blockExclusiveScan(cnt, sh, total);
+  if (threadIdx.x == 0) d.wCount[blockIdx.x] = total;
+}
+__global__ void k_wall_lists(Dev d) {
+  const SceneState& S = *d.S;
+  if (!S.runCollider || S.overflowRun) return;
+  __shared__ int sh[32];
+  const int w = blockIdx.x;
+  const int wid = d.walls[w];
+  int base = 0;
+  for (int w2 = 0; w2 < w; w2++) base += d.wCount[w2];
+  int off = base;
+  for (int e0 = 0; e0 < S.P; e0 += blockDim.x) {
+    int e = e0 + threadIdx.x;
+    int f = (e < S.P && d.A.partner[e] == wid) ? 1 : 0;
+    int t; int ex = blockExclusiveScan(f, sh, t);
+    if (f) d.wList[off + ex] = e;
+    off += t;
+  }
+  if (threadIdx.x == 0) d.wCount[d.W + w] = base;   // start of list w
+}
+
+// ---------------------------------------------------------------------------
+// Narrowphase + contact physics + law for one table entry.
+struct BodyView {
+  D3 pos, vel, angVel; double4 ori; double4 shpA, shpB; int4 info; double mass; unsigned blocked;
+};
+__device__ __forceinline__ BodyView loadBody(const Dev& d, int b) {
+  BodyView v;
+  v.pos = xyz(d.pos[b]); v.vel = xyz(d.vel[b]); v.angVel = xyz(d.angVel[b]); v.ori = d.ori[b];
+  v.shpA = d.shpA[b]; v.shpB = d.shpB[b]; v.info = d.info[b]; v.mass = d.mass[b]; v.blocked = d.blocked[b];
+  return v;
+}
+
+struct GeomOut {
+  bool precomputed;   // contact branch taken (precompute ran, normal/contactPoint updated)
+  double depth; double ang0, ang1; bool angSet;
+  D3 normal, cp, p1, p2, shearInc, twist, ortho, relVn, relVs;
+  bool isShearNew;
+  int lmIters, lmStop, lmCalls; bool nanNormal;
+};
+
+// SuperquadricsGeom::precompute (Superquadrics.cpp:1030-1050)
+__device__ __forceinline__ void precomputeD(GeomOut& g, const D3& oldNormal, const BodyView& b1, const BodyView& b2,
+                                            double dt, D3 currentNormal, bool isNew) {
+  if (!isNew) {
+    g.ortho = cross(oldNormal, currentNormal);
+    double angle = dt * 0.5 * dot(currentNormal, b1.angVel + b2.angVel);
+    g.twist = angle * currentNormal;
+  } else { g.twist = d3(0, 0, 0); g.ortho = d3(0, 0, 0); }
+  g.normal = currentNormal;
+  D3 c1x = g.cp - b1.pos;
+  D3 c2x = (g.cp - b2.pos) - d3(0, 0, 0);
+  D3 relVel = (b2.vel + cross(b2.angVel, c2x)) - (b1.vel + cross(b1.angVel, c1x));
+  g.relVn = dot(g.normal, relVel) * g.normal;
+  g.relVs = relVel - g.relVn;
+  g.shearInc = g.relVs * dt;
+}
+
+__device__ __forceinline__ void makeShape(SqShape& s, const BodyView& b) {
+  shapeInit(s, b.shpA.x, b.shpA.y, b.shpA.z, b.shpB.x, b.shpB.y, b.shpA.w);
+  s.R = quatToRot(b.ori.x, b.ori.y, b.ori.z, b.ori.w);
+  s.pos = b.pos;
+}
+
+// Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go (Superquadrics_Ig2.cpp:1880-2317)
+__device__ void geomSqSq(GeomOut& g, bool isNew, double prevDepth, double2 prevAngle, D3 oldNormal, D3 oldCp,
+                         const BodyView& b1, const BodyView& b2, double dt) {
+  g.precomputed = false; g.angSet = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 0; g.nanNormal = false;
+  g.cp = oldCp;
+  D3 position1 = b1.pos;
+  D3 position2 = b2.pos + d3(0, 0, 0);
+  double para[2];
+  if (isNew) { g.isShearNew = true; centerLine(position1, position2, para); }
+  else { g.isShearNew = prevDepth <= 0; para[0] = prevAngle.x; para[1] = prevAngle.y; }
+  D3 contactNormal = d3(0, 0, 0), center = d3(0, 0, 0);
+  double pDepth = 0.0;
+  D3 p1 = d3(0, 0, 0), p2 = d3(0, 0, 0);
+  const bool sphA = b1.info.z != 0, sphB = b2.info.z != 0;
+  const double rmaxA = b1.shpA.w, rmaxB = b2.shpA.w;
+  if (sphA && sphB) {
+    D3 dist = position2 - position1;
+    double r_sum = rmaxA + rmaxB;
+    double depth = r_sum - nrm(dist);
+    if (depth < 1E-18) { g.depth = 0; g.isShearNew = true; return; }
+    normalize(dist);
+    p1 = position1 + rmaxA * dist;
+    p2 = position2 - rmaxB * dist;
+    contactNormal = p1 - p2;
+    normalize(contactNormal);
+    g.p1 = p1; g.p2 = p2;
+    g.cp = 0.5 * (p1 + p2);
+    g.depth = depth;
+  } else {
+    double r_sum = rmaxA + rmaxB;
+    if (nrm(position1 - position2) > r_sum) { g.depth = 0; g.isShearNew = true; return; }
+    SqShape A, B;
+    makeShape(A, b1); makeShape(B, b2);
+    bool touching = true;
+    LMOut info = lmder2(A, B, para, 50, p1, p2, center, touching, contactNormal);
+    g.lmCalls++; g.lmIters += info.iters; if (info.stop == 3) g.lmStop = 3;
+    if (isnan(para[0]) || isnan(para[1]) || 7 == info.stop) {
+      if (touching) {
+        centerLine(position1, position2, para);
+        info = lmder2(A, B, para, 50, p1, p2, center, touching, contactNormal);
+        g.lmCalls++; g.lmIters += info.iters; if (info.stop == 3) g.lmStop = 3;
+      }
+    }
+    pDepth = dot(p1 - p2, contactNormal);
+    if (touching) {
+      if (10.0 * nrm(p2 - p1) > rmaxA) {
+        if (!isInside(A, p2 - position1) || !isInside(B, p1 - position2)) {
+          centerLine(position1, position2, para);
+          info = lmder2(A, B, para, 50, p1, p2, center, touching, contactNormal);
+          g.lmCalls++; g.lmIters += info.iters; if (info.stop == 3) g.lmStop = 3;
+          pDepth = dot(p1 - p2, contactNormal);
+        }
+      }
+    }
+    if (!touching) {
+      g.ang0 = para[0]; g.ang1 = para[1]; g.angSet = true;
+      g.depth = 0; g.isShearNew = true;
+      return;
+    }
+    g.p1 = p1; g.p2 = p2;
+    if (isnan(contactNormal.x)) g.nanNormal = true;
+    g.cp = center;
+    g.depth = pDepth;
+    normalize(contactNormal);
+  }
+  g.precomputed = true;
+  precomputeD(g, oldNormal, b1, b2, dt, contactNormal, g.isShearNew);
+  g.normal = contactNormal;
+  g.ang0 = para[0]; g.ang1 = para[1]; g.angSet = true;
+}
+
+// Ig2_Wall_Superquadrics_SuperquadricsGeom::go (Superquadrics_Ig2.cpp:2522-2611)
+__device__ void geomWallSq(GeomOut& g, bool isNew, double prevDepth, D3 oldNormal, D3 oldCp, const BodyView& w,
+                           const BodyView& b, double dt) {
+  g.precomputed = false; g.angSet = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 0; g.nanNormal = false;
+  g.cp = oldCp;
+  const int PA = w.info.w & 15;
+  const double sense = (double)((w.info.w >> 4) - 1);
+  g.isShearNew = isNew ? true : (prevDepth <= 0);
+  D3 normal = d3(0, 0, 0);
+  if (PA == 0) normal.x = sense; else if (PA == 1) normal.y = sense; else normal.z = sense;
+  const double wallc = PA == 0 ? w.pos.x : (PA == 1 ? w.pos.y : w.pos.z);
+  if (b.info.z != 0) {
+    D3 p1 = b.pos;
+    if (PA == 0) p1.x = wallc; else if (PA == 1) p1.y = wallc; else p1.z = wallc;
+    D3 point2 = b.pos - normal * b.shpA.w;
+    double depth = b.shpA.w - nrm(b.pos - p1);
+    if (depth < 0.0) { g.depth = 0; g.isShearNew = true; return; }
+    g.p1 = p1; g.p2 = point2;
+    g.cp = 0.5 * (point2 + p1);
+    g.depth = depth;
+  } else {
+    SqShape B;
+    makeShape(B, b);
+    double ph0, ph1;
+    normal2phi(B, -mulL(B.R, normal), ph0, ph1);
+    D3 point2 = mulG(B.R, surface(B, ph0, ph1)) + b.pos;
+    D3 p1 = point2;
+    if (PA == 0) p1.x = wallc; else if (PA == 1) p1.y = wallc; else p1.z = wallc;
+    D3 dd = point2 - p1;
+    double nd = PA == 0 ? normal.x * dd.x : (PA == 1 ? normal.y * dd.y : normal.z * dd.z);
+    if (nd >= 0.0) { g.depth = 0; g.isShearNew = true; return; }
+    g.p1 = p1; g.p2 = point2;
+    g.cp = 0.5 * (point2 + p1);
+    g.depth = nrm(dd);
+  }
+  g.precomputed = true;
+  precomputeD(g, oldNormal, w, b, dt, normal, g.isShearNew);
+  g.normal = normal;
+}
+
+// SuperquadricsGeom::rotate (Superquadrics.cpp:1053-1080)
+__device__ __forceinline__ D3 rotateShear(const GeomOut& g, D3 sf) {
+  sf = sf - cross(sf, g.ortho);
+  sf = sf - cross(sf, g.twist);
+  sf = sf - dot(g.normal, sf) * g.normal;
+  return sf;
+}
+
+__global__ void __launch_bounds__(128) k_contacts(Dev d) {
+  const SceneState& S = *d.S;
+  const Params& P = *d.prm;
+  const int Pn = S.P;
+  const bool full = P.recordFull != 0;
+  const double dt = P.dt;
+  unsigned long long lmCalls = 0, lmIters = 0, lmMax = 0, nanN = 0, nanF = 0;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < Pn; e += gridDim.x * blockDim.x) {
+    unsigned fl = d.A.flags[e];
+    const int owner = d.A.owner[e];
+    const int partner = d.A.partner[e];
+    const int id1 = (fl & F_OWNER_ID1) ? owner : partner;
+    const int id2 = (fl & F_OWNER_ID1) ? partner : owner;
+    // SuperquadricsLaw's bound-separation erase (Superquadrics.cpp:1194-1207): it discards
+    // whatever the geometry functor computed, so it is tested first.
+    const double4 amn = d.bmin[id1], amx = d.bmax[id1], bmn = d.bmin[id2], bmx = d.bmax[id2];
+    if (amn.x >= bmx.x || bmn.x >= amx.x || amn.y >= bmx.y || bmn.y >= amx.y || amn.z >= bmx.z || bmn.z >= amx.z) {
+      d.A.flags[e] = (fl & ~(F_GEOM | F_PHYS | F_FORCE)) | F_SHEARNEW;
+      d.A.nforce[e] = make_double4(0, 0, 0, 0);
+      d.A.shear[e] = make_double4(0, 0, 0, 0);
+      continue;
+    }
+    const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
+    const bool isNew = !(fl & F_GEOM);
+    double prevDepth = isNew ? 0.0 : d.A.depth[e];
+    double2 prevAngle = isNew ? make_double2(0, 0) : d.A.angle[e];
+    D3 oldNormal = isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
+    D3 oldCp = isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
+    GeomOut g;
+    if (b1.info.x == KIND_WALL) geomWallSq(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt);
+    else geomSqSq(g, isNew, prevDepth, prevAngle, oldNormal, oldCp, b1, b2, dt);
+    lmCalls += g.lmCalls; lmIters += g.lmIters; lmMax += (g.lmStop == 3); nanN += g.nanNormal;
+    fl |= F_GEOM;
+    fl = g.isShearNew ? (fl | F_SHEARNEW) : (fl & ~F_SHEARNEW);
+    // geometry history
+    d.A.depth[e] = g.depth;
+    if (g.angSet) d.A.angle[e] = make_double2(g.ang0, g.ang1);
+    else if (isNew) d.A.angle[e] = make_double2(0, 0);
+    if (g.precomputed) { d.A.normal[e] = dd4(g.normal, 0); d.A.cp[e] = dd4(g.cp, 0); }
+    else if (isNew) { d.A.normal[e] = make_double4(0, 0, 0, 0); d.A.cp[e] = make_double4(0, 0, 0, 0); }
+    if (full && g.precomputed) {
+      d.A.p1[e] = dd4(g.p1, 0); d.A.p2[e] = dd4(g.p2, 0); d.A.shearInc[e] = dd4(g.shearInc, 0);
+      d.A.twist[e] = dd4(g.twist, 0); d.A.ortho[e] = dd4(g.ortho, 0);
+      d.A.relVn[e] = dd4(g.relVn, 0); d.A.relVs[e] = dd4(g.relVs, 0);
+    } else if (full && isNew) {
+      const double4 z = make_double4(0, 0, 0, 0);
+      d.A.p1[e] = z; d.A.p2[e] = z; d.A.shearInc[e] = z; d.A.twist[e] = z; d.A.ortho[e] = z; d.A.relVn[e] = z; d.A.relVs[e] = z;
+    }
+    // Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys::go (Superquadrics.cpp:1086-1116)
+    double4 ph;
+    double2 beta;
+    if (!(fl & F_PHYS)) {
+      const double4 m1 = d.mats[b1.info.y], m2 = d.mats[b2.info.y];
+      const double2 mb1 = d.matsB[b1.info.y], mb2 = d.matsB[b2.info.y];
+      if (id1 > 5) {
+        double fa = fmin_ref(m1.z, m2.z);
+        ph.z = tan(fa);
+        ph.x = 2.0 * m1.x * m2.x / (m1.x + m2.x);
+        ph.y = 2.0 * m1.y * m2.y / (m1.y + m2.y);
+      } else {
+        ph.z = tan(m1.z); ph.x = m1.x; ph.y = m1.y;
+      }
+      beta.x = fmax_ref(mb1.x, mb2.x); beta.y = fmax_ref(mb1.y, mb2.y);
+      ph.w = 0;
+      d.A.phys[e] = ph;
+      fl |= F_PHYS;
+    } else {
+      ph = d.A.phys[e];
+      const double2 mb1 = d.matsB[b1.info.y], mb2 = d.matsB[b2.info.y];
+      beta.x = fmax_ref(mb1.x, mb2.x); beta.y = fmax_ref(mb1.y, mb2.y);
+    }
+    // SuperquadricsLaw::go (Superquadrics.cpp:1209-1361)
+    if (!(g.depth > 1E-18)) {
+      d.A.nforce[e] = make_double4(0, 0, 0, 0);
+      d.A.shear[e] = make_double4(0, 0, 0, 0);
+      fl &= ~F_FORCE;
+    } else {
+      D3 normalForce = g.normal * g.depth * ph.x;
+      const bool useDamping = (beta.x > 1e-5 || beta.y > 1e-5);
+      double cs = 0;
+      D3 shearViscous = d3(0, 0, 0);
+      if (useDamping) {
+        const bool Adyn = b1.blocked != DOF_ALL, Bdyn = b2.blocked != DOF_ALL;
+        double mbar = (!Adyn && Bdyn) ? b2.mass : ((!Bdyn && Adyn) ? b1.mass : (b1.mass * b2.mass / (b1.mass + b2.mass)));
+        double Cn_crit = 2. * sqrt(mbar * ph.x);
+        double Cs_crit = 2. * sqrt(mbar * ph.y);
+        double cn = Cn_crit * beta.x;
+        cs = Cs_crit * beta.y;
+        D3 normalViscous = cn * g.relVn;
+        D3 normTemp = normalForce - normalViscous;
+        if (dot(normTemp, g.normal) < 0.0) normalForce = d3(0, 0, 0);
+        else normalForce = normalForce - normalViscous;
+      }
+      D3 shearForce1;
+      if (g.isShearNew) shearForce1 = d3(0, 0, 0);
+      else shearForce1 = rotateShear(g, xyz(d.A.shear[e]));
+      shearForce1 = shearForce1 - ph.y * g.shearInc;
+      double maxFs = sqn(normalForce) * (ph.z * ph.z);
+      if (sqn(shearForce1) > maxFs) {
+        double ratio = sqrt(maxFs) / nrm(shearForce1);
+        shearForce1 = shearForce1 * ratio;
+      } else if (useDamping) {
+        shearViscous = cs * g.relVs;
+      }
+      if (isnan(shearForce1.x) || isnan(normalForce.x)) { normalForce = d3(0, 0, 0); shearForce1 = d3(0, 0, 0); nanF++; }
+      D3 Fv = ((-normalForce) - shearForce1) + shearViscous;
+      d.A.F[e] = dd4(Fv, 0);
+      d.A.nforce[e] = dd4(normalForce, 0);
+      d.A.shear[e] = dd4(shearForce1, 0);
+      fl |= F_FORCE;
+    }
+    d.A.flags[e] = fl;
+  }
+  // per-warp reduction of the counters
+  for (int o = 16; o > 0; o >>= 1) {
+    lmCalls += __shfl_down_sync(0xffffffffu, lmCalls, o); lmIters += __shfl_down_sync(0xffffffffu, lmIters, o);
+    lmMax += __shfl_down_sync(0xffffffffu, lmMax, o); nanN += __shfl_down_sync(0xffffffffu, nanN, o);
+    nanF += __shfl_down_sync(0xffffffffu, nanF, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (lmCalls) atomicAdd(&d.S->err[E_LM_CALLS], lmCalls);
+    if (lmIters) atomicAdd(&d.S->err[E_LM_ITERS], lmIters);
+    if (lmMax) atomicAdd(&d.S->err[E_LM_MAX], lmMax);
+    if (nanN) atomicAdd(&d.S->err[E_NAN_NORMAL], nanN);
+    if (nanF) atomicAdd(&d.S->err[E_NAN_FORCE], nanF);
+  }
+}
+
+// contribution of table entry e to body b (b is id1 when asId1)
+__device__ __forceinline__ void addContribution(const Dev& d, int e, bool asId1, D3 pos, D3& f, D3& t) {
+  const D3 F = xyz(d.A.F[e]);
+  const D3 cp = xyz(d.A.cp[e]);
+  if (asId1) { f = f + F; t = t + (-cross(pos - cp, F)); }
+  else { f = f + (-F); t = t + cross(pos - cp, F); }
+}
+
+// ForceContainer sum for walls: one block per wall, fixed-order reduction.
+__global__ void k_wall_forces(Dev d) {
+  const SceneState& S = *d.S;
+  __shared__ double sh[6][128];
+  const int w = blockIdx.x;
+  const int wid = d.walls[w];
+  const D3 pos = xyz(d.pos[wid]);
+  const int s = d.wCount[d.W + w], n = d.wCount[w];
+  D3 f = d3(0, 0, 0), t = d3(0, 0, 0);
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    int e = d.wList[s + k];
+    if (!(d.A.flags[e] & F_FORCE)) continue;
+    addContribution(d, e, !(d.A.flags[e] & F_OWNER_ID1), pos, f, t);
+  }
+  (void)S;
+  sh[0][threadIdx.x] = f.x; sh[1][threadIdx.x] = f.y; sh[2][threadIdx.x] = f.z;
+  sh[3][threadIdx.x] = t.x; sh[4][threadIdx.x] = t.y; sh[5][threadIdx.x] = t.z;
+  __syncthreads();
+  for (int o = 64; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+      for (int c = 0; c < 6; c++) sh[c][threadIdx.x] = sh[c][threadIdx.x] + sh[c][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    d.force[wid] = make_double4(sh[0][0], sh[1][0], sh[2][0], 0);
+    d.torque[wid] = make_double4(sh[3][0], sh[4][0], sh[5][0], 0);
+  }
+}
+
+// NewtonIntegrator (NewtonIntegrator.cpp): DotQ (:470-477)
+struct Q4 { double w, x, y, z; };
+__device__ __forceinline__ Q4 DotQ(D3 a, Q4 Q) {
+  Q4 r;
+  r.w = (-Q.x * a.x - Q.y * a.y - Q.z * a.z) / 2;
+  r.x = (Q.w * a.x - Q.z * a.y + Q.y * a.z) / 2;
+  r.y = (Q.z * a.x + Q.w * a.y - Q.x * a.z) / 2;
+  r.z = (-Q.y * a.x + Q.x * a.y + Q.w * a.z) / 2;
+  return r;
+}
+__device__ __forceinline__ void qnormalize(Q4& q) {
+  double z = (q.x * q.x + q.y * q.y) + (q.z * q.z + q.w * q.w);
+  if (z > 0) { double n = sqrt(z); q.x /= n; q.y /= n; q.z /= n; q.w /= n; }
+}
+__device__ __forceinline__ D3 qrotate(Q4 q, D3 v) {
+  D3 qv = d3(q.x, q.y, q.z);
+  D3 uv = cross(qv, v);
+  uv = uv + uv;
+  D3 c = cross(qv, uv);
+  return d3((v.x + q.w * uv.x) + c.x, (v.y + q.w * uv.y) + c.y, (v.z + q.w * uv.z) + c.z);
+}
+// leapfrogSphericalRotate without move/rot buffers (:319-335)
+__device__ __forceinline__ void sphericalRotate(Q4& o, D3 w, double dt) {
+  double angle2 = sqn(w);
+  if (angle2 != 0) {
+    double angle = sqrt(angle2);
+    D3 axis = d3(w.x / angle, w.y / angle, w.z / angle);
+    double h = 0.5 * (angle * dt);
+    double sh, ch; sincos(h, &sh, &ch);
+    Q4 q; q.w = ch; q.x = sh * axis.x; q.y = sh * axis.y; q.z = sh * axis.z;
+    Q4 r;
+    r.w = q.w * o.w - q.x * o.x - q.y * o.y - q.z * o.z;
+    r.x = q.w * o.x + q.x * o.w + q.y * o.z - q.z * o.y;
+    r.y = q.w * o.y + q.y * o.w + q.z * o.x - q.x * o.z;
+    r.z = q.w * o.z + q.z * o.w + q.x * o.y - q.y * o.x;
+    o = r;
+  }
+  qnormalize(o);
+}
+
+__global__ void __launch_bounds__(256) k_integrate(Dev d) {
+  const SceneState& S = *d.S;
+  const Params& P = *d.prm;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  int code = 0;
+  if (b < d.N) {
+    const int4 inf = d.info[b];
+    const double dt = P.dt;
+    D3 pos = xyz(d.pos[b]);
+    double4 o4 = d.ori[b];
+    Q4 ori; ori.w = o4.x; ori.x = o4.y; ori.y = o4.z; ori.z = o4.w;
+    D3 vel = xyz(d.vel[b]), angVel = xyz(d.angVel[b]), angMom = xyz(d.angMom[b]);
+    const unsigned blocked = d.blocked[b];
+    const bool damped = d.damped[b] != 0;
+    const bool aspherical = d.aspherical[b] != 0;
+    D3 f = d3(0, 0, 0), m = d3(0, 0, 0);
+    if (inf.x == KIND_SQ) {
+      for (int e = d.rowStart[b]; e < d.rowStart[b + 1]; e++) {
+        unsigned fl = d.A.flags[e];
+        if (fl & F_FORCE) addContribution(d, e, (fl & F_OWNER_ID1) != 0, pos, f, m);
+      }
+      for (int k = d.pStart[b]; k < d.pStart[b + 1]; k++) {
+        int e = d.pList[k];
+        unsigned fl = d.A.flags[e];
+        if (fl & F_FORCE) addContribution(d, e, (fl & F_OWNER_ID1) == 0, pos, f, m);
+      }
+      d.force[b] = dd4(f, 0); d.torque[b] = dd4(m, 0);
+    } else {
+      f = xyz(d.force[b]); m = xyz(d.torque[b]);
+    }
+    const double mass = d.mass[b];
+    const double4 I4 = d.inertia[b];
+    const D3 inertia = xyz(I4);
+    const bool useAspherical = (P.exactAsphericalRot && aspherical && blocked != DOF_ALL);
+    const bool isSphere = (inf.x == KIND_SQ) && inf.z != 0;
+    const double damping = P.damping;
+    if (blocked != DOF_ALL) {
+      D3 a;
+      if (blocked == 0) a = d3(f.x / mass + P.g[0], f.y / mass + P.g[1], f.z / mass + P.g[2]);
+      else {
+        a = d3(0, 0, 0);
+        if (!(blocked & 1u)) a.x += f.x / mass + P.g[0];
+        if (!(blocked & 2u)) a.y += f.y / mass + P.g[1];
+        if (!(blocked & 4u)) a.z += f.z / mass + P.g[2];
+      }
+      if (damped) {
+        a.x *= 1 - damping * sgn(a.x * (vel.x + 0.5 * dt * a.x));
+        a.y *= 1 - damping * sgn(a.y * (vel.y + 0.5 * dt * a.y));
+        a.z *= 1 - damping * sgn(a.z * (vel.z + 0.5 * dt * a.z));
+      }
+      vel = vel + dt * a;
+      if (!useAspherical || (P.isSuperquadrics && isSphere && damped)) {
+        D3 aa;
+        if (blocked == 0) aa = d3(m.x / inertia.x, m.y / inertia.y, m.z / inertia.z);
+        else {
+          aa = d3(0, 0, 0);
+          if (!(blocked & 8u)) aa.x += m.x / inertia.x;
+          if (!(blocked & 16u)) aa.y += m.y / inertia.y;
+          if (!(blocked & 32u)) aa.z += m.z / inertia.z;
+        }
+        if (damped) {
+          aa.x *= 1 - damping * sgn(aa.x * (angVel.x + 0.5 * dt * aa.x));
+          aa.y *= 1 - damping * sgn(aa.y * (angVel.y + 0.5 * dt * aa.y));
+          aa.z *= 1 - damping * sgn(aa.z * (angVel.z + 0.5 * dt * aa.z));
+        }
+        angVel = angVel + dt * aa;
+      } else {
+        if (blocked & 8u) m.x = 0;
+        if (blocked & 16u) m.y = 0;
+        if (blocked & 32u) m.z = 0;
+        if (damped) {  // cundallDamp1st on the torque (:19-21)
+          m.x *= 1 - damping * sgn(m.x * angVel.x);
+          m.y *= 1 - damping * sgn(m.y * angVel.y);
+          m.z *= 1 - damping * sgn(m.z * angVel.z);
+        }
+      }
+    }
+    if (!useAspherical || (P.isSuperquadrics && isSphere)) {
+      sphericalRotate(ori, angVel, dt);
+    } else if (P.isSuperquadrics) {
+      // leapfrogAsphericalRotate with A = rot_mat2local (:337-360, :391-429)
+      const Rot R = quatToRot(ori.w, ori.x, ori.y, ori.z);
+      const D3 l_n = angMom + dt / 2. * m;
+      const D3 l_b_n = mulL(R, l_n);
+      const D3 w_b_n = d3(l_b_n.x / inertia.x, l_b_n.y / inertia.y, l_b_n.z / inertia.z);
+      const Q4 dq = DotQ(w_b_n, ori);
+      const double hdt = dt / 2.;
+      Q4 Qh; Qh.w = ori.w + dq.w * hdt; Qh.x = ori.x + dq.x * hdt; Qh.y = ori.y + dq.y * hdt; Qh.z = ori.z + dq.z * hdt;
+      angMom = angMom + dt * m;
+      const D3 l_b_h = mulL(R, angMom);
+      const D3 w_b_h = d3(l_b_h.x / inertia.x, l_b_h.y / inertia.y, l_b_h.z / inertia.z);
+      const Q4 dqh = DotQ(w_b_h, Qh);
+      ori.w = ori.w + dqh.w * dt; ori.x = ori.x + dqh.x * dt; ori.y = ori.y + dqh.y * dt; ori.z = ori.z + dqh.z * dt;
+      angVel = qrotate(ori, w_b_h);
+      qnormalize(ori);
+    }
+    pos = pos + vel * dt;
+    d.pos[b] = dd4(pos, 0);
+    d.ori[b] = make_double4(ori.w, ori.x, ori.y, ori.z);
+    d.vel[b] = dd4(vel, 0); d.angVel[b] = dd4(angVel, 0); d.angMom[b] = dd4(angMom, 0);
+    // saveMaximaDisplacement (:72-85)
+    const double4 rf = d.ref[b];
+    if (rf.w != 0) {
+      D3 disp = pos - xyz(rf);
+      double maxDisp = fmax_ref(fabs(disp.x), fmax_ref(fabs(disp.y), fabs(disp.z)));
+      double sl = d.bmin[b].w;
+      code = (maxDisp == 0 || maxDisp < sl) ? 1 : 2;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) code = max(code, __shfl_down_sync(0xffffffffu, code, o));
+  if ((threadIdx.x & 31) == 0 && code) atomicMax(&d.S->maxDispCode, code);
+  if (b == 0) d.S->newtonRan = 1;
+  (void)S;
+}
+
+__global__ void k_end(Dev d) {
+  SceneState& S = *d.S;
+  S.iter++;
+  S.time += d.prm->dt;
+  S.err[E_STEPS]++;
+}
+
+}  // namespace sqdem
+
+// ===========================================================================
+// Host side: context, allocation, step sequence, C ABI.
+using namespace sqdem;
+
+struct sqdem_ctx {
+  int device = 0, precision = SQDEM_FP64, useGraph = 1, contactsPerBody = 16, maxCand = 64;
+  int numSMs = 152;
+  cudaStream_t stream = nullptr;
+  Dev d;
+  bool haveBodies = false, haveMats = false, haveParams = false;
+  cudaGraph_t graph = nullptr; cudaGraphExec_t exec = nullptr; bool graphValid = false;
+  std::string err;
+  std::vector<void*> allocs;
+  sqdem_params params;
+  int recordFull = 0;
+  std::vector<int> kind, wallIds, matIds, isSphere, axisSense;
+  std::vector<double> shape5;
+  int nMats = 0;
+  std::vector<double4> hostMats; std::vector<double2> hostMatsB;
+  long long launches = 0, launchesPerStep = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  float stageMs[3] = {0, 0, 0};
+};
+
+static sqdem_status fail(sqdem_ctx* c, sqdem_status s, const std::string& m) {
+  if (c) c->err = m;
+  return s;
+}
+#define CK(call)                                                                                     \
+  do {                                                                                               \
+    cudaError_t e_ = (call);                                                                         \
+    if (e_ != cudaSuccess) return fail(c, SQDEM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+static cudaError_t dalloc(sqdem_ctx* c, T** p, size_t n) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, sizeof(T) * (n ? n : 1));
+  if (e == cudaSuccess) { c->allocs.push_back(q); cudaMemsetAsync(q, 0, sizeof(T) * (n ? n : 1), c->stream); }
+  *p = (T*)q;
+  return e;
+}
+static void freeAll(sqdem_ctx* c) {
+  if (c->exec) { cudaGraphExecDestroy(c->exec); c->exec = nullptr; }
+  if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+  c->graphValid = false;
+  for (void* p : c->allocs) cudaFree(p);
+  c->allocs.clear();
+}
+static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+static sqdem_status allocTable(sqdem_ctx* c, Table& t, int cap) {
+  CK(dalloc(c, &t.owner, cap)); CK(dalloc(c, &t.partner, cap)); CK(dalloc(c, &t.flags, cap));
+  CK(dalloc(c, &t.angle, cap)); CK(dalloc(c, &t.depth, cap)); CK(dalloc(c, &t.normal, cap));
+  CK(dalloc(c, &t.shear, cap)); CK(dalloc(c, &t.nforce, cap)); CK(dalloc(c, &t.phys, cap));
+  CK(dalloc(c, &t.F, cap)); CK(dalloc(c, &t.cp, cap));
+  CK(dalloc(c, &t.p1, cap)); CK(dalloc(c, &t.p2, cap)); CK(dalloc(c, &t.shearInc, cap));
+  CK(dalloc(c, &t.twist, cap)); CK(dalloc(c, &t.ortho, cap)); CK(dalloc(c, &t.relVn, cap)); CK(dalloc(c, &t.relVs, cap));
+  return SQDEM_OK;
+}
+
+static int* gateRun(sqdem_ctx* c) { return (int*)((char*)c->d.S + offsetof(SceneState, runCollider)); }
+
+static void launchScan(sqdem_ctx* c, const int* in, int n, int* out, const int* gate) {
+  int nb = nblk(n + 1, SCAN_TILE);
+  k_scan_reduce<<<nb, SCAN_BS, 0, c->stream>>>(in, n, c->d.scanTmp, gate);
+  k_scan_blocks<<<1, SCAN_BS, 0, c->stream>>>(c->d.scanTmp, nb, gate);
+  k_scan_apply<<<nb, SCAN_BS, 0, c->stream>>>(in, n, c->d.scanTmp, out, gate);
+  c->launches += 3;
+}
+
+// One timestep of kernels on c->stream.
+static void enqueueStep(sqdem_ctx* c, bool timed) {
+  Dev& d = c->d;
+  cudaStream_t s = c->stream;
+  const int* gate = gateRun(c);
+  const int N = d.N;
+  if (timed) cudaEventRecord(c->ev[0], s);
+  k_gate<<<1, 1, 0, s>>>(d);
+  k_bounds<<<nblk(N, 256), 256, 0, s>>>(d);
+  k_grid_setup<<<1, 1, 0, s>>>(d);
+  k_zero_cells<<<std::min(nblk(d.Gmax + 1, 256), 4096), 256, 0, s>>>(d);
+  k_cell_count<<<nblk(N, 256), 256, 0, s>>>(d);
+  c->launches += 5;
+  launchScan(c, d.cellCount, d.Gmax, d.cellStart, gate);
+  k_cell_scatter<<<nblk(N, 256), 256, 0, s>>>(d);
+  k_candidates<<<nblk(N, 128), 128, 0, s>>>(d);
+  c->launches += 2;
+  launchScan(c, d.rowCount, N, d.rowStartNew, gate);
+  const int tblBlocks = std::min(nblk(d.Pcap, 256), c->numSMs * 8);
+  k_check_capacity<<<1, 1, 0, s>>>(d);
+  k_merge<<<nblk(N, 128), 128, 0, s>>>(d);
+  k_copy_back<<<tblBlocks, 256, 0, s>>>(d);
+  k_commit<<<1, 1, 0, s>>>(d);
+  k_pcount<<<tblBlocks, 256, 0, s>>>(d);
+  c->launches += 5;
+  launchScan(c, d.pCount, N, d.pStart, gate);
+  k_pscatter<<<tblBlocks, 256, 0, s>>>(d);
+  k_psort<<<nblk(N, 256), 256, 0, s>>>(d);
+  c->launches += 2;
+  if (d.W > 0) {
+    k_wall_count<<<d.W, 256, 0, s>>>(d);
+    k_wall_lists<<<d.W, 256, 0, s>>>(d);
+    c->launches += 2;
+  }
+  if (timed) cudaEventRecord(c->ev[1], s);
+  k_contacts<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, s>>>(d);
+  c->launches += 1;
+  if (timed) cudaEventRecord(c->ev[2], s);
+  if (d.W > 0) { k_wall_forces<<<d.W, 128, 0, s>>>(d); c->launches++; }
+  k_integrate<<<nblk(N, 256), 256, 0, s>>>(d);
+  k_end<<<1, 1, 0, s>>>(d);
+  c->launches += 2;
+  if (timed) cudaEventRecord(c->ev[3], s);
+}
+
+static sqdem_status ensureGraph(sqdem_ctx* c) {
+  if (c->graphValid) return SQDEM_OK;
+  if (c->exec) { cudaGraphExecDestroy(c->exec); c->exec = nullptr; }
+  if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+  long long l0 = c->launches;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  enqueueStep(c, false);
+  CK(cudaStreamEndCapture(c->stream, &c->graph));
+  c->launchesPerStep = c->launches - l0;
+  c->launches = l0;
+  CK(cudaGraphInstantiate(&c->exec, c->graph, 0));
+  c->graphValid = true;
+  return SQDEM_OK;
+}
+
+static double hostH0(sqdem_ctx* c) {
+  double rm = 0;
+  for (size_t i = 0; i < c->kind.size(); i++)
+    if (c->kind[i] == SQDEM_SUPERQUADRIC) {
+      const double* s = &c->shape5[5 * i];
+      double r = std::max(s[0], std::max(s[1], s[2]));
+      if (s[3] < 1.0 || s[4] < 1.0) r *= std::pow(2.0, 0.5);
+      rm = std::max(rm, r);
+    }
+  double vd = std::max(c->params.verletDist, 0.0);
+  double h = 2.0 * (rm + vd);
+  return h * (1.0 + 1e-9) + 1e-300;
+}
+
+static sqdem_status uploadParams(sqdem_ctx* c) {
+  Params P;
+  std::memset(&P, 0, sizeof(P));
+  P.dt = c->params.dt;
+  for (int k = 0; k < 3; k++) P.g[k] = c->params.gravity[k];
+  P.damping = c->params.damping; P.verletDist = c->params.verletDist;
+  P.minSweepDistFactor = c->params.minSweepDistFactor; P.targetInterv = c->params.targetInterv;
+  P.sortAxis = c->params.sortAxis; P.isSuperquadrics = c->params.isSuperquadrics;
+  P.exactAsphericalRot = c->params.exactAsphericalRot; P.recordFull = c->recordFull;
+  P.h0 = hostH0(c);
+  CK(cudaMemcpyAsync(c->d.prm, &P, sizeof(P), cudaMemcpyHostToDevice, c->stream));
+  return SQDEM_OK;
+}
+
+// Superquadrics::Initial (Superquadrics.cpp:47-93) with the Lanczos log-gamma of
+// lib/base/Math.hpp:192-212 (Numerical Recipes 3rd ed. coefficients, as the reference).
+static double gammlnH(const double xx) {
+  static const double cof[14] = {57.1562356658629235, -59.5979603554754912, 14.1360979747417471,
+                                 -0.491913816097620199, .339946499848118887e-4, .465236289270485756e-4,
+                                 -.983744753048795646e-4, .158088703224912494e-3, -.210264441724104883e-3,
+                                 .217439618115212643e-3, -.164318106536763890e-3, .844182239838527433e-4,
+                                 -.261908384015814087e-4, .368991826595316234e-5};
+  double x, tmp, y, ser;
+  y = x = xx;
+  tmp = x + 5.24218750000000000;
+  tmp = (x + 0.5) * std::log(tmp) - tmp;
+  ser = 0.999999999999997092;
+  for (int j = 0; j < 14; j++) ser += cof[j] / ++y;
+  return tmp + std::log(2.5066282746310005 * ser / x);
+}
+static double betaH(double z, double w) { return std::exp(gammlnH(z) + gammlnH(w) - gammlnH(z + w)); }
+
+static bool finiteRows(const double* a, int n, int stride, int cols) {
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < cols; k++)
+      if (!std::isfinite(a[(size_t)i * stride + k])) return false;
+  return true;
+}
+
+extern "C" {
+
+sqdem_status sqdem_shape_props(double rx, double ry, double rz, double e1, double e2, double* out5) {
+  if (!out5 || !(rx > 0) || !(ry > 0) || !(rz > 0) || !(e1 > 0) || !(e2 > 0)) return SQDEM_ERR_ARG;
+  double r_max = (rx > ry) ? rx : ry;
+  r_max = r_max > rz ? r_max : rz;
+  if ((e1 < 1.0) || (e2 < 1.0)) r_max *= std::pow(2.0, 0.5);
+  double a = rx * ry * rz * e1 * e2;
+  double beta1 = betaH(1.5 * e1, 0.5 * e1) * betaH(0.5 * e2, 2. * e2 + 1);
+  double beta2 = betaH(0.5 * e1, 0.5 * e1 + 1) * betaH(1.5 * e2, e2 + 1);
+  out5[0] = 2. * a * betaH(e1 * 0.5, e1 * 0.5) * betaH(e2 * 0.5 + 1, e2);
+  out5[1] = 0.5 * a * (std::pow(ry, 2.) * beta1 + 4. * std::pow(rz, 2.) * beta2);
+  out5[2] = 0.5 * a * (std::pow(rx, 2.) * beta1 + 4. * std::pow(rz, 2.) * beta2);
+  out5[3] = 0.5 * a * (std::pow(rx, 2.) + std::pow(ry, 2.)) * beta1;
+  out5[4] = r_max;
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_create(sqdem_ctx** out, const sqdem_config* cfg) {
+  if (!out) return SQDEM_ERR_ARG;
+  sqdem_ctx* c = new sqdem_ctx();
+  *out = c;
+  if (cfg) {
+    c->device = cfg->device; c->precision = cfg->precision; c->useGraph = cfg->use_graph;
+    if (cfg->contacts_per_body > 0) c->contactsPerBody = cfg->contacts_per_body;
+  }
+  if (c->precision != SQDEM_FP64 && c->precision != SQDEM_MIXED) return fail(c, SQDEM_ERR_ARG, "unknown precision");
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CK(cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, c->device));
+  for (int i = 0; i < 4; i++) CK(cudaEventCreate(&c->ev[i]));
+  std::memset(&c->d, 0, sizeof(Dev));
+  std::memset(&c->params, 0, sizeof(c->params));
+  c->params.dt = 1e-5; c->params.damping = 0.2; c->params.verletDist = -0.5; c->params.targetInterv = 50;
+  c->params.minSweepDistFactor = 0.1; c->params.sortAxis = 0; c->params.isSuperquadrics = 1;
+  c->params.exactAsphericalRot = 1;
+  return SQDEM_OK;
+}
+
+void sqdem_destroy(sqdem_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  freeAll(c);
+  for (int i = 0; i < 4; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* sqdem_last_error(sqdem_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+sqdem_status sqdem_set_materials(sqdem_ctx* c, int n, const double* Kn, const double* Ks, const double* fa,
+                                 const double* bn, const double* bs, const double* rho) {
+  if (!c || n <= 0 || !Kn || !Ks || !fa || !bn || !bs || !rho) return fail(c, SQDEM_ERR_ARG, "bad materials");
+  if (c->haveMats && n != c->nMats) return fail(c, SQDEM_ERR_ARG, "material count cannot change");
+  CK(cudaSetDevice(c->device));
+  std::vector<double4>& m = c->hostMats; std::vector<double2>& mb = c->hostMatsB;
+  m.resize(n); mb.resize(n);
+  for (int i = 0; i < n; i++) { m[i] = make_double4(Kn[i], Ks[i], fa[i], rho[i]); mb[i] = make_double2(bn[i], bs[i]); }
+  c->nMats = n; c->haveMats = true;
+  if (c->haveBodies) {
+    CK(cudaMemcpyAsync(c->d.mats, m.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d.matsB, mb.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_set_params(sqdem_ctx* c, const sqdem_params* p) {
+  if (!c || !p) return fail(c, SQDEM_ERR_ARG, "null params");
+  if (!(p->dt > 0)) return fail(c, SQDEM_ERR_ARG, "dt must be positive");
+  if (p->sortAxis < 0 || p->sortAxis > 2) return fail(c, SQDEM_ERR_ARG, "sortAxis must be 0, 1 or 2");
+  if (p->isSuperquadrics != 1)
+    return fail(c, SQDEM_ERR_ARG, "NewtonIntegrator.isSuperquadrics must be 1 for superellipsoid scenes");
+  CK(cudaSetDevice(c->device));
+  const bool vdChanged = !c->haveParams || p->verletDist != c->params.verletDist;
+  c->params = *p;
+  c->haveParams = true;
+  if (c->haveBodies) {
+    sqdem_status s = uploadParams(c);
+    if (s) return s;
+    if (vdChanged) {
+      double vd = p->verletDist;
+      CK(cudaMemcpyAsync((char*)c->d.S + offsetof(SceneState, verletDistCur), &vd, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return SQDEM_OK;
+}
+
+static void packState(sqdem_ctx* c, int n, const double* st, std::vector<double4>* v) {
+  // v: pos, ori, vel, angVel, angMom
+  for (int i = 0; i < n; i++) {
+    const double* o = st + (size_t)i * SQDEM_BODY_STRIDE;
+    v[0][i] = make_double4(o[0], o[1], o[2], 0);
+    v[1][i] = make_double4(o[3], o[4], o[5], o[6]);
+    v[2][i] = make_double4(o[7], o[8], o[9], 0);
+    v[3][i] = make_double4(o[10], o[11], o[12], 0);
+    v[4][i] = make_double4(o[13], o[14], o[15], 0);
+  }
+  (void)c;
+}
+
+sqdem_status sqdem_set_bodies(sqdem_ctx* c, int n, const int* kind, const double* shape5, const int* was,
+                              const int* mat, const int* isSphere, const double* state) {
+  if (!c || n <= 0 || !kind || !mat || !state) return fail(c, SQDEM_ERR_ARG, "bad bodies");
+  if (!c->haveMats) return fail(c, SQDEM_ERR_STATE, "set materials first");
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  freeAll(c);
+  c->haveBodies = false;
+  CK(dalloc(c, &c->d.mats, c->nMats)); CK(dalloc(c, &c->d.matsB, c->nMats));
+  CK(cudaMemcpyAsync(c->d.mats, c->hostMats.data(), sizeof(double4) * c->nMats, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d.matsB, c->hostMatsB.data(), sizeof(double2) * c->nMats, cudaMemcpyHostToDevice, c->stream));
+  c->kind.assign(kind, kind + n);
+  c->matIds.assign(mat, mat + n);
+  c->shape5.assign(5 * (size_t)n, 0.0);
+  c->isSphere.assign(n, 0); c->axisSense.assign(2 * (size_t)n, 0);
+  c->wallIds.clear();
+  int NP = 0;
+  for (int i = 0; i < n; i++) {
+    if (mat[i] < 0 || mat[i] >= c->nMats) return fail(c, SQDEM_ERR_ARG, "material id out of range");
+    if (kind[i] == SQDEM_WALL) {
+      if (!was) return fail(c, SQDEM_ERR_ARG, "wall axis/sense missing");
+      int ax = was[2 * i], se = was[2 * i + 1];
+      if (ax < 0 || ax > 2 || se < -1 || se > 1) return fail(c, SQDEM_ERR_ARG, "bad wall axis/sense");
+      c->axisSense[2 * i] = ax; c->axisSense[2 * i + 1] = se;
+      c->wallIds.push_back(i);
+    } else if (kind[i] == SQDEM_SUPERQUADRIC) {
+      if (!shape5) return fail(c, SQDEM_ERR_ARG, "shape missing");
+      for (int k = 0; k < 5; k++) c->shape5[5 * i + k] = shape5[5 * i + k];
+      for (int k = 0; k < 5; k++)
+        if (!(shape5[5 * i + k] > 0)) return fail(c, SQDEM_ERR_ARG, "shape parameters must be positive");
+      if (shape5[5 * i + 3] >= 2.0 || shape5[5 * i + 4] >= 2.0) return fail(c, SQDEM_ERR_ARG, "eps must be < 2");
+      c->isSphere[i] = isSphere ? (isSphere[i] != 0) : 0;
+      NP++;
+    } else return fail(c, SQDEM_ERR_ARG, "unknown body kind");
+  }
+  if (!finiteRows(state, n, SQDEM_BODY_STRIDE, 16)) return fail(c, SQDEM_ERR_ARG, "non-finite body state");
+  Dev& d = c->d;
+  d.N = n; d.NP = NP; d.W = (int)c->wallIds.size();
+  d.MAXC = c->maxCand;
+  d.Pcap = (int)std::min<long long>((long long)c->contactsPerBody * NP + 64, 0x7fffffffLL - 1024);
+  d.Gmax = std::max(8 * NP, 1 << 12);
+  CK(dalloc(c, &d.prm, 1)); CK(dalloc(c, &d.S, 1));
+  CK(dalloc(c, &d.pos, n)); CK(dalloc(c, &d.ori, n)); CK(dalloc(c, &d.vel, n)); CK(dalloc(c, &d.angVel, n));
+  CK(dalloc(c, &d.angMom, n)); CK(dalloc(c, &d.inertia, n)); CK(dalloc(c, &d.shpA, n)); CK(dalloc(c, &d.shpB, n));
+  CK(dalloc(c, &d.mass, n)); CK(dalloc(c, &d.info, n)); CK(dalloc(c, &d.blocked, n)); CK(dalloc(c, &d.damped, n));
+  CK(dalloc(c, &d.aspherical, n));
+  CK(dalloc(c, &d.bmin, n)); CK(dalloc(c, &d.bmax, n)); CK(dalloc(c, &d.ref, n)); CK(dalloc(c, &d.pmin, n));
+  CK(dalloc(c, &d.pmax, n)); CK(dalloc(c, &d.force, n)); CK(dalloc(c, &d.torque, n));
+  CK(dalloc(c, &d.walls, std::max(d.W, 1)));
+  sqdem_status s;
+  if ((s = allocTable(c, d.A, d.Pcap))) return s;
+  if ((s = allocTable(c, d.B, d.Pcap))) return s;
+  CK(dalloc(c, &d.rowStart, n + 1)); CK(dalloc(c, &d.rowStartNew, n + 1)); CK(dalloc(c, &d.rowCount, n + 1));
+  CK(dalloc(c, &d.cand, (size_t)n * d.MAXC)); CK(dalloc(c, &d.candCount, n));
+  CK(dalloc(c, &d.pCount, n + 1)); CK(dalloc(c, &d.pStart, n + 1)); CK(dalloc(c, &d.pFill, n + 1));
+  CK(dalloc(c, &d.pList, d.Pcap));
+  CK(dalloc(c, &d.wCount, 2 * std::max(d.W, 1))); CK(dalloc(c, &d.wList, d.Pcap));
+  CK(dalloc(c, &d.ww, std::max(d.W * d.W, 1)));
+  CK(dalloc(c, &d.bodyCell, n)); CK(dalloc(c, &d.cellCount, d.Gmax + 1)); CK(dalloc(c, &d.cellStart, d.Gmax + 1));
+  CK(dalloc(c, &d.cellFill, d.Gmax + 1)); CK(dalloc(c, &d.cellBodies, n));
+  CK(dalloc(c, &d.scanTmp, nblk((long)std::max(std::max(d.Gmax, d.Pcap), d.N) + 2, SCAN_TILE) + 2));
+  // host-side body arrays
+  std::vector<double4> v[5];
+  for (int k = 0; k < 5; k++) v[k].resize(n);
+  packState(c, n, state, v);
+  std::vector<double4> inertia(n), shpA(n), shpB(n), bmin(n), bmax(n), ref(n);
+  std::vector<double> mass(n);
+  std::vector<int4> info(n);
+  std::vector<unsigned> blocked(n);
+  std::vector<int> damped(n, 1), asph(n);
+  const double nan = std::numeric_limits<double>::quiet_NaN();
+  for (int i = 0; i < n; i++) {
+    const double* o = state + (size_t)i * SQDEM_BODY_STRIDE;
+    mass[i] = o[33];
+    inertia[i] = make_double4(o[34], o[35], o[36], 0);
+    bmin[i] = make_double4(0, 0, 0, 0);
+    bmax[i] = make_double4(0, 0, 0, 0);
+    if (kind[i] == SQDEM_SUPERQUADRIC) {
+      double props[5];
+      sqdem_shape_props(shape5[5 * i], shape5[5 * i + 1], shape5[5 * i + 2], shape5[5 * i + 3], shape5[5 * i + 4], props);
+      shpA[i] = make_double4(shape5[5 * i], shape5[5 * i + 1], shape5[5 * i + 2], props[4]);
+      shpB[i] = make_double4(shape5[5 * i + 3], shape5[5 * i + 4], 0, 0);
+      info[i] = make_int4(KIND_SQ, mat[i], c->isSphere[i], 0);
+      blocked[i] = 0; asph[i] = 1;
+      ref[i] = make_double4(nan, nan, nan, 1.0);   // Aabb created with the body, refPos NaN
+    } else {
+      shpA[i] = make_double4(0, 0, 0, 0); shpB[i] = make_double4(0, 0, 0, 0);
+      info[i] = make_int4(KIND_WALL, mat[i], 0, c->axisSense[2 * i] | ((c->axisSense[2 * i + 1] + 1) << 4));
+      blocked[i] = DOF_ALL; asph[i] = 0;
+      ref[i] = make_double4(nan, nan, nan, 0.0);   // no bound until the first collider pass
+    }
+  }
+  auto up = [&](void* dst, const void* src, size_t bytes) { return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream); };
+  CK(up(d.pos, v[0].data(), sizeof(double4) * n)); CK(up(d.ori, v[1].data(), sizeof(double4) * n));
+  CK(up(d.vel, v[2].data(), sizeof(double4) * n)); CK(up(d.angVel, v[3].data(), sizeof(double4) * n));
+  CK(up(d.angMom, v[4].data(), sizeof(double4) * n));
+  CK(up(d.inertia, inertia.data(), sizeof(double4) * n)); CK(up(d.shpA, shpA.data(), sizeof(double4) * n));
+  CK(up(d.shpB, shpB.data(), sizeof(double4) * n)); CK(up(d.mass, mass.data(), sizeof(double) * n));
+  CK(up(d.info, info.data(), sizeof(int4) * n)); CK(up(d.blocked, blocked.data(), sizeof(unsigned) * n));
+  CK(up(d.damped, damped.data(), sizeof(int) * n)); CK(up(d.aspherical, asph.data(), sizeof(int) * n));
+  CK(up(d.bmin, bmin.data(), sizeof(double4) * n)); CK(up(d.bmax, bmax.data(), sizeof(double4) * n));
+  CK(up(d.ref, ref.data(), sizeof(double4) * n)); CK(up(d.pmin, bmin.data(), sizeof(double4) * n));
+  CK(up(d.pmax, bmax.data(), sizeof(double4) * n));
+  if (d.W) CK(up(d.walls, c->wallIds.data(), sizeof(int) * d.W));
+  SceneState S;
+  std::memset(&S, 0, sizeof(S));
+  S.maxVelocitySq = nan; S.fastestBodyMaxDist = -1; S.verletDistCur = c->params.verletDist;
+  CK(up(d.S, &S, sizeof(S)));
+  c->haveBodies = true;
+  c->graphValid = false;
+  if ((s = uploadParams(c))) return s;
+  CK(cudaStreamSynchronize(c->stream));
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_step(sqdem_ctx* c, int nsteps) {
+  if (!c) return SQDEM_ERR_ARG;
+  if (!c->haveBodies || !c->haveMats) return fail(c, SQDEM_ERR_STATE, "bodies and materials must be set before stepping");
+  if (nsteps < 0) return fail(c, SQDEM_ERR_ARG, "negative step count");
+  CK(cudaSetDevice(c->device));
+  if (c->useGraph) {
+    sqdem_status s = ensureGraph(c);
+    if (s) return s;
+    for (int i = 0; i < nsteps; i++) CK(cudaGraphLaunch(c->exec, c->stream));
+    c->launches += c->launchesPerStep * nsteps;
+  } else {
+    float acc[3] = {0, 0, 0};
+    for (int i = 0; i < nsteps; i++) {
+      enqueueStep(c, true);
+      CK(cudaEventSynchronize(c->ev[3]));
+      float t;
+      cudaEventElapsedTime(&t, c->ev[0], c->ev[1]); acc[0] += t;
+      cudaEventElapsedTime(&t, c->ev[1], c->ev[2]); acc[1] += t;
+      cudaEventElapsedTime(&t, c->ev[2], c->ev[3]); acc[2] += t;
+    }
+    for (int k = 0; k < 3; k++) c->stageMs[k] = acc[k];
+  }
+  CK(cudaGetLastError());
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_sync(sqdem_ctx* c, sqdem_report* r) {
+  if (!c) return SQDEM_ERR_ARG;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  if (!c->haveBodies) { if (r) std::memset(r, 0, sizeof(*r)); return SQDEM_OK; }
+  unsigned long long e[E_NUM];
+  CK(cudaMemcpy(e, (char*)c->d.S + offsetof(SceneState, err), sizeof(e), cudaMemcpyDeviceToHost));
+  unsigned long long z[E_NUM]; std::memset(z, 0, sizeof(z));
+  CK(cudaMemcpy((char*)c->d.S + offsetof(SceneState, err), z, sizeof(z), cudaMemcpyHostToDevice));
+  if (r) {
+    r->nan_normals = (long long)e[E_NAN_NORMAL]; r->nan_forces = (long long)e[E_NAN_FORCE];
+    r->lm_calls = (long long)e[E_LM_CALLS]; r->lm_iterations = (long long)e[E_LM_ITERS];
+    r->lm_maxiter = (long long)e[E_LM_MAX]; r->overflow = (long long)e[E_OVERFLOW];
+    r->collider_runs = (long long)e[E_COLLIDER_RUNS]; r->steps = (long long)e[E_STEPS];
+  }
+  if (e[E_OVERFLOW]) return fail(c, SQDEM_ERR_CAPACITY, "contact table or candidate buffer overflow; increase contacts_per_body");
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_get_body_state(sqdem_ctx* c, double* out) {
+  if (!c || !out) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  const int n = c->d.N;
+  std::vector<double4> pos(n), ori(n), vel(n), av(n), am(n), f(n), t(n), mn(n), mx(n), rf(n), in(n);
+  std::vector<double> mass(n);
+  auto dn = [&](void* dst, const void* src, size_t bytes) { return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream); };
+  CK(dn(pos.data(), c->d.pos, 32 * n)); CK(dn(ori.data(), c->d.ori, 32 * n)); CK(dn(vel.data(), c->d.vel, 32 * n));
+  CK(dn(av.data(), c->d.angVel, 32 * n)); CK(dn(am.data(), c->d.angMom, 32 * n)); CK(dn(f.data(), c->d.force, 32 * n));
+  CK(dn(t.data(), c->d.torque, 32 * n)); CK(dn(mn.data(), c->d.bmin, 32 * n)); CK(dn(mx.data(), c->d.bmax, 32 * n));
+  CK(dn(rf.data(), c->d.ref, 32 * n)); CK(dn(in.data(), c->d.inertia, 32 * n)); CK(dn(mass.data(), c->d.mass, 8 * n));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < n; i++) {
+    double* o = out + (size_t)i * SQDEM_BODY_STRIDE;
+    o[0] = pos[i].x; o[1] = pos[i].y; o[2] = pos[i].z;
+    o[3] = ori[i].x; o[4] = ori[i].y; o[5] = ori[i].z; o[6] = ori[i].w;
+    o[7] = vel[i].x; o[8] = vel[i].y; o[9] = vel[i].z;
+    o[10] = av[i].x; o[11] = av[i].y; o[12] = av[i].z;
+    o[13] = am[i].x; o[14] = am[i].y; o[15] = am[i].z;
+    o[16] = f[i].x; o[17] = f[i].y; o[18] = f[i].z;
+    o[19] = t[i].x; o[20] = t[i].y; o[21] = t[i].z;
+    o[22] = mn[i].x; o[23] = mn[i].y; o[24] = mn[i].z;
+    o[25] = mx[i].x; o[26] = mx[i].y; o[27] = mx[i].z;
+    o[28] = rf[i].x; o[29] = rf[i].y; o[30] = rf[i].z;
+    o[31] = mn[i].w; o[32] = mx[i].w; o[33] = mass[i];
+    o[34] = in[i].x; o[35] = in[i].y; o[36] = in[i].z;
+  }
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_put_body_state(sqdem_ctx* c, const double* in) {
+  if (!c || !in) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  if (!finiteRows(in, c->d.N, SQDEM_BODY_STRIDE, 16))
+    return fail(c, SQDEM_ERR_ARG, "non-finite position, orientation or velocity");
+  CK(cudaSetDevice(c->device));
+  const int n = c->d.N;
+  std::vector<double4> v[5];
+  for (int k = 0; k < 5; k++) v[k].resize(n);
+  packState(c, n, in, v);
+  std::vector<double4> mn(n), mx(n), rf(n);
+  for (int i = 0; i < n; i++) {
+    const double* o = in + (size_t)i * SQDEM_BODY_STRIDE;
+    mn[i] = make_double4(o[22], o[23], o[24], o[31]);
+    mx[i] = make_double4(o[25], o[26], o[27], o[32]);
+    bool hasBound = (c->kind[i] == SQDEM_SUPERQUADRIC) || !std::isnan(o[28]);
+    rf[i] = make_double4(o[28], o[29], o[30], hasBound ? 1.0 : 0.0);
+  }
+  auto up = [&](void* dst, const void* src, size_t bytes) { return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream); };
+  CK(up(c->d.pos, v[0].data(), 32 * n)); CK(up(c->d.ori, v[1].data(), 32 * n)); CK(up(c->d.vel, v[2].data(), 32 * n));
+  CK(up(c->d.angVel, v[3].data(), 32 * n)); CK(up(c->d.angMom, v[4].data(), 32 * n));
+  CK(up(c->d.bmin, mn.data(), 32 * n)); CK(up(c->d.bmax, mx.data(), 32 * n)); CK(up(c->d.ref, rf.data(), 32 * n));
+  CK(up(c->d.pmin, mn.data(), 32 * n)); CK(up(c->d.pmax, mx.data(), 32 * n));
+  CK(cudaStreamSynchronize(c->stream));
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_get_kinematics(sqdem_ctx* c, double* out16) {
+  if (!c || !out16) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  const int n = c->d.N;
+  // five double4 planes -> 16 doubles per body, copied straight from device memory
+  CK(cudaMemcpy2DAsync(out16 + 0, 16 * 8, c->d.pos, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpy2DAsync(out16 + 3, 16 * 8, c->d.ori, 32, 32, n, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpy2DAsync(out16 + 7, 16 * 8, c->d.vel, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpy2DAsync(out16 + 10, 16 * 8, c->d.angVel, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpy2DAsync(out16 + 13, 16 * 8, c->d.angMom, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SQDEM_OK;
+}
+sqdem_status sqdem_put_kinematics(sqdem_ctx* c, const double* in16) {
+  if (!c || !in16) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  if (!finiteRows(in16, c->d.N, 16, 16)) return fail(c, SQDEM_ERR_ARG, "non-finite kinematic state");
+  CK(cudaSetDevice(c->device));
+  const int n = c->d.N;
+  CK(cudaMemcpy2DAsync(c->d.pos, 32, in16 + 0, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpy2DAsync(c->d.ori, 32, in16 + 3, 16 * 8, 32, n, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpy2DAsync(c->d.vel, 32, in16 + 7, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpy2DAsync(c->d.angVel, 32, in16 + 10, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpy2DAsync(c->d.angMom, 32, in16 + 13, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
+  return SQDEM_OK;
+}
+
+static sqdem_status readScene(sqdem_ctx* c, SceneState& S) {
+  CK(cudaMemcpyAsync(&S, c->d.S, sizeof(S), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_num_interactions(sqdem_ctx* c, int include_potential, long* n) {
+  if (!c || !n) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) { *n = 0; return SQDEM_OK; }
+  CK(cudaSetDevice(c->device));
+  SceneState S; sqdem_status s = readScene(c, S); if (s) return s;
+  if (include_potential) { *n = (long)S.P + S.nWW; return SQDEM_OK; }
+  std::vector<unsigned> fl(S.P);
+  if (S.P) CK(cudaMemcpy(fl.data(), c->d.A.flags, 4 * (size_t)S.P, cudaMemcpyDeviceToHost));
+  long k = 0;
+  for (int i = 0; i < S.P; i++) k += ((fl[i] & (F_GEOM | F_PHYS)) == (F_GEOM | F_PHYS));
+  *n = k;
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_get_interactions(sqdem_ctx* c, int include_potential, double* out, long cap, long* nout) {
+  if (!c || !nout) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) { *nout = 0; return SQDEM_OK; }
+  CK(cudaSetDevice(c->device));
+  SceneState S; sqdem_status s = readScene(c, S); if (s) return s;
+  const int P = S.P;
+  const Table& T = c->d.A;
+  std::vector<int> ow(P), pa(P); std::vector<unsigned> fl(P); std::vector<double2> an(P); std::vector<double> de(P);
+  std::vector<double4> nm(P), sh(P), nf(P), ph(P), cp(P), p1(P), p2(P), si(P), tw(P), orr(P), rn(P), rs(P);
+  std::vector<int2> ww(S.nWW);
+  if (P) {
+    CK(cudaMemcpy(ow.data(), T.owner, 4 * (size_t)P, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(pa.data(), T.partner, 4 * (size_t)P, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(fl.data(), T.flags, 4 * (size_t)P, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(an.data(), T.angle, 16 * (size_t)P, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(de.data(), T.depth, 8 * (size_t)P, cudaMemcpyDeviceToHost));
+    const size_t b4 = 32 * (size_t)P;
+    CK(cudaMemcpy(nm.data(), T.normal, b4, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(sh.data(), T.shear, b4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(nf.data(), T.nforce, b4, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(ph.data(), T.phys, b4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(cp.data(), T.cp, b4, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(p1.data(), T.p1, b4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(p2.data(), T.p2, b4, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(si.data(), T.shearInc, b4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(tw.data(), T.twist, b4, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(orr.data(), T.ortho, b4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(rn.data(), T.relVn, b4, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(rs.data(), T.relVs, b4, cudaMemcpyDeviceToHost));
+  }
+  if (S.nWW) CK(cudaMemcpy(ww.data(), c->d.ww, sizeof(int2) * S.nWW, cudaMemcpyDeviceToHost));
+  long k = 0;
+  auto put3 = [](double* o, double4 v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; };
+  for (int i = 0; i < P; i++) {
+    const bool real = (fl[i] & (F_GEOM | F_PHYS)) == (F_GEOM | F_PHYS);
+    if (!include_potential && !real) continue;
+    if (out && k < cap) {
+      double* o = out + (size_t)k * SQDEM_INTR_STRIDE;
+      std::memset(o, 0, sizeof(double) * SQDEM_INTR_STRIDE);
+      const bool ownerId1 = (fl[i] & F_OWNER_ID1) != 0;
+      o[0] = ownerId1 ? ow[i] : pa[i]; o[1] = ownerId1 ? pa[i] : ow[i];
+      o[2] = real; o[3] = (fl[i] & F_GEOM) ? 1 : 0; o[4] = de[i]; o[5] = an[i].x; o[6] = an[i].y;
+      put3(o + 7, cp[i]); put3(o + 10, nm[i]); put3(o + 13, si[i]); put3(o + 16, p1[i]); put3(o + 19, p2[i]);
+      o[22] = (fl[i] & F_SHEARNEW) ? 1 : 0;
+      o[23] = ph[i].x; o[24] = ph[i].y; o[25] = ph[i].z;
+      put3(o + 26, nf[i]); put3(o + 29, sh[i]); put3(o + 32, tw[i]); put3(o + 35, orr[i]); put3(o + 38, rn[i]); put3(o + 41, rs[i]);
+    }
+    k++;
+  }
+  if (include_potential)
+    for (int i = 0; i < S.nWW; i++) {
+      if (out && k < cap) {
+        double* o = out + (size_t)k * SQDEM_INTR_STRIDE;
+        std::memset(o, 0, sizeof(double) * SQDEM_INTR_STRIDE);
+        o[0] = ww[i].x; o[1] = ww[i].y; o[22] = 1;
+      }
+      k++;
+    }
+  *nout = k;
+  if (out && k > cap) return fail(c, SQDEM_ERR_ARG, "output capacity too small");
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_put_interactions(sqdem_ctx* c, long n, const double* in) {
+  if (!c || n < 0 || (n && !in)) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  const int N = c->d.N;
+  struct Rec { int owner, partner; long idx; };
+  std::vector<Rec> recs;
+  std::vector<int2> ww;
+  for (long i = 0; i < n; i++) {
+    const double* o = in + (size_t)i * SQDEM_INTR_STRIDE;
+    int a = (int)o[0], b = (int)o[1];
+    if (a < 0 || b < 0 || a >= N || b >= N || a == b) return fail(c, SQDEM_ERR_ARG, "bad interaction ids");
+    bool wa = c->kind[a] == SQDEM_WALL, wb = c->kind[b] == SQDEM_WALL;
+    if (wa && wb) { ww.push_back(make_int2(std::min(a, b), std::max(a, b))); continue; }
+    int owner = wa ? b : (wb ? a : std::min(a, b));
+    int partner = owner == a ? b : a;
+    recs.push_back(Rec{owner, partner, i});
+  }
+  std::sort(recs.begin(), recs.end(), [](const Rec& x, const Rec& y) {
+    return x.owner != y.owner ? x.owner < y.owner : x.partner < y.partner;
+  });
+  for (size_t i = 1; i < recs.size(); i++)
+    if (recs[i].owner == recs[i - 1].owner && recs[i].partner == recs[i - 1].partner)
+      return fail(c, SQDEM_ERR_ARG, "duplicate interaction");
+  const int P = (int)recs.size();
+  if (P > c->d.Pcap) return fail(c, SQDEM_ERR_CAPACITY, "too many interactions for the table");
+  std::vector<int> ow(P), pa(P), rowStart(N + 1, 0);
+  std::vector<unsigned> fl(P); std::vector<double2> an(P); std::vector<double> de(P);
+  std::vector<double4> nm(P), sh(P), nf(P), ph(P), cp(P), p1(P), p2(P), si(P), tw(P), orr(P), rn(P), rs(P), F(P);
+  auto g3 = [](const double* o) { return make_double4(o[0], o[1], o[2], 0); };
+  for (int e = 0; e < P; e++) {
+    const double* o = in + (size_t)recs[e].idx * SQDEM_INTR_STRIDE;
+    ow[e] = recs[e].owner; pa[e] = recs[e].partner;
+    rowStart[ow[e] + 1]++;
+    unsigned f = 0;
+    if (o[3] != 0) f |= F_GEOM;
+    if (o[2] != 0) f |= F_GEOM | F_PHYS;
+    if (o[22] != 0) f |= F_SHEARNEW;
+    if ((int)o[0] == ow[e]) f |= F_OWNER_ID1;
+    fl[e] = f;
+    de[e] = o[4]; an[e] = make_double2(o[5], o[6]);
+    cp[e] = g3(o + 7); nm[e] = g3(o + 10); si[e] = g3(o + 13); p1[e] = g3(o + 16); p2[e] = g3(o + 19);
+    ph[e] = make_double4(o[23], o[24], o[25], 0);
+    nf[e] = g3(o + 26); sh[e] = g3(o + 29); tw[e] = g3(o + 32); orr[e] = g3(o + 35); rn[e] = g3(o + 38); rs[e] = g3(o + 41);
+    F[e] = make_double4(0, 0, 0, 0);
+  }
+  for (int i = 0; i < N; i++) rowStart[i + 1] += rowStart[i];
+  // partner incidence lists (ascending entry index) and wall lists
+  std::vector<int> pStart(N + 1, 0), pList(P), wCount(2 * std::max(c->d.W, 1), 0), wList(P);
+  for (int e = 0; e < P; e++) if (c->kind[pa[e]] == SQDEM_SUPERQUADRIC) pStart[pa[e] + 1]++;
+  for (int i = 0; i < N; i++) pStart[i + 1] += pStart[i];
+  {
+    std::vector<int> fill(N, 0);
+    for (int e = 0; e < P; e++) if (c->kind[pa[e]] == SQDEM_SUPERQUADRIC) pList[pStart[pa[e]] + fill[pa[e]]++] = e;
+    int off = 0;
+    for (int w = 0; w < c->d.W; w++) {
+      int wid = c->wallIds[w], cnt = 0;
+      wCount[c->d.W + w] = off;
+      for (int e = 0; e < P; e++) if (pa[e] == wid) { wList[off + cnt] = e; cnt++; }
+      wCount[w] = cnt; off += cnt;
+    }
+  }
+  const Table& T = c->d.A;
+  auto up = [&](void* dst, const void* src, size_t bytes) { return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream) : cudaSuccess; };
+  CK(up(T.owner, ow.data(), 4 * (size_t)P)); CK(up(T.partner, pa.data(), 4 * (size_t)P)); CK(up(T.flags, fl.data(), 4 * (size_t)P));
+  CK(up(T.angle, an.data(), 16 * (size_t)P)); CK(up(T.depth, de.data(), 8 * (size_t)P));
+  const size_t b4 = 32 * (size_t)P;
+  CK(up(T.normal, nm.data(), b4)); CK(up(T.shear, sh.data(), b4)); CK(up(T.nforce, nf.data(), b4)); CK(up(T.phys, ph.data(), b4));
+  CK(up(T.cp, cp.data(), b4)); CK(up(T.p1, p1.data(), b4)); CK(up(T.p2, p2.data(), b4)); CK(up(T.shearInc, si.data(), b4));
+  CK(up(T.twist, tw.data(), b4)); CK(up(T.ortho, orr.data(), b4)); CK(up(T.relVn, rn.data(), b4)); CK(up(T.relVs, rs.data(), b4));
+  CK(up(T.F, F.data(), b4));
+  CK(up(c->d.rowStart, rowStart.data(), 4 * (size_t)(N + 1)));
+  CK(up(c->d.pStart, pStart.data(), 4 * (size_t)(N + 1))); CK(up(c->d.pList, pList.data(), 4 * (size_t)P));
+  CK(up(c->d.wCount, wCount.data(), 4 * wCount.size())); CK(up(c->d.wList, wList.data(), 4 * (size_t)P));
+  if (!ww.empty()) CK(up(c->d.ww, ww.data(), sizeof(int2) * ww.size()));
+  int Pi = P, nWW = (int)ww.size();
+  CK(up((char*)c->d.S + offsetof(SceneState, P), &Pi, sizeof(int)));
+  CK(up((char*)c->d.S + offsetof(SceneState, nWW), &nWW, sizeof(int)));
+  CK(cudaStreamSynchronize(c->stream));
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_get_scalars(sqdem_ctx* c, double* o) {
+  if (!c || !o) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  SceneState S; sqdem_status s = readScene(c, S); if (s) return s;
+  double mv = S.newtonRan ? (S.maxDispCode == 2 ? 2.0 : (S.maxDispCode == 1 ? 0.5 : 0.0)) : S.maxVelocitySq;
+  o[0] = (double)S.iter; o[1] = mv; o[2] = S.fastestBodyMaxDist; o[3] = S.strideActive; o[4] = S.newtonFound;
+  o[5] = S.verletDistCur; o[6] = S.numReinit; o[7] = (double)S.colliderRuns; o[8] = S.bbInit;
+  return SQDEM_OK;
+}
+sqdem_status sqdem_put_scalars(sqdem_ctx* c, const double* o) {
+  if (!c || !o) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  SceneState S; sqdem_status s = readScene(c, S); if (s) return s;
+  S.iter = (long long)o[0]; S.maxVelocitySq = o[1]; S.newtonRan = 0; S.maxDispCode = 0;
+  S.fastestBodyMaxDist = o[2]; S.strideActive = o[3] != 0; S.newtonFound = o[4] != 0; S.verletDistCur = o[5];
+  S.bbInit = o[8] != 0;
+  CK(cudaMemcpyAsync(c->d.S, &S, sizeof(S), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_stage_times(sqdem_ctx* c, double* out3) {
+  if (!c || !out3) return SQDEM_ERR_ARG;
+  for (int k = 0; k < 3; k++) out3[k] = c->stageMs[k];
+  return SQDEM_OK;
+}
+
+long long sqdem_launch_count(sqdem_ctx* c) { return c ? c->launches : 0; }
+
+// Device time of nsteps timesteps: cudaEvents recorded on the context stream around the
+// graph replays (or eager launches).
+sqdem_status sqdem_time_steps(sqdem_ctx* c, int nsteps, double* ms) {
+  if (!c || !ms || nsteps < 0) return SQDEM_ERR_ARG;
+  CK(cudaSetDevice(c->device));
+  if (c->useGraph) { sqdem_status s = ensureGraph(c); if (s) return s; }
+  CK(cudaEventRecord(c->ev[0], c->stream));
+  if (c->useGraph) {
+    for (int i = 0; i < nsteps; i++) CK(cudaGraphLaunch(c->exec, c->stream));
+    c->launches += c->launchesPerStep * nsteps;
+  } else for (int i = 0; i < nsteps; i++) enqueueStep(c, false);
+  CK(cudaEventRecord(c->ev[3], c->stream));
+  CK(cudaEventSynchronize(c->ev[3]));
+  float t = 0;
+  CK(cudaEventElapsedTime(&t, c->ev[0], c->ev[3]));
+  *ms = t;
+  return SQDEM_OK;
+}
+
+// End-to-end timing through the host interface: every step uploads the kinematic state
+// from host memory (in16, 16 doubles per body), advances one timestep and reads the state
+// back (out16).  Pinned host buffers make the copies asynchronous.
+sqdem_status sqdem_time_e2e(sqdem_ctx* c, int nsteps, const double* in16, double* out16, double* ms) {
+  if (!c || !ms || !in16 || !out16 || nsteps < 0) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  if (c->useGraph) { sqdem_status s = ensureGraph(c); if (s) return s; }
+  const int n = c->d.N;
+  CK(cudaEventRecord(c->ev[0], c->stream));
+  for (int i = 0; i < nsteps; i++) {
+    CK(cudaMemcpy2DAsync(c->d.pos, 32, in16 + 0, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpy2DAsync(c->d.ori, 32, in16 + 3, 16 * 8, 32, n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpy2DAsync(c->d.vel, 32, in16 + 7, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpy2DAsync(c->d.angVel, 32, in16 + 10, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpy2DAsync(c->d.angMom, 32, in16 + 13, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
+    if (c->useGraph) { CK(cudaGraphLaunch(c->exec, c->stream)); c->launches += c->launchesPerStep; }
+    else enqueueStep(c, false);
+    CK(cudaMemcpy2DAsync(out16 + 0, 16 * 8, c->d.pos, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpy2DAsync(out16 + 3, 16 * 8, c->d.ori, 32, 32, n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpy2DAsync(out16 + 7, 16 * 8, c->d.vel, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpy2DAsync(out16 + 10, 16 * 8, c->d.angVel, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpy2DAsync(out16 + 13, 16 * 8, c->d.angMom, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaEventRecord(c->ev[3], c->stream));
+  CK(cudaEventSynchronize(c->ev[3]));
+  float t = 0;
+  CK(cudaEventElapsedTime(&t, c->ev[0], c->ev[3]));
+  *ms = t;
+  return SQDEM_OK;
+}
+
+// Device time of the contact kernel (narrowphase + law) alone, averaged over nrep launches
+// on the current state (the state is advanced: the kernel updates contact history).
+sqdem_status sqdem_time_contacts(sqdem_ctx* c, int nrep, double* ms) {
+  if (!c || !ms || nrep <= 0) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  Dev& d = c->d;
+  CK(cudaEventRecord(c->ev[1], c->stream));
+  for (int i = 0; i < nrep; i++)
+    k_contacts<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, c->stream>>>(d);
+  CK(cudaEventRecord(c->ev[2], c->stream));
+  CK(cudaEventSynchronize(c->ev[2]));
+  CK(cudaGetLastError());
+  float t = 0;
+  CK(cudaEventElapsedTime(&t, c->ev[1], c->ev[2]));
+  *ms = t / nrep;
+  c->launches += nrep;
+  return SQDEM_OK;
+}
+
+// Switch between CUDA-graph replay (1) and eager launches with per-stage event timing (0).
+sqdem_status sqdem_set_use_graph(sqdem_ctx* c, int on) {
+  if (!c) return SQDEM_ERR_ARG;
+  c->useGraph = on ? 1 : 0;
+  return SQDEM_OK;
+}
+
+// Record the full contact geometry (point1/2, shearInc, twist/orthonormal axes, relative
+// velocities) in the table every step; off by default (extra HBM writes).
+sqdem_status sqdem_set_record_full(sqdem_ctx* c, int on) {
+  if (!c) return SQDEM_ERR_ARG;
+  c->recordFull = on ? 1 : 0;
+  if (c->haveBodies) { sqdem_status s = uploadParams(c); if (s) return s; CK(cudaStreamSynchronize(c->stream)); }
+  return SQDEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,47 @@
+"""The C-ABI library loads and exports every symbol include/sqdem.h declares (no GPU needed)."""
+import os
+import re
+
+import numpy as np
+
+import oracle as O
+from sudodem_gb300 import _native, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "sqdem.h")).read()
+    return sorted(set(re.findall(r"\b(sqdem_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_builds_and_exports_header_symbols():
+    build.build()
+    lib = _native.load_library()
+    decl = declared_symbols()
+    assert len(decl) >= 20
+    for name in decl:
+        assert hasattr(lib, name), name
+    assert set(decl) == set(_native.exported_symbols())
+
+
+def test_shape_props_host_helper_matches_oracle_bitwise():
+    rng = np.random.default_rng(3)
+    for _ in range(50):
+        s = [*rng.uniform(0.5e-3, 2e-3, 3), *rng.uniform(0.2, 1.8, 2)]
+        a = _native.shape_props(*s)
+        b = O.shape_props(*s)
+        assert np.array_equal(a, b)
+
+
+def test_engine_without_gpu_fails_loudly():
+    import pytest
+    try:
+        import torch
+        has = torch.cuda.is_available()
+    except Exception:
+        has = False
+    if has:
+        pytest.skip("a GPU is present")
+    with pytest.raises(_native.SqdemError):
+        _native.Engine(device=0)

@@ -1,0 +1,226 @@
+"""GPU engine (libsqdem_gpu.so, through the C ABI) against the CPU oracle.
+
+Bit-exact: bounds (BoundDispatcher + Bo1_*), the potential-pair set with its (id1, id2)
+orientation after every collider pass, and the real/potential state of each pair.
+
+Floating point (narrowphase, forces, integration): the reference's Levenberg-Marquardt
+search is ill-conditioned (its own result moves by up to ~1e-7 relative when an input is
+perturbed by one ulp), and CUDA's pow/atan2/sin/cos differ from glibc's in the last ulp.
+The tolerance is therefore stated against the oracle's own one-ulp sensitivity measured in
+the same test: the GPU-vs-oracle error quantiles must stay within a factor of the
+oracle-vs-perturbed-oracle quantiles, and the median error must be at the 1e-10 level.
+"""
+import numpy as np
+import pytest
+
+from oracle import OracleScene
+from sudodem_gb300 import Engine, SqdemError, assemblies
+
+pytestmark = pytest.mark.gpu
+
+
+def canon_pairs(recs, kind):
+    out = set()
+    for r in recs:
+        a, b = int(r[0]), int(r[1])
+        if kind[a] == 1 and kind[b] == 1:
+            a, b = min(a, b), max(a, b)
+        out.add((a, b))
+    return out
+
+
+def by_pair(recs):
+    return {(int(r[0]), int(r[1])): r for r in recs}
+
+
+def engine_for(spec, **kw):
+    e = Engine(device=0, **kw)
+    e.load(spec)
+    return e
+
+
+def snapshot_into(eng, orc, force_collider=False):
+    eng.put_body_state(orc.bodies())
+    eng.put_interactions(orc.interactions())
+    s = orc.scalars()
+    if force_collider:
+        s = s.copy()
+        s[1] = 2.0
+        orc.set_scalars(s)
+    eng.put_scalars(s)
+
+
+def dense_spec(seed=5, n=400):
+    return assemblies.walled_lattice(n, seed=seed, box=14e-3, per_side=5, spacing=2.1e-3)
+
+
+def rel_force_errors(G, R):
+    fg = G[:, 26:29] + G[:, 29:32]
+    fr = R[:, 26:29] + R[:, 29:32]
+    den = np.linalg.norm(fr, axis=1)
+    return np.linalg.norm(fg - fr, axis=1) / np.where(den > 0, den, 1)
+
+
+def touching_common(gi, ri):
+    G, R = by_pair(gi), by_pair(ri)
+    keys = [k for k, r in R.items() if k in G and r[4] > 0 and r[2] == 1]
+    return np.array([G[k] for k in keys]), np.array([R[k] for k in keys])
+
+
+def test_first_step_bounds_and_pair_set_bitexact(gpu):
+    spec = assemblies.config0(seed=11)
+    eng = engine_for(spec)
+    orc = OracleScene.from_spec(spec)
+    for _ in range(3):
+        eng.step(1); eng.sync(); orc.step(1)
+        g, r = eng.body_state(), orc.bodies()
+        assert np.array_equal(g[:, 22:33], r[:, 22:33])  # bmin bmax refPos sweepLength lastUpdateIter
+        gi, ri = eng.interactions(True), orc.interactions()
+        assert canon_pairs(gi, spec.kind) == canon_pairs(ri, spec.kind)
+        G, R = by_pair(gi), by_pair(ri)
+        assert all(G[k][2] == R[k][2] for k in R if k in G)
+
+
+@pytest.mark.parametrize("steps_before", [150, 400])
+def test_incremental_collider_pair_set_bitexact(gpu, steps_before):
+    spec = dense_spec(seed=6)
+    orc = OracleScene.from_spec(spec, threads=4)
+    orc.step(steps_before)
+    eng = engine_for(spec)
+    snapshot_into(eng, orc, force_collider=True)
+    eng.step(1); eng.sync(); orc.step(1)
+    assert orc.last_step_collided()
+    g, r = eng.body_state(), orc.bodies()
+    assert np.array_equal(g[:, 22:33], r[:, 22:33])
+    gi, ri = eng.interactions(True), orc.interactions()
+    assert canon_pairs(gi, spec.kind) == canon_pairs(ri, spec.kind)
+    G, R = by_pair(gi), by_pair(ri)
+    assert all(G[k][2] == R[k][2] for k in R if k in G)
+
+
+def oracle_self_sensitivity(spec, orc_state):
+    """Force errors of the oracle against itself with positions perturbed by one ulp."""
+    a = OracleScene.from_spec(spec)
+    b = OracleScene.from_spec(spec)
+    bodies, intr, sc = orc_state
+    rng = np.random.default_rng(0)
+    pert = bodies.copy()
+    sgn = rng.choice([-1.0, 1.0], size=pert[:, 0:3].shape)
+    pert[:, 0:3] = np.nextafter(pert[:, 0:3], pert[:, 0:3] + sgn * np.inf)
+    for o, bb in ((a, bodies), (b, pert)):
+        o.set_bodies(bb); o.set_interactions(intr); o.set_scalars(sc); o.rebuild_sorted_bounds()
+        o.step(1)
+    G, R = touching_common(b.interactions(), a.interactions())
+    return rel_force_errors(G, R)
+
+
+def test_single_step_contacts_within_oracle_conditioning(gpu):
+    spec = dense_spec(seed=5)
+    orc = OracleScene.from_spec(spec, threads=4)
+    orc.step(3)
+    state = (orc.bodies(), orc.interactions(), orc.scalars())
+    eng = engine_for(spec)
+    eng.set_record_full(True)
+    snapshot_into(eng, orc)
+    eng.step(1); eng.sync(); orc.step(1)
+    G, R = touching_common(eng.interactions(True), orc.interactions())
+    assert len(G) > 50
+    e = rel_force_errors(G, R)
+    depth = np.abs(G[:, 4] - R[:, 4]) / R[:, 4]
+    selfe = oracle_self_sensitivity(spec, state)
+    q = lambda x, p: float(np.quantile(x, p))
+    print(f"touching={len(e)} gpu-vs-oracle force err: median {q(e, .5):.2e} p90 {q(e, .9):.2e} max {e.max():.2e}; "
+          f"oracle 1-ulp self: median {q(selfe, .5):.2e} p90 {q(selfe, .9):.2e} max {selfe.max():.2e}; "
+          f"depth median {q(depth, .5):.2e}")
+    assert q(e, 0.5) < 1e-9
+    assert q(e, 0.9) < max(100 * q(selfe, 0.9), 1e-8)
+    assert np.mean(e < 1e-6) > 0.97
+
+
+def test_wall_contacts_tight(gpu):
+    spec = dense_spec(seed=8)
+    orc = OracleScene.from_spec(spec, threads=4)
+    orc.step(20)
+    eng = engine_for(spec)
+    snapshot_into(eng, orc)
+    eng.step(1); eng.sync(); orc.step(1)
+    G, R = touching_common(eng.interactions(True), orc.interactions())
+    wall = (G[:, 0] < 6)
+    assert wall.sum() > 5
+    e = rel_force_errors(G[wall], R[wall])
+    assert e.max() < 1e-12
+
+
+def test_body_update_parity(gpu):
+    spec = dense_spec(seed=12)
+    orc = OracleScene.from_spec(spec, threads=4)
+    orc.step(25)
+    eng = engine_for(spec)
+    snapshot_into(eng, orc)
+    x0 = orc.bodies()
+    eng.step(1); eng.sync(); orc.step(1)
+    g, r = eng.body_state(), orc.bodies()
+    p = 6
+    fr = np.linalg.norm(r[p:, 16:19], axis=1)
+    ef = np.linalg.norm(g[p:, 16:19] - r[p:, 16:19], axis=1) / np.where(fr > 0, fr, 1)
+    assert np.median(ef) < 1e-9 and np.mean(ef < 1e-6) > 0.97
+    dv = np.linalg.norm(r[p:, 7:10] - x0[p:, 7:10], axis=1)
+    ev = np.linalg.norm(g[p:, 7:10] - r[p:, 7:10], axis=1) / np.where(dv > 0, dv, 1)
+    assert np.median(ev) < 1e-9
+    assert np.max(np.abs(g[:, 0:3] - r[:, 0:3])) < 1e-13
+    qn = np.linalg.norm(g[:, 3:7], axis=1)
+    assert np.allclose(qn, 1.0, atol=1e-14)
+
+
+def test_graph_replay_equals_eager_launches(gpu):
+    spec = dense_spec(seed=3, n=200)
+    a = engine_for(spec, use_graph=True)
+    b = engine_for(spec, use_graph=False)
+    a.step(30); b.step(30)
+    a.sync(); b.sync()
+    assert np.array_equal(a.body_state(), b.body_state())
+
+
+def test_deterministic(gpu):
+    spec = dense_spec(seed=4, n=200)
+    a, b = engine_for(spec), engine_for(spec)
+    a.step(60); b.step(60)
+    a.sync(); b.sync()
+    assert np.array_equal(a.body_state(), b.body_state())
+    assert np.array_equal(a.interactions(True), b.interactions(True))
+
+
+def test_capacity_overflow_is_reported_not_faulted(gpu):
+    spec = dense_spec(seed=2, n=200)
+    eng = engine_for(spec, contacts_per_body=1)
+    eng.step(2)
+    with pytest.raises(SqdemError) as ei:
+        eng.sync()
+    assert ei.value.status == 3
+    g = eng.body_state()
+    assert np.all(np.isfinite(g[:, :16]))
+
+
+def test_nonfinite_input_rejected_on_host(gpu):
+    spec = dense_spec(seed=2, n=50)
+    eng = engine_for(spec)
+    st = eng.body_state()
+    st[10, 0] = np.nan
+    with pytest.raises(SqdemError) as ei:
+        eng.put_body_state(st)
+    assert ei.value.status == 1
+
+
+def test_deposition_statistics_match_oracle(gpu):
+    spec = assemblies.config0(seed=21)
+    eng = engine_for(spec)
+    orc = OracleScene.from_spec(spec, threads=8)
+    eng.step(2000); eng.sync(); orc.step(2000)
+    g, r = eng.body_state(), orc.bodies()
+    p = 6
+    assert abs(g[p:, 2].mean() - r[p:, 2].mean()) < 1e-3 * abs(r[p:, 2].mean())
+    ke = lambda b: 0.5 * np.sum(b[p:, 33] * np.sum(b[p:, 7:10] ** 2, axis=1))
+    assert abs(ke(g) - ke(r)) <= 0.05 * ke(r)
+    ng = np.sum(eng.interactions(False)[:, 4] > 0)
+    nr = np.sum(orc.interactions()[:, 4] > 0)
+    assert abs(int(ng) - int(nr)) <= max(3, 0.05 * nr)

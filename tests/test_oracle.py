@@ -1,0 +1,139 @@
+"""CPU tests of the oracle (the FP64 restatement of the reference's hot path)."""
+import math
+
+import numpy as np
+import pytest
+
+import kat
+import oracle as O
+from oracle import OracleScene
+from sudodem_gb300 import assemblies
+
+
+def test_shape_props_ellipsoid_closed_form():
+    # eps1 = eps2 = 1 is an ellipsoid: V = 4/3 pi abc, I_xx = V (b^2 + c^2) / 5 (unit density)
+    a, b, c = 1.1e-3, 0.9e-3, 0.8e-3
+    v, ixx, iyy, izz, rmax = O.shape_props(a, b, c, 1.0, 1.0)
+    V = 4.0 / 3.0 * math.pi * a * b * c
+    assert abs(v - V) / V < 1e-12
+    assert abs(ixx - V * (b * b + c * c) / 5) / ixx < 1e-12
+    assert abs(iyy - V * (a * a + c * c) / 5) / iyy < 1e-12
+    assert abs(izz - V * (a * a + b * b) / 5) / izz < 1e-12
+    assert rmax == a
+
+
+def test_shape_props_monte_carlo():
+    rng = np.random.default_rng(0)
+    a, b, c, e1, e2 = 1.0, 0.7, 0.5, 0.6, 1.4
+    v, ixx, iyy, izz, rmax = O.shape_props(a, b, c, e1, e2)
+    assert rmax == pytest.approx(a * math.sqrt(2))
+    p = rng.uniform(-1, 1, (400000, 3)) * np.array([a, b, c])
+    f = (np.abs(p[:, 0] / a) ** (2 / e1) + np.abs(p[:, 1] / b) ** (2 / e1)) ** (e1 / e2) + np.abs(p[:, 2] / c) ** (2 / e2)
+    inside = f < 1
+    box = 8 * a * b * c
+    vmc = box * inside.mean()
+    assert abs(vmc - v) / v < 0.01
+    izz_mc = box * np.mean(inside * (p[:, 0] ** 2 + p[:, 1] ** 2))
+    assert abs(izz_mc - izz) / izz < 0.02
+
+
+def test_surface_normal_roundtrip():
+    # Normal2Phi inverts getNormal: the angles of a surface point are recovered from its normal
+    rng = np.random.default_rng(1)
+    for _ in range(200):
+        s = np.array([*rng.uniform(0.5, 1.5, 3), *rng.uniform(0.3, 1.8, 2)])
+        ph = (rng.uniform(-3.0, 3.0), rng.uniform(-1.4, 1.4))
+        n = O.normal(s, *ph)
+        back = O.normal2phi(s, n / np.linalg.norm(n))
+        p0, p1 = O.surface(s, *ph), O.surface(s, *back)
+        assert np.linalg.norm(p0 - p1) < 1e-9 * np.max(s[:3])
+
+
+@pytest.mark.parametrize("delta_rel", [1e-4, 1e-3])
+def test_known_answer_narrowphase(delta_rel):
+    rng = np.random.default_rng(7)
+    errs = []
+    for _ in range(60):
+        sA, sB, qA, qB, pA, pB, n, delta, cp = kat.make_case(rng, eps_range=(0.6, 1.4), delta_rel=delta_rel)
+        o = OracleScene.from_spec(assemblies.pair_scene(sA, sB, pA, pB, qA, qB))
+        g = o.pair_geom(6, 7)
+        errs.append((abs(g["depth"] - delta) / delta, np.linalg.norm(g["normal"] - n)))
+    e = np.array(errs)
+    # The reference's LM stops once |dp| < 1e-5 rad (Superquadrics_Ig2.cpp:1226), so the normal
+    # carries up to ~1e-5 of that step; the depth is stationary in the direction (second order).
+    assert np.median(e[:, 0]) < 1e-4 and np.median(e[:, 1]) < 1e-4
+    assert np.mean(e[:, 0] < 1e-2) >= 0.9
+
+
+def test_sphere_flag_pair_is_analytic():
+    r = 1e-3
+    spec = assemblies.pair_scene([r, r, r, 1, 1], [r, r, r, 1, 1], [0, 0, 0], [1.9e-3, 0, 0], [1, 0, 0, 0], [1, 0, 0, 0])
+    spec.isSphere[6:] = 1
+    o = OracleScene.from_spec(spec)
+    g = o.pair_geom(6, 7)
+    assert g["depth"] == pytest.approx(0.1e-3, rel=1e-12)
+    assert np.allclose(g["normal"], [1, 0, 0])
+
+
+def test_wall_contact_closed_form():
+    # ellipsoid (eps=1) resting on the floor: depth = rz - height exactly for an unrotated body
+    spec = assemblies.walled_lattice(1, seed=0, box=10e-3, per_side=1)
+    st = spec.state
+    st[6, 0:3] = [5e-3, 5e-3, 0.9e-3]
+    spec.shape5[6] = [1e-3, 1e-3, 1e-3, 1.0, 1.0]
+    st[6, 3:7] = [1, 0, 0, 0]
+    o = OracleScene.from_spec(spec)
+    g = o.pair_geom(4, 6)
+    assert g["depth"] == pytest.approx(0.1e-3, rel=1e-9)
+    assert np.allclose(g["normal"], [0, 0, 1])
+
+
+def _brute_pairs(b, kinds):
+    mn, mx = b[:, 22:25], b[:, 25:28]
+    n = len(b)
+    out = set()
+    for i in range(n):
+        ov = np.all(mn[i] <= mx, axis=1) & np.all(mx[i] >= mn, axis=1)
+        for j in np.nonzero(ov)[0]:
+            if j > i:
+                out.add((i, int(j)))
+    return out
+
+
+def test_collider_pair_set_matches_bound_overlaps():
+    """After a step with a collider pass the container holds every pair whose closed bounds
+    overlap (InsertionSortCollider.cpp:316-383); any other pair was made non-real by the law's
+    bound-separation test in the same step (Superquadrics.cpp:1194-1207)."""
+    spec = assemblies.walled_lattice(120, seed=2, box=12e-3, per_side=4, spacing=2.2e-3)
+    o = OracleScene.from_spec(spec)
+    for _ in range(40):
+        o.step(5)
+        if not o.last_step_collided():
+            continue
+        b = o.bodies()
+        I = o.interactions()
+        have = {tuple(sorted(map(int, r[:2]))) for r in I}
+        nonreal = {tuple(sorted(map(int, r[:2]))) for r in I if r[2] == 0}
+        brute = _brute_pairs(b, spec.kind)
+        assert brute <= have
+        assert have - brute <= nonreal
+
+
+def test_deposition_runs_and_settles_downwards():
+    spec = assemblies.walled_lattice(150, seed=4, box=12e-3, per_side=4, spacing=2.6e-3)
+    o = OracleScene.from_spec(spec, threads=2)
+    z0 = o.bodies()[6:, 2].mean()
+    o.step(3000)
+    b = o.bodies()
+    assert np.all(np.isfinite(b[:, :16]))
+    assert b[6:, 2].mean() < z0
+    assert np.all(b[6:, 2] > 0)
+
+
+def test_threads_do_not_change_pair_set():
+    spec = assemblies.walled_lattice(120, seed=9, box=12e-3, per_side=4, spacing=2.2e-3)
+    a, b = OracleScene.from_spec(spec, threads=1), OracleScene.from_spec(spec, threads=4)
+    a.step(20); b.step(20)
+    ka = {tuple(map(int, r[:2])) for r in a.interactions()}
+    kb = {tuple(map(int, r[:2])) for r in b.interactions()}
+    assert ka == kb
