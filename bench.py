@@ -37,6 +37,10 @@ def workload_spec(name, seed):
         # 200,000 superellipsoids with the size distribution of the plain-vs-mixed config
         # (half-axes U[0.8,1.2] mm, eps1/eps2 U[0.3,1.8]) deposited in a walled box.
         return assemblies.deposition_box(200_000, seed=seed, eps_range=(0.3, 1.8))
+    if name == "sq200k_dense":
+        # same particles on a 2.1 mm lattice: most neighbours start in contact (a compressed state)
+        return assemblies.walled_lattice(200_000, seed=seed, box=0.2, per_side=94, spacing=2.1e-3,
+                                         eps_range=(0.3, 1.8))
     if name == "sq1k_config0":
         return assemblies.config0(seed=seed)
     if name.startswith("sq") and name.endswith("_walled"):

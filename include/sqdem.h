@@ -162,8 +162,9 @@ sqdem_status sqdem_set_use_graph(sqdem_ctx* ctx, int on);
 
 /* Timing entry points (cudaEvents on the context stream).
  * sqdem_time_steps: nsteps timesteps, device milliseconds in *ms.
- * sqdem_time_e2e:   nsteps x (upload 16 doubles/body from in16, one timestep, download to out16),
- *                   the end-to-end path of a host caller; use pinned host buffers.
+ * sqdem_time_e2e:   nsteps x (upload 16 doubles/body from host, one timestep, download to host),
+ *                   the end-to-end path of a host caller; in16 and out16 alternate as source and
+ *                   destination (the state of step i is the input of step i+1); use pinned buffers.
  * sqdem_time_contacts: one launch of the narrowphase+law kernel, averaged over nrep launches. */
 sqdem_status sqdem_time_steps(sqdem_ctx* ctx, int nsteps, double* ms);
 sqdem_status sqdem_time_e2e(sqdem_ctx* ctx, int nsteps, const double* in16, double* out16, double* ms);

@@ -47,6 +47,7 @@ def lib():
         "sqo_get_scalars": (None, [v, dp]), "sqo_set_scalars": (None, [v, dp]),
         "sqo_rebuild_sorted_bounds": (None, [v]),
         "sqo_pair_geom": (i, [v, i, i, i, dp, dp]),
+        "sqo_eval_hist": (None, [v, C.POINTER(l)]),
         "sqo_shape_props": (None, [d, d, d, d, d, dp]),
         "sqo_surface": (None, [d, d, d, d, d, d, d, dp]),
         "sqo_normal": (None, [d, d, d, d, d, d, d, dp]),
@@ -188,6 +189,11 @@ class OracleScene:
         out = (C.c_long * 5)()
         self.L.sqo_stats(self.h, out)
         return dict(zip(("lm_calls", "lm_iterations", "dis_calls", "restarts", "nan_normals"), list(out)))
+
+    def eval_hist(self):
+        out = (C.c_long * 16)()
+        self.L.sqo_eval_hist(self.h, out)
+        return list(out)
 
     def pair_geom(self, ia, ib, prior=None):
         out = np.zeros(15)

@@ -221,7 +221,8 @@ struct Bounds {
   bool operator>(const Bounds& b) const { if (id == b.id && coord == b.coord) return !isMin; return coord > b.coord; }
 };
 
-struct Stats { long lmCalls, lmIters, disCalls, restarts, nanNormals; };
+struct Stats { long lmCalls, lmIters, disCalls, restarts, nanNormals; long hist[16]; };
+
 
 struct Scene {
   std::vector<Body> bodies;
@@ -243,7 +244,7 @@ struct Scene {
   int nThreads = 1;
   std::vector<std::vector<V3>> fbuf, tbuf;
   std::vector<V3> force, torque;
-  Stats stats{0, 0, 0, 0, 0};
+  Stats stats{};
   std::vector<Stats> tstats;
   // user hook between InteractionLoop and NewtonIntegrator (boundary controllers)
   void (*midHook)(void*) = nullptr; void* midHookArg = nullptr;
@@ -612,8 +613,10 @@ static bool ig2SqSq(Scene& S, Interaction* I, const Body& b1, const Body& b2, co
     bool touching = true;
     PairCtx c{A, B, position1, position2, &st.disCalls};
     LMInfo info;
+    long dc0 = st.disCalls;
     lmder2(c, para, 50, p1, p2, center, touching, contactNormal, info);
     st.lmCalls++; st.lmIters += info.iters;
+    { long dc = st.disCalls - dc0; int b = 0; while ((1L << b) < dc && b < 15) b++; st.hist[b]++; }
     if (std::isnan(para[0]) || std::isnan(para[1]) || 7 == info.stop) {
       if (touching) {
         centerLine(position1, position2, para);
@@ -772,7 +775,7 @@ static bool law(Scene& S, Interaction* I, V3* F, V3* T) {
 static void interactionLoop(Scene& S) {
   const long size = (long)S.lin.size();
   const int nt = S.nThreads;
-  if ((int)S.fbuf.size() != nt) { S.fbuf.assign(nt, {}); S.tbuf.assign(nt, {}); S.tstats.assign(nt, Stats{0, 0, 0, 0, 0}); }
+  if ((int)S.fbuf.size() != nt) { S.fbuf.assign(nt, {}); S.tbuf.assign(nt, {}); S.tstats.assign(nt, Stats{}); }
   for (int t = 0; t < nt; t++) {
     S.fbuf[t].assign(S.bodies.size(), V3());
     S.tbuf[t].assign(S.bodies.size(), V3());
@@ -803,7 +806,8 @@ static void interactionLoop(Scene& S) {
     S.stats.lmCalls += S.tstats[t].lmCalls; S.stats.lmIters += S.tstats[t].lmIters;
     S.stats.disCalls += S.tstats[t].disCalls; S.stats.restarts += S.tstats[t].restarts;
     S.stats.nanNormals += S.tstats[t].nanNormals;
-    S.tstats[t] = Stats{0, 0, 0, 0, 0};
+    for (int k = 0; k < 16; k++) S.stats.hist[k] += S.tstats[t].hist[k];
+    S.tstats[t] = Stats{};
   }
   // ForceContainer::sync (core/ForceContainer.hpp:134-162): sum thread buffers in thread order
   const long nb = (long)S.bodies.size();
@@ -1019,6 +1023,8 @@ void sqo_stats(void* h, long* out5) {
   Stats& s = ((Scene*)h)->stats;
   out5[0] = s.lmCalls; out5[1] = s.lmIters; out5[2] = s.disCalls; out5[3] = s.restarts; out5[4] = s.nanNormals;
 }
+// histogram of Disfunction evaluations per LM solve, bucket b = ceil(log2(count))
+void sqo_eval_hist(void* h, long* out16) { for (int k = 0; k < 16; k++) out16[k] = ((Scene*)h)->stats.hist[k]; }
 double sqo_max_velocity_sq(void* h) { return ((Scene*)h)->maxVelocitySq; }
 
 // Body state, 37 doubles per body:
@@ -1152,7 +1158,7 @@ int sqo_pair_geom(void* h, int ia, int ib, int isNew, const double* prior4, doub
   if (!isNew) {
     I.hasGeom = true; I.g.contactAngle[0] = prior4[0]; I.g.contactAngle[1] = prior4[1]; I.g.PenetrationDepth = prior4[2];
   }
-  Stats st{0, 0, 0, 0, 0};
+  Stats st{};
   const Body& a = S->bodies[ia]; const Body& b = S->bodies[ib];
   if (a.kind == KIND_WALL) ig2WallSq(*S, &I, a, b, V3());
   else ig2SqSq(*S, &I, a, b, V3(), st);

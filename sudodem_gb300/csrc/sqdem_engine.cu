@@ -66,6 +66,7 @@ struct SceneState {
   int strideActive, newtonFound, doSort, dirty, bbInit;
   int runCollider, initSort, newtonRan, maxDispCode;
   int P, Pnew, nWW, overflowRun;
+  int lmCount, lmHead;
   int numReinit; long long colliderRuns;
   unsigned long long bbLo[3], bbHi[3];   // order-preserving encodings of the bbox of particle bound centres
   double org[3]; double h; int dim[3]; int nCells;
@@ -101,6 +102,7 @@ struct Dev {
   int* pCount; int* pStart; int* pFill; int* pList;
   int* wCount; int* wList;
   int2* ww;
+  int* lmQueue;
   // grid
   int* bodyCell; int* cellCount; int* cellStart; int* cellFill; int* cellBodies;
   int* scanTmp;
@@ -201,6 +203,7 @@ __global__ void k_gate(Dev d) {
     else run = 0;
   }
   S.runCollider = run;
+  S.lmCount = 0; S.lmHead = 0;
   if (run) {
     int init = 0;
     if (S.doSort) { init = 1; S.doSort = 0; }
@@ -712,6 +715,36 @@ __device__ void geomSqSq(GeomOut& g, bool isNew, double prevDepth, double2 prevA
   g.ang0 = para[0]; g.ang1 = para[1]; g.angSet = true;
 }
 
+// Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go for the two cases that need no
+// Levenberg-Marquardt search: both bodies flagged as spheres (Superquadrics_Ig2.cpp:1950-1970)
+// and centres farther apart than the bounding radii (:1973-1979).
+__device__ void geomSqSqSimple(GeomOut& g, bool isNew, double prevDepth, D3 oldNormal, D3 oldCp,
+                               const BodyView& b1, const BodyView& b2, double dt) {
+  g.precomputed = false; g.angSet = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 0; g.nanNormal = false;
+  g.cp = oldCp;
+  const D3 position1 = b1.pos, position2 = b2.pos + d3(0, 0, 0);
+  double para[2];
+  if (isNew) { g.isShearNew = true; centerLine(position1, position2, para); }
+  else { g.isShearNew = prevDepth <= 0; para[0] = 0; para[1] = 0; }
+  const double rmaxA = b1.shpA.w, rmaxB = b2.shpA.w;
+  if (!(b1.info.z != 0 && b2.info.z != 0)) { g.depth = 0; g.isShearNew = true; return; }
+  D3 dist = position2 - position1;
+  double depth = (rmaxA + rmaxB) - nrm(dist);
+  if (depth < 1E-18) { g.depth = 0; g.isShearNew = true; return; }
+  normalize(dist);
+  const D3 p1 = position1 + rmaxA * dist;
+  const D3 p2 = position2 - rmaxB * dist;
+  D3 contactNormal = p1 - p2;
+  normalize(contactNormal);
+  g.p1 = p1; g.p2 = p2;
+  g.cp = 0.5 * (p1 + p2);
+  g.depth = depth;
+  g.precomputed = true;
+  precomputeD(g, oldNormal, b1, b2, dt, contactNormal, g.isShearNew);
+  g.normal = contactNormal;
+  if (isNew) { g.ang0 = para[0]; g.ang1 = para[1]; g.angSet = true; }
+}
+
 // Ig2_Wall_Superquadrics_SuperquadricsGeom::go (Superquadrics_Ig2.cpp:2522-2611)
 __device__ void geomWallSq(GeomOut& g, bool isNew, double prevDepth, D3 oldNormal, D3 oldCp, const BodyView& w,
                            const BodyView& b, double dt) {
@@ -760,132 +793,376 @@ __device__ __forceinline__ D3 rotateShear(const GeomOut& g, D3 sf) {
   return sf;
 }
 
-__global__ void __launch_bounds__(128) k_contacts(Dev d) {
-  const SceneState& S = *d.S;
-  const Params& P = *d.prm;
-  const int Pn = S.P;
-  const bool full = P.recordFull != 0;
-  const double dt = P.dt;
-  unsigned long long lmCalls = 0, lmIters = 0, lmMax = 0, nanN = 0, nanF = 0;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < Pn; e += gridDim.x * blockDim.x) {
-    unsigned fl = d.A.flags[e];
-    const int owner = d.A.owner[e];
-    const int partner = d.A.partner[e];
-    const int id1 = (fl & F_OWNER_ID1) ? owner : partner;
-    const int id2 = (fl & F_OWNER_ID1) ? partner : owner;
-    // SuperquadricsLaw's bound-separation erase (Superquadrics.cpp:1194-1207): it discards
-    // whatever the geometry functor computed, so it is tested first.
-    const double4 amn = d.bmin[id1], amx = d.bmax[id1], bmn = d.bmin[id2], bmx = d.bmax[id2];
-    if (amn.x >= bmx.x || bmn.x >= amx.x || amn.y >= bmx.y || bmn.y >= amx.y || amn.z >= bmx.z || bmn.z >= amx.z) {
-      d.A.flags[e] = (fl & ~(F_GEOM | F_PHYS | F_FORCE)) | F_SHEARNEW;
-      d.A.nforce[e] = make_double4(0, 0, 0, 0);
-      d.A.shear[e] = make_double4(0, 0, 0, 0);
-      continue;
-    }
-    const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
-    const bool isNew = !(fl & F_GEOM);
-    double prevDepth = isNew ? 0.0 : d.A.depth[e];
-    double2 prevAngle = isNew ? make_double2(0, 0) : d.A.angle[e];
-    D3 oldNormal = isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
-    D3 oldCp = isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
-    GeomOut g;
-    if (b1.info.x == KIND_WALL) geomWallSq(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt);
-    else geomSqSq(g, isNew, prevDepth, prevAngle, oldNormal, oldCp, b1, b2, dt);
-    lmCalls += g.lmCalls; lmIters += g.lmIters; lmMax += (g.lmStop == 3); nanN += g.nanNormal;
-    fl |= F_GEOM;
-    fl = g.isShearNew ? (fl | F_SHEARNEW) : (fl & ~F_SHEARNEW);
-    // geometry history
-    d.A.depth[e] = g.depth;
-    if (g.angSet) d.A.angle[e] = make_double2(g.ang0, g.ang1);
-    else if (isNew) d.A.angle[e] = make_double2(0, 0);
-    if (g.precomputed) { d.A.normal[e] = dd4(g.normal, 0); d.A.cp[e] = dd4(g.cp, 0); }
-    else if (isNew) { d.A.normal[e] = make_double4(0, 0, 0, 0); d.A.cp[e] = make_double4(0, 0, 0, 0); }
-    if (full && g.precomputed) {
-      d.A.p1[e] = dd4(g.p1, 0); d.A.p2[e] = dd4(g.p2, 0); d.A.shearInc[e] = dd4(g.shearInc, 0);
-      d.A.twist[e] = dd4(g.twist, 0); d.A.ortho[e] = dd4(g.ortho, 0);
-      d.A.relVn[e] = dd4(g.relVn, 0); d.A.relVs[e] = dd4(g.relVs, 0);
-    } else if (full && isNew) {
-      const double4 z = make_double4(0, 0, 0, 0);
-      d.A.p1[e] = z; d.A.p2[e] = z; d.A.shearInc[e] = z; d.A.twist[e] = z; d.A.ortho[e] = z; d.A.relVn[e] = z; d.A.relVs[e] = z;
-    }
-    // Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys::go (Superquadrics.cpp:1086-1116)
-    double4 ph;
-    double2 beta;
-    if (!(fl & F_PHYS)) {
-      const double4 m1 = d.mats[b1.info.y], m2 = d.mats[b2.info.y];
-      const double2 mb1 = d.matsB[b1.info.y], mb2 = d.matsB[b2.info.y];
-      if (id1 > 5) {
-        double fa = fmin_ref(m1.z, m2.z);
-        ph.z = tan(fa);
-        ph.x = 2.0 * m1.x * m2.x / (m1.x + m2.x);
-        ph.y = 2.0 * m1.y * m2.y / (m1.y + m2.y);
-      } else {
-        ph.z = tan(m1.z); ph.x = m1.x; ph.y = m1.y;
-      }
-      beta.x = fmax_ref(mb1.x, mb2.x); beta.y = fmax_ref(mb1.y, mb2.y);
-      ph.w = 0;
-      d.A.phys[e] = ph;
-      fl |= F_PHYS;
-    } else {
-      ph = d.A.phys[e];
-      const double2 mb1 = d.matsB[b1.info.y], mb2 = d.matsB[b2.info.y];
-      beta.x = fmax_ref(mb1.x, mb2.x); beta.y = fmax_ref(mb1.y, mb2.y);
-    }
-    // SuperquadricsLaw::go (Superquadrics.cpp:1209-1361)
-    if (!(g.depth > 1E-18)) {
-      d.A.nforce[e] = make_double4(0, 0, 0, 0);
-      d.A.shear[e] = make_double4(0, 0, 0, 0);
-      fl &= ~F_FORCE;
-    } else {
-      D3 normalForce = g.normal * g.depth * ph.x;
-      const bool useDamping = (beta.x > 1e-5 || beta.y > 1e-5);
-      double cs = 0;
-      D3 shearViscous = d3(0, 0, 0);
-      if (useDamping) {
-        const bool Adyn = b1.blocked != DOF_ALL, Bdyn = b2.blocked != DOF_ALL;
-        double mbar = (!Adyn && Bdyn) ? b2.mass : ((!Bdyn && Adyn) ? b1.mass : (b1.mass * b2.mass / (b1.mass + b2.mass)));
-        double Cn_crit = 2. * sqrt(mbar * ph.x);
-        double Cs_crit = 2. * sqrt(mbar * ph.y);
-        double cn = Cn_crit * beta.x;
-        cs = Cs_crit * beta.y;
-        D3 normalViscous = cn * g.relVn;
-        D3 normTemp = normalForce - normalViscous;
-        if (dot(normTemp, g.normal) < 0.0) normalForce = d3(0, 0, 0);
-        else normalForce = normalForce - normalViscous;
-      }
-      D3 shearForce1;
-      if (g.isShearNew) shearForce1 = d3(0, 0, 0);
-      else shearForce1 = rotateShear(g, xyz(d.A.shear[e]));
-      shearForce1 = shearForce1 - ph.y * g.shearInc;
-      double maxFs = sqn(normalForce) * (ph.z * ph.z);
-      if (sqn(shearForce1) > maxFs) {
-        double ratio = sqrt(maxFs) / nrm(shearForce1);
-        shearForce1 = shearForce1 * ratio;
-      } else if (useDamping) {
-        shearViscous = cs * g.relVs;
-      }
-      if (isnan(shearForce1.x) || isnan(normalForce.x)) { normalForce = d3(0, 0, 0); shearForce1 = d3(0, 0, 0); nanF++; }
-      D3 Fv = ((-normalForce) - shearForce1) + shearViscous;
-      d.A.F[e] = dd4(Fv, 0);
-      d.A.nforce[e] = dd4(normalForce, 0);
-      d.A.shear[e] = dd4(shearForce1, 0);
-      fl |= F_FORCE;
-    }
-    d.A.flags[e] = fl;
-  }
-  // per-warp reduction of the counters
+struct Counters { unsigned long long lmCalls, lmIters, lmMax, nanN, nanF; };
+
+__device__ __forceinline__ void flushCounters(const Dev& d, Counters c) {
   for (int o = 16; o > 0; o >>= 1) {
-    lmCalls += __shfl_down_sync(0xffffffffu, lmCalls, o); lmIters += __shfl_down_sync(0xffffffffu, lmIters, o);
-    lmMax += __shfl_down_sync(0xffffffffu, lmMax, o); nanN += __shfl_down_sync(0xffffffffu, nanN, o);
-    nanF += __shfl_down_sync(0xffffffffu, nanF, o);
+    c.lmCalls += __shfl_down_sync(0xffffffffu, c.lmCalls, o); c.lmIters += __shfl_down_sync(0xffffffffu, c.lmIters, o);
+    c.lmMax += __shfl_down_sync(0xffffffffu, c.lmMax, o); c.nanN += __shfl_down_sync(0xffffffffu, c.nanN, o);
+    c.nanF += __shfl_down_sync(0xffffffffu, c.nanF, o);
   }
   if ((threadIdx.x & 31) == 0) {
-    if (lmCalls) atomicAdd(&d.S->err[E_LM_CALLS], lmCalls);
-    if (lmIters) atomicAdd(&d.S->err[E_LM_ITERS], lmIters);
-    if (lmMax) atomicAdd(&d.S->err[E_LM_MAX], lmMax);
-    if (nanN) atomicAdd(&d.S->err[E_NAN_NORMAL], nanN);
-    if (nanF) atomicAdd(&d.S->err[E_NAN_FORCE], nanF);
+    if (c.lmCalls) atomicAdd(&d.S->err[E_LM_CALLS], c.lmCalls);
+    if (c.lmIters) atomicAdd(&d.S->err[E_LM_ITERS], c.lmIters);
+    if (c.lmMax) atomicAdd(&d.S->err[E_LM_MAX], c.lmMax);
+    if (c.nanN) atomicAdd(&d.S->err[E_NAN_NORMAL], c.nanN);
+    if (c.nanF) atomicAdd(&d.S->err[E_NAN_FORCE], c.nanF);
   }
+}
+
+// Geometry history writes, Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys::go
+// (Superquadrics.cpp:1086-1116) and SuperquadricsLaw::go (Superquadrics.cpp:1209-1361) for
+// one entry whose geometry g was just computed.
+__device__ void finishEntry(const Dev& d, int e, unsigned fl, bool isNew, int id1, const BodyView& b1,
+                            const BodyView& b2, const GeomOut& g, Counters& cnt) {
+  const bool full = d.prm->recordFull != 0;
+  cnt.nanN += g.nanNormal;
+  fl |= F_GEOM;
+  fl = g.isShearNew ? (fl | F_SHEARNEW) : (fl & ~F_SHEARNEW);
+  d.A.depth[e] = g.depth;
+  if (g.angSet) d.A.angle[e] = make_double2(g.ang0, g.ang1);
+  else if (isNew) d.A.angle[e] = make_double2(0, 0);
+  if (g.precomputed) { d.A.normal[e] = dd4(g.normal, 0); d.A.cp[e] = dd4(g.cp, 0); }
+  else if (isNew) { d.A.normal[e] = make_double4(0, 0, 0, 0); d.A.cp[e] = make_double4(0, 0, 0, 0); }
+  if (full && g.precomputed) {
+    d.A.p1[e] = dd4(g.p1, 0); d.A.p2[e] = dd4(g.p2, 0); d.A.shearInc[e] = dd4(g.shearInc, 0);
+    d.A.twist[e] = dd4(g.twist, 0); d.A.ortho[e] = dd4(g.ortho, 0);
+    d.A.relVn[e] = dd4(g.relVn, 0); d.A.relVs[e] = dd4(g.relVs, 0);
+  } else if (full && isNew) {
+    const double4 z = make_double4(0, 0, 0, 0);
+    d.A.p1[e] = z; d.A.p2[e] = z; d.A.shearInc[e] = z; d.A.twist[e] = z; d.A.ortho[e] = z; d.A.relVn[e] = z; d.A.relVs[e] = z;
+  }
+  double4 ph;
+  double2 beta;
+  const double2 mb1 = d.matsB[b1.info.y], mb2 = d.matsB[b2.info.y];
+  beta.x = fmax_ref(mb1.x, mb2.x); beta.y = fmax_ref(mb1.y, mb2.y);
+  if (!(fl & F_PHYS)) {
+    const double4 m1 = d.mats[b1.info.y], m2 = d.mats[b2.info.y];
+    if (id1 > 5) {
+      double fa = fmin_ref(m1.z, m2.z);
+      ph.z = tan(fa);
+      ph.x = 2.0 * m1.x * m2.x / (m1.x + m2.x);
+      ph.y = 2.0 * m1.y * m2.y / (m1.y + m2.y);
+    } else {
+      ph.z = tan(m1.z); ph.x = m1.x; ph.y = m1.y;
+    }
+    ph.w = 0;
+    d.A.phys[e] = ph;
+    fl |= F_PHYS;
+  } else ph = d.A.phys[e];
+  if (!(g.depth > 1E-18)) {
+    d.A.nforce[e] = make_double4(0, 0, 0, 0);
+    d.A.shear[e] = make_double4(0, 0, 0, 0);
+    fl &= ~F_FORCE;
+  } else {
+    D3 normalForce = g.normal * g.depth * ph.x;
+    const bool useDamping = (beta.x > 1e-5 || beta.y > 1e-5);
+    double cs = 0;
+    D3 shearViscous = d3(0, 0, 0);
+    if (useDamping) {
+      const bool Adyn = b1.blocked != DOF_ALL, Bdyn = b2.blocked != DOF_ALL;
+      double mbar = (!Adyn && Bdyn) ? b2.mass : ((!Bdyn && Adyn) ? b1.mass : (b1.mass * b2.mass / (b1.mass + b2.mass)));
+      double Cn_crit = 2. * sqrt(mbar * ph.x);
+      double Cs_crit = 2. * sqrt(mbar * ph.y);
+      double cn = Cn_crit * beta.x;
+      cs = Cs_crit * beta.y;
+      D3 normalViscous = cn * g.relVn;
+      D3 normTemp = normalForce - normalViscous;
+      if (dot(normTemp, g.normal) < 0.0) normalForce = d3(0, 0, 0);
+      else normalForce = normalForce - normalViscous;
+    }
+    D3 shearForce1;
+    if (g.isShearNew) shearForce1 = d3(0, 0, 0);
+    else shearForce1 = rotateShear(g, xyz(d.A.shear[e]));
+    shearForce1 = shearForce1 - ph.y * g.shearInc;
+    double maxFs = sqn(normalForce) * (ph.z * ph.z);
+    if (sqn(shearForce1) > maxFs) {
+      double ratio = sqrt(maxFs) / nrm(shearForce1);
+      shearForce1 = shearForce1 * ratio;
+    } else if (useDamping) {
+      shearViscous = cs * g.relVs;
+    }
+    if (isnan(shearForce1.x) || isnan(normalForce.x)) { normalForce = d3(0, 0, 0); shearForce1 = d3(0, 0, 0); cnt.nanF++; }
+    D3 Fv = ((-normalForce) - shearForce1) + shearViscous;
+    d.A.F[e] = dd4(Fv, 0);
+    d.A.nforce[e] = dd4(normalForce, 0);
+    d.A.shear[e] = dd4(shearForce1, 0);
+    fl |= F_FORCE;
+  }
+  d.A.flags[e] = fl;
+}
+
+__device__ __forceinline__ void entryIds(const Dev& d, int e, unsigned fl, int& id1, int& id2) {
+  const int owner = d.A.owner[e], partner = d.A.partner[e];
+  id1 = (fl & F_OWNER_ID1) ? owner : partner;
+  id2 = (fl & F_OWNER_ID1) ? partner : owner;
+}
+
+// Pass 1 over the table: every entry that needs no Levenberg-Marquardt solve is finished here
+// (bound-separated pairs, wall contacts, sphere pairs, bounding-sphere rejections); the rest
+// is queued for k_contacts_lm.
+__global__ void __launch_bounds__(128) k_contacts_pre(Dev d) {
+  const SceneState& S = *d.S;
+  const int Pn = S.P;
+  const double dt = d.prm->dt;
+  Counters cnt = {0, 0, 0, 0, 0};
+  const int stride = gridDim.x * blockDim.x;
+  for (int e0 = blockIdx.x * blockDim.x; e0 < Pn; e0 += stride) {
+    const int e = e0 + threadIdx.x;
+    bool queue = false;
+    if (e < Pn) {
+      unsigned fl = d.A.flags[e];
+      int id1, id2;
+      entryIds(d, e, fl, id1, id2);
+      // SuperquadricsLaw's bound-separation erase (Superquadrics.cpp:1194-1207) discards what
+      // the geometry functor computed, so it is tested first.
+      const double4 amn = d.bmin[id1], amx = d.bmax[id1], bmn = d.bmin[id2], bmx = d.bmax[id2];
+      if (amn.x >= bmx.x || bmn.x >= amx.x || amn.y >= bmx.y || bmn.y >= amx.y || amn.z >= bmx.z || bmn.z >= amx.z) {
+        d.A.flags[e] = (fl & ~(F_GEOM | F_PHYS | F_FORCE)) | F_SHEARNEW;
+        d.A.nforce[e] = make_double4(0, 0, 0, 0);
+        d.A.shear[e] = make_double4(0, 0, 0, 0);
+      } else {
+        const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
+        const bool isNew = !(fl & F_GEOM);
+        const double prevDepth = isNew ? 0.0 : d.A.depth[e];
+        const D3 oldNormal = isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
+        const D3 oldCp = isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
+        GeomOut g;
+        bool done = true;
+        if (b1.info.x == KIND_WALL) geomWallSq(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt);
+        else {
+          const bool sph = (b1.info.z != 0) && (b2.info.z != 0);
+          if (!sph && !(nrm(b1.pos - b2.pos) > b1.shpA.w + b2.shpA.w)) done = false;
+          else geomSqSqSimple(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt);
+        }
+        if (done) finishEntry(d, e, fl, isNew, id1, b1, b2, g, cnt);
+        else queue = true;
+      }
+    }
+    // warp-aggregated append to the LM queue
+    const unsigned m = __ballot_sync(0xffffffffu, queue);
+    if (m) {
+      const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&d.S->lmCount, __popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (queue) d.lmQueue[base + __popc(m & ((1u << lane) - 1))] = e;
+    }
+  }
+  flushCounters(d, cnt);
+}
+
+// Pass 2: the Levenberg-Marquardt searches of lmder2 (Superquadrics_Ig2.cpp:1057-1354),
+// restated as a per-lane state machine.  Every round each lane of a warp evaluates exactly
+// one Disfunction (Superquadrics_Ig2.cpp:622-687) at the point its state asks for, so the
+// warp stays converged on the expensive evaluation while lanes sit at different iterations
+// of different contacts; a lane that finishes a contact takes the next one from the queue.
+// The sequence of evaluations, decisions and results per contact is that of the reference:
+// only JacfunctionApp's re-evaluation at the current point is skipped, whose outputs equal
+// the stored ones bit for bit and are overwritten by the two probes that follow.
+enum { ST_INIT = 1, ST_PROBE0 = 2, ST_PROBE1 = 3, ST_TRIAL = 4 };
+
+struct LMLane {
+  int e, st, phase, k, stop, nu;
+  bool stopFlag, touching, isNew;
+  double p0, p1, q0, q1, mu, Dp0, Dp1, pfL2, pL2;
+  double j00, j01, j11, diag0, diag1, jt0, jt1;
+  D3 pf, f1, contact, P1, P2, C;
+  unsigned calls, iters, maxit;
+};
+
+static const int LM_BS = 128;
+
+__device__ __forceinline__ void lmStartSolve(LMLane& L) {
+  L.touching = true; L.stopFlag = false; L.stop = 0;
+  L.q0 = L.p0; L.q1 = L.p1; L.st = ST_INIT;
+}
+
+// top of lmder2's for-loop: loop condition, then the checks before the Jacobian
+__device__ __forceinline__ bool lmOuter(LMLane& L) {
+  if (!(L.k < 50 && !L.stop)) { if (L.k >= 50) L.stop = 3; return false; }
+  if (L.pfL2 <= 1e-20) { L.stop = 6; return false; }
+  if (L.stopFlag) { L.stop = 9; L.touching = false; return false; }
+  double s0, c0, s1, c1;
+  sincos(L.p0, &s0, &c0);
+  sincos(L.p1, &s1, &c1);
+  L.contact = d3(c0 * c1, s0 * c1, s1);
+  double angle = dot(L.pf, L.contact) / (nrm(L.pf) * nrm(L.contact));
+  if (fabs(angle) > 0.95) { L.stop = 8; return false; }
+  L.q0 = L.p0 + L.Dp0; L.q1 = L.p1; L.st = ST_PROBE0;
+  return true;
+}
+// top of the damping while-loop
+__device__ __forceinline__ bool lmInner(LMLane& L) {
+  L.j00 += L.mu;
+  L.j11 += L.mu;
+  const double n_a = L.j00 * L.j11 - L.j01 * L.j01;
+  L.Dp0 = (L.jt0 * L.j11 - L.jt1 * L.j01) / n_a;
+  L.Dp1 = (L.jt1 * L.j00 - L.jt0 * L.j01) / n_a;
+  const double Dp_L2 = sqrt(L.Dp0 * L.Dp0 + L.Dp1 * L.Dp1);
+  if (Dp_L2 < 1e-5) { L.stop = 2; L.k++; return lmOuter(L); }
+  L.q0 = L.p0 + L.Dp0; L.q1 = L.p1 + L.Dp1;
+  if (Dp_L2 >= (L.pL2 + 1e-3) / (1e-12 * 1e-12)) { L.stop = 4; L.k++; return lmOuter(L); }
+  L.st = ST_TRIAL;
+  return true;
+}
+// consume the evaluation the lane asked for; returns true while the solve continues
+__device__ __forceinline__ bool lmConsume(LMLane& L) {
+  switch (L.st) {
+    case ST_INIT:
+      L.pf = L.P2 - L.P1;
+      L.pfL2 = nrm(L.pf);
+      L.stop = isfinite(L.pfL2) ? 0 : 7;
+      L.k = 0; L.mu = 0; L.nu = 2; L.Dp0 = 1e-7; L.Dp1 = 1e-7;
+      return lmOuter(L);
+    case ST_PROBE0:
+      L.f1 = L.P2 - L.P1;
+      L.q0 = L.p0; L.q1 = L.p1 + L.Dp1; L.st = ST_PROBE1;
+      return true;
+    case ST_PROBE1: {
+      const D3 f2 = L.P2 - L.P1, f0 = L.pf;
+      const double J00 = (L.f1.x - f0.x) / L.Dp0, J10 = (L.f1.y - f0.y) / L.Dp0, J20 = (L.f1.z - f0.z) / L.Dp0;
+      const double J01 = (f2.x - f0.x) / L.Dp1, J11 = (f2.y - f0.y) / L.Dp1, J21 = (f2.z - f0.z) / L.Dp1;
+      L.j00 = J00 * J00 + (J10 * J10 + J20 * J20);
+      L.j01 = J00 * J01 + (J10 * J11 + J20 * J21);
+      L.j11 = J01 * J01 + (J11 * J11 + J21 * J21);
+      L.jt0 = J00 * (-1.0 * f0.x) + (J10 * (-1.0 * f0.y) + J20 * (-1.0 * f0.z));
+      L.jt1 = J01 * (-1.0 * f0.x) + (J11 * (-1.0 * f0.y) + J21 * (-1.0 * f0.z));
+      const double jinf = (fabs(L.jt0) > fabs(L.jt1) ? fabs(L.jt0) : fabs(L.jt1));
+      L.pL2 = sqrt(L.p0 * L.p0 + L.p1 * L.p1);
+      if (jinf <= 1e-15) { L.stop = 1; return false; }
+      if (L.k == 0) L.mu = 1.0 * (L.j00 > L.j11 ? L.j00 : L.j11);
+      L.diag0 = L.j00; L.diag1 = L.j11;
+      return lmInner(L);
+    }
+    default: {  // ST_TRIAL
+      const D3 pDp_f = L.P2 - L.P1;
+      const double pDp_fL2 = nrm(pDp_f);
+      if (!isfinite(pDp_fL2)) { L.stop = 7; L.k++; return lmOuter(L); }
+      const double dL = L.Dp0 * (L.mu * L.Dp0 + L.jt0) + L.Dp1 * (L.mu * L.Dp1 + L.jt1);
+      const double dF = L.pfL2 - pDp_fL2;
+      double tmp = dF / dL;
+      if (tmp > 0.0) {
+        tmp = 1.0 - pow(2 * tmp - 1., 3.);
+        L.mu = L.mu * ((tmp >= 0.3333333333333334) ? tmp : 0.3333333333333334);
+        L.nu = 2;
+        L.p0 = L.q0; L.p1 = L.q1;
+        L.pf = pDp_f; L.pfL2 = pDp_fL2;
+        L.k++;
+        return lmOuter(L);
+      }
+      L.mu *= L.nu;
+      const int nu2 = (int)((unsigned)L.nu << 1);
+      if (nu2 <= L.nu) { L.stop = 5; L.k++; return lmOuter(L); }
+      L.nu = nu2;
+      L.j00 = L.diag0; L.j11 = L.diag1;
+      return lmInner(L);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
+  __shared__ SqShape shA[LM_BS], shB[LM_BS];
+  SqShape& A = shA[threadIdx.x];
+  SqShape& B = shB[threadIdx.x];
+  const SceneState& S = *d.S;
+  const int count = S.lmCount;
+  const double dt = d.prm->dt;
+  const int lane = threadIdx.x & 31;
+  Counters cnt = {0, 0, 0, 0, 0};
+  LMLane L;
+  bool active = false, exhausted = false;
+  while (true) {
+    const unsigned idle = __ballot_sync(0xffffffffu, !active && !exhausted);
+    if (idle) {
+      const int leader = __ffs(idle) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&d.S->lmHead, __popc(idle));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (!active && !exhausted) {
+        const int idx = base + __popc(idle & ((1u << lane) - 1));
+        if (idx < count) {
+          // start a contact: Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go up to lmder2
+          L.e = d.lmQueue[idx];
+          const unsigned fl = d.A.flags[L.e];
+          int id1, id2;
+          entryIds(d, L.e, fl, id1, id2);
+          const double4 o1 = d.ori[id1], o2 = d.ori[id2];
+          const double4 a1 = d.shpA[id1], a2 = d.shpA[id2], e1 = d.shpB[id1], e2 = d.shpB[id2];
+          shapeInit(A, a1.x, a1.y, a1.z, e1.x, e1.y, a1.w); A.R = quatToRot(o1.x, o1.y, o1.z, o1.w); A.pos = xyz(d.pos[id1]);
+          shapeInit(B, a2.x, a2.y, a2.z, e2.x, e2.y, a2.w); B.R = quatToRot(o2.x, o2.y, o2.z, o2.w); B.pos = xyz(d.pos[id2]);
+          L.isNew = !(fl & F_GEOM);
+          if (L.isNew) { double para[2]; centerLine(A.pos, B.pos + d3(0, 0, 0), para); L.p0 = para[0]; L.p1 = para[1]; }
+          else { const double2 an = d.A.angle[L.e]; L.p0 = an.x; L.p1 = an.y; }
+          L.contact = d3(0, 0, 0); L.P1 = d3(0, 0, 0); L.P2 = d3(0, 0, 0); L.C = d3(0, 0, 0);
+          L.phase = 0; L.calls = 0; L.iters = 0; L.maxit = 0;
+          lmStartSolve(L);
+          active = true;
+        } else exhausted = true;
+      }
+    }
+    if (!__any_sync(0xffffffffu, active)) break;
+    if (active) {
+      disfunction(A, B, L.q0, L.q1, L.C, L.P1, L.P2, L.stopFlag);
+      if (!lmConsume(L)) {
+        // one lmder2 call finished: the restart rules of Superquadrics_Ig2.cpp:2013-2053
+        L.calls++; L.iters += L.k; L.maxit += (L.stop == 3);
+        bool restart = false;
+        if (L.phase == 0) {
+          L.phase = 1;
+          if ((isnan(L.p0) || isnan(L.p1) || 7 == L.stop) && L.touching) restart = true;
+        } else if (L.phase == 1) {
+          L.phase = 3;
+          if (L.touching && 10.0 * nrm(L.P2 - L.P1) > A.rmax && (!isInside(A, L.P2 - A.pos) || !isInside(B, L.P1 - B.pos))) {
+            L.phase = 2; restart = true;
+          }
+        } else L.phase = 3;
+        if (!restart && L.phase == 1) {  // no NaN restart: continue with the local-minimum check
+          L.phase = 3;
+          if (L.touching && 10.0 * nrm(L.P2 - L.P1) > A.rmax && (!isInside(A, L.P2 - A.pos) || !isInside(B, L.P1 - B.pos))) {
+            L.phase = 2; restart = true;
+          }
+        }
+        if (restart) {
+          double para[2];
+          centerLine(A.pos, B.pos + d3(0, 0, 0), para);
+          L.p0 = para[0]; L.p1 = para[1];
+          lmStartSolve(L);
+        } else {
+          // end of Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go, then Ip2 + law
+          const int e = L.e;
+          const unsigned fl = d.A.flags[e];
+          int id1, id2;
+          entryIds(d, e, fl, id1, id2);
+          const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
+          GeomOut g;
+          g.lmCalls = L.calls; g.lmIters = L.iters; g.lmStop = 0; g.nanNormal = false;
+          g.isShearNew = L.isNew ? true : (d.A.depth[e] <= 0);
+          g.cp = L.isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
+          g.ang0 = L.p0; g.ang1 = L.p1; g.angSet = true;
+          if (!L.touching) {
+            g.precomputed = false; g.depth = 0; g.isShearNew = true;
+          } else {
+            const double pDepth = dot(L.P1 - L.P2, L.contact);
+            g.p1 = L.P1; g.p2 = L.P2;
+            if (isnan(L.contact.x)) g.nanNormal = true;
+            g.cp = L.C;
+            g.depth = pDepth;
+            D3 cn = L.contact;
+            normalize(cn);
+            const D3 oldNormal = L.isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
+            g.precomputed = true;
+            precomputeD(g, oldNormal, b1, b2, dt, cn, g.isShearNew);
+            g.normal = cn;
+          }
+          cnt.lmCalls += L.calls; cnt.lmIters += L.iters; cnt.lmMax += L.maxit;
+          finishEntry(d, e, fl, L.isNew, id1, b1, b2, g, cnt);
+          active = false;
+        }
+      }
+    }
+  }
+  flushCounters(d, cnt);
 }
 
 // contribution of table entry e to body b (b is id1 when asId1)
@@ -1080,6 +1357,8 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d) {
   (void)S;
 }
 
+__global__ void k_reset_queue(Dev d) { d.S->lmCount = 0; d.S->lmHead = 0; }
+
 __global__ void k_end(Dev d) {
   SceneState& S = *d.S;
   S.iter++;
@@ -1096,6 +1375,7 @@ using namespace sqdem;
 struct sqdem_ctx {
   int device = 0, precision = SQDEM_FP64, useGraph = 1, contactsPerBody = 16, maxCand = 64;
   int numSMs = 152;
+  int lmBlocksPerSM = 4;
   cudaStream_t stream = nullptr;
   Dev d;
   bool haveBodies = false, haveMats = false, haveParams = false;
@@ -1195,8 +1475,9 @@ static void enqueueStep(sqdem_ctx* c, bool timed) {
     c->launches += 2;
   }
   if (timed) cudaEventRecord(c->ev[1], s);
-  k_contacts<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, s>>>(d);
-  c->launches += 1;
+  k_contacts_pre<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, s>>>(d);
+  k_contacts_lm<<<c->numSMs * c->lmBlocksPerSM, LM_BS, 0, s>>>(d);
+  c->launches += 2;
   if (timed) cudaEventRecord(c->ev[2], s);
   if (d.W > 0) { k_wall_forces<<<d.W, 128, 0, s>>>(d); c->launches++; }
   k_integrate<<<nblk(N, 256), 256, 0, s>>>(d);
@@ -1303,6 +1584,11 @@ sqdem_status sqdem_create(sqdem_ctx** out, const sqdem_config* cfg) {
   CK(cudaSetDevice(c->device));
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   CK(cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, c->device));
+  {
+    int nb = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_contacts_lm, LM_BS, 0));
+    c->lmBlocksPerSM = nb > 0 ? nb : 1;
+  }
   for (int i = 0; i < 4; i++) CK(cudaEventCreate(&c->ev[i]));
   std::memset(&c->d, 0, sizeof(Dev));
   std::memset(&c->params, 0, sizeof(c->params));
@@ -1434,6 +1720,7 @@ sqdem_status sqdem_set_bodies(sqdem_ctx* c, int n, const int* kind, const double
   CK(dalloc(c, &d.pList, d.Pcap));
   CK(dalloc(c, &d.wCount, 2 * std::max(d.W, 1))); CK(dalloc(c, &d.wList, d.Pcap));
   CK(dalloc(c, &d.ww, std::max(d.W * d.W, 1)));
+  CK(dalloc(c, &d.lmQueue, d.Pcap));
   CK(dalloc(c, &d.bodyCell, n)); CK(dalloc(c, &d.cellCount, d.Gmax + 1)); CK(dalloc(c, &d.cellStart, d.Gmax + 1));
   CK(dalloc(c, &d.cellFill, d.Gmax + 1)); CK(dalloc(c, &d.cellBodies, n));
   CK(dalloc(c, &d.scanTmp, nblk((long)std::max(std::max(d.Gmax, d.Pcap), d.N) + 2, SCAN_TILE) + 2));
@@ -1832,8 +2119,9 @@ sqdem_status sqdem_time_steps(sqdem_ctx* c, int nsteps, double* ms) {
 }
 
 // End-to-end timing through the host interface: every step uploads the kinematic state
-// from host memory (in16, 16 doubles per body), advances one timestep and reads the state
-// back (out16).  Pinned host buffers make the copies asynchronous.
+// from host memory (16 doubles per body), advances one timestep and reads the state back;
+// the two host buffers alternate (step i reads the buffer step i-1 wrote, starting from in16)
+// so the trajectory continues.  Pinned host buffers make the copies asynchronous.
 sqdem_status sqdem_time_e2e(sqdem_ctx* c, int nsteps, const double* in16, double* out16, double* ms) {
   if (!c || !ms || !in16 || !out16 || nsteps < 0) return SQDEM_ERR_ARG;
   if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
@@ -1841,19 +2129,22 @@ sqdem_status sqdem_time_e2e(sqdem_ctx* c, int nsteps, const double* in16, double
   if (c->useGraph) { sqdem_status s = ensureGraph(c); if (s) return s; }
   const int n = c->d.N;
   CK(cudaEventRecord(c->ev[0], c->stream));
+  double* bufs[2] = {const_cast<double*>(in16), out16};
   for (int i = 0; i < nsteps; i++) {
-    CK(cudaMemcpy2DAsync(c->d.pos, 32, in16 + 0, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpy2DAsync(c->d.ori, 32, in16 + 3, 16 * 8, 32, n, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpy2DAsync(c->d.vel, 32, in16 + 7, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpy2DAsync(c->d.angVel, 32, in16 + 10, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpy2DAsync(c->d.angMom, 32, in16 + 13, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
+    const double* src = bufs[i & 1];
+    double* dst = bufs[(i + 1) & 1];
+    CK(cudaMemcpy2DAsync(c->d.pos, 32, src + 0, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpy2DAsync(c->d.ori, 32, src + 3, 16 * 8, 32, n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpy2DAsync(c->d.vel, 32, src + 7, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpy2DAsync(c->d.angVel, 32, src + 10, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpy2DAsync(c->d.angMom, 32, src + 13, 16 * 8, 24, n, cudaMemcpyHostToDevice, c->stream));
     if (c->useGraph) { CK(cudaGraphLaunch(c->exec, c->stream)); c->launches += c->launchesPerStep; }
     else enqueueStep(c, false);
-    CK(cudaMemcpy2DAsync(out16 + 0, 16 * 8, c->d.pos, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpy2DAsync(out16 + 3, 16 * 8, c->d.ori, 32, 32, n, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpy2DAsync(out16 + 7, 16 * 8, c->d.vel, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpy2DAsync(out16 + 10, 16 * 8, c->d.angVel, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpy2DAsync(out16 + 13, 16 * 8, c->d.angMom, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpy2DAsync(dst + 0, 16 * 8, c->d.pos, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpy2DAsync(dst + 3, 16 * 8, c->d.ori, 32, 32, n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpy2DAsync(dst + 7, 16 * 8, c->d.vel, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpy2DAsync(dst + 10, 16 * 8, c->d.angVel, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpy2DAsync(dst + 13, 16 * 8, c->d.angMom, 32, 24, n, cudaMemcpyDeviceToHost, c->stream));
   }
   CK(cudaEventRecord(c->ev[3], c->stream));
   CK(cudaEventSynchronize(c->ev[3]));
@@ -1871,15 +2162,18 @@ sqdem_status sqdem_time_contacts(sqdem_ctx* c, int nrep, double* ms) {
   CK(cudaSetDevice(c->device));
   Dev& d = c->d;
   CK(cudaEventRecord(c->ev[1], c->stream));
-  for (int i = 0; i < nrep; i++)
-    k_contacts<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, c->stream>>>(d);
+  for (int i = 0; i < nrep; i++) {
+    k_reset_queue<<<1, 1, 0, c->stream>>>(d);
+    k_contacts_pre<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, c->stream>>>(d);
+    k_contacts_lm<<<c->numSMs * c->lmBlocksPerSM, LM_BS, 0, c->stream>>>(d);
+  }
   CK(cudaEventRecord(c->ev[2], c->stream));
   CK(cudaEventSynchronize(c->ev[2]));
   CK(cudaGetLastError());
   float t = 0;
   CK(cudaEventElapsedTime(&t, c->ev[1], c->ev[2]));
   *ms = t / nrep;
-  c->launches += nrep;
+  c->launches += 3 * nrep;
   return SQDEM_OK;
 }
 
