@@ -86,6 +86,8 @@ typedef struct {
   long long overflow;         /* contact-table or candidate-buffer overflows */
   long long collider_runs;    /* collider passes executed */
   long long steps;            /* timesteps executed */
+  long long evals_fp32;       /* Disfunction evaluations in FP32 (mixed form) */
+  long long evals_fp64;       /* Disfunction evaluations in FP64 */
 } sqdem_report;
 
 /* Record layouts shared with the CPU oracle (doubles per record). */

@@ -221,3 +221,54 @@ __device__ __forceinline__ void centerLine(D3 pos1, D3 pos2, double para[2]) {
 }
 
 }  // namespace sqdem
+
+namespace sqdem {
+// ---------------------------------------------------------------------------
+// FP32 form of the shape evaluation, in the frame of body A (A at the origin).
+struct SqShapeF {
+  float rx, ry, rz, e1, e2, a1, i1, i2;
+  float R[9];
+  float px, py, pz;
+};
+struct F3 { float x, y, z; };
+__device__ __forceinline__ F3 f3(float a, float b, float c) { F3 r; r.x = a; r.y = b; r.z = c; return r; }
+__device__ __forceinline__ float dotf(F3 a, F3 b) { return a.x * b.x + (a.y * b.y + a.z * b.z); }
+__device__ __forceinline__ float nrmf(F3 a) { return sqrtf(dotf(a, a)); }
+__device__ __forceinline__ float sgnf(float f) { return f < 0 ? -1.f : (f > 0 ? 1.f : 0.f); }
+
+__device__ __forceinline__ void shapeInitF(SqShapeF& s, double rx, double ry, double rz, double e1, double e2,
+                                           const Rot& R, D3 relPos) {
+  s.rx = (float)rx; s.ry = (float)ry; s.rz = (float)rz; s.e1 = (float)e1; s.e2 = (float)e2;
+  s.a1 = (float)(2. - e1); s.i1 = (float)(1 / (2. - e1)); s.i2 = (float)(1 / (2. - e2));
+  for (int k = 0; k < 9; k++) s.R[k] = (float)R.m[k];
+  s.px = (float)relPos.x; s.py = (float)relPos.y; s.pz = (float)relPos.z;
+}
+// point of the surface of s whose outward normal is parallel to the global direction n
+__device__ __forceinline__ F3 supportF(const SqShapeF& s, F3 n) {
+  const F3 l = f3(s.R[0] * n.x + (s.R[3] * n.y + s.R[6] * n.z), s.R[1] * n.x + (s.R[4] * n.y + s.R[7] * n.z),
+                  s.R[2] * n.x + (s.R[5] * n.y + s.R[8] * n.z));
+  const float ph0 = atan2f(sgnf(l.y) * powf(fabsf(s.ry * l.y), s.i1), sgnf(l.x) * powf(fabsf(s.rx * l.x), s.i1));
+  float s0, c0;
+  sincosf(ph0, &s0, &c0);
+  const float ph1 = atan2f(sgnf(l.z) * powf(fabsf(s.rz * l.z * powf(fabsf(c0), s.a1)), s.i2),
+                           powf(fabsf(s.rx * l.x), s.i2));
+  float s1, c1;
+  sincosf(ph1, &s1, &c1);
+  const float pc1 = powf(fabsf(c1), s.e2);
+  const F3 q = f3(sgnf(c0) * s.rx * powf(fabsf(c0), s.e1) * pc1, sgnf(s0) * s.ry * powf(fabsf(s0), s.e1) * pc1,
+                  sgnf(s1) * s.rz * powf(fabsf(s1), s.e2));
+  return f3(s.R[0] * q.x + (s.R[1] * q.y + s.R[2] * q.z) + s.px, s.R[3] * q.x + (s.R[4] * q.y + s.R[5] * q.z) + s.py,
+            s.R[6] * q.x + (s.R[7] * q.y + s.R[8] * q.z) + s.pz);
+}
+// Disfunction in FP32: support points of A along c and of B along -c; sepOut = c.(p2 - p1)
+__device__ __forceinline__ void disfunctionF(const SqShapeF& A, const SqShapeF& B, float pa0, float pa1, F3& p1,
+                                             F3& p2, float& sep) {
+  float sa0, ca0, sa1, ca1;
+  sincosf(pa0, &sa0, &ca0);
+  sincosf(pa1, &sa1, &ca1);
+  const F3 c = f3(ca0 * ca1, sa0 * ca1, sa1);
+  p1 = supportF(A, c);
+  p2 = supportF(B, f3(-c.x, -c.y, -c.z));
+  sep = dotf(c, f3(p2.x - p1.x, p2.y - p1.y, p2.z - p1.z));
+}
+}  // namespace sqdem

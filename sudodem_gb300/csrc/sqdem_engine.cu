@@ -58,7 +58,7 @@ struct Params {
   int targetInterv, sortAxis, isSuperquadrics, exactAsphericalRot, recordFull;
 };
 
-enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_NUM };
+enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_EVAL32, E_EVAL64, E_NUM };
 
 struct SceneState {
   long long iter; double time;
@@ -898,9 +898,28 @@ __device__ __forceinline__ void entryIds(const Dev& d, int e, unsigned fl, int& 
   id2 = (fl & F_OWNER_ID1) ? partner : owner;
 }
 
-// Pass 1 over the table: every entry that needs no Levenberg-Marquardt solve is finished here
-// (bound-separated pairs, wall contacts, sphere pairs, bounding-sphere rejections); the rest
-// is queued for k_contacts_lm.
+// Separation screen of a superquadric pair at the point where lmder2 would start.  If one FP32
+// Disfunction evaluation there shows a support gap c.(p2 - p1) larger than SCREEN_MARGIN times
+// the summed bounding radii (FP32 error is ~1e-7 of the size), the FP64 evaluation at the same
+// point has a positive gap too, so lmder2 stops at its first check with stop_flag set
+// (Superquadrics_Ig2.cpp:1138-1143): not touching, contactAngle unchanged, depth 0.
+static const float SCREEN_MARGIN = 1e-4f;
+__device__ bool screenSeparated(const BodyView& b1, const BodyView& b2, double pa0, double pa1) {
+  if (!isfinite(pa0) || !isfinite(pa1)) return false;
+  SqShapeF A, B;
+  shapeInitF(A, b1.shpA.x, b1.shpA.y, b1.shpA.z, b1.shpB.x, b1.shpB.y, quatToRot(b1.ori.x, b1.ori.y, b1.ori.z, b1.ori.w),
+             d3(0, 0, 0));
+  shapeInitF(B, b2.shpA.x, b2.shpA.y, b2.shpA.z, b2.shpB.x, b2.shpB.y, quatToRot(b2.ori.x, b2.ori.y, b2.ori.z, b2.ori.w),
+             b2.pos - b1.pos);
+  F3 p1, p2;
+  float sep;
+  disfunctionF(A, B, (float)pa0, (float)pa1, p1, p2, sep);
+  return sep > SCREEN_MARGIN * (float)(b1.shpA.w + b2.shpA.w);
+}
+
+// Pass 1 over the table: every entry that needs no Levenberg-Marquardt iteration is finished
+// here (bound-separated pairs, wall contacts, sphere pairs, bounding-sphere rejections, pairs the
+// FP32 screen proves separated at the LM start point); the rest is queued for k_contacts_lm.
 __global__ void __launch_bounds__(128) k_contacts_pre(Dev d) {
   const SceneState& S = *d.S;
   const int Pn = S.P;
@@ -932,8 +951,17 @@ __global__ void __launch_bounds__(128) k_contacts_pre(Dev d) {
         if (b1.info.x == KIND_WALL) geomWallSq(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt);
         else {
           const bool sph = (b1.info.z != 0) && (b2.info.z != 0);
-          if (!sph && !(nrm(b1.pos - b2.pos) > b1.shpA.w + b2.shpA.w)) done = false;
-          else geomSqSqSimple(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt);
+          if (!sph && !(nrm(b1.pos - b2.pos) > b1.shpA.w + b2.shpA.w)) {
+            double para[2];
+            if (isNew) centerLine(b1.pos, b2.pos + d3(0, 0, 0), para);
+            else { const double2 an = d.A.angle[e]; para[0] = an.x; para[1] = an.y; }
+            if (screenSeparated(b1, b2, para[0], para[1])) {
+              g.precomputed = false; g.nanNormal = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 1;
+              g.cp = oldCp; g.depth = 0; g.isShearNew = true;
+              g.ang0 = para[0]; g.ang1 = para[1]; g.angSet = true;
+              cnt.lmCalls++;
+            } else done = false;
+          } else geomSqSqSimple(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt);
         }
         if (done) finishEntry(d, e, fl, isNew, id1, b1, b2, g, cnt);
         else queue = true;
@@ -1070,6 +1098,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
   const double dt = d.prm->dt;
   const int lane = threadIdx.x & 31;
   Counters cnt = {0, 0, 0, 0, 0};
+  unsigned long long ev64 = 0;
   LMLane L;
   bool active = false, exhausted = false;
   while (true) {
@@ -1104,6 +1133,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
     if (!__any_sync(0xffffffffu, active)) break;
     if (active) {
       disfunction(A, B, L.q0, L.q1, L.C, L.P1, L.P2, L.stopFlag);
+      ev64++;
       if (!lmConsume(L)) {
         // one lmder2 call finished: the restart rules of Superquadrics_Ig2.cpp:2013-2053
         L.calls++; L.iters += L.k; L.maxit += (L.stop == 3);
@@ -1163,6 +1193,264 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
     }
   }
   flushCounters(d, cnt);
+  for (int o = 16; o > 0; o >>= 1) ev64 += __shfl_down_sync(0xffffffffu, ev64, o);
+  if (lane == 0) atomicAdd(&d.S->err[E_EVAL64], ev64);
+}
+
+// ---------------------------------------------------------------------------
+// Mixed form of pass 2.  The Levenberg-Marquardt rules of lmder2 run first with FP32
+// Disfunction evaluations in the frame of body A; the same FP64 state machine as the plain
+// form then continues from the FP32 solution (warm start), with its evaluations capped at
+// MIX_EVAL64 so that non-converging searches cannot serialise the warp on the FP64 pipe.
+// A pair the FP32 search shows to be separated by more than MIX_SEP_MARGIN of the summed
+// bounding radii along some direction is separated in exact arithmetic (separating axis of
+// two convex bodies), so it is finished without FP64 work.
+static const int MIX_EVAL64 = 12;
+static const float MIX_SEP_MARGIN = 1e-4f;
+// Smallest forward-difference step of the FP32 search: FP32 evaluations resolve ~1e-7 of
+// the particle size, so steps much below 1e-4 rad give a noise-dominated Jacobian.
+static const float MIX_FD_MIN = 3e-4f;
+__device__ __forceinline__ float fdStep(float dp) { return fabsf(dp) >= MIX_FD_MIN ? dp : (dp < 0 ? -MIX_FD_MIN : MIX_FD_MIN); }
+
+struct LMLaneF {
+  int st, k, stop, nu;
+  bool stopFlag, moved;
+  float sepMax;
+  float p0, p1, q0, q1, mu, Dp0, Dp1, pfL2, pL2, j00, j01, j11, diag0, diag1, jt0, jt1;
+  F3 pf, f1, P1, P2;
+};
+
+__device__ __forceinline__ void lmfStart(LMLaneF& L, float p0, float p1) {
+  L.stopFlag = false; L.moved = false; L.stop = 0; L.sepMax = -INFINITY;
+  L.p0 = p0; L.p1 = p1; L.q0 = p0; L.q1 = p1; L.st = ST_INIT;
+}
+__device__ __forceinline__ bool lmfOuter(LMLaneF& L) {
+  if (!(L.k < 50 && !L.stop)) { if (L.k >= 50) L.stop = 3; return false; }
+  if (L.pfL2 <= 1e-20f) { L.stop = 6; return false; }
+  if (L.stopFlag) { L.stop = 9; return false; }
+  float s0, c0, s1, c1;
+  sincosf(L.p0, &s0, &c0);
+  sincosf(L.p1, &s1, &c1);
+  const F3 c = f3(c0 * c1, s0 * c1, s1);
+  const float angle = dotf(L.pf, c) / (nrmf(L.pf) * nrmf(c));
+  if (fabsf(angle) > 0.95f) { L.stop = 8; return false; }
+  L.Dp0 = fdStep(L.Dp0); L.Dp1 = fdStep(L.Dp1);
+  L.q0 = L.p0 + L.Dp0; L.q1 = L.p1; L.st = ST_PROBE0;
+  return true;
+}
+__device__ __forceinline__ bool lmfInner(LMLaneF& L) {
+  L.j00 += L.mu;
+  L.j11 += L.mu;
+  const float n_a = L.j00 * L.j11 - L.j01 * L.j01;
+  L.Dp0 = (L.jt0 * L.j11 - L.jt1 * L.j01) / n_a;
+  L.Dp1 = (L.jt1 * L.j00 - L.jt0 * L.j01) / n_a;
+  const float Dp_L2 = sqrtf(L.Dp0 * L.Dp0 + L.Dp1 * L.Dp1);
+  if (Dp_L2 < 1e-5f) { L.stop = 2; L.k++; return lmfOuter(L); }
+  L.q0 = L.p0 + L.Dp0; L.q1 = L.p1 + L.Dp1;
+  if (Dp_L2 >= (L.pL2 + 1e-3f) * 1e24f) { L.stop = 4; L.k++; return lmfOuter(L); }
+  L.st = ST_TRIAL;
+  return true;
+}
+__device__ __forceinline__ bool lmfConsume(LMLaneF& L) {
+  const F3 f = f3(L.P2.x - L.P1.x, L.P2.y - L.P1.y, L.P2.z - L.P1.z);
+  switch (L.st) {
+    case ST_INIT:
+      L.pf = f; L.pfL2 = nrmf(f);
+      L.stop = isfinite(L.pfL2) ? 0 : 7;
+      L.k = 0; L.mu = 0; L.nu = 2; L.Dp0 = 1e-7f; L.Dp1 = 1e-7f;
+      return lmfOuter(L);
+    case ST_PROBE0:
+      L.f1 = f;
+      L.q0 = L.p0; L.q1 = L.p1 + L.Dp1; L.st = ST_PROBE1;
+      return true;
+    case ST_PROBE1: {
+      const F3 f0 = L.pf;
+      const float J00 = (L.f1.x - f0.x) / L.Dp0, J10 = (L.f1.y - f0.y) / L.Dp0, J20 = (L.f1.z - f0.z) / L.Dp0;
+      const float J01 = (f.x - f0.x) / L.Dp1, J11 = (f.y - f0.y) / L.Dp1, J21 = (f.z - f0.z) / L.Dp1;
+      L.j00 = J00 * J00 + (J10 * J10 + J20 * J20);
+      L.j01 = J00 * J01 + (J10 * J11 + J20 * J21);
+      L.j11 = J01 * J01 + (J11 * J11 + J21 * J21);
+      L.jt0 = -(J00 * f0.x + (J10 * f0.y + J20 * f0.z));
+      L.jt1 = -(J01 * f0.x + (J11 * f0.y + J21 * f0.z));
+      const float jinf = fmaxf(fabsf(L.jt0), fabsf(L.jt1));
+      L.pL2 = sqrtf(L.p0 * L.p0 + L.p1 * L.p1);
+      if (jinf <= 1e-15f) { L.stop = 1; return false; }
+      if (L.k == 0) L.mu = fmaxf(L.j00, L.j11);
+      L.diag0 = L.j00; L.diag1 = L.j11;
+      return lmfInner(L);
+    }
+    default: {
+      const float fl2 = nrmf(f);
+      if (!isfinite(fl2)) { L.stop = 7; L.k++; return lmfOuter(L); }
+      const float dL = L.Dp0 * (L.mu * L.Dp0 + L.jt0) + L.Dp1 * (L.mu * L.Dp1 + L.jt1);
+      float tmp = (L.pfL2 - fl2) / dL;
+      if (tmp > 0.0f) {
+        const float t = 2 * tmp - 1.f;
+        tmp = 1.0f - t * t * t;
+        L.mu = L.mu * fmaxf(tmp, 0.33333334f);
+        L.nu = 2;
+        L.p0 = L.q0; L.p1 = L.q1;
+        L.pf = f; L.pfL2 = fl2;
+        L.moved = true;
+        L.k++;
+        return lmfOuter(L);
+      }
+      L.mu *= L.nu;
+      const int nu2 = (int)((unsigned)L.nu << 1);
+      if (nu2 <= L.nu) { L.stop = 5; L.k++; return lmfOuter(L); }
+      L.nu = nu2;
+      L.j00 = L.diag0; L.j11 = L.diag1;
+      return lmfInner(L);
+    }
+  }
+}
+
+union ShapePair {
+  struct { SqShape A, B; } d;
+  struct { SqShapeF A, B; } f;
+};
+
+__device__ __forceinline__ void buildShapes64(ShapePair& sp, const Dev& d, int id1, int id2) {
+  const double4 o1 = d.ori[id1], o2 = d.ori[id2];
+  const double4 a1 = d.shpA[id1], a2 = d.shpA[id2], e1 = d.shpB[id1], e2 = d.shpB[id2];
+  shapeInit(sp.d.A, a1.x, a1.y, a1.z, e1.x, e1.y, a1.w); sp.d.A.R = quatToRot(o1.x, o1.y, o1.z, o1.w); sp.d.A.pos = xyz(d.pos[id1]);
+  shapeInit(sp.d.B, a2.x, a2.y, a2.z, e2.x, e2.y, a2.w); sp.d.B.R = quatToRot(o2.x, o2.y, o2.z, o2.w); sp.d.B.pos = xyz(d.pos[id2]);
+}
+__device__ __forceinline__ void buildShapes32(ShapePair& sp, const Dev& d, int id1, int id2) {
+  const double4 o1 = d.ori[id1], o2 = d.ori[id2];
+  const double4 a1 = d.shpA[id1], a2 = d.shpA[id2], e1 = d.shpB[id1], e2 = d.shpB[id2];
+  const D3 rel = xyz(d.pos[id2]) - xyz(d.pos[id1]);
+  shapeInitF(sp.f.A, a1.x, a1.y, a1.z, e1.x, e1.y, quatToRot(o1.x, o1.y, o1.z, o1.w), d3(0, 0, 0));
+  shapeInitF(sp.f.B, a2.x, a2.y, a2.z, e2.x, e2.y, quatToRot(o2.x, o2.y, o2.z, o2.w), rel);
+}
+
+__global__ void __launch_bounds__(LM_BS) k_contacts_lm_mixed(Dev d) {
+  __shared__ ShapePair shp[LM_BS];
+  ShapePair& SP = shp[threadIdx.x];
+  const SceneState& S = *d.S;
+  const int count = S.lmCount;
+  const double dt = d.prm->dt;
+  const int lane = threadIdx.x & 31;
+  Counters cnt = {0, 0, 0, 0, 0};
+  unsigned long long ev32 = 0, ev64 = 0;
+  LMLane L;
+  LMLaneF F;
+  bool active = false, exhausted = false, fp32 = true;
+  int id1 = 0, id2 = 0, budget = 0;
+  double rsum = 0;
+  while (true) {
+    const unsigned idle = __ballot_sync(0xffffffffu, !active && !exhausted);
+    if (idle) {
+      const int leader = __ffs(idle) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&d.S->lmHead, __popc(idle));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (!active && !exhausted) {
+        const int idx = base + __popc(idle & ((1u << lane) - 1));
+        if (idx < count) {
+          L.e = d.lmQueue[idx];
+          const unsigned fl = d.A.flags[L.e];
+          entryIds(d, L.e, fl, id1, id2);
+          rsum = d.shpA[id1].w + d.shpA[id2].w;
+          L.isNew = !(fl & F_GEOM);
+          if (L.isNew) {
+            double para[2];
+            centerLine(xyz(d.pos[id1]), xyz(d.pos[id2]) + d3(0, 0, 0), para);
+            L.p0 = para[0]; L.p1 = para[1];
+          } else { const double2 an = d.A.angle[L.e]; L.p0 = an.x; L.p1 = an.y; }
+          L.contact = d3(0, 0, 0); L.P1 = d3(0, 0, 0); L.P2 = d3(0, 0, 0); L.C = d3(0, 0, 0);
+          L.phase = 0; L.calls = 0; L.iters = 0; L.maxit = 0; L.touching = true;
+          buildShapes32(SP, d, id1, id2);
+          lmfStart(F, (float)L.p0, (float)L.p1);
+          fp32 = true;
+          active = true;
+        } else exhausted = true;
+      }
+    }
+    if (!__any_sync(0xffffffffu, active)) break;
+    bool fin = false;
+    if (active && fp32) {
+      float sep;
+      disfunctionF(SP.f.A, SP.f.B, F.q0, F.q1, F.P1, F.P2, sep);
+      ev32++;
+      if (sep > 0) { F.stopFlag = true; F.sepMax = fmaxf(F.sepMax, sep); }
+      if (!lmfConsume(F)) {
+        L.iters += F.k;
+        if (F.stop == 9 && F.sepMax > MIX_SEP_MARGIN * (float)rsum) {
+          // separated: finish as the reference does for a non-touching pair
+          L.touching = false; L.p0 = F.p0; L.p1 = F.p1; L.calls++;
+          fin = true;
+        } else {
+          buildShapes64(SP, d, id1, id2);
+          // continue in FP64 from the FP32 solution, or from the exact FP64 start if the
+          // FP32 search accepted no step
+          if (F.moved) { L.p0 = (double)F.p0; L.p1 = (double)F.p1; }
+          lmStartSolve(L);
+          budget = MIX_EVAL64;
+          fp32 = false;
+        }
+      }
+    } else if (active) {
+      disfunction(SP.d.A, SP.d.B, L.q0, L.q1, L.C, L.P1, L.P2, L.stopFlag);
+      ev64++;
+      bool more = lmConsume(L);
+      if (more && --budget <= 0) { L.stop = 3; more = false; }
+      if (!more) {
+        L.calls++; L.iters += L.k; L.maxit += (L.stop == 3);
+        bool restart = false;
+        if (L.phase == 0) {
+          L.phase = 1;
+          if ((isnan(L.p0) || isnan(L.p1) || 7 == L.stop) && L.touching) restart = true;
+        }
+        if (!restart && L.phase == 1) {
+          L.phase = 3;
+          if (L.touching && 10.0 * nrm(L.P2 - L.P1) > SP.d.A.rmax &&
+              (!isInside(SP.d.A, L.P2 - SP.d.A.pos) || !isInside(SP.d.B, L.P1 - SP.d.B.pos))) {
+            L.phase = 2; restart = true;
+          }
+        } else if (!restart) L.phase = 3;
+        if (restart) {
+          double para[2];
+          centerLine(SP.d.A.pos, SP.d.B.pos + d3(0, 0, 0), para);
+          L.p0 = para[0]; L.p1 = para[1];
+          buildShapes32(SP, d, id1, id2);
+          lmfStart(F, (float)L.p0, (float)L.p1);
+          fp32 = true;
+        } else fin = true;
+      }
+    }
+    if (fin) {
+      // end of the geometry functor, then Ip2 + law
+      const int e = L.e;
+      const unsigned fl = d.A.flags[e];
+      const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
+      GeomOut g;
+      g.lmCalls = L.calls; g.lmIters = L.iters; g.lmStop = 0; g.nanNormal = false;
+      g.isShearNew = L.isNew ? true : (d.A.depth[e] <= 0);
+      g.cp = L.isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
+      g.ang0 = L.p0; g.ang1 = L.p1; g.angSet = true;
+      if (!L.touching) {
+        g.precomputed = false; g.depth = 0; g.isShearNew = true;
+      } else {
+        g.p1 = L.P1; g.p2 = L.P2;
+        if (isnan(L.contact.x)) g.nanNormal = true;
+        g.cp = L.C;
+        g.depth = dot(L.P1 - L.P2, L.contact);
+        D3 cn = L.contact;
+        normalize(cn);
+        const D3 oldNormal = L.isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
+        g.precomputed = true;
+        precomputeD(g, oldNormal, b1, b2, dt, cn, g.isShearNew);
+        g.normal = cn;
+      }
+      cnt.lmCalls += L.calls; cnt.lmIters += L.iters; cnt.lmMax += L.maxit;
+      finishEntry(d, e, fl, L.isNew, id1, b1, b2, g, cnt);
+      active = false;
+    }
+  }
+  flushCounters(d, cnt);
+  for (int o = 16; o > 0; o >>= 1) { ev32 += __shfl_down_sync(0xffffffffu, ev32, o); ev64 += __shfl_down_sync(0xffffffffu, ev64, o); }
+  if (lane == 0) { atomicAdd(&d.S->err[E_EVAL32], ev32); atomicAdd(&d.S->err[E_EVAL64], ev64); }
 }
 
 // contribution of table entry e to body b (b is id1 when asId1)
@@ -1375,7 +1663,7 @@ using namespace sqdem;
 struct sqdem_ctx {
   int device = 0, precision = SQDEM_FP64, useGraph = 1, contactsPerBody = 16, maxCand = 64;
   int numSMs = 152;
-  int lmBlocksPerSM = 4;
+  int lmBlocksPerSM = 4, lmBlocksPerSMmixed = 4;
   cudaStream_t stream = nullptr;
   Dev d;
   bool haveBodies = false, haveMats = false, haveParams = false;
@@ -1476,7 +1764,8 @@ static void enqueueStep(sqdem_ctx* c, bool timed) {
   }
   if (timed) cudaEventRecord(c->ev[1], s);
   k_contacts_pre<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, s>>>(d);
-  k_contacts_lm<<<c->numSMs * c->lmBlocksPerSM, LM_BS, 0, s>>>(d);
+  if (c->precision == SQDEM_MIXED) k_contacts_lm_mixed<<<c->numSMs * c->lmBlocksPerSMmixed, LM_BS, 0, s>>>(d);
+  else k_contacts_lm<<<c->numSMs * c->lmBlocksPerSM, LM_BS, 0, s>>>(d);
   c->launches += 2;
   if (timed) cudaEventRecord(c->ev[2], s);
   if (d.W > 0) { k_wall_forces<<<d.W, 128, 0, s>>>(d); c->launches++; }
@@ -1588,6 +1877,8 @@ sqdem_status sqdem_create(sqdem_ctx** out, const sqdem_config* cfg) {
     int nb = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_contacts_lm, LM_BS, 0));
     c->lmBlocksPerSM = nb > 0 ? nb : 1;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_contacts_lm_mixed, LM_BS, 0));
+    c->lmBlocksPerSMmixed = nb > 0 ? nb : 1;
   }
   for (int i = 0; i < 4; i++) CK(cudaEventCreate(&c->ev[i]));
   std::memset(&c->d, 0, sizeof(Dev));
@@ -1818,6 +2109,7 @@ sqdem_status sqdem_sync(sqdem_ctx* c, sqdem_report* r) {
     r->lm_calls = (long long)e[E_LM_CALLS]; r->lm_iterations = (long long)e[E_LM_ITERS];
     r->lm_maxiter = (long long)e[E_LM_MAX]; r->overflow = (long long)e[E_OVERFLOW];
     r->collider_runs = (long long)e[E_COLLIDER_RUNS]; r->steps = (long long)e[E_STEPS];
+    r->evals_fp32 = (long long)e[E_EVAL32]; r->evals_fp64 = (long long)e[E_EVAL64];
   }
   if (e[E_OVERFLOW]) return fail(c, SQDEM_ERR_CAPACITY, "contact table or candidate buffer overflow; increase contacts_per_body");
   return SQDEM_OK;
@@ -2165,7 +2457,8 @@ sqdem_status sqdem_time_contacts(sqdem_ctx* c, int nrep, double* ms) {
   for (int i = 0; i < nrep; i++) {
     k_reset_queue<<<1, 1, 0, c->stream>>>(d);
     k_contacts_pre<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, c->stream>>>(d);
-    k_contacts_lm<<<c->numSMs * c->lmBlocksPerSM, LM_BS, 0, c->stream>>>(d);
+    if (c->precision == SQDEM_MIXED) k_contacts_lm_mixed<<<c->numSMs * c->lmBlocksPerSMmixed, LM_BS, 0, c->stream>>>(d);
+    else k_contacts_lm<<<c->numSMs * c->lmBlocksPerSM, LM_BS, 0, c->stream>>>(d);
   }
   CK(cudaEventRecord(c->ev[2], c->stream));
   CK(cudaEventSynchronize(c->ev[2]));

@@ -1,0 +1,729 @@
+"""SudoDEM3D-compatible scripting surface for the GPU engines.
+
+A script written for SudoDEM3D's superellipsoid path runs unchanged::
+
+    from sudodem_gb300.sim import *
+    mat = SuperquadricsMat(Kn=1e5, Ks=5e4, frictionAngle=math.atan(0.5), density=2650)
+    O.materials.append(mat)
+    O.bodies.append(utils.wall(0, axis=2, sense=1, material=mat))
+    b = NewSuperquadrics2(1e-3, 1e-3, 1e-3, 0.8, 1.2, mat, True, False)
+    b.state.pos = (0, 0, 2e-3)
+    O.bodies.append(b)
+    O.engines = [ForceResetter(),
+                 InsertionSortCollider([Bo1_Superquadrics_Aabb(), Bo1_Wall_Aabb()], verletDist=2e-4),
+                 InteractionLoop([Ig2_Wall_Superquadrics_SuperquadricsGeom(),
+                                  Ig2_Superquadrics_Superquadrics_SuperquadricsGeom()],
+                                 [Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys()],
+                                 [SuperquadricsLaw()]),
+                 NewtonIntegrator(damping=0.3, gravity=(0, 0, -9.81), isSuperquadrics=1)]
+    O.dt = 1e-6
+    O.run(1000, True)
+
+Classes, attribute names and defaults follow the reference:
+  Omega / O            py/wrapper/sudodemWrapper.cpp:937-987
+  Superquadrics        pkg/dem/Superquadrics.hpp:139-146
+  SuperquadricsMat     pkg/dem/Superquadrics.hpp:247-264
+  Wall                 pkg/common/Wall.hpp:11-13
+  InsertionSortCollider pkg/common/InsertionSortCollider.hpp:212-222
+  NewtonIntegrator     pkg/dem/NewtonIntegrator.hpp:70-89
+  utils.wall           py/utils.py:311-327
+  NewSuperquadrics*    py/_superquadrics_utils.cpp:251-380
+The four engines run as one GPU timestep (libsqdem_gpu.so); PyRunner engines run on the
+host between timesteps.  ``Ip2_FrictMat_FrictMat_FrictPhys`` and
+``Law2_ScGeom_FrictPhys_CundallStrack`` are accepted as aliases of the superquadric
+physics and law (FrictMat.young is read as the normal stiffness Kn and FrictMat.poisson as
+Ks/Kn, the reading the ElastMat docstring gives, pkg/common/ElastMat.hpp:9).
+"""
+import math
+import random as _random
+import types
+
+import numpy as np
+
+from . import _native
+
+__all__ = ["O", "Omega", "utils", "Body", "State", "Superquadrics", "Wall", "SuperquadricsMat", "FrictMat",
+           "ForceResetter", "InsertionSortCollider", "Bo1_Superquadrics_Aabb", "Bo1_Wall_Aabb", "InteractionLoop",
+           "Ig2_Superquadrics_Superquadrics_SuperquadricsGeom", "Ig2_Wall_Superquadrics_SuperquadricsGeom",
+           "Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys", "SuperquadricsLaw",
+           "Ip2_FrictMat_FrictMat_FrictPhys", "Law2_ScGeom_FrictPhys_CundallStrack", "NewtonIntegrator",
+           "PyRunner", "NewSuperquadrics", "NewSuperquadrics2", "NewSuperquadrics_rot", "NewSuperquadrics_rot2",
+           "Vector3", "Quaternion"]
+
+
+def Vector3(x=0.0, y=0.0, z=0.0):
+    return np.array([x, y, z], dtype=np.float64)
+
+
+def Quaternion(w=1.0, x=0.0, y=0.0, z=0.0):
+    """Quaternion stored as (w, x, y, z)."""
+    return np.array([w, x, y, z], dtype=np.float64)
+
+
+class _Attr:
+    """Keyword-attribute base mirroring SUDODEM_CLASS_BASE_DOC_ATTRS (lib/serialization/Serializable.hpp:205-227)."""
+    _defaults = {}
+
+    def __init__(self, **kw):
+        for k, v in self._defaults.items():
+            setattr(self, k, v() if callable(v) else v)
+        for k, v in kw.items():
+            if k not in self._defaults and k != "label":
+                raise AttributeError(f"{type(self).__name__} has no attribute {k!r}")
+            setattr(self, k, v)
+        if not hasattr(self, "label"):
+            self.label = ""
+
+    def __repr__(self):
+        return f"<{type(self).__name__}>"
+
+
+# ----------------------------------------------------------------------------------------------
+# Materials
+class SuperquadricsMat(_Attr):
+    _defaults = {"Kn": 1e8, "Ks": 1e5, "frictionAngle": 0.5, "betan": 0.0, "betas": 0.0, "density": 1000.0,
+                 "IsSplitable": False, "strength": 100.0}
+
+
+class FrictMat(_Attr):
+    """FrictMat read through the alias mapping: young -> Kn, poisson -> Ks/Kn."""
+    _defaults = {"young": 1e9, "poisson": 0.25, "frictionAngle": 0.5, "density": 1000.0}
+
+    def as_superquadrics(self):
+        return SuperquadricsMat(Kn=self.young, Ks=self.young * self.poisson, frictionAngle=self.frictionAngle,
+                                density=self.density)
+
+
+# ----------------------------------------------------------------------------------------------
+# Shapes, state, bodies
+class Superquadrics:
+    """Superellipsoid (rx, ry, rz, eps1, eps2), Superquadrics.hpp:48-166."""
+
+    def __init__(self, rx=1.0, ry=1.0, rz=1.0, eps1=1.0, eps2=1.0, isSphere=False):
+        self.rx, self.ry, self.rz, self.eps1, self.eps2 = float(rx), float(ry), float(rz), float(eps1), float(eps2)
+        self.isSphere = bool(isSphere)
+
+    @property
+    def rxyz(self):
+        return Vector3(self.rx, self.ry, self.rz)
+
+    @property
+    def eps(self):
+        return np.array([self.eps1, self.eps2])
+
+    def _props(self):
+        return _native.shape_props(self.rx, self.ry, self.rz, self.eps1, self.eps2)
+
+    def getVolume(self):
+        return float(self._props()[0])
+
+    def getInertia(self):
+        return self._props()[1:4].copy()
+
+    def getr_max(self):
+        return float(self._props()[4])
+
+
+class Wall:
+    """Axis-aligned plane (Wall.hpp:11-13): sense -1, 0 or +1."""
+
+    def __init__(self, axis=0, sense=0):
+        self.axis, self.sense = int(axis), int(sense)
+
+
+class State:
+    def __init__(self):
+        self.pos = Vector3()
+        self.ori = Quaternion()
+        self.vel = Vector3()
+        self.angVel = Vector3()
+        self.angMom = Vector3()
+        self.mass = 0.0
+        self.inertia = Vector3()
+        self.blockedDOFs = ""
+        self.isDamped = True
+        self.refPos = Vector3()
+
+    def __setattr__(self, k, v):
+        if k in ("pos", "vel", "angVel", "angMom", "inertia", "refPos", "ori"):
+            v = np.array(v, dtype=np.float64)
+        object.__setattr__(self, k, v)
+        sc = getattr(self, "_scene", None)
+        if sc is not None and k != "_scene":
+            sc._hostDirty = True
+
+
+_DOF = {"x": 1, "y": 2, "z": 4, "X": 8, "Y": 16, "Z": 32}
+
+
+def _dof_mask(s):
+    if isinstance(s, (int, np.integer)):
+        return int(s)
+    m = 0
+    for ch in s:
+        m |= _DOF[ch]
+    return m
+
+
+class Body:
+    def __init__(self):
+        self.id = -1
+        self.shape = None
+        self.state = State()
+        self.mat = None
+        self.material = None
+        self.mask = 1
+        self.aspherical = False
+        self.bounded = True
+
+    @property
+    def dynamic(self):
+        return _dof_mask(self.state.blockedDOFs) != 63
+
+    def isStandalone(self):
+        return True
+
+
+# ----------------------------------------------------------------------------------------------
+# Engines and functors (names and attributes of the reference)
+class ForceResetter(_Attr):
+    _defaults = {"dead": False}
+
+
+class Bo1_Superquadrics_Aabb(_Attr):
+    pass
+
+
+class Bo1_Wall_Aabb(_Attr):
+    pass
+
+
+class InsertionSortCollider(_Attr):
+    _defaults = {"verletDist": -0.5, "targetInterv": 50, "minSweepDistFactor": 0.1, "sortAxis": 0,
+                 "doSort": False, "updatingDispFactor": -1.0, "sortThenCollide": False, "dead": False}
+
+    def __init__(self, boundFunctors=None, **kw):
+        super().__init__(**kw)
+        self.boundFunctors = list(boundFunctors or [])
+
+
+class Ig2_Superquadrics_Superquadrics_SuperquadricsGeom(_Attr):
+    # GPU-only attribute: arithmetic form of the narrowphase ('fp64' or 'mixed')
+    _defaults = {"precision": "fp64"}
+
+
+class Ig2_Wall_Superquadrics_SuperquadricsGeom(_Attr):
+    pass
+
+
+class Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys(_Attr):
+    pass
+
+
+class SuperquadricsLaw(_Attr):
+    pass
+
+
+class Ip2_FrictMat_FrictMat_FrictPhys(Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys):
+    """Alias with SuperquadricsPhys arithmetic (see the module docstring)."""
+
+
+class Law2_ScGeom_FrictPhys_CundallStrack(SuperquadricsLaw):
+    """Alias with SuperquadricsLaw arithmetic (see the module docstring)."""
+
+
+class InteractionLoop(_Attr):
+    _defaults = {"dead": False}
+
+    def __init__(self, geoms=None, physs=None, laws=None, **kw):
+        super().__init__(**kw)
+        self.geomDispatcher = list(geoms or [])
+        self.physDispatcher = list(physs or [])
+        self.lawDispatcher = list(laws or [])
+
+
+class NewtonIntegrator(_Attr):
+    _defaults = {"damping": 0.2, "gravity": (0.0, 0.0, 0.0), "isSuperquadrics": 0, "exactAsphericalRot": True,
+                 "dead": False, "maxVelocitySq": float("nan")}
+
+
+class PyRunner(_Attr):
+    """Python command executed every iterPeriod steps (on the host, between timesteps)."""
+    _defaults = {"command": "", "iterPeriod": 1, "initRun": False, "dead": False}
+
+    def __init__(self, command="", iterPeriod=1, **kw):
+        super().__init__(command=command, iterPeriod=iterPeriod, **kw)
+        self.iterLast = 0
+
+
+# ----------------------------------------------------------------------------------------------
+# Containers
+class BodyContainer:
+    def __init__(self, scene):
+        self._scene = scene
+        self._b = []
+
+    def append(self, b):
+        if isinstance(b, (list, tuple)):
+            return [self.append(x) for x in b]
+        b.id = len(self._b)
+        b.state._scene = self._scene
+        self._b.append(b)
+        self._scene._structDirty = True
+        return b.id
+
+    def __getitem__(self, i):
+        self._scene._pull()
+        return self._b[i]
+
+    def __len__(self):
+        return len(self._b)
+
+    def __iter__(self):
+        self._scene._pull()
+        return iter(self._b)
+
+    def clear(self):
+        self._b = []
+        self._scene._structDirty = True
+
+
+class MaterialContainer(list):
+    def append(self, m):
+        super().append(m)
+        return len(self) - 1
+
+    def __getitem__(self, k):
+        if isinstance(k, str):
+            for m in self:
+                if m.label == k:
+                    return m
+            raise KeyError(k)
+        return super().__getitem__(k)
+
+
+class _Geom:
+    pass
+
+
+class _Phys:
+    pass
+
+
+class Interaction:
+    def __init__(self, rec):
+        self.id1, self.id2 = int(rec[0]), int(rec[1])
+        self._real = bool(rec[2])
+        g = _Geom()
+        g.penetrationDepth = g.PenetrationDepth = rec[4]
+        g.contactAngle = rec[5:7].copy()
+        g.contactPoint = rec[7:10].copy()
+        g.normal = rec[10:13].copy()
+        g.shearInc = rec[13:16].copy()
+        g.point1, g.point2 = rec[16:19].copy(), rec[19:22].copy()
+        g.isShearNew = bool(rec[22])
+        p = _Phys()
+        p.kn, p.ks, p.tangensOfFrictionAngle = rec[23], rec[24], rec[25]
+        p.normalForce, p.shearForce = rec[26:29].copy(), rec[29:32].copy()
+        self.geom = g if bool(rec[3]) else None
+        self.phys = p if self._real else None
+
+    def isReal(self):
+        return self._real
+
+
+class InteractionContainer:
+    def __init__(self, scene):
+        self._scene = scene
+
+    def _recs(self):
+        s = self._scene
+        if s._engine is None:
+            return np.zeros((0, _native.INTR_STRIDE))
+        return s._engine.interactions(True)
+
+    def __iter__(self):
+        for r in self._recs():
+            if r[2]:
+                yield Interaction(r)
+
+    def all(self):
+        return [Interaction(r) for r in self._recs()]
+
+    def __len__(self):
+        return len(self._recs())
+
+    def countReal(self):
+        return int(np.sum(self._recs()[:, 2] != 0))
+
+    def __getitem__(self, ids):
+        a, b = ids
+        for r in self._recs():
+            if {int(r[0]), int(r[1])} == {a, b}:
+                return Interaction(r)
+        raise IndexError(f"no interaction {a}+{b}")
+
+
+class ForceContainer:
+    def __init__(self, scene):
+        self._scene = scene
+
+    def f(self, i):
+        self._scene._pull()
+        return self._scene._state[i, 16:19].copy()
+
+    def t(self, i):
+        self._scene._pull()
+        return self._scene._state[i, 19:22].copy()
+
+
+# ----------------------------------------------------------------------------------------------
+class Omega:
+    """The scene and its timestep loop (core/Omega.cpp, core/Scene.cpp:70-138)."""
+
+    def __init__(self, device=0):
+        self.device = device
+        self.reset()
+
+    def reset(self):
+        self.bodies = BodyContainer(self)
+        self.materials = MaterialContainer()
+        self.interactions = InteractionContainer(self)
+        self.forces = ForceContainer(self)
+        self._engines = []
+        self.dt = 1e-8
+        self._engine = None
+        self._structDirty = True
+        self._hostDirty = False
+        self._state = None
+        self._pulled = True
+        self._iter0 = 0
+        self.tags = {}
+
+    # engines -------------------------------------------------------------------------------
+    @property
+    def engines(self):
+        return self._engines
+
+    @engines.setter
+    def engines(self, e):
+        self._engines = list(e)
+        self._structDirty = True
+
+    def _parse_engines(self):
+        col = ilp = newton = None
+        runners = []
+        for e in self._engines:
+            if isinstance(e, ForceResetter):
+                continue
+            if isinstance(e, InsertionSortCollider):
+                col = e
+            elif isinstance(e, InteractionLoop):
+                ilp = e
+            elif isinstance(e, NewtonIntegrator):
+                newton = e
+            elif isinstance(e, PyRunner):
+                runners.append(e)
+            else:
+                raise NotImplementedError(f"engine {type(e).__name__} is not available on the GPU path")
+        if col is None or ilp is None or newton is None:
+            raise RuntimeError("O.engines must contain InsertionSortCollider, InteractionLoop and NewtonIntegrator")
+        for g in ilp.geomDispatcher:
+            if not isinstance(g, (Ig2_Superquadrics_Superquadrics_SuperquadricsGeom,
+                                  Ig2_Wall_Superquadrics_SuperquadricsGeom)):
+                raise NotImplementedError(f"geometry functor {type(g).__name__} is not available on the GPU path")
+        for p in ilp.physDispatcher:
+            if not isinstance(p, Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys):
+                raise NotImplementedError(f"physics functor {type(p).__name__} is not available on the GPU path")
+        for lw in ilp.lawDispatcher:
+            if not isinstance(lw, SuperquadricsLaw):
+                raise NotImplementedError(f"law functor {type(lw).__name__} is not available on the GPU path")
+        return col, ilp, newton, runners
+
+    # state exchange --------------------------------------------------------------------------
+    def _material_table(self):
+        mats, index = [], {}
+        for b in self.bodies._b:
+            m = b.mat if b.mat is not None else b.material
+            if m is None:
+                if not self.materials:
+                    self.materials.append(SuperquadricsMat())
+                m = self.materials[-1]
+            if isinstance(m, int):
+                m = self.materials[m]
+            if isinstance(m, str):
+                m = self.materials[m]
+            if isinstance(m, FrictMat):
+                key = id(m)
+                if key not in index:
+                    index[key] = len(mats)
+                    mats.append(m.as_superquadrics())
+                b._matIdx = index[key]
+                continue
+            if id(m) not in index:
+                index[id(m)] = len(mats)
+                mats.append(m)
+            b._matIdx = index[id(m)]
+        return mats
+
+    def _body_arrays(self):
+        n = len(self.bodies._b)
+        kind = np.zeros(n, np.int32)
+        shape5 = np.zeros((n, 5))
+        was = np.zeros((n, 2), np.int32)
+        mat = np.zeros(n, np.int32)
+        sph = np.zeros(n, np.int32)
+        st = np.zeros((n, _native.BODY_STRIDE))
+        blocked = np.zeros(n, np.int32)
+        for i, b in enumerate(self.bodies._b):
+            s = b.state
+            mat[i] = b._matIdx
+            if isinstance(b.shape, Wall):
+                kind[i] = 1
+                was[i] = (b.shape.axis, b.shape.sense)
+            elif isinstance(b.shape, Superquadrics):
+                kind[i] = 0
+                shape5[i] = (b.shape.rx, b.shape.ry, b.shape.rz, b.shape.eps1, b.shape.eps2)
+                sph[i] = int(b.shape.isSphere)
+            else:
+                raise NotImplementedError(f"shape {type(b.shape).__name__} is not available on the GPU path")
+            st[i, 0:3] = s.pos
+            st[i, 3:7] = s.ori
+            st[i, 7:10] = s.vel
+            st[i, 10:13] = s.angVel
+            st[i, 13:16] = s.angMom
+            st[i, 28:31] = np.nan
+            st[i, 33] = s.mass
+            st[i, 34:37] = s.inertia
+            blocked[i] = _dof_mask(s.blockedDOFs)
+        return kind, shape5, was, mat, sph, st, blocked
+
+    def _build(self):
+        col, ilp, newton, runners = self._parse_engines()
+        prec = "fp64"
+        for g in ilp.geomDispatcher:
+            if isinstance(g, Ig2_Superquadrics_Superquadrics_SuperquadricsGeom):
+                prec = g.precision
+        mats = self._material_table()
+        kind, shape5, was, mat, sph, st, blocked = self._body_arrays()
+        for i, b in enumerate(self.bodies._b):
+            want = 63 if kind[i] == 1 else 0
+            if blocked[i] != want:
+                raise NotImplementedError("blockedDOFs other than the defaults (walls fixed, particles free) "
+                                          "are not exposed through this surface yet")
+        eng = _native.Engine(device=self.device, precision=prec)
+        eng.set_materials([m.Kn for m in mats], [m.Ks for m in mats], [m.frictionAngle for m in mats],
+                          [m.betan for m in mats], [m.betas for m in mats], [m.density for m in mats])
+        self._set_params(eng, col, newton)
+        eng.set_bodies(kind, shape5, was, mat, sph, st)
+        self._engine = eng
+        self._parts = (col, ilp, newton, runners)
+        self._structDirty = False
+        self._hostDirty = False
+        self._pulled = False
+
+    def _set_params(self, eng, col, newton):
+        eng.set_params(dt=self.dt, gravity=tuple(float(x) for x in newton.gravity), damping=newton.damping,
+                       verletDist=col.verletDist, targetInterv=col.targetInterv,
+                       minSweepDistFactor=col.minSweepDistFactor, sortAxis=col.sortAxis,
+                       isSuperquadrics=newton.isSuperquadrics if newton.isSuperquadrics else 1,
+                       exactAsphericalRot=int(newton.exactAsphericalRot))
+        self._paramsKey = self._params_key(col, newton)
+
+    def _params_key(self, col, newton):
+        return (self.dt, tuple(newton.gravity), newton.damping, col.verletDist, col.targetInterv,
+                col.minSweepDistFactor, col.sortAxis, newton.exactAsphericalRot)
+
+    def _push(self):
+        """Upload host-side modifications of body states."""
+        st = self._engine.body_state()
+        for i, b in enumerate(self.bodies._b):
+            s = b.state
+            st[i, 0:3] = s.pos
+            st[i, 3:7] = s.ori
+            st[i, 7:10] = s.vel
+            st[i, 10:13] = s.angVel
+            st[i, 13:16] = s.angMom
+        self._engine.put_body_state(st)
+        self._hostDirty = False
+
+    def _pull(self):
+        """Copy the GPU state into the Python body objects (after a run)."""
+        if self._engine is None or self._pulled:
+            return
+        st = self._engine.body_state()
+        self._state = st
+        for i, b in enumerate(self.bodies._b):
+            s = b.state
+            d = s.__dict__
+            d["pos"], d["ori"], d["vel"] = st[i, 0:3].copy(), st[i, 3:7].copy(), st[i, 7:10].copy()
+            d["angVel"], d["angMom"] = st[i, 10:13].copy(), st[i, 13:16].copy()
+        self._pulled = True
+
+    # running ---------------------------------------------------------------------------------
+    @property
+    def iter(self):
+        if self._engine is None:
+            return self._iter0
+        return int(self._engine.scalars()[0])
+
+    @property
+    def time(self):
+        return self.iter * self.dt
+
+    def _prepare(self):
+        if self._structDirty or self._engine is None:
+            self._build()
+        elif self._hostDirty:
+            self._pull()
+            self._push()
+        col, ilp, newton, runners = self._parts
+        if self._params_key(col, newton) != self._paramsKey:
+            self._set_params(self._engine, col, newton)
+
+    def step(self):
+        self.run(1, True)
+
+    def run(self, nSteps=1, wait=True):
+        """Advance nSteps timesteps (PyRunner commands run between steps on the host)."""
+        self._prepare()
+        col, ilp, newton, runners = self._parts
+        runners = [r for r in runners if not r.dead]
+        done = 0
+        while done < nSteps:
+            it = self.iter
+            chunk = nSteps - done
+            for r in runners:
+                nxt = r.iterPeriod - (it % r.iterPeriod) if r.iterPeriod > 0 else chunk
+                chunk = min(chunk, max(1, nxt))
+            self._engine.step(chunk)
+            done += chunk
+            self._pulled = False
+            if runners:
+                self._engine.sync()
+                it = self.iter
+                for r in runners:
+                    if r.iterPeriod > 0 and it % r.iterPeriod == 0:
+                        import __main__
+                        exec(r.command, __main__.__dict__)
+                        r.iterLast = it
+                if self._structDirty or self._hostDirty:
+                    self._prepare()
+        if wait:
+            self.report = self._engine.sync()
+
+    def wait(self):
+        if self._engine is not None:
+            self.report = self._engine.sync()
+
+
+O = Omega()
+
+
+# ----------------------------------------------------------------------------------------------
+# Body factories
+def _common_body(b, mat):
+    b.mat = mat
+    b.material = mat
+    return b
+
+
+def _mat_obj(mat):
+    if isinstance(mat, int):
+        return O.materials[mat]
+    if isinstance(mat, str):
+        return O.materials[mat]
+    if mat is None:
+        if not O.materials:
+            O.materials.append(SuperquadricsMat())
+        return O.materials[-1]
+    return mat
+
+
+def _density(m):
+    return m.density
+
+
+def NewSuperquadrics_rot2(x, y, z, ep1, ep2, mat, q0, q1, q2, q3, isSphere=False):
+    """Superquadric body with a given orientation quaternion (py/_superquadrics_utils.cpp:354-380)."""
+    m = _mat_obj(mat)
+    b = _common_body(Body(), m)
+    b.shape = Superquadrics(x, y, z, ep1, ep2, isSphere)
+    props = b.shape._props()
+    b.state.mass = _density(m) * props[0]
+    b.state.inertia = props[1:4] * _density(m)
+    b.aspherical = True
+    q = np.array([q0, q1, q2, q3], dtype=np.float64)
+    w, xx, yy, zz = q
+    n = math.sqrt((xx * xx + yy * yy) + (zz * zz + w * w))
+    b.state.ori = q / n
+    return b
+
+
+def NewSuperquadrics_rot(x, y, z, ep1, ep2, mat, q0, q1, q2, q3):
+    return NewSuperquadrics_rot2(x, y, z, ep1, ep2, mat, q0, q1, q2, q3, False)
+
+
+def NewSuperquadrics2(x, y, z, ep1, ep2, mat, rotate=False, isSphere=False):
+    """Superquadric body (py/_superquadrics_utils.cpp:289-325).  With rotate=True the
+    orientation is normalize(Identity + q(heading, attitude, bank)) for three uniform random
+    Euler angles, as the reference does; Python's seeded ``random`` replaces C rand()."""
+    if rotate:
+        h, a, bk = (_random.random() * 2.0 * math.pi for _ in range(3))
+        c1, s1 = math.cos(h / 2), math.sin(h / 2)
+        c2, s2 = math.cos(a / 2), math.sin(a / 2)
+        c3, s3 = math.cos(bk / 2), math.sin(bk / 2)
+        c1c2, s1s2 = c1 * c2, s1 * s2
+        w = c1c2 * c3 - s1s2 * s3
+        qx = c1c2 * s3 + s1s2 * c3
+        qy = s1 * c2 * c3 + c1 * s2 * s3
+        qz = c1 * s2 * c3 - s1 * c2 * s3
+        return NewSuperquadrics_rot2(x, y, z, ep1, ep2, mat, 1.0 + w, qx, qy, qz, isSphere)
+    return NewSuperquadrics_rot2(x, y, z, ep1, ep2, mat, 1.0, 0.0, 0.0, 0.0, isSphere)
+
+
+def NewSuperquadrics(x, y, z, ep1, ep2, mat, rotate=False):
+    return NewSuperquadrics2(x, y, z, ep1, ep2, mat, rotate, False)
+
+
+def _wall(position, axis, sense=0, color=None, material=-1, mask=1):
+    """Fixed axis-aligned wall body (py/utils.py:311-327)."""
+    b = Body()
+    b.shape = Wall(axis=axis, sense=sense)
+    if isinstance(position, (int, float)):
+        p = Vector3()
+        p[axis] = position
+    else:
+        p = np.array(position, dtype=np.float64)
+    if isinstance(material, int) and material < 0:
+        if not O.materials:
+            O.materials.append(SuperquadricsMat())
+        m = O.materials[material]
+    else:
+        m = _mat_obj(material)
+    _common_body(b, m)
+    b.state.pos = p
+    b.state.refPos = p
+    b.state.blockedDOFs = "xyzXYZ"
+    b.aspherical = False
+    b.mask = mask
+    return b
+
+
+def _avgNumInteractions(cutoff=0.0, skipFree=False, considerClumps=False):
+    """Average number of real touching interactions per particle (cf. py/utils.py:498)."""
+    recs = O.interactions._recs()
+    parts = [b.id for b in O.bodies._b if isinstance(b.shape, Superquadrics)]
+    touch = recs[(recs[:, 2] != 0) & (recs[:, 4] > 0)]
+    cnt = {i: 0 for i in parts}
+    for r in touch:
+        for k in (int(r[0]), int(r[1])):
+            if k in cnt:
+                cnt[k] += 1
+    vals = list(cnt.values())
+    if skipFree:
+        vals = [v for v in vals if v > 0]
+    return 2.0 * len(touch) / max(len(parts), 1) if not skipFree else (sum(vals) / max(len(vals), 1))
+
+
+utils = types.SimpleNamespace(wall=_wall, avgNumInteractions=_avgNumInteractions)
