@@ -37,6 +37,12 @@ def workload_spec(name, seed):
         # 200,000 superellipsoids with the size distribution of the plain-vs-mixed config
         # (half-axes U[0.8,1.2] mm, eps1/eps2 U[0.3,1.8]) deposited in a walled box.
         return assemblies.deposition_box(200_000, seed=seed, eps_range=(0.3, 1.8))
+    if name == "config1":
+        # 200,000 superellipsoids, half-axes U[0.8,1.2] mm, eps U[0.3,1.8], periodic cell at
+        # solid fraction 0.3 under isotropic strain-controlled compression (velGrad = -1/s I)
+        return assemblies.config1(seed=seed)
+    if name.startswith("config1_n"):
+        return assemblies.periodic_cell(int(name[9:]), seed=seed)
     if name == "sq200k_dense":
         # same particles on a 2.1 mm lattice: most neighbours start in contact (a compressed state)
         return assemblies.walled_lattice(200_000, seed=seed, box=0.2, per_side=94, spacing=2.1e-3,
@@ -259,7 +265,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="sq200k_walled")
+    ap.add_argument("--workload", default="config1")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--contacts-per-body", type=int, default=16)

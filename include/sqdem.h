@@ -94,9 +94,9 @@ typedef struct {
 #define SQDEM_BODY_STRIDE 37
 /* pos3 ori4(w,x,y,z) vel3 angVel3 angMom3 force3 torque3 bmin3 bmax3 refPos3
    sweepLength lastUpdateIter mass inertia3 */
-#define SQDEM_INTR_STRIDE 44
+#define SQDEM_INTR_STRIDE 47
 /* id1 id2 isReal hasGeom depth contactAngle2 contactPoint3 normal3 shearInc3 point1_3 point2_3
-   isShearNew kn ks tanphi normalForce3 shearForce3 twist3 orthonormal3 relVn3 relVs3 */
+   isShearNew kn ks tanphi normalForce3 shearForce3 twist3 orthonormal3 relVn3 relVs3 cellDist3 */
 #define SQDEM_SCALARS 9
 /* iter maxVelocitySq fastestBodyMaxDist strideActive newtonFound verletDist numReinit colliderRuns
    sortedBoundsValid (0: the next collider pass is a full sort, InsertionSortCollider.cpp:213-222) */
@@ -157,6 +157,16 @@ sqdem_status sqdem_set_record_full(sqdem_ctx* ctx, int on);
  * context stream; only when the context was created with use_graph == 0):
  * out[0] collider gate+passes, out[1] contacts (narrowphase+law), out[2] integrator+reductions. */
 sqdem_status sqdem_stage_times(sqdem_ctx* ctx, double* out3);
+
+/* Periodic cell (Scene.isPeriodic with core/Cell.hpp): hSize9 row-major, its columns are the cell
+ * base vectors (Cell::setHSize); velGrad9 (may be NULL) is applied at the next integrator pass
+ * (Cell::setVelGrad), homoDeform on.  Positions stay unwrapped; interactions carry cellDist and
+ * shift2 = hSize*cellDist (InteractionLoop.cpp:100-106).  Walls are not supported in a periodic scene.
+ * sqdem_get_cell / sqdem_put_cell: hSize9 velGrad9 prevVelGrad9 size3 prevCellSize3 (33 doubles). */
+sqdem_status sqdem_set_periodic(sqdem_ctx* ctx, const double* hSize9, const double* velGrad9);
+sqdem_status sqdem_set_velgrad(sqdem_ctx* ctx, const double* velGrad9);
+sqdem_status sqdem_get_cell(sqdem_ctx* ctx, double* out33);
+sqdem_status sqdem_put_cell(sqdem_ctx* ctx, const double* in33);
 
 /* Replay the timestep as a CUDA graph (on = 1, default) or launch its kernels one by one with
  * per-stage event timing readable through sqdem_stage_times (on = 0). */

@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libsqdem_oracle.so")
 BODY_STRIDE = 37
-INTR_STRIDE = 44
+INTR_STRIDE = 47
 
 _lib = None
 
@@ -48,6 +48,8 @@ def lib():
         "sqo_rebuild_sorted_bounds": (None, [v]),
         "sqo_pair_geom": (i, [v, i, i, i, dp, dp]),
         "sqo_eval_hist": (None, [v, C.POINTER(l)]),
+        "sqo_set_periodic": (None, [v, dp, dp]), "sqo_set_velgrad": (None, [v, dp]),
+        "sqo_get_cell": (None, [v, dp]), "sqo_set_cell": (None, [v, dp]),
         "sqo_shape_props": (None, [d, d, d, d, d, dp]),
         "sqo_surface": (None, [d, d, d, d, d, d, d, dp]),
         "sqo_normal": (None, [d, d, d, d, d, d, d, dp]),
@@ -132,12 +134,32 @@ class OracleScene:
         o.L.sqo_set_params(o.h, p["dt"], _dp(g), p["damping"], p["verletDist"], int(p["targetInterv"]),
                            p["minSweepDistFactor"], int(p["sortAxis"]))
         o.n = spec.n_bodies
+        if spec.info.get("periodic"):
+            o.set_periodic(spec.info["hSize"], spec.info.get("velGrad"))
         # velocities from the spec (the factory leaves them zero)
         if np.any(spec.state[:, 7:16] != 0):
             b = o.bodies()
             b[:, 7:16] = spec.state[:, 7:16]
             o.set_bodies(b)
         return o
+
+    def set_periodic(self, hSize, velGrad=None):
+        h = np.ascontiguousarray(hSize, dtype=np.float64).reshape(9)
+        vg = None if velGrad is None else np.ascontiguousarray(velGrad, dtype=np.float64).reshape(9)
+        self.L.sqo_set_periodic(self.h, _dp(h), _dp(vg) if vg is not None else None)
+
+    def set_velgrad(self, velGrad):
+        vg = np.ascontiguousarray(velGrad, dtype=np.float64).reshape(9)
+        self.L.sqo_set_velgrad(self.h, _dp(vg))
+
+    def cell(self):
+        out = np.zeros(33)
+        self.L.sqo_get_cell(self.h, _dp(out))
+        return out
+
+    def put_cell(self, c):
+        c = np.ascontiguousarray(c, dtype=np.float64).reshape(33)
+        self.L.sqo_set_cell(self.h, _dp(c))
 
     def step(self, n=1):
         self.L.sqo_step(self.h, int(n))

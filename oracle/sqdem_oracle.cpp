@@ -73,6 +73,14 @@ static inline V3 mul(const M3& M, const V3& x) {
             M.m[3] * x[0] + (M.m[4] * x[1] + M.m[5] * x[2]),
             M.m[6] * x[0] + (M.m[7] * x[1] + M.m[8] * x[2]));
 }
+static inline M3 mmul(const M3& A, const M3& B) {
+  M3 r;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      r.m[3 * i + j] = A.m[3 * i + 0] * B.m[0 + j] + (A.m[3 * i + 1] * B.m[3 + j] + A.m[3 * i + 2] * B.m[6 + j]);
+  return r;
+}
+static inline bool m3zero(const M3& A) { for (int k = 0; k < 9; k++) if (A.m[k] != 0) return false; return true; }
 struct Quat { Real w, x, y, z; };
 // Geometry/Quaternion.h:536-568
 static inline M3 toRot(const Quat& q) {
@@ -246,6 +254,13 @@ struct Scene {
   std::vector<V3> force, torque;
   Stats stats{};
   std::vector<Stats> tstats;
+  // periodic cell (core/Cell.hpp, Cell.cpp:6-26)
+  bool isPeriodic = false, colliderPeriodic = false, homoDeform = true, velGradChanged = false;
+  M3 hSize{{1, 0, 0, 0, 1, 0, 0, 0, 1}}, trsf{{1, 0, 0, 0, 1, 0, 0, 0, 1}};
+  M3 velGrad{{0, 0, 0, 0, 0, 0, 0, 0, 0}}, nextVelGrad{{0, 0, 0, 0, 0, 0, 0, 0, 0}};
+  M3 prevVelGrad{{0, 0, 0, 0, 0, 0, 0, 0, 0}};   // NewtonIntegrator::prevVelGrad
+  V3 cellSize = V3(1, 1, 1), prevCellSize = V3(NaN, NaN, NaN);
+  long loIdx[3] = {0, 0, 0};
   // user hook between InteractionLoop and NewtonIntegrator (boundary controllers)
   void (*midHook)(void*) = nullptr; void* midHookArg = nullptr;
 };
@@ -292,6 +307,34 @@ static inline void requestErase(Interaction* I) { I->hasGeom = false; I->hasPhys
 static inline bool mayCollide(const Body& a, const Body& b) { return (a.groupMask & b.groupMask) != 0; }
 
 // ---------------------------------------------------------------------------
+// Cell::integrateAndUpdate (core/Cell.cpp:6-26), the parts the hot path reads
+static void cellIntegrate(Scene& S) {
+  M3 inc;
+  for (int k = 0; k < 9; k++) inc.m[k] = S.dt * S.velGrad.m[k];
+  M3 t = mmul(inc, S.trsf);
+  for (int k = 0; k < 9; k++) S.trsf.m[k] += t.m[k];
+  M3 h = mmul(inc, S.hSize);
+  for (int k = 0; k < 9; k++) S.hSize.m[k] += h.m[k];
+  for (int i = 0; i < 3; i++) {
+    V3 base(S.hSize.m[0 + i], S.hSize.m[3 + i], S.hSize.m[6 + i]);
+    S.cellSize[i] = norm(base);
+  }
+}
+static inline V3 cellShift(const Scene& S, const int cd[3]) {
+  return mul(S.hSize, V3((Real)cd[0], (Real)cd[1], (Real)cd[2]));
+}
+// InsertionSortCollider::cellWrap / cellWrapRel (InsertionSortCollider.cpp:404-414)
+static inline Real cellWrap(const Real x, const Real x0, const Real x1, int& period) {
+  Real xNorm = (x - x0) / (x1 - x0);
+  period = (int)std::floor(xNorm);
+  return x0 + (xNorm - period) * (x1 - x0);
+}
+static inline Real cellWrapRel(const Real x, const Real x0, const Real x1) {
+  Real xNorm = (x - x0) / (x1 - x0);
+  return (xNorm - std::floor(xNorm)) * (x1 - x0);
+}
+
+// ---------------------------------------------------------------------------
 // BoundDispatcher::processBody (pkg/common/Dispatching.cpp:30-62) with
 // Bo1_Superquadrics_Aabb::go (Superquadrics.cpp:639-686) and Bo1_Wall_Aabb::go (Wall.cpp:13-21)
 static void processBody(Scene& S, Body& b, Real sweepDist) {
@@ -333,6 +376,61 @@ static inline bool spatialOverlap(const Scene& S, int id1, int id2) {
          (mn[3 * id1 + 2] <= mx[3 * id2 + 2]) && (mx[3 * id1 + 2] >= mn[3 * id2 + 2]);
 }
 
+// InsertionSortCollider::spatialOverlapPeri (InsertionSortCollider.cpp:491-543); bodies wider
+// than half the cell are not supported (the reference throws unless allowBiggerThanPeriod).
+static bool spatialOverlapPeri(const Scene& S, int id1, int id2, int periods[3]) {
+  for (int axis = 0; axis < 3; axis++) {
+    Real dim = S.cellSize[axis];
+    Real m1 = S.minima[3 * id1 + axis], m2 = S.minima[3 * id2 + axis];
+    Real wMn = (cellWrapRel(m1, m2, m2 + dim) < cellWrapRel(m2, m1, m1 + dim)) ? m2 : m1;
+    int pmn1, pmx1, pmn2, pmx2;
+    Real mn1 = cellWrap(m1, wMn, wMn + dim, pmn1), mx1 = cellWrap(S.maxima[3 * id1 + axis], wMn, wMn + dim, pmx1);
+    Real mn2 = cellWrap(m2, wMn, wMn + dim, pmn2), mx2 = cellWrap(S.maxima[3 * id2 + axis], wMn, wMn + dim, pmx2);
+    if ((pmn1 != pmx1) || (pmn2 != pmx2)) { periods[axis] = 0; return false; }
+    periods[axis] = (int)(pmn1 - pmn2);
+    if (!(mn1 <= mx2 && mx1 >= mn2)) return false;
+  }
+  return true;
+}
+// InsertionSortCollider::handleBoundInversionPeri (InsertionSortCollider.cpp:465-475)
+static void handleBoundInversionPeri(Scene& S, int id1, int id2) {
+  int periods[3];
+  bool overlap = spatialOverlapPeri(S, id1, id2, periods);
+  if (overlap && mayCollide(S.bodies[id1], S.bodies[id2]) && !S.byKey.count(pairKey(id1, id2))) {
+    icInsert(S, id1, id2);
+    Interaction* I = S.lin.back();
+    for (int k = 0; k < 3; k++) I->cellDist[k] = periods[k];
+  }
+}
+// InsertionSortCollider::insertionSortPeri (InsertionSortCollider.cpp:416-463)
+static void insertionSortPeri(Scene& S, std::vector<Bounds>& v, int axis, bool doCollide) {
+  long& loIdx = S.loIdx[axis];
+  const long size = (long)v.size();
+  const Real cellDim = S.cellSize[axis];
+  auto norm_ = [size](long i) { if (i < 0) i += size; return i % size; };
+  for (long _i = 0; _i < size; _i++) {
+    const long i = norm_(_i);
+    const long i_1 = norm_(i - 1);
+    if (i == loIdx && v[i].coord < 0) { v[i].period -= 1; v[i].coord += cellDim; loIdx = norm_(loIdx + 1); }
+    const Real iCmpCoord = v[i].coord + (i == loIdx ? cellDim : 0);
+    if (v[i_1].coord <= iCmpCoord) continue;
+    long j = i_1; Bounds vi = v[i]; const bool viHasBB = vi.hasBB;
+    const bool isMin = v[i].isMin;
+    while (v[j].coord > vi.coord + (norm_(j + 1) == loIdx ? cellDim : 0)) {
+      long j1 = norm_(j + 1);
+      Bounds& vNew = v[j1];
+      vNew = v[j];
+      if (j == loIdx && vi.coord < 0) { vi.period -= 1; vi.coord += cellDim; loIdx = norm_(loIdx + 1); }
+      else if (j1 == loIdx) { vNew.period += 1; vNew.coord -= cellDim; loIdx = norm_(loIdx - 1); }
+      if (isMin && !v[j].isMin && (doCollide && viHasBB && v[j].hasBB)) {
+        if (vi.id != vNew.id) handleBoundInversionPeri(S, vi.id, vNew.id);
+      }
+      j = norm_(j - 1);
+    }
+    v[norm_(j + 1)] = vi;
+  }
+}
+
 // InsertionSortCollider::handleBoundInversion (InsertionSortCollider.cpp:22-27)
 static void handleBoundInversion(Scene& S, int id1, int id2) {
   if (spatialOverlap(S, id1, id2) && mayCollide(S.bodies[id1], S.bodies[id2]) && !S.byKey.count(pairKey(id1, id2)))
@@ -370,6 +468,8 @@ static bool colliderIsActivated(Scene& S) {
 // InsertionSortCollider::action, non-periodic (InsertionSortCollider.cpp:191-400)
 static void colliderAction(Scene& S) {
   long nBodies = (long)S.bodies.size();
+  if (S.isPeriodic != S.colliderPeriodic) { for (int i = 0; i < 3; i++) S.BB[i].clear(); S.colliderPeriodic = S.isPeriodic; }
+  const bool periodic = S.colliderPeriodic;
   bool doInitSort = false;
   if (S.doSort) { doInitSort = true; S.doSort = false; }
   if ((long)S.BB[0].size() != 2 * nBodies) {
@@ -396,8 +496,10 @@ static void colliderAction(Scene& S) {
     for (int j = 0; j < 3; j++) {
       Bounds& B = S.BB[j][i];
       const Body& b = S.bodies[B.id];
+      const Real cellDim = S.cellSize[j];
       B.hasBB = b.hasBound;
-      B.coord = b.hasBound ? (B.isMin ? b.bmin[j] : b.bmax[j]) : b.pos[j];
+      B.coord = (b.hasBound ? (B.isMin ? b.bmin[j] : b.bmax[j]) : b.pos[j]) - (periodic ? cellDim * B.period : 0.);
+      if (doInitSort && periodic) B.coord = cellWrap(B.coord, 0, cellDim, B.period);
       if (B.isMin && j == 1 && b.hasBound) {
         for (int k = 0; k < 3; k++) { S.minima[3 * B.id + k] = b.bmin[k]; S.maxima[3 * B.id + k] = b.bmax[k]; }
       }
@@ -406,11 +508,30 @@ static void colliderAction(Scene& S) {
   for (long linPos = 0; linPos < (long)S.lin.size();) {
     Interaction* I = S.lin[linPos];
     bool real = I->hasGeom && I->hasPhys;
-    if (!real && !spatialOverlap(S, I->id1, I->id2)) icEraseAt(S, linPos);
+    int per[3];
+    bool ov = periodic ? spatialOverlapPeri(S, I->id1, I->id2, per) : spatialOverlap(S, I->id1, I->id2);
+    if (!real && !ov) icEraseAt(S, linPos);
     else linPos++;
   }
   if (!doInitSort) {
-    for (int i = 0; i < 3; i++) insertionSort(S, S.BB[i], true);
+    if (!periodic) for (int i = 0; i < 3; i++) insertionSort(S, S.BB[i], true);
+    else for (int i = 0; i < 3; i++) insertionSortPeri(S, S.BB[i], i, true);
+  } else if (periodic) {
+    for (int i = 0; i < 3; i++) { S.loIdx[i] = 0; std::sort(S.BB[i].begin(), S.BB[i].end()); }
+    S.numReinit++;
+    std::vector<Bounds>& V = S.BB[S.sortAxis];
+    const long n2 = 2 * nBodies;
+    for (long i = 0; i < n2; i++) {
+      if (!(V[i].isMin && V[i].hasBB)) continue;
+      const int iid = V[i].id;
+      long cnt = 0;
+      for (long j = (i + 1) % n2; V[j].id != iid; j = (j + 1) % n2) {
+        const int jid = V[j].id;
+        if (!(V[j].isMin && V[j].hasBB)) continue;
+        handleBoundInversionPeri(S, iid, jid);
+        if (cnt++ > 2 * nBodies) break;
+      }
+    }
   } else {
     for (int i = 0; i < 3; i++) std::sort(S.BB[i].begin(), S.BB[i].end());
     S.numReinit++;
@@ -726,6 +847,11 @@ static bool law(Scene& S, Interaction* I, V3* F, V3* T) {
   const Body& B = S.bodies[I->id2];
   Geom& g = I->g; Phys& ph = I->p;
   V3 ab_min = B.bmin, ab_max = B.bmax;
+  if (S.isPeriodic) {
+    V3 sh = cellShift(S, I->cellDist);
+    ab_min = ab_min + sh;
+    ab_max = ab_max + sh;
+  }
   if (A.bmin[0] >= ab_max[0] || ab_min[0] >= A.bmax[0] || A.bmin[1] >= ab_max[1] || ab_min[1] >= A.bmax[1] ||
       A.bmin[2] >= ab_max[2] || ab_min[2] >= A.bmax[2]) {
     ph.normalForce = V3(); ph.shearForce = V3();
@@ -797,6 +923,7 @@ static void interactionLoop(Scene& S) {
     const Body& b1 = S.bodies[I->id1];
     const Body& b2 = S.bodies[I->id2];
     V3 shift2;
+    if (S.isPeriodic) shift2 = cellShift(S, I->cellDist);
     if (b1.kind == KIND_WALL) ig2WallSq(S, I, b1, b2, shift2);
     else ig2SqSq(S, I, b1, b2, shift2, S.tstats[tn]);
     ip2(S, I);
@@ -878,7 +1005,19 @@ static void leapfrogSphericalRotate(Scene& S, Body& b) {
 static void newtonAction(Scene& S) {
   const Real dt = S.dt;
   const long nb = (long)S.bodies.size();
-  S.maxVelocitySq = 0;
+  if (S.velGradChanged || !m3zero(S.nextVelGrad)) {
+    S.velGrad = S.nextVelGrad;
+    S.velGradChanged = false;
+    for (int k = 0; k < 9; k++) S.nextVelGrad.m[k] = 0;
+  }
+  const bool periodic = S.isPeriodic, homoDeform = S.homoDeform;
+  M3 dVelGrad, dtPrevVelGrad;
+  for (int k = 0; k < 9; k++) { dVelGrad.m[k] = S.velGrad.m[k] - S.prevVelGrad.m[k]; dtPrevVelGrad.m[k] = dt * S.prevVelGrad.m[k]; }
+  const M3 prevVelGrad = S.prevVelGrad;
+  const bool sizeDiffers = S.prevCellSize[0] != S.cellSize[0] || S.prevCellSize[1] != S.cellSize[1] || S.prevCellSize[2] != S.cellSize[2];
+  if (periodic && sizeDiffers && !std::isnan(S.prevCellSize[0]))
+    S.maxVelocitySq = sqnorm(S.prevCellSize - S.cellSize) / std::pow(dt, 2);
+  else S.maxVelocitySq = 0;
   std::vector<Real> thrMax(S.nThreads, 0.0);
 #pragma omp parallel for num_threads(S.nThreads)
   for (long id = 0; id < nb; id++) {
@@ -886,12 +1025,14 @@ static void newtonAction(Scene& S) {
     V3 f = S.force[id], m = S.torque[id];
     const bool useAspherical = (S.exactAsphericalRot && b.aspherical && b.blockedDOFs != DOF_ALL);
     const bool isSphere = (b.kind == KIND_SQ) && b.sq.isSphere;
+    const V3 fluctVel = periodic ? b.vel - mul(prevVelGrad, b.pos) : b.vel;
     if (b.blockedDOFs != DOF_ALL) {
       V3 linAccel;
       if (b.blockedDOFs == 0) linAccel = V3(f[0] / b.mass + S.gravity[0], f[1] / b.mass + S.gravity[1], f[2] / b.mass + S.gravity[2]);
       else for (int i = 0; i < 3; i++) if (!(b.blockedDOFs & (1u << i))) linAccel[i] += f[i] / b.mass + S.gravity[i];
       if (b.isDamped)  // cundallDamp2nd (:23-25)
-        for (int i = 0; i < 3; i++) linAccel[i] *= 1 - S.damping * Sign(linAccel[i] * (b.vel[i] + 0.5 * dt * linAccel[i]));
+        for (int i = 0; i < 3; i++) linAccel[i] *= 1 - S.damping * Sign(linAccel[i] * (fluctVel[i] + 0.5 * dt * linAccel[i]));
+      if (periodic && homoDeform) linAccel = linAccel + mul(prevVelGrad, b.vel);
       b.vel = b.vel + dt * linAccel;
       if (!useAspherical) {
         V3 angAccel;
@@ -914,13 +1055,14 @@ static void newtonAction(Scene& S) {
           }
         }
       }
-    }
+    } else if (periodic && homoDeform) b.vel = b.vel + mul(dtPrevVelGrad, b.vel);
     if (!useAspherical) leapfrogSphericalRotate(S, b);
     else if (S.isSuperquadrics) {
       if (!isSphere) leapfrogSqRotate(S, b, m);
       else leapfrogSphericalRotate(S, b);
     }
-    b.pos = b.pos + b.vel * dt;  // leapfrogTranslate (:306-317)
+    if (periodic && homoDeform) b.vel = b.vel + mul(dVelGrad, b.pos);  // leapfrogTranslate (:306-317)
+    b.pos = b.pos + b.vel * dt;
     // saveMaximaDisplacement (:72-85)
     if (b.hasBound) {
       V3 disp = b.pos - b.refPos;
@@ -931,12 +1073,14 @@ static void newtonAction(Scene& S) {
     }
   }
   for (Real t : thrMax) S.maxVelocitySq = std::max(S.maxVelocitySq, t);
+  if (periodic) { S.prevCellSize = S.cellSize; S.prevVelGrad = S.velGrad; }
 }
 
 // Scene::moveToNextTimeStep (core/Scene.cpp:70-138) for
 // O.engines = [ForceResetter, InsertionSortCollider, InteractionLoop, (hook), NewtonIntegrator]
 static void step(Scene& S) {
   S.lastStepCollided = false;
+  if (S.isPeriodic) cellIntegrate(S);
   if (colliderIsActivated(S)) { colliderAction(S); S.lastStepCollided = true; }
   interactionLoop(S);
   if (S.midHook) S.midHook(S.midHookArg);
@@ -1008,6 +1152,35 @@ void sqo_set_params(void* h, double dt, const double* gravity, double damping, d
   S->sortAxis = sortAxis;
 }
 
+// Periodic cell (Cell::setHSize + Cell::setVelGrad semantics): hSize columns are the cell
+// base vectors, velGrad takes effect at the next NewtonIntegrator pass.
+void sqo_set_periodic(void* h, const double* hSize9, const double* velGrad9) {
+  Scene* S = (Scene*)h;
+  S->isPeriodic = true;
+  for (int k = 0; k < 9; k++) S->hSize.m[k] = hSize9[k];
+  S->trsf = M3{{1, 0, 0, 0, 1, 0, 0, 0, 1}};
+  for (int i = 0; i < 3; i++) S->cellSize[i] = norm(V3(S->hSize.m[0 + i], S->hSize.m[3 + i], S->hSize.m[6 + i]));
+  if (velGrad9) { for (int k = 0; k < 9; k++) S->nextVelGrad.m[k] = velGrad9[k]; S->velGradChanged = true; }
+}
+void sqo_set_velgrad(void* h, const double* velGrad9) {
+  Scene* S = (Scene*)h;
+  for (int k = 0; k < 9; k++) S->nextVelGrad.m[k] = velGrad9[k];
+  S->velGradChanged = true;
+}
+// hSize9 velGrad9 prevVelGrad9 size3 prevCellSize3 -> 33 doubles
+void sqo_get_cell(void* h, double* o) {
+  Scene* S = (Scene*)h;
+  for (int k = 0; k < 9; k++) { o[k] = S->hSize.m[k]; o[9 + k] = S->velGrad.m[k]; o[18 + k] = S->prevVelGrad.m[k]; }
+  for (int k = 0; k < 3; k++) { o[27 + k] = S->cellSize[k]; o[30 + k] = S->prevCellSize[k]; }
+}
+void sqo_set_cell(void* h, const double* o) {
+  Scene* S = (Scene*)h;
+  for (int k = 0; k < 9; k++) { S->hSize.m[k] = o[k]; S->velGrad.m[k] = o[9 + k]; S->prevVelGrad.m[k] = o[18 + k]; }
+  for (int k = 0; k < 3; k++) { S->cellSize[k] = o[27 + k]; S->prevCellSize[k] = o[30 + k]; }
+  S->velGradChanged = false;
+  for (int k = 0; k < 9; k++) S->nextVelGrad.m[k] = 0;
+}
+
 void sqo_step(void* h, int n) { Scene* S = (Scene*)h; for (int i = 0; i < n; i++) step(*S); }
 // Run only the collider (if activated) and return whether it ran; for pair-set checks.
 int sqo_collide(void* h) {
@@ -1059,10 +1232,10 @@ void sqo_set_bodies(void* h, const double* in) {
   }
 }
 
-// Interaction records, 44 doubles each:
+// Interaction records, 47 doubles each:
 // id1 id2 real hasGeom depth angle2 contactPoint3 normal3 shearInc3 point1_3 point2_3 isShearNew
-// kn ks tanphi normalForce3 shearForce3 twist3 ortho3 relVn3 relVs3
-enum { INTR_STRIDE = 44 };
+// kn ks tanphi normalForce3 shearForce3 twist3 ortho3 relVn3 relVs3 cellDist3
+enum { INTR_STRIDE = 47 };
 void sqo_get_interactions(void* h, double* out) {
   Scene* S = (Scene*)h;
   for (size_t i = 0; i < S->lin.size(); i++) {
@@ -1080,6 +1253,7 @@ void sqo_get_interactions(void* h, double* out) {
       o[26 + k] = p.normalForce[k]; o[29 + k] = p.shearForce[k]; o[32 + k] = g.twist_axis[k];
       o[35 + k] = g.orthonormal_axis[k]; o[38 + k] = g.relativeVn[k]; o[41 + k] = g.relativeVs[k];
     }
+    for (int k = 0; k < 3; k++) o[44 + k] = I->cellDist[k];
   }
 }
 // Replace the whole interaction container by the given records (same layout); the
@@ -1110,6 +1284,7 @@ void sqo_set_interactions(void* h, long n, const double* in) {
       p.normalForce[k] = o[26 + k]; p.shearForce[k] = o[29 + k]; g.twist_axis[k] = o[32 + k];
       g.orthonormal_axis[k] = o[35 + k]; g.relativeVn[k] = o[38 + k]; g.relativeVs[k] = o[41 + k];
     }
+    for (int k = 0; k < 3; k++) I->cellDist[k] = (int)o[44 + k];
   }
 }
 

@@ -11,7 +11,7 @@ import numpy as np
 from . import build as _build
 
 BODY_STRIDE = 37
-INTR_STRIDE = 44
+INTR_STRIDE = 47
 NSCALARS = 9
 
 SQDEM_SUPERQUADRIC = 0
@@ -91,6 +91,10 @@ def load_library(build_if_missing=True):
         "sqdem_time_e2e": (i, [v, i, v, v, dp]),
         "sqdem_time_contacts": (i, [v, i, dp]),
         "sqdem_set_use_graph": (i, [v, i]),
+        "sqdem_set_periodic": (i, [v, dp, dp]),
+        "sqdem_set_velgrad": (i, [v, dp]),
+        "sqdem_get_cell": (i, [v, dp]),
+        "sqdem_put_cell": (i, [v, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -106,7 +110,8 @@ def exported_symbols():
             "sqdem_get_kinematics", "sqdem_put_kinematics", "sqdem_num_interactions", "sqdem_get_interactions",
             "sqdem_put_interactions", "sqdem_get_scalars", "sqdem_put_scalars", "sqdem_stage_times",
             "sqdem_shape_props", "sqdem_launch_count", "sqdem_set_record_full", "sqdem_time_steps",
-            "sqdem_time_e2e", "sqdem_time_contacts", "sqdem_set_use_graph"]
+            "sqdem_time_e2e", "sqdem_time_contacts", "sqdem_set_use_graph", "sqdem_set_periodic",
+            "sqdem_set_velgrad", "sqdem_get_cell", "sqdem_put_cell"]
 
 
 def _dp(a):
@@ -185,6 +190,8 @@ class Engine:
         self.set_materials(m["Kn"], m["Ks"], m["frictionAngle"], m["betan"], m["betas"], m["density"])
         self.set_params(**spec.params)
         self.set_bodies(spec.kind, spec.shape5, spec.wall_axis_sense, spec.mat, spec.isSphere, spec.state)
+        if spec.info.get("periodic"):
+            self.set_periodic(spec.info["hSize"], spec.info.get("velGrad"))
 
     def set_use_graph(self, on=True):
         self._check(self.lib.sqdem_set_use_graph(self.h, 1 if on else 0))
@@ -261,6 +268,24 @@ class Engine:
     def put_interactions(self, recs):
         recs = np.ascontiguousarray(recs, dtype=np.float64).reshape(-1, INTR_STRIDE)
         self._check(self.lib.sqdem_put_interactions(self.h, len(recs), _dp(recs)))
+
+    def set_periodic(self, hSize, velGrad=None):
+        h = np.ascontiguousarray(hSize, dtype=np.float64).reshape(9)
+        vg = None if velGrad is None else np.ascontiguousarray(velGrad, dtype=np.float64).reshape(9)
+        self._check(self.lib.sqdem_set_periodic(self.h, _dp(h), _dp(vg) if vg is not None else None))
+
+    def set_velgrad(self, velGrad):
+        vg = np.ascontiguousarray(velGrad, dtype=np.float64).reshape(9)
+        self._check(self.lib.sqdem_set_velgrad(self.h, _dp(vg)))
+
+    def cell(self):
+        out = np.zeros(33)
+        self._check(self.lib.sqdem_get_cell(self.h, _dp(out)))
+        return out
+
+    def put_cell(self, c):
+        c = np.ascontiguousarray(c, dtype=np.float64).reshape(33)
+        self._check(self.lib.sqdem_put_cell(self.h, _dp(c)))
 
     def scalars(self):
         out = np.zeros(NSCALARS)

@@ -181,3 +181,43 @@ def pair_scene(shapeA, shapeB, posA, posB, qA, qB, kn=1e5, friction=0.5, walls=T
     params = {"dt": 1e-6, "gravity": (0.0, 0.0, 0.0), "damping": 0.0, "verletDist": 0.0, "targetInterv": 50,
               "minSweepDistFactor": 0.1, "sortAxis": 0, "isSuperquadrics": 1, "exactAsphericalRot": 1}
     return _finish(b, default_material(kn=kn, friction=friction), params, {})
+
+
+def periodic_cell(n_particles, seed=0, solid_fraction=0.3, r_range=(0.8e-3, 1.2e-3), eps_range=(0.3, 1.8),
+                  strain_rate=1.0, damping=0.3, kn=1e5, friction=0.5, verletDist=0.2e-3, dt_factor=0.5):
+    """Particles on a jittered cubic lattice filling a periodic cube at the given solid
+    fraction (the cell side follows from the summed particle volumes), no gravity, and the
+    isotropic strain-controlled compression velGrad = -strain_rate * I.  The returned spec
+    carries ``info['hSize']`` and ``info['velGrad']`` (row-major 3x3)."""
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(r_range[0], r_range[1], size=(n_particles, 3))
+    eps = rng.uniform(eps_range[0], eps_range[1], size=(n_particles, 2))
+    q = random_quaternions(rng, n_particles)
+    vol = np.array([_native.shape_props(*r[p], *eps[p])[0] for p in range(n_particles)])
+    L = (vol.sum() / solid_fraction) ** (1.0 / 3.0)
+    m = int(math.ceil(n_particles ** (1.0 / 3.0)))
+    spacing = L / m
+    jit = rng.uniform(-0.05, 0.05, size=(n_particles, 3)) * spacing
+    b = _builder()
+    density = 2650.0
+    for p in range(n_particles):
+        iz, rem = divmod(p, m * m)
+        iy, ix = divmod(rem, m)
+        pos = (np.array([ix, iy, iz]) + 0.5) * spacing + jit[p]
+        _add_sq(b, r[p], eps[p], q[p], pos, density)
+    mats = default_material(kn=kn, friction=friction, density=density)
+    params = {"dt": 1.0, "gravity": (0.0, 0.0, 0.0), "damping": damping, "verletDist": verletDist,
+              "targetInterv": 50, "minSweepDistFactor": 0.1, "sortAxis": 0, "isSuperquadrics": 1,
+              "exactAsphericalRot": 1}
+    hSize = np.diag([L, L, L]).reshape(9)
+    velGrad = (-strain_rate * np.eye(3)).reshape(9)
+    spec = _finish(b, mats, params, {"periodic": True, "hSize": hSize, "velGrad": velGrad, "cell_side": L,
+                                     "seed": seed})
+    spec.params["dt"] = critical_dt(spec, dt_factor)
+    return spec
+
+
+def config1(seed=0, n=200_000):
+    """200,000 superellipsoids, half-axes U[0.8,1.2] mm, eps1/eps2 U[0.3,1.8], periodic cell at
+    initial solid fraction 0.3, isotropic strain-controlled compression (velGrad = -1.0/s * I)."""
+    return periodic_cell(n, seed=seed)

@@ -70,6 +70,10 @@ struct SceneState {
   int numReinit; long long colliderRuns;
   unsigned long long bbLo[3], bbHi[3];   // order-preserving encodings of the bbox of particle bound centres
   double org[3]; double h; int dim[3]; int nCells;
+  // periodic cell (core/Cell.hpp): hSize and velocity gradients row-major
+  int periodic, homoDeform, velGradChanged;
+  double hSize[9], trsf[9], velGrad[9], nextVelGrad[9], prevVelGrad[9], dVelGrad[9], dtPrevVelGrad[9];
+  double cellSize[3], prevCellSize[3], prevRunCellSize[3], cellTerm;
   unsigned long long err[E_NUM];
 };
 
@@ -79,6 +83,7 @@ struct Table {
   double2* angle; double* depth; double4* normal; double4* shear; double4* nforce;
   double4* phys;          // kn, ks, tanphi, -
   double4* F; double4* cp;
+  int4* cd;               // Interaction::cellDist in (id1, id2) order: shift2 = hSize*cd moves id2
   // full geometry record (written only when Params::recordFull)
   double4* p1; double4* p2; double4* shearInc; double4* twist; double4* ortho; double4* relVn; double4* relVs;
 };
@@ -120,6 +125,45 @@ __device__ __forceinline__ double decOrd(unsigned long long u) {
 __device__ __forceinline__ D3 xyz(double4 v) { return d3(v.x, v.y, v.z); }
 __device__ __forceinline__ double4 dd4(D3 a, double w) { return make_double4(a.x, a.y, a.z, w); }
 __device__ __forceinline__ double comp(double4 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+// 3x3 row-major matrix times vector with the coefficient-product order of Eigen
+__device__ __forceinline__ D3 m3v(const double* M, D3 v) {
+  return d3(M[0] * v.x + (M[1] * v.y + M[2] * v.z), M[3] * v.x + (M[4] * v.y + M[5] * v.z),
+            M[6] * v.x + (M[7] * v.y + M[8] * v.z));
+}
+// shift2 = hSize * cellDist (InteractionLoop.cpp:100-106)
+__device__ __forceinline__ D3 cellShift(const SceneState& S, int4 cd) {
+  if (!S.periodic) return d3(0, 0, 0);
+  return m3v(S.hSize, d3((double)cd.x, (double)cd.y, (double)cd.z));
+}
+// InsertionSortCollider::cellWrap / cellWrapRel (InsertionSortCollider.cpp:404-414)
+__device__ __forceinline__ double cellWrapD(double x, double x0, double x1, int& period) {
+  double xNorm = (x - x0) / (x1 - x0);
+  period = (int)floor(xNorm);
+  return x0 + (xNorm - period) * (x1 - x0);
+}
+__device__ __forceinline__ double cellWrapRelD(double x, double x0, double x1) {
+  double xNorm = (x - x0) / (x1 - x0);
+  return (xNorm - floor(xNorm)) * (x1 - x0);
+}
+// InsertionSortCollider::spatialOverlapPeri (InsertionSortCollider.cpp:491-543) on the bounds
+// of bodies 1 and 2; periods = image of body 2 relative to body 1.
+__device__ __forceinline__ bool overlapPeri(const SceneState& S, double4 mn1v, double4 mx1v, double4 mn2v, double4 mx2v,
+                                            int per[3]) {
+#pragma unroll
+  for (int axis = 0; axis < 3; axis++) {
+    const double dim = S.cellSize[axis];
+    const double m1 = comp(mn1v, axis), m2 = comp(mn2v, axis);
+    const double wMn = (cellWrapRelD(m1, m2, m2 + dim) < cellWrapRelD(m2, m1, m1 + dim)) ? m2 : m1;
+    int pmn1, pmx1, pmn2, pmx2;
+    const double mn1 = cellWrapD(m1, wMn, wMn + dim, pmn1), mx1 = cellWrapD(comp(mx1v, axis), wMn, wMn + dim, pmx1);
+    const double mn2 = cellWrapD(m2, wMn, wMn + dim, pmn2), mx2 = cellWrapD(comp(mx2v, axis), wMn, wMn + dim, pmx2);
+    if ((pmn1 != pmx1) || (pmn2 != pmx2)) { per[axis] = 0; return false; }
+    per[axis] = pmn1 - pmn2;
+    if (!(mn1 <= mx2 && mx1 >= mn2)) return false;
+  }
+  return true;
+}
 
 // ---------------------------------------------------------------------------
 // Exclusive scan over n+1 ints (in[n] treated as 0), three launches, gated.
@@ -188,8 +232,20 @@ __global__ void k_scan_apply(const int* __restrict__ in, int n, const int* __res
 __global__ void k_gate(Dev d) {
   SceneState& S = *d.S;
   if (S.newtonRan) {
-    S.maxVelocitySq = S.maxDispCode == 2 ? 2.0 : (S.maxDispCode == 1 ? 0.5 : 0.0);
+    const double code = S.maxDispCode == 2 ? 2.0 : (S.maxDispCode == 1 ? 0.5 : 0.0);
+    S.maxVelocitySq = fmax_ref(S.cellTerm, code);
     S.maxDispCode = 0; S.newtonRan = 0;
+  }
+  if (S.periodic) {  // Cell::integrateAndUpdate (core/Cell.cpp:6-26), step prologue
+    double inc[9], t[9], h[9];
+    for (int k = 0; k < 9; k++) inc[k] = d.prm->dt * S.velGrad[k];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        t[3 * i + j] = inc[3 * i] * S.trsf[j] + (inc[3 * i + 1] * S.trsf[3 + j] + inc[3 * i + 2] * S.trsf[6 + j]);
+        h[3 * i + j] = inc[3 * i] * S.hSize[j] + (inc[3 * i + 1] * S.hSize[3 + j] + inc[3 * i + 2] * S.hSize[6 + j]);
+      }
+    for (int k = 0; k < 9; k++) { S.trsf[k] += t[k]; S.hSize[k] += h[k]; }
+    for (int i = 0; i < 3; i++) S.cellSize[i] = nrm(d3(S.hSize[i], S.hSize[3 + i], S.hSize[6 + i]));
   }
   int run;
   if (!S.strideActive) run = 1;
@@ -296,6 +352,7 @@ __global__ void k_grid_setup(Dev d) {
     else { lo[k] = decOrd(S.bbLo[k]); hi[k] = decOrd(S.bbHi[k]); }
   }
   if (!any) for (int k = 0; k < 3; k++) { lo[k] = 0; hi[k] = 0; }
+  if (S.periodic) { for (int k = 0; k < 3; k++) { lo[k] = 0; hi[k] = S.cellSize[k]; } }
   for (int k = 0; k < 3; k++)
     if (!isfinite(lo[k]) || !isfinite(hi[k]) || !(hi[k] >= lo[k])) { lo[k] = 0; hi[k] = 0; }
   double h = P.h0;
@@ -313,6 +370,20 @@ __global__ void k_grid_setup(Dev d) {
     h *= 1.25;
   }
   if (cells > d.Gmax) { dim[0] = dim[1] = dim[2] = 1; cells = 1; }
+  if (S.periodic) {
+    // cells tile the periodic box exactly: cell edge = size/dim >= h
+    cells = 1;
+    for (int k = 0; k < 3; k++) {
+      double q = floor(S.cellSize[k] / h);
+      int n = (q >= 1 && q < (double)(1 << 20)) ? (int)q : 1;
+      dim[k] = n; cells *= n;
+    }
+    while (cells > d.Gmax) { for (int k = 0; k < 3; k++) dim[k] = max(1, dim[k] / 2); cells = (long long)dim[0] * dim[1] * dim[2]; }
+    for (int k = 0; k < 3; k++) { S.org[k] = 0; S.dim[k] = dim[k]; }
+    S.h = h;
+    S.nCells = (int)cells;
+    return;
+  }
   for (int k = 0; k < 3; k++) { S.org[k] = lo[k] - h; S.dim[k] = dim[k]; }
   S.h = h;
   S.nCells = (int)cells;
@@ -333,6 +404,27 @@ __device__ __forceinline__ int cellCoord(double c, double org, double h, int dim
   return (int)f;
 }
 
+// periodic: wrapped coordinate (Cell::wrapNum) mapped onto dim cells of the box
+__device__ __forceinline__ int cellCoordPeri(double c, double L, int dim) {
+  double norm = c / L;
+  double w = norm - floor(norm);
+  double f = floor(w * dim);
+  if (!(f >= 0)) return 0;
+  if (f > (double)(dim - 1)) return dim - 1;
+  return (int)f;
+}
+__device__ __forceinline__ void bodyCellCoords(const SceneState& S, double4 mn, double4 mx, int& cx, int& cy, int& cz) {
+  if (S.periodic) {
+    cx = cellCoordPeri(0.5 * (mn.x + mx.x), S.cellSize[0], S.dim[0]);
+    cy = cellCoordPeri(0.5 * (mn.y + mx.y), S.cellSize[1], S.dim[1]);
+    cz = cellCoordPeri(0.5 * (mn.z + mx.z), S.cellSize[2], S.dim[2]);
+  } else {
+    cx = cellCoord(0.5 * (mn.x + mx.x), S.org[0], S.h, S.dim[0]);
+    cy = cellCoord(0.5 * (mn.y + mx.y), S.org[1], S.h, S.dim[1]);
+    cz = cellCoord(0.5 * (mn.z + mx.z), S.org[2], S.h, S.dim[2]);
+  }
+}
+
 __global__ void k_cell_count(Dev d) {
   const SceneState& S = *d.S;
   if (!S.runCollider) return;
@@ -340,9 +432,8 @@ __global__ void k_cell_count(Dev d) {
   if (b >= d.N) return;
   if (d.info[b].x != KIND_SQ) { d.bodyCell[b] = -1; return; }
   double4 mn = d.bmin[b], mx = d.bmax[b];
-  int cx = cellCoord(0.5 * (mn.x + mx.x), S.org[0], S.h, S.dim[0]);
-  int cy = cellCoord(0.5 * (mn.y + mx.y), S.org[1], S.h, S.dim[1]);
-  int cz = cellCoord(0.5 * (mn.z + mx.z), S.org[2], S.h, S.dim[2]);
+  int cx, cy, cz;
+  bodyCellCoords(S, mn, mx, cx, cy, cz);
   int cell = (cz * S.dim[1] + cy) * S.dim[0] + cx;
   d.bodyCell[b] = cell;
   atomicAdd(&d.cellCount[cell], 1);
@@ -371,19 +462,32 @@ __device__ __forceinline__ bool overlapClosed(double4 amn, double4 amx, double4 
 //    bound of one body moved below the upper bound of the other since the previous pass,
 //    the body whose lower bound moved is id1 (InsertionSortCollider.cpp:29-54).
 __device__ __forceinline__ int orientNew(const Dev& d, int i, int j, int initSort, int sortAxis) {
+  const SceneState& S = *d.S;
   double4 imn = d.bmin[i], jmn = d.bmin[j];
+  double4 imx = d.bmax[i], jmx = d.bmax[j];
+  // periodic: compare i with the image of j that overlaps it (shift of j by per * size)
+  double shNow[3] = {0, 0, 0}, shPrev[3] = {0, 0, 0};
+  if (S.periodic) {
+    int per[3];
+    overlapPeri(S, imn, imx, jmn, jmx, per);
+    for (int k = 0; k < 3; k++) {
+      shNow[k] = per[k] * S.cellSize[k];
+      shPrev[k] = per[k] * S.prevRunCellSize[k];
+    }
+  }
   if (initSort) {
-    double a = comp(imn, sortAxis), b = comp(jmn, sortAxis);
+    double a = comp(imn, sortAxis), b = comp(jmn, sortAxis) + shNow[sortAxis];
     if (a < b) return 1;
     if (b < a) return 0;
     return i < j ? 1 : 0;
   }
-  double4 imx = d.bmax[i], jmx = d.bmax[j];
   double4 ipn = d.pmin[i], ipx = d.pmax[i], jpn = d.pmin[j], jpx = d.pmax[j];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    if (comp(jpx, k) < comp(ipn, k) && comp(jmx, k) > comp(imn, k)) return 1;
-    if (comp(ipx, k) < comp(jpn, k) && comp(imx, k) > comp(jmn, k)) return 0;
+    const double jpxk = comp(jpx, k) + shPrev[k], jpnk = comp(jpn, k) + shPrev[k];
+    const double jmxk = comp(jmx, k) + shNow[k], jmnk = comp(jmn, k) + shNow[k];
+    if (jpxk < comp(ipn, k) && jmxk > comp(imn, k)) return 1;
+    if (comp(ipx, k) < jpnk && comp(imx, k) > jmnk) return 0;
   }
   return -1;
 }
@@ -402,21 +506,32 @@ __global__ void k_candidates(Dev d) {
   const double4 imn = d.bmin[i], imx = d.bmax[i];
   int* cand = d.cand + (size_t)i * d.MAXC;
   int n = 0; bool over = false;
-  const int cx = cellCoord(0.5 * (imn.x + imx.x), S.org[0], S.h, S.dim[0]);
-  const int cy = cellCoord(0.5 * (imn.y + imx.y), S.org[1], S.h, S.dim[1]);
-  const int cz = cellCoord(0.5 * (imn.z + imx.z), S.org[2], S.h, S.dim[2]);
+  int cx, cy, cz;
+  bodyCellCoords(S, imn, imx, cx, cy, cz);
+  int seen[27];
+  int nseen = 0;
   for (int dz = -1; dz <= 1; dz++) {
-    int z = cz + dz; if (z < 0 || z >= S.dim[2]) continue;
+    int z = cz + dz;
+    if (S.periodic) z = (z + S.dim[2]) % S.dim[2]; else if (z < 0 || z >= S.dim[2]) continue;
     for (int dy = -1; dy <= 1; dy++) {
-      int y = cy + dy; if (y < 0 || y >= S.dim[1]) continue;
+      int y = cy + dy;
+      if (S.periodic) y = (y + S.dim[1]) % S.dim[1]; else if (y < 0 || y >= S.dim[1]) continue;
       for (int dx = -1; dx <= 1; dx++) {
-        int x = cx + dx; if (x < 0 || x >= S.dim[0]) continue;
+        int x = cx + dx;
+        if (S.periodic) x = (x + S.dim[0]) % S.dim[0]; else if (x < 0 || x >= S.dim[0]) continue;
         int cell = (z * S.dim[1] + y) * S.dim[0] + x;
-        int s = d.cellStart[cell], e = d.cellStart[cell + 1];
-        for (int k = s; k < e; k++) {
+        bool dup = false;
+        for (int q = 0; q < nseen; q++) dup |= (seen[q] == cell);
+        if (dup) continue;
+        seen[nseen++] = cell;
+        int s0 = d.cellStart[cell], e0 = d.cellStart[cell + 1];
+        for (int k = s0; k < e0; k++) {
           int j = d.cellBodies[k];
           if (j <= i) continue;
-          if (overlapClosed(imn, imx, d.bmin[j], d.bmax[j])) {
+          bool ov;
+          if (S.periodic) { int per[3]; ov = overlapPeri(S, imn, imx, d.bmin[j], d.bmax[j], per); }
+          else ov = overlapClosed(imn, imx, d.bmin[j], d.bmax[j]);
+          if (ov) {
             if (n < d.MAXC) cand[n++] = j; else over = true;
           }
         }
@@ -471,7 +586,7 @@ __global__ void k_check_capacity(Dev d) {
 __device__ __forceinline__ void copyEntry(const Table& s, int a, const Table& t, int b, bool full) {
   t.owner[b] = s.owner[a]; t.partner[b] = s.partner[a]; t.flags[b] = s.flags[a];
   t.angle[b] = s.angle[a]; t.depth[b] = s.depth[a]; t.normal[b] = s.normal[a]; t.shear[b] = s.shear[a];
-  t.nforce[b] = s.nforce[a]; t.phys[b] = s.phys[a]; t.F[b] = s.F[a]; t.cp[b] = s.cp[a];
+  t.nforce[b] = s.nforce[a]; t.phys[b] = s.phys[a]; t.F[b] = s.F[a]; t.cp[b] = s.cp[a]; t.cd[b] = s.cd[a];
   if (full) {
     t.p1[b] = s.p1[a]; t.p2[b] = s.p2[a]; t.shearInc[b] = s.shearInc[a]; t.twist[b] = s.twist[a];
     t.ortho[b] = s.ortho[a]; t.relVn[b] = s.relVn[a]; t.relVs[b] = s.relVs[a];
@@ -481,7 +596,7 @@ __device__ __forceinline__ void initEntry(const Table& t, int b, int owner, int 
   const double4 z = make_double4(0, 0, 0, 0);
   t.owner[b] = owner; t.partner[b] = partner; t.flags[b] = F_SHEARNEW | (ownerIsId1 ? F_OWNER_ID1 : 0u);
   t.angle[b] = make_double2(0, 0); t.depth[b] = 0; t.normal[b] = z; t.shear[b] = z; t.nforce[b] = z;
-  t.phys[b] = z; t.F[b] = z; t.cp[b] = z;
+  t.phys[b] = z; t.F[b] = z; t.cp[b] = z; t.cd[b] = make_int4(0, 0, 0, 0);
   if (full) { t.p1[b] = z; t.p2[b] = z; t.shearInc[b] = z; t.twist[b] = z; t.ortho[b] = z; t.relVn[b] = z; t.relVs[b] = z; }
 }
 
@@ -505,7 +620,17 @@ __global__ void k_merge(Dev d) {
     else if (po < pc) {
       if ((d.A.flags[o] & (F_GEOM | F_PHYS)) == (F_GEOM | F_PHYS)) copyEntry(d.A, o, d.B, out++, full);
       o++;
-    } else { initEntry(d.B, out++, i, pc, (raw & 0x80000000) != 0, full); c++; }
+    } else {
+      const bool ownerIsId1 = (raw & 0x80000000) != 0;
+      initEntry(d.B, out, i, pc, ownerIsId1, full);
+      if (S.periodic) {
+        const int a = ownerIsId1 ? i : pc, b = ownerIsId1 ? pc : i;
+        int per[3];
+        overlapPeri(S, d.bmin[a], d.bmax[a], d.bmin[b], d.bmax[b], per);
+        d.B.cd[out] = make_int4(per[0], per[1], per[2], 0);
+      }
+      out++; c++;
+    }
   }
 }
 
@@ -526,6 +651,7 @@ __global__ void k_commit(Dev d) {
   if (!S.runCollider) return;
   if (!S.overflowRun) S.P = S.Pnew;
   S.bbInit = 1;
+  for (int k = 0; k < 3; k++) S.prevRunCellSize[k] = S.cellSize[k];
   if (S.initSort) S.numReinit++;
   S.colliderRuns++;
   S.err[E_COLLIDER_RUNS]++;
@@ -623,7 +749,7 @@ struct GeomOut {
 
 // SuperquadricsGeom::precompute (Superquadrics.cpp:1030-1050)
 __device__ __forceinline__ void precomputeD(GeomOut& g, const D3& oldNormal, const BodyView& b1, const BodyView& b2,
-                                            double dt, D3 currentNormal, bool isNew) {
+                                            double dt, D3 currentNormal, bool isNew, D3 shift2) {
   if (!isNew) {
     g.ortho = cross(oldNormal, currentNormal);
     double angle = dt * 0.5 * dot(currentNormal, b1.angVel + b2.angVel);
@@ -631,7 +757,7 @@ __device__ __forceinline__ void precomputeD(GeomOut& g, const D3& oldNormal, con
   } else { g.twist = d3(0, 0, 0); g.ortho = d3(0, 0, 0); }
   g.normal = currentNormal;
   D3 c1x = g.cp - b1.pos;
-  D3 c2x = (g.cp - b2.pos) - d3(0, 0, 0);
+  D3 c2x = (g.cp - b2.pos) - shift2;
   D3 relVel = (b2.vel + cross(b2.angVel, c2x)) - (b1.vel + cross(b1.angVel, c1x));
   g.relVn = dot(g.normal, relVel) * g.normal;
   g.relVs = relVel - g.relVn;
@@ -644,85 +770,14 @@ __device__ __forceinline__ void makeShape(SqShape& s, const BodyView& b) {
   s.pos = b.pos;
 }
 
-// Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go (Superquadrics_Ig2.cpp:1880-2317)
-__device__ void geomSqSq(GeomOut& g, bool isNew, double prevDepth, double2 prevAngle, D3 oldNormal, D3 oldCp,
-                         const BodyView& b1, const BodyView& b2, double dt) {
-  g.precomputed = false; g.angSet = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 0; g.nanNormal = false;
-  g.cp = oldCp;
-  D3 position1 = b1.pos;
-  D3 position2 = b2.pos + d3(0, 0, 0);
-  double para[2];
-  if (isNew) { g.isShearNew = true; centerLine(position1, position2, para); }
-  else { g.isShearNew = prevDepth <= 0; para[0] = prevAngle.x; para[1] = prevAngle.y; }
-  D3 contactNormal = d3(0, 0, 0), center = d3(0, 0, 0);
-  double pDepth = 0.0;
-  D3 p1 = d3(0, 0, 0), p2 = d3(0, 0, 0);
-  const bool sphA = b1.info.z != 0, sphB = b2.info.z != 0;
-  const double rmaxA = b1.shpA.w, rmaxB = b2.shpA.w;
-  if (sphA && sphB) {
-    D3 dist = position2 - position1;
-    double r_sum = rmaxA + rmaxB;
-    double depth = r_sum - nrm(dist);
-    if (depth < 1E-18) { g.depth = 0; g.isShearNew = true; return; }
-    normalize(dist);
-    p1 = position1 + rmaxA * dist;
-    p2 = position2 - rmaxB * dist;
-    contactNormal = p1 - p2;
-    normalize(contactNormal);
-    g.p1 = p1; g.p2 = p2;
-    g.cp = 0.5 * (p1 + p2);
-    g.depth = depth;
-  } else {
-    double r_sum = rmaxA + rmaxB;
-    if (nrm(position1 - position2) > r_sum) { g.depth = 0; g.isShearNew = true; return; }
-    SqShape A, B;
-    makeShape(A, b1); makeShape(B, b2);
-    bool touching = true;
-    LMOut info = lmder2(A, B, para, 50, p1, p2, center, touching, contactNormal);
-    g.lmCalls++; g.lmIters += info.iters; if (info.stop == 3) g.lmStop = 3;
-    if (isnan(para[0]) || isnan(para[1]) || 7 == info.stop) {
-      if (touching) {
-        centerLine(position1, position2, para);
-        info = lmder2(A, B, para, 50, p1, p2, center, touching, contactNormal);
-        g.lmCalls++; g.lmIters += info.iters; if (info.stop == 3) g.lmStop = 3;
-      }
-    }
-    pDepth = dot(p1 - p2, contactNormal);
-    if (touching) {
-      if (10.0 * nrm(p2 - p1) > rmaxA) {
-        if (!isInside(A, p2 - position1) || !isInside(B, p1 - position2)) {
-          centerLine(position1, position2, para);
-          info = lmder2(A, B, para, 50, p1, p2, center, touching, contactNormal);
-          g.lmCalls++; g.lmIters += info.iters; if (info.stop == 3) g.lmStop = 3;
-          pDepth = dot(p1 - p2, contactNormal);
-        }
-      }
-    }
-    if (!touching) {
-      g.ang0 = para[0]; g.ang1 = para[1]; g.angSet = true;
-      g.depth = 0; g.isShearNew = true;
-      return;
-    }
-    g.p1 = p1; g.p2 = p2;
-    if (isnan(contactNormal.x)) g.nanNormal = true;
-    g.cp = center;
-    g.depth = pDepth;
-    normalize(contactNormal);
-  }
-  g.precomputed = true;
-  precomputeD(g, oldNormal, b1, b2, dt, contactNormal, g.isShearNew);
-  g.normal = contactNormal;
-  g.ang0 = para[0]; g.ang1 = para[1]; g.angSet = true;
-}
-
 // Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go for the two cases that need no
 // Levenberg-Marquardt search: both bodies flagged as spheres (Superquadrics_Ig2.cpp:1950-1970)
 // and centres farther apart than the bounding radii (:1973-1979).
 __device__ void geomSqSqSimple(GeomOut& g, bool isNew, double prevDepth, D3 oldNormal, D3 oldCp,
-                               const BodyView& b1, const BodyView& b2, double dt) {
+                               const BodyView& b1, const BodyView& b2, double dt, D3 shift2) {
   g.precomputed = false; g.angSet = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 0; g.nanNormal = false;
   g.cp = oldCp;
-  const D3 position1 = b1.pos, position2 = b2.pos + d3(0, 0, 0);
+  const D3 position1 = b1.pos, position2 = b2.pos + shift2;
   double para[2];
   if (isNew) { g.isShearNew = true; centerLine(position1, position2, para); }
   else { g.isShearNew = prevDepth <= 0; para[0] = 0; para[1] = 0; }
@@ -740,7 +795,7 @@ __device__ void geomSqSqSimple(GeomOut& g, bool isNew, double prevDepth, D3 oldN
   g.cp = 0.5 * (p1 + p2);
   g.depth = depth;
   g.precomputed = true;
-  precomputeD(g, oldNormal, b1, b2, dt, contactNormal, g.isShearNew);
+  precomputeD(g, oldNormal, b1, b2, dt, contactNormal, g.isShearNew, shift2);
   g.normal = contactNormal;
   if (isNew) { g.ang0 = para[0]; g.ang1 = para[1]; g.angSet = true; }
 }
@@ -781,7 +836,7 @@ __device__ void geomWallSq(GeomOut& g, bool isNew, double prevDepth, D3 oldNorma
     g.depth = nrm(dd);
   }
   g.precomputed = true;
-  precomputeD(g, oldNormal, w, b, dt, normal, g.isShearNew);
+  precomputeD(g, oldNormal, w, b, dt, normal, g.isShearNew, d3(0, 0, 0));
   g.normal = normal;
 }
 
@@ -904,13 +959,13 @@ __device__ __forceinline__ void entryIds(const Dev& d, int e, unsigned fl, int& 
 // point has a positive gap too, so lmder2 stops at its first check with stop_flag set
 // (Superquadrics_Ig2.cpp:1138-1143): not touching, contactAngle unchanged, depth 0.
 static const float SCREEN_MARGIN = 1e-4f;
-__device__ bool screenSeparated(const BodyView& b1, const BodyView& b2, double pa0, double pa1) {
+__device__ bool screenSeparated(const BodyView& b1, const BodyView& b2, double pa0, double pa1, D3 shift2) {
   if (!isfinite(pa0) || !isfinite(pa1)) return false;
   SqShapeF A, B;
   shapeInitF(A, b1.shpA.x, b1.shpA.y, b1.shpA.z, b1.shpB.x, b1.shpB.y, quatToRot(b1.ori.x, b1.ori.y, b1.ori.z, b1.ori.w),
              d3(0, 0, 0));
   shapeInitF(B, b2.shpA.x, b2.shpA.y, b2.shpA.z, b2.shpB.x, b2.shpB.y, quatToRot(b2.ori.x, b2.ori.y, b2.ori.z, b2.ori.w),
-             b2.pos - b1.pos);
+             (b2.pos + shift2) - b1.pos);
   F3 p1, p2;
   float sep;
   disfunctionF(A, B, (float)pa0, (float)pa1, p1, p2, sep);
@@ -933,9 +988,15 @@ __global__ void __launch_bounds__(128) k_contacts_pre(Dev d) {
       unsigned fl = d.A.flags[e];
       int id1, id2;
       entryIds(d, e, fl, id1, id2);
+      const D3 shift2 = cellShift(S, d.A.cd[e]);
       // SuperquadricsLaw's bound-separation erase (Superquadrics.cpp:1194-1207) discards what
-      // the geometry functor computed, so it is tested first.
-      const double4 amn = d.bmin[id1], amx = d.bmax[id1], bmn = d.bmin[id2], bmx = d.bmax[id2];
+      // the geometry functor computed, so it is tested first (B's bounds shifted by shift2).
+      const double4 amn = d.bmin[id1], amx = d.bmax[id1];
+      double4 bmn = d.bmin[id2], bmx = d.bmax[id2];
+      if (S.periodic) {
+        bmn.x += shift2.x; bmn.y += shift2.y; bmn.z += shift2.z;
+        bmx.x += shift2.x; bmx.y += shift2.y; bmx.z += shift2.z;
+      }
       if (amn.x >= bmx.x || bmn.x >= amx.x || amn.y >= bmx.y || bmn.y >= amx.y || amn.z >= bmx.z || bmn.z >= amx.z) {
         d.A.flags[e] = (fl & ~(F_GEOM | F_PHYS | F_FORCE)) | F_SHEARNEW;
         d.A.nforce[e] = make_double4(0, 0, 0, 0);
@@ -951,17 +1012,17 @@ __global__ void __launch_bounds__(128) k_contacts_pre(Dev d) {
         if (b1.info.x == KIND_WALL) geomWallSq(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt);
         else {
           const bool sph = (b1.info.z != 0) && (b2.info.z != 0);
-          if (!sph && !(nrm(b1.pos - b2.pos) > b1.shpA.w + b2.shpA.w)) {
+          if (!sph && !(nrm(b1.pos - (b2.pos + shift2)) > b1.shpA.w + b2.shpA.w)) {
             double para[2];
-            if (isNew) centerLine(b1.pos, b2.pos + d3(0, 0, 0), para);
+            if (isNew) centerLine(b1.pos, b2.pos + shift2, para);
             else { const double2 an = d.A.angle[e]; para[0] = an.x; para[1] = an.y; }
-            if (screenSeparated(b1, b2, para[0], para[1])) {
+            if (screenSeparated(b1, b2, para[0], para[1], shift2)) {
               g.precomputed = false; g.nanNormal = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 1;
               g.cp = oldCp; g.depth = 0; g.isShearNew = true;
               g.ang0 = para[0]; g.ang1 = para[1]; g.angSet = true;
               cnt.lmCalls++;
             } else done = false;
-          } else geomSqSqSimple(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt);
+          } else geomSqSqSimple(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt, shift2);
         }
         if (done) finishEntry(d, e, fl, isNew, id1, b1, b2, g, cnt);
         else queue = true;
@@ -1119,9 +1180,10 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
           const double4 o1 = d.ori[id1], o2 = d.ori[id2];
           const double4 a1 = d.shpA[id1], a2 = d.shpA[id2], e1 = d.shpB[id1], e2 = d.shpB[id2];
           shapeInit(A, a1.x, a1.y, a1.z, e1.x, e1.y, a1.w); A.R = quatToRot(o1.x, o1.y, o1.z, o1.w); A.pos = xyz(d.pos[id1]);
-          shapeInit(B, a2.x, a2.y, a2.z, e2.x, e2.y, a2.w); B.R = quatToRot(o2.x, o2.y, o2.z, o2.w); B.pos = xyz(d.pos[id2]);
+          shapeInit(B, a2.x, a2.y, a2.z, e2.x, e2.y, a2.w); B.R = quatToRot(o2.x, o2.y, o2.z, o2.w);
+          B.pos = xyz(d.pos[id2]) + cellShift(S, d.A.cd[L.e]);
           L.isNew = !(fl & F_GEOM);
-          if (L.isNew) { double para[2]; centerLine(A.pos, B.pos + d3(0, 0, 0), para); L.p0 = para[0]; L.p1 = para[1]; }
+          if (L.isNew) { double para[2]; centerLine(A.pos, B.pos, para); L.p0 = para[0]; L.p1 = para[1]; }
           else { const double2 an = d.A.angle[L.e]; L.p0 = an.x; L.p1 = an.y; }
           L.contact = d3(0, 0, 0); L.P1 = d3(0, 0, 0); L.P2 = d3(0, 0, 0); L.C = d3(0, 0, 0);
           L.phase = 0; L.calls = 0; L.iters = 0; L.maxit = 0;
@@ -1155,7 +1217,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
         }
         if (restart) {
           double para[2];
-          centerLine(A.pos, B.pos + d3(0, 0, 0), para);
+          centerLine(A.pos, B.pos, para);
           L.p0 = para[0]; L.p1 = para[1];
           lmStartSolve(L);
         } else {
@@ -1182,7 +1244,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
             normalize(cn);
             const D3 oldNormal = L.isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
             g.precomputed = true;
-            precomputeD(g, oldNormal, b1, b2, dt, cn, g.isShearNew);
+            precomputeD(g, oldNormal, b1, b2, dt, cn, g.isShearNew, cellShift(S, d.A.cd[e]));
             g.normal = cn;
           }
           cnt.lmCalls += L.calls; cnt.lmIters += L.iters; cnt.lmMax += L.maxit;
@@ -1310,16 +1372,17 @@ union ShapePair {
   struct { SqShapeF A, B; } f;
 };
 
-__device__ __forceinline__ void buildShapes64(ShapePair& sp, const Dev& d, int id1, int id2) {
+__device__ __forceinline__ void buildShapes64(ShapePair& sp, const Dev& d, int id1, int id2, D3 shift2) {
   const double4 o1 = d.ori[id1], o2 = d.ori[id2];
   const double4 a1 = d.shpA[id1], a2 = d.shpA[id2], e1 = d.shpB[id1], e2 = d.shpB[id2];
   shapeInit(sp.d.A, a1.x, a1.y, a1.z, e1.x, e1.y, a1.w); sp.d.A.R = quatToRot(o1.x, o1.y, o1.z, o1.w); sp.d.A.pos = xyz(d.pos[id1]);
-  shapeInit(sp.d.B, a2.x, a2.y, a2.z, e2.x, e2.y, a2.w); sp.d.B.R = quatToRot(o2.x, o2.y, o2.z, o2.w); sp.d.B.pos = xyz(d.pos[id2]);
+  shapeInit(sp.d.B, a2.x, a2.y, a2.z, e2.x, e2.y, a2.w); sp.d.B.R = quatToRot(o2.x, o2.y, o2.z, o2.w);
+  sp.d.B.pos = xyz(d.pos[id2]) + shift2;
 }
-__device__ __forceinline__ void buildShapes32(ShapePair& sp, const Dev& d, int id1, int id2) {
+__device__ __forceinline__ void buildShapes32(ShapePair& sp, const Dev& d, int id1, int id2, D3 shift2) {
   const double4 o1 = d.ori[id1], o2 = d.ori[id2];
   const double4 a1 = d.shpA[id1], a2 = d.shpA[id2], e1 = d.shpB[id1], e2 = d.shpB[id2];
-  const D3 rel = xyz(d.pos[id2]) - xyz(d.pos[id1]);
+  const D3 rel = (xyz(d.pos[id2]) + shift2) - xyz(d.pos[id1]);
   shapeInitF(sp.f.A, a1.x, a1.y, a1.z, e1.x, e1.y, quatToRot(o1.x, o1.y, o1.z, o1.w), d3(0, 0, 0));
   shapeInitF(sp.f.B, a2.x, a2.y, a2.z, e2.x, e2.y, quatToRot(o2.x, o2.y, o2.z, o2.w), rel);
 }
@@ -1338,6 +1401,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_mixed(Dev d) {
   bool active = false, exhausted = false, fp32 = true;
   int id1 = 0, id2 = 0, budget = 0;
   double rsum = 0;
+  D3 shift2 = d3(0, 0, 0);
   while (true) {
     const unsigned idle = __ballot_sync(0xffffffffu, !active && !exhausted);
     if (idle) {
@@ -1351,16 +1415,17 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_mixed(Dev d) {
           L.e = d.lmQueue[idx];
           const unsigned fl = d.A.flags[L.e];
           entryIds(d, L.e, fl, id1, id2);
+          shift2 = cellShift(S, d.A.cd[L.e]);
           rsum = d.shpA[id1].w + d.shpA[id2].w;
           L.isNew = !(fl & F_GEOM);
           if (L.isNew) {
             double para[2];
-            centerLine(xyz(d.pos[id1]), xyz(d.pos[id2]) + d3(0, 0, 0), para);
+            centerLine(xyz(d.pos[id1]), xyz(d.pos[id2]) + shift2, para);
             L.p0 = para[0]; L.p1 = para[1];
           } else { const double2 an = d.A.angle[L.e]; L.p0 = an.x; L.p1 = an.y; }
           L.contact = d3(0, 0, 0); L.P1 = d3(0, 0, 0); L.P2 = d3(0, 0, 0); L.C = d3(0, 0, 0);
           L.phase = 0; L.calls = 0; L.iters = 0; L.maxit = 0; L.touching = true;
-          buildShapes32(SP, d, id1, id2);
+          buildShapes32(SP, d, id1, id2, shift2);
           lmfStart(F, (float)L.p0, (float)L.p1);
           fp32 = true;
           active = true;
@@ -1381,7 +1446,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_mixed(Dev d) {
           L.touching = false; L.p0 = F.p0; L.p1 = F.p1; L.calls++;
           fin = true;
         } else {
-          buildShapes64(SP, d, id1, id2);
+          buildShapes64(SP, d, id1, id2, shift2);
           // continue in FP64 from the FP32 solution, or from the exact FP64 start if the
           // FP32 search accepted no step
           if (F.moved) { L.p0 = (double)F.p0; L.p1 = (double)F.p1; }
@@ -1411,9 +1476,9 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_mixed(Dev d) {
         } else if (!restart) L.phase = 3;
         if (restart) {
           double para[2];
-          centerLine(SP.d.A.pos, SP.d.B.pos + d3(0, 0, 0), para);
+          centerLine(SP.d.A.pos, SP.d.B.pos, para);
           L.p0 = para[0]; L.p1 = para[1];
-          buildShapes32(SP, d, id1, id2);
+          buildShapes32(SP, d, id1, id2, shift2);
           lmfStart(F, (float)L.p0, (float)L.p1);
           fp32 = true;
         } else fin = true;
@@ -1440,7 +1505,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_mixed(Dev d) {
         normalize(cn);
         const D3 oldNormal = L.isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
         g.precomputed = true;
-        precomputeD(g, oldNormal, b1, b2, dt, cn, g.isShearNew);
+        precomputeD(g, oldNormal, b1, b2, dt, cn, g.isShearNew, shift2);
         g.normal = cn;
       }
       cnt.lmCalls += L.calls; cnt.lmIters += L.iters; cnt.lmMax += L.maxit;
@@ -1566,6 +1631,8 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d) {
     const bool useAspherical = (P.exactAsphericalRot && aspherical && blocked != DOF_ALL);
     const bool isSphere = (inf.x == KIND_SQ) && inf.z != 0;
     const double damping = P.damping;
+    const bool peri = S.periodic != 0, homo = peri && S.homoDeform;
+    const D3 fluctVel = peri ? vel - m3v(S.prevVelGrad, pos) : vel;   // Cell::bodyFluctuationVel
     if (blocked != DOF_ALL) {
       D3 a;
       if (blocked == 0) a = d3(f.x / mass + P.g[0], f.y / mass + P.g[1], f.z / mass + P.g[2]);
@@ -1576,10 +1643,11 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d) {
         if (!(blocked & 4u)) a.z += f.z / mass + P.g[2];
       }
       if (damped) {
-        a.x *= 1 - damping * sgn(a.x * (vel.x + 0.5 * dt * a.x));
-        a.y *= 1 - damping * sgn(a.y * (vel.y + 0.5 * dt * a.y));
-        a.z *= 1 - damping * sgn(a.z * (vel.z + 0.5 * dt * a.z));
+        a.x *= 1 - damping * sgn(a.x * (fluctVel.x + 0.5 * dt * a.x));
+        a.y *= 1 - damping * sgn(a.y * (fluctVel.y + 0.5 * dt * a.y));
+        a.z *= 1 - damping * sgn(a.z * (fluctVel.z + 0.5 * dt * a.z));
       }
+      if (homo) a = a + m3v(S.prevVelGrad, vel);
       vel = vel + dt * a;
       if (!useAspherical || (P.isSuperquadrics && isSphere && damped)) {
         D3 aa;
@@ -1606,7 +1674,7 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d) {
           m.z *= 1 - damping * sgn(m.z * angVel.z);
         }
       }
-    }
+    } else if (homo) vel = vel + m3v(S.dtPrevVelGrad, vel);
     if (!useAspherical || (P.isSuperquadrics && isSphere)) {
       sphericalRotate(ori, angVel, dt);
     } else if (P.isSuperquadrics) {
@@ -1626,6 +1694,7 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d) {
       angVel = qrotate(ori, w_b_h);
       qnormalize(ori);
     }
+    if (homo) vel = vel + m3v(S.dVelGrad, pos);   // leapfrogTranslate (:306-317)
     pos = pos + vel * dt;
     d.pos[b] = dd4(pos, 0);
     d.ori[b] = make_double4(ori.w, ori.x, ori.y, ori.z);
@@ -1647,8 +1716,32 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d) {
 
 __global__ void k_reset_queue(Dev d) { d.S->lmCount = 0; d.S->lmHead = 0; }
 
+// Start of NewtonIntegrator::action (NewtonIntegrator.cpp:107-117): pending velGrad, the
+// cell-size-change velocity that seeds maxVelocitySq, and the gradients the body update uses.
+__global__ void k_newton_begin(Dev d) {
+  SceneState& S = *d.S;
+  if (!S.periodic) { S.cellTerm = 0; return; }
+  bool nz = false;
+  for (int k = 0; k < 9; k++) nz |= (S.nextVelGrad[k] != 0);
+  if (S.velGradChanged || nz) {
+    for (int k = 0; k < 9; k++) { S.velGrad[k] = S.nextVelGrad[k]; S.nextVelGrad[k] = 0; }
+    S.velGradChanged = 0;
+  }
+  const double dt = d.prm->dt;
+  for (int k = 0; k < 9; k++) { S.dVelGrad[k] = S.velGrad[k] - S.prevVelGrad[k]; S.dtPrevVelGrad[k] = dt * S.prevVelGrad[k]; }
+  const bool differs = S.prevCellSize[0] != S.cellSize[0] || S.prevCellSize[1] != S.cellSize[1] || S.prevCellSize[2] != S.cellSize[2];
+  if (differs && !isnan(S.prevCellSize[0])) {
+    const D3 dd = d3(S.prevCellSize[0] - S.cellSize[0], S.prevCellSize[1] - S.cellSize[1], S.prevCellSize[2] - S.cellSize[2]);
+    S.cellTerm = sqn(dd) / (dt * dt);
+  } else S.cellTerm = 0;
+}
+
 __global__ void k_end(Dev d) {
   SceneState& S = *d.S;
+  if (S.periodic) {  // end of NewtonIntegrator::action (:300-302)
+    for (int k = 0; k < 3; k++) S.prevCellSize[k] = S.cellSize[k];
+    for (int k = 0; k < 9; k++) S.prevVelGrad[k] = S.velGrad[k];
+  }
   S.iter++;
   S.time += d.prm->dt;
   S.err[E_STEPS]++;
@@ -1712,7 +1805,7 @@ static sqdem_status allocTable(sqdem_ctx* c, Table& t, int cap) {
   CK(dalloc(c, &t.owner, cap)); CK(dalloc(c, &t.partner, cap)); CK(dalloc(c, &t.flags, cap));
   CK(dalloc(c, &t.angle, cap)); CK(dalloc(c, &t.depth, cap)); CK(dalloc(c, &t.normal, cap));
   CK(dalloc(c, &t.shear, cap)); CK(dalloc(c, &t.nforce, cap)); CK(dalloc(c, &t.phys, cap));
-  CK(dalloc(c, &t.F, cap)); CK(dalloc(c, &t.cp, cap));
+  CK(dalloc(c, &t.F, cap)); CK(dalloc(c, &t.cp, cap)); CK(dalloc(c, &t.cd, cap));
   CK(dalloc(c, &t.p1, cap)); CK(dalloc(c, &t.p2, cap)); CK(dalloc(c, &t.shearInc, cap));
   CK(dalloc(c, &t.twist, cap)); CK(dalloc(c, &t.ortho, cap)); CK(dalloc(c, &t.relVn, cap)); CK(dalloc(c, &t.relVs, cap));
   return SQDEM_OK;
@@ -1769,9 +1862,10 @@ static void enqueueStep(sqdem_ctx* c, bool timed) {
   c->launches += 2;
   if (timed) cudaEventRecord(c->ev[2], s);
   if (d.W > 0) { k_wall_forces<<<d.W, 128, 0, s>>>(d); c->launches++; }
+  k_newton_begin<<<1, 1, 0, s>>>(d);
   k_integrate<<<nblk(N, 256), 256, 0, s>>>(d);
   k_end<<<1, 1, 0, s>>>(d);
-  c->launches += 2;
+  c->launches += 3;
   if (timed) cudaEventRecord(c->ev[3], s);
 }
 
@@ -2230,6 +2324,7 @@ sqdem_status sqdem_get_interactions(sqdem_ctx* c, int include_potential, double*
   const Table& T = c->d.A;
   std::vector<int> ow(P), pa(P); std::vector<unsigned> fl(P); std::vector<double2> an(P); std::vector<double> de(P);
   std::vector<double4> nm(P), sh(P), nf(P), ph(P), cp(P), p1(P), p2(P), si(P), tw(P), orr(P), rn(P), rs(P);
+  std::vector<int4> cdv(P);
   std::vector<int2> ww(S.nWW);
   if (P) {
     CK(cudaMemcpy(ow.data(), T.owner, 4 * (size_t)P, cudaMemcpyDeviceToHost));
@@ -2244,6 +2339,7 @@ sqdem_status sqdem_get_interactions(sqdem_ctx* c, int include_potential, double*
     CK(cudaMemcpy(p2.data(), T.p2, b4, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(si.data(), T.shearInc, b4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(tw.data(), T.twist, b4, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(orr.data(), T.ortho, b4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(rn.data(), T.relVn, b4, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(rs.data(), T.relVs, b4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(cdv.data(), T.cd, sizeof(int4) * (size_t)P, cudaMemcpyDeviceToHost));
   }
   if (S.nWW) CK(cudaMemcpy(ww.data(), c->d.ww, sizeof(int2) * S.nWW, cudaMemcpyDeviceToHost));
   long k = 0;
@@ -2261,6 +2357,7 @@ sqdem_status sqdem_get_interactions(sqdem_ctx* c, int include_potential, double*
       o[22] = (fl[i] & F_SHEARNEW) ? 1 : 0;
       o[23] = ph[i].x; o[24] = ph[i].y; o[25] = ph[i].z;
       put3(o + 26, nf[i]); put3(o + 29, sh[i]); put3(o + 32, tw[i]); put3(o + 35, orr[i]); put3(o + 38, rn[i]); put3(o + 41, rs[i]);
+      o[44] = cdv[i].x; o[45] = cdv[i].y; o[46] = cdv[i].z;   // stored for (id1, id2)
     }
     k++;
   }
@@ -2307,6 +2404,7 @@ sqdem_status sqdem_put_interactions(sqdem_ctx* c, long n, const double* in) {
   std::vector<int> ow(P), pa(P), rowStart(N + 1, 0);
   std::vector<unsigned> fl(P); std::vector<double2> an(P); std::vector<double> de(P);
   std::vector<double4> nm(P), sh(P), nf(P), ph(P), cp(P), p1(P), p2(P), si(P), tw(P), orr(P), rn(P), rs(P), F(P);
+  std::vector<int4> cdv(P);
   auto g3 = [](const double* o) { return make_double4(o[0], o[1], o[2], 0); };
   for (int e = 0; e < P; e++) {
     const double* o = in + (size_t)recs[e].idx * SQDEM_INTR_STRIDE;
@@ -2323,6 +2421,7 @@ sqdem_status sqdem_put_interactions(sqdem_ctx* c, long n, const double* in) {
     ph[e] = make_double4(o[23], o[24], o[25], 0);
     nf[e] = g3(o + 26); sh[e] = g3(o + 29); tw[e] = g3(o + 32); orr[e] = g3(o + 35); rn[e] = g3(o + 38); rs[e] = g3(o + 41);
     F[e] = make_double4(0, 0, 0, 0);
+    cdv[e] = make_int4((int)o[44], (int)o[45], (int)o[46], 0);
   }
   for (int i = 0; i < N; i++) rowStart[i + 1] += rowStart[i];
   // partner incidence lists (ascending entry index) and wall lists
@@ -2349,6 +2448,7 @@ sqdem_status sqdem_put_interactions(sqdem_ctx* c, long n, const double* in) {
   CK(up(T.cp, cp.data(), b4)); CK(up(T.p1, p1.data(), b4)); CK(up(T.p2, p2.data(), b4)); CK(up(T.shearInc, si.data(), b4));
   CK(up(T.twist, tw.data(), b4)); CK(up(T.ortho, orr.data(), b4)); CK(up(T.relVn, rn.data(), b4)); CK(up(T.relVs, rs.data(), b4));
   CK(up(T.F, F.data(), b4));
+  CK(up(T.cd, cdv.data(), sizeof(int4) * (size_t)P));
   CK(up(c->d.rowStart, rowStart.data(), 4 * (size_t)(N + 1)));
   CK(up(c->d.pStart, pStart.data(), 4 * (size_t)(N + 1))); CK(up(c->d.pList, pList.data(), 4 * (size_t)P));
   CK(up(c->d.wCount, wCount.data(), 4 * wCount.size())); CK(up(c->d.wList, wList.data(), 4 * (size_t)P));
@@ -2467,6 +2567,64 @@ sqdem_status sqdem_time_contacts(sqdem_ctx* c, int nrep, double* ms) {
   CK(cudaEventElapsedTime(&t, c->ev[1], c->ev[2]));
   *ms = t / nrep;
   c->launches += 3 * nrep;
+  return SQDEM_OK;
+}
+
+// Periodic cell: Cell::setHSize (columns of hSize9, row-major, are the base vectors) and
+// Cell::setVelGrad (applied at the next NewtonIntegrator pass); walls are not supported in a
+// periodic scene.
+sqdem_status sqdem_set_periodic(sqdem_ctx* c, const double* hSize9, const double* velGrad9) {
+  if (!c || !hSize9) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "set bodies first");
+  if (c->d.W > 0) return fail(c, SQDEM_ERR_ARG, "walls are not supported in a periodic scene");
+  CK(cudaSetDevice(c->device));
+  SceneState S; sqdem_status st = readScene(c, S); if (st) return st;
+  S.periodic = 1; S.homoDeform = 1;
+  double t[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  for (int k = 0; k < 9; k++) { S.hSize[k] = hSize9[k]; S.trsf[k] = t[k]; }
+  for (int i = 0; i < 3; i++) {
+    const double a = hSize9[i], b = hSize9[3 + i], cc = hSize9[6 + i];
+    S.cellSize[i] = std::sqrt(a * a + (b * b + cc * cc));
+    S.prevRunCellSize[i] = S.cellSize[i];
+    S.prevCellSize[i] = std::numeric_limits<double>::quiet_NaN();
+  }
+  if (velGrad9) { for (int k = 0; k < 9; k++) S.nextVelGrad[k] = velGrad9[k]; S.velGradChanged = 1; }
+  S.bbInit = 0;
+  CK(cudaMemcpyAsync(c->d.S, &S, sizeof(S), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SQDEM_OK;
+}
+sqdem_status sqdem_set_velgrad(sqdem_ctx* c, const double* velGrad9) {
+  if (!c || !velGrad9) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "set bodies first");
+  CK(cudaSetDevice(c->device));
+  SceneState S; sqdem_status st = readScene(c, S); if (st) return st;
+  for (int k = 0; k < 9; k++) S.nextVelGrad[k] = velGrad9[k];
+  S.velGradChanged = 1;
+  CK(cudaMemcpyAsync(c->d.S, &S, sizeof(S), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SQDEM_OK;
+}
+// hSize9 velGrad9 prevVelGrad9 size3 prevCellSize3 (33 doubles)
+sqdem_status sqdem_get_cell(sqdem_ctx* c, double* o) {
+  if (!c || !o) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  SceneState S; sqdem_status st = readScene(c, S); if (st) return st;
+  for (int k = 0; k < 9; k++) { o[k] = S.hSize[k]; o[9 + k] = S.velGrad[k]; o[18 + k] = S.prevVelGrad[k]; }
+  for (int k = 0; k < 3; k++) { o[27 + k] = S.cellSize[k]; o[30 + k] = S.prevCellSize[k]; }
+  return SQDEM_OK;
+}
+sqdem_status sqdem_put_cell(sqdem_ctx* c, const double* o) {
+  if (!c || !o) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  SceneState S; sqdem_status st = readScene(c, S); if (st) return st;
+  for (int k = 0; k < 9; k++) { S.hSize[k] = o[k]; S.velGrad[k] = o[9 + k]; S.prevVelGrad[k] = o[18 + k]; S.nextVelGrad[k] = 0; }
+  for (int k = 0; k < 3; k++) { S.cellSize[k] = o[27 + k]; S.prevCellSize[k] = o[30 + k]; S.prevRunCellSize[k] = o[27 + k]; }
+  S.velGradChanged = 0;
+  CK(cudaMemcpyAsync(c->d.S, &S, sizeof(S), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   return SQDEM_OK;
 }
 

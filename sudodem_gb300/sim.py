@@ -47,7 +47,7 @@ __all__ = ["O", "Omega", "utils", "Body", "State", "Superquadrics", "Wall", "Sup
            "Ig2_Superquadrics_Superquadrics_SuperquadricsGeom", "Ig2_Wall_Superquadrics_SuperquadricsGeom",
            "Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys", "SuperquadricsLaw",
            "Ip2_FrictMat_FrictMat_FrictPhys", "Law2_ScGeom_FrictPhys_CundallStrack", "NewtonIntegrator",
-           "PyRunner", "NewSuperquadrics", "NewSuperquadrics2", "NewSuperquadrics_rot", "NewSuperquadrics_rot2",
+           "PyRunner", "Cell", "NewSuperquadrics", "NewSuperquadrics2", "NewSuperquadrics_rot", "NewSuperquadrics_rot2",
            "Vector3", "Quaternion"]
 
 
@@ -378,6 +378,61 @@ class ForceContainer:
 
 
 # ----------------------------------------------------------------------------------------------
+class Cell:
+    """Periodic cell (core/Cell.hpp): hSize columns are the base vectors; velGrad takes
+    effect at the next integrator pass (Cell::setVelGrad); homoDeform is always on."""
+
+    def __init__(self, scene):
+        self._scene = scene
+        self._hSize = np.eye(3)
+        self._velGrad = np.zeros((3, 3))
+        self._pending = None
+        self.homoDeform = True
+
+    def setBox(self, *size):
+        if len(size) == 1:
+            size = size[0]
+        self.hSize = np.diag(np.array(size, dtype=np.float64))
+
+    @property
+    def hSize(self):
+        e = self._scene._engine
+        if e is not None and self._scene.periodic:
+            return e.cell()[0:9].reshape(3, 3)
+        return self._hSize.copy()
+
+    @hSize.setter
+    def hSize(self, m):
+        self._hSize = np.array(m, dtype=np.float64).reshape(3, 3)
+        self._scene._structDirty = True
+
+    @property
+    def size(self):
+        h = self.hSize
+        return np.linalg.norm(h, axis=0)
+
+    @property
+    def volume(self):
+        return float(np.linalg.det(self.hSize))
+
+    @property
+    def velGrad(self):
+        e = self._scene._engine
+        if e is not None and self._scene.periodic:
+            return e.cell()[9:18].reshape(3, 3)
+        return self._velGrad.copy()
+
+    @velGrad.setter
+    def velGrad(self, m):
+        m = np.array(m, dtype=np.float64).reshape(3, 3)
+        self._velGrad = m
+        e = self._scene._engine
+        if e is not None and not self._scene._structDirty:
+            e.set_velgrad(m)
+        else:
+            self._pending = m
+
+
 class Omega:
     """The scene and its timestep loop (core/Omega.cpp, core/Scene.cpp:70-138)."""
 
@@ -399,6 +454,8 @@ class Omega:
         self._pulled = True
         self._iter0 = 0
         self.tags = {}
+        self.periodic = False
+        self.cell = Cell(self)
 
     # engines -------------------------------------------------------------------------------
     @property
@@ -516,6 +573,10 @@ class Omega:
                           [m.betan for m in mats], [m.betas for m in mats], [m.density for m in mats])
         self._set_params(eng, col, newton)
         eng.set_bodies(kind, shape5, was, mat, sph, st)
+        if self.periodic:
+            vg = self.cell._pending if self.cell._pending is not None else self.cell._velGrad
+            eng.set_periodic(self.cell._hSize, vg if np.any(vg != 0) else None)
+            self.cell._pending = None
         self._engine = eng
         self._parts = (col, ilp, newton, runners)
         self._structDirty = False

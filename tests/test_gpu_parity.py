@@ -224,3 +224,69 @@ def test_deposition_statistics_match_oracle(gpu):
     ng = np.sum(eng.interactions(False)[:, 4] > 0)
     nr = np.sum(orc.interactions()[:, 4] > 0)
     assert abs(int(ng) - int(nr)) <= max(3, 0.05 * nr)
+
+
+def brute_periodic(b, L):
+    from test_oracle import _brute_pairs_periodic
+    return _brute_pairs_periodic(b, L)
+
+
+def test_periodic_pair_set_equals_image_overlaps(gpu):
+    """GPU periodic collider: after each pass the table holds exactly the pairs whose bounds
+    overlap under a periodic image, plus real pairs the law has not yet erased."""
+    spec = assemblies.periodic_cell(300, seed=9, solid_fraction=0.38, strain_rate=3.0)
+    eng = engine_for(spec)
+    checked = 0
+    for _ in range(25):
+        before = eng.scalars()[7]
+        eng.step(5); eng.sync()
+        if eng.scalars()[7] == before:
+            continue
+        b = eng.body_state()
+        L = eng.cell()[27:30]
+        I = eng.interactions(True)
+        have = {tuple(sorted(map(int, r[:2]))) for r in I}
+        nonreal = {tuple(sorted(map(int, r[:2]))) for r in I if r[2] == 0}
+        brute = brute_periodic(b, L)
+        assert brute <= have
+        assert have - brute <= nonreal
+        checked += 1
+    assert checked >= 2
+
+
+def periodic_spec(seed=3, n=400):
+    return assemblies.periodic_cell(n, seed=seed, solid_fraction=0.42, strain_rate=3.0)
+
+
+def test_periodic_first_steps_pair_set_celldist_bitexact(gpu):
+    spec = periodic_spec()
+    eng = engine_for(spec)
+    orc = OracleScene.from_spec(spec)
+    for _ in range(3):
+        eng.step(1); eng.sync(); orc.step(1)
+        assert np.array_equal(eng.cell(), orc.cell())
+        g, r = eng.body_state(), orc.bodies()
+        assert np.array_equal(g[:, 22:33], r[:, 22:33])
+        gi, ri = eng.interactions(True), orc.interactions()
+        G, R = by_pair(gi), by_pair(ri)
+        assert set(G) == set(R)
+        assert all(np.array_equal(G[k][44:47], R[k][44:47]) for k in R)
+        assert all(G[k][2] == R[k][2] for k in R)
+
+
+def test_periodic_single_step_within_oracle_conditioning(gpu):
+    spec = periodic_spec(seed=4)
+    orc = OracleScene.from_spec(spec, threads=4)
+    orc.step(40)
+    eng = engine_for(spec)
+    snapshot_into(eng, orc)
+    eng.put_cell(orc.cell())
+    eng.step(1); eng.sync(); orc.step(1)
+    assert np.array_equal(eng.cell(), orc.cell())
+    G, R = touching_common(eng.interactions(True), orc.interactions())
+    assert len(G) > 30
+    e = rel_force_errors(G, R)
+    assert np.median(e) < 1e-9 and np.mean(e < 1e-6) > 0.97
+    g, r = eng.body_state(), orc.bodies()
+    assert np.max(np.abs(g[:, 0:3] - r[:, 0:3])) < 1e-13
+    assert np.max(np.abs(g[:, 7:10] - r[:, 7:10])) < 1e-6 * np.max(np.abs(r[:, 7:10]))

@@ -103,10 +103,10 @@ def test_script_runs_on_gpu_and_matches_engine(gpu):
     kind, shape5, was, mat, sph, st, blocked = O._body_arrays()
     O2 = sim.Omega()
     build_example(O2, n=8)
+    m = O2._material_table()[0]
     kind2, shape52, was2, mat2, sph2, st2, _ = O2._body_arrays()
     from sudodem_gb300 import Engine
     e = Engine(device=0)
-    m = O2._material_table()[0]
     e.set_materials([m.Kn], [m.Ks], [m.frictionAngle], [m.betan], [m.betas], [m.density])
     e.set_params(dt=1e-6, gravity=(0, 0, -9.81), damping=0.3, verletDist=2e-4)
     e.set_bodies(kind2, shape52, was2, mat2, sph2, st2)
