@@ -489,6 +489,16 @@ __device__ __forceinline__ int orientNew(const Dev& d, int i, int j, int initSor
     if (jpxk < comp(ipn, k) && jmxk > comp(imn, k)) return 1;
     if (comp(ipx, k) < jpnk && comp(imx, k) > jmnk) return 0;
   }
+  // No crossing seen.  Without periodicity this needs exactly equal coordinates, and the
+  // reference's sort would not insert the pair either.  In a periodic cell the image shifts
+  // above only approximate the circular sort order, so an overlapping pair is inserted with
+  // the full-sort orientation rather than missed.
+  if (S.periodic) {
+    double a = comp(imn, sortAxis), b = comp(jmn, sortAxis) + shNow[sortAxis];
+    if (a < b) return 1;
+    if (b < a) return 0;
+    return i < j ? 1 : 0;
+  }
   return -1;
 }
 
