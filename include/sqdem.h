@@ -182,6 +182,18 @@ sqdem_status sqdem_time_steps(sqdem_ctx* ctx, int nsteps, double* ms);
 sqdem_status sqdem_time_e2e(sqdem_ctx* ctx, int nsteps, const double* in16, double* out16, double* ms);
 sqdem_status sqdem_time_contacts(sqdem_ctx* ctx, int nrep, double* ms);
 
+/* One pass of the contact stage (narrowphase, contact physics and law; the work of
+ * sqdem_time_contacts without its timing) that allocates nothing: its work queue is a fixed
+ * static device array of SQDEM_STATIC_QUEUE_MAX ints (4 MiB per GPU, held until exit) instead
+ * of a buffer owned by the context.  For callers that cannot call cudaMalloc at that point
+ * (inside a stream capture, under a host framework that forbids raw allocations after
+ * start-up).  Rejects tables larger than the array with SQDEM_ERR_CAPACITY.  The first call on
+ * a device looks up the array's address (cudaGetSymbolAddress); make it before any stream
+ * capture.  Calls share the array, so calls that overlap on the GPU race.  Asynchronous on the
+ * context stream.  No counterpart in the reference. */
+#define SQDEM_STATIC_QUEUE_MAX (1 << 20)
+sqdem_status sqdem_contacts_static_queue(sqdem_ctx* ctx);
+
 /* Superquadrics::Initial (pkg/dem/Superquadrics.cpp:47-93): volume, geometric inertia (3),
  * bounding radius r_max, for unit density.  Host-only helper. */
 sqdem_status sqdem_shape_props(double rx, double ry, double rz, double eps1, double eps2, double* out5);

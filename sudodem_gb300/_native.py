@@ -95,6 +95,7 @@ def load_library(build_if_missing=True):
         "sqdem_set_velgrad": (i, [v, dp]),
         "sqdem_get_cell": (i, [v, dp]),
         "sqdem_put_cell": (i, [v, dp]),
+        "sqdem_contacts_static_queue": (i, [v]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -111,7 +112,7 @@ def exported_symbols():
             "sqdem_put_interactions", "sqdem_get_scalars", "sqdem_put_scalars", "sqdem_stage_times",
             "sqdem_shape_props", "sqdem_launch_count", "sqdem_set_record_full", "sqdem_time_steps",
             "sqdem_time_e2e", "sqdem_time_contacts", "sqdem_set_use_graph", "sqdem_set_periodic",
-            "sqdem_set_velgrad", "sqdem_get_cell", "sqdem_put_cell"]
+            "sqdem_set_velgrad", "sqdem_get_cell", "sqdem_put_cell", "sqdem_contacts_static_queue"]
 
 
 def _dp(a):
@@ -232,6 +233,11 @@ class Engine:
         ms = C.c_double()
         self._check(self.lib.sqdem_time_contacts(self.h, int(nrep), C.byref(ms)))
         return ms.value
+
+    def contacts_static_queue(self):
+        """One contact-stage pass with the work queue in the library's static device array
+        (no allocation; see include/sqdem.h)."""
+        self._check(self.lib.sqdem_contacts_static_queue(self.h))
 
     def launch_count(self):
         return int(self.lib.sqdem_launch_count(self.h))

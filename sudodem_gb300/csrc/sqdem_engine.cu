@@ -39,6 +39,11 @@
 #include "sq_device.cuh"
 #include "../../include/sqdem.h"
 
+// Work queue of the contact stage for sqdem_contacts_static_queue: a fixed device array so
+// that entry point needs no allocation.  Every GPU that loads the library holds it (4 MiB)
+// until the process exits; all calls share it.  SQDEM_STATIC_QUEUE_MAX comes from sqdem.h.
+static __device__ __align__(256) int g_static_lm_queue[SQDEM_STATIC_QUEUE_MAX];
+
 namespace sqdem {
 
 // ---------------------------------------------------------------------------
@@ -2635,6 +2640,67 @@ sqdem_status sqdem_put_cell(sqdem_ctx* c, const double* o) {
   S.velGradChanged = 0;
   CK(cudaMemcpyAsync(c->d.S, &S, sizeof(S), cudaMemcpyHostToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  return SQDEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Contact stage without allocation.
+//
+// Some callers cannot call cudaMalloc at the point where they advance the contacts: code
+// running while a CUDA stream is being captured into a graph (allocation is not allowed
+// there), host frameworks that own all device memory through their own pool and forbid raw
+// allocations after start-up, or real-time loops that must not block in the allocator.  For
+// them this entry point runs one pass of the contact stage (pre-pass, Levenberg-Marquardt
+// kernel, contact physics and law) on the context's state with its work queue (scratch) in
+// g_static_lm_queue instead of a buffer owned by the context.  It calls no cudaMalloc,
+// cudaFree or allocating library routine.
+//
+// Limits and rules:
+//  * at most SQDEM_STATIC_QUEUE_MAX (1,048,576) contact-table entries; larger tables are
+//    rejected with SQDEM_ERR_CAPACITY before anything is launched;
+//  * the first call on a device looks up the array's device address with
+//    cudaGetSymbolAddress (with that device current); make that first call before any
+//    stream capture;
+//  * all calls share the one array, which keeps the last call's contents; nothing in it needs
+//    to start at zero (the queue counters live in the context and are reset by the call), but
+//    calls that overlap on the GPU (other streams or contexts at the same time) race on it;
+//  * the launches are asynchronous on the context stream, like sqdem_step.
+static int* g_static_queue_addr[128];
+static bool g_static_queue_ready[128];
+
+static sqdem_status staticQueueAddress(sqdem_ctx* c, int** out) {
+  if (c->device < 0 || c->device >= 128) return fail(c, SQDEM_ERR_ARG, "device ordinal out of range");
+  if (!g_static_queue_ready[c->device]) {
+    CK(cudaSetDevice(c->device));
+    int* ptr = nullptr;
+    CK(cudaGetSymbolAddress((void**)&ptr, g_static_lm_queue));
+    g_static_queue_addr[c->device] = ptr;
+    g_static_queue_ready[c->device] = true;
+  }
+  *out = g_static_queue_addr[c->device];
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_contacts_static_queue(sqdem_ctx* c) {
+  if (!c) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "bodies must be set before the contact stage");
+  CK(cudaSetDevice(c->device));
+  int P = 0;
+  CK(cudaMemcpy(&P, (char*)c->d.S + offsetof(SceneState, P), sizeof(int), cudaMemcpyDeviceToHost));
+  if (P > SQDEM_STATIC_QUEUE_MAX)
+    return fail(c, SQDEM_ERR_CAPACITY, "contact table has " + std::to_string(P) +
+                " entries; sqdem_contacts_static_queue handles at most " + std::to_string(SQDEM_STATIC_QUEUE_MAX));
+  int* queue = nullptr;
+  sqdem_status st = staticQueueAddress(c, &queue);
+  if (st) return st;
+  Dev d = c->d;
+  d.lmQueue = queue;
+  k_reset_queue<<<1, 1, 0, c->stream>>>(d);
+  k_contacts_pre<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, c->stream>>>(d);
+  if (c->precision == SQDEM_MIXED) k_contacts_lm_mixed<<<c->numSMs * c->lmBlocksPerSMmixed, LM_BS, 0, c->stream>>>(d);
+  else k_contacts_lm<<<c->numSMs * c->lmBlocksPerSM, LM_BS, 0, c->stream>>>(d);
+  c->launches += 3;
+  CK(cudaGetLastError());
   return SQDEM_OK;
 }
 
