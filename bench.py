@@ -118,7 +118,7 @@ def measured_peaks():
 
 def profiled_traffic_per_pair():
     """dram bytes per table entry of one k_contacts launch from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "k_contacts_sq200k.txt")
+    p = os.path.join(ROOT, "profiles", "k_contacts_periodic100k.txt")
     if not os.path.exists(p):
         return None
     for ln in open(p):
