@@ -194,6 +194,7 @@ def run_ours(args):
     from sudodem_gb300 import Engine
     spec = workload_spec(args.workload, args.seed + rank)
     eng = Engine(device=0, precision=args.precision, contacts_per_body=args.contacts_per_body)
+    eng.set_lm_spread(not args.no_lm_spread)
     eng.load(spec)
     npart = spec.n_particles
     eng.step(args.warmup)
@@ -253,6 +254,7 @@ def run_ours(args):
                 "data": "synthetic",
                 "config": {"workload": args.workload, "particles": npart, "bodies": spec.n_bodies,
                            "table_entries": nentries, "precision": args.precision, "parallelism": "replicas",
+                           "lm_spread": not args.no_lm_spread,
                            "l2": f"inputs larger than L2: contact table {nentries} entries x >= 256 B"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
                 "report": rep}
@@ -271,6 +273,8 @@ def main():
     ap.add_argument("--contacts-per-body", type=int, default=16)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-lm-spread", action="store_true",
+                    help="one Levenberg-Marquardt evaluation point per lane and round (same results)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -153,6 +153,13 @@ sqdem_status sqdem_put_scalars(sqdem_ctx* ctx, const double* in9);
  * the step then writes only the history the next step needs. */
 sqdem_status sqdem_set_record_full(sqdem_ctx* ctx, int on);
 
+/* Schedule of the Levenberg-Marquardt evaluations (no counterpart in the reference, which
+ * runs one search per thread).  on = 1 (default): once the contact queue is drained, lanes
+ * without a contact evaluate the points the searches still running in their warp will ask
+ * for next; on = 0: every lane evaluates only its own search's point.  Results are identical
+ * bit for bit; only the time of the longest searches changes. */
+sqdem_status sqdem_set_lm_spread(sqdem_ctx* ctx, int on);
+
 /* Per-stage device time of the last sqdem_step call in milliseconds (cudaEvent pairs on the
  * context stream; only when the context was created with use_graph == 0):
  * out[0] collider gate+passes, out[1] contacts (narrowphase+law), out[2] integrator+reductions. */

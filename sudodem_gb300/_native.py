@@ -91,6 +91,7 @@ def load_library(build_if_missing=True):
         "sqdem_time_e2e": (i, [v, i, v, v, dp]),
         "sqdem_time_contacts": (i, [v, i, dp]),
         "sqdem_set_use_graph": (i, [v, i]),
+        "sqdem_set_lm_spread": (i, [v, i]),
         "sqdem_set_periodic": (i, [v, dp, dp]),
         "sqdem_set_velgrad": (i, [v, dp]),
         "sqdem_get_cell": (i, [v, dp]),
@@ -111,7 +112,7 @@ def exported_symbols():
             "sqdem_get_kinematics", "sqdem_put_kinematics", "sqdem_num_interactions", "sqdem_get_interactions",
             "sqdem_put_interactions", "sqdem_get_scalars", "sqdem_put_scalars", "sqdem_stage_times",
             "sqdem_shape_props", "sqdem_launch_count", "sqdem_set_record_full", "sqdem_time_steps",
-            "sqdem_time_e2e", "sqdem_time_contacts", "sqdem_set_use_graph", "sqdem_set_periodic",
+            "sqdem_time_e2e", "sqdem_time_contacts", "sqdem_set_use_graph", "sqdem_set_lm_spread", "sqdem_set_periodic",
             "sqdem_set_velgrad", "sqdem_get_cell", "sqdem_put_cell", "sqdem_contacts_static_queue"]
 
 
@@ -196,6 +197,9 @@ class Engine:
 
     def set_use_graph(self, on=True):
         self._check(self.lib.sqdem_set_use_graph(self.h, 1 if on else 0))
+
+    def set_lm_spread(self, on=True):
+        self._check(self.lib.sqdem_set_lm_spread(self.h, 1 if on else 0))
 
     def set_record_full(self, on=True):
         self._check(self.lib.sqdem_set_record_full(self.h, 1 if on else 0))

@@ -61,6 +61,7 @@ static const unsigned DOF_ALL = 63u;
 struct Params {
   double dt, g[3], damping, verletDist, minSweepDistFactor, h0;
   int targetInterv, sortAxis, isSuperquadrics, exactAsphericalRot, recordFull;
+  int lmSpread;   // idle lanes evaluate the points running searches ask for next
 };
 
 enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_EVAL32, E_EVAL64, E_NUM };
@@ -1165,14 +1166,128 @@ __device__ __forceinline__ bool lmConsume(LMLane& L) {
   }
 }
 
+// Points lmder2 evaluates next, the requested one first, then the points that follow it
+// under each outcome of the requested evaluation: after INIT the two probes at the start
+// point; after PROBE0 the second probe; after a TRIAL the two probes at the trial point
+// (accepted) and the next trial with mu*nu (rejected), recursively.  Every point is computed
+// with the operations the state machine itself uses, so a point it later asks for matches
+// bit for bit.  Returns the number of points written (at most S).
+__device__ __forceinline__ int lmPlan(const LMLane& L, double2* q, int S) {
+  int n = 0;
+  q[n++] = make_double2(L.q0, L.q1);
+  if (L.st == ST_INIT) {
+    if (n < S) q[n++] = make_double2(L.p0 + 1e-7, L.p1);
+    if (n < S) q[n++] = make_double2(L.p0, L.p1 + 1e-7);
+  } else if (L.st == ST_PROBE0) {
+    if (n < S) q[n++] = make_double2(L.p0, L.p1 + L.Dp1);
+  } else if (L.st == ST_TRIAL) {
+    double mu = L.mu, t0 = L.q0, t1 = L.q1, d0 = L.Dp0, d1 = L.Dp1;
+    int nu = L.nu;
+    while (n < S) {
+      q[n++] = make_double2(t0 + d0, t1);
+      if (n >= S) break;
+      q[n++] = make_double2(t0, t1 + d1);
+      if (n >= S) break;
+      mu *= nu;
+      const int nu2 = (int)((unsigned)nu << 1);
+      if (nu2 <= nu) break;
+      nu = nu2;
+      const double j00 = L.diag0 + mu, j11 = L.diag1 + mu;
+      const double n_a = j00 * j11 - L.j01 * L.j01;
+      d0 = (L.jt0 * j11 - L.jt1 * L.j01) / n_a;
+      d1 = (L.jt1 * j00 - L.jt0 * L.j01) / n_a;
+      const double Dp_L2 = sqrt(d0 * d0 + d1 * d1);
+      if (Dp_L2 < 1e-5) break;
+      t0 = L.p0 + d0; t1 = L.p1 + d1;
+      if (Dp_L2 >= (L.pL2 + 1e-3) / (1e-12 * 1e-12)) break;
+      q[n++] = make_double2(t0, t1);
+    }
+  }
+  return n;
+}
+
+__device__ __forceinline__ bool sameBits(double2 a, double q0, double q1) {
+  return __double_as_longlong(a.x) == __double_as_longlong(q0) && __double_as_longlong(a.y) == __double_as_longlong(q1);
+}
+
+// One lmder2 call finished: the restart rules of Superquadrics_Ig2.cpp:2013-2053, and when no
+// restart follows, the end of Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go, Ip2 and
+// the law.  Returns true when the contact is finished.
+__device__ __forceinline__ bool lmCallEnd(const Dev& d, LMLane& L, const SqShape& A, const SqShape& B, Counters& cnt) {
+  const SceneState& S = *d.S;
+  L.calls++; L.iters += L.k; L.maxit += (L.stop == 3);
+  bool restart = false;
+  if (L.phase == 0) {
+    L.phase = 1;
+    if ((isnan(L.p0) || isnan(L.p1) || 7 == L.stop) && L.touching) restart = true;
+  } else if (L.phase == 1) {
+    L.phase = 3;
+    if (L.touching && 10.0 * nrm(L.P2 - L.P1) > A.rmax && (!isInside(A, L.P2 - A.pos) || !isInside(B, L.P1 - B.pos))) {
+      L.phase = 2; restart = true;
+    }
+  } else L.phase = 3;
+  if (!restart && L.phase == 1) {  // no NaN restart: continue with the local-minimum check
+    L.phase = 3;
+    if (L.touching && 10.0 * nrm(L.P2 - L.P1) > A.rmax && (!isInside(A, L.P2 - A.pos) || !isInside(B, L.P1 - B.pos))) {
+      L.phase = 2; restart = true;
+    }
+  }
+  if (restart) {
+    double para[2];
+    centerLine(A.pos, B.pos, para);
+    L.p0 = para[0]; L.p1 = para[1];
+    lmStartSolve(L);
+    return false;
+  }
+  // end of Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go, then Ip2 + law
+  const int e = L.e;
+  const unsigned fl = d.A.flags[e];
+  int id1, id2;
+  entryIds(d, e, fl, id1, id2);
+  const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
+  GeomOut g;
+  g.lmCalls = L.calls; g.lmIters = L.iters; g.lmStop = 0; g.nanNormal = false;
+  g.isShearNew = L.isNew ? true : (d.A.depth[e] <= 0);
+  g.cp = L.isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
+  g.ang0 = L.p0; g.ang1 = L.p1; g.angSet = true;
+  if (!L.touching) {
+    g.precomputed = false; g.depth = 0; g.isShearNew = true;
+  } else {
+    const double pDepth = dot(L.P1 - L.P2, L.contact);
+    g.p1 = L.P1; g.p2 = L.P2;
+    if (isnan(L.contact.x)) g.nanNormal = true;
+    g.cp = L.C;
+    g.depth = pDepth;
+    D3 cn = L.contact;
+    normalize(cn);
+    const D3 oldNormal = L.isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
+    g.precomputed = true;
+    precomputeD(g, oldNormal, b1, b2, d.prm->dt, cn, g.isShearNew, cellShift(S, d.A.cd[e]));
+    g.normal = cn;
+  }
+  cnt.lmCalls += L.calls; cnt.lmIters += L.iters; cnt.lmMax += L.maxit;
+  finishEntry(d, e, fl, L.isNew, id1, b1, b2, g, cnt);
+  return true;
+}
+
+// Pass 2, FP64.  Rounds of one Disfunction evaluation per lane.  While the queue has work,
+// every lane evaluates the point its own search asks for.  Once the queue is drained, the
+// lanes left without a contact evaluate, for the searches still running in their warp, the
+// points those searches will ask for next (lmPlan); each search then consumes, in its own
+// order, every evaluation whose point is the one it asks for.  A search with 31 idle lanes
+// beside it thus advances one whole iteration (trial + two probes, or a run of rejected
+// trials) per round instead of one evaluation, which shortens the dependency chain of the
+// longest searches that bound the kernel.  Results are those of the one-point rounds: an
+// evaluation depends only on its point and the two shapes.
 __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
   __shared__ SqShape shA[LM_BS], shB[LM_BS];
-  SqShape& A = shA[threadIdx.x];
-  SqShape& B = shB[threadIdx.x];
+  __shared__ double2 slotQ[LM_BS];
+  __shared__ int slotOwner[LM_BS];
   const SceneState& S = *d.S;
   const int count = S.lmCount;
-  const double dt = d.prm->dt;
   const int lane = threadIdx.x & 31;
+  const int wbase = threadIdx.x & ~31;
+  const bool spread = d.prm->lmSpread != 0;
   Counters cnt = {0, 0, 0, 0, 0};
   unsigned long long ev64 = 0;
   LMLane L;
@@ -1188,6 +1303,8 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
         const int idx = base + __popc(idle & ((1u << lane) - 1));
         if (idx < count) {
           // start a contact: Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go up to lmder2
+          SqShape& A = shA[threadIdx.x];
+          SqShape& B = shB[threadIdx.x];
           L.e = d.lmQueue[idx];
           const unsigned fl = d.A.flags[L.e];
           int id1, id2;
@@ -1207,67 +1324,43 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
         } else exhausted = true;
       }
     }
-    if (!__any_sync(0xffffffffu, active)) break;
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!act) break;
+    // slots per running search: 1 while the queue has work, else the warp's lanes shared out
+    const int spc = (spread && __any_sync(0xffffffffu, exhausted)) ? 32 / __popc(act) : 1;
+    const int base = __popc(act & ((1u << lane) - 1)) * spc;
+    slotOwner[threadIdx.x] = -1;
+    __syncwarp();
     if (active) {
-      disfunction(A, B, L.q0, L.q1, L.C, L.P1, L.P2, L.stopFlag);
+      const int n = lmPlan(L, &slotQ[wbase + base], spc);
+      for (int j = 0; j < n; j++) slotOwner[wbase + base + j] = lane;
+    }
+    __syncwarp();
+    D3 P1 = d3(0, 0, 0), P2 = d3(0, 0, 0);
+    bool flag = false;
+    const int own = slotOwner[threadIdx.x];
+    if (own >= 0) {
+      const double2 q = slotQ[threadIdx.x];
+      D3 C;
+      disfunction(shA[wbase + own], shB[wbase + own], q.x, q.y, C, P1, P2, flag);
       ev64++;
-      if (!lmConsume(L)) {
-        // one lmder2 call finished: the restart rules of Superquadrics_Ig2.cpp:2013-2053
-        L.calls++; L.iters += L.k; L.maxit += (L.stop == 3);
-        bool restart = false;
-        if (L.phase == 0) {
-          L.phase = 1;
-          if ((isnan(L.p0) || isnan(L.p1) || 7 == L.stop) && L.touching) restart = true;
-        } else if (L.phase == 1) {
-          L.phase = 3;
-          if (L.touching && 10.0 * nrm(L.P2 - L.P1) > A.rmax && (!isInside(A, L.P2 - A.pos) || !isInside(B, L.P1 - B.pos))) {
-            L.phase = 2; restart = true;
-          }
-        } else L.phase = 3;
-        if (!restart && L.phase == 1) {  // no NaN restart: continue with the local-minimum check
-          L.phase = 3;
-          if (L.touching && 10.0 * nrm(L.P2 - L.P1) > A.rmax && (!isInside(A, L.P2 - A.pos) || !isInside(B, L.P1 - B.pos))) {
-            L.phase = 2; restart = true;
-          }
-        }
-        if (restart) {
-          double para[2];
-          centerLine(A.pos, B.pos, para);
-          L.p0 = para[0]; L.p1 = para[1];
-          lmStartSolve(L);
-        } else {
-          // end of Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go, then Ip2 + law
-          const int e = L.e;
-          const unsigned fl = d.A.flags[e];
-          int id1, id2;
-          entryIds(d, e, fl, id1, id2);
-          const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
-          GeomOut g;
-          g.lmCalls = L.calls; g.lmIters = L.iters; g.lmStop = 0; g.nanNormal = false;
-          g.isShearNew = L.isNew ? true : (d.A.depth[e] <= 0);
-          g.cp = L.isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
-          g.ang0 = L.p0; g.ang1 = L.p1; g.angSet = true;
-          if (!L.touching) {
-            g.precomputed = false; g.depth = 0; g.isShearNew = true;
-          } else {
-            const double pDepth = dot(L.P1 - L.P2, L.contact);
-            g.p1 = L.P1; g.p2 = L.P2;
-            if (isnan(L.contact.x)) g.nanNormal = true;
-            g.cp = L.C;
-            g.depth = pDepth;
-            D3 cn = L.contact;
-            normalize(cn);
-            const D3 oldNormal = L.isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
-            g.precomputed = true;
-            precomputeD(g, oldNormal, b1, b2, dt, cn, g.isShearNew, cellShift(S, d.A.cd[e]));
-            g.normal = cn;
-          }
-          cnt.lmCalls += L.calls; cnt.lmIters += L.iters; cnt.lmMax += L.maxit;
-          finishEntry(d, e, fl, L.isNew, id1, b1, b2, g, cnt);
-          active = false;
-        }
+    }
+    for (int j = 0; j < spc; j++) {
+      const int src = active ? base + j : lane;
+      const double x1 = __shfl_sync(0xffffffffu, P1.x, src), y1 = __shfl_sync(0xffffffffu, P1.y, src),
+                   z1 = __shfl_sync(0xffffffffu, P1.z, src);
+      const double x2 = __shfl_sync(0xffffffffu, P2.x, src), y2 = __shfl_sync(0xffffffffu, P2.y, src),
+                   z2 = __shfl_sync(0xffffffffu, P2.z, src);
+      const bool f = __shfl_sync(0xffffffffu, (int)flag, src) != 0;
+      if (active && slotOwner[wbase + src] == lane && sameBits(slotQ[wbase + src], L.q0, L.q1)) {
+        L.P1 = d3(x1, y1, z1);
+        L.P2 = d3(x2, y2, z2);
+        L.C = 0.5 * (L.P1 + L.P2);
+        if (f) L.stopFlag = true;
+        if (!lmConsume(L) && lmCallEnd(d, L, shA[threadIdx.x], shB[threadIdx.x], cnt)) active = false;
       }
     }
+    __syncwarp();
   }
   flushCounters(d, cnt);
   for (int o = 16; o > 0; o >>= 1) ev64 += __shfl_down_sync(0xffffffffu, ev64, o);
@@ -1780,6 +1873,7 @@ struct sqdem_ctx {
   std::vector<void*> allocs;
   sqdem_params params;
   int recordFull = 0;
+  int lmSpread = 1;
   std::vector<int> kind, wallIds, matIds, isSphere, axisSense;
   std::vector<double> shape5;
   int nMats = 0;
@@ -1922,6 +2016,7 @@ static sqdem_status uploadParams(sqdem_ctx* c) {
   P.minSweepDistFactor = c->params.minSweepDistFactor; P.targetInterv = c->params.targetInterv;
   P.sortAxis = c->params.sortAxis; P.isSuperquadrics = c->params.isSuperquadrics;
   P.exactAsphericalRot = c->params.exactAsphericalRot; P.recordFull = c->recordFull;
+  P.lmSpread = c->lmSpread;
   P.h0 = hostH0(c);
   CK(cudaMemcpyAsync(c->d.prm, &P, sizeof(P), cudaMemcpyHostToDevice, c->stream));
   return SQDEM_OK;
@@ -2716,6 +2811,13 @@ sqdem_status sqdem_set_use_graph(sqdem_ctx* c, int on) {
 sqdem_status sqdem_set_record_full(sqdem_ctx* c, int on) {
   if (!c) return SQDEM_ERR_ARG;
   c->recordFull = on ? 1 : 0;
+  if (c->haveBodies) { sqdem_status s = uploadParams(c); if (s) return s; CK(cudaStreamSynchronize(c->stream)); }
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_set_lm_spread(sqdem_ctx* c, int on) {
+  if (!c) return SQDEM_ERR_ARG;
+  c->lmSpread = on ? 1 : 0;
   if (c->haveBodies) { sqdem_status s = uploadParams(c); if (s) return s; CK(cudaStreamSynchronize(c->stream)); }
   return SQDEM_OK;
 }
