@@ -88,6 +88,8 @@ typedef struct {
   long long steps;            /* timesteps executed */
   long long evals_fp32;       /* Disfunction evaluations in FP32 (mixed form) */
   long long evals_fp64;       /* Disfunction evaluations in FP64 */
+  long long lm_rounds_max;    /* longest contact, in evaluation rounds of the FP64 LM kernel
+                                 (the critical path of the contact stage), max over steps */
 } sqdem_report;
 
 /* Record layouts shared with the CPU oracle (doubles per record). */

@@ -41,7 +41,8 @@ class _Params(C.Structure):
 
 class _Report(C.Structure):
     _fields_ = [(n, C.c_longlong) for n in ("nan_normals", "nan_forces", "lm_calls", "lm_iterations", "lm_maxiter",
-                                             "overflow", "collider_runs", "steps", "evals_fp32", "evals_fp64")]
+                                             "overflow", "collider_runs", "steps", "evals_fp32", "evals_fp64",
+                                             "lm_rounds_max")]
 
 
 _LIB = None

@@ -78,21 +78,25 @@ __device__ __forceinline__ void shapeInit(SqShape& s, double rx, double ry, doub
   s.i1 = 1 / (2. - e1); s.i2 = 1 / (2. - e2);
 }
 
-// Superquadrics::Normal2Phi (pkg/dem/Superquadrics.cpp:269-307), local frame.
-__device__ __forceinline__ void normal2phi(const SqShape& s, D3 n, double& ph0, double& ph1) {
-  ph0 = atan2(sgn(n.y) * pow(fabs(s.ry * n.y), s.i1), sgn(n.x) * pow(fabs(s.rx * n.x), s.i1));
-  ph1 = atan2(sgn(n.z) * pow(fabs(s.rz * n.z * pow(fabs(cos(ph0)), s.a1)), s.i2), pow(fabs(s.rx * n.x), s.i2));
-}
-// Superquadrics::getSurface (Superquadrics.cpp:110-120), local frame.
-__device__ __forceinline__ D3 surface(const SqShape& s, double ph0, double ph1) {
-  double s0, c0, s1, c1;
+// Superquadrics::Normal2Phi (pkg/dem/Superquadrics.cpp:269-307) followed by
+// Superquadrics::getSurface (:110-120): the point of the surface, in the local frame, whose
+// outward normal is n.  One sincos of phi0 serves both, as one cos value does in the
+// reference.  The evaluation order of every product is the reference's.
+__device__ __forceinline__ D3 supportLocal(const SqShape& s, D3 n) {
+  const double Y = pow(fabs(s.ry * n.y), s.i1), X = pow(fabs(s.rx * n.x), s.i1), W = pow(fabs(s.rx * n.x), s.i2);
+  const double ph0 = atan2(sgn(n.y) * Y, sgn(n.x) * X);
+  double s0, c0;
   sincos(ph0, &s0, &c0);
+  const double t = pow(fabs(c0), s.a1), u = pow(fabs(c0), s.e1), v = pow(fabs(s0), s.e1);
+  const double Z = pow(fabs(s.rz * n.z * t), s.i2);
+  const double ph1 = atan2(sgn(n.z) * Z, W);
+  double s1, c1;
   sincos(ph1, &s1, &c1);
-  const double pc1 = pow(fabs(c1), s.e2);
+  const double pc1 = pow(fabs(c1), s.e2), w = pow(fabs(s1), s.e2);
   D3 r;
-  r.x = sgn(c0) * s.rx * pow(fabs(c0), s.e1) * pc1;
-  r.y = sgn(s0) * s.ry * pow(fabs(s0), s.e1) * pc1;
-  r.z = sgn(s1) * s.rz * pow(fabs(s1), s.e2);
+  r.x = sgn(c0) * s.rx * u * pc1;
+  r.y = sgn(s0) * s.ry * v * pc1;
+  r.z = sgn(s1) * s.rz * w;
   return r;
 }
 // Superquadrics::isInside (Superquadrics.cpp:103-108); p is relative to the centre.
@@ -109,108 +113,11 @@ __device__ __forceinline__ void disfunction(const SqShape& A, const SqShape& B, 
   sincos(pa0, &sa0, &ca0);
   sincos(pa1, &sa1, &ca1);
   D3 contact = d3(ca0 * ca1, sa0 * ca1, sa1);
-  double ph0, ph1;
-  normal2phi(A, mulL(A.R, contact), ph0, ph1);
-  p1 = mulG(A.R, surface(A, ph0, ph1)) + A.pos;
-  normal2phi(B, (-1.0) * mulL(B.R, contact), ph0, ph1);
-  p2 = mulG(B.R, surface(B, ph0, ph1)) + B.pos;
+  p1 = mulG(A.R, supportLocal(A, mulL(A.R, contact))) + A.pos;
+  p2 = mulG(B.R, supportLocal(B, (-1.0) * mulL(B.R, contact))) + B.pos;
   D3 d = p2 - p1;
   center = 0.5 * (p1 + p2);
   if (dot(contact, d) > 0) stop_flag = true;
-}
-
-struct LMOut { int iters; int stop; };
-
-// lmder2 (Superquadrics_Ig2.cpp:1057-1354) with the JacfunctionApp forward-difference
-// Jacobian (:1033-1054) and opts {1.0, 1e-15, 1e-3, 1e-20}.
-__device__ __noinline__ LMOut lmder2(const SqShape& A, const SqShape& B, double p[2], int itmax, D3& p1, D3& p2,
-                                     D3& center, bool& touching, D3& contact) {
-  const double tau = 1.0, eps1 = 1e-15, eps2 = 1e-3, eps3 = 1e-20;
-  const double EPSILON = 1e-12, ONE_THIRD = 0.3333333333333334;
-  touching = true;
-  D3 p_f, pDp_f;
-  double jacTf0, jacTf1, diag0, diag1;
-  double j00, j01, j10, j11;  // J^T J
-  double Dp0 = 1e-7, Dp1 = 1e-7;
-  bool stop_flag = false;
-  double mu = 0, tmp;
-  double jacTf_inf, p_L2, Dp_L2, dF, dL, p_fL2, pDp_fL2;
-  int nu = 2, nu2, stop = 0, k;
-  disfunction(A, B, p[0], p[1], center, p1, p2, stop_flag);
-  p_f = p2 - p1;
-  p_fL2 = nrm(p_f);
-  if (!isfinite(p_fL2)) stop = 7;
-  for (k = 0; k < itmax && !stop; ++k) {
-    if (p_fL2 <= eps3) { stop = 6; break; }
-    if (stop_flag) { stop = 9; touching = false; break; }
-    {
-      double s0, c0, s1, c1;
-      sincos(p[0], &s0, &c0);
-      sincos(p[1], &s1, &c1);
-      contact = d3(c0 * c1, s0 * c1, s1);
-      double angle = dot(p_f, contact) / (nrm(p_f) * nrm(contact));
-      if (fabs(angle) > 0.95) { stop = 8; break; }
-    }
-    D3 f0, f1, f2;
-    disfunction(A, B, p[0], p[1], center, p1, p2, stop_flag);
-    f0 = p2 - p1;
-    disfunction(A, B, p[0] + Dp0, p[1], center, p1, p2, stop_flag);
-    f1 = p2 - p1;
-    disfunction(A, B, p[0], p[1] + Dp1, center, p1, p2, stop_flag);
-    f2 = p2 - p1;
-    const double J00 = (f1.x - f0.x) / Dp0, J10 = (f1.y - f0.y) / Dp0, J20 = (f1.z - f0.z) / Dp0;
-    const double J01 = (f2.x - f0.x) / Dp1, J11 = (f2.y - f0.y) / Dp1, J21 = (f2.z - f0.z) / Dp1;
-    j00 = J00 * J00 + (J10 * J10 + J20 * J20);
-    j01 = J00 * J01 + (J10 * J11 + J20 * J21);
-    j10 = J01 * J00 + (J11 * J10 + J21 * J20);
-    j11 = J01 * J01 + (J11 * J11 + J21 * J21);
-    (void)j10;
-    jacTf0 = J00 * (-1.0 * p_f.x) + (J10 * (-1.0 * p_f.y) + J20 * (-1.0 * p_f.z));
-    jacTf1 = J01 * (-1.0 * p_f.x) + (J11 * (-1.0 * p_f.y) + J21 * (-1.0 * p_f.z));
-    jacTf_inf = (fabs(jacTf0) > fabs(jacTf1) ? fabs(jacTf0) : fabs(jacTf1));
-    p_L2 = sqrt(p[0] * p[0] + p[1] * p[1]);
-    if (jacTf_inf <= eps1) { stop = 1; break; }
-    if (k == 0) {
-      tmp = (j00 > j11 ? j00 : j11);
-      mu = tau * tmp;
-    }
-    diag0 = j00; diag1 = j11;
-    while (1) {
-      j00 += mu;
-      j11 += mu;
-      const double n_a = j00 * j11 - j01 * j01;
-      Dp0 = (jacTf0 * j11 - jacTf1 * j01) / n_a;
-      Dp1 = (jacTf1 * j00 - jacTf0 * j01) / n_a;
-      Dp_L2 = sqrt(Dp0 * Dp0 + Dp1 * Dp1);
-      if (Dp_L2 < 1e-5) { stop = 2; break; }
-      const double q0 = p[0] + Dp0, q1 = p[1] + Dp1;
-      if (Dp_L2 >= (p_L2 + eps2) / (EPSILON * EPSILON)) { stop = 4; break; }
-      disfunction(A, B, q0, q1, center, p1, p2, stop_flag);
-      pDp_f = p2 - p1;
-      pDp_fL2 = nrm(pDp_f);
-      if (!isfinite(pDp_fL2)) { stop = 7; break; }
-      dL = Dp0 * (mu * Dp0 + jacTf0) + Dp1 * (mu * Dp1 + jacTf1);
-      dF = p_fL2 - pDp_fL2;
-      tmp = dF / dL;
-      if (tmp > 0.0) {
-        tmp = 1.0 - pow(2 * tmp - 1., 3.);
-        mu = mu * ((tmp >= ONE_THIRD) ? tmp : ONE_THIRD);
-        nu = 2;
-        p[0] = q0; p[1] = q1;
-        p_f = pDp_f;
-        p_fL2 = pDp_fL2;
-        break;
-      }
-      mu *= nu;
-      nu2 = (int)((unsigned)nu << 1);
-      if (nu2 <= nu) { stop = 5; break; }
-      nu = nu2;
-      j00 = diag0; j11 = diag1;
-    }
-  }
-  if (k >= itmax) stop = 3;
-  LMOut o; o.iters = k; o.stop = stop;
-  return o;
 }
 
 __device__ __forceinline__ void centerLine(D3 pos1, D3 pos2, double para[2]) {

@@ -64,7 +64,7 @@ struct Params {
   int lmSpread;   // idle lanes evaluate the points running searches ask for next
 };
 
-enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_EVAL32, E_EVAL64, E_NUM };
+enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_EVAL32, E_EVAL64, E_ROUNDS_MAX, E_NUM };
 
 struct SceneState {
   long long iter; double time;
@@ -839,9 +839,7 @@ __device__ void geomWallSq(GeomOut& g, bool isNew, double prevDepth, D3 oldNorma
   } else {
     SqShape B;
     makeShape(B, b);
-    double ph0, ph1;
-    normal2phi(B, -mulL(B.R, normal), ph0, ph1);
-    D3 point2 = mulG(B.R, surface(B, ph0, ph1)) + b.pos;
+    D3 point2 = mulG(B.R, supportLocal(B, -mulL(B.R, normal))) + b.pos;
     D3 p1 = point2;
     if (PA == 0) p1.x = wallc; else if (PA == 1) p1.y = wallc; else p1.z = wallc;
     D3 dd = point2 - p1;
@@ -1069,11 +1067,11 @@ enum { ST_INIT = 1, ST_PROBE0 = 2, ST_PROBE1 = 3, ST_TRIAL = 4 };
 
 struct LMLane {
   int e, st, phase, k, stop, nu;
-  bool stopFlag, touching, isNew;
+  bool stopFlag, touching, isNew, fromCenter;
   double p0, p1, q0, q1, mu, Dp0, Dp1, pfL2, pL2;
   double j00, j01, j11, diag0, diag1, jt0, jt1;
   D3 pf, f1, contact, P1, P2, C;
-  unsigned calls, iters, maxit;
+  unsigned calls, iters, maxit, rounds;
 };
 
 static const int LM_BS = 128;
@@ -1166,28 +1164,32 @@ __device__ __forceinline__ bool lmConsume(LMLane& L) {
   }
 }
 
-// Points lmder2 evaluates next, the requested one first, then the points that follow it
+// Points lmder2 evaluates next: the requested one in slot 0, then the points that follow it
 // under each outcome of the requested evaluation: after INIT the two probes at the start
 // point; after PROBE0 the second probe; after a TRIAL the two probes at the trial point
-// (accepted) and the next trial with mu*nu (rejected), recursively.  Every point is computed
-// with the operations the state machine itself uses, so a point it later asks for matches
-// bit for bit.  Returns the number of points written (at most S).
-__device__ __forceinline__ int lmPlan(const LMLane& L, double2* q, int S) {
+// (accepted), then the next trial with mu*nu (rejected) and its probes, and so on.  Along
+// every outcome the points asked for appear in increasing slot order (the order of the
+// consume pass).  Every point is computed with the operations the state machine itself
+// uses, so a point it later asks for matches bit for bit.  (Ordering the trials first when
+// the last iteration had rejections was measured slower.)  Writes q[i] and own[i] = lane
+// for each planned slot i < S.
+__device__ __forceinline__ void lmPlan(const LMLane& L, double2* q, int* own, int S, int lane) {
   int n = 0;
-  q[n++] = make_double2(L.q0, L.q1);
+  q[n] = make_double2(L.q0, L.q1); own[n++] = lane;
   if (L.st == ST_INIT) {
-    if (n < S) q[n++] = make_double2(L.p0 + 1e-7, L.p1);
-    if (n < S) q[n++] = make_double2(L.p0, L.p1 + 1e-7);
+    if (n < S) { q[n] = make_double2(L.p0 + 1e-7, L.p1); own[n++] = lane; }
+    if (n < S) { q[n] = make_double2(L.p0, L.p1 + 1e-7); own[n++] = lane; }
   } else if (L.st == ST_PROBE0) {
-    if (n < S) q[n++] = make_double2(L.p0, L.p1 + L.Dp1);
+    if (n < S) { q[n] = make_double2(L.p0, L.p1 + L.Dp1); own[n++] = lane; }
   } else if (L.st == ST_TRIAL) {
     double mu = L.mu, t0 = L.q0, t1 = L.q1, d0 = L.Dp0, d1 = L.Dp1;
     int nu = L.nu;
     while (n < S) {
-      q[n++] = make_double2(t0 + d0, t1);
+      q[n] = make_double2(t0 + d0, t1); own[n++] = lane;
       if (n >= S) break;
-      q[n++] = make_double2(t0, t1 + d1);
+      q[n] = make_double2(t0, t1 + d1); own[n++] = lane;
       if (n >= S) break;
+      // the trial after a rejection of this one (lmConsume's rejection branch, then lmInner)
       mu *= nu;
       const int nu2 = (int)((unsigned)nu << 1);
       if (nu2 <= nu) break;
@@ -1200,10 +1202,9 @@ __device__ __forceinline__ int lmPlan(const LMLane& L, double2* q, int S) {
       if (Dp_L2 < 1e-5) break;
       t0 = L.p0 + d0; t1 = L.p1 + d1;
       if (Dp_L2 >= (L.pL2 + 1e-3) / (1e-12 * 1e-12)) break;
-      q[n++] = make_double2(t0, t1);
+      q[n] = make_double2(t0, t1); own[n++] = lane;
     }
   }
-  return n;
 }
 
 __device__ __forceinline__ bool sameBits(double2 a, double q0, double q1) {
@@ -1215,29 +1216,36 @@ __device__ __forceinline__ bool sameBits(double2 a, double q0, double q1) {
 // the law.  Returns true when the contact is finished.
 __device__ __forceinline__ bool lmCallEnd(const Dev& d, LMLane& L, const SqShape& A, const SqShape& B, Counters& cnt) {
   const SceneState& S = *d.S;
-  L.calls++; L.iters += L.k; L.maxit += (L.stop == 3);
-  bool restart = false;
-  if (L.phase == 0) {
-    L.phase = 1;
-    if ((isnan(L.p0) || isnan(L.p1) || 7 == L.stop) && L.touching) restart = true;
-  } else if (L.phase == 1) {
-    L.phase = 3;
-    if (L.touching && 10.0 * nrm(L.P2 - L.P1) > A.rmax && (!isInside(A, L.P2 - A.pos) || !isInside(B, L.P1 - B.pos))) {
-      L.phase = 2; restart = true;
+  for (;;) {
+    L.calls++; L.iters += L.k; L.maxit += (L.stop == 3);
+    bool restart = false;
+    if (L.phase == 0) {
+      L.phase = 1;
+      if ((isnan(L.p0) || isnan(L.p1) || 7 == L.stop) && L.touching) restart = true;
+    } else if (L.phase == 1) {
+      L.phase = 3;
+      if (L.touching && 10.0 * nrm(L.P2 - L.P1) > A.rmax && (!isInside(A, L.P2 - A.pos) || !isInside(B, L.P1 - B.pos))) {
+        L.phase = 2; restart = true;
+      }
+    } else L.phase = 3;
+    if (!restart && L.phase == 1) {  // no NaN restart: continue with the local-minimum check
+      L.phase = 3;
+      if (L.touching && 10.0 * nrm(L.P2 - L.P1) > A.rmax && (!isInside(A, L.P2 - A.pos) || !isInside(B, L.P1 - B.pos))) {
+        L.phase = 2; restart = true;
+      }
     }
-  } else L.phase = 3;
-  if (!restart && L.phase == 1) {  // no NaN restart: continue with the local-minimum check
-    L.phase = 3;
-    if (L.touching && 10.0 * nrm(L.P2 - L.P1) > A.rmax && (!isInside(A, L.P2 - A.pos) || !isInside(B, L.P1 - B.pos))) {
-      L.phase = 2; restart = true;
+    if (!restart) break;
+    if (!L.fromCenter) {
+      double para[2];
+      centerLine(A.pos, B.pos, para);
+      L.p0 = para[0]; L.p1 = para[1];
+      L.fromCenter = true;
+      lmStartSolve(L);
+      return false;
     }
-  }
-  if (restart) {
-    double para[2];
-    centerLine(A.pos, B.pos, para);
-    L.p0 = para[0]; L.p1 = para[1];
-    lmStartSolve(L);
-    return false;
+    // The restarted call would start where the call that just ended started (the centre
+    // line), from the state lmStartSolve sets: it is the same computation, and its outcome
+    // is the one at hand.  It is counted as run, and the restart rules go on from there.
   }
   // end of Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go, then Ip2 + law
   const int e = L.e;
@@ -1270,6 +1278,80 @@ __device__ __forceinline__ bool lmCallEnd(const Dev& d, LMLane& L, const SqShape
   return true;
 }
 
+// One Disfunction evaluation (Superquadrics_Ig2.cpp:622-687) by a group of six lanes:
+// lanes 0-2 of the group compute body A's support point, lanes 3-5 body B's, and the
+// independent pow calls of each level of supportLocal run on separate lanes (Y,X,W |
+// t,u,v | Z | pc1,w), so that the dependency chain is 4 pow + 2 atan2 + 3 sincos instead of
+// 18 pow + 4 atan2 + 6 sincos.  Every value is computed with the operations of
+// disfunction/supportLocal (bitwise the same results).  Lane 0 of the group ends with p1,
+// p2 and the stop predicate.  All 32 lanes call it (full-warp shuffles); g0 is the group's
+// first lane, sub the lane's place in it.  (Four-lane groups, eight points per round, were
+// measured slower: one more pow on the chain.)
+static const int COOP_LANES = 6, COOP_POINTS = 5;
+__device__ __forceinline__ void coopEval(const SqShape& A, const SqShape& B, double q0, double q1, int g0, int sub,
+                                         D3& p1, D3& p2, bool& flag) {
+  const unsigned FULL = 0xffffffffu;
+  const int body = sub >= 3 ? 1 : 0;
+  const int k = sub - 3 * body;
+  const int gb = g0 + 3 * body;
+  const SqShape& s = body ? B : A;
+  double sv, cv;
+  sincos(sub == 1 ? q1 : q0, &sv, &cv);
+  const double sa0 = __shfl_sync(FULL, sv, g0), ca0 = __shfl_sync(FULL, cv, g0);
+  const double sa1 = __shfl_sync(FULL, sv, g0 + 1), ca1 = __shfl_sync(FULL, cv, g0 + 1);
+  const D3 contact = d3(ca0 * ca1, sa0 * ca1, sa1);
+  D3 n = mulL(s.R, contact);
+  if (body) n = (-1.0) * n;
+  const double v1 = pow(k == 0 ? fabs(s.ry * n.y) : fabs(s.rx * n.x), k == 2 ? s.i2 : s.i1);
+  const double Y = __shfl_sync(FULL, v1, gb), X = __shfl_sync(FULL, v1, gb + 1), W = __shfl_sync(FULL, v1, gb + 2);
+  const double ph0 = atan2(sgn(n.y) * Y, sgn(n.x) * X);
+  double s0, c0;
+  sincos(ph0, &s0, &c0);
+  const double v2 = pow(k == 2 ? fabs(s0) : fabs(c0), k == 0 ? s.a1 : s.e1);
+  const double t = __shfl_sync(FULL, v2, gb), u = __shfl_sync(FULL, v2, gb + 1), v = __shfl_sync(FULL, v2, gb + 2);
+  const double Z = pow(fabs(s.rz * n.z * t), s.i2);
+  const double ph1 = atan2(sgn(n.z) * Z, W);
+  double s1, c1;
+  sincos(ph1, &s1, &c1);
+  const double v3 = pow(k == 1 ? fabs(s1) : fabs(c1), s.e2);
+  const double pc1 = __shfl_sync(FULL, v3, gb), w = __shfl_sync(FULL, v3, gb + 1);
+  D3 r;
+  r.x = sgn(c0) * s.rx * u * pc1;
+  r.y = sgn(s0) * s.ry * v * pc1;
+  r.z = sgn(s1) * s.rz * w;
+  const D3 p = mulG(s.R, r) + s.pos;
+  const double x2 = __shfl_sync(FULL, p.x, g0 + 3), y2 = __shfl_sync(FULL, p.y, g0 + 3), z2 = __shfl_sync(FULL, p.z, g0 + 3);
+  p1 = p;
+  p2 = d3(x2, y2, z2);
+  const D3 dd = p2 - p1;
+  flag = dot(contact, dd) > 0;
+}
+
+// Slot allocation of one evaluation round: every searching lane (in) gets one slot, the rest
+// of the budget goes evenly to all, the remainder to the searches that have run the most
+// rounds.  Returns the lane's slot count (spc) and first slot (base), and the round's
+// largest slot count (jmax) for the uniform consume pass.
+__device__ __forceinline__ void allocSlots(bool in, unsigned rounds, int budget, int& spc, int& base, int& jmax) {
+  const int lane = threadIdx.x & 31;
+  const unsigned act = __ballot_sync(0xffffffffu, in);
+  const int nA = __popc(act);
+  const int share = budget / nA, extra = budget - share * nA;
+  const unsigned prio = in ? rounds : 0u;
+  int before = 0;
+  for (int o = 0; o < 32; o++) {
+    const unsigned po = __shfl_sync(0xffffffffu, prio, o);
+    if ((act >> o) & 1u) before += (po > prio || (po == prio && o < lane)) ? 1 : 0;
+  }
+  spc = in ? share + (before < extra ? 1 : 0) : 0;
+  base = spc;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, base, o);
+    if (lane >= o) base += y;
+  }
+  base -= spc;
+  jmax = share + (extra > 0 ? 1 : 0);
+}
+
 // Pass 2, FP64.  Rounds of one Disfunction evaluation per lane.  While the queue has work,
 // every lane evaluates the point its own search asks for.  Once the queue is drained, the
 // lanes left without a contact evaluate, for the searches still running in their warp, the
@@ -1277,8 +1359,10 @@ __device__ __forceinline__ bool lmCallEnd(const Dev& d, LMLane& L, const SqShape
 // order, every evaluation whose point is the one it asks for.  A search with 31 idle lanes
 // beside it thus advances one whole iteration (trial + two probes, or a run of rejected
 // trials) per round instead of one evaluation, which shortens the dependency chain of the
-// longest searches that bound the kernel.  Results are those of the one-point rounds: an
-// evaluation depends only on its point and the two shapes.
+// longest searches that bound the kernel.  While at most COOP_POINTS searches run in the
+// warp, each point is evaluated by a group of six lanes (coopEval), which shortens each
+// round as well.  Results are those of the one-point rounds: an evaluation depends only on
+// its point and the two shapes.
 __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
   __shared__ SqShape shA[LM_BS], shB[LM_BS];
   __shared__ double2 slotQ[LM_BS];
@@ -1290,6 +1374,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
   const bool spread = d.prm->lmSpread != 0;
   Counters cnt = {0, 0, 0, 0, 0};
   unsigned long long ev64 = 0;
+  unsigned roundsMax = 0;
   LMLane L;
   bool active = false, exhausted = false;
   while (true) {
@@ -1317,8 +1402,9 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
           L.isNew = !(fl & F_GEOM);
           if (L.isNew) { double para[2]; centerLine(A.pos, B.pos, para); L.p0 = para[0]; L.p1 = para[1]; }
           else { const double2 an = d.A.angle[L.e]; L.p0 = an.x; L.p1 = an.y; }
+          L.fromCenter = L.isNew;
           L.contact = d3(0, 0, 0); L.P1 = d3(0, 0, 0); L.P2 = d3(0, 0, 0); L.C = d3(0, 0, 0);
-          L.phase = 0; L.calls = 0; L.iters = 0; L.maxit = 0;
+          L.phase = 0; L.calls = 0; L.iters = 0; L.maxit = 0; L.rounds = 0;
           lmStartSolve(L);
           active = true;
         } else exhausted = true;
@@ -1326,45 +1412,72 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
     }
     const unsigned act = __ballot_sync(0xffffffffu, active);
     if (!act) break;
-    // slots per running search: 1 while the queue has work, else the warp's lanes shared out
-    const int spc = (spread && __any_sync(0xffffffffu, exhausted)) ? 32 / __popc(act) : 1;
-    const int base = __popc(act & ((1u << lane) - 1)) * spc;
+    // Points per running search: 1 while the queue has work.  Once it is drained, the warp's
+    // evaluation slots (five groups of six lanes, coopEval, while at most COOP_POINTS
+    // searches run, else 32 single lanes) are shared out evenly, the remainder going to the
+    // searches that have run the most rounds, the likeliest to bound the kernel.
+    const int nA = __popc(act);
+    const bool drained = spread && __any_sync(0xffffffffu, exhausted);
+    const bool coop = drained && nA <= COOP_POINTS;
+    int spc, base, jmax;
+    allocSlots(active, L.rounds, drained ? (coop ? COOP_POINTS : 32) : nA, spc, base, jmax);
     slotOwner[threadIdx.x] = -1;
     __syncwarp();
-    if (active) {
-      const int n = lmPlan(L, &slotQ[wbase + base], spc);
-      for (int j = 0; j < n; j++) slotOwner[wbase + base + j] = lane;
-    }
+    if (active) lmPlan(L, &slotQ[wbase + base], &slotOwner[wbase + base], spc, lane);
     __syncwarp();
     D3 P1 = d3(0, 0, 0), P2 = d3(0, 0, 0);
     bool flag = false;
-    const int own = slotOwner[threadIdx.x];
-    if (own >= 0) {
-      const double2 q = slotQ[threadIdx.x];
-      D3 C;
-      disfunction(shA[wbase + own], shB[wbase + own], q.x, q.y, C, P1, P2, flag);
-      ev64++;
+    if (coop) {
+      // group g of six lanes evaluates slot g; lanes 30-31 and groups without a point mirror
+      // slot 0 (its owner always exists) so that every lane computes on valid inputs
+      const int graw = lane / COOP_LANES;
+      const int grp = graw < COOP_POINTS ? graw : 0;
+      const int sub = graw < COOP_POINTS ? lane - grp * COOP_LANES : lane - COOP_POINTS * COOP_LANES;
+      const int o = slotOwner[wbase + grp];
+      const bool has = graw < COOP_POINTS && o >= 0;
+      const int slot = has ? grp : 0;
+      const int src = wbase + slotOwner[wbase + slot];
+      const double2 q = slotQ[wbase + slot];
+      coopEval(shA[src], shB[src], q.x, q.y, grp * COOP_LANES, sub, P1, P2, flag);
+      if (has && sub == 0) ev64++;
+    } else {
+      const int own = slotOwner[threadIdx.x];
+      if (own >= 0) {
+        const double2 q = slotQ[threadIdx.x];
+        D3 C;
+        disfunction(shA[wbase + own], shB[wbase + own], q.x, q.y, C, P1, P2, flag);
+        ev64++;
+      }
     }
-    for (int j = 0; j < spc; j++) {
-      const int src = active ? base + j : lane;
+    if (active) L.rounds++;
+    for (int j = 0; j < jmax; j++) {
+      const int si = base + j;
+      const bool mine = j < spc;
+      const int src = mine ? (coop ? si * COOP_LANES : si) : lane;
       const double x1 = __shfl_sync(0xffffffffu, P1.x, src), y1 = __shfl_sync(0xffffffffu, P1.y, src),
                    z1 = __shfl_sync(0xffffffffu, P1.z, src);
       const double x2 = __shfl_sync(0xffffffffu, P2.x, src), y2 = __shfl_sync(0xffffffffu, P2.y, src),
                    z2 = __shfl_sync(0xffffffffu, P2.z, src);
       const bool f = __shfl_sync(0xffffffffu, (int)flag, src) != 0;
-      if (active && slotOwner[wbase + src] == lane && sameBits(slotQ[wbase + src], L.q0, L.q1)) {
+      if (mine && active && slotOwner[wbase + si] == lane && sameBits(slotQ[wbase + si], L.q0, L.q1)) {
         L.P1 = d3(x1, y1, z1);
         L.P2 = d3(x2, y2, z2);
         L.C = 0.5 * (L.P1 + L.P2);
         if (f) L.stopFlag = true;
-        if (!lmConsume(L) && lmCallEnd(d, L, shA[threadIdx.x], shB[threadIdx.x], cnt)) active = false;
+        if (!lmConsume(L) && lmCallEnd(d, L, shA[threadIdx.x], shB[threadIdx.x], cnt)) {
+          active = false;
+          roundsMax = max(roundsMax, L.rounds);
+        }
       }
     }
     __syncwarp();
   }
   flushCounters(d, cnt);
-  for (int o = 16; o > 0; o >>= 1) ev64 += __shfl_down_sync(0xffffffffu, ev64, o);
-  if (lane == 0) atomicAdd(&d.S->err[E_EVAL64], ev64);
+  for (int o = 16; o > 0; o >>= 1) {
+    ev64 += __shfl_down_sync(0xffffffffu, ev64, o);
+    roundsMax = max(roundsMax, __shfl_down_sync(0xffffffffu, roundsMax, o));
+  }
+  if (lane == 0) { atomicAdd(&d.S->err[E_EVAL64], ev64); atomicMax(&d.S->err[E_ROUNDS_MAX], (unsigned long long)roundsMax); }
 }
 
 // ---------------------------------------------------------------------------
@@ -1495,13 +1608,23 @@ __device__ __forceinline__ void buildShapes32(ShapePair& sp, const Dev& d, int i
   shapeInitF(sp.f.B, a2.x, a2.y, a2.z, e2.x, e2.y, quatToRot(o2.x, o2.y, o2.z, o2.w), rel);
 }
 
+// Pass 2, mixed form.  Each round, the lanes whose search is in its FP32 phase take one FP32
+// evaluation each; then the searches in their FP64 phase share the warp's 32 lanes for FP64
+// evaluations (FP32-phase and idle lanes help: an FP64 warp instruction costs the same
+// whatever the number of lanes taking part), planned and consumed as in k_contacts_lm.
+// A restart from the centre line that would repeat a call which also started there is
+// counted, not run (same computation, same outcome).
 __global__ void __launch_bounds__(LM_BS) k_contacts_lm_mixed(Dev d) {
   __shared__ ShapePair shp[LM_BS];
+  __shared__ double2 slotQ[LM_BS];
+  __shared__ int slotOwner[LM_BS];
   ShapePair& SP = shp[threadIdx.x];
   const SceneState& S = *d.S;
   const int count = S.lmCount;
   const double dt = d.prm->dt;
   const int lane = threadIdx.x & 31;
+  const int wbase = threadIdx.x & ~31;
+  const bool spread = d.prm->lmSpread != 0;
   Counters cnt = {0, 0, 0, 0, 0};
   unsigned long long ev32 = 0, ev64 = 0;
   LMLane L;
@@ -1533,6 +1656,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_mixed(Dev d) {
           } else { const double2 an = d.A.angle[L.e]; L.p0 = an.x; L.p1 = an.y; }
           L.contact = d3(0, 0, 0); L.P1 = d3(0, 0, 0); L.P2 = d3(0, 0, 0); L.C = d3(0, 0, 0);
           L.phase = 0; L.calls = 0; L.iters = 0; L.maxit = 0; L.touching = true;
+          L.fromCenter = L.isNew; L.rounds = 0;
           buildShapes32(SP, d, id1, id2, shift2);
           lmfStart(F, (float)L.p0, (float)L.p1);
           fp32 = true;
@@ -1563,33 +1687,97 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_mixed(Dev d) {
           fp32 = false;
         }
       }
-    } else if (active) {
-      disfunction(SP.d.A, SP.d.B, L.q0, L.q1, L.C, L.P1, L.P2, L.stopFlag);
-      ev64++;
-      bool more = lmConsume(L);
-      if (more && --budget <= 0) { L.stop = 3; more = false; }
-      if (!more) {
-        L.calls++; L.iters += L.k; L.maxit += (L.stop == 3);
-        bool restart = false;
-        if (L.phase == 0) {
-          L.phase = 1;
-          if ((isnan(L.p0) || isnan(L.p1) || 7 == L.stop) && L.touching) restart = true;
+    }
+    // FP64 round
+    const bool in64 = active && !fp32 && !fin;
+    const unsigned act64 = __ballot_sync(0xffffffffu, in64);
+    if (act64) {
+      const int nA = __popc(act64);
+      const bool coop = spread && nA <= COOP_POINTS;
+      int spc, base, jmax;
+      allocSlots(in64, L.rounds, spread ? (coop ? COOP_POINTS : 32) : nA, spc, base, jmax);
+      slotOwner[threadIdx.x] = -1;
+      __syncwarp();
+      if (in64) { L.rounds++; lmPlan(L, &slotQ[wbase + base], &slotOwner[wbase + base], spc, lane); }
+      __syncwarp();
+      D3 P1 = d3(0, 0, 0), P2 = d3(0, 0, 0);
+      bool flag = false;
+      if (coop) {
+        // group g of six lanes evaluates slot g; lanes 30-31 and groups without a point
+        // mirror slot 0 (its owner always exists) so that every lane computes on valid inputs
+        const int graw = lane / COOP_LANES;
+        const int grp = graw < COOP_POINTS ? graw : 0;
+        const int sub = graw < COOP_POINTS ? lane - grp * COOP_LANES : lane - COOP_POINTS * COOP_LANES;
+        const int o = slotOwner[wbase + grp];
+        const bool has = graw < COOP_POINTS && o >= 0;
+        const int slot = has ? grp : 0;
+        const int src = wbase + slotOwner[wbase + slot];
+        const double2 q = slotQ[wbase + slot];
+        coopEval(shp[src].d.A, shp[src].d.B, q.x, q.y, grp * COOP_LANES, sub, P1, P2, flag);
+        if (has && sub == 0) ev64++;
+      } else {
+        const int own = slotOwner[threadIdx.x];
+        if (own >= 0) {
+          const double2 q = slotQ[threadIdx.x];
+          D3 C;
+          disfunction(shp[wbase + own].d.A, shp[wbase + own].d.B, q.x, q.y, C, P1, P2, flag);
+          ev64++;
         }
-        if (!restart && L.phase == 1) {
-          L.phase = 3;
-          if (L.touching && 10.0 * nrm(L.P2 - L.P1) > SP.d.A.rmax &&
-              (!isInside(SP.d.A, L.P2 - SP.d.A.pos) || !isInside(SP.d.B, L.P1 - SP.d.B.pos))) {
-            L.phase = 2; restart = true;
+      }
+      __syncwarp();
+      bool mine64 = in64;
+      for (int j = 0; j < jmax; j++) {
+        const int si = base + j;
+        const bool mine = mine64 && j < spc;
+        const int src = mine ? (coop ? si * COOP_LANES : si) : lane;
+        const double x1 = __shfl_sync(0xffffffffu, P1.x, src), y1 = __shfl_sync(0xffffffffu, P1.y, src),
+                     z1 = __shfl_sync(0xffffffffu, P1.z, src);
+        const double x2 = __shfl_sync(0xffffffffu, P2.x, src), y2 = __shfl_sync(0xffffffffu, P2.y, src),
+                     z2 = __shfl_sync(0xffffffffu, P2.z, src);
+        const bool f = __shfl_sync(0xffffffffu, (int)flag, src) != 0;
+        if (mine && slotOwner[wbase + si] == lane && sameBits(slotQ[wbase + si], L.q0, L.q1)) {
+          L.P1 = d3(x1, y1, z1);
+          L.P2 = d3(x2, y2, z2);
+          L.C = 0.5 * (L.P1 + L.P2);
+          if (f) L.stopFlag = true;
+          bool more = lmConsume(L);
+          if (more && --budget <= 0) { L.stop = 3; more = false; }
+          if (!more) {
+            mine64 = false;   // this call ended: the rest of the round's slots are stale
+            for (;;) {
+              L.calls++; L.iters += L.k; L.maxit += (L.stop == 3);
+              bool restart = false;
+              if (L.phase == 0) {
+                L.phase = 1;
+                if ((isnan(L.p0) || isnan(L.p1) || 7 == L.stop) && L.touching) restart = true;
+              }
+              if (!restart && L.phase == 1) {
+                L.phase = 3;
+                if (L.touching && 10.0 * nrm(L.P2 - L.P1) > SP.d.A.rmax &&
+                    (!isInside(SP.d.A, L.P2 - SP.d.A.pos) || !isInside(SP.d.B, L.P1 - SP.d.B.pos))) {
+                  L.phase = 2; restart = true;
+                }
+              } else if (!restart) L.phase = 3;
+              if (!restart) { fin = true; break; }
+              if (!L.fromCenter) {
+                double para[2];
+                centerLine(SP.d.A.pos, SP.d.B.pos, para);
+                L.p0 = para[0]; L.p1 = para[1];
+                L.fromCenter = true;
+                fp32 = true;   // FP32 shapes are rebuilt after the round (helpers may still read these)
+                break;
+              }
+              // the restarted search (FP32 then FP64 from the centre line) would repeat the
+              // one that just ended: count it and go on with its outcome
+              L.iters += F.k;
+            }
           }
-        } else if (!restart) L.phase = 3;
-        if (restart) {
-          double para[2];
-          centerLine(SP.d.A.pos, SP.d.B.pos, para);
-          L.p0 = para[0]; L.p1 = para[1];
-          buildShapes32(SP, d, id1, id2, shift2);
-          lmfStart(F, (float)L.p0, (float)L.p1);
-          fp32 = true;
-        } else fin = true;
+        }
+      }
+      __syncwarp();
+      if (in64 && fp32) {  // restart: FP32 search from the centre line
+        buildShapes32(SP, d, id1, id2, shift2);
+        lmfStart(F, (float)L.p0, (float)L.p1);
       }
     }
     if (fin) {
@@ -2314,6 +2502,7 @@ sqdem_status sqdem_sync(sqdem_ctx* c, sqdem_report* r) {
     r->lm_maxiter = (long long)e[E_LM_MAX]; r->overflow = (long long)e[E_OVERFLOW];
     r->collider_runs = (long long)e[E_COLLIDER_RUNS]; r->steps = (long long)e[E_STEPS];
     r->evals_fp32 = (long long)e[E_EVAL32]; r->evals_fp64 = (long long)e[E_EVAL64];
+    r->lm_rounds_max = (long long)e[E_ROUNDS_MAX];
   }
   if (e[E_OVERFLOW]) return fail(c, SQDEM_ERR_CAPACITY, "contact table or candidate buffer overflow; increase contacts_per_body");
   return SQDEM_OK;

@@ -190,17 +190,18 @@ def test_deterministic(gpu):
     assert np.array_equal(a.interactions(True), b.interactions(True))
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("kind", ["walled", "periodic"])
-def test_lm_spread_rounds_equal_one_point_rounds(gpu, kind):
-    """Idle lanes evaluating the points running searches ask for next changes nothing."""
+def test_lm_spread_rounds_equal_one_point_rounds(gpu, kind, precision):
+    """Spare lanes evaluating the points running searches ask for next changes nothing."""
     spec = dense_spec(seed=7, n=400) if kind == "walled" else periodic_spec(seed=4, n=400)
-    a, b = engine_for(spec), engine_for(spec)
+    a, b = engine_for(spec, precision=precision), engine_for(spec, precision=precision)
     b.set_lm_spread(False)
     a.step(40); b.step(40)
     ra, rb = a.sync(), b.sync()
     assert np.array_equal(a.body_state(), b.body_state())
     assert np.array_equal(a.interactions(True), b.interactions(True))
-    for k in ("lm_calls", "lm_iterations", "lm_maxiter", "nan_normals", "nan_forces"):
+    for k in ("lm_calls", "lm_iterations", "lm_maxiter", "nan_normals", "nan_forces", "evals_fp32"):
         assert ra[k] == rb[k], k
     assert ra["evals_fp64"] >= rb["evals_fp64"] > 0
 
