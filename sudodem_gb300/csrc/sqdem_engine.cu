@@ -116,6 +116,7 @@ struct Dev {
   int* lmQueue;
   // grid
   int* bodyCell; int* cellCount; int* cellStart; int* cellFill; int* cellBodies;
+  float4* cellBox;   // per cell slot: bound centre (xyz) and, in the next entry, half extents (xyz)
   int* scanTmp;
   unsigned long long* bbPart;
 };
@@ -452,6 +453,28 @@ __global__ void k_cell_scatter(Dev d) {
   if (cell < 0) return;
   int slot = d.cellStart[cell] + atomicAdd(&d.cellFill[cell], 1);
   d.cellBodies[slot] = b;
+  const double4 mn = d.bmin[b], mx = d.bmax[b];
+  d.cellBox[2 * slot] = make_float4((float)(0.5 * (mn.x + mx.x)), (float)(0.5 * (mn.y + mx.y)), (float)(0.5 * (mn.z + mx.z)), 0.f);
+  d.cellBox[2 * slot + 1] = make_float4((float)(0.5 * (mx.x - mn.x)), (float)(0.5 * (mx.y - mn.y)), (float)(0.5 * (mx.z - mn.z)), 0.f);
+}
+
+// FP32 pre-filter of the candidate search: true when the two bounds cannot overlap, in any
+// periodic image (minimum-image distance of the centres above the summed half extents on
+// some axis).  The margin (1e-6 of the coordinates' scale, ~20 FP32 ulps) keeps it
+// conservative, so the exact FP64 tests below decide every pair it lets through and the
+// pair set is unchanged; it spares most candidates the 18 FP64 divisions of overlapPeri.
+__device__ __forceinline__ bool boxesApart(float4 ca, float4 ha, float4 cb, float4 hb, bool periodic, const float* L,
+                                           const float* invL) {
+  const float c1[3] = {ca.x, ca.y, ca.z}, h1[3] = {ha.x, ha.y, ha.z};
+  const float c2[3] = {cb.x, cb.y, cb.z}, h2[3] = {hb.x, hb.y, hb.z};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float dc = c2[k] - c1[k];
+    float scale = fabsf(c1[k]) + fabsf(c2[k]) + h1[k] + h2[k];
+    if (periodic) { dc -= L[k] * rintf(dc * invL[k]); scale += L[k]; }
+    if (fabsf(dc) > h1[k] + h2[k] + 1e-6f * scale) return true;
+  }
+  return false;
 }
 
 // closed overlap test, InsertionSortCollider::spatialOverlap (InsertionSortCollider.hpp:166-171)
@@ -513,12 +536,17 @@ __device__ __forceinline__ int orientNew(const Dev& d, int i, int j, int initSor
 // i's previous row gives the new row length: old entries survive if real or overlapping
 // (conditionalyEraseNonReal), new overlapping pairs are inserted when the sort would insert
 // them.
+// Threads take the particles in cell order (cellBodies), so that a warp scans neighbouring
+// cells and its loads of cellBodies/cellBox overlap; bodies outside the grid (walls) get an
+// empty row from the thread of their own index.
 __global__ void k_candidates(Dev d) {
   const SceneState& S = *d.S;
   if (!S.runCollider) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.N) return;
-  if (d.info[i].x != KIND_SQ) { d.rowCount[i] = 0; d.candCount[i] = 0; return; }
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.N) return;
+  if (d.bodyCell[t] < 0) { d.rowCount[t] = 0; d.candCount[t] = 0; }
+  if (t >= d.cellStart[S.nCells]) return;
+  const int i = d.cellBodies[t];
   const double4 imn = d.bmin[i], imx = d.bmax[i];
   int* cand = d.cand + (size_t)i * d.MAXC;
   int n = 0; bool over = false;
@@ -526,6 +554,11 @@ __global__ void k_candidates(Dev d) {
   bodyCellCoords(S, imn, imx, cx, cy, cz);
   int seen[27];
   int nseen = 0;
+  const float4 ci = make_float4((float)(0.5 * (imn.x + imx.x)), (float)(0.5 * (imn.y + imx.y)), (float)(0.5 * (imn.z + imx.z)), 0.f);
+  const float4 hi = make_float4((float)(0.5 * (imx.x - imn.x)), (float)(0.5 * (imx.y - imn.y)), (float)(0.5 * (imx.z - imn.z)), 0.f);
+  float Lf[3] = {1.f, 1.f, 1.f}, invLf[3] = {1.f, 1.f, 1.f};
+  if (S.periodic)
+    for (int k = 0; k < 3; k++) { Lf[k] = (float)S.cellSize[k]; invLf[k] = 1.f / Lf[k]; }
   for (int dz = -1; dz <= 1; dz++) {
     int z = cz + dz;
     if (S.periodic) z = (z + S.dim[2]) % S.dim[2]; else if (z < 0 || z >= S.dim[2]) continue;
@@ -544,6 +577,7 @@ __global__ void k_candidates(Dev d) {
         for (int k = s0; k < e0; k++) {
           int j = d.cellBodies[k];
           if (j <= i) continue;
+          if (boxesApart(ci, hi, d.cellBox[2 * k], d.cellBox[2 * k + 1], S.periodic != 0, Lf, invLf)) continue;
           bool ov;
           if (S.periodic) { int per[3]; ov = overlapPeri(S, imn, imx, d.bmin[j], d.bmax[j], per); }
           else ov = overlapClosed(imn, imx, d.bmin[j], d.bmax[j]);
@@ -2405,7 +2439,7 @@ sqdem_status sqdem_set_bodies(sqdem_ctx* c, int n, const int* kind, const double
   CK(dalloc(c, &d.ww, std::max(d.W * d.W, 1)));
   CK(dalloc(c, &d.lmQueue, d.Pcap));
   CK(dalloc(c, &d.bodyCell, n)); CK(dalloc(c, &d.cellCount, d.Gmax + 1)); CK(dalloc(c, &d.cellStart, d.Gmax + 1));
-  CK(dalloc(c, &d.cellFill, d.Gmax + 1)); CK(dalloc(c, &d.cellBodies, n));
+  CK(dalloc(c, &d.cellFill, d.Gmax + 1)); CK(dalloc(c, &d.cellBodies, n)); CK(dalloc(c, &d.cellBox, 2 * (size_t)n));
   CK(dalloc(c, &d.scanTmp, nblk((long)std::max(std::max(d.Gmax, d.Pcap), d.N) + 2, SCAN_TILE) + 2));
   // host-side body arrays
   std::vector<double4> v[5];
