@@ -120,7 +120,8 @@ sqdem_status sqdem_set_materials(sqdem_ctx* ctx, int n, const double* Kn, const 
  * (ignored for particles); state = SQDEM_BODY_STRIDE doubles per body (force/torque and bound
  * columns are ignored: bounds start unset, as after NewSuperquadrics_rot2 and utils.wall,
  * py/_superquadrics_utils.cpp:354-380, py/utils.py:311-327).  Mass and inertia are taken
- * from the state columns; sqdem_shape_props gives the reference's values. */
+ * from the state columns; sqdem_shape_props gives the reference's values.  At most 64 walls
+ * (SQDEM_ERR_CAPACITY beyond). */
 sqdem_status sqdem_set_bodies(sqdem_ctx* ctx, int n, const int* kind, const double* shape5,
                               const int* wall_axis_sense, const int* mat, const int* isSphere,
                               const double* state);

@@ -111,7 +111,7 @@ struct Dev {
   int* rowStart; int* rowStartNew; int* rowCount;
   int* cand; int* candCount;
   int* pCount; int* pStart; int* pFill; int* pList;
-  int* wCount; int* wList;
+  int* wCount; int* wList; int* wBlk;
   int2* ww;
   int* lmQueue;
   // grid
@@ -477,6 +477,38 @@ __device__ __forceinline__ bool boxesApart(float4 ca, float4 ha, float4 cb, floa
   return false;
 }
 
+// InsertionSortCollider::spatialOverlapPeri (the exact test, overlapPeri) decided from FP32
+// bound centres and half extents wherever its outcome does not hang on rounding: returns 1
+// (overlap), -1 (no overlap) or 0 (undecided: run overlapPeri).  Per axis, with d the offset
+// of body 1's lower bound after body 2's modulo the cell size L: for d < L/2 the exact test's
+// window starts at body 2's lower bound, no bound straddles it, and the axis overlaps iff
+// d <= len2; for d > L/2 the window starts at body 1's lower bound and the axis overlaps iff
+// L - d <= len1.  Within a margin (1e-5 of the coordinates' scale, ~40x the FP32 error) of
+// d = 0, L/2 or L, of d = len2 (L - d = len1), or for a body longer than L/2, the exact test
+// decides.  Any axis that is clearly apart makes the pair apart, as in the exact test.
+__device__ __forceinline__ int overlapPeriFast(float4 c1, float4 h1, float4 c2, float4 h2, const float* L,
+                                               const float* invL) {
+  const float a1[3] = {c1.x, c1.y, c1.z}, b1[3] = {h1.x, h1.y, h1.z};
+  const float a2[3] = {c2.x, c2.y, c2.z}, b2[3] = {h2.x, h2.y, h2.z};
+  int res = 1;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float D = L[k];
+    const float len1 = 2.f * b1[k], len2 = 2.f * b2[k];
+    const float eps = 1e-5f * (fabsf(a1[k]) + fabsf(a2[k]) + b1[k] + b2[k] + D);
+    float dd = (a1[k] - b1[k]) - (a2[k] - b2[k]);
+    dd -= D * floorf(dd * invL[k]);
+    if (!(len1 < 0.5f * D - eps && len2 < 0.5f * D - eps && dd > eps && dd < D - eps && fabsf(dd - 0.5f * D) > eps)) {
+      res = 0;
+      continue;
+    }
+    const float gap = dd < 0.5f * D ? dd - len2 : (D - dd) - len1;
+    if (gap > eps) return -1;
+    if (gap > -eps) res = 0;
+  }
+  return res;
+}
+
 // closed overlap test, InsertionSortCollider::spatialOverlap (InsertionSortCollider.hpp:166-171)
 __device__ __forceinline__ bool overlapClosed(double4 amn, double4 amx, double4 bmn, double4 bmx) {
   return (amn.x <= bmx.x) && (amx.x >= bmn.x) && (amn.y <= bmx.y) && (amx.y >= bmn.y) && (amn.z <= bmx.z) &&
@@ -536,6 +568,8 @@ __device__ __forceinline__ int orientNew(const Dev& d, int i, int j, int initSor
 // i's previous row gives the new row length: old entries survive if real or overlapping
 // (conditionalyEraseNonReal), new overlapping pairs are inserted when the sort would insert
 // them.
+static const int UNDECIDED = 0x40000000;   // candidate tag: overlap left to the exact test
+
 // Threads take the particles in cell order (cellBodies), so that a warp scans neighbouring
 // cells and its loads of cellBodies/cellBox overlap; bodies outside the grid (walls) get an
 // empty row from the thread of their own index.
@@ -577,16 +611,32 @@ __global__ void k_candidates(Dev d) {
         for (int k = s0; k < e0; k++) {
           int j = d.cellBodies[k];
           if (j <= i) continue;
-          if (boxesApart(ci, hi, d.cellBox[2 * k], d.cellBox[2 * k + 1], S.periodic != 0, Lf, invLf)) continue;
-          bool ov;
-          if (S.periodic) { int per[3]; ov = overlapPeri(S, imn, imx, d.bmin[j], d.bmax[j], per); }
-          else ov = overlapClosed(imn, imx, d.bmin[j], d.bmax[j]);
-          if (ov) {
-            if (n < d.MAXC) cand[n++] = j; else over = true;
-          }
+          const float4 cj = d.cellBox[2 * k], hj = d.cellBox[2 * k + 1];
+          int v;   // 1 overlap, 0 undecided (exact test below), -1 apart
+          if (S.periodic) v = overlapPeriFast(ci, hi, cj, hj, Lf, invLf);
+          else v = boxesApart(ci, hi, cj, hj, false, Lf, invLf) ? -1 : 0;
+          if (v < 0) continue;
+          if (n < d.MAXC) cand[n++] = v > 0 ? j : (j | UNDECIDED); else over = true;
         }
       }
     }
+  }
+  // exact tests of the undecided candidates, in a loop of their own so that the lanes of a
+  // warp run the FP64 work of spatialOverlapPeri together
+  {
+    int m = 0;
+    for (int a = 0; a < n; a++) {
+      int j = cand[a];
+      if (j & UNDECIDED) {
+        j &= ~UNDECIDED;
+        bool ov;
+        if (S.periodic) { int per[3]; ov = overlapPeri(S, imn, imx, d.bmin[j], d.bmax[j], per); }
+        else ov = overlapClosed(imn, imx, d.bmin[j], d.bmax[j]);
+        if (!ov) continue;
+      }
+      cand[m++] = j;
+    }
+    n = m;
   }
   for (int w = 0; w < d.W; w++) {
     int j = d.walls[w];
@@ -745,36 +795,75 @@ __global__ void k_psort(Dev d) {
     d.pList[c + 1] = v;
   }
 }
-// per-wall lists by ordered block compaction over the table (one block per wall):
-// k_wall_count writes the list lengths, k_wall_lists the lists in table order.
+// Per-wall lists of table entries in table order (the order the wall force sums follow).
+// The table is cut into WALL_CHUNKS contiguous chunks, one block each: k_wall_count counts
+// each wall's entries per chunk; k_wall_lists places chunk b's entries of wall w after
+// those of the walls before w and of the chunks before b, in table order within the chunk
+// (one block scan per wall and tile).
+static const int WALL_CHUNKS = 256, MAX_WALLS = 64;
+__device__ __forceinline__ int wallSlot(const Dev& d, int p) {
+  if (d.info[p].x != KIND_WALL) return -1;
+  for (int w = 0; w < d.W; w++) if (d.walls[w] == p) return w;
+  return -1;
+}
+__device__ __forceinline__ void wallChunk(int P, int b, int& lo, int& hi) {
+  const int len = (P + WALL_CHUNKS - 1) / WALL_CHUNKS;
+  lo = min(P, b * len); hi = min(P, lo + len);
+}
 __global__ void k_wall_count(Dev d) {
   const SceneState& S = *d.S;
   if (!S.runCollider || S.overflowRun) return;
-  __shared__ int sh[32];
-  const int wid = d.walls[blockIdx.x];
-  int cnt = 0;
-  for (int e = threadIdx.x; e < S.P; e += blockDim.x) cnt += (d.A.partner[e] == wid);
-  int total;
-  blockExclusiveScan(cnt, sh, total);
-  if (threadIdx.x == 0) d.wCount[blockIdx.x] = total;
+  __shared__ int cnt[MAX_WALLS];
+  for (int w = threadIdx.x; w < d.W; w += blockDim.x) cnt[w] = 0;
+  __syncthreads();
+  int lo, hi;
+  wallChunk(S.P, blockIdx.x, lo, hi);
+  for (int e = lo + threadIdx.x; e < hi; e += blockDim.x) {
+    const int w = wallSlot(d, d.A.partner[e]);
+    if (w >= 0) atomicAdd(&cnt[w], 1);
+  }
+  __syncthreads();
+  for (int w = threadIdx.x; w < d.W; w += blockDim.x) d.wBlk[blockIdx.x * d.W + w] = cnt[w];
 }
 __global__ void k_wall_lists(Dev d) {
   const SceneState& S = *d.S;
   if (!S.runCollider || S.overflowRun) return;
   __shared__ int sh[32];
-  const int w = blockIdx.x;
-  const int wid = d.walls[w];
-  int base = 0;
-  for (int w2 = 0; w2 < w; w2++) base += d.wCount[w2];
-  int off = base;
-  for (int e0 = 0; e0 < S.P; e0 += blockDim.x) {
-    int e = e0 + threadIdx.x;
-    int f = (e < S.P && d.A.partner[e] == wid) ? 1 : 0;
-    int t; int ex = blockExclusiveScan(f, sh, t);
-    if (f) d.wList[off + ex] = e;
-    off += t;
+  __shared__ int tot[MAX_WALLS], off[MAX_WALLS];
+  for (int w = threadIdx.x; w < d.W; w += blockDim.x) {
+    int before = 0, all = 0;
+    for (int b = 0; b < WALL_CHUNKS; b++) {
+      const int c = d.wBlk[b * d.W + w];
+      all += c;
+      if (b < blockIdx.x) before += c;
+    }
+    tot[w] = all; off[w] = before;
   }
-  if (threadIdx.x == 0) d.wCount[d.W + w] = base;   // start of list w
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int start = 0;
+    for (int w = 0; w < d.W; w++) {
+      off[w] += start;
+      if (blockIdx.x == 0) { d.wCount[w] = tot[w]; d.wCount[d.W + w] = start; }
+      start += tot[w];
+    }
+  }
+  __syncthreads();
+  int lo, hi;
+  wallChunk(S.P, blockIdx.x, lo, hi);
+  for (int e0 = lo; e0 < hi; e0 += blockDim.x) {
+    const int e = e0 + threadIdx.x;
+    const int ws = e < hi ? wallSlot(d, d.A.partner[e]) : -1;
+    for (int w = 0; w < d.W; w++) {
+      const int f = ws == w ? 1 : 0;
+      int tt;
+      const int ex = blockExclusiveScan(f, sh, tt);
+      if (f) d.wList[off[w] + ex] = e;
+      __syncthreads();
+      if (threadIdx.x == 0) off[w] += tt;
+      __syncthreads();
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -2182,8 +2271,8 @@ static void enqueueStep(sqdem_ctx* c, bool timed) {
   k_psort<<<nblk(N, 256), 256, 0, s>>>(d);
   c->launches += 2;
   if (d.W > 0) {
-    k_wall_count<<<d.W, 256, 0, s>>>(d);
-    k_wall_lists<<<d.W, 256, 0, s>>>(d);
+    k_wall_count<<<WALL_CHUNKS, 256, 0, s>>>(d);
+    k_wall_lists<<<WALL_CHUNKS, 256, 0, s>>>(d);
     c->launches += 2;
   }
   if (timed) cudaEventRecord(c->ev[1], s);
@@ -2382,6 +2471,7 @@ static void packState(sqdem_ctx* c, int n, const double* st, std::vector<double4
 sqdem_status sqdem_set_bodies(sqdem_ctx* c, int n, const int* kind, const double* shape5, const int* was,
                               const int* mat, const int* isSphere, const double* state) {
   if (!c || n <= 0 || !kind || !mat || !state) return fail(c, SQDEM_ERR_ARG, "bad bodies");
+  if (n >= (1 << 30)) return fail(c, SQDEM_ERR_CAPACITY, "at most 2^30 - 1 bodies");
   if (!c->haveMats) return fail(c, SQDEM_ERR_STATE, "set materials first");
   CK(cudaSetDevice(c->device));
   CK(cudaStreamSynchronize(c->stream));
@@ -2415,6 +2505,7 @@ sqdem_status sqdem_set_bodies(sqdem_ctx* c, int n, const int* kind, const double
     } else return fail(c, SQDEM_ERR_ARG, "unknown body kind");
   }
   if (!finiteRows(state, n, SQDEM_BODY_STRIDE, 16)) return fail(c, SQDEM_ERR_ARG, "non-finite body state");
+  if ((int)c->wallIds.size() > MAX_WALLS) return fail(c, SQDEM_ERR_CAPACITY, "more than 64 walls");
   Dev& d = c->d;
   d.N = n; d.NP = NP; d.W = (int)c->wallIds.size();
   d.MAXC = c->maxCand;
@@ -2436,6 +2527,7 @@ sqdem_status sqdem_set_bodies(sqdem_ctx* c, int n, const int* kind, const double
   CK(dalloc(c, &d.pCount, n + 1)); CK(dalloc(c, &d.pStart, n + 1)); CK(dalloc(c, &d.pFill, n + 1));
   CK(dalloc(c, &d.pList, d.Pcap));
   CK(dalloc(c, &d.wCount, 2 * std::max(d.W, 1))); CK(dalloc(c, &d.wList, d.Pcap));
+  CK(dalloc(c, &d.wBlk, (size_t)WALL_CHUNKS * std::max(d.W, 1)));
   CK(dalloc(c, &d.ww, std::max(d.W * d.W, 1)));
   CK(dalloc(c, &d.lmQueue, d.Pcap));
   CK(dalloc(c, &d.bodyCell, n)); CK(dalloc(c, &d.cellCount, d.Gmax + 1)); CK(dalloc(c, &d.cellStart, d.Gmax + 1));
