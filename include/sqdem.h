@@ -211,6 +211,38 @@ sqdem_status sqdem_shape_props(double rx, double ry, double rz, double eps1, dou
 /* Number of kernel launches issued by the last sqdem_step call. */
 long long sqdem_launch_count(sqdem_ctx* ctx);
 
+/* ---------------------------------------------------------------------------------------
+ * Boundary controller: CompressionEngine for a cubic specimen (pkg/dem/Compression.hpp:39-252,
+ * action_cubic Compression.cpp:395-604, as compiled with SOLE_GAIN and NEW_SCHEME), run each
+ * step between InteractionLoop and NewtonIntegrator.  Bodies 0-5 must be the walls left,
+ * right, front, back, bottom, top.  Configuration, SQDEM_SERVO_CONFIG doubles: enabled,
+ * z_servo, continueFlag, hydroStrain, shearMode, left/right/front/back/bottom/top
+ * _wall_activated, iterate_num_max, solve_num_max, echo_interval, savedata_interval,
+ * ramp_interval, ramp_chunks, goalx, goaly, goalz, gain_alpha, target_strain, f_threshold,
+ * fmin_threshold, unbf_tol, max_vel, hydroStrainRate, width0, height0, depth0.  enabled = 0
+ * removes the engine.  Setting it starts the engine afresh (its first run initialises). */
+#define SQDEM_SERVO_CONFIG 30
+/* Engine state, SQDEM_SERVO_STATE doubles: width, depth, height, x_area, y_area, z_area,
+ * wsxx, wsyy, wszz, wsxx_left, wsxx_right, wsyy_front, wsyy_back, wszz_bottom, wszz_top,
+ * gain_x, gain_x1, gain_y, gain_y1, gain_z, gain_z1, UnbalancedForce, particlesVolume,
+ * Init_boxVolume, Current_boxVolume, strain[2], iterate_num, solve_num, rampNum,
+ * Flag_ForceTarget, firstRun, width0, height0, depth0, stopAtIter (-1: none), quiet flag.
+ * When an engine sets Scene::stopAtIter (consolidation complete, target strain reached),
+ * the steps from that iteration on do nothing, as O.run stops there; sqdem_put_servo with
+ * stopAtIter = -1 resumes. */
+#define SQDEM_SERVO_STATE 36
+sqdem_status sqdem_set_servo(sqdem_ctx* ctx, const double* config);
+sqdem_status sqdem_get_servo(sqdem_ctx* ctx, double* state);
+sqdem_status sqdem_put_servo(sqdem_ctx* ctx, const double* state);
+/* NewtonIntegrator::quiet_system_flag (NewtonIntegrator.hpp:73): the next step zeroes all
+ * velocities instead of moving the bodies, then clears the flag (NewtonIntegrator.cpp:246-299). */
+sqdem_status sqdem_set_quiet(sqdem_ctx* ctx, int on);
+/* Shop::unbalancedForce(useMaxForce) (pkg/dem/Shop_01.cpp:148-188) on the forces of the last
+ * step; Shop::getStress(volume) (pkg/dem/Shop_02.cpp:350-376), 9 doubles row-major, volume 0
+ * meaning the periodic cell's volume (1 without a cell).  Sums follow table order. */
+sqdem_status sqdem_unbalanced_force(sqdem_ctx* ctx, int use_max, double* out);
+sqdem_status sqdem_get_stress(sqdem_ctx* ctx, double volume, double* out9);
+
 #ifdef __cplusplus
 }
 #endif

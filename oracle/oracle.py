@@ -48,6 +48,9 @@ def lib():
         "sqo_rebuild_sorted_bounds": (None, [v]),
         "sqo_pair_geom": (i, [v, i, i, i, dp, dp]),
         "sqo_eval_hist": (None, [v, C.POINTER(l)]),
+        "sqo_set_servo": (None, [v, dp]), "sqo_get_servo": (None, [v, dp]), "sqo_put_servo": (None, [v, dp]),
+        "sqo_set_quiet": (None, [v, C.c_int]), "sqo_unbalanced_force": (d, [v, C.c_int]),
+        "sqo_get_stress": (None, [v, d, dp]),
         "sqo_set_periodic": (None, [v, dp, dp]), "sqo_set_velgrad": (None, [v, dp]),
         "sqo_get_cell": (None, [v, dp]), "sqo_set_cell": (None, [v, dp]),
         "sqo_shape_props": (None, [d, d, d, d, d, dp]),
@@ -211,6 +214,31 @@ class OracleScene:
         out = (C.c_long * 5)()
         self.L.sqo_stats(self.h, out)
         return dict(zip(("lm_calls", "lm_iterations", "dis_calls", "restarts", "nan_normals"), list(out)))
+
+    def set_servo(self, config):
+        cfg = np.ascontiguousarray(config, dtype=np.float64)
+        assert cfg.shape == (30,)
+        self.L.sqo_set_servo(self.h, _dp(cfg))
+
+    def servo_state(self):
+        out = np.zeros(36)
+        self.L.sqo_get_servo(self.h, _dp(out))
+        return out
+
+    def put_servo(self, state):
+        st = np.ascontiguousarray(state, dtype=np.float64)
+        self.L.sqo_put_servo(self.h, _dp(st))
+
+    def set_quiet(self, on=True):
+        self.L.sqo_set_quiet(self.h, 1 if on else 0)
+
+    def unbalanced_force(self, use_max=False):
+        return float(self.L.sqo_unbalanced_force(self.h, 1 if use_max else 0))
+
+    def get_stress(self, volume=0.0):
+        out = np.zeros(9)
+        self.L.sqo_get_stress(self.h, float(volume), _dp(out))
+        return out.reshape(3, 3)
 
     def eval_hist(self):
         out = (C.c_long * 16)()

@@ -73,6 +73,11 @@ static inline V3 mul(const M3& M, const V3& x) {
             M.m[3] * x[0] + (M.m[4] * x[1] + M.m[5] * x[2]),
             M.m[6] * x[0] + (M.m[7] * x[1] + M.m[8] * x[2]));
 }
+// determinant by cofactor expansion along the first row
+static inline Real det(const M3& A) {
+  return A.m[0] * (A.m[4] * A.m[8] - A.m[5] * A.m[7]) - A.m[1] * (A.m[3] * A.m[8] - A.m[5] * A.m[6]) +
+         A.m[2] * (A.m[3] * A.m[7] - A.m[4] * A.m[6]);
+}
 static inline M3 mmul(const M3& A, const M3& B) {
   M3 r;
   for (int i = 0; i < 3; i++)
@@ -263,6 +268,11 @@ struct Scene {
   long loIdx[3] = {0, 0, 0};
   // user hook between InteractionLoop and NewtonIntegrator (boundary controllers)
   void (*midHook)(void*) = nullptr; void* midHookArg = nullptr;
+  // NewtonIntegrator::quiet_system_flag (NewtonIntegrator.hpp:73, .cpp:246-250,299)
+  bool quietSystem = false;
+  // CompressionEngine (pkg/dem/Compression.hpp:39-252), run between InteractionLoop and Newton
+  struct Servo* servo = nullptr;
+  long stopAtIter = -1;   // Scene::stopAtIter as the engine requests it
 };
 
 static inline uint64_t pairKey(int a, int b) {
@@ -1056,13 +1066,18 @@ static void newtonAction(Scene& S) {
         }
       }
     } else if (periodic && homoDeform) b.vel = b.vel + mul(dtPrevVelGrad, b.vel);
-    if (!useAspherical) leapfrogSphericalRotate(S, b);
-    else if (S.isSuperquadrics) {
-      if (!isSphere) leapfrogSqRotate(S, b, m);
-      else leapfrogSphericalRotate(S, b);
+    if (S.quietSystem) {   // quiet_system_flag (:246-250): zero velocities, no move
+      b.vel = V3(0, 0, 0);
+      b.angVel = V3(0, 0, 0);
+    } else {
+      if (!useAspherical) leapfrogSphericalRotate(S, b);
+      else if (S.isSuperquadrics) {
+        if (!isSphere) leapfrogSqRotate(S, b, m);
+        else leapfrogSphericalRotate(S, b);
+      }
+      if (periodic && homoDeform) b.vel = b.vel + mul(dVelGrad, b.pos);  // leapfrogTranslate (:306-317)
+      b.pos = b.pos + b.vel * dt;
     }
-    if (periodic && homoDeform) b.vel = b.vel + mul(dVelGrad, b.pos);  // leapfrogTranslate (:306-317)
-    b.pos = b.pos + b.vel * dt;
     // saveMaximaDisplacement (:72-85)
     if (b.hasBound) {
       V3 disp = b.pos - b.refPos;
@@ -1072,8 +1087,268 @@ static void newtonAction(Scene& S) {
       t = std::max(t, maxDisp);
     }
   }
+  if (S.quietSystem) S.quietSystem = false;
   for (Real t : thrMax) S.maxVelocitySq = std::max(S.maxVelocitySq, t);
   if (periodic) { S.prevCellSize = S.cellSize; S.prevVelGrad = S.velGrad; }
+}
+
+// ---------------------------------------------------------------------------
+// Shop::unbalancedForce (pkg/dem/Shop_01.cpp:148-188): sum over dynamic bodies of |F + m g|
+// (the reference returns the sum, not the mean), divided by twice the sum of |Fn + Fs| over
+// real contacts with a non-zero normal force; with useMax, the largest body force divided by
+// the summed contact forces on that body.
+static Real unbalancedForce(const Scene& S, bool useMax) {
+  Real sumF = 0, maxF = 0; long idMax = -1;
+  for (size_t id = 0; id < S.bodies.size(); id++) {
+    const Body& b = S.bodies[id];
+    if (b.blockedDOFs == DOF_ALL) continue;   // !isDynamic()
+    const Real currF = norm(S.force[id] + b.mass * S.gravity);
+    if (currF > maxF) { maxF = currF; idMax = (long)id; }
+    sumF += currF;
+  }
+  const Real meanF = sumF;
+  sumF = 0; Real maxCF = 0;
+  for (const Interaction* I : S.lin) {
+    if (!(I->hasGeom && I->hasPhys)) continue;
+    if (norm(I->p.normalForce) == 0) continue;
+    const Real f = norm(I->p.normalForce + I->p.shearForce);
+    sumF += f;
+    if (I->id1 == idMax || I->id2 == idMax) maxCF += f;
+  }
+  sumF *= 2.0;
+  return useMax ? maxF / maxCF : meanF / sumF;
+}
+
+// Shop::getStress (pkg/dem/Shop_02.cpp:350-376): sum over real contacts of
+// (Fn + Fs) (pos1 - pos2 - hSize cellDist)^T, divided by the volume (the cell volume when 0).
+static M3 shopGetStress(const Scene& S, Real volume) {
+  if (volume == 0) volume = S.isPeriodic ? det(S.hSize) : 1;
+  M3 st{{0, 0, 0, 0, 0, 0, 0, 0, 0}};
+  for (const Interaction* I : S.lin) {
+    if (!(I->hasGeom && I->hasPhys)) continue;
+    V3 branch = S.bodies[I->id1].pos - S.bodies[I->id2].pos;
+    if (S.isPeriodic) branch = branch - mul(S.hSize, V3(I->cellDist[0], I->cellDist[1], I->cellDist[2]));
+    const V3 f = I->p.normalForce + I->p.shearForce;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) st.m[3 * i + j] += f[i] * branch[j];
+  }
+  for (int k = 0; k < 9; k++) st.m[k] /= volume;
+  return st;
+}
+
+// CompressionEngine, cubic specimen, as compiled in the reference (SOLE_GAIN and NEW_SCHEME
+// defined, Compression.hpp:24-31): walls are bodies 0-5 (left, right, front, back, bottom,
+// top); each wall is moved directly by its own gain times (wall stress - goal), clamped to
+// max_vel*dt.  recordData's file output is left out; its state side effects (box size,
+// volume, strain) are kept.
+struct Servo {
+  // attributes (Compression.hpp:160-215)
+  bool z_servo = true, continueFlag = false, hydroStrain = false;
+  unsigned shearMode = 1;
+  Real gain_alpha = 0.5, target_strain = 0.15;
+  unsigned iterate_num_max = 100, solve_num_max = 2000, echo_interval = 1000, savedata_interval = 12;
+  unsigned ramp_interval = 10000, ramp_chunks = 400;
+  Real f_threshold = 0.01, fmin_threshold = 0.01, unbf_tol = 0.01, max_vel = 1.0, hydroStrainRate = 0;
+  Real goalx = 0, goaly = 0, goalz = 0;
+  bool activated[6] = {true, true, true, true, true, true};
+  Real height0 = 0, width0 = 0, depth0 = 0;
+  // state (constructor, Compression.hpp:217-240)
+  bool firstRun = true, Flag_ForceTarget = false;
+  Real width = 0, depth = 0, height = 0, x_area = 0, y_area = 0, z_area = 0;
+  Real Init_boxVolume = 0, Current_boxVolume = 0, particlesVolume = 0, strain2 = 0;
+  Real gain_x = 0, gain_y = 0, gain_z = 0, gain_x1 = 0, gain_y1 = 0, gain_z1 = 0;
+  Real wsxx_left = 0, wsxx_right = 0, wsyy_front = 0, wsyy_back = 0, wszz_bottom = 0, wszz_top = 0;
+  Real wsxx = 0, wsyy = 0, wszz = 0;
+  unsigned iterate_num = 0, solve_num = 0, rampNum = 0;
+  Real UnbalancedForce = 1;
+};
+
+static void svUpdateBoxSize(Scene& S, Servo& C) {   // Compression.cpp:99-114
+  const Real left = S.bodies[0].pos[0], right = S.bodies[1].pos[0];
+  const Real front = S.bodies[2].pos[1], back = S.bodies[3].pos[1];
+  const Real top = S.bodies[5].pos[2], bottom = S.bodies[4].pos[2];
+  C.width = right - left; C.depth = back - front; C.height = top - bottom;
+  C.x_area = C.depth * C.height; C.y_area = C.width * C.height; C.z_area = C.depth * C.width;
+}
+static void svConsolSS(Scene& S, Servo& C) {        // Compression.cpp:1330-1362 (SOLE_GAIN)
+  svUpdateBoxSize(S, C);
+  C.wsxx_right = S.force[1][0] / C.x_area;
+  C.wsxx_left = -S.force[0][0] / C.x_area;
+  C.wsxx = 0.5 * (C.wsxx_left + C.wsxx_right);
+  C.wsyy_back = S.force[3][1] / C.y_area;
+  C.wsyy_front = -S.force[2][1] / C.y_area;
+  C.wsyy = 0.5 * (C.wsyy_back + C.wsyy_front);
+  C.wszz_top = S.force[5][2] / C.z_area;
+  C.wszz_bottom = -S.force[4][2] / C.z_area;
+  C.wszz = 0.5 * (C.wszz_top + C.wszz_bottom);
+}
+static void svGetGain(Scene& S, Servo& C) {          // Compression.cpp:1125-1220 (SOLE_GAIN)
+  Real st[6] = {0, 0, 0, 0, 0, 0};
+  for (const Interaction* I : S.lin) {
+    if (!(I->hasGeom && I->hasPhys)) continue;
+    const int id = I->id1 < I->id2 ? I->id1 : I->id2;
+    if (id < 6) st[id] += I->p.kn;
+  }
+  C.gain_x = C.gain_alpha * C.x_area / st[0];
+  C.gain_y = C.gain_alpha * C.y_area / st[2];
+  C.gain_z = C.gain_alpha * C.z_area / st[4];
+  C.gain_x1 = C.gain_alpha * C.x_area / st[1];
+  C.gain_y1 = C.gain_alpha * C.y_area / st[3];
+  C.gain_z1 = C.gain_alpha * C.z_area / st[5];
+}
+static inline Real svStep(Real gain, Real ws, Real goal, Real maxStep) {   // Sign(u) * min(|u|, max_vel dt)
+  const Real u = gain * (ws - goal);
+  const Real a = std::abs(u);
+  return Sign(u) * ((maxStep < a) ? maxStep : a);
+}
+static void svServo(Scene& S, Servo& C, Real dt) {   // Compression.cpp:1252-1303 (SOLE_GAIN)
+  svConsolSS(S, C);
+  const Real ms = C.max_vel * dt;
+  if (C.activated[0]) S.bodies[0].pos[0] += -svStep(C.gain_x, C.wsxx_left, C.goalx, ms);
+  if (C.activated[1]) S.bodies[1].pos[0] += svStep(C.gain_x1, C.wsxx_right, C.goalx, ms);
+  if (C.activated[2]) S.bodies[2].pos[1] += -svStep(C.gain_y, C.wsyy_front, C.goaly, ms);
+  if (C.activated[3]) S.bodies[3].pos[1] += svStep(C.gain_y1, C.wsyy_back, C.goaly, ms);
+  if (C.z_servo) {
+    S.bodies[4].pos[2] += -svStep(C.gain_z, C.wszz_bottom, C.goalz, ms);
+    S.bodies[5].pos[2] += svStep(C.gain_z1, C.wszz_top, C.goalz, ms);
+  }
+}
+// getStressTensor (Compression.cpp:764-829) and getStress (:831-841): mean and deviatoric
+// stress of the contact stress tensor in the box volume.
+static void svGetStress(Scene& S, Servo& C, Real& mean, Real& dev) {
+  svUpdateBoxSize(S, C);
+  C.Current_boxVolume = C.height * C.z_area;
+  Real sg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};   // row-major Sigma(i,j)
+  for (const Interaction* I : S.lin) {
+    if (!(I->hasGeom && I->hasPhys)) continue;
+    const V3 fn = I->p.normalForce, fs = I->p.shearForce;
+    if (norm(fn) == 0) continue;
+    if (I->id1 == I->id2) continue;
+    const V3 l = S.bodies[I->id2].pos - S.bodies[I->id1].pos;
+    const V3 f = fn + fs;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) sg[3 * i + j] += f[i] * l[j];
+  }
+  for (int k = 0; k < 9; k++) sg[k] /= C.Current_boxVolume;
+  // Matrix3r::trace (diagonal sum, a0 + (a1 + a2)) and norm (column-major squaredNorm, Eigen's
+  // unrolled halving reduction over 9 coefficients)
+  mean = (sg[0] + (sg[4] + sg[8])) / 3.0;
+  sg[0] -= mean; sg[4] -= mean; sg[8] -= mean;
+  Real c[9];
+  for (int k = 0; k < 9; k++) c[k] = sg[3 * (k % 3) + k / 3];
+  const Real sq = ((c[0] * c[0] + c[1] * c[1]) + (c[2] * c[2] + c[3] * c[3])) +
+                  ((c[4] * c[4] + c[5] * c[5]) + (c[6] * c[6] + (c[7] * c[7] + c[8] * c[8])));
+  dev = std::sqrt(sq) * std::sqrt(1.5);
+}
+static void svRecordData(Scene& S, Servo& C) {       // Compression.cpp:843-925, state only
+  Real mean, dev;
+  svGetStress(S, C, mean, dev);
+  C.strain2 = std::log(C.height0 / C.height);
+}
+static void svAction(Scene& S, Servo& C) {            // action_cubic, Compression.cpp:395-604
+  if (C.firstRun) {
+    const Real left = S.bodies[0].pos[0], right = S.bodies[1].pos[0];
+    const Real front = S.bodies[2].pos[1], back = S.bodies[3].pos[1];
+    const Real top = S.bodies[5].pos[2], bottom = S.bodies[4].pos[2];
+    if (C.continueFlag) { C.width = right - left; C.depth = back - front; C.height = top - bottom; }
+    else {
+      C.width = C.width0 = right - left; C.depth = C.depth0 = back - front; C.height = C.height0 = top - bottom;
+    }
+    C.x_area = C.depth * C.height; C.y_area = C.width * C.height; C.z_area = C.depth * C.width;
+    C.Init_boxVolume = C.height0 * C.width0 * C.depth0;
+    C.particlesVolume = 0;
+    for (const Body& b : S.bodies) if (b.kind == KIND_SQ) C.particlesVolume += b.sq.volume;
+    C.rampNum = 0; C.firstRun = false;
+    C.iterate_num = 0; C.solve_num = 0;
+    svGetGain(S, C);
+    C.Flag_ForceTarget = false;
+  }
+  const Real dt = S.dt;
+  if (C.z_servo) {
+    if (C.hydroStrain) {   // hydroConsolidation, Compression.cpp:264-322
+      svUpdateBoxSize(S, C);
+      const Real ls = S.force[0][0] / C.x_area, rs = S.force[1][0] / C.x_area;
+      const Real fs = S.force[2][1] / C.y_area, bs = S.force[3][1] / C.y_area;
+      const Real bos = S.force[4][2] / C.z_area, ts = S.force[5][2] / C.z_area;
+      const Real dl = C.goalx - std::abs(ls), dr = C.goalx - std::abs(rs);
+      const Real df = C.goaly - std::abs(fs), dbk = C.goaly - std::abs(bs);
+      const Real dbo = C.goalz - std::abs(bos), dtp = C.goalz - std::abs(ts);
+      auto mn = [](Real a, Real b) { return (b < a) ? b : a; };
+      if (dl > 0) S.bodies[0].pos[0] += mn(0.1 * C.gain_x * dl, C.hydroStrainRate * C.width * dt);
+      if (dr > 0) S.bodies[1].pos[0] -= mn(0.1 * C.gain_x1 * dr, C.hydroStrainRate * C.width * dt);
+      if (df > 0) S.bodies[2].pos[1] += mn(0.1 * C.gain_y * df, C.hydroStrainRate * C.depth * dt);
+      if (dbk > 0) S.bodies[3].pos[1] -= mn(0.1 * C.gain_y1 * dbk, C.hydroStrainRate * C.depth * dt);
+      if (dbo > 0) S.bodies[4].pos[2] += mn(0.1 * C.gain_z * dbo, C.hydroStrainRate * C.height * dt);
+      if (dtp > 0) S.bodies[5].pos[2] -= mn(0.1 * C.gain_z1 * dtp, C.hydroStrainRate * C.height * dt);
+      C.iterate_num += 1;
+      if (C.iterate_num >= C.iterate_num_max) { C.iterate_num = 1; svGetGain(S, C); }
+      C.solve_num += 1;
+      if (C.solve_num >= C.solve_num_max) {
+        C.solve_num = 1;
+        Real mean, dev;
+        svGetStress(S, C, mean, dev);
+        if ((std::abs(mean - C.goalx) / C.goalx < C.f_threshold) && (dev / mean < C.fmin_threshold))
+          if (C.UnbalancedForce < C.unbf_tol) S.stopAtIter = S.iter + 1;
+      }
+    } else {               // generalConsolidation, NEW_SCHEME, Compression.cpp:324-358
+      C.iterate_num += 1;
+      C.solve_num += 1;
+      svServo(S, C, dt);
+      if (C.iterate_num >= C.iterate_num_max) { C.iterate_num = 0; svGetGain(S, C); }
+      if (C.solve_num >= C.solve_num_max) {
+        C.solve_num = 0;
+        Real mean, dev;
+        svGetStress(S, C, mean, dev);
+        if ((std::abs(mean - C.goalx) < C.goalx * C.f_threshold) && (dev / mean < C.fmin_threshold)) {
+          C.UnbalancedForce = unbalancedForce(S, false);
+          if (C.UnbalancedForce < C.unbf_tol) { S.stopAtIter = S.iter + 1; S.quietSystem = true; }
+        }
+      }
+    }
+    if (S.iter % C.savedata_interval == 0) svRecordData(S, C);
+    if (S.iter % C.echo_interval == 0) { C.UnbalancedForce = unbalancedForce(S, false); svConsolSS(S, C); }
+  } else {                 // shear
+    if (!C.continueFlag && C.rampNum < C.ramp_interval) {
+      if (C.rampNum < 1 && C.Flag_ForceTarget) {
+        svUpdateBoxSize(S, C);
+        C.width0 = C.width; C.height0 = C.height; C.depth0 = C.depth;
+      }
+      C.rampNum++;
+      const double ramp_inter = 0.5 * C.ramp_interval;
+      double vel;
+      if (C.rampNum < ramp_inter)
+        vel = (double)(float(C.rampNum / (ramp_inter / C.ramp_chunks) + 1) / float(C.ramp_chunks)) * C.goalz * 2.0;
+      else
+        vel = ((double)(float((C.ramp_interval - C.rampNum) / (ramp_inter / C.ramp_chunks) + 1) / float(C.ramp_chunks)) + 1.0) * C.goalz;
+      S.bodies[4].pos[2] += vel * dt * C.height;
+      S.bodies[5].pos[2] += -vel * dt * C.height;
+    } else {
+      if (C.shearMode & 1) {
+        C.iterate_num += 1;
+        if (C.iterate_num >= C.iterate_num_max) { C.iterate_num = 1; svGetGain(S, C); }
+      }
+      S.bodies[4].pos[2] += C.goalz * dt * C.height;
+      S.bodies[5].pos[2] += -C.goalz * dt * C.height;
+    }
+    if (C.shearMode & 1) svServo(S, C, dt);
+    else {                 // constant volume (undrained)
+      const Real left = S.bodies[0].pos[0], right = S.bodies[1].pos[0];
+      const Real front = S.bodies[2].pos[1], back = S.bodies[3].pos[1];
+      const Real top = S.bodies[5].pos[2], bottom = S.bodies[4].pos[2];
+      C.width = right - left; C.depth = back - front; C.height = top - bottom;
+      const double Sa = C.Init_boxVolume / C.height;
+      const double dd = 0.5 * (Sa / C.width - C.depth);
+      const double dw = Sa / (C.depth + dd) - C.width;
+      S.bodies[0].pos[0] += -0.5 * dw; S.bodies[1].pos[0] += 0.5 * dw;
+      S.bodies[2].pos[1] += -0.5 * dd; S.bodies[3].pos[1] += 0.5 * dd;
+    }
+    if (std::log(C.height0 / C.height) > C.target_strain) S.stopAtIter = S.iter + 1;
+    if (S.iter % C.savedata_interval == 0) svRecordData(S, C);
+    if (S.iter % C.echo_interval == 0) {
+      C.UnbalancedForce = unbalancedForce(S, false);
+      if (C.shearMode & 2) svConsolSS(S, C);
+    }
+  }
 }
 
 // Scene::moveToNextTimeStep (core/Scene.cpp:70-138) for
@@ -1084,6 +1359,7 @@ static void step(Scene& S) {
   if (colliderIsActivated(S)) { colliderAction(S); S.lastStepCollided = true; }
   interactionLoop(S);
   if (S.midHook) S.midHook(S.midHookArg);
+  if (S.servo) svAction(S, *S.servo);
   newtonAction(S);
   S.iter++;
   S.time += S.dt;
@@ -1098,6 +1374,7 @@ extern "C" {
 
 void* sqo_create(void) { return new Scene(); }
 void sqo_destroy(void* h) {
+  delete ((Scene*)h)->servo;
   Scene* S = (Scene*)h;
   for (Interaction* I : S->lin) delete I;
   delete S;
@@ -1181,7 +1458,14 @@ void sqo_set_cell(void* h, const double* o) {
   for (int k = 0; k < 9; k++) S->nextVelGrad.m[k] = 0;
 }
 
-void sqo_step(void* h, int n) { Scene* S = (Scene*)h; for (int i = 0; i < n; i++) step(*S); }
+// O.run(n): stops at Scene::stopAtIter when an engine has set it
+void sqo_step(void* h, int n) {
+  Scene* S = (Scene*)h;
+  for (int i = 0; i < n; i++) {
+    if (S->stopAtIter >= 0 && S->iter >= S->stopAtIter) break;
+    step(*S);
+  }
+}
 // Run only the collider (if activated) and return whether it ran; for pair-set checks.
 int sqo_collide(void* h) {
   Scene* S = (Scene*)h;
@@ -1365,4 +1649,63 @@ void sqo_normal2phi(double rx, double ry, double rz, double e1, double e2, const
   sqNormal2Phi(s, V3(n3[0], n3[1], n3[2]), out2[0], out2[1]);
 }
 
+
+// CompressionEngine configuration, 30 doubles: enabled, z_servo, continueFlag, hydroStrain,
+// shearMode, activated[6] (left,right,front,back,bottom,top), iterate_num_max, solve_num_max,
+// echo_interval, savedata_interval, ramp_interval, ramp_chunks, goalx, goaly, goalz,
+// gain_alpha, target_strain, f_threshold, fmin_threshold, unbf_tol, max_vel, hydroStrainRate,
+// width0, height0, depth0.
+void sqo_set_servo(void* h, const double* c) {
+  Scene& S = *(Scene*)h;
+  delete S.servo; S.servo = nullptr;
+  if (!(c[0] != 0)) return;
+  Servo* C = new Servo();
+  C->z_servo = c[1] != 0; C->continueFlag = c[2] != 0; C->hydroStrain = c[3] != 0; C->shearMode = (unsigned)c[4];
+  for (int k = 0; k < 6; k++) C->activated[k] = c[5 + k] != 0;
+  C->iterate_num_max = (unsigned)c[11]; C->solve_num_max = (unsigned)c[12]; C->echo_interval = (unsigned)c[13];
+  C->savedata_interval = (unsigned)c[14]; C->ramp_interval = (unsigned)c[15]; C->ramp_chunks = (unsigned)c[16];
+  C->goalx = c[17]; C->goaly = c[18]; C->goalz = c[19];
+  C->gain_alpha = c[20]; C->target_strain = c[21]; C->f_threshold = c[22]; C->fmin_threshold = c[23];
+  C->unbf_tol = c[24]; C->max_vel = c[25]; C->hydroStrainRate = c[26];
+  C->width0 = c[27]; C->height0 = c[28]; C->depth0 = c[29];
+  S.servo = C;
+}
+// CompressionEngine state, 36 doubles: width, depth, height, x_area, y_area, z_area, wsxx, wsyy,
+// wszz, wsxx_left, wsxx_right, wsyy_front, wsyy_back, wszz_bottom, wszz_top, gain_x, gain_x1,
+// gain_y, gain_y1, gain_z, gain_z1, UnbalancedForce, particlesVolume, Init_boxVolume,
+// Current_boxVolume, strain2, iterate_num, solve_num, rampNum, Flag_ForceTarget, firstRun,
+// width0, height0, depth0, stopAtIter, quiet_system_flag.
+void sqo_get_servo(void* h, double* o) {
+  Scene& S = *(Scene*)h;
+  for (int k = 0; k < 36; k++) o[k] = 0;
+  o[34] = (double)S.stopAtIter; o[35] = S.quietSystem ? 1 : 0;
+  if (!S.servo) return;
+  const Servo& C = *S.servo;
+  const double v[34] = {C.width, C.depth, C.height, C.x_area, C.y_area, C.z_area, C.wsxx, C.wsyy, C.wszz,
+                        C.wsxx_left, C.wsxx_right, C.wsyy_front, C.wsyy_back, C.wszz_bottom, C.wszz_top,
+                        C.gain_x, C.gain_x1, C.gain_y, C.gain_y1, C.gain_z, C.gain_z1, C.UnbalancedForce,
+                        C.particlesVolume, C.Init_boxVolume, C.Current_boxVolume, C.strain2,
+                        (double)C.iterate_num, (double)C.solve_num, (double)C.rampNum, C.Flag_ForceTarget ? 1.0 : 0.0,
+                        C.firstRun ? 1.0 : 0.0, C.width0, C.height0, C.depth0};
+  for (int k = 0; k < 34; k++) o[k] = v[k];
+}
+void sqo_put_servo(void* h, const double* o) {
+  Scene& S = *(Scene*)h;
+  S.stopAtIter = (long)o[34]; S.quietSystem = o[35] != 0;
+  if (!S.servo) return;
+  Servo& C = *S.servo;
+  C.width = o[0]; C.depth = o[1]; C.height = o[2]; C.x_area = o[3]; C.y_area = o[4]; C.z_area = o[5];
+  C.wsxx = o[6]; C.wsyy = o[7]; C.wszz = o[8]; C.wsxx_left = o[9]; C.wsxx_right = o[10]; C.wsyy_front = o[11];
+  C.wsyy_back = o[12]; C.wszz_bottom = o[13]; C.wszz_top = o[14];
+  C.gain_x = o[15]; C.gain_x1 = o[16]; C.gain_y = o[17]; C.gain_y1 = o[18]; C.gain_z = o[19]; C.gain_z1 = o[20];
+  C.UnbalancedForce = o[21]; C.particlesVolume = o[22]; C.Init_boxVolume = o[23]; C.Current_boxVolume = o[24];
+  C.strain2 = o[25]; C.iterate_num = (unsigned)o[26]; C.solve_num = (unsigned)o[27]; C.rampNum = (unsigned)o[28];
+  C.Flag_ForceTarget = o[29] != 0; C.firstRun = o[30] != 0; C.width0 = o[31]; C.height0 = o[32]; C.depth0 = o[33];
+}
+void sqo_set_quiet(void* h, int on) { ((Scene*)h)->quietSystem = on != 0; }
+double sqo_unbalanced_force(void* h, int useMax) { return unbalancedForce(*(Scene*)h, useMax != 0); }
+void sqo_get_stress(void* h, double volume, double* out9) {
+  const M3 st = shopGetStress(*(Scene*)h, volume);
+  for (int k = 0; k < 9; k++) out9[k] = st.m[k];
+}
 }  // extern "C"

@@ -93,6 +93,9 @@ def load_library(build_if_missing=True):
         "sqdem_time_contacts": (i, [v, i, dp]),
         "sqdem_set_use_graph": (i, [v, i]),
         "sqdem_set_lm_spread": (i, [v, i]),
+        "sqdem_set_servo": (i, [v, dp]), "sqdem_get_servo": (i, [v, dp]), "sqdem_put_servo": (i, [v, dp]),
+        "sqdem_set_quiet": (i, [v, i]), "sqdem_unbalanced_force": (i, [v, i, dp]),
+        "sqdem_get_stress": (i, [v, C.c_double, dp]),
         "sqdem_set_periodic": (i, [v, dp, dp]),
         "sqdem_set_velgrad": (i, [v, dp]),
         "sqdem_get_cell": (i, [v, dp]),
@@ -114,7 +117,9 @@ def exported_symbols():
             "sqdem_put_interactions", "sqdem_get_scalars", "sqdem_put_scalars", "sqdem_stage_times",
             "sqdem_shape_props", "sqdem_launch_count", "sqdem_set_record_full", "sqdem_time_steps",
             "sqdem_time_e2e", "sqdem_time_contacts", "sqdem_set_use_graph", "sqdem_set_lm_spread", "sqdem_set_periodic",
-            "sqdem_set_velgrad", "sqdem_get_cell", "sqdem_put_cell", "sqdem_contacts_static_queue"]
+            "sqdem_set_velgrad", "sqdem_get_cell", "sqdem_put_cell", "sqdem_contacts_static_queue",
+            "sqdem_set_servo", "sqdem_get_servo", "sqdem_put_servo", "sqdem_set_quiet", "sqdem_unbalanced_force",
+            "sqdem_get_stress"]
 
 
 def _dp(a):
@@ -201,6 +206,36 @@ class Engine:
 
     def set_lm_spread(self, on=True):
         self._check(self.lib.sqdem_set_lm_spread(self.h, 1 if on else 0))
+
+    # CompressionEngine, quiet flag, Shop reductions
+    def set_servo(self, config):
+        from .servo import CONFIG_SIZE
+        cfg = np.ascontiguousarray(config, dtype=np.float64)
+        assert cfg.shape == (CONFIG_SIZE,)
+        self._check(self.lib.sqdem_set_servo(self.h, _dp(cfg)))
+
+    def servo_state(self):
+        from .servo import STATE_SIZE
+        out = np.zeros(STATE_SIZE)
+        self._check(self.lib.sqdem_get_servo(self.h, _dp(out)))
+        return out
+
+    def put_servo(self, state):
+        st = np.ascontiguousarray(state, dtype=np.float64)
+        self._check(self.lib.sqdem_put_servo(self.h, _dp(st)))
+
+    def set_quiet(self, on=True):
+        self._check(self.lib.sqdem_set_quiet(self.h, 1 if on else 0))
+
+    def unbalanced_force(self, use_max=False):
+        out = np.zeros(1)
+        self._check(self.lib.sqdem_unbalanced_force(self.h, 1 if use_max else 0, _dp(out)))
+        return float(out[0])
+
+    def get_stress(self, volume=0.0):
+        out = np.zeros(9)
+        self._check(self.lib.sqdem_get_stress(self.h, float(volume), _dp(out)))
+        return out.reshape(3, 3)
 
     def set_record_full(self, on=True):
         self._check(self.lib.sqdem_set_record_full(self.h, 1 if on else 0))

@@ -221,3 +221,63 @@ def config1(seed=0, n=200_000):
     """200,000 superellipsoids, half-axes U[0.8,1.2] mm, eps1/eps2 U[0.3,1.8], periodic cell at
     initial solid fraction 0.3, isotropic strain-controlled compression (velGrad = -1.0/s * I)."""
     return periodic_cell(n, seed=seed)
+
+
+def cubic_specimen(n_particles, seed=0, friction=0.5, eps_range=(0.4, 1.6), r_range=(0.8e-3, 1.2e-3),
+                   spacing=2.6e-3, jitter=0.1e-3, kn=1e5, damping=0.3, verletDist=0.2e-3, dt_factor=0.5,
+                   wall_gap=0.2e-3):
+    """A closed cubic box of six walls around particles on a jittered cubic lattice, no gravity
+    (the specimen of a CompressionEngine test, examples/SudoDEM3D/example2_consol.py:63-93).
+
+    Walls are bodies 0-5 in CompressionEngine's order: left (x-), right (x+), front (y-),
+    back (y+), bottom (z-), top (z+), each wall_gap outside the outermost lattice bounds.
+    """
+    rng = np.random.default_rng(seed)
+    nx = max(1, int(math.ceil(n_particles ** (1.0 / 3.0))))
+    ny = nx
+    nz = int(math.ceil(n_particles / (nx * ny)))
+    rmax = r_range[1] * (math.sqrt(2.0) if eps_range[0] < 1.0 else 1.0)
+    lo = rmax + wall_gap
+    side = [2 * lo + (nx - 1) * spacing, 2 * lo + (ny - 1) * spacing, 2 * lo + (nz - 1) * spacing]
+    b = _builder()
+    _add_wall(b, [0, 0, 0], 0, +1)
+    _add_wall(b, [side[0], 0, 0], 0, -1)
+    _add_wall(b, [0, 0, 0], 1, +1)
+    _add_wall(b, [0, side[1], 0], 1, -1)
+    _add_wall(b, [0, 0, 0], 2, +1)
+    _add_wall(b, [0, 0, side[2]], 2, -1)
+    density = 2650.0
+    r = rng.uniform(r_range[0], r_range[1], size=(n_particles, 3))
+    eps = rng.uniform(eps_range[0], eps_range[1], size=(n_particles, 2))
+    q = random_quaternions(rng, n_particles)
+    jit = rng.uniform(-jitter, jitter, size=(n_particles, 3))
+    for p in range(n_particles):
+        layer, rem = divmod(p, nx * ny)
+        iy, ix = divmod(rem, nx)
+        pos = np.array([lo + ix * spacing, lo + iy * spacing, lo + layer * spacing]) + jit[p]
+        _add_sq(b, r[p], eps[p], q[p], pos, density)
+    mats = default_material(kn=kn, friction=friction, density=density)
+    params = {"dt": 1.0, "gravity": (0.0, 0.0, 0.0), "damping": damping, "verletDist": verletDist,
+              "targetInterv": 50, "minSweepDistFactor": 0.1, "sortAxis": 0, "isSuperquadrics": 1,
+              "exactAsphericalRot": 1}
+    spec = _finish(b, mats, params, {"box": side, "seed": seed, "friction": friction})
+    spec.params["dt"] = critical_dt(spec, dt_factor)
+    return spec
+
+
+def config2(seed=0, n_specimens=512, n_range=(300, 8000), friction_range=(0.2, 0.8), eps_range=(0.4, 1.6)):
+    """512 walled specimens with particle counts log-uniform in [300, 8000] (~1.3M particles),
+    friction U[0.2, 0.8] per specimen, eps U[0.4, 1.6]; each a cubic_specimen.  Returns the
+    list of specs and the CompressionEngine configuration they run with (100 kPa on the
+    lateral walls, axial strain at the top and bottom walls: the shear phase of
+    action_cubic, Compression.cpp:485-590)."""
+    from .servo import servo_config
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1]), size=n_specimens)).astype(int)
+    mus = rng.uniform(friction_range[0], friction_range[1], size=n_specimens)
+    specs = [cubic_specimen(int(n), seed=seed * 100003 + i, friction=float(mu), eps_range=eps_range)
+             for i, (n, mu) in enumerate(zip(ns, mus))]
+    servo = servo_config(z_servo=0, shearMode=1, goalx=1e5, goaly=1e5, goalz=0.05, max_vel=1.0,
+                         gain_alpha=0.5, ramp_interval=200, ramp_chunks=20, echo_interval=1000,
+                         savedata_interval=1000, target_strain=10.0)
+    return specs, servo

@@ -66,8 +66,27 @@ struct Params {
 
 enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_EVAL32, E_EVAL64, E_ROUNDS_MAX, E_NUM };
 
+// CompressionEngine (pkg/dem/Compression.hpp:39-252), cubic specimen: configuration and state.
+struct ServoDev {
+  int enabled, z_servo, continueFlag, hydroStrain, shearMode, activated[6];
+  unsigned iterate_num_max, solve_num_max, echo_interval, savedata_interval, ramp_interval, ramp_chunks;
+  double goalx, goaly, goalz, gain_alpha, target_strain, f_threshold, fmin_threshold, unbf_tol, max_vel, hydroStrainRate;
+  double height0, width0, depth0;
+  int firstRun, Flag_ForceTarget;
+  double width, depth, height, x_area, y_area, z_area, Init_boxVolume, Current_boxVolume, particlesVolume, strain2;
+  double gain_x, gain_y, gain_z, gain_x1, gain_y1, gain_z1;
+  double wsxx_left, wsxx_right, wsyy_front, wsyy_back, wszz_bottom, wszz_top, wsxx, wsyy, wszz;
+  unsigned iterate_num, solve_num, rampNum;
+  double UnbalancedForce;
+  double pvol;   // summed particle volumes in body order (host), particlesVolume at the first run
+  int need;      // reductions this step: 1 contact stress tensor, 2 unbalanced force
+};
+
 struct SceneState {
   long long iter; double time;
+  long long haltAt;   // Scene::stopAtIter as an engine requested it (-1: none); steps from there on do nothing
+  int skip, quiet;    // this step does nothing; NewtonIntegrator::quiet_system_flag
+  ServoDev sv;
   double maxVelocitySq, fastestBodyMaxDist, verletDistCur;
   int strideActive, newtonFound, doSort, dirty, bbInit;
   int runCollider, initSort, newtonRan, maxDispCode;
@@ -119,6 +138,8 @@ struct Dev {
   float4* cellBox;   // per cell slot: bound centre (xyz) and, in the next entry, half extents (xyz)
   int* scanTmp;
   unsigned long long* bbPart;
+  // boundary controller: per-wall kn sums of real contacts, per-block partial sums
+  double* wallKn; double* svPart; int svBlocks;
 };
 
 __device__ __forceinline__ unsigned long long encOrd(double x) {
@@ -238,6 +259,8 @@ __global__ void k_scan_apply(const int* __restrict__ in, int n, const int* __res
 // plus the start of action() (:205-252) and the NewtonIntegrator maxVelocitySq readout.
 __global__ void k_gate(Dev d) {
   SceneState& S = *d.S;
+  S.skip = (S.haltAt >= 0 && S.iter >= S.haltAt) ? 1 : 0;
+  if (S.skip) { S.runCollider = 0; S.lmCount = 0; S.lmHead = 0; return; }
   if (S.newtonRan) {
     const double code = S.maxDispCode == 2 ? 2.0 : (S.maxDispCode == 1 ? 0.5 : 0.0);
     S.maxVelocitySq = fmax_ref(S.cellTerm, code);
@@ -1114,6 +1137,7 @@ __device__ bool screenSeparated(const BodyView& b1, const BodyView& b2, double p
 // FP32 screen proves separated at the LM start point); the rest is queued for k_contacts_lm.
 __global__ void __launch_bounds__(128) k_contacts_pre(Dev d) {
   const SceneState& S = *d.S;
+  if (S.skip) return;
   const int Pn = S.P;
   const double dt = d.prm->dt;
   Counters cnt = {0, 0, 0, 0, 0};
@@ -1945,32 +1969,310 @@ __device__ __forceinline__ void addContribution(const Dev& d, int e, bool asId1,
   else { f = f + (-F); t = t + cross(pos - cp, F); }
 }
 
-// ForceContainer sum for walls: one block per wall, fixed-order reduction.
+// ForceContainer sum for walls: one block per wall, fixed-order reduction; also the sum of
+// kn over the wall's real contacts (CompressionEngine::get_gain, Compression.cpp:1125-1220).
 __global__ void k_wall_forces(Dev d) {
   const SceneState& S = *d.S;
-  __shared__ double sh[6][128];
+  if (S.skip) return;
+  __shared__ double sh[7][128];
   const int w = blockIdx.x;
   const int wid = d.walls[w];
   const D3 pos = xyz(d.pos[wid]);
   const int s = d.wCount[d.W + w], n = d.wCount[w];
   D3 f = d3(0, 0, 0), t = d3(0, 0, 0);
+  double kn = 0;
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
     int e = d.wList[s + k];
-    if (!(d.A.flags[e] & F_FORCE)) continue;
-    addContribution(d, e, !(d.A.flags[e] & F_OWNER_ID1), pos, f, t);
+    const unsigned fl = d.A.flags[e];
+    if ((fl & (F_GEOM | F_PHYS)) == (F_GEOM | F_PHYS)) kn += d.A.phys[e].x;
+    if (!(fl & F_FORCE)) continue;
+    addContribution(d, e, !(fl & F_OWNER_ID1), pos, f, t);
   }
-  (void)S;
   sh[0][threadIdx.x] = f.x; sh[1][threadIdx.x] = f.y; sh[2][threadIdx.x] = f.z;
-  sh[3][threadIdx.x] = t.x; sh[4][threadIdx.x] = t.y; sh[5][threadIdx.x] = t.z;
+  sh[3][threadIdx.x] = t.x; sh[4][threadIdx.x] = t.y; sh[5][threadIdx.x] = t.z; sh[6][threadIdx.x] = kn;
   __syncthreads();
   for (int o = 64; o > 0; o >>= 1) {
     if ((int)threadIdx.x < o)
-      for (int c = 0; c < 6; c++) sh[c][threadIdx.x] = sh[c][threadIdx.x] + sh[c][threadIdx.x + o];
+      for (int c = 0; c < 7; c++) sh[c][threadIdx.x] = sh[c][threadIdx.x] + sh[c][threadIdx.x + o];
     __syncthreads();
   }
   if (threadIdx.x == 0) {
     d.force[wid] = make_double4(sh[0][0], sh[1][0], sh[2][0], 0);
     d.torque[wid] = make_double4(sh[3][0], sh[4][0], sh[5][0], 0);
+    d.wallKn[w] = sh[6][0];
+  }
+}
+
+// Per-body force sum as NewtonIntegrator sees it (rows owned, then the incidence list).
+__device__ __forceinline__ void gatherBody(const Dev& d, int b, D3 pos, D3& f, D3& m) {
+  f = d3(0, 0, 0); m = d3(0, 0, 0);
+  for (int e = d.rowStart[b]; e < d.rowStart[b + 1]; e++) {
+    unsigned fl = d.A.flags[e];
+    if (fl & F_FORCE) addContribution(d, e, (fl & F_OWNER_ID1) != 0, pos, f, m);
+  }
+  for (int k = d.pStart[b]; k < d.pStart[b + 1]; k++) {
+    int e = d.pList[k];
+    unsigned fl = d.A.flags[e];
+    if (fl & F_FORCE) addContribution(d, e, (fl & F_OWNER_ID1) == 0, pos, f, m);
+  }
+}
+
+// Reductions of the boundary controller and of Shop::getStress / Shop::unbalancedForce, one
+// block partial each (summed in block order by the reader: deterministic).  Partial layout:
+// [0..8] sum over real contacts with |Fn| != 0 of (Fn+Fs)(pos_id2 - pos_id1)^T (row-major),
+// [9] sum of |Fn+Fs| over the same contacts, [10] sum over dynamic bodies of |F + m g|,
+// [11..19] sum over all real contacts of (Fn+Fs)(pos_id1 - pos_id2 - hSize cellDist)^T.
+// need: 1 stress tensors, 2 force sums; midStep: body forces gathered from the table (the
+// controller runs before NewtonIntegrator), else the forces of the last step.
+static const int SV_PART = 20;
+__device__ __forceinline__ void blockSum(double* sh, int nv, double* v, double* out) {
+  // sh: nv x blockDim doubles
+  for (int c = 0; c < nv; c++) sh[c * blockDim.x + threadIdx.x] = v[c];
+  __syncthreads();
+  for (int o = blockDim.x >> 1; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+      for (int c = 0; c < nv; c++) sh[c * blockDim.x + threadIdx.x] += sh[c * blockDim.x + threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) for (int c = 0; c < nv; c++) out[c] = sh[c * blockDim.x];
+}
+__global__ void __launch_bounds__(128) k_servo_sums(Dev d, int needArg, int midStep) {
+  const SceneState& S = *d.S;
+  const int need = needArg < 0 ? S.sv.need : needArg;
+  if ((needArg < 0 && S.skip) || !need) return;
+  __shared__ double sh[SV_PART * 128];
+  double v[SV_PART];
+  for (int c = 0; c < SV_PART; c++) v[c] = 0;
+  const int stride = gridDim.x * blockDim.x;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < S.P; e += stride) {
+    const unsigned fl = d.A.flags[e];
+    if ((fl & (F_GEOM | F_PHYS)) != (F_GEOM | F_PHYS)) continue;
+    int id1, id2;
+    entryIds(d, e, fl, id1, id2);
+    const D3 fn = xyz(d.A.nforce[e]), fs = xyz(d.A.shear[e]);
+    const D3 f = fn + fs;
+    const D3 p1 = xyz(d.pos[id1]), p2 = xyz(d.pos[id2]);
+    if (need & 1) {
+      D3 br = p1 - p2;
+      if (S.periodic) br = br - cellShift(S, d.A.cd[e]);
+      const double fa[3] = {f.x, f.y, f.z}, ba[3] = {br.x, br.y, br.z};
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) v[11 + 3 * i + j] += fa[i] * ba[j];
+    }
+    if (nrm(fn) == 0) continue;
+    if (need & 1) {
+      const D3 l = p2 - p1;
+      const double fa[3] = {f.x, f.y, f.z}, la[3] = {l.x, l.y, l.z};
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) v[3 * i + j] += fa[i] * la[j];
+    }
+    if (need & 2) v[9] += nrm(f);
+  }
+  if (need & 2) {
+    const Params& P = *d.prm;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < d.N; b += stride) {
+      if (d.blocked[b] == DOF_ALL) continue;
+      D3 F, M;
+      if (midStep && d.info[b].x == KIND_SQ) gatherBody(d, b, xyz(d.pos[b]), F, M);
+      else F = xyz(d.force[b]);
+      const double m = d.mass[b];
+      v[10] += nrm(d3(F.x + m * P.g[0], F.y + m * P.g[1], F.z + m * P.g[2]));
+    }
+  }
+  blockSum(sh, SV_PART, v, d.svPart + (size_t)blockIdx.x * SV_PART);
+}
+
+// CompressionEngine::action for a cubic specimen as compiled in the reference (SOLE_GAIN and
+// NEW_SCHEME, Compression.hpp:24-31; action_cubic, Compression.cpp:395-604), one thread,
+// between the wall force sums and NewtonIntegrator.  Walls are bodies 0-5 (left, right, front,
+// back, bottom, top), each moved directly by its own gain times (wall stress - goal), clamped
+// to max_vel*dt.  recordData's file output is left out; its state side effects (box size,
+// volume, strain) are kept.  Sums over contacts follow table order.
+__device__ __forceinline__ void svBox(const Dev& d, ServoDev& C) {   // updateBoxSize (:99-114)
+  const double left = d.pos[0].x, right = d.pos[1].x, front = d.pos[2].y, back = d.pos[3].y;
+  const double top = d.pos[5].z, bottom = d.pos[4].z;
+  C.width = right - left; C.depth = back - front; C.height = top - bottom;
+  C.x_area = C.depth * C.height; C.y_area = C.width * C.height; C.z_area = C.depth * C.width;
+}
+__device__ __forceinline__ void svConsol(const Dev& d, ServoDev& C) {   // consol_ss (:1330-1362)
+  svBox(d, C);
+  C.wsxx_right = d.force[1].x / C.x_area;
+  C.wsxx_left = -d.force[0].x / C.x_area;
+  C.wsxx = 0.5 * (C.wsxx_left + C.wsxx_right);
+  C.wsyy_back = d.force[3].y / C.y_area;
+  C.wsyy_front = -d.force[2].y / C.y_area;
+  C.wsyy = 0.5 * (C.wsyy_back + C.wsyy_front);
+  C.wszz_top = d.force[5].z / C.z_area;
+  C.wszz_bottom = -d.force[4].z / C.z_area;
+  C.wszz = 0.5 * (C.wszz_top + C.wszz_bottom);
+}
+__device__ __forceinline__ void svGain(const Dev& d, ServoDev& C) {     // get_gain (:1125-1220)
+  C.gain_x = C.gain_alpha * C.x_area / d.wallKn[0];
+  C.gain_y = C.gain_alpha * C.y_area / d.wallKn[2];
+  C.gain_z = C.gain_alpha * C.z_area / d.wallKn[4];
+  C.gain_x1 = C.gain_alpha * C.x_area / d.wallKn[1];
+  C.gain_y1 = C.gain_alpha * C.y_area / d.wallKn[3];
+  C.gain_z1 = C.gain_alpha * C.z_area / d.wallKn[5];
+}
+__device__ __forceinline__ double svStep(double gain, double ws, double goal, double maxStep) {
+  const double u = gain * (ws - goal);
+  const double a = fabs(u);
+  return sgn(u) * ((maxStep < a) ? maxStep : a);
+}
+__device__ __forceinline__ void svServo(const Dev& d, ServoDev& C, double dt) {   // servo (:1252-1303)
+  svConsol(d, C);
+  const double ms = C.max_vel * dt;
+  if (C.activated[0]) d.pos[0].x += -svStep(C.gain_x, C.wsxx_left, C.goalx, ms);
+  if (C.activated[1]) d.pos[1].x += svStep(C.gain_x1, C.wsxx_right, C.goalx, ms);
+  if (C.activated[2]) d.pos[2].y += -svStep(C.gain_y, C.wsyy_front, C.goaly, ms);
+  if (C.activated[3]) d.pos[3].y += svStep(C.gain_y1, C.wsyy_back, C.goaly, ms);
+  if (C.z_servo) {
+    d.pos[4].z += -svStep(C.gain_z, C.wszz_bottom, C.goalz, ms);
+    d.pos[5].z += svStep(C.gain_z1, C.wszz_top, C.goalz, ms);
+  }
+}
+__device__ __forceinline__ double svTotal(const Dev& d, int c) {
+  double s = 0;
+  for (int b = 0; b < d.svBlocks; b++) s += d.svPart[(size_t)b * SV_PART + c];
+  return s;
+}
+// getStressTensor (:764-829) and getStress (:831-841)
+__device__ __forceinline__ void svStress(const Dev& d, ServoDev& C, double& mean, double& dev) {
+  svBox(d, C);
+  C.Current_boxVolume = C.height * C.z_area;
+  double sg[9];
+  for (int k = 0; k < 9; k++) sg[k] = svTotal(d, k) / C.Current_boxVolume;
+  mean = (sg[0] + (sg[4] + sg[8])) / 3.0;
+  sg[0] -= mean; sg[4] -= mean; sg[8] -= mean;
+  double c[9];
+  for (int k = 0; k < 9; k++) c[k] = sg[3 * (k % 3) + k / 3];
+  const double sq = ((c[0] * c[0] + c[1] * c[1]) + (c[2] * c[2] + c[3] * c[3])) +
+                    ((c[4] * c[4] + c[5] * c[5]) + (c[6] * c[6] + (c[7] * c[7] + c[8] * c[8])));
+  dev = sqrt(sq) * sqrt(1.5);
+}
+// recordData (:843-925) without its file: getStress's box update and the axial strain
+__device__ __forceinline__ void svRecord(const Dev& d, ServoDev& C) {
+  svBox(d, C);
+  C.Current_boxVolume = C.height * C.z_area;
+  C.strain2 = log(C.height0 / C.height);
+}
+__device__ __forceinline__ double svUnbalanced(const Dev& d) {   // Shop::unbalancedForce(false)
+  return svTotal(d, 10) / (svTotal(d, 9) * 2.0);
+}
+// which reductions this step's action reads (the counters as the action will see them)
+__global__ void k_servo_gate(Dev d) {
+  SceneState& S = *d.S;
+  ServoDev& C = S.sv;
+  C.need = 0;
+  if (S.skip || !C.enabled) return;
+  const bool echo = C.echo_interval != 0 && S.iter % C.echo_interval == 0;
+  if (C.z_servo) {
+    const unsigned solve = (C.firstRun ? 0u : C.solve_num) + 1;
+    if (solve >= C.solve_num_max) C.need |= C.hydroStrain ? 1 : 3;
+    if (echo) C.need |= 2;
+  } else if (echo) C.need |= 2;
+}
+__global__ void k_servo(Dev d) {
+  SceneState& S = *d.S;
+  ServoDev& C = S.sv;
+  if (S.skip || !C.enabled) return;
+  const double dt = d.prm->dt;
+  if (C.firstRun) {
+    const double left = d.pos[0].x, right = d.pos[1].x, front = d.pos[2].y, back = d.pos[3].y;
+    const double top = d.pos[5].z, bottom = d.pos[4].z;
+    if (C.continueFlag) { C.width = right - left; C.depth = back - front; C.height = top - bottom; }
+    else {
+      C.width = C.width0 = right - left; C.depth = C.depth0 = back - front; C.height = C.height0 = top - bottom;
+    }
+    C.x_area = C.depth * C.height; C.y_area = C.width * C.height; C.z_area = C.depth * C.width;
+    C.Init_boxVolume = C.height0 * C.width0 * C.depth0;
+    C.particlesVolume = C.pvol;
+    C.rampNum = 0; C.firstRun = 0;
+    C.iterate_num = 0; C.solve_num = 0;
+    svGain(d, C);
+    C.Flag_ForceTarget = 0;
+  }
+  const bool echo = C.echo_interval != 0 && S.iter % C.echo_interval == 0;
+  const bool save = C.savedata_interval != 0 && S.iter % C.savedata_interval == 0;
+  if (C.z_servo) {
+    if (C.hydroStrain) {   // hydroConsolidation (:264-322)
+      svBox(d, C);
+      const double ls = d.force[0].x / C.x_area, rs = d.force[1].x / C.x_area;
+      const double fs = d.force[2].y / C.y_area, bs = d.force[3].y / C.y_area;
+      const double bos = d.force[4].z / C.z_area, ts = d.force[5].z / C.z_area;
+      const double dl = C.goalx - fabs(ls), dr = C.goalx - fabs(rs);
+      const double df = C.goaly - fabs(fs), dbk = C.goaly - fabs(bs);
+      const double dbo = C.goalz - fabs(bos), dtp = C.goalz - fabs(ts);
+      if (dl > 0) d.pos[0].x += fmin_ref(0.1 * C.gain_x * dl, C.hydroStrainRate * C.width * dt);
+      if (dr > 0) d.pos[1].x -= fmin_ref(0.1 * C.gain_x1 * dr, C.hydroStrainRate * C.width * dt);
+      if (df > 0) d.pos[2].y += fmin_ref(0.1 * C.gain_y * df, C.hydroStrainRate * C.depth * dt);
+      if (dbk > 0) d.pos[3].y -= fmin_ref(0.1 * C.gain_y1 * dbk, C.hydroStrainRate * C.depth * dt);
+      if (dbo > 0) d.pos[4].z += fmin_ref(0.1 * C.gain_z * dbo, C.hydroStrainRate * C.height * dt);
+      if (dtp > 0) d.pos[5].z -= fmin_ref(0.1 * C.gain_z1 * dtp, C.hydroStrainRate * C.height * dt);
+      C.iterate_num += 1;
+      if (C.iterate_num >= C.iterate_num_max) { C.iterate_num = 1; svGain(d, C); }
+      C.solve_num += 1;
+      if (C.solve_num >= C.solve_num_max) {
+        C.solve_num = 1;
+        double mean, dev;
+        svStress(d, C, mean, dev);
+        if ((fabs(mean - C.goalx) / C.goalx < C.f_threshold) && (dev / mean < C.fmin_threshold))
+          if (C.UnbalancedForce < C.unbf_tol && S.haltAt < 0) S.haltAt = S.iter + 1;
+      }
+    } else {               // generalConsolidation, NEW_SCHEME (:324-358)
+      C.iterate_num += 1;
+      C.solve_num += 1;
+      svServo(d, C, dt);
+      if (C.iterate_num >= C.iterate_num_max) { C.iterate_num = 0; svGain(d, C); }
+      if (C.solve_num >= C.solve_num_max) {
+        C.solve_num = 0;
+        double mean, dev;
+        svStress(d, C, mean, dev);
+        if ((fabs(mean - C.goalx) < C.goalx * C.f_threshold) && (dev / mean < C.fmin_threshold)) {
+          C.UnbalancedForce = svUnbalanced(d);
+          if (C.UnbalancedForce < C.unbf_tol) { if (S.haltAt < 0) S.haltAt = S.iter + 1; S.quiet = 1; }
+        }
+      }
+    }
+    if (save) svRecord(d, C);
+    if (echo) { C.UnbalancedForce = svUnbalanced(d); svConsol(d, C); }
+  } else {                 // shear
+    if (!C.continueFlag && C.rampNum < C.ramp_interval) {
+      if (C.rampNum < 1 && C.Flag_ForceTarget) {
+        svBox(d, C);
+        C.width0 = C.width; C.height0 = C.height; C.depth0 = C.depth;
+      }
+      C.rampNum++;
+      const double ramp_inter = 0.5 * C.ramp_interval;
+      double vel;
+      if (C.rampNum < ramp_inter)
+        vel = (double)((float)(C.rampNum / (ramp_inter / C.ramp_chunks) + 1) / (float)C.ramp_chunks) * C.goalz * 2.0;
+      else
+        vel = ((double)((float)((C.ramp_interval - C.rampNum) / (ramp_inter / C.ramp_chunks) + 1) / (float)C.ramp_chunks) + 1.0) * C.goalz;
+      d.pos[4].z += vel * dt * C.height;
+      d.pos[5].z += -vel * dt * C.height;
+    } else {
+      if (C.shearMode & 1) {
+        C.iterate_num += 1;
+        if (C.iterate_num >= C.iterate_num_max) { C.iterate_num = 1; svGain(d, C); }
+      }
+      d.pos[4].z += C.goalz * dt * C.height;
+      d.pos[5].z += -C.goalz * dt * C.height;
+    }
+    if (C.shearMode & 1) svServo(d, C, dt);
+    else {                 // constant volume (undrained)
+      const double left = d.pos[0].x, right = d.pos[1].x, front = d.pos[2].y, back = d.pos[3].y;
+      const double top = d.pos[5].z, bottom = d.pos[4].z;
+      C.width = right - left; C.depth = back - front; C.height = top - bottom;
+      const double Sa = C.Init_boxVolume / C.height;
+      const double dd = 0.5 * (Sa / C.width - C.depth);
+      const double dw = Sa / (C.depth + dd) - C.width;
+      d.pos[0].x += -0.5 * dw; d.pos[1].x += 0.5 * dw;
+      d.pos[2].y += -0.5 * dd; d.pos[3].y += 0.5 * dd;
+    }
+    if (log(C.height0 / C.height) > C.target_strain && S.haltAt < 0) S.haltAt = S.iter + 1;
+    if (save) svRecord(d, C);
+    if (echo) { C.UnbalancedForce = svUnbalanced(d); if (C.shearMode & 2) svConsol(d, C); }
   }
 }
 
@@ -2016,6 +2318,7 @@ __device__ __forceinline__ void sphericalRotate(Q4& o, D3 w, double dt) {
 
 __global__ void __launch_bounds__(256) k_integrate(Dev d) {
   const SceneState& S = *d.S;
+  if (S.skip) return;
   const Params& P = *d.prm;
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   int code = 0;
@@ -2094,7 +2397,10 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d) {
         }
       }
     } else if (homo) vel = vel + m3v(S.dtPrevVelGrad, vel);
-    if (!useAspherical || (P.isSuperquadrics && isSphere)) {
+    if (S.quiet) {   // quiet_system_flag (NewtonIntegrator.cpp:246-250): zero velocities, no move
+      vel = d3(0, 0, 0);
+      angVel = d3(0, 0, 0);
+    } else if (!useAspherical || (P.isSuperquadrics && isSphere)) {
       sphericalRotate(ori, angVel, dt);
     } else if (P.isSuperquadrics) {
       // leapfrogAsphericalRotate with A = rot_mat2local (:337-360, :391-429)
@@ -2113,8 +2419,10 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d) {
       angVel = qrotate(ori, w_b_h);
       qnormalize(ori);
     }
-    if (homo) vel = vel + m3v(S.dVelGrad, pos);   // leapfrogTranslate (:306-317)
-    pos = pos + vel * dt;
+    if (!S.quiet) {
+      if (homo) vel = vel + m3v(S.dVelGrad, pos);   // leapfrogTranslate (:306-317)
+      pos = pos + vel * dt;
+    }
     d.pos[b] = dd4(pos, 0);
     d.ori[b] = make_double4(ori.w, ori.x, ori.y, ori.z);
     d.vel[b] = dd4(vel, 0); d.angVel[b] = dd4(angVel, 0); d.angMom[b] = dd4(angMom, 0);
@@ -2139,6 +2447,7 @@ __global__ void k_reset_queue(Dev d) { d.S->lmCount = 0; d.S->lmHead = 0; }
 // cell-size-change velocity that seeds maxVelocitySq, and the gradients the body update uses.
 __global__ void k_newton_begin(Dev d) {
   SceneState& S = *d.S;
+  if (S.skip) return;
   if (!S.periodic) { S.cellTerm = 0; return; }
   bool nz = false;
   for (int k = 0; k < 9; k++) nz |= (S.nextVelGrad[k] != 0);
@@ -2157,6 +2466,8 @@ __global__ void k_newton_begin(Dev d) {
 
 __global__ void k_end(Dev d) {
   SceneState& S = *d.S;
+  if (S.skip) return;
+  S.quiet = 0;       // NewtonIntegrator resets quiet_system_flag (:299)
   if (S.periodic) {  // end of NewtonIntegrator::action (:300-302)
     for (int k = 0; k < 3; k++) S.prevCellSize[k] = S.cellSize[k];
     for (int k = 0; k < 9; k++) S.prevVelGrad[k] = S.velGrad[k];
@@ -2185,6 +2496,7 @@ struct sqdem_ctx {
   sqdem_params params;
   int recordFull = 0;
   int lmSpread = 1;
+  bool servoOn = false;
   std::vector<int> kind, wallIds, matIds, isSphere, axisSense;
   std::vector<double> shape5;
   int nMats = 0;
@@ -2282,6 +2594,12 @@ static void enqueueStep(sqdem_ctx* c, bool timed) {
   c->launches += 2;
   if (timed) cudaEventRecord(c->ev[2], s);
   if (d.W > 0) { k_wall_forces<<<d.W, 128, 0, s>>>(d); c->launches++; }
+  if (c->servoOn) {   // CompressionEngine between InteractionLoop and NewtonIntegrator
+    k_servo_gate<<<1, 1, 0, s>>>(d);
+    k_servo_sums<<<d.svBlocks, 128, 0, s>>>(d, -1, 1);
+    k_servo<<<1, 1, 0, s>>>(d);
+    c->launches += 3;
+  }
   k_newton_begin<<<1, 1, 0, s>>>(d);
   k_integrate<<<nblk(N, 256), 256, 0, s>>>(d);
   k_end<<<1, 1, 0, s>>>(d);
@@ -2528,6 +2846,9 @@ sqdem_status sqdem_set_bodies(sqdem_ctx* c, int n, const int* kind, const double
   CK(dalloc(c, &d.pList, d.Pcap));
   CK(dalloc(c, &d.wCount, 2 * std::max(d.W, 1))); CK(dalloc(c, &d.wList, d.Pcap));
   CK(dalloc(c, &d.wBlk, (size_t)WALL_CHUNKS * std::max(d.W, 1)));
+  d.svBlocks = std::max(1, std::min(nblk(d.Pcap, 128), c->numSMs * 2));
+  CK(dalloc(c, &d.wallKn, std::max(d.W, 1))); CK(dalloc(c, &d.svPart, (size_t)d.svBlocks * SV_PART));
+  c->servoOn = false;
   CK(dalloc(c, &d.ww, std::max(d.W * d.W, 1)));
   CK(dalloc(c, &d.lmQueue, d.Pcap));
   CK(dalloc(c, &d.bodyCell, n)); CK(dalloc(c, &d.cellCount, d.Gmax + 1)); CK(dalloc(c, &d.cellStart, d.Gmax + 1));
@@ -2579,6 +2900,7 @@ sqdem_status sqdem_set_bodies(sqdem_ctx* c, int n, const int* kind, const double
   SceneState S;
   std::memset(&S, 0, sizeof(S));
   S.maxVelocitySq = nan; S.fastestBodyMaxDist = -1; S.verletDistCur = c->params.verletDist;
+  S.haltAt = -1;
   CK(up(d.S, &S, sizeof(S)));
   c->haveBodies = true;
   c->graphValid = false;
@@ -3137,4 +3459,176 @@ sqdem_status sqdem_set_lm_spread(sqdem_ctx* c, int on) {
   return SQDEM_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Boundary controller (CompressionEngine), quiet flag, Shop reductions.
+sqdem_status sqdem_set_servo(sqdem_ctx* c, const double* g) {
+  if (!c || !g) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "set bodies first");
+  CK(cudaSetDevice(c->device));
+  ServoDev C;
+  std::memset(&C, 0, sizeof(C));
+  const bool on = g[0] != 0;
+  if (on) {
+    for (int k = 0; k < 6; k++)
+      if ((int)c->kind.size() <= k || c->kind[k] != SQDEM_WALL || (int)c->wallIds.size() <= k || c->wallIds[k] != k)
+        return fail(c, SQDEM_ERR_ARG, "CompressionEngine needs bodies 0-5 to be the six walls (left, right, front, back, bottom, top)");
+    for (int k = 0; k < 30; k++) if (!std::isfinite(g[k])) return fail(c, SQDEM_ERR_ARG, "non-finite servo parameter");
+    if (!(g[13] >= 1) || !(g[14] >= 1)) return fail(c, SQDEM_ERR_ARG, "echo_interval and savedata_interval must be >= 1");
+    C.z_servo = g[1] != 0; C.continueFlag = g[2] != 0; C.hydroStrain = g[3] != 0; C.shearMode = (int)g[4];
+    for (int k = 0; k < 6; k++) C.activated[k] = g[5 + k] != 0;
+    C.iterate_num_max = (unsigned)g[11]; C.solve_num_max = (unsigned)g[12]; C.echo_interval = (unsigned)g[13];
+    C.savedata_interval = (unsigned)g[14]; C.ramp_interval = (unsigned)g[15]; C.ramp_chunks = (unsigned)g[16];
+    C.goalx = g[17]; C.goaly = g[18]; C.goalz = g[19];
+    C.gain_alpha = g[20]; C.target_strain = g[21]; C.f_threshold = g[22]; C.fmin_threshold = g[23];
+    C.unbf_tol = g[24]; C.max_vel = g[25]; C.hydroStrainRate = g[26];
+    C.width0 = g[27]; C.height0 = g[28]; C.depth0 = g[29];
+    C.firstRun = 1; C.UnbalancedForce = 1;
+    double pv = 0, props[5];
+    for (size_t i = 0; i < c->kind.size(); i++)
+      if (c->kind[i] == SQDEM_SUPERQUADRIC) {
+        const double* s5 = &c->shape5[5 * i];
+        sqdem_shape_props(s5[0], s5[1], s5[2], s5[3], s5[4], props);
+        pv += props[0];
+      }
+    C.pvol = pv;
+  }
+  C.enabled = on ? 1 : 0;
+  CK(cudaMemcpyAsync((char*)c->d.S + offsetof(SceneState, sv), &C, sizeof(C), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->servoOn != on) { c->servoOn = on; c->graphValid = false; }
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_get_servo(sqdem_ctx* c, double* o) {
+  if (!c || !o) return SQDEM_ERR_ARG;
+  for (int k = 0; k < SQDEM_SERVO_STATE; k++) o[k] = 0;
+  if (!c->haveBodies) return SQDEM_OK;
+  CK(cudaSetDevice(c->device));
+  SceneState S; sqdem_status st = readScene(c, S); if (st) return st;
+  const ServoDev& C = S.sv;
+  const double v[34] = {C.width, C.depth, C.height, C.x_area, C.y_area, C.z_area, C.wsxx, C.wsyy, C.wszz,
+                        C.wsxx_left, C.wsxx_right, C.wsyy_front, C.wsyy_back, C.wszz_bottom, C.wszz_top,
+                        C.gain_x, C.gain_x1, C.gain_y, C.gain_y1, C.gain_z, C.gain_z1, C.UnbalancedForce,
+                        C.particlesVolume, C.Init_boxVolume, C.Current_boxVolume, C.strain2,
+                        (double)C.iterate_num, (double)C.solve_num, (double)C.rampNum, (double)C.Flag_ForceTarget,
+                        (double)C.firstRun, C.width0, C.height0, C.depth0};
+  if (C.enabled) for (int k = 0; k < 34; k++) o[k] = v[k];
+  o[34] = (double)S.haltAt; o[35] = S.quiet ? 1 : 0;
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_put_servo(sqdem_ctx* c, const double* o) {
+  if (!c || !o) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  SceneState S; sqdem_status st = readScene(c, S); if (st) return st;
+  ServoDev& C = S.sv;
+  if (C.enabled) {
+    C.width = o[0]; C.depth = o[1]; C.height = o[2]; C.x_area = o[3]; C.y_area = o[4]; C.z_area = o[5];
+    C.wsxx = o[6]; C.wsyy = o[7]; C.wszz = o[8]; C.wsxx_left = o[9]; C.wsxx_right = o[10]; C.wsyy_front = o[11];
+    C.wsyy_back = o[12]; C.wszz_bottom = o[13]; C.wszz_top = o[14];
+    C.gain_x = o[15]; C.gain_x1 = o[16]; C.gain_y = o[17]; C.gain_y1 = o[18]; C.gain_z = o[19]; C.gain_z1 = o[20];
+    C.UnbalancedForce = o[21]; C.particlesVolume = o[22]; C.Init_boxVolume = o[23]; C.Current_boxVolume = o[24];
+    C.strain2 = o[25]; C.iterate_num = (unsigned)o[26]; C.solve_num = (unsigned)o[27]; C.rampNum = (unsigned)o[28];
+    C.Flag_ForceTarget = o[29] != 0; C.firstRun = o[30] != 0; C.width0 = o[31]; C.height0 = o[32]; C.depth0 = o[33];
+    CK(cudaMemcpyAsync((char*)c->d.S + offsetof(SceneState, sv), &C, sizeof(C), cudaMemcpyHostToDevice, c->stream));
+  }
+  long long halt = (long long)o[34];
+  int quiet = o[35] != 0;
+  CK(cudaMemcpyAsync((char*)c->d.S + offsetof(SceneState, haltAt), &halt, sizeof(halt), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync((char*)c->d.S + offsetof(SceneState, quiet), &quiet, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_set_quiet(sqdem_ctx* c, int on) {
+  if (!c) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  int q = on ? 1 : 0;
+  CK(cudaMemcpyAsync((char*)c->d.S + offsetof(SceneState, quiet), &q, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SQDEM_OK;
+}
+
+// block partials of k_servo_sums summed in block order
+static sqdem_status svSums(sqdem_ctx* c, int need, double* tot) {
+  k_servo_sums<<<c->d.svBlocks, 128, 0, c->stream>>>(c->d, need, 0);
+  CK(cudaGetLastError());
+  std::vector<double> part((size_t)c->d.svBlocks * SV_PART);
+  CK(cudaMemcpyAsync(part.data(), c->d.svPart, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < SV_PART; k++) {
+    double s = 0;
+    for (int b = 0; b < c->d.svBlocks; b++) s += part[(size_t)b * SV_PART + k];
+    tot[k] = s;
+  }
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_unbalanced_force(sqdem_ctx* c, int use_max, double* out) {
+  if (!c || !out) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  if (!use_max) {
+    double tot[SV_PART];
+    sqdem_status s = svSums(c, 2, tot); if (s) return s;
+    *out = tot[10] / (tot[9] * 2.0);
+    return SQDEM_OK;
+  }
+  // largest |F + m g| over dynamic bodies (first in id order), over the sum of |Fn + Fs| of its
+  // contacts with a non-zero normal force
+  const int n = c->d.N;
+  std::vector<double4> F(n); std::vector<double> m(n); std::vector<unsigned> bl(n);
+  CK(cudaMemcpy(F.data(), c->d.force, sizeof(double4) * n, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(m.data(), c->d.mass, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(bl.data(), c->d.blocked, sizeof(unsigned) * n, cudaMemcpyDeviceToHost));
+  double maxF = 0; int idMax = -1;
+  for (int b = 0; b < n; b++) {
+    if (bl[b] == DOF_ALL) continue;
+    const double x = F[b].x + m[b] * c->params.gravity[0], y = F[b].y + m[b] * c->params.gravity[1],
+                 z = F[b].z + m[b] * c->params.gravity[2];
+    const double f = std::sqrt(x * x + (y * y + z * z));
+    if (f > maxF) { maxF = f; idMax = b; }
+  }
+  SceneState S; sqdem_status st = readScene(c, S); if (st) return st;
+  const int P = S.P;
+  std::vector<int> ow(P), pa(P); std::vector<unsigned> fl(P); std::vector<double4> nf(P), sh(P);
+  if (P) {
+    CK(cudaMemcpy(ow.data(), c->d.A.owner, 4 * (size_t)P, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(pa.data(), c->d.A.partner, 4 * (size_t)P, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(fl.data(), c->d.A.flags, 4 * (size_t)P, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(nf.data(), c->d.A.nforce, sizeof(double4) * P, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(sh.data(), c->d.A.shear, sizeof(double4) * P, cudaMemcpyDeviceToHost));
+  }
+  double maxCF = 0;
+  for (int e = 0; e < P; e++) {
+    if ((fl[e] & (F_GEOM | F_PHYS)) != (F_GEOM | F_PHYS)) continue;
+    if (!(ow[e] == idMax || pa[e] == idMax)) continue;
+    const double nn = std::sqrt(nf[e].x * nf[e].x + (nf[e].y * nf[e].y + nf[e].z * nf[e].z));
+    if (nn == 0) continue;
+    const double x = nf[e].x + sh[e].x, y = nf[e].y + sh[e].y, z = nf[e].z + sh[e].z;
+    maxCF += std::sqrt(x * x + (y * y + z * z));
+  }
+  *out = maxF / maxCF;
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_get_stress(sqdem_ctx* c, double volume, double* out9) {
+  if (!c || !out9) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  SceneState S; sqdem_status st = readScene(c, S); if (st) return st;
+  if (volume == 0) {
+    if (S.periodic) {
+      const double* A = S.hSize;
+      volume = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) + A[2] * (A[3] * A[7] - A[4] * A[6]);
+    } else volume = 1;
+  }
+  double tot[SV_PART];
+  sqdem_status s = svSums(c, 1, tot); if (s) return s;
+  for (int k = 0; k < 9; k++) out9[k] = tot[11 + k] / volume;
+  return SQDEM_OK;
+}
 }  // extern "C"
