@@ -35,6 +35,7 @@ extern "C" {
 #endif
 
 typedef struct sqdem_ctx sqdem_ctx;
+typedef struct sqdem_batch sqdem_batch;
 
 typedef enum {
   SQDEM_OK = 0,
@@ -242,6 +243,32 @@ sqdem_status sqdem_set_quiet(sqdem_ctx* ctx, int on);
  * meaning the periodic cell's volume (1 without a cell).  Sums follow table order. */
 sqdem_status sqdem_unbalanced_force(sqdem_ctx* ctx, int use_max, double* out);
 sqdem_status sqdem_get_stress(sqdem_ctx* ctx, double volume, double* out9);
+
+/* ---------------------------------------------------------------------------------------
+ * Batches of independent specimens (no counterpart in the reference, which runs one Scene per
+ * process): n scenes, each a full context set up through the functions above
+ * (sqdem_batch_scene gives its handle), stepped together by one CUDA graph launch per step in
+ * which every scene's step is a parallel branch.  A scene's results are exactly those of its
+ * context stepped alone.  Changing a scene (bodies, engine) rebuilds the graph at the next
+ * step.  Scenes of a batch share one device; sqdem_destroy must not be called on them. */
+sqdem_status sqdem_batch_create(sqdem_batch** out, int n_scenes, const sqdem_config* cfg);
+void sqdem_batch_destroy(sqdem_batch* batch);
+const char* sqdem_batch_last_error(sqdem_batch* batch);
+int sqdem_batch_size(sqdem_batch* batch);
+sqdem_status sqdem_batch_scene(sqdem_batch* batch, int i, sqdem_ctx** ctx);
+/* Advance every scene nsteps timesteps (asynchronous on the batch stream). */
+sqdem_status sqdem_batch_step(sqdem_batch* batch, int nsteps);
+/* Wait, read and clear every scene's error words: counters summed, lm_rounds_max the largest;
+ * returns the first scene's error (e.g. SQDEM_ERR_CAPACITY). */
+sqdem_status sqdem_batch_sync(sqdem_batch* batch, sqdem_report* total);
+/* Device time of nsteps batch steps (graph launches, inputs resident), milliseconds. */
+sqdem_status sqdem_batch_time_steps(sqdem_batch* batch, int nsteps, double* ms);
+/* End to end: per step, all scenes' kinematics (16 doubles per body, scenes in order, the
+ * sqdem_get_kinematics layout) copied from host in16 (alternating with out16) to the device,
+ * one batch step, and copied back. */
+sqdem_status sqdem_batch_time_e2e(sqdem_batch* batch, int nsteps, const double* in16, double* out16, double* ms);
+/* Kernel launches of one batch step (all scenes). */
+long long sqdem_batch_launch_count(sqdem_batch* batch);
 
 #ifdef __cplusplus
 }

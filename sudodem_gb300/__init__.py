@@ -7,4 +7,4 @@ SuperquadricsLaw, NewtonIntegrator, ForceResetter) so that an ``O.engines`` list
 SudoDEM3D runs unchanged; the timestep itself runs on the GPU through libsqdem_gpu.so.
 """
 from . import assemblies  # noqa: F401
-from ._native import Engine, SqdemError, shape_props  # noqa: F401
+from ._native import Batch, Engine, SqdemError, shape_props  # noqa: F401

@@ -96,6 +96,12 @@ def load_library(build_if_missing=True):
         "sqdem_set_servo": (i, [v, dp]), "sqdem_get_servo": (i, [v, dp]), "sqdem_put_servo": (i, [v, dp]),
         "sqdem_set_quiet": (i, [v, i]), "sqdem_unbalanced_force": (i, [v, i, dp]),
         "sqdem_get_stress": (i, [v, C.c_double, dp]),
+        "sqdem_batch_create": (i, [C.POINTER(v), i, C.c_void_p]), "sqdem_batch_destroy": (None, [v]),
+        "sqdem_batch_last_error": (C.c_char_p, [v]), "sqdem_batch_size": (i, [v]),
+        "sqdem_batch_scene": (i, [v, i, C.POINTER(v)]), "sqdem_batch_step": (i, [v, i]),
+        "sqdem_batch_sync": (i, [v, C.c_void_p]), "sqdem_batch_time_steps": (i, [v, i, dp]),
+        "sqdem_batch_time_e2e": (i, [v, i, C.c_void_p, C.c_void_p, dp]),
+        "sqdem_batch_launch_count": (C.c_longlong, [v]),
         "sqdem_set_periodic": (i, [v, dp, dp]),
         "sqdem_set_velgrad": (i, [v, dp]),
         "sqdem_get_cell": (i, [v, dp]),
@@ -119,7 +125,9 @@ def exported_symbols():
             "sqdem_time_e2e", "sqdem_time_contacts", "sqdem_set_use_graph", "sqdem_set_lm_spread", "sqdem_set_periodic",
             "sqdem_set_velgrad", "sqdem_get_cell", "sqdem_put_cell", "sqdem_contacts_static_queue",
             "sqdem_set_servo", "sqdem_get_servo", "sqdem_put_servo", "sqdem_set_quiet", "sqdem_unbalanced_force",
-            "sqdem_get_stress"]
+            "sqdem_get_stress", "sqdem_batch_create", "sqdem_batch_destroy", "sqdem_batch_last_error",
+            "sqdem_batch_size", "sqdem_batch_scene", "sqdem_batch_step", "sqdem_batch_sync", "sqdem_batch_time_steps",
+            "sqdem_batch_time_e2e", "sqdem_batch_launch_count"]
 
 
 def _dp(a):
@@ -143,8 +151,13 @@ def shape_props(rx, ry, rz, eps1, eps2):
 class Engine:
     """One GPU scene behind the C ABI."""
 
-    def __init__(self, device=0, precision="fp64", contacts_per_body=16, use_graph=True):
+    def __init__(self, device=0, precision="fp64", contacts_per_body=16, use_graph=True, _handle=None):
         self.lib = load_library()
+        self.n = 0
+        if _handle is not None:     # a scene of a Batch: the batch owns the context
+            self.h, self._owned = _handle, False
+            return
+        self._owned = True
         self.h = C.c_void_p()
         cfg = _Config(device, PRECISION[precision], contacts_per_body, 1 if use_graph else 0)
         st = self.lib.sqdem_create(C.byref(self.h), C.byref(cfg))
@@ -160,9 +173,9 @@ class Engine:
             raise SqdemError(st, self.lib.sqdem_last_error(self.h).decode())
 
     def close(self):
-        if self.h:
+        if self.h and self._owned:
             self.lib.sqdem_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -341,3 +354,74 @@ class Engine:
     def put_scalars(self, s):
         s = np.ascontiguousarray(s, dtype=np.float64)
         self._check(self.lib.sqdem_put_scalars(self.h, _dp(s)))
+
+
+class Batch:
+    """Independent specimens stepped together: one context per scene (``scenes[i]``, an
+    Engine), one CUDA graph launch per step running every scene's step as a parallel branch."""
+
+    def __init__(self, n_scenes, device=0, precision="fp64", contacts_per_body=16):
+        self.lib = load_library()
+        self.h = C.c_void_p()
+        cfg = _Config(device, PRECISION[precision], contacts_per_body, 1)
+        st = self.lib.sqdem_batch_create(C.byref(self.h), int(n_scenes), C.c_void_p(C.addressof(cfg)))
+        if st:
+            msg = self.lib.sqdem_batch_last_error(self.h).decode()
+            self.lib.sqdem_batch_destroy(self.h)
+            self.h = None
+            raise SqdemError(st, msg)
+        self.scenes = []
+        for i in range(n_scenes):
+            ctx = C.c_void_p()
+            self._check(self.lib.sqdem_batch_scene(self.h, i, C.byref(ctx)))
+            self.scenes.append(Engine(_handle=ctx))
+
+    def _check(self, st):
+        if st:
+            raise SqdemError(st, self.lib.sqdem_batch_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            for e in self.scenes:
+                e.h = None
+            self.lib.sqdem_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load(self, specs, servo=None):
+        for e, spec in zip(self.scenes, specs):
+            e.load(spec)
+            if servo is not None:
+                e.set_servo(servo)
+
+    @property
+    def n_bodies(self):
+        return sum(e.n for e in self.scenes)
+
+    def step(self, n=1):
+        self._check(self.lib.sqdem_batch_step(self.h, int(n)))
+
+    def sync(self):
+        r = _Report()
+        st = self.lib.sqdem_batch_sync(self.h, C.c_void_p(C.addressof(r)))
+        rep = {f: getattr(r, f) for f, _ in _Report._fields_}
+        self._check(st)
+        return rep
+
+    def time_steps(self, n):
+        ms = np.zeros(1)
+        self._check(self.lib.sqdem_batch_time_steps(self.h, int(n), _dp(ms)))
+        return float(ms[0])
+
+    def time_e2e(self, n, in_ptr, out_ptr):
+        ms = np.zeros(1)
+        self._check(self.lib.sqdem_batch_time_e2e(self.h, int(n), C.c_void_p(in_ptr), C.c_void_p(out_ptr), _dp(ms)))
+        return float(ms[0])
+
+    def launch_count(self):
+        return int(self.lib.sqdem_batch_launch_count(self.h))

@@ -140,6 +140,7 @@ struct Dev {
   unsigned long long* bbPart;
   // boundary controller: per-wall kn sums of real contacts, per-block partial sums
   double* wallKn; double* svPart; int svBlocks;
+  int wallChunks, lmBlocks;   // grids sized to the scene
 };
 
 __device__ __forceinline__ unsigned long long encOrd(double x) {
@@ -823,14 +824,14 @@ __global__ void k_psort(Dev d) {
 // each wall's entries per chunk; k_wall_lists places chunk b's entries of wall w after
 // those of the walls before w and of the chunks before b, in table order within the chunk
 // (one block scan per wall and tile).
-static const int WALL_CHUNKS = 256, MAX_WALLS = 64;
+static const int WALL_CHUNKS = 256, MAX_WALLS = 64;   // WALL_CHUNKS: most chunks of a table
 __device__ __forceinline__ int wallSlot(const Dev& d, int p) {
   if (d.info[p].x != KIND_WALL) return -1;
   for (int w = 0; w < d.W; w++) if (d.walls[w] == p) return w;
   return -1;
 }
-__device__ __forceinline__ void wallChunk(int P, int b, int& lo, int& hi) {
-  const int len = (P + WALL_CHUNKS - 1) / WALL_CHUNKS;
+__device__ __forceinline__ void wallChunk(int P, int chunks, int b, int& lo, int& hi) {
+  const int len = (P + chunks - 1) / chunks;
   lo = min(P, b * len); hi = min(P, lo + len);
 }
 __global__ void k_wall_count(Dev d) {
@@ -840,7 +841,7 @@ __global__ void k_wall_count(Dev d) {
   for (int w = threadIdx.x; w < d.W; w += blockDim.x) cnt[w] = 0;
   __syncthreads();
   int lo, hi;
-  wallChunk(S.P, blockIdx.x, lo, hi);
+  wallChunk(S.P, d.wallChunks, blockIdx.x, lo, hi);
   for (int e = lo + threadIdx.x; e < hi; e += blockDim.x) {
     const int w = wallSlot(d, d.A.partner[e]);
     if (w >= 0) atomicAdd(&cnt[w], 1);
@@ -855,7 +856,7 @@ __global__ void k_wall_lists(Dev d) {
   __shared__ int tot[MAX_WALLS], off[MAX_WALLS];
   for (int w = threadIdx.x; w < d.W; w += blockDim.x) {
     int before = 0, all = 0;
-    for (int b = 0; b < WALL_CHUNKS; b++) {
+    for (int b = 0; b < d.wallChunks; b++) {
       const int c = d.wBlk[b * d.W + w];
       all += c;
       if (b < blockIdx.x) before += c;
@@ -873,7 +874,7 @@ __global__ void k_wall_lists(Dev d) {
   }
   __syncthreads();
   int lo, hi;
-  wallChunk(S.P, blockIdx.x, lo, hi);
+  wallChunk(S.P, d.wallChunks, blockIdx.x, lo, hi);
   for (int e0 = lo; e0 < hi; e0 += blockDim.x) {
     const int e = e0 + threadIdx.x;
     const int ws = e < hi ? wallSlot(d, d.A.partner[e]) : -1;
@@ -2491,6 +2492,7 @@ struct sqdem_ctx {
   Dev d;
   bool haveBodies = false, haveMats = false, haveParams = false;
   cudaGraph_t graph = nullptr; cudaGraphExec_t exec = nullptr; bool graphValid = false;
+  unsigned epoch = 0;   // counts changes of the step's kernel sequence (graphs capturing it are stale)
   std::string err;
   std::vector<void*> allocs;
   sqdem_params params;
@@ -2527,7 +2529,7 @@ static cudaError_t dalloc(sqdem_ctx* c, T** p, size_t n) {
 static void freeAll(sqdem_ctx* c) {
   if (c->exec) { cudaGraphExecDestroy(c->exec); c->exec = nullptr; }
   if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
-  c->graphValid = false;
+  c->graphValid = false; c->epoch++;
   for (void* p : c->allocs) cudaFree(p);
   c->allocs.clear();
 }
@@ -2583,14 +2585,17 @@ static void enqueueStep(sqdem_ctx* c, bool timed) {
   k_psort<<<nblk(N, 256), 256, 0, s>>>(d);
   c->launches += 2;
   if (d.W > 0) {
-    k_wall_count<<<WALL_CHUNKS, 256, 0, s>>>(d);
-    k_wall_lists<<<WALL_CHUNKS, 256, 0, s>>>(d);
+    k_wall_count<<<d.wallChunks, 256, 0, s>>>(d);
+    k_wall_lists<<<d.wallChunks, 256, 0, s>>>(d);
     c->launches += 2;
   }
   if (timed) cudaEventRecord(c->ev[1], s);
   k_contacts_pre<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, s>>>(d);
-  if (c->precision == SQDEM_MIXED) k_contacts_lm_mixed<<<c->numSMs * c->lmBlocksPerSMmixed, LM_BS, 0, s>>>(d);
-  else k_contacts_lm<<<c->numSMs * c->lmBlocksPerSM, LM_BS, 0, s>>>(d);
+  // LM grid: all resident blocks, fewer for a small table (at most one lane per 4 entries)
+  const int lmFull = c->numSMs * (c->precision == SQDEM_MIXED ? c->lmBlocksPerSMmixed : c->lmBlocksPerSM);
+  const int lmGrid = std::max(1, std::min(lmFull, nblk(d.Pcap, LM_BS * 4)));
+  if (c->precision == SQDEM_MIXED) k_contacts_lm_mixed<<<lmGrid, LM_BS, 0, s>>>(d);
+  else k_contacts_lm<<<lmGrid, LM_BS, 0, s>>>(d);
   c->launches += 2;
   if (timed) cudaEventRecord(c->ev[2], s);
   if (d.W > 0) { k_wall_forces<<<d.W, 128, 0, s>>>(d); c->launches++; }
@@ -2845,7 +2850,8 @@ sqdem_status sqdem_set_bodies(sqdem_ctx* c, int n, const int* kind, const double
   CK(dalloc(c, &d.pCount, n + 1)); CK(dalloc(c, &d.pStart, n + 1)); CK(dalloc(c, &d.pFill, n + 1));
   CK(dalloc(c, &d.pList, d.Pcap));
   CK(dalloc(c, &d.wCount, 2 * std::max(d.W, 1))); CK(dalloc(c, &d.wList, d.Pcap));
-  CK(dalloc(c, &d.wBlk, (size_t)WALL_CHUNKS * std::max(d.W, 1)));
+  d.wallChunks = std::max(1, std::min(WALL_CHUNKS, nblk(d.Pcap, 4096)));
+  CK(dalloc(c, &d.wBlk, (size_t)d.wallChunks * std::max(d.W, 1)));
   d.svBlocks = std::max(1, std::min(nblk(d.Pcap, 128), c->numSMs * 2));
   CK(dalloc(c, &d.wallKn, std::max(d.W, 1))); CK(dalloc(c, &d.svPart, (size_t)d.svBlocks * SV_PART));
   c->servoOn = false;
@@ -2903,7 +2909,7 @@ sqdem_status sqdem_set_bodies(sqdem_ctx* c, int n, const int* kind, const double
   S.haltAt = -1;
   CK(up(d.S, &S, sizeof(S)));
   c->haveBodies = true;
-  c->graphValid = false;
+  c->graphValid = false; c->epoch++;
   if ((s = uploadParams(c))) return s;
   CK(cudaStreamSynchronize(c->stream));
   return SQDEM_OK;
@@ -3496,7 +3502,7 @@ sqdem_status sqdem_set_servo(sqdem_ctx* c, const double* g) {
   C.enabled = on ? 1 : 0;
   CK(cudaMemcpyAsync((char*)c->d.S + offsetof(SceneState, sv), &C, sizeof(C), cudaMemcpyHostToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
-  if (c->servoOn != on) { c->servoOn = on; c->graphValid = false; }
+  if (c->servoOn != on) { c->servoOn = on; c->graphValid = false; c->epoch++; }
   return SQDEM_OK;
 }
 
@@ -3631,4 +3637,233 @@ sqdem_status sqdem_get_stress(sqdem_ctx* c, double volume, double* out9) {
   for (int k = 0; k < 9; k++) out9[k] = tot[11 + k] / volume;
   return SQDEM_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Batches of independent scenes (specimens): one context per scene, one CUDA graph that runs
+// one step of every scene as parallel branches, so that the scenes' kernels share the GPU.
+// Each scene's kernels and results are exactly those of a context stepped alone.
+}  // extern "C"
+struct BatchPtrs { double4 *pos, *ori, *vel, *angVel, *angMom; long long off; int n; };
+
+__global__ void k_batch_kin(const BatchPtrs* P, int ns, double* kin, long long rows, int toDevice) {
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < rows; r += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = ns - 1;
+    while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (P[mid].off <= r) lo = mid; else hi = mid - 1; }
+    const BatchPtrs& s = P[lo];
+    const int b = (int)(r - s.off);
+    double* k = kin + r * 16;
+    if (toDevice) {
+      s.pos[b] = make_double4(k[0], k[1], k[2], 0); s.ori[b] = make_double4(k[3], k[4], k[5], k[6]);
+      s.vel[b] = make_double4(k[7], k[8], k[9], 0); s.angVel[b] = make_double4(k[10], k[11], k[12], 0);
+      s.angMom[b] = make_double4(k[13], k[14], k[15], 0);
+    } else {
+      const double4 p = s.pos[b], o = s.ori[b], v = s.vel[b], w = s.angVel[b], m = s.angMom[b];
+      k[0] = p.x; k[1] = p.y; k[2] = p.z; k[3] = o.x; k[4] = o.y; k[5] = o.z; k[6] = o.w;
+      k[7] = v.x; k[8] = v.y; k[9] = v.z; k[10] = w.x; k[11] = w.y; k[12] = w.z; k[13] = m.x; k[14] = m.y; k[15] = m.z;
+    }
+  }
+}
+
+struct sqdem_batch {
+  int device = 0;
+  std::vector<sqdem_ctx*> scenes;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraph_t graph = nullptr; cudaGraphExec_t exec = nullptr;
+  std::vector<unsigned> epochs;
+  long long launchesPerStep = 0;
+  BatchPtrs* dPtrs = nullptr; double* dKin = nullptr; long long rows = 0;
+  std::string err;
+};
+
+static sqdem_status bfail(sqdem_batch* b, sqdem_status s, const std::string& m) {
+  if (b) b->err = m;
+  return s;
+}
+#define BK(call)                                                                                     \
+  do {                                                                                               \
+    cudaError_t e_ = (call);                                                                         \
+    if (e_ != cudaSuccess) return bfail(B, SQDEM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+static void batchFreeGraph(sqdem_batch* B) {
+  if (B->exec) { cudaGraphExecDestroy(B->exec); B->exec = nullptr; }
+  if (B->graph) { cudaGraphDestroy(B->graph); B->graph = nullptr; }
+  B->epochs.clear();
+}
+
+static sqdem_status batchReady(sqdem_batch* B) {
+  for (size_t i = 0; i < B->scenes.size(); i++) {
+    const sqdem_ctx* c = B->scenes[i];
+    if (!c->haveBodies || !c->haveMats) return bfail(B, SQDEM_ERR_STATE, "scene " + std::to_string(i) + ": bodies and materials must be set");
+  }
+  bool stale = B->exec == nullptr || B->epochs.size() != B->scenes.size();
+  for (size_t i = 0; !stale && i < B->scenes.size(); i++) stale = B->epochs[i] != B->scenes[i]->epoch;
+  if (!stale) return SQDEM_OK;
+  batchFreeGraph(B);
+  BK(cudaSetDevice(B->device));
+  BK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+  BK(cudaEventRecord(B->fork, B->stream));
+  long long l = 0;
+  for (size_t i = 0; i < B->scenes.size(); i++) {
+    sqdem_ctx* c = B->scenes[i];
+    BK(cudaStreamWaitEvent(c->stream, B->fork, 0));
+    const long long l0 = c->launches;
+    enqueueStep(c, false);
+    l += c->launches - l0;
+    c->launches = l0;
+    BK(cudaEventRecord(B->join[i], c->stream));
+    BK(cudaStreamWaitEvent(B->stream, B->join[i], 0));
+  }
+  BK(cudaStreamEndCapture(B->stream, &B->graph));
+  BK(cudaGraphInstantiate(&B->exec, B->graph, 0));
+  B->launchesPerStep = l;
+  for (sqdem_ctx* c : B->scenes) B->epochs.push_back(c->epoch);
+  return SQDEM_OK;
+}
+
+extern "C" {
+
+sqdem_status sqdem_batch_create(sqdem_batch** out, int n_scenes, const sqdem_config* cfg) {
+  if (!out || n_scenes <= 0) return SQDEM_ERR_ARG;
+  sqdem_batch* B = new sqdem_batch();
+  *out = B;
+  B->device = cfg ? cfg->device : 0;
+  BK(cudaSetDevice(B->device));
+  BK(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+  BK(cudaEventCreateWithFlags(&B->fork, cudaEventDisableTiming));
+  BK(cudaEventCreate(&B->t0)); BK(cudaEventCreate(&B->t1));
+  B->join.resize(n_scenes);
+  for (int i = 0; i < n_scenes; i++) {
+    BK(cudaEventCreateWithFlags(&B->join[i], cudaEventDisableTiming));
+    sqdem_ctx* c = nullptr;
+    sqdem_status s = sqdem_create(&c, cfg);
+    B->scenes.push_back(c);
+    if (s) return bfail(B, s, "scene " + std::to_string(i) + ": " + (c ? c->err : std::string("create failed")));
+    if (c->device != B->device) return bfail(B, SQDEM_ERR_ARG, "all scenes of a batch share one device");
+  }
+  return SQDEM_OK;
+}
+
+void sqdem_batch_destroy(sqdem_batch* B) {
+  if (!B) return;
+  cudaSetDevice(B->device);
+  if (B->stream) cudaStreamSynchronize(B->stream);
+  batchFreeGraph(B);
+  if (B->dPtrs) cudaFree(B->dPtrs);
+  if (B->dKin) cudaFree(B->dKin);
+  for (cudaEvent_t e : B->join) cudaEventDestroy(e);
+  if (B->fork) cudaEventDestroy(B->fork);
+  if (B->t0) cudaEventDestroy(B->t0);
+  if (B->t1) cudaEventDestroy(B->t1);
+  for (sqdem_ctx* c : B->scenes) sqdem_destroy(c);
+  if (B->stream) cudaStreamDestroy(B->stream);
+  delete B;
+}
+
+const char* sqdem_batch_last_error(sqdem_batch* B) { return B ? B->err.c_str() : "null batch"; }
+
+int sqdem_batch_size(sqdem_batch* B) { return B ? (int)B->scenes.size() : 0; }
+
+sqdem_status sqdem_batch_scene(sqdem_batch* B, int i, sqdem_ctx** ctx) {
+  if (!B || !ctx || i < 0 || i >= (int)B->scenes.size()) return SQDEM_ERR_ARG;
+  *ctx = B->scenes[i];
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_batch_step(sqdem_batch* B, int nsteps) {
+  if (!B || nsteps < 0) return SQDEM_ERR_ARG;
+  BK(cudaSetDevice(B->device));
+  // work queued on a scene's own stream (uploads) precedes the batch's steps
+  for (sqdem_ctx* c : B->scenes) BK(cudaStreamSynchronize(c->stream));
+  sqdem_status s = batchReady(B);
+  if (s) return s;
+  for (int i = 0; i < nsteps; i++) BK(cudaGraphLaunch(B->exec, B->stream));
+  BK(cudaGetLastError());
+  return SQDEM_OK;
+}
+
+// Waits for the batch, then reads every scene's report (summed into total, lm_rounds_max the
+// largest); returns the first scene error (SQDEM_ERR_CAPACITY on an overflow).
+sqdem_status sqdem_batch_sync(sqdem_batch* B, sqdem_report* total) {
+  if (!B) return SQDEM_ERR_ARG;
+  BK(cudaSetDevice(B->device));
+  BK(cudaStreamSynchronize(B->stream));
+  if (total) std::memset(total, 0, sizeof(*total));
+  sqdem_status first = SQDEM_OK;
+  for (size_t i = 0; i < B->scenes.size(); i++) {
+    sqdem_report r;
+    sqdem_status s = sqdem_sync(B->scenes[i], &r);
+    if (s && !first) { first = s; B->err = "scene " + std::to_string(i) + ": " + B->scenes[i]->err; }
+    if (total) {
+      total->nan_normals += r.nan_normals; total->nan_forces += r.nan_forces; total->lm_calls += r.lm_calls;
+      total->lm_iterations += r.lm_iterations; total->lm_maxiter += r.lm_maxiter; total->overflow += r.overflow;
+      total->collider_runs += r.collider_runs; total->steps += r.steps; total->evals_fp32 += r.evals_fp32;
+      total->evals_fp64 += r.evals_fp64; total->lm_rounds_max = std::max(total->lm_rounds_max, r.lm_rounds_max);
+    }
+  }
+  return first;
+}
+
+sqdem_status sqdem_batch_time_steps(sqdem_batch* B, int nsteps, double* ms) {
+  if (!B || !ms || nsteps < 0) return SQDEM_ERR_ARG;
+  BK(cudaSetDevice(B->device));
+  for (sqdem_ctx* c : B->scenes) BK(cudaStreamSynchronize(c->stream));
+  sqdem_status s = batchReady(B);
+  if (s) return s;
+  BK(cudaEventRecord(B->t0, B->stream));
+  for (int i = 0; i < nsteps; i++) BK(cudaGraphLaunch(B->exec, B->stream));
+  BK(cudaEventRecord(B->t1, B->stream));
+  BK(cudaEventSynchronize(B->t1));
+  float t = 0;
+  BK(cudaEventElapsedTime(&t, B->t0, B->t1));
+  *ms = t;
+  return SQDEM_OK;
+}
+
+// End to end through host buffers: every step copies the kinematics of all scenes' bodies
+// (16 doubles per body in scene order, the sqdem_get_kinematics layout) to the device,
+// steps all scenes, and copies them back; in16 and out16 alternate as in sqdem_time_e2e.
+sqdem_status sqdem_batch_time_e2e(sqdem_batch* B, int nsteps, const double* in16, double* out16, double* ms) {
+  if (!B || !ms || !in16 || !out16 || nsteps < 0) return SQDEM_ERR_ARG;
+  BK(cudaSetDevice(B->device));
+  for (sqdem_ctx* c : B->scenes) BK(cudaStreamSynchronize(c->stream));
+  sqdem_status s = batchReady(B);
+  if (s) return s;
+  const int ns = (int)B->scenes.size();
+  long long rows = 0;
+  std::vector<BatchPtrs> hp(ns);
+  for (int i = 0; i < ns; i++) {
+    const Dev& d = B->scenes[i]->d;
+    hp[i] = BatchPtrs{d.pos, d.ori, d.vel, d.angVel, d.angMom, rows, d.N};
+    rows += d.N;
+  }
+  if (!B->dPtrs) BK(cudaMalloc(&B->dPtrs, sizeof(BatchPtrs) * ns));
+  if (B->rows != rows) {
+    if (B->dKin) BK(cudaFree(B->dKin));
+    BK(cudaMalloc(&B->dKin, sizeof(double) * 16 * (size_t)rows));
+    B->rows = rows;
+  }
+  BK(cudaMemcpyAsync(B->dPtrs, hp.data(), sizeof(BatchPtrs) * ns, cudaMemcpyHostToDevice, B->stream));
+  const int grid = std::max(1, std::min(nblk(rows, 256), 4096));
+  const size_t bytes = sizeof(double) * 16 * (size_t)rows;
+  double* bufs[2] = {const_cast<double*>(in16), out16};
+  BK(cudaEventRecord(B->t0, B->stream));
+  for (int i = 0; i < nsteps; i++) {
+    BK(cudaMemcpyAsync(B->dKin, bufs[i & 1], bytes, cudaMemcpyHostToDevice, B->stream));
+    k_batch_kin<<<grid, 256, 0, B->stream>>>(B->dPtrs, ns, B->dKin, rows, 1);
+    BK(cudaGraphLaunch(B->exec, B->stream));
+    k_batch_kin<<<grid, 256, 0, B->stream>>>(B->dPtrs, ns, B->dKin, rows, 0);
+    BK(cudaMemcpyAsync(bufs[(i + 1) & 1], B->dKin, bytes, cudaMemcpyDeviceToHost, B->stream));
+  }
+  BK(cudaEventRecord(B->t1, B->stream));
+  BK(cudaEventSynchronize(B->t1));
+  float t = 0;
+  BK(cudaEventElapsedTime(&t, B->t0, B->t1));
+  *ms = t;
+  return SQDEM_OK;
+}
+
+long long sqdem_batch_launch_count(sqdem_batch* B) { return B ? B->launchesPerStep : 0; }
 }  // extern "C"
