@@ -147,6 +147,48 @@ def cpu_baseline(spec, budget_s=20.0, threads=None):
                       f"{threads} OpenMP threads, {el:.1f} s"}
 
 
+def config2_workload(name, seed):
+    """config2: 512 walled specimens (assemblies.config2); config2_s<K>: its first K specimens."""
+    from sudodem_gb300 import assemblies
+    specs, servo = assemblies.config2(seed=seed)
+    if name.startswith("config2_s"):
+        specs = specs[:int(name[9:])]
+    return specs, servo
+
+
+def _oracle_specimen(args):
+    spec, servo, budget = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import OracleScene
+    o = OracleScene.from_spec(spec, threads=1)
+    o.set_servo(servo)
+    o.step(1)
+    t0 = time.perf_counter()
+    n = 0
+    while n < 200 and time.perf_counter() - t0 < budget:
+        o.step(1)
+        n += 1
+    return spec.n_particles * n, time.perf_counter() - t0
+
+
+def cpu_baseline_batch(specs, servo, budget_s=15.0):
+    """The oracle on a sample of the specimens, one specimen per host core (1 thread each, as the
+    reference runs one scene per process), for about budget_s of wall time."""
+    import multiprocessing as mproc
+    cores = os.cpu_count()
+    sample = specs[:cores]
+    t0 = time.perf_counter()
+    with mproc.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_oracle_specimen, [(sp, servo, budget_s) for sp in sample])
+    wall = time.perf_counter() - t0
+    ps = sum(r[0] for r in res)
+    el = max(r[1] for r in res)
+    return {"value": ps / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"CPU oracle with the CompressionEngine on the first {len(sample)} specimens "
+                      f"({sum(sp.n_particles for sp in sample)} particles), one specimen per core, 1 thread each, "
+                      f"{el:.1f} s timed of {wall:.1f} s wall"}
+
+
 def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
@@ -162,6 +204,19 @@ def dist_setup():
 def run_reference(args):
     rank, ws, dist = dist_setup()
     if rank != 0:
+        return
+    if args.workload.startswith("config2"):
+        specs, servo = config2_workload(args.workload, args.seed)
+        cb = cpu_baseline_batch(specs, servo, budget_s=min(30.0, 3.0 * max(args.steps, 1)))
+        v = cb["value"]
+        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "strong",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+                "config": {"workload": args.workload, "specimens": len(specs),
+                           "particles": int(sum(sp.n_particles for sp in specs)), "precision": "fp64"},
+                "cpu_baseline": cb,
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
         return
     spec = workload_spec(args.workload, args.seed)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -189,7 +244,81 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_ours_batch(args):
+    """Batched specimens (config2): each rank steps its share of the specimens as one batch."""
+    rank, ws, dist = dist_setup()
+    from sudodem_gb300 import Batch
+    from sudodem_gb300.partition import rank_share
+    specs, servo = config2_workload(args.workload, args.seed)
+    sizes = [sp.n_particles for sp in specs]
+    mine = rank_share(sizes, rank, ws)
+    my_specs = [specs[i] for i in mine]
+    b = Batch(len(my_specs), device=0, precision=args.precision, contacts_per_body=args.contacts_per_body)
+    for e in b.scenes:
+        e.set_lm_spread(not args.no_lm_spread)
+    b.load(my_specs, servo=servo)
+    npart = sum(sp.n_particles for sp in my_specs)
+    nbodies = sum(sp.n_bodies for sp in my_specs)
+    b.step(args.warmup)
+    b.sync()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    if dist:
+        dist.barrier()
+    clocks.start()
+    ms = b.time_steps(args.steps)
+    rep = b.sync()
+    clk = clocks.stop()
+    launches = b.launch_count() * args.steps
+    total_particles = sum(sizes)
+    if dist:
+        import torch
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = total_particles * args.steps / (ms / 1e3)
+    nentries = sum(len(e.interactions(True)) for e in b.scenes)
+    peak, peak_kind = measured_peaks()
+    alg_bytes = BYTES_PER_BODY * nbodies + BYTES_PER_PAIR * nentries
+    step_ms = ms / args.steps
+    achieved = alg_bytes / (step_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "batch step (all specimens' kernels, concurrent graph branches)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": None, "algorithmic_bytes": alg_bytes, "launch_ms": step_ms,
+                "note": "contact-stage algorithmic bytes of all specimens per batch step over the step time"}
+    import torch
+    kin = np.concatenate([e.kinematics() for e in b.scenes])
+    hin = torch.empty(kin.shape, dtype=torch.float64, pin_memory=True)
+    hout = torch.empty(kin.shape, dtype=torch.float64, pin_memory=True)
+    hin.numpy()[:] = kin
+    e2e_steps = max(3, min(args.steps, 10))
+    ems = b.time_e2e(e2e_steps, hin.data_ptr(), hout.data_ptr())
+    if dist:
+        t = torch.tensor([ems], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ems = float(t.item())
+    e2e = {"value": total_particles * e2e_steps / (ems / 1e3), "unit": UNIT,
+           "h2d_bytes_per_step": 128 * nbodies, "d2h_bytes_per_step": 128 * nbodies}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_batch(specs, servo, budget_s=min(args.cpu_budget, 15.0))
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "strong",
+                "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+                "data": "synthetic",
+                "config": {"workload": args.workload, "specimens": len(specs), "particles": total_particles,
+                           "particles_rank0": npart, "table_entries_rank0": nentries, "precision": args.precision,
+                           "parallelism": "specimens sharded across ranks (balanced particle counts)",
+                           "engine": "CompressionEngine shear phase, lateral walls at 100 kPa",
+                           "l2": f"inputs larger than L2: {nentries} table entries x >= 256 B on rank 0"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
+                "report": rep}
+        print(json.dumps(line))
+
+
 def run_ours(args):
+    if args.workload.startswith("config2"):
+        return run_ours_batch(args)
     rank, ws, dist = dist_setup()
     from sudodem_gb300 import Engine
     spec = workload_spec(args.workload, args.seed + rank)

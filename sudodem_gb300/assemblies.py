@@ -270,12 +270,16 @@ def config2(seed=0, n_specimens=512, n_range=(300, 8000), friction_range=(0.2, 0
     friction U[0.2, 0.8] per specimen, eps U[0.4, 1.6]; each a cubic_specimen.  Returns the
     list of specs and the CompressionEngine configuration they run with (100 kPa on the
     lateral walls, axial strain at the top and bottom walls: the shear phase of
-    action_cubic, Compression.cpp:485-590)."""
+    action_cubic, Compression.cpp:485-590).  Particles sit on a 2.1 mm lattice with the walls
+    against the outer ones, so most neighbours start in contact."""
     from .servo import servo_config
     rng = np.random.default_rng(seed)
     ns = np.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1]), size=n_specimens)).astype(int)
     mus = rng.uniform(friction_range[0], friction_range[1], size=n_specimens)
-    specs = [cubic_specimen(int(n), seed=seed * 100003 + i, friction=float(mu), eps_range=eps_range)
+    # dense lattice (2.1 mm) with the walls against the outer particles: a compressed
+    # specimen whose contact network is in place from the first step
+    specs = [cubic_specimen(int(n), seed=seed * 100003 + i, friction=float(mu), eps_range=eps_range,
+                            spacing=2.1e-3, wall_gap=0.0)
              for i, (n, mu) in enumerate(zip(ns, mus))]
     servo = servo_config(z_servo=0, shearMode=1, goalx=1e5, goaly=1e5, goalz=0.05, max_vel=1.0,
                          gain_alpha=0.5, ramp_interval=200, ramp_chunks=20, echo_interval=1000,
