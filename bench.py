@@ -47,6 +47,9 @@ def workload_spec(name, seed):
         # same particles on a 2.1 mm lattice: most neighbours start in contact (a compressed state)
         return assemblies.walled_lattice(200_000, seed=seed, box=0.2, per_side=94, spacing=2.1e-3,
                                          eps_range=(0.3, 1.8))
+    if name == "sq20k_dense":
+        return assemblies.walled_lattice(20_000, seed=seed, box=0.095, per_side=44, spacing=2.1e-3,
+                                         eps_range=(0.3, 1.8))
     if name == "sq1k_config0":
         return assemblies.config0(seed=seed)
     if name.startswith("sq") and name.endswith("_walled"):
