@@ -47,7 +47,7 @@ __all__ = ["O", "Omega", "utils", "Body", "State", "Superquadrics", "Wall", "Sup
            "Ig2_Superquadrics_Superquadrics_SuperquadricsGeom", "Ig2_Wall_Superquadrics_SuperquadricsGeom",
            "Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys", "SuperquadricsLaw",
            "Ip2_FrictMat_FrictMat_FrictPhys", "Law2_ScGeom_FrictPhys_CundallStrack", "NewtonIntegrator",
-           "PyRunner", "Cell", "NewSuperquadrics", "NewSuperquadrics2", "NewSuperquadrics_rot", "NewSuperquadrics_rot2",
+           "PyRunner", "CompressionEngine", "unbalancedForce", "getStress", "Cell", "NewSuperquadrics", "NewSuperquadrics2", "NewSuperquadrics_rot", "NewSuperquadrics_rot2",
            "Vector3", "Quaternion"]
 
 
@@ -244,7 +244,63 @@ class InteractionLoop(_Attr):
 
 class NewtonIntegrator(_Attr):
     _defaults = {"damping": 0.2, "gravity": (0.0, 0.0, 0.0), "isSuperquadrics": 0, "exactAsphericalRot": True,
-                 "dead": False, "maxVelocitySq": float("nan")}
+                 "dead": False, "maxVelocitySq": float("nan"), "quiet_system_flag": False}
+
+
+class CompressionEngine(_Attr):
+    """Servo-controlled walls of a cubic specimen (pkg/dem/Compression.hpp:39-252): bodies 0-5 are
+    the walls left, right, front, back, bottom, top.  Runs on the GPU between InteractionLoop and
+    NewtonIntegrator.  Read-only results (UnbalancedForce, width, depth, height, strain,
+    porosity) are refreshed after each run; recordData's file output is not written."""
+    _defaults = {"cubic_specimen": True, "z_servo": True, "continueFlag": False, "shearMode": 1,
+                 "wall_radius": 5.0, "wall_fix": True, "wall_radius0": 0.0, "gain_alpha": 0.5, "target_strain": 0.15,
+                 "iterate_num_max": 100, "solve_num_max": 2000, "echo_interval": 1000, "ramp_interval": 10000,
+                 "ramp_chunks": 400, "f_threshold": 0.01, "fmin_threshold": 0.01, "unbf_tol": 0.01,
+                 "wall_max_vel": 1.0, "alpha": 0.5, "height0": 0.0, "width0": 0.0, "depth0": 0.0,
+                 "height": 0.0, "width": 0.0, "depth": 0.0,
+                 "left_wall_activated": True, "right_wall_activated": True, "front_wall_activated": True,
+                 "back_wall_activated": True, "bottom_wall_activated": True, "top_wall_activated": True,
+                 "hydroStrain": False, "hydroStrainRate": 0.0, "debug": False, "goalx": 0.0, "goaly": 0.0,
+                 "goalz": 0.0, "savedata_interval": 12, "max_vel": 1.0, "externalWork": 0.0, "UnbalancedForce": 1.0,
+                 "interStressControl": False, "file": "recordData", "dead": False,
+                 "strain": (0.0, 0.0, 0.0), "porosity": 1.0}
+
+    def _config(self):
+        from .servo import servo_config
+        if not self.cubic_specimen:
+            raise NotImplementedError("CompressionEngine with a cylindrical wall is not available on the GPU path")
+        kw = {k: float(getattr(self, k)) for k in (
+            "z_servo", "continueFlag", "hydroStrain", "shearMode", "left_wall_activated", "right_wall_activated",
+            "front_wall_activated", "back_wall_activated", "bottom_wall_activated", "top_wall_activated",
+            "iterate_num_max", "solve_num_max", "echo_interval", "savedata_interval", "ramp_interval",
+            "ramp_chunks", "goalx", "goaly", "goalz", "gain_alpha", "target_strain", "f_threshold",
+            "fmin_threshold", "unbf_tol", "max_vel", "hydroStrainRate", "width0", "height0", "depth0")}
+        return servo_config(enabled=1, **kw)
+
+    def _absorb(self, st):
+        from .servo import state_dict
+        d = state_dict(st)
+        a = self.__dict__
+        a["UnbalancedForce"] = d["UnbalancedForce"]
+        a["width"], a["depth"], a["height"] = d["width"], d["depth"], d["height"]
+        a["width0"], a["depth0"], a["height0"] = d["width0"], d["depth0"], d["height0"]
+        a["strain"] = (0.0, 0.0, d["strain2"])
+        pv = d["particlesVolume"]
+        a["porosity"] = 1.0 - pv / (d["width"] * d["depth"] * d["height"]) if pv > 0 and d["height"] else 1.0
+
+    def getStress(self):
+        """(mean stress, deviator stress) of the contact stress tensor in the box
+        (Compression.cpp:764-841)."""
+        eng = O._engine
+        O.wait()
+        st = eng.servo_state()
+        from .servo import state_dict
+        d = state_dict(st)
+        vol = d["height"] * d["depth"] * d["width"]
+        sig = -eng.get_stress(vol)
+        mean = (sig[0, 0] + (sig[1, 1] + sig[2, 2])) / 3.0
+        dev = sig - mean * np.eye(3)
+        return (mean, float(np.sqrt(np.sum(dev * dev)) * np.sqrt(1.5)))
 
 
 class PyRunner(_Attr):
@@ -468,7 +524,7 @@ class Omega:
         self._structDirty = True
 
     def _parse_engines(self):
-        col = ilp = newton = None
+        col = ilp = newton = servo = None
         runners = []
         for e in self._engines:
             if isinstance(e, ForceResetter):
@@ -479,10 +535,18 @@ class Omega:
                 ilp = e
             elif isinstance(e, NewtonIntegrator):
                 newton = e
+            elif isinstance(e, CompressionEngine):
+                if e.dead:
+                    continue
+                if ilp is None or newton is not None:
+                    raise NotImplementedError("CompressionEngine runs on the GPU path only between InteractionLoop "
+                                              "and NewtonIntegrator")
+                servo = e
             elif isinstance(e, PyRunner):
                 runners.append(e)
             else:
                 raise NotImplementedError(f"engine {type(e).__name__} is not available on the GPU path")
+        self._servo = servo
         if col is None or ilp is None or newton is None:
             raise RuntimeError("O.engines must contain InsertionSortCollider, InteractionLoop and NewtonIntegrator")
         for g in ilp.geomDispatcher:
@@ -577,6 +641,9 @@ class Omega:
             vg = self.cell._pending if self.cell._pending is not None else self.cell._velGrad
             eng.set_periodic(self.cell._hSize, vg if np.any(vg != 0) else None)
             self.cell._pending = None
+        if self._servo is not None:
+            eng.set_servo(self._servo._config())
+            self._servoKey = tuple(self._servo._config())
         self._engine = eng
         self._parts = (col, ilp, newton, runners)
         self._structDirty = False
@@ -641,6 +708,21 @@ class Omega:
         col, ilp, newton, runners = self._parts
         if self._params_key(col, newton) != self._paramsKey:
             self._set_params(self._engine, col, newton)
+        eng = self._engine
+        st = eng.servo_state()
+        if self._servo is not None:
+            key = tuple(self._servo._config())
+            if key != self._servoKey:   # attributes changed: new configuration, same engine state
+                eng.set_servo(np.array(key))
+                eng.put_servo(st)
+                self._servoKey = key
+        if st[34] >= 0:        # O.run(n) sets Scene::stopAtIter = iter + n (sudodemWrapper.cpp:739)
+            st = st.copy()
+            st[34] = -1
+            eng.put_servo(st)
+        if newton.quiet_system_flag:
+            eng.set_quiet(True)
+            newton.quiet_system_flag = False
 
     def step(self):
         self.run(1, True)
@@ -672,10 +754,16 @@ class Omega:
                     self._prepare()
         if wait:
             self.report = self._engine.sync()
+            self._after()
+
+    def _after(self):
+        if self._servo is not None:
+            self._servo._absorb(self._engine.servo_state())
 
     def wait(self):
         if self._engine is not None:
             self.report = self._engine.sync()
+            self._after()
 
 
 O = Omega()
@@ -787,4 +875,19 @@ def _avgNumInteractions(cutoff=0.0, skipFree=False, considerClumps=False):
     return 2.0 * len(touch) / max(len(parts), 1) if not skipFree else (sum(vals) / max(len(vals), 1))
 
 
-utils = types.SimpleNamespace(wall=_wall, avgNumInteractions=_avgNumInteractions)
+def _unbalancedForce(useMaxForce=False):
+    """Shop::unbalancedForce (py/_utils.cpp:428,570; pkg/dem/Shop_01.cpp:148-188)."""
+    O.wait()
+    return O._engine.unbalanced_force(bool(useMaxForce))
+
+
+def _getStress(volume=0):
+    """Shop::getStress (py/_utils.cpp:592; pkg/dem/Shop_02.cpp:350-376), 3x3."""
+    O.wait()
+    return O._engine.get_stress(float(volume))
+
+
+utils = types.SimpleNamespace(wall=_wall, avgNumInteractions=_avgNumInteractions, unbalancedForce=_unbalancedForce,
+                              getStress=_getStress)
+unbalancedForce = _unbalancedForce
+getStress = _getStress

@@ -113,3 +113,88 @@ def test_script_runs_on_gpu_and_matches_engine(gpu):
     e.step(200)
     e.sync()
     assert np.array_equal(e.body_state()[:, 0:3], np.array([b.state.pos for b in O.bodies]))
+
+
+def build_consolidation(O, n=27, seed=2):
+    """example2_consol.py-style specimen: six walls first (left, right, front, back, bottom, top),
+    particles inside, CompressionEngine between InteractionLoop and NewtonIntegrator."""
+    import random
+    random.seed(seed)
+    mat = sim.SuperquadricsMat(label="mat1", Kn=1e5, Ks=5e4, frictionAngle=math.atan(0.3), density=2650)
+    wmat = sim.SuperquadricsMat(label="wallmat", Kn=1e5, Ks=0.0, frictionAngle=0.0)
+    O.materials.append(mat)
+    O.materials.append(wmat)
+    side = 6e-3
+    for pos, ax, se in ((0, 0, 1), (side, 0, -1), (0, 1, 1), (side, 1, -1), (0, 2, 1), (side, 2, -1)):
+        O.bodies.append(sim.utils.wall(pos, axis=ax, sense=se, material=wmat))
+    for k in range(n):
+        b = sim.NewSuperquadrics2(1e-3, 0.9e-3, 0.8e-3, 1.2, 1.2, mat, True, False)
+        b.state.pos = (1.2e-3 + 1.8e-3 * (k % 3), 1.2e-3 + 1.8e-3 * ((k // 3) % 3), 1.2e-3 + 1.8e-3 * (k // 9))
+        O.bodies.append(b)
+    triax = sim.CompressionEngine(goalx=1e5, goaly=1e5, goalz=1e5, max_vel=1.0, gain_alpha=0.5,
+                                  iterate_num_max=20, echo_interval=50)
+    newton = sim.NewtonIntegrator(damping=0.3, gravity=(0, 0, 0), isSuperquadrics=1)
+    O.engines = [sim.ForceResetter(),
+                 sim.InsertionSortCollider([sim.Bo1_Superquadrics_Aabb(), sim.Bo1_Wall_Aabb()], verletDist=1e-4),
+                 sim.InteractionLoop([sim.Ig2_Wall_Superquadrics_SuperquadricsGeom(),
+                                      sim.Ig2_Superquadrics_Superquadrics_SuperquadricsGeom()],
+                                     [sim.Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys()],
+                                     [sim.SuperquadricsLaw()]),
+                 triax, newton]
+    O.dt = 2e-6
+    return triax, newton
+
+
+def test_compression_engine_attributes_and_placement():
+    ce = sim.CompressionEngine()
+    # reference defaults (Compression.hpp:160-215)
+    assert (ce.goalx, ce.max_vel, ce.gain_alpha, ce.iterate_num_max, ce.solve_num_max) == (0, 1, 0.5, 100, 2000)
+    assert (ce.savedata_interval, ce.ramp_interval, ce.ramp_chunks, ce.unbf_tol) == (12, 10000, 400, 0.01)
+    with pytest.raises(AttributeError):
+        sim.CompressionEngine(goal_x=1)
+    from sudodem_gb300.servo import CONFIG_NAMES
+    cfg = sim.CompressionEngine(goalx=2e5, z_servo=False, top_wall_activated=False)._config()
+    assert cfg[CONFIG_NAMES.index("goalx")] == 2e5 and cfg[CONFIG_NAMES.index("z_servo")] == 0
+    assert cfg[CONFIG_NAMES.index("top_wall_activated")] == 0 and cfg[0] == 1
+    O = sim.Omega()
+    triax, newton = build_consolidation(O)
+    O._parse_engines()
+    assert O._servo is triax
+    O.engines = O.engines[:3] + [newton, triax]     # after Newton: not the reference's order
+    with pytest.raises(NotImplementedError):
+        O._parse_engines()
+
+
+@pytest.mark.gpu
+def test_consolidation_script_matches_engine(gpu):
+    O = sim.O          # utils functions act on the global scene, as in the reference
+    O.reset()
+    triax, newton = build_consolidation(O)
+    O.run(300, True)
+    assert triax.width < 6e-3 and triax.height < 6e-3   # walls moved in
+    pos = np.array([b.state.pos for b in O.bodies])
+    # the same through the C ABI
+    O2 = sim.Omega()
+    t2, n2 = build_consolidation(O2)
+    mats = O2._material_table()
+    kind, shape5, was, mat, sph, st, _ = O2._body_arrays()
+    from sudodem_gb300 import Engine
+    e = Engine(device=0)
+    e.set_materials([m.Kn for m in mats], [m.Ks for m in mats], [m.frictionAngle for m in mats],
+                    [m.betan for m in mats], [m.betas for m in mats], [m.density for m in mats])
+    e.set_params(dt=2e-6, gravity=(0, 0, 0), damping=0.3, verletDist=1e-4)
+    e.set_bodies(kind, shape5, was, mat, sph, st)
+    e.set_servo(t2._config())
+    e.step(300)
+    e.sync()
+    assert np.array_equal(e.body_state()[:, 0:3], pos)
+    # quiet flag through NewtonIntegrator, Shop functions through utils
+    newton.quiet_system_flag = True
+    O.run(1, True)
+    assert np.all(np.array([b.state.vel for b in O.bodies]) == 0)
+    assert not newton.quiet_system_flag
+    assert np.isfinite(sim.utils.unbalancedForce())
+    assert sim.utils.getStress(1e-6).shape == (3, 3)
+    mean, dev = triax.getStress()
+    assert np.isfinite(mean) and np.isfinite(dev)
+    O.reset()
