@@ -244,6 +244,16 @@ sqdem_status sqdem_set_quiet(sqdem_ctx* ctx, int on);
 sqdem_status sqdem_unbalanced_force(sqdem_ctx* ctx, int use_max, double* out);
 sqdem_status sqdem_get_stress(sqdem_ctx* ctx, double volume, double* out9);
 
+/* Snapshot of the whole context state as one byte blob: materials, parameters, bodies (with
+ * bounds and previous-pass bounds), the contact table with its history, iteration, collider
+ * and integrator bookkeeping, periodic cell and CompressionEngine.  buf = NULL returns the size
+ * in *size.  sqdem_restore loads a blob into a context (any precision / capacity config; the
+ * table must fit): it then continues bit for bit as the original.  Replaces O.save / O.load
+ * (core/Omega.cpp:230-279) within this library; the blob is not the reference's .xml.bz2 and
+ * is refused by a build whose state records differ in size. */
+sqdem_status sqdem_snapshot(sqdem_ctx* ctx, void* buf, size_t* size);
+sqdem_status sqdem_restore(sqdem_ctx* ctx, const void* buf, size_t size);
+
 /* ---------------------------------------------------------------------------------------
  * Batches of independent specimens (no counterpart in the reference, which runs one Scene per
  * process): n scenes, each a full context set up through the functions above

@@ -102,6 +102,7 @@ def load_library(build_if_missing=True):
         "sqdem_batch_sync": (i, [v, C.c_void_p]), "sqdem_batch_time_steps": (i, [v, i, dp]),
         "sqdem_batch_time_e2e": (i, [v, i, C.c_void_p, C.c_void_p, dp]),
         "sqdem_batch_launch_count": (C.c_longlong, [v]),
+        "sqdem_snapshot": (i, [v, C.c_void_p, C.POINTER(C.c_size_t)]), "sqdem_restore": (i, [v, C.c_void_p, C.c_size_t]),
         "sqdem_set_periodic": (i, [v, dp, dp]),
         "sqdem_set_velgrad": (i, [v, dp]),
         "sqdem_get_cell": (i, [v, dp]),
@@ -127,7 +128,7 @@ def exported_symbols():
             "sqdem_set_servo", "sqdem_get_servo", "sqdem_put_servo", "sqdem_set_quiet", "sqdem_unbalanced_force",
             "sqdem_get_stress", "sqdem_batch_create", "sqdem_batch_destroy", "sqdem_batch_last_error",
             "sqdem_batch_size", "sqdem_batch_scene", "sqdem_batch_step", "sqdem_batch_sync", "sqdem_batch_time_steps",
-            "sqdem_batch_time_e2e", "sqdem_batch_launch_count"]
+            "sqdem_batch_time_e2e", "sqdem_batch_launch_count", "sqdem_snapshot", "sqdem_restore"]
 
 
 def _dp(a):
@@ -236,6 +237,19 @@ class Engine:
     def put_servo(self, state):
         st = np.ascontiguousarray(state, dtype=np.float64)
         self._check(self.lib.sqdem_put_servo(self.h, _dp(st)))
+
+    def snapshot(self):
+        """The whole state as bytes (sqdem_snapshot); restore() continues bit for bit from it."""
+        size = C.c_size_t(0)
+        self._check(self.lib.sqdem_snapshot(self.h, None, C.byref(size)))
+        buf = C.create_string_buffer(size.value)
+        self._check(self.lib.sqdem_snapshot(self.h, C.cast(buf, C.c_void_p), C.byref(size)))
+        return buf.raw[:size.value]
+
+    def restore(self, blob):
+        buf = C.create_string_buffer(blob, len(blob))
+        self._check(self.lib.sqdem_restore(self.h, C.cast(buf, C.c_void_p), len(blob)))
+        self.n = int(np.frombuffer(blob[32:40], dtype=np.int64)[0])   # SnapHeader.N
 
     def set_quiet(self, on=True):
         self._check(self.lib.sqdem_set_quiet(self.h, 1 if on else 0))

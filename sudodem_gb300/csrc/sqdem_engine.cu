@@ -3639,6 +3639,122 @@ sqdem_status sqdem_get_stress(sqdem_ctx* c, double volume, double* out9) {
 }
 
 // ---------------------------------------------------------------------------
+// Snapshot / restore: the whole state of a context as one byte blob (materials, parameters,
+// bodies with bounds and previous-pass bounds, the contact table with its history in table
+// order, and the scene words: iteration, collider and integrator bookkeeping, periodic cell,
+// CompressionEngine).  A context restored from it continues bit for bit as the original
+// would.  The blob records the library's state-record sizes; a blob from a build with other
+// sizes is refused.
+static const char SNAP_MAGIC[8] = {'S', 'Q', 'D', 'E', 'M', 'S', 'N', '1'};
+struct SnapHeader {
+  char magic[8];
+  unsigned long long sceneBytes, servoBytes, paramsBytes;
+  long long N, nMats, nRec;
+  int recordFull, lmSpread, servoOn, pad;
+};
+
+sqdem_status sqdem_snapshot(sqdem_ctx* c, void* buf, size_t* size) {
+  if (!c || !size) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  CK(cudaSetDevice(c->device));
+  const long long N = c->d.N;
+  long nRec = 0;
+  sqdem_status s = sqdem_num_interactions(c, 1, &nRec);
+  if (s) return s;
+  const size_t need = sizeof(SnapHeader) + sizeof(sqdem_params) + sizeof(double) * 6 * c->nMats +
+                      N * (sizeof(int) * 5 + sizeof(double) * 5) + sizeof(double) * SQDEM_BODY_STRIDE * N +
+                      sizeof(double4) * 2 * N + sizeof(double) * SQDEM_INTR_STRIDE * nRec + sizeof(SceneState);
+  if (!buf) { *size = need; return SQDEM_OK; }
+  if (*size < need) { *size = need; return fail(c, SQDEM_ERR_CAPACITY, "snapshot buffer too small"); }
+  char* w = (char*)buf;
+  auto put = [&](const void* src, size_t bytes) { std::memcpy(w, src, bytes); w += bytes; };
+  SnapHeader h;
+  std::memset(&h, 0, sizeof(h));
+  std::memcpy(h.magic, SNAP_MAGIC, 8);
+  h.sceneBytes = sizeof(SceneState); h.servoBytes = sizeof(ServoDev); h.paramsBytes = sizeof(sqdem_params);
+  h.N = N; h.nMats = c->nMats; h.nRec = nRec;
+  h.recordFull = c->recordFull; h.lmSpread = c->lmSpread; h.servoOn = c->servoOn ? 1 : 0;
+  put(&h, sizeof(h));
+  put(&c->params, sizeof(sqdem_params));
+  for (int i = 0; i < c->nMats; i++) {
+    const double m[6] = {c->hostMats[i].x, c->hostMats[i].y, c->hostMats[i].z, c->hostMatsB[i].x, c->hostMatsB[i].y,
+                         c->hostMats[i].w};
+    put(m, sizeof(m));
+  }
+  put(c->kind.data(), sizeof(int) * N);
+  put(c->axisSense.data(), sizeof(int) * 2 * N);
+  put(c->matIds.data(), sizeof(int) * N);
+  put(c->isSphere.data(), sizeof(int) * N);
+  put(c->shape5.data(), sizeof(double) * 5 * N);
+  std::vector<double> st(SQDEM_BODY_STRIDE * N);
+  if ((s = sqdem_get_body_state(c, st.data()))) return s;
+  put(st.data(), sizeof(double) * st.size());
+  std::vector<double4> pm(2 * N);
+  CK(cudaMemcpy(pm.data(), c->d.pmin, sizeof(double4) * N, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(pm.data() + N, c->d.pmax, sizeof(double4) * N, cudaMemcpyDeviceToHost));
+  put(pm.data(), sizeof(double4) * 2 * N);
+  std::vector<double> rec(SQDEM_INTR_STRIDE * (size_t)nRec);
+  long got = 0;
+  if ((s = sqdem_get_interactions(c, 1, rec.data(), nRec, &got))) return s;
+  put(rec.data(), sizeof(double) * rec.size());
+  SceneState S;
+  if ((s = readScene(c, S))) return s;
+  put(&S, sizeof(S));
+  *size = need;
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_restore(sqdem_ctx* c, const void* buf, size_t size) {
+  if (!c || !buf) return SQDEM_ERR_ARG;
+  const char* r = (const char*)buf;
+  const char* end = r + size;
+  auto get = [&](void* dst, size_t bytes) -> bool {
+    if (r + bytes > end) return false;
+    std::memcpy(dst, r, bytes); r += bytes; return true;
+  };
+  SnapHeader h;
+  if (!get(&h, sizeof(h)) || std::memcmp(h.magic, SNAP_MAGIC, 8) != 0)
+    return fail(c, SQDEM_ERR_ARG, "not a snapshot of this library");
+  if (h.sceneBytes != sizeof(SceneState) || h.servoBytes != sizeof(ServoDev) || h.paramsBytes != sizeof(sqdem_params))
+    return fail(c, SQDEM_ERR_ARG, "snapshot written by a build with other state records");
+  if (h.N <= 0 || h.nMats <= 0 || h.nRec < 0 || h.N >= (1LL << 30)) return fail(c, SQDEM_ERR_ARG, "corrupt snapshot header");
+  const long long N = h.N;
+  sqdem_params P;
+  if (!get(&P, sizeof(P))) return fail(c, SQDEM_ERR_ARG, "truncated snapshot");
+  std::vector<double> m(6 * h.nMats);
+  if (!get(m.data(), sizeof(double) * m.size())) return fail(c, SQDEM_ERR_ARG, "truncated snapshot");
+  std::vector<int> kind(N), was(2 * N), mat(N), sph(N);
+  std::vector<double> s5(5 * N), st(SQDEM_BODY_STRIDE * N), rec(SQDEM_INTR_STRIDE * (size_t)h.nRec);
+  std::vector<double4> pm(2 * N);
+  SceneState S;
+  if (!get(kind.data(), 4 * N) || !get(was.data(), 8 * N) || !get(mat.data(), 4 * N) || !get(sph.data(), 4 * N) ||
+      !get(s5.data(), 40 * N) || !get(st.data(), sizeof(double) * st.size()) || !get(pm.data(), sizeof(double4) * 2 * N) ||
+      !get(rec.data(), sizeof(double) * rec.size()) || !get(&S, sizeof(S)))
+    return fail(c, SQDEM_ERR_ARG, "truncated snapshot");
+  std::vector<double> Kn(h.nMats), Ks(h.nMats), fa(h.nMats), bn(h.nMats), bs(h.nMats), rho(h.nMats);
+  for (long long i = 0; i < h.nMats; i++) {
+    Kn[i] = m[6 * i]; Ks[i] = m[6 * i + 1]; fa[i] = m[6 * i + 2]; bn[i] = m[6 * i + 3]; bs[i] = m[6 * i + 4]; rho[i] = m[6 * i + 5];
+  }
+  c->haveMats = false;
+  sqdem_status s;
+  if ((s = sqdem_set_materials(c, (int)h.nMats, Kn.data(), Ks.data(), fa.data(), bn.data(), bs.data(), rho.data()))) return s;
+  if ((s = sqdem_set_params(c, &P))) return s;
+  c->recordFull = h.recordFull; c->lmSpread = h.lmSpread;
+  if ((s = sqdem_set_bodies(c, (int)N, kind.data(), s5.data(), was.data(), mat.data(), sph.data(), st.data()))) return s;
+  if ((s = sqdem_put_body_state(c, st.data()))) return s;
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpy(c->d.pmin, pm.data(), sizeof(double4) * N, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d.pmax, pm.data() + N, sizeof(double4) * N, cudaMemcpyHostToDevice));
+  if ((s = sqdem_put_interactions(c, (long)h.nRec, rec.data()))) return s;
+  std::memset(S.err, 0, sizeof(S.err));
+  CK(cudaMemcpyAsync(c->d.S, &S, sizeof(S), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->servoOn = h.servoOn != 0;
+  c->graphValid = false; c->epoch++;
+  return uploadParams(c);
+}
+
+// ---------------------------------------------------------------------------
 // Batches of independent scenes (specimens): one context per scene, one CUDA graph that runs
 // one step of every scene as parallel branches, so that the scenes' kernels share the GPU.
 // Each scene's kernels and results are exactly those of a context stepped alone.

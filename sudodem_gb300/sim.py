@@ -765,6 +765,65 @@ class Omega:
             self.report = self._engine.sync()
             self._after()
 
+    # saving and loading ------------------------------------------------------------------------
+    def save(self, fileName):
+        """Save the scene (O.save, core/Omega.cpp:230-279): the Python objects (bodies, materials,
+        engines, cell) and the GPU state (sqdem_snapshot: contact history, collider and engine
+        state), in this library's own format, not the reference's .xml.bz2."""
+        import pickle
+        if self._engine is None or self._structDirty or self._hostDirty:
+            self._prepare()
+        self.wait()
+        self._pull()
+        blob = self._engine.snapshot()
+        bodies = self.bodies._b
+        scenes = [b.state.__dict__.pop("_scene", None) for b in bodies]
+        try:
+            payload = {"version": 1, "blob": blob, "bodies": bodies, "materials": list(self.materials),
+                       "engines": self._engines, "dt": self.dt, "periodic": self.periodic, "tags": self.tags,
+                       "cell": (self.cell._hSize, self.cell._velGrad), "device": self.device}
+            with open(fileName, "wb") as f:
+                pickle.dump(payload, f)
+        finally:
+            for bd, sc in zip(bodies, scenes):
+                if sc is not None:
+                    bd.state.__dict__["_scene"] = sc
+
+    def load(self, fileName):
+        """Load a scene written by save(): the run continues bit for bit from where it was saved."""
+        import pickle
+        with open(fileName, "rb") as f:
+            d = pickle.load(f)
+        if not isinstance(d, dict) or d.get("version") != 1:
+            raise ValueError("not a scene saved by this library")
+        self.reset()
+        self.device = d["device"]
+        for m in d["materials"]:
+            self.materials.append(m)
+        for bd in d["bodies"]:
+            self.bodies.append(bd)
+        self._engines = list(d["engines"])
+        self.dt = d["dt"]
+        self.periodic = d["periodic"]
+        self.tags = d["tags"]
+        self.cell._hSize, self.cell._velGrad = d["cell"]
+        col, ilp, newton, runners = self._parse_engines()
+        prec = "fp64"
+        for g in ilp.geomDispatcher:
+            if isinstance(g, Ig2_Superquadrics_Superquadrics_SuperquadricsGeom):
+                prec = g.precision
+        self._material_table()
+        eng = _native.Engine(device=self.device, precision=prec)
+        eng.restore(d["blob"])
+        self._engine = eng
+        self._parts = (col, ilp, newton, runners)
+        self._paramsKey = self._params_key(col, newton)
+        if self._servo is not None:
+            self._servoKey = tuple(self._servo._config())
+        self._structDirty = False
+        self._hostDirty = False
+        self._pulled = False
+
 
 O = Omega()
 
