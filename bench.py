@@ -47,6 +47,12 @@ def workload_spec(name, seed):
         # same particles on a 2.1 mm lattice: most neighbours start in contact (a compressed state)
         return assemblies.walled_lattice(200_000, seed=seed, box=0.2, per_side=94, spacing=2.1e-3,
                                          eps_range=(0.3, 1.8))
+    if name == "config4":
+        # 1,000,000 superellipsoids, half-axes log-uniform [0.5, 2] mm, eps U[0.2, 1.0], 200 x 200 mm
+        # walled box under gravity, size-sorted layers (the large deposition case)
+        return assemblies.config4(seed=seed)
+    if name.startswith("config4_n"):
+        return assemblies.config4(seed=seed, n=int(name[9:]))
     if name == "sq20k_dense":
         return assemblies.walled_lattice(20_000, seed=seed, box=0.095, per_side=44, spacing=2.1e-3,
                                          eps_range=(0.3, 1.8))

@@ -285,3 +285,58 @@ def config2(seed=0, n_specimens=512, n_range=(300, 8000), friction_range=(0.2, 0
                          gain_alpha=0.5, ramp_interval=200, ramp_chunks=20, echo_interval=1000,
                          savedata_interval=1000, target_strain=10.0)
     return specs, servo
+
+
+def config4(seed=0, n=1_000_000, r_range=(0.5e-3, 2.0e-3), eps_range=(0.2, 1.0), box=0.2, friction=0.5,
+            kn=1e5, damping=0.3, verletDist=0.2e-3, dt_factor=0.5):
+    """1,000,000 superellipsoids, half-axes log-uniform in [0.5, 2.0] mm, eps U[0.2, 1.0], in a
+    200 x 200 mm walled box under gravity (the large deposition case).  Particles are sorted by
+    bounding radius and placed layer by layer on square lattices whose spacing is 1.25 times
+    the largest bounding radius of the layer (the lattice/size ratio of sq200k_dense: most
+    neighbours start in contact, a settled column rather than a free fall).  Six walls first:
+    x-, x+, y-, y+, floor and a lid far above."""
+    rng = np.random.default_rng(seed)
+    r = np.exp(rng.uniform(math.log(r_range[0]), math.log(r_range[1]), size=(n, 3)))
+    eps = rng.uniform(eps_range[0], eps_range[1], size=(n, 2))
+    q = random_quaternions(rng, n)
+    rb = r.max(axis=1) * np.where((eps < 1.0).any(axis=1), math.sqrt(2.0), 1.0)
+    order = np.argsort(rb, kind="stable")
+    pos = np.zeros((n, 3))
+    z = 0.0
+    k = 0
+    while k < n:
+        rmax = rb[order[min(n - 1, k + 1)]]
+        sp = 1.25 * rmax
+        per = max(1, int((box - 2 * rmax) // sp) + 1)
+        take = order[k:k + per * per]
+        rl = rb[take].max()
+        sp = 1.25 * rl
+        per = max(1, int((box - 2 * rl) // sp) + 1)
+        take = order[k:k + per * per]
+        z += 0.5 * sp if k else 1.02 * rl
+        idx = np.arange(len(take))
+        iy, ix = np.divmod(idx, per)
+        x0 = 0.5 * box - 0.5 * (per - 1) * sp
+        pos[take, 0] = x0 + ix * sp
+        pos[take, 1] = x0 + iy * sp
+        pos[take, 2] = z
+        z += 0.5 * sp
+        k += len(take)
+    b = _builder()
+    lid = max(2.0 * z, 0.5)
+    _add_wall(b, [0, 0, 0], 0, +1)
+    _add_wall(b, [box, 0, 0], 0, -1)
+    _add_wall(b, [0, 0, 0], 1, +1)
+    _add_wall(b, [0, box, 0], 1, -1)
+    _add_wall(b, [0, 0, 0], 2, +1)
+    _add_wall(b, [0, 0, lid], 2, -1)
+    density = 2650.0
+    for p in range(n):
+        _add_sq(b, r[p], eps[p], q[p], pos[p], density)
+    mats = default_material(kn=kn, friction=friction, density=density)
+    params = {"dt": 1.0, "gravity": (0.0, 0.0, -9.81), "damping": damping, "verletDist": verletDist,
+              "targetInterv": 50, "minSweepDistFactor": 0.1, "sortAxis": 0, "isSuperquadrics": 1,
+              "exactAsphericalRot": 1}
+    spec = _finish(b, mats, params, {"box": box, "height": z, "seed": seed})
+    spec.params["dt"] = critical_dt(spec, dt_factor)
+    return spec
