@@ -52,6 +52,21 @@ enum { SQDEM_SUPERQUADRIC = 0, SQDEM_WALL = 1 };
 /* Arithmetic form of the narrowphase. */
 enum { SQDEM_FP64 = 0, SQDEM_MIXED = 1 };
 
+/* Contact model (the functor set of the InteractionLoop):
+ *   SQDEM_CONTACT_LINEAR         Ig2_Wall_Superquadrics_SuperquadricsGeom, Ig2_Superquadrics_
+ *                                Superquadrics_SuperquadricsGeom (Levenberg-Marquardt),
+ *                                Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys,
+ *                                SuperquadricsLaw                      (the default)
+ *   SQDEM_CONTACT_HERTZ_MINDLIN  Ig2_Wall_Superquadrics_SuperquadricsGeom2, Ig2_Superquadrics_
+ *                                Superquadrics_SuperquadricsGeom2 (Nelder-Mead),
+ *                                Ip2_SuperquadricsMat2_SuperquadricsMat2_HertzMindlinPhys,
+ *                                SuperquadricsLaw2
+ *                                (pkg/dem/Superquadrics_Ig2.cpp:1624-1878, 2322-2517, 2615-2700;
+ *                                 pkg/dem/Superquadrics.cpp:974-1013, 1118-1160, 1367-1557)
+ * The Hertz-Mindlin search always runs in FP64 (sqdem_config.precision applies to the linear
+ * model's search). */
+enum { SQDEM_CONTACT_LINEAR = 0, SQDEM_CONTACT_HERTZ_MINDLIN = 1 };
+
 typedef struct {
   int device;              /* CUDA device ordinal */
   int precision;           /* SQDEM_FP64 or SQDEM_MIXED */
@@ -97,9 +112,11 @@ typedef struct {
 #define SQDEM_BODY_STRIDE 37
 /* pos3 ori4(w,x,y,z) vel3 angVel3 angMom3 force3 torque3 bmin3 bmax3 refPos3
    sweepLength lastUpdateIter mass inertia3 */
-#define SQDEM_INTR_STRIDE 47
+#define SQDEM_INTR_STRIDE 57
 /* id1 id2 isReal hasGeom depth contactAngle2 contactPoint3 normal3 shearInc3 point1_3 point2_3
-   isShearNew kn ks tanphi normalForce3 shearForce3 twist3 orthonormal3 relVn3 relVs3 cellDist3 */
+   isShearNew kn ks tanphi normalForce3 shearForce3 twist3 orthonormal3 relVn3 relVs3 cellDist3
+   curvatures1_2 curvatures2_2 curvatureAngle alpha K E curvatures_sum isSphere
+   (the last ten: SuperquadricsGeom2, Hertz-Mindlin model; zero under the linear model) */
 #define SQDEM_SCALARS 9
 /* iter maxVelocitySq fastestBodyMaxDist strideActive newtonFound verletDist numReinit colliderRuns
    sortedBoundsValid (0: the next collider pass is a full sort, InsertionSortCollider.cpp:213-222) */
@@ -127,6 +144,18 @@ sqdem_status sqdem_set_bodies(sqdem_ctx* ctx, int n, const int* kind, const doub
                               const int* wall_axis_sense, const int* mat, const int* isSphere,
                               const double* state);
 sqdem_status sqdem_set_params(sqdem_ctx* ctx, const sqdem_params* p);
+
+/* Contact model (SQDEM_CONTACT_*); takes effect at the next step, existing contacts keep
+ * their state.  sqdem_contact_model returns the current one (-1 for a NULL context). */
+sqdem_status sqdem_set_contact_model(sqdem_ctx* ctx, int model);
+int sqdem_contact_model(sqdem_ctx* ctx);
+/* Number of materials set (0 before sqdem_set_materials). */
+int sqdem_num_materials(sqdem_ctx* ctx);
+/* SuperquadricsMat2{G, nu} (pkg/dem/Superquadrics.hpp:266-277) per material, n = the count
+ * given to sqdem_set_materials; defaults G = 29e9 Pa, nu = 0.15.  Used by the Hertz-Mindlin
+ * model only. */
+sqdem_status sqdem_set_material_moduli(sqdem_ctx* ctx, int n, const double* G, const double* nu);
+sqdem_status sqdem_get_material_moduli(sqdem_ctx* ctx, double* G, double* nu);
 
 /* Advance nsteps timesteps (asynchronous on the context stream). */
 sqdem_status sqdem_step(sqdem_ctx* ctx, int nsteps);

@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libsqdem_oracle.so")
 BODY_STRIDE = 37
-INTR_STRIDE = 47
+INTR_STRIDE = 57
 
 _lib = None
 
@@ -57,6 +57,11 @@ def lib():
         "sqo_surface": (None, [d, d, d, d, d, d, d, dp]),
         "sqo_normal": (None, [d, d, d, d, d, d, d, dp]),
         "sqo_normal2phi": (None, [d, d, d, d, d, dp, dp]),
+        "sqo_set_contact_model": (None, [v, i]), "sqo_set_moduli": (None, [v, i, d, d]),
+        "sqo_stats_nan_forces": (None, [v, C.POINTER(l)]),
+        "sqo_pair_geom2": (i, [v, i, i, i, dp, dp]),
+        "sqo_curvatures": (None, [d, d, d, d, d, d, d, dp]),
+        "sqo_hertz_mindlin": (None, [dp, dp, d, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -86,6 +91,22 @@ def normal(shape5, ph0, ph1):
     out = np.zeros(3)
     lib().sqo_normal(*[float(x) for x in shape5], ph0, ph1, _dp(out))
     return out
+
+
+def curvatures(shape5, ph0, ph1):
+    """Superquadrics::Curvatures of an unrotated shape: (k1, k2), dirMax, dirMin, maxFlag."""
+    out = np.zeros(9)
+    lib().sqo_curvatures(*[float(x) for x in shape5], float(ph0), float(ph1), _dp(out))
+    return out[0:2], out[2:5], out[5:8], bool(out[8])
+
+
+def hertz_mindlin(c1, c2, theta):
+    """SuperquadricsGeom2::HertzMindlin: (curvatures_sum, alpha, K, E)."""
+    a = np.ascontiguousarray(c1, dtype=np.float64)
+    b = np.ascontiguousarray(c2, dtype=np.float64)
+    out = np.zeros(4)
+    lib().sqo_hertz_mindlin(_dp(a), _dp(b), float(theta), _dp(out))
+    return tuple(out)
 
 
 def normal2phi(shape5, n):
@@ -137,6 +158,11 @@ class OracleScene:
         o.L.sqo_set_params(o.h, p["dt"], _dp(g), p["damping"], p["verletDist"], int(p["targetInterv"]),
                            p["minSweepDistFactor"], int(p["sortAxis"]))
         o.n = spec.n_bodies
+        if "G" in m:
+            for k in range(len(m["G"])):
+                o.L.sqo_set_moduli(o.h, k, float(m["G"][k]), float(m["nu"][k]))
+        if spec.info.get("contact_model", "linear") == "hertz_mindlin":
+            o.set_contact_model("hertz_mindlin")
         if spec.info.get("periodic"):
             o.set_periodic(spec.info["hSize"], spec.info.get("velGrad"))
         # velocities from the spec (the factory leaves them zero)
@@ -228,6 +254,26 @@ class OracleScene:
     def put_servo(self, state):
         st = np.ascontiguousarray(state, dtype=np.float64)
         self.L.sqo_put_servo(self.h, _dp(st))
+
+    def set_contact_model(self, model):
+        self.L.sqo_set_contact_model(self.h, {"linear": 0, "hertz_mindlin": 1}[model])
+
+    def set_moduli(self, mat, G, nu):
+        self.L.sqo_set_moduli(self.h, int(mat), float(G), float(nu))
+
+    def nan_forces(self):
+        out = C.c_long(0)
+        self.L.sqo_stats_nan_forces(self.h, C.byref(out))
+        return out.value
+
+    def pair_geom2(self, ia, ib, prior=None):
+        out = np.zeros(25)
+        pr = np.zeros(4) if prior is None else np.ascontiguousarray(prior, dtype=np.float64)
+        it = self.L.sqo_pair_geom2(self.h, ia, ib, 1 if prior is None else 0, _dp(pr), _dp(out))
+        return {"depth": out[0], "normal": out[1:4], "contactPoint": out[4:7], "point1": out[7:10],
+                "point2": out[10:13], "contactAngle": out[13:15], "curvatures1": out[15:17],
+                "curvatures2": out[17:19], "curvatureAngle": out[19], "alpha": out[20], "K": out[21], "E": out[22],
+                "curvatures_sum": out[23], "isSphere": bool(out[24]), "nm_evaluations": it}
 
     def set_quiet(self, on=True):
         self.L.sqo_set_quiet(self.h, 1 if on else 0)

@@ -195,7 +195,7 @@ static inline V3 sqNormal(const SQ& s, Real ph0, Real ph1) {
 enum { KIND_SQ = 0, KIND_WALL = 1 };
 static const unsigned DOF_ALL = 63u;
 
-struct Mat { Real Kn, Ks, frictionAngle, betan, betas, density; };
+struct Mat { Real Kn, Ks, frictionAngle, betan, betas, density; Real G = 29e9, nu = 0.15; };   // G, nu: SuperquadricsMat2 (Superquadrics.hpp:266-277)
 
 struct Body {
   int kind;
@@ -214,6 +214,9 @@ struct Geom {
   Real PenetrationDepth; Real contactAngle[2];
   V3 contactPoint, shearInc, relativeVn, relativeVs, normal, twist_axis, orthonormal_axis, point1, point2;
   bool isShearNew;
+  // SuperquadricsGeom2 (Superquadrics.hpp:211-233), Hertz-Mindlin contact model
+  Real curvatures1[2], curvatures2[2], curvatureAngle, alpha, K, E, curvatures_sum;
+  bool isSphere;
 };
 // SuperquadricsPhys : FrictPhys (Superquadrics.hpp:303-321, FrictPhys.hpp:15-25)
 struct Phys { Real kn, ks, tanphi, betan, betas; V3 normalForce, shearForce; };
@@ -234,7 +237,7 @@ struct Bounds {
   bool operator>(const Bounds& b) const { if (id == b.id && coord == b.coord) return !isMin; return coord > b.coord; }
 };
 
-struct Stats { long lmCalls, lmIters, disCalls, restarts, nanNormals; long hist[16]; };
+struct Stats { long lmCalls, lmIters, disCalls, restarts, nanNormals; long hist[16]; long nanForces; };
 
 
 struct Scene {
@@ -273,6 +276,10 @@ struct Scene {
   // CompressionEngine (pkg/dem/Compression.hpp:39-252), run between InteractionLoop and Newton
   struct Servo* servo = nullptr;
   long stopAtIter = -1;   // Scene::stopAtIter as the engine requests it
+  // contact model: 0 SuperquadricsGeom + SuperquadricsPhys + SuperquadricsLaw, 1 the Hertz-Mindlin
+  // set Ig2_*_SuperquadricsGeom2 + Ip2_SuperquadricsMat2_SuperquadricsMat2_HertzMindlinPhys +
+  // SuperquadricsLaw2
+  int contactModel = 0;
 };
 
 static inline uint64_t pairKey(int a, int b) {
@@ -907,6 +914,348 @@ static bool law(Scene& S, Interaction* I, V3* F, V3* T) {
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// Hertz-Mindlin contact model.
+// CRotationMat (Superquadrics_Ig2.cpp:295-316): rotation taking x onto the direction from
+// particle 1 to particle 2 (the frame of the Nelder-Mead angles).
+static M3 cRotationMat(const V3& position1, const V3& position2) {
+  const V3 x1(1., 0, 0);
+  const V3 e1 = position2 - position1;
+  const Real cos_phi = dot(x1, e1) / (norm(x1) * norm(e1));
+  const Real cos_halfphi = std::sqrt(0.5 * (1 + cos_phi));
+  const Real sin_halfphi = std::sqrt(0.5 * (1 - cos_phi));
+  Quat q;
+  if (std::fabs(cos_phi) > 1.0 - 1e-10) q = Quat{cos_halfphi, 0, 0, sin_halfphi};
+  else {
+    V3 n1 = cross(x1, e1);
+    normalize(n1);
+    n1 = n1 * sin_halfphi;
+    q = Quat{cos_halfphi, n1[0], n1[1], n1[2]};
+  }
+  return toRot(q);
+}
+// Disfun (Superquadrics_Ig2.cpp:1624-1667): distance between the support points along the
+// direction given by the angles in the CRotationMat frame
+static Real disfun(const Real para[2], const SQ& A, const SQ& B, const V3& position1, const V3& position2, V3& p1,
+                   V3& p2, const M3& gc, bool& touching, long* nev) {
+  V3 contact(std::cos(para[0]) * std::cos(para[1]), std::sin(para[0]) * std::cos(para[1]), std::sin(para[1]));
+  contact = mul(gc, contact);
+  Real ph0, ph1;
+  sqNormal2Phi(A, mul(A.loc, contact), ph0, ph1);
+  p1 = mul(A.glob, sqSurface(A, ph0, ph1)) + position1;
+  sqNormal2Phi(B, (-1.0) * mul(B.loc, contact), ph0, ph1);
+  p2 = mul(B.glob, sqSurface(B, ph0, ph1)) + position2;
+  const V3 d = p2 - p1;
+  if (dot(contact, d) > 0) touching = false;
+  if (nev) (*nev)++;
+  return norm(d);
+}
+struct NMCtx { const SQ* A; const SQ* B; V3 pos1, pos2; M3 gc; long* nev; };
+// amotry (:1668-1700)
+static Real amotry(Real p[3][2], Real y[3], Real psum[2], int ihi, Real fac, const NMCtx& c, V3& pt1, V3& pt2,
+                   bool& touching) {
+  const Real fac1 = (1.0 - fac) / 2.0;
+  const Real fac2 = fac1 - fac;
+  Real ptry[2] = {psum[0] * fac1 - p[ihi][0] * fac2, psum[1] * fac1 - p[ihi][1] * fac2};
+  const Real ytry = disfun(ptry, *c.A, *c.B, c.pos1, c.pos2, pt1, pt2, c.gc, touching, c.nev);
+  if (ytry < y[ihi]) {
+    y[ihi] = ytry;
+    psum[0] += ptry[0] - p[ihi][0]; psum[1] += ptry[1] - p[ihi][1];
+    p[ihi][0] = ptry[0]; p[ihi][1] = ptry[1];
+  }
+  return ytry;
+}
+// neldermead_simplex (:1701-1878).  The reference leaves its evaluation counter uninitialised
+// (undefined behaviour in the NMAX test); it starts at 0 here.
+static void neldermeadSimplex(const Real point[2], const Real dels[2], Real info[2], const NMCtx& c, V3& pt1, V3& pt2,
+                              bool& touching, Real out[2]) {
+  const Real ftol = 1e-3, TINY = 1.0e-10;
+  const int NMAX = 5000;
+  int nfunc = 0;
+  Real fmin = 0;
+  Real p[3][2], y[3], psum[2];
+  for (int i = 0; i < 3; i++) { p[i][0] = point[0]; p[i][1] = point[1]; }
+  p[1][0] += dels[0];
+  p[2][1] += dels[1];
+  auto ret = [&](const Real* v, Real dist) { info[0] = nfunc; info[1] = dist; out[0] = v[0]; out[1] = v[1]; };
+  for (int i = 0; i < 3; i++) {
+    y[i] = disfun(p[i], *c.A, *c.B, c.pos1, c.pos2, pt1, pt2, c.gc, touching, c.nev);
+    nfunc++;
+    if (!touching) { ret(p[0], y[0]); return; }
+  }
+  psum[0] = (p[0][0] + p[1][0]) + p[2][0]; psum[1] = (p[0][1] + p[1][1]) + p[2][1];
+  for (;;) {
+    int ilo = 0, ihi, inhi;
+    if (!touching) { ret(p[0], fmin); return; }
+    if (y[0] > y[1]) { inhi = 1; ihi = 0; } else { inhi = 0; ihi = 1; }
+    for (int i = 0; i < 3; i++) {
+      if (y[i] <= y[ilo]) ilo = i;
+      if (y[i] > y[ihi]) { inhi = ihi; ihi = i; }
+      else if (y[i] > y[inhi] && i != ihi) inhi = i;
+    }
+    const Real rtol = 2.0 * std::fabs(y[ihi] - y[ilo]) / (std::fabs(y[ihi]) + std::fabs(y[ilo]) + TINY);
+    if (rtol < ftol) {
+      std::swap(y[0], y[ilo]);
+      std::swap(p[ilo][0], p[0][0]); std::swap(p[ilo][1], p[0][1]);
+      fmin = y[0];
+      ret(p[0], fmin);
+      return;
+    }
+    if (nfunc >= NMAX) { ret(p[0], y[0]); return; }
+    Real ytry = amotry(p, y, psum, ihi, -1.0, c, pt1, pt2, touching); nfunc++;
+    if (!touching) { ret(p[0], y[0]); return; }
+    if (ytry <= y[ilo]) {
+      ytry = amotry(p, y, psum, ihi, 2.0, c, pt1, pt2, touching); nfunc++;
+      if (!touching) { ret(p[0], y[0]); return; }
+    } else if (ytry >= y[inhi]) {
+      const Real ysave = y[ihi];
+      ytry = amotry(p, y, psum, ihi, 0.5, c, pt1, pt2, touching); nfunc++;
+      if (!touching) { ret(p[0], y[0]); return; }
+      if (ytry >= ysave) {
+        for (int i = 0; i < 3; i++) {
+          if (i != ilo) {
+            p[i][0] = psum[0] = 0.5 * (p[i][0] + p[ilo][0]);
+            p[i][1] = psum[1] = 0.5 * (p[i][1] + p[ilo][1]);
+            y[i] = disfun(psum, *c.A, *c.B, c.pos1, c.pos2, pt1, pt2, c.gc, touching, c.nev); nfunc++;
+            if (!touching) { ret(p[0], y[0]); return; }
+          }
+        }
+        psum[0] = (p[0][0] + p[1][0]) + p[2][0]; psum[1] = (p[0][1] + p[1][1]) + p[2][1];
+      }
+    }
+  }
+}
+// Superquadrics::Curvatures (Superquadrics.cpp:128-224): principal curvatures from the first
+// and second fundamental forms (the mixed term of the second form is left out, as in the
+// reference) and the principal directions in the global frame.
+static void sqCurvatures(const SQ& q, Real ph0, Real ph1, V3& dirMax, V3& dirMin, bool& maxFlag, Real k[2]) {
+  maxFlag = true;
+  if (std::fabs(ph0) < 1E-20) ph0 = 1E-20;
+  if (std::fabs(ph1) < 1E-20) ph1 = 1E-20;
+  const Real rx = q.rx, ry = q.ry, rz = q.rz, eps1 = q.eps1, eps2 = q.eps2;
+  const Real s1 = std::sin(ph0), s2 = std::sin(ph1), c1 = std::cos(ph0), c2 = std::cos(ph1);
+  const Real s_s1 = Sign(s1), s_s2 = Sign(s2), s_c1 = Sign(c1), s_c2 = Sign(c2);
+  const Real abs_s1 = std::fabs(s1), abs_s2 = std::fabs(s2), abs_c1 = std::fabs(c1), abs_c2 = std::fabs(c2);
+  const Real s10 = s_s1 * std::pow(abs_s1, eps1), s20 = s_s2 * std::pow(abs_s2, eps2);
+  const Real c10 = s_c1 * std::pow(abs_c1, eps1), c20 = s_c2 * std::pow(abs_c2, eps2);
+  const Real s12 = s_s1 * std::pow(abs_s1, eps1 - 2.0), s22 = s_s2 * std::pow(abs_s2, eps2 - 2.0);
+  const Real c12 = s_c1 * std::pow(abs_c1, eps1 - 2.0), c22 = s_c2 * std::pow(abs_c2, eps2 - 2.0);
+  const V3 R1(-rx * eps1 * c12 * c1 * c20 * s1, ry * eps1 * c1 * c20 * s12 * s1, 0);
+  const V3 R2(-rx * eps2 * c10 * c22 * c2 * s2, -ry * eps2 * c22 * c2 * s10 * s2, rz * eps2 * c2 * s22 * s2);
+  const V3 R11(rx * eps1 * c12 * s20 * s1 * s1 * (eps1 - 1.0) - rx * eps1 * c10 * c20,
+               ry * eps1 * c1 * c1 * c20 * s12 * (eps1 - 1.0) - ry * eps1 * c20 * s10, 0);
+  const V3 R22(rx * eps2 * c10 * c22 * s2 * s2 * (eps2 - 1.0) - rx * eps2 * c10 * c20,
+               ry * eps2 * s10 * s1 * s1 * (eps2 - 1.0) - ry * eps2 * c20 * s10,
+               rz * eps2 * c2 * c2 * s22 * (eps2 - 1.0) - rz * eps2 * s20);
+  const V3 RR = cross(R1, R2);
+  const Real rrn = norm(RR);
+  const V3 n(RR[0] / rrn, RR[1] / rrn, RR[2] / rrn);
+  const Real L = dot(R11, n), N = dot(R22, n), E = dot(R1, R1), F = dot(R1, R2), G = dot(R2, R2);
+  const Real Kg = L * N / (E * G - F * F);
+  const Real H = 0.5 * (E * N + G * L) / (E * G - F * F);
+  const Real tmp0 = std::sqrt(std::fabs(H * H - Kg));
+  const Real k1 = H + tmp0, k2 = H - tmp0;
+  V3 d1 = R1 * (N - k1 * G) + R2 * k1 * F;
+  if (norm(d1) == 0) maxFlag = false;
+  else { normalize(d1); dirMax = mul(q.glob, d1); }
+  V3 d2 = R1 * (N - k2 * G) + R2 * k2 * F;
+  normalize(d2);
+  dirMin = mul(q.glob, d2);
+  k[0] = k1; k[1] = k2;
+}
+// SuperquadricsGeom2::HertzMindlin (Superquadrics.cpp:965-996): contact ellipse from the
+// relative curvatures (semi-axis ratio alpha and the complete elliptic integrals K, E by the
+// reference's polynomial fits)
+static void hertzMindlin(Geom& g, const Real c1[2], const Real c2[2], Real theta) {
+  Real rho11 = std::fabs(c1[0]), rho12 = std::fabs(c1[1]), rho21 = std::fabs(c2[0]), rho22 = std::fabs(c2[1]);
+  if (rho11 * rho12 < 1E-18) rho11 = rho12 = 0.0;
+  if (rho21 * rho22 < 1E-18) rho21 = rho22 = 0.0;
+  const Real sum_rho = ((rho11 + rho12) + rho21) + rho22;
+  const Real F_rho = -std::sqrt((std::pow(rho11 - rho12, 2) + std::pow(rho21 - rho22, 2)) +
+                                2 * (std::fabs(rho11 - rho12)) * std::fabs(rho21 - rho22) * std::cos(2 * theta));
+  const Real A = (sum_rho + F_rho) / 4., B = (sum_rho - F_rho) / 4.;
+  g.curvatures_sum = A + B;
+  const Real x_squ = std::pow(std::log10(B / A), 2);
+  const Real gamma1 = 2 * (1 + x_squ * (0.40227436 + x_squ * (3.7491752e-2 + x_squ * (7.4855761e-4 + x_squ * 2.1667028e-6))));
+  const Real gamma2 = 3 * (1 + x_squ * (0.42678878 + x_squ * (4.2605401e-2 + x_squ * (9.0786922e-4 + x_squ * 2.7868927e-6))));
+  g.alpha = std::pow((B / A), gamma1 / gamma2);
+  const Real m1 = 1 / std::pow(g.alpha, 2);
+  g.K = (1.3862944 + m1 * (0.1119723 + 0.0725296 * m1)) - std::log(m1) * (0.5 + m1 * (0.1213478 + 0.0288729 * m1));
+  g.E = (1 + m1 * (0.4630151 + 0.1077812 * m1)) - std::log(m1) * (0.2452727 + 0.0412496 * m1) * m1;
+}
+// Ig2_Superquadrics_Superquadrics_SuperquadricsGeom2::go (Superquadrics_Ig2.cpp:2322-2517).  The
+// positions are used without the periodic shift, as in the reference.
+static bool ig2SqSq2(Scene& S, Interaction* I, const Body& b1, const Body& b2, const V3& shift2, Stats& st) {
+  const V3 position1 = b1.pos, position2 = b2.pos;
+  const SQ* A = &b1.sq; const SQ* B = &b2.sq;
+  const bool isNew = !I->hasGeom;
+  Geom& g = I->g;
+  Real dels[2] = {0.01, 0.01}, para[2] = {0.0, 0.0};
+  if (isNew) {
+    std::memset(&g, 0, sizeof(Geom));
+    g.isShearNew = true;
+    I->hasGeom = true;
+    dels[0] = dels[1] = 0.1;
+  } else {
+    g.isShearNew = g.PenetrationDepth <= 0;
+    dels[0] = dels[1] = 0.001;
+  }
+  V3 contactNormal, p1, p2;
+  if (A->isSphere && B->isSphere) {
+    V3 dist = position2 - position1;
+    const Real r_sum = A->r_max + B->r_max;
+    const Real depth = r_sum - norm(dist);
+    if (depth < 1E-18) { g.PenetrationDepth = 0; g.isShearNew = true; return true; }
+    normalize(dist);
+    p1 = position1 + A->r_max * dist;
+    p2 = position2 - B->r_max * dist;
+    contactNormal = p1 - p2;
+    normalize(contactNormal);
+    g.point1 = p1; g.point2 = p2;
+    g.contactPoint = 0.5 * (p1 + p2);
+    g.PenetrationDepth = depth;
+    g.curvatures_sum = r_sum / (A->r_max * B->r_max);
+    g.isSphere = true;
+  } else {
+    const Real r_sum = A->r_max + B->r_max;
+    if (norm(position1 - position2) > r_sum) { g.PenetrationDepth = 0; g.isShearNew = true; return true; }
+    const M3 gc = cRotationMat(position1, position2);
+    para[0] = g.contactAngle[0]; para[1] = g.contactAngle[1];
+    bool touching = true;
+    Real info[2];
+    NMCtx c{A, B, position1, position2, gc, &st.disCalls};
+    Real out[2];
+    neldermeadSimplex(para, dels, info, c, p1, p2, touching, out);
+    para[0] = out[0]; para[1] = out[1];
+    st.lmCalls++; st.lmIters += (long)info[0];
+    if (!touching) {
+      g.contactAngle[0] = para[0]; g.contactAngle[1] = para[1];
+      g.PenetrationDepth = 0; g.isShearNew = true;
+      return true;
+    }
+    contactNormal = p1 - p2;
+    normalize(contactNormal);
+    g.point1 = p1; g.point2 = p2;
+    g.contactPoint = 0.5 * (p1 + p2);
+    g.PenetrationDepth = info[1];
+    V3 contact(std::cos(para[0]) * std::sin(para[1]), std::sin(para[0]) * std::sin(para[1]), std::cos(para[1]));
+    contact = mul(gc, contact);
+    const V3 contact1 = mul(A->loc, contact), contact2 = mul(B->loc, contact);
+    V3 dmax1, dmax2, dmin1, dmin2;
+    bool f1, f2;
+    Real c1[2], c2[2], ph0, ph1;
+    sqNormal2Phi(*A, contact1, ph0, ph1);
+    sqCurvatures(*A, ph0, ph1, dmax1, dmin1, f1, c1);
+    sqNormal2Phi(*B, (-1) * contact2, ph0, ph1);
+    sqCurvatures(*B, ph0, ph1, dmax2, dmin2, f2, c2);
+    const V3 cd1 = (f1 && f2) ? dmax1 : dmin1, cd2 = (f1 && f2) ? dmax2 : dmin2;
+    const V3 nd = contactNormal;
+    const V3 dir1 = V3(cd1[0] * nd[0], cd1[1] * nd[1], cd1[2] * nd[2]) - cd1;
+    const V3 dir2 = V3(cd2[0] * nd[0], cd2[1] * nd[1], cd2[2] * nd[2]) - cd2;
+    Real angle = std::acos(dot(dir1, dir2) / (norm(dir1) * norm(dir2)));
+    if (std::isnan(angle)) angle = 0.0;
+    g.curvatures1[0] = c1[0]; g.curvatures1[1] = c1[1];
+    g.curvatures2[0] = c2[0]; g.curvatures2[1] = c2[1];
+    g.curvatureAngle = angle;
+    hertzMindlin(g, c1, c2, angle);
+  }
+  precompute(g, b1, b2, S.dt, contactNormal, g.isShearNew, shift2);
+  g.normal = contactNormal;
+  g.contactAngle[0] = para[0]; g.contactAngle[1] = para[1];
+  return true;
+}
+// Ip2_SuperquadricsMat2_SuperquadricsMat2_HertzMindlinPhys::go (Superquadrics.cpp:1118-1160)
+struct HMPhys { Real nuab, Gab, mu1, mu2; };
+static HMPhys hmPhysOf(const Mat& m1, const Mat& m2) {
+  HMPhys h;
+  h.nuab = 0.5 * (m1.nu + m2.nu);
+  h.Gab = 1.0 / ((1 - m1.nu) / m1.G + (1 - m2.nu) / m2.G);
+  h.mu1 = 1. / m1.G + 1. / m2.G;
+  h.mu2 = m1.nu / m1.G + m2.nu / m2.G;
+  return h;
+}
+static void ip2HM(Scene& S, Interaction* I) {
+  if (I->hasPhys) return;
+  const Mat& m1 = S.mats[S.bodies[I->id1].mat];
+  const Mat& m2 = S.mats[S.bodies[I->id2].mat];
+  Phys& p = I->p;
+  std::memset(&p, 0, sizeof(Phys));
+  I->hasPhys = true;
+  if (I->id1 > 5) p.tanphi = std::tan(std::min(m1.frictionAngle, m2.frictionAngle));
+  else { p.tanphi = std::tan(m1.frictionAngle); p.kn = m1.Kn; p.ks = m1.Ks; }
+  p.betan = std::max(m1.betan, m2.betan);
+  p.betas = std::max(m1.betas, m2.betas);
+}
+// SuperquadricsLaw2::go (Superquadrics.cpp:1367-1557)
+static bool law2(Scene& S, Interaction* I, V3* F, V3* T, Stats& st) {
+  if (!I->hasGeom) return true;
+  const int idA = I->id1, idB = I->id2;
+  const Body& A = S.bodies[idA];
+  const Body& B = S.bodies[idB];
+  Geom& g = I->g; Phys& ph = I->p;
+  if (A.bmin[0] >= B.bmax[0] || B.bmin[0] >= A.bmax[0] || A.bmin[1] >= B.bmax[1] || B.bmin[1] >= A.bmax[1] ||
+      A.bmin[2] >= B.bmax[2] || B.bmin[2] >= A.bmax[2]) {
+    ph.normalForce = V3(); ph.shearForce = V3();
+    requestErase(I);
+    return false;
+  }
+  if (!(g.PenetrationDepth > 1E-18)) { ph.normalForce = V3(); ph.shearForce = V3(); return true; }
+  if (idA > 5) {
+    const HMPhys h = hmPhysOf(S.mats[A.mat], S.mats[B.mat]);
+    const Real depth = g.PenetrationDepth, cs_ = g.curvatures_sum;
+    if (g.isSphere) {
+      const Real tmp = std::sqrt(depth / cs_);
+      ph.kn = 8. / 3. * h.Gab * tmp;
+      ph.ks = 8. / (2.0 * h.mu1 - h.mu2) * tmp;
+    } else {
+      const Real E = g.E, K = g.K, alpha = g.alpha;
+      const Real a = std::sqrt(depth * E / cs_ / K);
+      ph.kn = (Real)((long double)(4. / 3.) * M_PIl * a * h.Gab * alpha / K);   // long double as the reference
+      const Real e2 = 1 - 1 / std::pow(alpha, 2.0);
+      const Real ksx = h.mu1 * K - h.mu2 * (K - E) / e2;
+      const Real ksy = h.mu1 * K + h.mu2 * ((1 - e2) * K - E) / e2;
+      ph.ks = (Real)(M_PIl * alpha * a * (1. / ksx + 1. / ksy));
+    }
+  }
+  V3 normalForce = g.normal * g.PenetrationDepth * ph.kn;
+  V3 shearForce1;
+  const bool useDamping = (ph.betan > 0.00001 || ph.betas > 0.00001);
+  Real cs = 0;
+  if (useDamping) {
+    const bool Adyn = A.blockedDOFs != DOF_ALL, Bdyn = B.blockedDOFs != DOF_ALL;
+    const Real mbar = (!Adyn && Bdyn) ? B.mass : ((!Bdyn && Adyn) ? A.mass : (A.mass * B.mass / (A.mass + B.mass)));
+    const Real Cn_crit = 2. * std::sqrt(mbar * ph.kn), Cs_crit = 2. * std::sqrt(mbar * ph.ks);
+    const Real cn = Cn_crit * ph.betan;
+    cs = Cs_crit * ph.betas;
+    const V3 normalViscous = cn * g.relativeVn;
+    const V3 normTemp = normalForce - normalViscous;
+    if (dot(normTemp, g.normal) < 0.0) normalForce = V3();
+    else normalForce = normalForce - normalViscous;
+  }
+  if (g.isShearNew) shearForce1 = V3();
+  else shearForce1 = rotateShear(g, ph.shearForce);
+  shearForce1 = shearForce1 - ph.ks * g.shearInc;
+  const Real maxFs = sqnorm(normalForce) * std::pow(ph.tanphi, 2);
+  if (sqnorm(shearForce1) > maxFs) {
+    const Real ratio = std::sqrt(maxFs) / norm(shearForce1);
+    shearForce1 = shearForce1 * ratio;
+  } else if (useDamping) {
+    shearForce1 = shearForce1 - cs * g.relativeVs;
+  }
+  if (std::isnan(shearForce1[0]) || std::isnan(normalForce[0])) {
+    normalForce = V3(); shearForce1 = V3();
+    st.nanForces++;   // the reference stops the run after this step (Scene::stopAtIter = iter + 1)
+  }
+  const V3 Fv = (-normalForce) - shearForce1;
+  F[idA] = F[idA] + Fv;
+  F[idB] = F[idB] + (-Fv);
+  T[idA] = T[idA] + (-cross(A.pos - g.contactPoint, Fv));
+  T[idB] = T[idB] + cross(B.pos - g.contactPoint, Fv);
+  ph.normalForce = normalForce;
+  ph.shearForce = shearForce1;
+  return true;
+}
+
 // InteractionLoop::action (pkg/common/InteractionLoop.cpp:23-149)
 static void interactionLoop(Scene& S) {
   const long size = (long)S.lin.size();
@@ -934,6 +1283,13 @@ static void interactionLoop(Scene& S) {
     const Body& b2 = S.bodies[I->id2];
     V3 shift2;
     if (S.isPeriodic) shift2 = cellShift(S, I->cellDist);
+    if (S.contactModel == 1) {
+      if (b1.kind == KIND_WALL) ig2WallSq(S, I, b1, b2, shift2);   // Ig2_Wall_..._SuperquadricsGeom2: same geometry
+      else ig2SqSq2(S, I, b1, b2, shift2, S.tstats[tn]);
+      ip2HM(S, I);
+      if (!law2(S, I, S.fbuf[tn].data(), S.tbuf[tn].data(), S.tstats[tn])) requestErase(I);
+      continue;
+    }
     if (b1.kind == KIND_WALL) ig2WallSq(S, I, b1, b2, shift2);
     else ig2SqSq(S, I, b1, b2, shift2, S.tstats[tn]);
     ip2(S, I);
@@ -943,6 +1299,8 @@ static void interactionLoop(Scene& S) {
     S.stats.lmCalls += S.tstats[t].lmCalls; S.stats.lmIters += S.tstats[t].lmIters;
     S.stats.disCalls += S.tstats[t].disCalls; S.stats.restarts += S.tstats[t].restarts;
     S.stats.nanNormals += S.tstats[t].nanNormals;
+    if (S.tstats[t].nanForces) S.stopAtIter = S.iter + 1;
+    S.stats.nanForces += S.tstats[t].nanForces;
     for (int k = 0; k < 16; k++) S.stats.hist[k] += S.tstats[t].hist[k];
     S.tstats[t] = Stats{};
   }
@@ -1516,10 +1874,11 @@ void sqo_set_bodies(void* h, const double* in) {
   }
 }
 
-// Interaction records, 47 doubles each:
+// Interaction records, 57 doubles each:
 // id1 id2 real hasGeom depth angle2 contactPoint3 normal3 shearInc3 point1_3 point2_3 isShearNew
 // kn ks tanphi normalForce3 shearForce3 twist3 ortho3 relVn3 relVs3 cellDist3
-enum { INTR_STRIDE = 47 };
+// curvatures1_2 curvatures2_2 curvatureAngle alpha K E curvatures_sum isSphere (SuperquadricsGeom2)
+enum { INTR_STRIDE = 57 };
 void sqo_get_interactions(void* h, double* out) {
   Scene* S = (Scene*)h;
   for (size_t i = 0; i < S->lin.size(); i++) {
@@ -1538,6 +1897,8 @@ void sqo_get_interactions(void* h, double* out) {
       o[35 + k] = g.orthonormal_axis[k]; o[38 + k] = g.relativeVn[k]; o[41 + k] = g.relativeVs[k];
     }
     for (int k = 0; k < 3; k++) o[44 + k] = I->cellDist[k];
+    o[47] = g.curvatures1[0]; o[48] = g.curvatures1[1]; o[49] = g.curvatures2[0]; o[50] = g.curvatures2[1];
+    o[51] = g.curvatureAngle; o[52] = g.alpha; o[53] = g.K; o[54] = g.E; o[55] = g.curvatures_sum; o[56] = g.isSphere ? 1 : 0;
   }
 }
 // Replace the whole interaction container by the given records (same layout); the
@@ -1569,6 +1930,8 @@ void sqo_set_interactions(void* h, long n, const double* in) {
       g.orthonormal_axis[k] = o[35 + k]; g.relativeVn[k] = o[38 + k]; g.relativeVs[k] = o[41 + k];
     }
     for (int k = 0; k < 3; k++) I->cellDist[k] = (int)o[44 + k];
+    g.curvatures1[0] = o[47]; g.curvatures1[1] = o[48]; g.curvatures2[0] = o[49]; g.curvatures2[1] = o[50];
+    g.curvatureAngle = o[51]; g.alpha = o[52]; g.K = o[53]; g.E = o[54]; g.curvatures_sum = o[55]; g.isSphere = o[56] != 0;
   }
 }
 
@@ -1626,6 +1989,48 @@ int sqo_pair_geom(void* h, int ia, int ib, int isNew, const double* prior4, doub
   for (int k = 0; k < 3; k++) { out[1 + k] = g.normal[k]; out[4 + k] = g.contactPoint[k]; out[7 + k] = g.point1[k]; out[10 + k] = g.point2[k]; }
   out[13] = g.contactAngle[0]; out[14] = g.contactAngle[1];
   return (int)st.lmIters;
+}
+
+// Stand-alone Hertz-Mindlin geometry (Ig2_Superquadrics_Superquadrics_SuperquadricsGeom2) of
+// bodies a, b, with the prior (contactAngle, depth) when isNew == 0.  Writes depth, normal3,
+// contactPoint3, point1_3, point2_3, angle2, curvatures1_2, curvatures2_2, curvatureAngle,
+// alpha, K, E, curvatures_sum, isSphere -> 25 doubles; returns the Nelder-Mead evaluations.
+int sqo_pair_geom2(void* h, int ia, int ib, int isNew, const double* prior4, double* out) {
+  Scene* S = (Scene*)h;
+  Interaction I; std::memset(&I, 0, sizeof(I));
+  I.id1 = ia; I.id2 = ib;
+  if (!isNew) {
+    I.hasGeom = true; I.g.contactAngle[0] = prior4[0]; I.g.contactAngle[1] = prior4[1]; I.g.PenetrationDepth = prior4[2];
+  }
+  Stats st{};
+  const Body& a = S->bodies[ia]; const Body& b = S->bodies[ib];
+  ig2SqSq2(*S, &I, a, b, V3(), st);
+  const Geom& g = I.g;
+  out[0] = g.PenetrationDepth;
+  for (int k = 0; k < 3; k++) { out[1 + k] = g.normal[k]; out[4 + k] = g.contactPoint[k]; out[7 + k] = g.point1[k]; out[10 + k] = g.point2[k]; }
+  out[13] = g.contactAngle[0]; out[14] = g.contactAngle[1];
+  out[15] = g.curvatures1[0]; out[16] = g.curvatures1[1]; out[17] = g.curvatures2[0]; out[18] = g.curvatures2[1];
+  out[19] = g.curvatureAngle; out[20] = g.alpha; out[21] = g.K; out[22] = g.E; out[23] = g.curvatures_sum; out[24] = g.isSphere ? 1 : 0;
+  return (int)st.lmIters;
+}
+// Superquadrics::Curvatures at surface angles (ph0, ph1) of a shape with identity orientation:
+// k1, k2, dirMax3, dirMin3, maxFlag -> 9 doubles
+void sqo_curvatures(double rx, double ry, double rz, double e1, double e2, double ph0, double ph1, double* out) {
+  SQ q; std::memset(&q, 0, sizeof(q));
+  q.rx = rx; q.ry = ry; q.rz = rz; q.eps1 = e1; q.eps2 = e2;
+  sqInitial(q);
+  q.loc = toRot(Quat{1, 0, 0, 0}); q.glob = q.loc;
+  V3 dmax, dmin; bool f; Real k[2];
+  sqCurvatures(q, ph0, ph1, dmax, dmin, f, k);
+  out[0] = k[0]; out[1] = k[1];
+  for (int j = 0; j < 3; j++) { out[2 + j] = dmax[j]; out[5 + j] = dmin[j]; }
+  out[8] = f ? 1 : 0;
+}
+// SuperquadricsGeom2::HertzMindlin: curvature_sum, alpha, K, E
+void sqo_hertz_mindlin(const double* c1, const double* c2, double theta, double* out4) {
+  Geom g; std::memset(&g, 0, sizeof(g));
+  hertzMindlin(g, c1, c2, theta);
+  out4[0] = g.curvatures_sum; out4[1] = g.alpha; out4[2] = g.K; out4[3] = g.E;
 }
 
 // Shape properties (Superquadrics::Initial): volume, inertia3 (geometric), r_max
@@ -1702,6 +2107,11 @@ void sqo_put_servo(void* h, const double* o) {
   C.strain2 = o[25]; C.iterate_num = (unsigned)o[26]; C.solve_num = (unsigned)o[27]; C.rampNum = (unsigned)o[28];
   C.Flag_ForceTarget = o[29] != 0; C.firstRun = o[30] != 0; C.width0 = o[31]; C.height0 = o[32]; C.depth0 = o[33];
 }
+// Contact model: 0 SuperquadricsGeom/Phys/Law, 1 SuperquadricsGeom2 + HertzMindlinPhys + Law2
+void sqo_set_contact_model(void* h, int model) { ((Scene*)h)->contactModel = model; }
+// SuperquadricsMat2 {G, nu} of material m
+void sqo_set_moduli(void* h, int m, double G, double nu) { ((Scene*)h)->mats[m].G = G; ((Scene*)h)->mats[m].nu = nu; }
+void sqo_stats_nan_forces(void* h, long* out) { *out = ((Scene*)h)->stats.nanForces; }
 void sqo_set_quiet(void* h, int on) { ((Scene*)h)->quietSystem = on != 0; }
 double sqo_unbalanced_force(void* h, int useMax) { return unbalancedForce(*(Scene*)h, useMax != 0); }
 void sqo_get_stress(void* h, double volume, double* out9) {

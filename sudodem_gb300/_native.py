@@ -11,7 +11,7 @@ import numpy as np
 from . import build as _build
 
 BODY_STRIDE = 37
-INTR_STRIDE = 47
+INTR_STRIDE = 57
 NSCALARS = 9
 
 SQDEM_SUPERQUADRIC = 0
@@ -108,6 +108,8 @@ def load_library(build_if_missing=True):
         "sqdem_get_cell": (i, [v, dp]),
         "sqdem_put_cell": (i, [v, dp]),
         "sqdem_contacts_static_queue": (i, [v]),
+        "sqdem_set_contact_model": (i, [v, i]), "sqdem_contact_model": (i, [v]), "sqdem_num_materials": (i, [v]),
+        "sqdem_set_material_moduli": (i, [v, i, dp, dp]), "sqdem_get_material_moduli": (i, [v, dp, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -128,7 +130,9 @@ def exported_symbols():
             "sqdem_set_servo", "sqdem_get_servo", "sqdem_put_servo", "sqdem_set_quiet", "sqdem_unbalanced_force",
             "sqdem_get_stress", "sqdem_batch_create", "sqdem_batch_destroy", "sqdem_batch_last_error",
             "sqdem_batch_size", "sqdem_batch_scene", "sqdem_batch_step", "sqdem_batch_sync", "sqdem_batch_time_steps",
-            "sqdem_batch_time_e2e", "sqdem_batch_launch_count", "sqdem_snapshot", "sqdem_restore"]
+            "sqdem_batch_time_e2e", "sqdem_batch_launch_count", "sqdem_snapshot", "sqdem_restore",
+            "sqdem_set_contact_model", "sqdem_contact_model", "sqdem_num_materials", "sqdem_set_material_moduli",
+            "sqdem_get_material_moduli"]
 
 
 def _dp(a):
@@ -211,15 +215,45 @@ class Engine:
         m = spec.materials
         self.set_materials(m["Kn"], m["Ks"], m["frictionAngle"], m["betan"], m["betas"], m["density"])
         self.set_params(**spec.params)
+        if "G" in m:
+            self.set_material_moduli(m["G"], m["nu"])
         self.set_bodies(spec.kind, spec.shape5, spec.wall_axis_sense, spec.mat, spec.isSphere, spec.state)
         if spec.info.get("periodic"):
             self.set_periodic(spec.info["hSize"], spec.info.get("velGrad"))
+        self.set_contact_model(spec.info.get("contact_model", "linear"))
 
     def set_use_graph(self, on=True):
         self._check(self.lib.sqdem_set_use_graph(self.h, 1 if on else 0))
 
     def set_lm_spread(self, on=True):
         self._check(self.lib.sqdem_set_lm_spread(self.h, 1 if on else 0))
+
+    CONTACT_MODELS = {"linear": 0, "hertz_mindlin": 1}
+
+    def set_contact_model(self, model):
+        """'linear' (SuperquadricsGeom/Phys/Law) or 'hertz_mindlin' (SuperquadricsGeom2,
+        HertzMindlinPhys, SuperquadricsLaw2)."""
+        if model not in self.CONTACT_MODELS:
+            raise ValueError("contact model must be 'linear' or 'hertz_mindlin'")
+        self._check(self.lib.sqdem_set_contact_model(self.h, self.CONTACT_MODELS[model]))
+
+    def contact_model(self):
+        k = self.lib.sqdem_contact_model(self.h)
+        return {v: n for n, v in self.CONTACT_MODELS.items()}[k]
+
+    def set_material_moduli(self, G, nu):
+        """SuperquadricsMat2 shear modulus G and Poisson's ratio nu per material."""
+        G = np.ascontiguousarray(G, dtype=np.float64)
+        nu = np.ascontiguousarray(nu, dtype=np.float64)
+        if G.shape != nu.shape or G.ndim != 1:
+            raise ValueError("G and nu must be 1-D arrays of the same length")
+        self._check(self.lib.sqdem_set_material_moduli(self.h, len(G), _dp(G), _dp(nu)))
+
+    def material_moduli(self):
+        n = self.lib.sqdem_num_materials(self.h)
+        G, nu = np.zeros(n), np.zeros(n)
+        self._check(self.lib.sqdem_get_material_moduli(self.h, _dp(G), _dp(nu)))
+        return G, nu
 
     # CompressionEngine, quiet flag, Shop reductions
     def set_servo(self, config):

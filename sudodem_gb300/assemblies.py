@@ -340,3 +340,28 @@ def config4(seed=0, n=1_000_000, r_range=(0.5e-3, 2.0e-3), eps_range=(0.2, 1.0),
     spec = _finish(b, mats, params, {"box": box, "height": z, "seed": seed})
     spec.params["dt"] = critical_dt(spec, dt_factor)
     return spec
+
+
+def hertz_mindlin(spec, G=2e8, nu=0.3, dt_factor=0.5, overlap=0.05):
+    """The scene with the Hertz-Mindlin contact model (SuperquadricsGeom2, SuperquadricsMat2
+    {G, nu}, Ip2_SuperquadricsMat2_SuperquadricsMat2_HertzMindlinPhys, SuperquadricsLaw2).
+    Walls (ids 0-5) keep the linear Kn, Ks of their material, as Ip2 gives them.  dt is
+    dt_factor * sqrt(m_min / k), k the larger of the wall Kn and the Hertz normal stiffness
+    8/3 Gab sqrt(depth R) of the smallest particle pair at the given relative overlap."""
+    m = dict(spec.materials)
+    nm = len(m["Kn"])
+    m["G"] = np.full(nm, float(G))
+    m["nu"] = np.full(nm, float(nu))
+    info = dict(spec.info)
+    info["contact_model"] = "hertz_mindlin"
+    out = SceneSpec(kind=spec.kind, shape5=spec.shape5, wall_axis_sense=spec.wall_axis_sense, mat=spec.mat,
+                    isSphere=spec.isSphere, state=spec.state, materials=m, params=dict(spec.params), info=info)
+    sq = spec.kind == 0
+    rmin = float(np.min(spec.shape5[sq, 0:3]))
+    gab = 1.0 / (2 * (1 - nu) / G)
+    r_eff = 0.5 * rmin
+    k_hm = 8.0 / 3.0 * gab * math.sqrt(overlap * rmin * r_eff)
+    k = max(k_hm, float(np.max(m["Kn"])))
+    mmin = float(np.min(spec.state[sq, 33]))
+    out.params["dt"] = dt_factor * math.sqrt(mmin / k)
+    return out

@@ -37,6 +37,7 @@
 #include <algorithm>
 #include <limits>
 #include "sq_device.cuh"
+#include "sq_hm.cuh"
 #include "../../include/sqdem.h"
 
 // Work queue of the contact stage for sqdem_contacts_static_queue: a fixed device array so
@@ -62,6 +63,7 @@ struct Params {
   double dt, g[3], damping, verletDist, minSweepDistFactor, h0;
   int targetInterv, sortAxis, isSuperquadrics, exactAsphericalRot, recordFull;
   int lmSpread;   // idle lanes evaluate the points running searches ask for next
+  int contactModel;   // SQDEM_CONTACT_LINEAR or SQDEM_CONTACT_HERTZ_MINDLIN
 };
 
 enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_EVAL32, E_EVAL64, E_ROUNDS_MAX, E_NUM };
@@ -111,6 +113,9 @@ struct Table {
   int4* cd;               // Interaction::cellDist in (id1, id2) order: shift2 = hSize*cd moves id2
   // full geometry record (written only when Params::recordFull)
   double4* p1; double4* p2; double4* shearInc; double4* twist; double4* ortho; double4* relVn; double4* relVs;
+  // SuperquadricsGeom2 fields (Hertz-Mindlin model, full record only): curvatures1 (2),
+  // curvatures2 (2) | curvatureAngle, alpha, K, E | curvatures_sum, isSphere
+  double4* hmCurv; double4* hmEll; double2* hmSum;
 };
 
 struct Dev {
@@ -125,6 +130,7 @@ struct Dev {
   int* walls;                 // ids of walls
   double4* mats;              // Kn, Ks, frictionAngle, density
   double2* matsB;             // betan, betas
+  double2* matsE;             // SuperquadricsMat2 G, nu
   // tables
   Table A, B;
   int* rowStart; int* rowStartNew; int* rowCount;
@@ -714,6 +720,7 @@ __device__ __forceinline__ void copyEntry(const Table& s, int a, const Table& t,
   if (full) {
     t.p1[b] = s.p1[a]; t.p2[b] = s.p2[a]; t.shearInc[b] = s.shearInc[a]; t.twist[b] = s.twist[a];
     t.ortho[b] = s.ortho[a]; t.relVn[b] = s.relVn[a]; t.relVs[b] = s.relVs[a];
+    t.hmCurv[b] = s.hmCurv[a]; t.hmEll[b] = s.hmEll[a]; t.hmSum[b] = s.hmSum[a];
   }
 }
 __device__ __forceinline__ void initEntry(const Table& t, int b, int owner, int partner, bool ownerIsId1, bool full) {
@@ -721,7 +728,10 @@ __device__ __forceinline__ void initEntry(const Table& t, int b, int owner, int 
   t.owner[b] = owner; t.partner[b] = partner; t.flags[b] = F_SHEARNEW | (ownerIsId1 ? F_OWNER_ID1 : 0u);
   t.angle[b] = make_double2(0, 0); t.depth[b] = 0; t.normal[b] = z; t.shear[b] = z; t.nforce[b] = z;
   t.phys[b] = z; t.F[b] = z; t.cp[b] = z; t.cd[b] = make_int4(0, 0, 0, 0);
-  if (full) { t.p1[b] = z; t.p2[b] = z; t.shearInc[b] = z; t.twist[b] = z; t.ortho[b] = z; t.relVn[b] = z; t.relVs[b] = z; }
+  if (full) {
+    t.p1[b] = z; t.p2[b] = z; t.shearInc[b] = z; t.twist[b] = z; t.ortho[b] = z; t.relVn[b] = z; t.relVs[b] = z;
+    t.hmCurv[b] = z; t.hmEll[b] = z; t.hmSum[b] = make_double2(0, 0);
+  }
 }
 
 __global__ void k_merge(Dev d) {
@@ -908,6 +918,9 @@ struct GeomOut {
   D3 normal, cp, p1, p2, shearInc, twist, ortho, relVn, relVs;
   bool isShearNew;
   int lmIters, lmStop, lmCalls; bool nanNormal;
+  // SuperquadricsGeom2 fields set this step: 0 none, 1 sphere pair (curvatures_sum, isSphere),
+  // 2 curvatures, curvature angle and contact ellipse
+  int hm; double hc[4], hAng; HMEllipse hEll;
 };
 
 // SuperquadricsGeom::precompute (Superquadrics.cpp:1030-1050)
@@ -938,7 +951,7 @@ __device__ __forceinline__ void makeShape(SqShape& s, const BodyView& b) {
 // and centres farther apart than the bounding radii (:1973-1979).
 __device__ void geomSqSqSimple(GeomOut& g, bool isNew, double prevDepth, D3 oldNormal, D3 oldCp,
                                const BodyView& b1, const BodyView& b2, double dt, D3 shift2) {
-  g.precomputed = false; g.angSet = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 0; g.nanNormal = false;
+  g.precomputed = false; g.angSet = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 0; g.nanNormal = false; g.hm = 0;
   g.cp = oldCp;
   const D3 position1 = b1.pos, position2 = b2.pos + shift2;
   double para[2];
@@ -966,7 +979,7 @@ __device__ void geomSqSqSimple(GeomOut& g, bool isNew, double prevDepth, D3 oldN
 // Ig2_Wall_Superquadrics_SuperquadricsGeom::go (Superquadrics_Ig2.cpp:2522-2611)
 __device__ void geomWallSq(GeomOut& g, bool isNew, double prevDepth, D3 oldNormal, D3 oldCp, const BodyView& w,
                            const BodyView& b, double dt) {
-  g.precomputed = false; g.angSet = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 0; g.nanNormal = false;
+  g.precomputed = false; g.angSet = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 0; g.nanNormal = false; g.hm = 0;
   g.cp = oldCp;
   const int PA = w.info.w & 15;
   const double sense = (double)((w.info.w >> 4) - 1);
@@ -1001,6 +1014,37 @@ __device__ void geomWallSq(GeomOut& g, bool isNew, double prevDepth, D3 oldNorma
   g.normal = normal;
 }
 
+// Ig2_Superquadrics_Superquadrics_SuperquadricsGeom2::go for the cases without a Nelder-Mead
+// search (Superquadrics_Ig2.cpp:2348-2390): both bodies spheres, or centres farther apart than
+// the bounding radii.  The reference uses the unshifted positions here (only precompute
+// sees shift2).
+__device__ void geomSqSq2Simple(GeomOut& g, bool isNew, double prevDepth, D3 oldNormal, D3 oldCp,
+                                const BodyView& b1, const BodyView& b2, double dt, D3 shift2) {
+  g.precomputed = false; g.angSet = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 0; g.nanNormal = false; g.hm = 0;
+  g.cp = oldCp;
+  g.isShearNew = isNew ? true : (prevDepth <= 0);
+  const D3 position1 = b1.pos, position2 = b2.pos;
+  const double rmaxA = b1.shpA.w, rmaxB = b2.shpA.w;
+  const double r_sum = rmaxA + rmaxB;
+  if (!(b1.info.z != 0 && b2.info.z != 0)) { g.depth = 0; g.isShearNew = true; return; }
+  D3 dist = position2 - position1;
+  const double depth = r_sum - nrm(dist);
+  if (depth < 1E-18) { g.depth = 0; g.isShearNew = true; return; }
+  normalize(dist);
+  const D3 p1 = position1 + rmaxA * dist;
+  const D3 p2 = position2 - rmaxB * dist;
+  D3 contactNormal = p1 - p2;
+  normalize(contactNormal);
+  g.p1 = p1; g.p2 = p2;
+  g.cp = 0.5 * (p1 + p2);
+  g.depth = depth;
+  g.hm = 1; g.hEll.sum = r_sum / (rmaxA * rmaxB);
+  g.precomputed = true;
+  precomputeD(g, oldNormal, b1, b2, dt, contactNormal, g.isShearNew, shift2);
+  g.normal = contactNormal;
+  g.ang0 = 0; g.ang1 = 0; g.angSet = true;
+}
+
 // SuperquadricsGeom::rotate (Superquadrics.cpp:1053-1080)
 __device__ __forceinline__ D3 rotateShear(const GeomOut& g, D3 sf) {
   sf = sf - cross(sf, g.ortho);
@@ -1026,6 +1070,91 @@ __device__ __forceinline__ void flushCounters(const Dev& d, Counters c) {
   }
 }
 
+// Ip2_SuperquadricsMat2_SuperquadricsMat2_HertzMindlinPhys::go (Superquadrics.cpp:1118-1160) and
+// SuperquadricsLaw2::go (Superquadrics.cpp:1367-1557) for one entry whose geometry g was just
+// computed.  phys = (kn, ks, tanphi, -); particle pairs (id1 > 5) get kn and ks from the contact
+// ellipse every step they touch, walls (ids 0-5) keep their material's Kn, Ks.  kn and ks are
+// computed in double where the reference uses long double for pi and the products (a relative
+// difference of a few 1e-16).  A NaN force stops the run after this step (Scene::stopAtIter).
+__device__ void finishHM(const Dev& d, int e, unsigned fl, int id1, const BodyView& b1, const BodyView& b2,
+                         const GeomOut& g, Counters& cnt) {
+  const double4 m1 = d.mats[b1.info.y], m2 = d.mats[b2.info.y];
+  const double2 mb1 = d.matsB[b1.info.y], mb2 = d.matsB[b2.info.y];
+  double4 ph;
+  if (!(fl & F_PHYS)) {
+    if (id1 > 5) {
+      ph.x = 0; ph.y = 0; ph.z = tan(fmin_ref(m1.z, m2.z));
+    } else {
+      ph.z = tan(m1.z); ph.x = m1.x; ph.y = m1.y;
+    }
+    ph.w = 0;
+    fl |= F_PHYS;
+  } else ph = d.A.phys[e];
+  const double2 beta = make_double2(fmax_ref(mb1.x, mb2.x), fmax_ref(mb1.y, mb2.y));
+  if (!(g.depth > 1E-18)) {
+    d.A.phys[e] = ph;
+    d.A.nforce[e] = make_double4(0, 0, 0, 0);
+    d.A.shear[e] = make_double4(0, 0, 0, 0);
+    d.A.flags[e] = fl & ~F_FORCE;
+    return;
+  }
+  if (id1 > 5) {
+    const double2 E1 = d.matsE[b1.info.y], E2 = d.matsE[b2.info.y];   // (G, nu)
+    const double Gab = 1.0 / ((1 - E1.y) / E1.x + (1 - E2.y) / E2.x);
+    const double mu1 = 1. / E1.x + 1. / E2.x;
+    const double mu2 = E1.y / E1.x + E2.y / E2.x;
+    const double depth = g.depth;
+    const double csum = g.hEll.sum;
+    if (g.hm == 1) {
+      const double tmp = sqrt(depth / csum);
+      ph.x = 8. / 3. * Gab * tmp;
+      ph.y = 8. / (2.0 * mu1 - mu2) * tmp;
+    } else {
+      const double E = g.hEll.E, K = g.hEll.K, alpha = g.hEll.alpha;
+      const double a = sqrt(depth * E / csum / K);
+      ph.x = 4. / 3. * M_PI * a * Gab * alpha / K;
+      const double e2 = 1 - 1 / (alpha * alpha);
+      const double ksx = mu1 * K - mu2 * (K - E) / e2;
+      const double ksy = mu1 * K + mu2 * ((1 - e2) * K - E) / e2;
+      ph.y = M_PI * alpha * a * (1. / ksx + 1. / ksy);
+    }
+  }
+  d.A.phys[e] = ph;
+  D3 normalForce = g.normal * g.depth * ph.x;
+  const bool useDamping = (beta.x > 0.00001 || beta.y > 0.00001);
+  double cs = 0;
+  if (useDamping) {
+    const bool Adyn = b1.blocked != DOF_ALL, Bdyn = b2.blocked != DOF_ALL;
+    const double mbar = (!Adyn && Bdyn) ? b2.mass : ((!Bdyn && Adyn) ? b1.mass : (b1.mass * b2.mass / (b1.mass + b2.mass)));
+    const double Cn_crit = 2. * sqrt(mbar * ph.x), Cs_crit = 2. * sqrt(mbar * ph.y);
+    const double cn = Cn_crit * beta.x;
+    cs = Cs_crit * beta.y;
+    const D3 normalViscous = cn * g.relVn;
+    const D3 normTemp = normalForce - normalViscous;
+    if (dot(normTemp, g.normal) < 0.0) normalForce = d3(0, 0, 0);
+    else normalForce = normalForce - normalViscous;
+  }
+  D3 shearForce1;
+  if (g.isShearNew) shearForce1 = d3(0, 0, 0);
+  else shearForce1 = rotateShear(g, xyz(d.A.shear[e]));
+  shearForce1 = shearForce1 - ph.y * g.shearInc;
+  const double maxFs = sqn(normalForce) * (ph.z * ph.z);   // std::pow(x, 2) is x*x correctly rounded
+  if (sqn(shearForce1) > maxFs) {
+    const double ratio = sqrt(maxFs) / nrm(shearForce1);
+    shearForce1 = shearForce1 * ratio;
+  } else if (useDamping) {
+    shearForce1 = shearForce1 - cs * g.relVs;
+  }
+  if (isnan(shearForce1.x) || isnan(normalForce.x)) {
+    normalForce = d3(0, 0, 0); shearForce1 = d3(0, 0, 0); cnt.nanF++;
+    d.S->haltAt = d.S->iter + 1;
+  }
+  d.A.F[e] = dd4((-normalForce) - shearForce1, 0);
+  d.A.nforce[e] = dd4(normalForce, 0);
+  d.A.shear[e] = dd4(shearForce1, 0);
+  d.A.flags[e] = fl | F_FORCE;
+}
+
 // Geometry history writes, Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys::go
 // (Superquadrics.cpp:1086-1116) and SuperquadricsLaw::go (Superquadrics.cpp:1209-1361) for
 // one entry whose geometry g was just computed.
@@ -1048,6 +1177,14 @@ __device__ void finishEntry(const Dev& d, int e, unsigned fl, bool isNew, int id
     const double4 z = make_double4(0, 0, 0, 0);
     d.A.p1[e] = z; d.A.p2[e] = z; d.A.shearInc[e] = z; d.A.twist[e] = z; d.A.ortho[e] = z; d.A.relVn[e] = z; d.A.relVs[e] = z;
   }
+  if (full && isNew) { d.A.hmCurv[e] = make_double4(0, 0, 0, 0); d.A.hmEll[e] = make_double4(0, 0, 0, 0); d.A.hmSum[e] = make_double2(0, 0); }
+  if (full && g.hm == 1) d.A.hmSum[e] = make_double2(g.hEll.sum, 1.0);
+  if (full && g.hm == 2) {
+    d.A.hmCurv[e] = make_double4(g.hc[0], g.hc[1], g.hc[2], g.hc[3]);
+    d.A.hmEll[e] = make_double4(g.hAng, g.hEll.alpha, g.hEll.K, g.hEll.E);
+    d.A.hmSum[e] = make_double2(g.hEll.sum, d.A.hmSum[e].y);
+  }
+  if (d.prm->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN) { finishHM(d, e, fl, id1, b1, b2, g, cnt); return; }
   double4 ph;
   double2 beta;
   const double2 mb1 = d.matsB[b1.info.y], mb2 = d.matsB[b2.info.y];
@@ -1172,7 +1309,12 @@ __global__ void __launch_bounds__(128) k_contacts_pre(Dev d) {
         GeomOut g;
         bool done = true;
         if (b1.info.x == KIND_WALL) geomWallSq(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt);
-        else {
+        else if (d.prm->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN) {
+          const bool sph = (b1.info.z != 0) && (b2.info.z != 0);
+          if (sph || nrm(b1.pos - b2.pos) > b1.shpA.w + b2.shpA.w)
+            geomSqSq2Simple(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt, shift2);
+          else done = false;
+        } else {
           const bool sph = (b1.info.z != 0) && (b2.info.z != 0);
           if (!sph && !(nrm(b1.pos - (b2.pos + shift2)) > b1.shpA.w + b2.shpA.w)) {
             double para[2];
@@ -1616,6 +1758,136 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
           active = false;
           roundsMax = max(roundsMax, L.rounds);
         }
+      }
+    }
+    __syncwarp();
+  }
+  flushCounters(d, cnt);
+  for (int o = 16; o > 0; o >>= 1) {
+    ev64 += __shfl_down_sync(0xffffffffu, ev64, o);
+    roundsMax = max(roundsMax, __shfl_down_sync(0xffffffffu, roundsMax, o));
+  }
+  if (lane == 0) { atomicAdd(&d.S->err[E_EVAL64], ev64); atomicMax(&d.S->err[E_ROUNDS_MAX], (unsigned long long)roundsMax); }
+}
+
+// ---------------------------------------------------------------------------
+// Pass 2 of the Hertz-Mindlin model: the Nelder-Mead searches of
+// Ig2_Superquadrics_Superquadrics_SuperquadricsGeom2::go (Superquadrics_Ig2.cpp:2391-2430),
+// one per lane, each round one Disfun evaluation per lane (NMState asks for one point per
+// step), a lane that finishes a contact taking the next one from the queue.  The search
+// starts at the stored contactAngle with the simplex size 0.1 rad for a new geometry and
+// 0.001 rad for an existing one.
+struct NMLane {
+  int e;
+  bool isNew;
+  NMState M;
+  D3 P1, P2;   // support points of the last evaluation (the reference keeps those)
+  unsigned rounds;
+};
+
+// End of Ig2_Superquadrics_Superquadrics_SuperquadricsGeom2::go after the search
+// (Superquadrics_Ig2.cpp:2431-2516), then Ip2 + Law2.
+__device__ void nmFinish(const Dev& d, const NMLane& L, const SqShape& A, const SqShape& B, const Rot& gc,
+                         Counters& cnt) {
+  const SceneState& S = *d.S;
+  const int e = L.e;
+  const unsigned fl = d.A.flags[e];
+  int id1, id2;
+  entryIds(d, e, fl, id1, id2);
+  const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
+  GeomOut g;
+  g.lmCalls = 1; g.lmIters = L.M.nfunc; g.lmStop = 0; g.nanNormal = false; g.hm = 0;
+  g.isShearNew = L.isNew ? true : (d.A.depth[e] <= 0);
+  g.cp = L.isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
+  g.ang0 = L.M.r0; g.ang1 = L.M.r1; g.angSet = true;
+  if (!L.M.touching) {
+    g.precomputed = false; g.depth = 0; g.isShearNew = true;
+  } else {
+    D3 contactNormal = L.P1 - L.P2;
+    normalize(contactNormal);
+    g.p1 = L.P1; g.p2 = L.P2;
+    g.cp = 0.5 * (L.P1 + L.P2);
+    g.depth = L.M.dist;
+    double sa0, ca0, sa1, ca1;
+    sincos(L.M.r0, &sa0, &ca0);
+    sincos(L.M.r1, &sa1, &ca1);
+    const D3 contact = mulG(gc, d3(ca0 * sa1, sa0 * sa1, ca1));
+    const D3 contact1 = mulL(A.R, contact), contact2 = mulL(B.R, contact);
+    D3 dmax1, dmin1, dmax2, dmin2;
+    bool f1, f2;
+    double c1[2], c2[2], ph0, ph1;
+    normal2Phi(A, contact1, ph0, ph1);
+    curvatures(A, ph0, ph1, dmax1, dmin1, f1, c1);
+    normal2Phi(B, (-1.0) * contact2, ph0, ph1);
+    curvatures(B, ph0, ph1, dmax2, dmin2, f2, c2);
+    const D3 cd1 = (f1 && f2) ? dmax1 : dmin1, cd2 = (f1 && f2) ? dmax2 : dmin2;
+    const D3 nd = contactNormal;
+    const D3 dir1 = d3(cd1.x * nd.x, cd1.y * nd.y, cd1.z * nd.z) - cd1;
+    const D3 dir2 = d3(cd2.x * nd.x, cd2.y * nd.y, cd2.z * nd.z) - cd2;
+    double angle = acos(dot(dir1, dir2) / (nrm(dir1) * nrm(dir2)));
+    if (isnan(angle)) angle = 0.0;
+    g.hm = 2;
+    g.hc[0] = c1[0]; g.hc[1] = c1[1]; g.hc[2] = c2[0]; g.hc[3] = c2[1]; g.hAng = angle;
+    g.hEll = hertzMindlin(c1, c2, angle);
+    const D3 oldNormal = L.isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
+    g.precomputed = true;
+    precomputeD(g, oldNormal, b1, b2, d.prm->dt, contactNormal, g.isShearNew, cellShift(S, d.A.cd[e]));
+    g.normal = contactNormal;
+  }
+  cnt.lmCalls += 1; cnt.lmIters += L.M.nfunc; cnt.lmMax += (L.M.nfunc >= NM_NMAX);
+  finishEntry(d, e, fl, L.isNew, id1, b1, b2, g, cnt);
+}
+
+__global__ void __launch_bounds__(LM_BS) k_contacts_nm(Dev d) {
+  __shared__ SqShape shA[LM_BS], shB[LM_BS];
+  __shared__ Rot shG[LM_BS];
+  const SceneState& S = *d.S;
+  const int count = S.lmCount;
+  const int lane = threadIdx.x & 31;
+  Counters cnt = {0, 0, 0, 0, 0};
+  unsigned long long ev64 = 0;
+  unsigned roundsMax = 0;
+  NMLane L;
+  bool active = false, exhausted = false;
+  while (true) {
+    const unsigned idle = __ballot_sync(0xffffffffu, !active && !exhausted);
+    if (idle) {
+      const int leader = __ffs(idle) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&d.S->lmHead, __popc(idle));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (!active && !exhausted) {
+        const int idx = base + __popc(idle & ((1u << lane) - 1));
+        if (idx < count) {
+          SqShape& A = shA[threadIdx.x];
+          SqShape& B = shB[threadIdx.x];
+          L.e = d.lmQueue[idx];
+          const unsigned fl = d.A.flags[L.e];
+          int id1, id2;
+          entryIds(d, L.e, fl, id1, id2);
+          const double4 o1 = d.ori[id1], o2 = d.ori[id2];
+          const double4 a1 = d.shpA[id1], a2 = d.shpA[id2], e1 = d.shpB[id1], e2 = d.shpB[id2];
+          shapeInit(A, a1.x, a1.y, a1.z, e1.x, e1.y, a1.w); A.R = quatToRot(o1.x, o1.y, o1.z, o1.w); A.pos = xyz(d.pos[id1]);
+          shapeInit(B, a2.x, a2.y, a2.z, e2.x, e2.y, a2.w); B.R = quatToRot(o2.x, o2.y, o2.z, o2.w); B.pos = xyz(d.pos[id2]);
+          shG[threadIdx.x] = cRotationMat(A.pos, B.pos);
+          L.isNew = !(fl & F_GEOM);
+          const double2 an = L.isNew ? make_double2(0, 0) : d.A.angle[L.e];
+          nmStart(L.M, an.x, an.y, L.isNew ? 0.1 : 0.001);
+          L.P1 = d3(0, 0, 0); L.P2 = d3(0, 0, 0); L.rounds = 0;
+          active = true;
+        } else exhausted = true;
+      }
+    }
+    if (!__any_sync(0xffffffffu, active)) break;
+    if (active) {
+      bool apart;
+      const double f = disfunNM(shA[threadIdx.x], shB[threadIdx.x], shG[threadIdx.x], L.M.q0, L.M.q1, L.P1, L.P2, apart);
+      ev64++;
+      L.rounds++;
+      if (!nmConsume(L.M, f, apart)) {
+        nmFinish(d, L, shA[threadIdx.x], shB[threadIdx.x], shG[threadIdx.x], cnt);
+        active = false;
+        roundsMax = max(roundsMax, L.rounds);
       }
     }
     __syncwarp();
@@ -2498,11 +2770,12 @@ struct sqdem_ctx {
   sqdem_params params;
   int recordFull = 0;
   int lmSpread = 1;
+  int contactModel = SQDEM_CONTACT_LINEAR;
   bool servoOn = false;
   std::vector<int> kind, wallIds, matIds, isSphere, axisSense;
   std::vector<double> shape5;
   int nMats = 0;
-  std::vector<double4> hostMats; std::vector<double2> hostMatsB;
+  std::vector<double4> hostMats; std::vector<double2> hostMatsB, hostMatsE;
   long long launches = 0, launchesPerStep = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   float stageMs[3] = {0, 0, 0};
@@ -2542,6 +2815,7 @@ static sqdem_status allocTable(sqdem_ctx* c, Table& t, int cap) {
   CK(dalloc(c, &t.F, cap)); CK(dalloc(c, &t.cp, cap)); CK(dalloc(c, &t.cd, cap));
   CK(dalloc(c, &t.p1, cap)); CK(dalloc(c, &t.p2, cap)); CK(dalloc(c, &t.shearInc, cap));
   CK(dalloc(c, &t.twist, cap)); CK(dalloc(c, &t.ortho, cap)); CK(dalloc(c, &t.relVn, cap)); CK(dalloc(c, &t.relVs, cap));
+  CK(dalloc(c, &t.hmCurv, cap)); CK(dalloc(c, &t.hmEll, cap)); CK(dalloc(c, &t.hmSum, cap));
   return SQDEM_OK;
 }
 
@@ -2594,7 +2868,8 @@ static void enqueueStep(sqdem_ctx* c, bool timed) {
   // LM grid: all resident blocks, fewer for a small table (at most one lane per 4 entries)
   const int lmFull = c->numSMs * (c->precision == SQDEM_MIXED ? c->lmBlocksPerSMmixed : c->lmBlocksPerSM);
   const int lmGrid = std::max(1, std::min(lmFull, nblk(d.Pcap, LM_BS * 4)));
-  if (c->precision == SQDEM_MIXED) k_contacts_lm_mixed<<<lmGrid, LM_BS, 0, s>>>(d);
+  if (c->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN) k_contacts_nm<<<lmGrid, LM_BS, 0, s>>>(d);
+  else if (c->precision == SQDEM_MIXED) k_contacts_lm_mixed<<<lmGrid, LM_BS, 0, s>>>(d);
   else k_contacts_lm<<<lmGrid, LM_BS, 0, s>>>(d);
   c->launches += 2;
   if (timed) cudaEventRecord(c->ev[2], s);
@@ -2651,6 +2926,7 @@ static sqdem_status uploadParams(sqdem_ctx* c) {
   P.sortAxis = c->params.sortAxis; P.isSuperquadrics = c->params.isSuperquadrics;
   P.exactAsphericalRot = c->params.exactAsphericalRot; P.recordFull = c->recordFull;
   P.lmSpread = c->lmSpread;
+  P.contactModel = c->contactModel;
   P.h0 = hostH0(c);
   CK(cudaMemcpyAsync(c->d.prm, &P, sizeof(P), cudaMemcpyHostToDevice, c->stream));
   return SQDEM_OK;
@@ -2746,6 +3022,7 @@ sqdem_status sqdem_set_materials(sqdem_ctx* c, int n, const double* Kn, const do
   CK(cudaSetDevice(c->device));
   std::vector<double4>& m = c->hostMats; std::vector<double2>& mb = c->hostMatsB;
   m.resize(n); mb.resize(n);
+  if ((int)c->hostMatsE.size() != n) c->hostMatsE.assign(n, make_double2(29e9, 0.15));   // SuperquadricsMat2 defaults
   for (int i = 0; i < n; i++) { m[i] = make_double4(Kn[i], Ks[i], fa[i], rho[i]); mb[i] = make_double2(bn[i], bs[i]); }
   c->nMats = n; c->haveMats = true;
   if (c->haveBodies) {
@@ -2800,9 +3077,10 @@ sqdem_status sqdem_set_bodies(sqdem_ctx* c, int n, const int* kind, const double
   CK(cudaStreamSynchronize(c->stream));
   freeAll(c);
   c->haveBodies = false;
-  CK(dalloc(c, &c->d.mats, c->nMats)); CK(dalloc(c, &c->d.matsB, c->nMats));
+  CK(dalloc(c, &c->d.mats, c->nMats)); CK(dalloc(c, &c->d.matsB, c->nMats)); CK(dalloc(c, &c->d.matsE, c->nMats));
   CK(cudaMemcpyAsync(c->d.mats, c->hostMats.data(), sizeof(double4) * c->nMats, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(c->d.matsB, c->hostMatsB.data(), sizeof(double2) * c->nMats, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d.matsE, c->hostMatsE.data(), sizeof(double2) * c->nMats, cudaMemcpyHostToDevice, c->stream));
   c->kind.assign(kind, kind + n);
   c->matIds.assign(mat, mat + n);
   c->shape5.assign(5 * (size_t)n, 0.0);
@@ -3076,7 +3354,8 @@ sqdem_status sqdem_get_interactions(sqdem_ctx* c, int include_potential, double*
   const int P = S.P;
   const Table& T = c->d.A;
   std::vector<int> ow(P), pa(P); std::vector<unsigned> fl(P); std::vector<double2> an(P); std::vector<double> de(P);
-  std::vector<double4> nm(P), sh(P), nf(P), ph(P), cp(P), p1(P), p2(P), si(P), tw(P), orr(P), rn(P), rs(P);
+  std::vector<double4> nm(P), sh(P), nf(P), ph(P), cp(P), p1(P), p2(P), si(P), tw(P), orr(P), rn(P), rs(P), hc(P), he(P);
+  std::vector<double2> hs(P);
   std::vector<int4> cdv(P);
   std::vector<int2> ww(S.nWW);
   if (P) {
@@ -3092,6 +3371,8 @@ sqdem_status sqdem_get_interactions(sqdem_ctx* c, int include_potential, double*
     CK(cudaMemcpy(p2.data(), T.p2, b4, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(si.data(), T.shearInc, b4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(tw.data(), T.twist, b4, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(orr.data(), T.ortho, b4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(rn.data(), T.relVn, b4, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(rs.data(), T.relVs, b4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hc.data(), T.hmCurv, b4, cudaMemcpyDeviceToHost)); CK(cudaMemcpy(he.data(), T.hmEll, b4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hs.data(), T.hmSum, 16 * (size_t)P, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(cdv.data(), T.cd, sizeof(int4) * (size_t)P, cudaMemcpyDeviceToHost));
   }
   if (S.nWW) CK(cudaMemcpy(ww.data(), c->d.ww, sizeof(int2) * S.nWW, cudaMemcpyDeviceToHost));
@@ -3111,6 +3392,8 @@ sqdem_status sqdem_get_interactions(sqdem_ctx* c, int include_potential, double*
       o[23] = ph[i].x; o[24] = ph[i].y; o[25] = ph[i].z;
       put3(o + 26, nf[i]); put3(o + 29, sh[i]); put3(o + 32, tw[i]); put3(o + 35, orr[i]); put3(o + 38, rn[i]); put3(o + 41, rs[i]);
       o[44] = cdv[i].x; o[45] = cdv[i].y; o[46] = cdv[i].z;   // stored for (id1, id2)
+      o[47] = hc[i].x; o[48] = hc[i].y; o[49] = hc[i].z; o[50] = hc[i].w;
+      o[51] = he[i].x; o[52] = he[i].y; o[53] = he[i].z; o[54] = he[i].w; o[55] = hs[i].x; o[56] = hs[i].y;
     }
     k++;
   }
@@ -3156,7 +3439,8 @@ sqdem_status sqdem_put_interactions(sqdem_ctx* c, long n, const double* in) {
   if (P > c->d.Pcap) return fail(c, SQDEM_ERR_CAPACITY, "too many interactions for the table");
   std::vector<int> ow(P), pa(P), rowStart(N + 1, 0);
   std::vector<unsigned> fl(P); std::vector<double2> an(P); std::vector<double> de(P);
-  std::vector<double4> nm(P), sh(P), nf(P), ph(P), cp(P), p1(P), p2(P), si(P), tw(P), orr(P), rn(P), rs(P), F(P);
+  std::vector<double4> nm(P), sh(P), nf(P), ph(P), cp(P), p1(P), p2(P), si(P), tw(P), orr(P), rn(P), rs(P), F(P), hc(P), he(P);
+  std::vector<double2> hs(P);
   std::vector<int4> cdv(P);
   auto g3 = [](const double* o) { return make_double4(o[0], o[1], o[2], 0); };
   for (int e = 0; e < P; e++) {
@@ -3175,6 +3459,8 @@ sqdem_status sqdem_put_interactions(sqdem_ctx* c, long n, const double* in) {
     nf[e] = g3(o + 26); sh[e] = g3(o + 29); tw[e] = g3(o + 32); orr[e] = g3(o + 35); rn[e] = g3(o + 38); rs[e] = g3(o + 41);
     F[e] = make_double4(0, 0, 0, 0);
     cdv[e] = make_int4((int)o[44], (int)o[45], (int)o[46], 0);
+    hc[e] = make_double4(o[47], o[48], o[49], o[50]); he[e] = make_double4(o[51], o[52], o[53], o[54]);
+    hs[e] = make_double2(o[55], o[56]);
   }
   for (int i = 0; i < N; i++) rowStart[i + 1] += rowStart[i];
   // partner incidence lists (ascending entry index) and wall lists
@@ -3201,6 +3487,7 @@ sqdem_status sqdem_put_interactions(sqdem_ctx* c, long n, const double* in) {
   CK(up(T.cp, cp.data(), b4)); CK(up(T.p1, p1.data(), b4)); CK(up(T.p2, p2.data(), b4)); CK(up(T.shearInc, si.data(), b4));
   CK(up(T.twist, tw.data(), b4)); CK(up(T.ortho, orr.data(), b4)); CK(up(T.relVn, rn.data(), b4)); CK(up(T.relVs, rs.data(), b4));
   CK(up(T.F, F.data(), b4));
+  CK(up(T.hmCurv, hc.data(), b4)); CK(up(T.hmEll, he.data(), b4)); CK(up(T.hmSum, hs.data(), 16 * (size_t)P));
   CK(up(T.cd, cdv.data(), sizeof(int4) * (size_t)P));
   CK(up(c->d.rowStart, rowStart.data(), 4 * (size_t)(N + 1)));
   CK(up(c->d.pStart, pStart.data(), 4 * (size_t)(N + 1))); CK(up(c->d.pList, pList.data(), 4 * (size_t)P));
@@ -3465,6 +3752,39 @@ sqdem_status sqdem_set_lm_spread(sqdem_ctx* c, int on) {
   return SQDEM_OK;
 }
 
+sqdem_status sqdem_set_contact_model(sqdem_ctx* c, int model) {
+  if (!c) return SQDEM_ERR_ARG;
+  if (model != SQDEM_CONTACT_LINEAR && model != SQDEM_CONTACT_HERTZ_MINDLIN)
+    return fail(c, SQDEM_ERR_ARG, "contact model must be SQDEM_CONTACT_LINEAR or SQDEM_CONTACT_HERTZ_MINDLIN");
+  if (model != c->contactModel) { c->contactModel = model; c->graphValid = false; c->epoch++; }
+  if (c->haveBodies) { CK(cudaSetDevice(c->device)); sqdem_status s = uploadParams(c); if (s) return s; CK(cudaStreamSynchronize(c->stream)); }
+  return SQDEM_OK;
+}
+
+int sqdem_contact_model(sqdem_ctx* c) { return c ? c->contactModel : -1; }
+int sqdem_num_materials(sqdem_ctx* c) { return (c && c->haveMats) ? c->nMats : 0; }
+
+sqdem_status sqdem_set_material_moduli(sqdem_ctx* c, int n, const double* G, const double* nu) {
+  if (!c || !G || !nu) return SQDEM_ERR_ARG;
+  if (!c->haveMats || n != c->nMats) return fail(c, SQDEM_ERR_ARG, "moduli need one (G, nu) per material, after sqdem_set_materials");
+  for (int i = 0; i < n; i++)
+    if (!(G[i] > 0) || !std::isfinite(G[i]) || !std::isfinite(nu[i])) return fail(c, SQDEM_ERR_ARG, "G must be positive and finite, nu finite");
+  for (int i = 0; i < n; i++) c->hostMatsE[i] = make_double2(G[i], nu[i]);
+  if (c->haveBodies) {
+    CK(cudaSetDevice(c->device));
+    CK(cudaMemcpyAsync(c->d.matsE, c->hostMatsE.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_get_material_moduli(sqdem_ctx* c, double* G, double* nu) {
+  if (!c || !G || !nu) return SQDEM_ERR_ARG;
+  if (!c->haveMats) return fail(c, SQDEM_ERR_STATE, "no materials");
+  for (int i = 0; i < c->nMats; i++) { G[i] = c->hostMatsE[i].x; nu[i] = c->hostMatsE[i].y; }
+  return SQDEM_OK;
+}
+
 
 // ---------------------------------------------------------------------------
 // Boundary controller (CompressionEngine), quiet flag, Shop reductions.
@@ -3645,12 +3965,12 @@ sqdem_status sqdem_get_stress(sqdem_ctx* c, double volume, double* out9) {
 // CompressionEngine).  A context restored from it continues bit for bit as the original
 // would.  The blob records the library's state-record sizes; a blob from a build with other
 // sizes is refused.
-static const char SNAP_MAGIC[8] = {'S', 'Q', 'D', 'E', 'M', 'S', 'N', '1'};
+static const char SNAP_MAGIC[8] = {'S', 'Q', 'D', 'E', 'M', 'S', 'N', '2'};
 struct SnapHeader {
   char magic[8];
   unsigned long long sceneBytes, servoBytes, paramsBytes;
   long long N, nMats, nRec;
-  int recordFull, lmSpread, servoOn, pad;
+  int recordFull, lmSpread, servoOn, contactModel;
 };
 
 sqdem_status sqdem_snapshot(sqdem_ctx* c, void* buf, size_t* size) {
@@ -3661,7 +3981,7 @@ sqdem_status sqdem_snapshot(sqdem_ctx* c, void* buf, size_t* size) {
   long nRec = 0;
   sqdem_status s = sqdem_num_interactions(c, 1, &nRec);
   if (s) return s;
-  const size_t need = sizeof(SnapHeader) + sizeof(sqdem_params) + sizeof(double) * 6 * c->nMats +
+  const size_t need = sizeof(SnapHeader) + sizeof(sqdem_params) + sizeof(double) * 8 * c->nMats +
                       N * (sizeof(int) * 5 + sizeof(double) * 5) + sizeof(double) * SQDEM_BODY_STRIDE * N +
                       sizeof(double4) * 2 * N + sizeof(double) * SQDEM_INTR_STRIDE * nRec + sizeof(SceneState);
   if (!buf) { *size = need; return SQDEM_OK; }
@@ -3673,12 +3993,12 @@ sqdem_status sqdem_snapshot(sqdem_ctx* c, void* buf, size_t* size) {
   std::memcpy(h.magic, SNAP_MAGIC, 8);
   h.sceneBytes = sizeof(SceneState); h.servoBytes = sizeof(ServoDev); h.paramsBytes = sizeof(sqdem_params);
   h.N = N; h.nMats = c->nMats; h.nRec = nRec;
-  h.recordFull = c->recordFull; h.lmSpread = c->lmSpread; h.servoOn = c->servoOn ? 1 : 0;
+  h.recordFull = c->recordFull; h.lmSpread = c->lmSpread; h.servoOn = c->servoOn ? 1 : 0; h.contactModel = c->contactModel;
   put(&h, sizeof(h));
   put(&c->params, sizeof(sqdem_params));
   for (int i = 0; i < c->nMats; i++) {
-    const double m[6] = {c->hostMats[i].x, c->hostMats[i].y, c->hostMats[i].z, c->hostMatsB[i].x, c->hostMatsB[i].y,
-                         c->hostMats[i].w};
+    const double m[8] = {c->hostMats[i].x, c->hostMats[i].y, c->hostMats[i].z, c->hostMatsB[i].x, c->hostMatsB[i].y,
+                         c->hostMats[i].w, c->hostMatsE[i].x, c->hostMatsE[i].y};
     put(m, sizeof(m));
   }
   put(c->kind.data(), sizeof(int) * N);
@@ -3721,7 +4041,7 @@ sqdem_status sqdem_restore(sqdem_ctx* c, const void* buf, size_t size) {
   const long long N = h.N;
   sqdem_params P;
   if (!get(&P, sizeof(P))) return fail(c, SQDEM_ERR_ARG, "truncated snapshot");
-  std::vector<double> m(6 * h.nMats);
+  std::vector<double> m(8 * h.nMats);
   if (!get(m.data(), sizeof(double) * m.size())) return fail(c, SQDEM_ERR_ARG, "truncated snapshot");
   std::vector<int> kind(N), was(2 * N), mat(N), sph(N);
   std::vector<double> s5(5 * N), st(SQDEM_BODY_STRIDE * N), rec(SQDEM_INTR_STRIDE * (size_t)h.nRec);
@@ -3731,15 +4051,19 @@ sqdem_status sqdem_restore(sqdem_ctx* c, const void* buf, size_t size) {
       !get(s5.data(), 40 * N) || !get(st.data(), sizeof(double) * st.size()) || !get(pm.data(), sizeof(double4) * 2 * N) ||
       !get(rec.data(), sizeof(double) * rec.size()) || !get(&S, sizeof(S)))
     return fail(c, SQDEM_ERR_ARG, "truncated snapshot");
-  std::vector<double> Kn(h.nMats), Ks(h.nMats), fa(h.nMats), bn(h.nMats), bs(h.nMats), rho(h.nMats);
+  std::vector<double> Kn(h.nMats), Ks(h.nMats), fa(h.nMats), bn(h.nMats), bs(h.nMats), rho(h.nMats), G(h.nMats), nu(h.nMats);
   for (long long i = 0; i < h.nMats; i++) {
-    Kn[i] = m[6 * i]; Ks[i] = m[6 * i + 1]; fa[i] = m[6 * i + 2]; bn[i] = m[6 * i + 3]; bs[i] = m[6 * i + 4]; rho[i] = m[6 * i + 5];
+    Kn[i] = m[8 * i]; Ks[i] = m[8 * i + 1]; fa[i] = m[8 * i + 2]; bn[i] = m[8 * i + 3]; bs[i] = m[8 * i + 4]; rho[i] = m[8 * i + 5];
+    G[i] = m[8 * i + 6]; nu[i] = m[8 * i + 7];
   }
+  if (h.contactModel != SQDEM_CONTACT_LINEAR && h.contactModel != SQDEM_CONTACT_HERTZ_MINDLIN)
+    return fail(c, SQDEM_ERR_ARG, "corrupt snapshot header");
   c->haveMats = false;
   sqdem_status s;
   if ((s = sqdem_set_materials(c, (int)h.nMats, Kn.data(), Ks.data(), fa.data(), bn.data(), bs.data(), rho.data()))) return s;
+  if ((s = sqdem_set_material_moduli(c, (int)h.nMats, G.data(), nu.data()))) return s;
   if ((s = sqdem_set_params(c, &P))) return s;
-  c->recordFull = h.recordFull; c->lmSpread = h.lmSpread;
+  c->recordFull = h.recordFull; c->lmSpread = h.lmSpread; c->contactModel = h.contactModel;
   if ((s = sqdem_set_bodies(c, (int)N, kind.data(), s5.data(), was.data(), mat.data(), sph.data(), st.data()))) return s;
   if ((s = sqdem_put_body_state(c, st.data()))) return s;
   CK(cudaSetDevice(c->device));

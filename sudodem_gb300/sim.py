@@ -23,6 +23,7 @@ Classes, attribute names and defaults follow the reference:
   Omega / O            py/wrapper/sudodemWrapper.cpp:937-987
   Superquadrics        pkg/dem/Superquadrics.hpp:139-146
   SuperquadricsMat     pkg/dem/Superquadrics.hpp:247-264
+  SuperquadricsMat2    pkg/dem/Superquadrics.hpp:266-277
   Wall                 pkg/common/Wall.hpp:11-13
   InsertionSortCollider pkg/common/InsertionSortCollider.hpp:212-222
   NewtonIntegrator     pkg/dem/NewtonIntegrator.hpp:70-89
@@ -33,6 +34,13 @@ host between timesteps.  ``Ip2_FrictMat_FrictMat_FrictPhys`` and
 ``Law2_ScGeom_FrictPhys_CundallStrack`` are accepted as aliases of the superquadric
 physics and law (FrictMat.young is read as the normal stiffness Kn and FrictMat.poisson as
 Ks/Kn, the reading the ElastMat docstring gives, pkg/common/ElastMat.hpp:9).
+
+The Hertz-Mindlin functor set -- Ig2_Wall_Superquadrics_SuperquadricsGeom2,
+Ig2_Superquadrics_Superquadrics_SuperquadricsGeom2,
+Ip2_SuperquadricsMat2_SuperquadricsMat2_HertzMindlinPhys and SuperquadricsLaw2 with
+SuperquadricsMat2 materials -- selects the Nelder-Mead geometry and the Hertz-Mindlin law
+(pkg/dem/Superquadrics_Ig2.cpp:2322-2700, pkg/dem/Superquadrics.cpp:1118-1557).  A plain
+SuperquadricsMat under that set reads as SuperquadricsMat2 with the default G and nu.
 """
 import math
 import random as _random
@@ -48,7 +56,9 @@ __all__ = ["O", "Omega", "utils", "Body", "State", "Superquadrics", "Wall", "Sup
            "Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys", "SuperquadricsLaw",
            "Ip2_FrictMat_FrictMat_FrictPhys", "Law2_ScGeom_FrictPhys_CundallStrack", "NewtonIntegrator",
            "PyRunner", "CompressionEngine", "unbalancedForce", "getStress", "Cell", "NewSuperquadrics", "NewSuperquadrics2", "NewSuperquadrics_rot", "NewSuperquadrics_rot2",
-           "Vector3", "Quaternion"]
+           "Vector3", "Quaternion", "SuperquadricsMat2", "Ig2_Superquadrics_Superquadrics_SuperquadricsGeom2",
+           "Ig2_Wall_Superquadrics_SuperquadricsGeom2", "Ip2_SuperquadricsMat2_SuperquadricsMat2_HertzMindlinPhys",
+           "SuperquadricsLaw2"]
 
 
 def Vector3(x=0.0, y=0.0, z=0.0):
@@ -83,6 +93,11 @@ class _Attr:
 class SuperquadricsMat(_Attr):
     _defaults = {"Kn": 1e8, "Ks": 1e5, "frictionAngle": 0.5, "betan": 0.0, "betas": 0.0, "density": 1000.0,
                  "IsSplitable": False, "strength": 100.0}
+
+
+class SuperquadricsMat2(SuperquadricsMat):
+    """SuperquadricsMat with the shear modulus G and Poisson's ratio nu of the Hertz-Mindlin model."""
+    _defaults = dict(SuperquadricsMat._defaults, G=29e9, nu=0.15)
 
 
 class FrictMat(_Attr):
@@ -230,6 +245,28 @@ class Ip2_FrictMat_FrictMat_FrictPhys(Ip2_SuperquadricsMat_SuperquadricsMat_Supe
 
 class Law2_ScGeom_FrictPhys_CundallStrack(SuperquadricsLaw):
     """Alias with SuperquadricsLaw arithmetic (see the module docstring)."""
+
+
+class Ig2_Superquadrics_Superquadrics_SuperquadricsGeom2(_Attr):
+    pass
+
+
+class Ig2_Wall_Superquadrics_SuperquadricsGeom2(_Attr):
+    pass
+
+
+class Ip2_SuperquadricsMat2_SuperquadricsMat2_HertzMindlinPhys(_Attr):
+    pass
+
+
+class SuperquadricsLaw2(_Attr):
+    pass
+
+
+_LINEAR_SET = (Ig2_Superquadrics_Superquadrics_SuperquadricsGeom, Ig2_Wall_Superquadrics_SuperquadricsGeom,
+               Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys, SuperquadricsLaw)
+_HM_SET = (Ig2_Superquadrics_Superquadrics_SuperquadricsGeom2, Ig2_Wall_Superquadrics_SuperquadricsGeom2,
+           Ip2_SuperquadricsMat2_SuperquadricsMat2_HertzMindlinPhys, SuperquadricsLaw2)
 
 
 class InteractionLoop(_Attr):
@@ -381,6 +418,10 @@ class Interaction:
         p = _Phys()
         p.kn, p.ks, p.tangensOfFrictionAngle = rec[23], rec[24], rec[25]
         p.normalForce, p.shearForce = rec[26:29].copy(), rec[29:32].copy()
+        # SuperquadricsGeom2 fields (zero under the linear model)
+        g.curvatures1, g.curvatures2 = rec[47:49].copy(), rec[49:51].copy()
+        g.curvatureAngle, g.alpha, g.K, g.E = rec[51], rec[52], rec[53], rec[54]
+        g.curvatures_sum, g.isSphere = rec[55], bool(rec[56])
         self.geom = g if bool(rec[3]) else None
         self.phys = p if self._real else None
 
@@ -549,16 +590,15 @@ class Omega:
         self._servo = servo
         if col is None or ilp is None or newton is None:
             raise RuntimeError("O.engines must contain InsertionSortCollider, InteractionLoop and NewtonIntegrator")
-        for g in ilp.geomDispatcher:
-            if not isinstance(g, (Ig2_Superquadrics_Superquadrics_SuperquadricsGeom,
-                                  Ig2_Wall_Superquadrics_SuperquadricsGeom)):
-                raise NotImplementedError(f"geometry functor {type(g).__name__} is not available on the GPU path")
-        for p in ilp.physDispatcher:
-            if not isinstance(p, Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys):
-                raise NotImplementedError(f"physics functor {type(p).__name__} is not available on the GPU path")
-        for lw in ilp.lawDispatcher:
-            if not isinstance(lw, SuperquadricsLaw):
-                raise NotImplementedError(f"law functor {type(lw).__name__} is not available on the GPU path")
+        functors = list(ilp.geomDispatcher) + list(ilp.physDispatcher) + list(ilp.lawDispatcher)
+        for f in functors:
+            if not isinstance(f, _LINEAR_SET + _HM_SET):
+                raise NotImplementedError(f"functor {type(f).__name__} is not available on the GPU path")
+        hm = [isinstance(f, _HM_SET) for f in functors]
+        if any(hm) and not all(hm):
+            raise NotImplementedError("the InteractionLoop mixes the linear (SuperquadricsGeom/Phys/Law) and the "
+                                      "Hertz-Mindlin (SuperquadricsGeom2/HertzMindlinPhys/Law2) functor sets")
+        self._contactModel = "hertz_mindlin" if functors and all(hm) else "linear"
         return col, ilp, newton, runners
 
     # state exchange --------------------------------------------------------------------------
@@ -635,6 +675,9 @@ class Omega:
         eng = _native.Engine(device=self.device, precision=prec)
         eng.set_materials([m.Kn for m in mats], [m.Ks for m in mats], [m.frictionAngle for m in mats],
                           [m.betan for m in mats], [m.betas for m in mats], [m.density for m in mats])
+        d2 = SuperquadricsMat2._defaults
+        eng.set_material_moduli([getattr(m, "G", d2["G"]) for m in mats], [getattr(m, "nu", d2["nu"]) for m in mats])
+        eng.set_contact_model(self._contactModel)
         self._set_params(eng, col, newton)
         eng.set_bodies(kind, shape5, was, mat, sph, st)
         if self.periodic:

@@ -198,3 +198,56 @@ def test_consolidation_script_matches_engine(gpu):
     mean, dev = triax.getStress()
     assert np.isfinite(mean) and np.isfinite(dev)
     O.reset()
+
+
+def use_hertz_mindlin(O, G=2e8, nu=0.3):
+    """Switch an example scene to the Hertz-Mindlin functor set and SuperquadricsMat2."""
+    m = O.materials[0]
+    m2 = sim.SuperquadricsMat2(label=m.label, Kn=m.Kn, Ks=m.Ks, frictionAngle=m.frictionAngle, density=m.density,
+                               G=G, nu=nu)
+    O.materials[0] = m2
+    for b in O.bodies:
+        b.mat = m2
+    ilp = O.engines[2]
+    ilp.geomDispatcher = [sim.Ig2_Wall_Superquadrics_SuperquadricsGeom2(),
+                          sim.Ig2_Superquadrics_Superquadrics_SuperquadricsGeom2()]
+    ilp.physDispatcher = [sim.Ip2_SuperquadricsMat2_SuperquadricsMat2_HertzMindlinPhys()]
+    ilp.lawDispatcher = [sim.SuperquadricsLaw2()]
+    return m2
+
+
+def test_hertz_mindlin_functor_set():
+    assert sim.SuperquadricsMat2().G == 29e9 and sim.SuperquadricsMat2().nu == 0.15   # Superquadrics.hpp:270-271
+    O = sim.Omega()
+    build_example(O, n=4)
+    O._parse_engines()
+    assert O._contactModel == "linear"
+    use_hertz_mindlin(O)
+    O._parse_engines()
+    assert O._contactModel == "hertz_mindlin"
+    O.engines[2].lawDispatcher = [sim.SuperquadricsLaw()]
+    with pytest.raises(NotImplementedError):
+        O._parse_engines()
+
+
+@pytest.mark.gpu
+def test_hertz_mindlin_script_matches_engine(gpu):
+    O = sim.Omega()
+    build_example(O, n=8)
+    m2 = use_hertz_mindlin(O)
+    O.run(300, True)
+    assert O._engine.contact_model() == "hertz_mindlin"
+    O2 = sim.Omega()
+    build_example(O2, n=8)
+    m = O2._material_table()[0]
+    kind, shape5, was, mat, sph, st, _ = O2._body_arrays()
+    from sudodem_gb300 import Engine
+    e = Engine(device=0)
+    e.set_materials([m.Kn], [m.Ks], [m.frictionAngle], [m.betan], [m.betas], [m.density])
+    e.set_material_moduli([m2.G], [m2.nu])
+    e.set_contact_model("hertz_mindlin")
+    e.set_params(dt=1e-6, gravity=(0, 0, -9.81), damping=0.3, verletDist=2e-4)
+    e.set_bodies(kind, shape5, was, mat, sph, st)
+    e.step(300)
+    e.sync()
+    assert np.array_equal(e.body_state()[:, 0:3], np.array([b.state.pos for b in O.bodies]))
