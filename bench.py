@@ -58,6 +58,15 @@ def workload_spec(name, seed):
                                          eps_range=(0.3, 1.8))
     if name == "sq1k_config0":
         return assemblies.config0(seed=seed)
+    if name in ("hm200k_dense", "hm20k_dense"):
+        # Hertz-Mindlin contact model (SuperquadricsGeom2 Nelder-Mead geometry, HertzMindlinPhys,
+        # SuperquadricsLaw2): superellipsoids with half-axes U[0.8,1.2] mm, eps U[0.5,1.5] on a
+        # 2.1 mm lattice in a walled box (most neighbours start in contact), SuperquadricsMat2
+        # G = 1 MPa, nu = 0.3; walls keep the linear Kn = 1e5 N/m
+        n, box, per = (200_000, 0.2, 94) if name == "hm200k_dense" else (20_000, 0.095, 44)
+        return assemblies.hertz_mindlin(
+            assemblies.walled_lattice(n, seed=seed, box=box, per_side=per, spacing=2.1e-3, eps_range=(0.5, 1.5)),
+            G=1e6, nu=0.3)
     if name.startswith("sq") and name.endswith("_walled"):
         n = int(float(name[2:-7].replace("k", "e3").replace("m", "e6")))
         return assemblies.deposition_box(n, seed=seed, eps_range=(0.3, 1.8))
@@ -347,6 +356,9 @@ def run_ours(args):
     rep = eng.sync()
     clk = clocks.stop()
     launches = eng.launch_count() - l0
+    if spec.info.get("contact_model") == "hertz_mindlin" and rep["nan_forces"]:
+        # SuperquadricsLaw2 stops the run after a NaN force (later steps do nothing)
+        raise SystemExit("the run stopped on a NaN contact force: timing invalid")
     if dist:
         import torch
         t = torch.tensor([ms], device="cuda")
@@ -371,7 +383,9 @@ def run_ours(args):
                 "traffic": (tpp * nentries) if tpp else None,
                 "algorithmic_bytes": alg_bytes, "launch_ms": contacts_ms,
                 "stage_ms_per_step": {"collider": st[0] / k2, "contacts": st[1] / k2, "integrate": st[2] / k2},
-                "note": "FP64-issue bound on GB300 (transcendental-heavy LM narrowphase); HBM fraction stated for the contact kernel"}
+                "note": ("FP64-issue bound on GB300 (transcendental-heavy " +
+                         ("Nelder-Mead" if spec.info.get("contact_model") == "hertz_mindlin" else "LM") +
+                         " narrowphase); HBM fraction stated for the contact kernel")}
     # end to end through the C ABI with pinned host buffers
     import torch
     kin = eng.kinematics()
@@ -392,6 +406,7 @@ def run_ours(args):
                 "data": "synthetic",
                 "config": {"workload": args.workload, "particles": npart, "bodies": spec.n_bodies,
                            "table_entries": nentries, "precision": args.precision, "parallelism": "replicas",
+                           "contact_model": spec.info.get("contact_model", "linear"),
                            "lm_spread": not args.no_lm_spread,
                            "l2": f"inputs larger than L2: contact table {nentries} entries x >= 256 B"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,

@@ -242,4 +242,52 @@ __device__ __forceinline__ bool nmConsume(NMState& M, double f, bool apart) {
   }
 }
 
+// amotry's trial point for the factor fac from the vertex sum ps and the high vertex ph
+__device__ __forceinline__ double2 nmTryPoint(const double ps[2], const double ph[2], double fac) {
+  const double fac1 = (1.0 - fac) / 2.0;
+  const double fac2 = fac1 - fac;
+  return make_double2(ps[0] * fac1 - ph[0] * fac2, ps[1] * fac1 - ph[1] * fac2);
+}
+
+// Points the search asks for after the one it asks for now, under the outcomes of that
+// evaluation (written to q[1..], at most S - 1 of them; returns how many points, q[0] being
+// the current one).  Every point is computed with the operations the state machine uses, so
+// one that the search later asks for matches bit for bit.  The vertex order after an
+// evaluation follows from the comparison that selects the branch (all values distinct).
+__device__ __forceinline__ int nmPlan(const NMState& M, double2* q, int S) {
+  int n = 0;
+  q[n++] = make_double2(M.q0, M.q1);
+  if (M.st == NM_V0 || M.st == NM_V1) {
+    for (int v = M.st + 1; v < 3 && n < S; v++) q[n++] = make_double2(M.p[v][0], M.p[v][1]);
+    return n;
+  }
+  const double* ph = M.p[M.ihi];
+  double psA[2];   // vertex sum once the trial point replaces the high vertex
+  psA[0] = M.psum[0] + (M.ptry[0] - ph[0]);
+  psA[1] = M.psum[1] + (M.ptry[1] - ph[1]);
+  if (M.st == NM_REFLECT) {
+    // better than the best: expansion; worse than the second highest: contraction (from the
+    // simplex with or without the trial point); in between: the next reflection, through the
+    // old second-highest vertex, now the highest
+    if (n < S) q[n++] = nmTryPoint(psA, M.ptry, 2.0);
+    if (n < S) q[n++] = nmTryPoint(psA, M.ptry, 0.5);
+    if (n < S) q[n++] = nmTryPoint(M.psum, ph, 0.5);
+    if (n < S) q[n++] = nmTryPoint(psA, M.p[M.inhi], -1.0);
+  } else if (M.st == NM_EXPAND) {
+    // the expanded vertex stays the lowest; the next reflection goes through the old
+    // second-highest vertex, with or without the expansion point in the sum
+    if (n < S) q[n++] = nmTryPoint(psA, M.p[M.inhi], -1.0);
+    if (n < S) q[n++] = nmTryPoint(M.psum, M.p[M.inhi], -1.0);
+  } else {
+    // a rejected contraction (or a shrink step) continues with the shrink towards the low vertex
+    const int from = M.st == NM_SHRINK ? M.si + 1 : 0;
+    for (int i = from; i < 3 && n < S; i++)
+      if (i != M.ilo) {
+        q[n++] = make_double2(0.5 * (M.p[i][0] + M.p[M.ilo][0]), 0.5 * (M.p[i][1] + M.p[M.ilo][1]));
+        break;
+      }
+  }
+  return n;
+}
+
 }  // namespace sqdem

@@ -94,6 +94,8 @@ struct SceneState {
   int runCollider, initSort, newtonRan, maxDispCode;
   int P, Pnew, nWW, overflowRun;
   int lmCount, lmHead;
+  int nmFin;   // Hertz-Mindlin searches that ended touching, for the finish pass
+  int nmShort; // Hertz-Mindlin searches queued from the back of the queue (expected short)
   int numReinit; long long colliderRuns;
   unsigned long long bbLo[3], bbHi[3];   // order-preserving encodings of the bbox of particle bound centres
   double org[3]; double h; int dim[3]; int nCells;
@@ -138,7 +140,7 @@ struct Dev {
   int* pCount; int* pStart; int* pFill; int* pList;
   int* wCount; int* wList; int* wBlk;
   int2* ww;
-  int* lmQueue;
+  int* lmQueue; int qCap;   // work queue of the contact searches and its capacity
   // grid
   int* bodyCell; int* cellCount; int* cellStart; int* cellFill; int* cellBodies;
   float4* cellBox;   // per cell slot: bound centre (xyz) and, in the next entry, half extents (xyz)
@@ -267,7 +269,7 @@ __global__ void k_scan_apply(const int* __restrict__ in, int n, const int* __res
 __global__ void k_gate(Dev d) {
   SceneState& S = *d.S;
   S.skip = (S.haltAt >= 0 && S.iter >= S.haltAt) ? 1 : 0;
-  if (S.skip) { S.runCollider = 0; S.lmCount = 0; S.lmHead = 0; return; }
+  if (S.skip) { S.runCollider = 0; S.lmCount = 0; S.lmHead = 0; S.nmFin = 0; S.nmShort = 0; return; }
   if (S.newtonRan) {
     const double code = S.maxDispCode == 2 ? 2.0 : (S.maxDispCode == 1 ? 0.5 : 0.0);
     S.maxVelocitySq = fmax_ref(S.cellTerm, code);
@@ -296,7 +298,7 @@ __global__ void k_gate(Dev d) {
     else run = 0;
   }
   S.runCollider = run;
-  S.lmCount = 0; S.lmHead = 0;
+  S.lmCount = 0; S.lmHead = 0; S.nmFin = 0; S.nmShort = 0;
   if (run) {
     int init = 0;
     if (S.doSort) { init = 1; S.doSort = 0; }
@@ -1270,6 +1272,43 @@ __device__ bool screenSeparated(const BodyView& b1, const BodyView& b2, double p
   return sep > SCREEN_MARGIN * (float)(b1.shpA.w + b2.shpA.w);
 }
 
+// The same screen for the Nelder-Mead search of the Hertz-Mindlin geometry over the three
+// vertices of its first simplex, in the order the search evaluates them
+// (Superquadrics_Ig2.cpp:1724-1739).  Along the direction of each vertex (angles in the
+// CRotationMat frame) the FP32 gap c.(p2 - p1) is compared with +-SCREEN_MARGIN of the summed
+// bounding radii: when the vertices before vertex k are clearly not separating and vertex k
+// clearly is, the FP64 search ends at its k-th evaluation with the particles apart and returns
+// the first vertex.  Returns that evaluation count (1-3), or 0 when the FP64 search must run.
+// The frame is computed in FP64 (a few square roots), the support points in FP32.
+__device__ int screenSeparatedNM(const BodyView& b1, const BodyView& b2, double pa0, double pa1, double del) {
+  if (!isfinite(pa0) || !isfinite(pa1)) return 0;
+  const D3 rel = b2.pos - b1.pos;   // unshifted positions, as the Hertz-Mindlin geometry
+  const Rot gc = cRotationMat(b1.pos, b2.pos);
+  SqShapeF A, B;
+  shapeInitF(A, b1.shpA.x, b1.shpA.y, b1.shpA.z, b1.shpB.x, b1.shpB.y, quatToRot(b1.ori.x, b1.ori.y, b1.ori.z, b1.ori.w),
+             d3(0, 0, 0));
+  shapeInitF(B, b2.shpA.x, b2.shpA.y, b2.shpA.z, b2.shpB.x, b2.shpB.y, quatToRot(b2.ori.x, b2.ori.y, b2.ori.z, b2.ori.w),
+             rel);
+  float g[9];
+  for (int k = 0; k < 9; k++) g[k] = (float)gc.m[k];
+  const float margin = SCREEN_MARGIN * (float)(b1.shpA.w + b2.shpA.w);
+  for (int k = 0; k < 3; k++) {
+    const double q0 = k == 1 ? pa0 + del : pa0, q1 = k == 2 ? pa1 + del : pa1;
+    float s0, c0, s1, c1;
+    sincosf((float)q0, &s0, &c0);
+    sincosf((float)q1, &s1, &c1);
+    const F3 l = f3(c0 * c1, s0 * c1, s1);
+    const F3 c = f3(g[0] * l.x + (g[1] * l.y + g[2] * l.z), g[3] * l.x + (g[4] * l.y + g[5] * l.z),
+                    g[6] * l.x + (g[7] * l.y + g[8] * l.z));
+    const F3 p1 = supportF(A, c);
+    const F3 p2 = supportF(B, f3(-c.x, -c.y, -c.z));
+    const float sep = dotf(c, f3(p2.x - p1.x, p2.y - p1.y, p2.z - p1.z));
+    if (sep > margin) return k + 1;
+    if (!(sep < -margin)) return 0;
+  }
+  return 0;
+}
+
 // Pass 1 over the table: every entry that needs no Levenberg-Marquardt iteration is finished
 // here (bound-separated pairs, wall contacts, sphere pairs, bounding-sphere rejections, pairs the
 // FP32 screen proves separated at the LM start point); the rest is queued for k_contacts_lm.
@@ -1282,7 +1321,7 @@ __global__ void __launch_bounds__(128) k_contacts_pre(Dev d) {
   const int stride = gridDim.x * blockDim.x;
   for (int e0 = blockIdx.x * blockDim.x; e0 < Pn; e0 += stride) {
     const int e = e0 + threadIdx.x;
-    bool queue = false;
+    bool queue = false, shortq = false;
     if (e < Pn) {
       unsigned fl = d.A.flags[e];
       int id1, id2;
@@ -1311,9 +1350,18 @@ __global__ void __launch_bounds__(128) k_contacts_pre(Dev d) {
         if (b1.info.x == KIND_WALL) geomWallSq(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt);
         else if (d.prm->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN) {
           const bool sph = (b1.info.z != 0) && (b2.info.z != 0);
-          if (sph || nrm(b1.pos - b2.pos) > b1.shpA.w + b2.shpA.w)
+          if (sph || nrm(b1.pos - b2.pos) > b1.shpA.w + b2.shpA.w) {
             geomSqSq2Simple(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt, shift2);
-          else done = false;
+          } else {
+            const double2 an = isNew ? make_double2(0, 0) : d.A.angle[e];
+            const int nev = screenSeparatedNM(b1, b2, an.x, an.y, isNew ? 0.1 : 0.001);
+            if (nev) {
+              g.precomputed = false; g.nanNormal = false; g.lmIters = nev; g.lmStop = 0; g.lmCalls = 1; g.hm = 0;
+              g.cp = oldCp; g.depth = 0; g.isShearNew = true;
+              g.ang0 = an.x; g.ang1 = an.y; g.angSet = true;
+              cnt.lmCalls++; cnt.lmIters += nev;
+            } else done = false;
+          }
         } else {
           const bool sph = (b1.info.z != 0) && (b2.info.z != 0);
           if (!sph && !(nrm(b1.pos - (b2.pos + shift2)) > b1.shpA.w + b2.shpA.w)) {
@@ -1329,17 +1377,32 @@ __global__ void __launch_bounds__(128) k_contacts_pre(Dev d) {
           } else geomSqSqSimple(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt, shift2);
         }
         if (done) finishEntry(d, e, fl, isNew, id1, b1, b2, g, cnt);
-        else queue = true;
+        else {
+          queue = true;
+          // Nelder-Mead searches expected short (a contact touching at the previous step: the
+          // warm start usually converges on its first simplex) go to the back of the queue, so
+          // that the long ones (new or re-touching contacts) start first
+          shortq = d.prm->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN && !isNew && prevDepth > 0;
+        }
       }
     }
-    // warp-aggregated append to the LM queue
-    const unsigned m = __ballot_sync(0xffffffffu, queue);
+    // warp-aggregated appends to the queue: front (lmCount) and back (nmShort)
+    const int lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(0xffffffffu, queue && !shortq);
     if (m) {
-      const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+      const int leader = __ffs(m) - 1;
       int base = 0;
       if (lane == leader) base = atomicAdd(&d.S->lmCount, __popc(m));
       base = __shfl_sync(0xffffffffu, base, leader);
-      if (queue) d.lmQueue[base + __popc(m & ((1u << lane) - 1))] = e;
+      if (queue && !shortq) d.lmQueue[base + __popc(m & ((1u << lane) - 1))] = e;
+    }
+    const unsigned ms = __ballot_sync(0xffffffffu, shortq);
+    if (ms) {
+      const int leader = __ffs(ms) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&d.S->nmShort, __popc(ms));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (shortq) d.lmQueue[d.qCap - 1 - (base + __popc(ms & ((1u << lane) - 1)))] = e;
     }
   }
   flushCounters(d, cnt);
@@ -1579,7 +1642,7 @@ __device__ __forceinline__ bool lmCallEnd(const Dev& d, LMLane& L, const SqShape
 // measured slower: one more pow on the chain.)
 static const int COOP_LANES = 6, COOP_POINTS = 5;
 __device__ __forceinline__ void coopEval(const SqShape& A, const SqShape& B, double q0, double q1, int g0, int sub,
-                                         D3& p1, D3& p2, bool& flag) {
+                                         D3& p1, D3& p2, bool& flag, const Rot* G = nullptr, double* dist = nullptr) {
   const unsigned FULL = 0xffffffffu;
   const int body = sub >= 3 ? 1 : 0;
   const int k = sub - 3 * body;
@@ -1589,7 +1652,7 @@ __device__ __forceinline__ void coopEval(const SqShape& A, const SqShape& B, dou
   sincos(sub == 1 ? q1 : q0, &sv, &cv);
   const double sa0 = __shfl_sync(FULL, sv, g0), ca0 = __shfl_sync(FULL, cv, g0);
   const double sa1 = __shfl_sync(FULL, sv, g0 + 1), ca1 = __shfl_sync(FULL, cv, g0 + 1);
-  const D3 contact = d3(ca0 * ca1, sa0 * ca1, sa1);
+  const D3 contact = G ? mulG(*G, d3(ca0 * ca1, sa0 * ca1, sa1)) : d3(ca0 * ca1, sa0 * ca1, sa1);
   D3 n = mulL(s.R, contact);
   if (body) n = (-1.0) * n;
   const double v1 = pow(k == 0 ? fabs(s.ry * n.y) : fabs(s.rx * n.x), k == 2 ? s.i2 : s.i1);
@@ -1615,6 +1678,7 @@ __device__ __forceinline__ void coopEval(const SqShape& A, const SqShape& B, dou
   p2 = d3(x2, y2, z2);
   const D3 dd = p2 - p1;
   flag = dot(contact, dd) > 0;
+  if (dist) *dist = nrm(dd);
 }
 
 // Slot allocation of one evaluation round: every searching lane (in) gets one slot, the rest
@@ -1785,65 +1849,104 @@ struct NMLane {
   unsigned rounds;
 };
 
-// End of Ig2_Superquadrics_Superquadrics_SuperquadricsGeom2::go after the search
-// (Superquadrics_Ig2.cpp:2431-2516), then Ip2 + Law2.
-__device__ void nmFinish(const Dev& d, const NMLane& L, const SqShape& A, const SqShape& B, const Rot& gc,
-                         Counters& cnt) {
-  const SceneState& S = *d.S;
-  const int e = L.e;
+// End of Ig2_Superquadrics_Superquadrics_SuperquadricsGeom2::go after a search that found the
+// particles apart (Superquadrics_Ig2.cpp:2392-2397): contactAngle = the returned vertex, no
+// contact; then Ip2 + Law2.
+__device__ void nmFinishApart(const Dev& d, int e, double r0, double r1, int nfunc, Counters& cnt) {
   const unsigned fl = d.A.flags[e];
   int id1, id2;
   entryIds(d, e, fl, id1, id2);
   const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
+  const bool isNew = !(fl & F_GEOM);
   GeomOut g;
-  g.lmCalls = 1; g.lmIters = L.M.nfunc; g.lmStop = 0; g.nanNormal = false; g.hm = 0;
-  g.isShearNew = L.isNew ? true : (d.A.depth[e] <= 0);
-  g.cp = L.isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
-  g.ang0 = L.M.r0; g.ang1 = L.M.r1; g.angSet = true;
-  if (!L.M.touching) {
-    g.precomputed = false; g.depth = 0; g.isShearNew = true;
-  } else {
-    D3 contactNormal = L.P1 - L.P2;
-    normalize(contactNormal);
-    g.p1 = L.P1; g.p2 = L.P2;
-    g.cp = 0.5 * (L.P1 + L.P2);
-    g.depth = L.M.dist;
-    double sa0, ca0, sa1, ca1;
-    sincos(L.M.r0, &sa0, &ca0);
-    sincos(L.M.r1, &sa1, &ca1);
-    const D3 contact = mulG(gc, d3(ca0 * sa1, sa0 * sa1, ca1));
-    const D3 contact1 = mulL(A.R, contact), contact2 = mulL(B.R, contact);
-    D3 dmax1, dmin1, dmax2, dmin2;
-    bool f1, f2;
-    double c1[2], c2[2], ph0, ph1;
-    normal2Phi(A, contact1, ph0, ph1);
-    curvatures(A, ph0, ph1, dmax1, dmin1, f1, c1);
-    normal2Phi(B, (-1.0) * contact2, ph0, ph1);
-    curvatures(B, ph0, ph1, dmax2, dmin2, f2, c2);
-    const D3 cd1 = (f1 && f2) ? dmax1 : dmin1, cd2 = (f1 && f2) ? dmax2 : dmin2;
-    const D3 nd = contactNormal;
-    const D3 dir1 = d3(cd1.x * nd.x, cd1.y * nd.y, cd1.z * nd.z) - cd1;
-    const D3 dir2 = d3(cd2.x * nd.x, cd2.y * nd.y, cd2.z * nd.z) - cd2;
-    double angle = acos(dot(dir1, dir2) / (nrm(dir1) * nrm(dir2)));
-    if (isnan(angle)) angle = 0.0;
-    g.hm = 2;
-    g.hc[0] = c1[0]; g.hc[1] = c1[1]; g.hc[2] = c2[0]; g.hc[3] = c2[1]; g.hAng = angle;
-    g.hEll = hertzMindlin(c1, c2, angle);
-    const D3 oldNormal = L.isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
-    g.precomputed = true;
-    precomputeD(g, oldNormal, b1, b2, d.prm->dt, contactNormal, g.isShearNew, cellShift(S, d.A.cd[e]));
-    g.normal = contactNormal;
+  g.lmCalls = 1; g.lmIters = nfunc; g.lmStop = 0; g.nanNormal = false; g.hm = 0;
+  g.cp = isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
+  g.ang0 = r0; g.ang1 = r1; g.angSet = true;
+  g.precomputed = false; g.depth = 0; g.isShearNew = true;
+  cnt.lmCalls += 1; cnt.lmIters += nfunc;
+  finishEntry(d, e, fl, isNew, id1, b1, b2, g, cnt);
+}
+
+// Pass 3 of the Hertz-Mindlin model: the end of
+// Ig2_Superquadrics_Superquadrics_SuperquadricsGeom2::go for every search that ended touching
+// (Superquadrics_Ig2.cpp:2398-2516): normal and depth from the last evaluation's support
+// points, principal curvatures of both surfaces at the returned direction, the contact
+// ellipse; then Ip2 + Law2.  One thread per contact.  The searches leave their results in the
+// merge buffer of the collider (free until the next collider pass): owner = entry,
+// flags = evaluations, angle = returned vertex, depth = distance, p1/p2 = support points.
+__global__ void __launch_bounds__(128) k_contacts_nm_finish(Dev d) {
+  const SceneState& S = *d.S;
+  if (S.skip) return;
+  const int n = S.nmFin;
+  Counters cnt = {0, 0, 0, 0, 0};
+  for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+    const int i = i0 + threadIdx.x;
+    if (i < n) {
+      const int e = d.B.owner[i];
+      const int nfunc = (int)d.B.flags[i];
+      const double2 r = d.B.angle[i];
+      const double dist = d.B.depth[i];
+      const D3 P1 = xyz(d.B.p1[i]), P2 = xyz(d.B.p2[i]);
+      const unsigned fl = d.A.flags[e];
+      int id1, id2;
+      entryIds(d, e, fl, id1, id2);
+      const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
+      const bool isNew = !(fl & F_GEOM);
+      SqShape A, B;
+      makeShape(A, b1);
+      makeShape(B, b2);
+      const Rot gc = cRotationMat(b1.pos, b2.pos);
+      GeomOut g;
+      g.lmCalls = 1; g.lmIters = nfunc; g.lmStop = 0; g.nanNormal = false;
+      g.isShearNew = isNew ? true : (d.A.depth[e] <= 0);
+      g.ang0 = r.x; g.ang1 = r.y; g.angSet = true;
+      D3 contactNormal = P1 - P2;
+      normalize(contactNormal);
+      g.p1 = P1; g.p2 = P2;
+      g.cp = 0.5 * (P1 + P2);
+      g.depth = dist;
+      double sa0, ca0, sa1, ca1;
+      sincos(r.x, &sa0, &ca0);
+      sincos(r.y, &sa1, &ca1);
+      const D3 contact = mulG(gc, d3(ca0 * sa1, sa0 * sa1, ca1));
+      const D3 contact1 = mulL(A.R, contact), contact2 = mulL(B.R, contact);
+      D3 dmax1 = d3(0, 0, 0), dmin1, dmax2 = d3(0, 0, 0), dmin2;
+      bool f1, f2;
+      double c1[2], c2[2], ph0, ph1;
+      normal2Phi(A, contact1, ph0, ph1);
+      curvatures(A, ph0, ph1, dmax1, dmin1, f1, c1);
+      normal2Phi(B, (-1.0) * contact2, ph0, ph1);
+      curvatures(B, ph0, ph1, dmax2, dmin2, f2, c2);
+      const D3 cd1 = (f1 && f2) ? dmax1 : dmin1, cd2 = (f1 && f2) ? dmax2 : dmin2;
+      const D3 nd = contactNormal;
+      const D3 dir1 = d3(cd1.x * nd.x, cd1.y * nd.y, cd1.z * nd.z) - cd1;
+      const D3 dir2 = d3(cd2.x * nd.x, cd2.y * nd.y, cd2.z * nd.z) - cd2;
+      double angle = acos(dot(dir1, dir2) / (nrm(dir1) * nrm(dir2)));
+      if (isnan(angle)) angle = 0.0;
+      g.hm = 2;
+      g.hc[0] = c1[0]; g.hc[1] = c1[1]; g.hc[2] = c2[0]; g.hc[3] = c2[1]; g.hAng = angle;
+      g.hEll = hertzMindlin(c1, c2, angle);
+      const D3 oldNormal = isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
+      g.precomputed = true;
+      precomputeD(g, oldNormal, b1, b2, d.prm->dt, contactNormal, g.isShearNew, cellShift(S, d.A.cd[e]));
+      g.normal = contactNormal;
+      cnt.lmCalls += 1; cnt.lmIters += nfunc; cnt.lmMax += (nfunc >= NM_NMAX);
+      finishEntry(d, e, fl, isNew, id1, b1, b2, g, cnt);
+    }
   }
-  cnt.lmCalls += 1; cnt.lmIters += L.M.nfunc; cnt.lmMax += (L.M.nfunc >= NM_NMAX);
-  finishEntry(d, e, fl, L.isNew, id1, b1, b2, g, cnt);
+  flushCounters(d, cnt);
 }
 
 __global__ void __launch_bounds__(LM_BS) k_contacts_nm(Dev d) {
   __shared__ SqShape shA[LM_BS], shB[LM_BS];
   __shared__ Rot shG[LM_BS];
+  __shared__ double2 slotQ[LM_BS];
+  __shared__ int slotOwner[LM_BS];
   const SceneState& S = *d.S;
-  const int count = S.lmCount;
+  const int nFront = S.lmCount, count = S.lmCount + S.nmShort;
   const int lane = threadIdx.x & 31;
+  const int wbase = threadIdx.x & ~31;
+  const bool spread = d.prm->lmSpread != 0;
   Counters cnt = {0, 0, 0, 0, 0};
   unsigned long long ev64 = 0;
   unsigned roundsMax = 0;
@@ -1861,7 +1964,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_nm(Dev d) {
         if (idx < count) {
           SqShape& A = shA[threadIdx.x];
           SqShape& B = shB[threadIdx.x];
-          L.e = d.lmQueue[idx];
+          L.e = idx < nFront ? d.lmQueue[idx] : d.lmQueue[d.qCap - 1 - (idx - nFront)];
           const unsigned fl = d.A.flags[L.e];
           int id1, id2;
           entryIds(d, L.e, fl, id1, id2);
@@ -1878,17 +1981,79 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_nm(Dev d) {
         } else exhausted = true;
       }
     }
-    if (!__any_sync(0xffffffffu, active)) break;
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!act) break;
+    // One point per search while the queue has work.  Once it is drained the warp's slots
+    // (five groups of six lanes, coopEval, while at most COOP_POINTS searches run, else 32
+    // lanes) are shared out, and each search fills its share with the points nmPlan says it
+    // may ask for next.
+    const int nA = __popc(act);
+    const bool drained = spread && __any_sync(0xffffffffu, exhausted);
+    const bool coop = drained && nA <= COOP_POINTS;
+    int spc, base, jmax;
+    allocSlots(active, L.rounds, drained ? (coop ? COOP_POINTS : 32) : nA, spc, base, jmax);
+    slotOwner[threadIdx.x] = -1;
+    __syncwarp();
     if (active) {
-      bool apart;
-      const double f = disfunNM(shA[threadIdx.x], shB[threadIdx.x], shG[threadIdx.x], L.M.q0, L.M.q1, L.P1, L.P2, apart);
-      ev64++;
-      L.rounds++;
-      if (!nmConsume(L.M, f, apart)) {
-        nmFinish(d, L, shA[threadIdx.x], shB[threadIdx.x], shG[threadIdx.x], cnt);
-        active = false;
-        roundsMax = max(roundsMax, L.rounds);
+      const int n = nmPlan(L.M, &slotQ[wbase + base], spc);
+      for (int i = 0; i < n; i++) slotOwner[wbase + base + i] = lane;
+    }
+    __syncwarp();
+    D3 P1 = d3(0, 0, 0), P2 = d3(0, 0, 0);
+    bool flag = false;
+    double f = 0;
+    if (coop) {
+      const int graw = lane / COOP_LANES;
+      const int grp = graw < COOP_POINTS ? graw : 0;
+      const int sub = graw < COOP_POINTS ? lane - grp * COOP_LANES : lane - COOP_POINTS * COOP_LANES;
+      const int o = slotOwner[wbase + grp];
+      const bool has = graw < COOP_POINTS && o >= 0;
+      const int slot = has ? grp : 0;
+      const int src = wbase + slotOwner[wbase + slot];
+      const double2 q = slotQ[wbase + slot];
+      coopEval(shA[src], shB[src], q.x, q.y, grp * COOP_LANES, sub, P1, P2, flag, &shG[src], &f);
+      if (has && sub == 0) ev64++;
+    } else {
+      const int own = slotOwner[threadIdx.x];
+      if (own >= 0) {
+        const double2 q = slotQ[threadIdx.x];
+        f = disfunNM(shA[wbase + own], shB[wbase + own], shG[wbase + own], q.x, q.y, P1, P2, flag);
+        ev64++;
       }
+    }
+    if (active) L.rounds++;
+    for (int j = 0; j < jmax; j++) {
+      const int si = base + j;
+      const bool mine = j < spc;
+      const int src = mine ? (coop ? si * COOP_LANES : si) : lane;
+      const double x1 = __shfl_sync(0xffffffffu, P1.x, src), y1 = __shfl_sync(0xffffffffu, P1.y, src),
+                   z1 = __shfl_sync(0xffffffffu, P1.z, src);
+      const double x2 = __shfl_sync(0xffffffffu, P2.x, src), y2 = __shfl_sync(0xffffffffu, P2.y, src),
+                   z2 = __shfl_sync(0xffffffffu, P2.z, src);
+      const double fs = __shfl_sync(0xffffffffu, f, src);
+      const bool apart = __shfl_sync(0xffffffffu, (int)flag, src) != 0;
+      bool done = false;
+      if (mine && active && slotOwner[wbase + si] == lane && sameBits(slotQ[wbase + si], L.M.q0, L.M.q1)) {
+        L.P1 = d3(x1, y1, z1); L.P2 = d3(x2, y2, z2);
+        done = !nmConsume(L.M, fs, apart);
+      }
+      // searches that ended touching go to the finish pass (warp-aggregated append)
+      const bool fin = done && L.M.touching;
+      const unsigned m = __ballot_sync(0xffffffffu, fin);
+      if (m) {
+        const int leader = __ffs(m) - 1;
+        int b0 = 0;
+        if (lane == leader) b0 = atomicAdd(&d.S->nmFin, __popc(m));
+        b0 = __shfl_sync(0xffffffffu, b0, leader);
+        if (fin) {
+          const int i = b0 + __popc(m & ((1u << lane) - 1));
+          d.B.owner[i] = L.e; d.B.flags[i] = (unsigned)L.M.nfunc;
+          d.B.angle[i] = make_double2(L.M.r0, L.M.r1); d.B.depth[i] = L.M.dist;
+          d.B.p1[i] = dd4(L.P1, 0); d.B.p2[i] = dd4(L.P2, 0);
+        }
+      }
+      if (done && !L.M.touching) nmFinishApart(d, L.e, L.M.r0, L.M.r1, L.M.nfunc, cnt);
+      if (done) { active = false; roundsMax = max(roundsMax, L.rounds); }
     }
     __syncwarp();
   }
@@ -2714,7 +2879,7 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d) {
   (void)S;
 }
 
-__global__ void k_reset_queue(Dev d) { d.S->lmCount = 0; d.S->lmHead = 0; }
+__global__ void k_reset_queue(Dev d) { d.S->lmCount = 0; d.S->lmHead = 0; d.S->nmFin = 0; d.S->nmShort = 0; }
 
 // Start of NewtonIntegrator::action (NewtonIntegrator.cpp:107-117): pending velGrad, the
 // cell-size-change velocity that seeds maxVelocitySq, and the gradients the body update uses.
@@ -2829,6 +2994,22 @@ static void launchScan(sqdem_ctx* c, const int* in, int n, int* out, const int* 
   c->launches += 3;
 }
 
+// The contact stage on c->stream: pass 1, then the searches of the selected contact model
+// (and, for Hertz-Mindlin, the finish pass of the contacts found touching).
+static void launchContactStage(sqdem_ctx* c, const Dev& d, int grid) {
+  cudaStream_t s = c->stream;
+  k_contacts_pre<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, s>>>(d);
+  if (c->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN) {
+    k_contacts_nm<<<grid, LM_BS, 0, s>>>(d);
+    k_contacts_nm_finish<<<std::min(nblk(d.Pcap, 128), c->numSMs * 8), 128, 0, s>>>(d);
+    c->launches += 3;
+  } else {
+    if (c->precision == SQDEM_MIXED) k_contacts_lm_mixed<<<grid, LM_BS, 0, s>>>(d);
+    else k_contacts_lm<<<grid, LM_BS, 0, s>>>(d);
+    c->launches += 2;
+  }
+}
+
 // One timestep of kernels on c->stream.
 static void enqueueStep(sqdem_ctx* c, bool timed) {
   Dev& d = c->d;
@@ -2864,14 +3045,9 @@ static void enqueueStep(sqdem_ctx* c, bool timed) {
     c->launches += 2;
   }
   if (timed) cudaEventRecord(c->ev[1], s);
-  k_contacts_pre<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, s>>>(d);
   // LM grid: all resident blocks, fewer for a small table (at most one lane per 4 entries)
   const int lmFull = c->numSMs * (c->precision == SQDEM_MIXED ? c->lmBlocksPerSMmixed : c->lmBlocksPerSM);
-  const int lmGrid = std::max(1, std::min(lmFull, nblk(d.Pcap, LM_BS * 4)));
-  if (c->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN) k_contacts_nm<<<lmGrid, LM_BS, 0, s>>>(d);
-  else if (c->precision == SQDEM_MIXED) k_contacts_lm_mixed<<<lmGrid, LM_BS, 0, s>>>(d);
-  else k_contacts_lm<<<lmGrid, LM_BS, 0, s>>>(d);
-  c->launches += 2;
+  launchContactStage(c, d, std::max(1, std::min(lmFull, nblk(d.Pcap, LM_BS * 4))));
   if (timed) cudaEventRecord(c->ev[2], s);
   if (d.W > 0) { k_wall_forces<<<d.W, 128, 0, s>>>(d); c->launches++; }
   if (c->servoOn) {   // CompressionEngine between InteractionLoop and NewtonIntegrator
@@ -3135,6 +3311,7 @@ sqdem_status sqdem_set_bodies(sqdem_ctx* c, int n, const int* kind, const double
   c->servoOn = false;
   CK(dalloc(c, &d.ww, std::max(d.W * d.W, 1)));
   CK(dalloc(c, &d.lmQueue, d.Pcap));
+  d.qCap = d.Pcap;
   CK(dalloc(c, &d.bodyCell, n)); CK(dalloc(c, &d.cellCount, d.Gmax + 1)); CK(dalloc(c, &d.cellStart, d.Gmax + 1));
   CK(dalloc(c, &d.cellFill, d.Gmax + 1)); CK(dalloc(c, &d.cellBodies, n)); CK(dalloc(c, &d.cellBox, 2 * (size_t)n));
   CK(dalloc(c, &d.scanTmp, nblk((long)std::max(std::max(d.Gmax, d.Pcap), d.N) + 2, SCAN_TILE) + 2));
@@ -3596,9 +3773,7 @@ sqdem_status sqdem_time_contacts(sqdem_ctx* c, int nrep, double* ms) {
   CK(cudaEventRecord(c->ev[1], c->stream));
   for (int i = 0; i < nrep; i++) {
     k_reset_queue<<<1, 1, 0, c->stream>>>(d);
-    k_contacts_pre<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, c->stream>>>(d);
-    if (c->precision == SQDEM_MIXED) k_contacts_lm_mixed<<<c->numSMs * c->lmBlocksPerSMmixed, LM_BS, 0, c->stream>>>(d);
-    else k_contacts_lm<<<c->numSMs * c->lmBlocksPerSM, LM_BS, 0, c->stream>>>(d);
+    launchContactStage(c, d, c->numSMs * (c->precision == SQDEM_MIXED ? c->lmBlocksPerSMmixed : c->lmBlocksPerSM));
   }
   CK(cudaEventRecord(c->ev[2], c->stream));
   CK(cudaEventSynchronize(c->ev[2]));
@@ -3720,11 +3895,10 @@ sqdem_status sqdem_contacts_static_queue(sqdem_ctx* c) {
   if (st) return st;
   Dev d = c->d;
   d.lmQueue = queue;
+  d.qCap = SQDEM_STATIC_QUEUE_MAX;
   k_reset_queue<<<1, 1, 0, c->stream>>>(d);
-  k_contacts_pre<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, c->stream>>>(d);
-  if (c->precision == SQDEM_MIXED) k_contacts_lm_mixed<<<c->numSMs * c->lmBlocksPerSMmixed, LM_BS, 0, c->stream>>>(d);
-  else k_contacts_lm<<<c->numSMs * c->lmBlocksPerSM, LM_BS, 0, c->stream>>>(d);
-  c->launches += 3;
+  c->launches += 1;
+  launchContactStage(c, d, c->numSMs * (c->precision == SQDEM_MIXED ? c->lmBlocksPerSMmixed : c->lmBlocksPerSM));
   CK(cudaGetLastError());
   return SQDEM_OK;
 }

@@ -236,3 +236,20 @@ def test_gpu_deterministic_and_graph_equals_eager(gpu):
     assert np.array_equal(a.body_state(), b.body_state())
     assert np.array_equal(a.interactions(True), b.interactions(True))
     assert np.array_equal(a.body_state(), c.body_state())
+
+
+@pytest.mark.gpu
+def test_gpu_cooperative_evaluations_change_nothing(gpu):
+    """Drained warps evaluate the points the remaining searches may ask for next, with six
+    lanes per point when few remain (set_lm_spread switches that off): bitwise the same
+    results."""
+    spec = dense_hm(seed=7, n=400)
+    a, b = engine_for(spec), engine_for(spec)
+    b.set_lm_spread(False)
+    a.step(40); b.step(40)
+    ra, rb = a.sync(), b.sync()
+    assert np.array_equal(a.body_state(), b.body_state())
+    assert np.array_equal(a.interactions(True), b.interactions(True))
+    for k in ("lm_calls", "lm_iterations", "nan_forces"):
+        assert ra[k] == rb[k], k
+    assert ra["evals_fp64"] >= rb["evals_fp64"] > 0   # speculative points evaluated in spare slots
