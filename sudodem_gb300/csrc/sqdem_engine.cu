@@ -1253,6 +1253,21 @@ __device__ __forceinline__ void entryIds(const Dev& d, int e, unsigned fl, int& 
   id2 = (fl & F_OWNER_ID1) ? partner : owner;
 }
 
+// FP32 shape of a body for the separation screens (all in FP32)
+__device__ __forceinline__ void shapeInitF32(SqShapeF& s, const BodyView& b, F3 relPos) {
+  s.rx = (float)b.shpA.x; s.ry = (float)b.shpA.y; s.rz = (float)b.shpA.z;
+  s.e1 = (float)b.shpB.x; s.e2 = (float)b.shpB.y;
+  s.a1 = 2.f - s.e1; s.i1 = 1.f / (2.f - s.e1); s.i2 = 1.f / (2.f - s.e2);
+  const float w = (float)b.ori.x, x = (float)b.ori.y, y = (float)b.ori.z, z = (float)b.ori.w;
+  const float tx = 2.f * x, ty = 2.f * y, tz = 2.f * z;
+  const float twx = tx * w, twy = ty * w, twz = tz * w, txx = tx * x, txy = ty * x, txz = tz * x;
+  const float tyy = ty * y, tyz = tz * y, tzz = tz * z;
+  s.R[0] = 1.f - (tyy + tzz); s.R[1] = txy - twz; s.R[2] = txz + twy;
+  s.R[3] = txy + twz; s.R[4] = 1.f - (txx + tzz); s.R[5] = tyz - twx;
+  s.R[6] = txz - twy; s.R[7] = tyz + twx; s.R[8] = 1.f - (txx + tyy);
+  s.px = relPos.x; s.py = relPos.y; s.pz = relPos.z;
+}
+
 // Separation screen of a superquadric pair at the point where lmder2 would start.  If one FP32
 // Disfunction evaluation there shows a support gap c.(p2 - p1) larger than SCREEN_MARGIN times
 // the summed bounding radii (FP32 error is ~1e-7 of the size), the FP64 evaluation at the same
@@ -1262,10 +1277,9 @@ static const float SCREEN_MARGIN = 1e-4f;
 __device__ bool screenSeparated(const BodyView& b1, const BodyView& b2, double pa0, double pa1, D3 shift2) {
   if (!isfinite(pa0) || !isfinite(pa1)) return false;
   SqShapeF A, B;
-  shapeInitF(A, b1.shpA.x, b1.shpA.y, b1.shpA.z, b1.shpB.x, b1.shpB.y, quatToRot(b1.ori.x, b1.ori.y, b1.ori.z, b1.ori.w),
-             d3(0, 0, 0));
-  shapeInitF(B, b2.shpA.x, b2.shpA.y, b2.shpA.z, b2.shpB.x, b2.shpB.y, quatToRot(b2.ori.x, b2.ori.y, b2.ori.z, b2.ori.w),
-             (b2.pos + shift2) - b1.pos);
+  const D3 rel = (b2.pos + shift2) - b1.pos;
+  shapeInitF32(A, b1, f3(0, 0, 0));
+  shapeInitF32(B, b2, f3((float)rel.x, (float)rel.y, (float)rel.z));
   F3 p1, p2;
   float sep;
   disfunctionF(A, B, (float)pa0, (float)pa1, p1, p2, sep);
@@ -1279,18 +1293,29 @@ __device__ bool screenSeparated(const BodyView& b1, const BodyView& b2, double p
 // bounding radii: when the vertices before vertex k are clearly not separating and vertex k
 // clearly is, the FP64 search ends at its k-th evaluation with the particles apart and returns
 // the first vertex.  Returns that evaluation count (1-3), or 0 when the FP64 search must run.
-// The frame is computed in FP64 (a few square roots), the support points in FP32.
+// The frame and the support points are computed in FP32 (the frame's branch on the FP64 cosine).
 __device__ int screenSeparatedNM(const BodyView& b1, const BodyView& b2, double pa0, double pa1, double del) {
   if (!isfinite(pa0) || !isfinite(pa1)) return 0;
   const D3 rel = b2.pos - b1.pos;   // unshifted positions, as the Hertz-Mindlin geometry
-  const Rot gc = cRotationMat(b1.pos, b2.pos);
+  const F3 e = f3((float)rel.x, (float)rel.y, (float)rel.z);
   SqShapeF A, B;
-  shapeInitF(A, b1.shpA.x, b1.shpA.y, b1.shpA.z, b1.shpB.x, b1.shpB.y, quatToRot(b1.ori.x, b1.ori.y, b1.ori.z, b1.ori.w),
-             d3(0, 0, 0));
-  shapeInitF(B, b2.shpA.x, b2.shpA.y, b2.shpA.z, b2.shpB.x, b2.shpB.y, quatToRot(b2.ori.x, b2.ori.y, b2.ori.z, b2.ori.w),
-             rel);
-  float g[9];
-  for (int k = 0; k < 9; k++) g[k] = (float)gc.m[k];
+  shapeInitF32(A, b1, f3(0, 0, 0));
+  shapeInitF32(B, b2, e);
+  // CRotationMat in FP32 (x onto e: a rotation about x cross e), with the branch for e along
+  // x taken on the FP64 cosine, as the FP64 frame takes it
+  const double cphi64 = dot(d3(1., 0, 0), rel) / (nrm(d3(1., 0, 0)) * nrm(rel));
+  const float cphi = (float)cphi64;
+  const float ch = sqrtf(0.5f * (1 + cphi)), sh = sqrtf(0.5f * (1 - cphi));
+  float qw = ch, qx = 0, qy = 0, qz = sh;
+  if (!(fabs(cphi64) > 1.0 - 1e-10)) {
+    const float ny = -e.z, nz = e.y, nn = sqrtf(ny * ny + nz * nz);
+    qy = ny / nn * sh; qz = nz / nn * sh;
+  }
+  const float tx = 2.f * qx, ty = 2.f * qy, tz = 2.f * qz;
+  const float twx = tx * qw, twy = ty * qw, twz = tz * qw, txx = tx * qx, txy = ty * qx, txz = tz * qx;
+  const float tyy = ty * qy, tyz = tz * qy, tzz = tz * qz;
+  const float g[9] = {1.f - (tyy + tzz), txy - twz, txz + twy, txy + twz, 1.f - (txx + tzz), tyz - twx,
+                      txz - twy, tyz + twx, 1.f - (txx + tyy)};
   const float margin = SCREEN_MARGIN * (float)(b1.shpA.w + b2.shpA.w);
   for (int k = 0; k < 3; k++) {
     const double q0 = k == 1 ? pa0 + del : pa0, q1 = k == 2 ? pa1 + del : pa1;
@@ -1312,7 +1337,7 @@ __device__ int screenSeparatedNM(const BodyView& b1, const BodyView& b2, double 
 // Pass 1 over the table: every entry that needs no Levenberg-Marquardt iteration is finished
 // here (bound-separated pairs, wall contacts, sphere pairs, bounding-sphere rejections, pairs the
 // FP32 screen proves separated at the LM start point); the rest is queued for k_contacts_lm.
-__global__ void __launch_bounds__(128) k_contacts_pre(Dev d) {
+__global__ void __launch_bounds__(128, 3) k_contacts_pre(Dev d) {
   const SceneState& S = *d.S;
   if (S.skip) return;
   const int Pn = S.P;
@@ -2924,7 +2949,7 @@ using namespace sqdem;
 struct sqdem_ctx {
   int device = 0, precision = SQDEM_FP64, useGraph = 1, contactsPerBody = 16, maxCand = 64;
   int numSMs = 152;
-  int lmBlocksPerSM = 4, lmBlocksPerSMmixed = 4;
+  int lmBlocksPerSM = 4, lmBlocksPerSMmixed = 4, nmBlocksPerSM = 4;
   cudaStream_t stream = nullptr;
   Dev d;
   bool haveBodies = false, haveMats = false, haveParams = false;
@@ -2994,6 +3019,12 @@ static void launchScan(sqdem_ctx* c, const int* in, int n, int* out, const int* 
   c->launches += 3;
 }
 
+// Resident blocks per SM of the search kernel the context launches.
+static int searchBlocksPerSM(const sqdem_ctx* c) {
+  if (c->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN) return c->nmBlocksPerSM;
+  return c->precision == SQDEM_MIXED ? c->lmBlocksPerSMmixed : c->lmBlocksPerSM;
+}
+
 // The contact stage on c->stream: pass 1, then the searches of the selected contact model
 // (and, for Hertz-Mindlin, the finish pass of the contacts found touching).
 static void launchContactStage(sqdem_ctx* c, const Dev& d, int grid) {
@@ -3046,7 +3077,7 @@ static void enqueueStep(sqdem_ctx* c, bool timed) {
   }
   if (timed) cudaEventRecord(c->ev[1], s);
   // LM grid: all resident blocks, fewer for a small table (at most one lane per 4 entries)
-  const int lmFull = c->numSMs * (c->precision == SQDEM_MIXED ? c->lmBlocksPerSMmixed : c->lmBlocksPerSM);
+  const int lmFull = c->numSMs * searchBlocksPerSM(c);
   launchContactStage(c, d, std::max(1, std::min(lmFull, nblk(d.Pcap, LM_BS * 4))));
   if (timed) cudaEventRecord(c->ev[2], s);
   if (d.W > 0) { k_wall_forces<<<d.W, 128, 0, s>>>(d); c->launches++; }
@@ -3169,6 +3200,8 @@ sqdem_status sqdem_create(sqdem_ctx** out, const sqdem_config* cfg) {
     c->lmBlocksPerSM = nb > 0 ? nb : 1;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_contacts_lm_mixed, LM_BS, 0));
     c->lmBlocksPerSMmixed = nb > 0 ? nb : 1;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_contacts_nm, LM_BS, 0));
+    c->nmBlocksPerSM = nb > 0 ? nb : 1;
   }
   for (int i = 0; i < 4; i++) CK(cudaEventCreate(&c->ev[i]));
   std::memset(&c->d, 0, sizeof(Dev));
@@ -3773,7 +3806,7 @@ sqdem_status sqdem_time_contacts(sqdem_ctx* c, int nrep, double* ms) {
   CK(cudaEventRecord(c->ev[1], c->stream));
   for (int i = 0; i < nrep; i++) {
     k_reset_queue<<<1, 1, 0, c->stream>>>(d);
-    launchContactStage(c, d, c->numSMs * (c->precision == SQDEM_MIXED ? c->lmBlocksPerSMmixed : c->lmBlocksPerSM));
+    launchContactStage(c, d, c->numSMs * searchBlocksPerSM(c));
   }
   CK(cudaEventRecord(c->ev[2], c->stream));
   CK(cudaEventSynchronize(c->ev[2]));
@@ -3898,7 +3931,7 @@ sqdem_status sqdem_contacts_static_queue(sqdem_ctx* c) {
   d.qCap = SQDEM_STATIC_QUEUE_MAX;
   k_reset_queue<<<1, 1, 0, c->stream>>>(d);
   c->launches += 1;
-  launchContactStage(c, d, c->numSMs * (c->precision == SQDEM_MIXED ? c->lmBlocksPerSMmixed : c->lmBlocksPerSM));
+  launchContactStage(c, d, c->numSMs * searchBlocksPerSM(c));
   CK(cudaGetLastError());
   return SQDEM_OK;
 }
