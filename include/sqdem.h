@@ -145,6 +145,21 @@ sqdem_status sqdem_set_bodies(sqdem_ctx* ctx, int n, const int* kind, const doub
                               const double* state);
 sqdem_status sqdem_set_params(sqdem_ctx* ctx, const sqdem_params* p);
 
+/* Launch shapes of the contact stage: resident blocks per SM of the search kernel (at most
+ * what its occupancy allows) and grid-stride blocks per SM of the first contact pass; 0 keeps
+ * the default.  Shapes change no result, only the time. */
+sqdem_status sqdem_set_launch_shape(sqdem_ctx* ctx, int search_blocks_per_sm, int pass1_blocks_per_sm);
+typedef struct {
+  int search_blocks_per_sm, pass1_blocks_per_sm;   /* the shape chosen and set */
+  double ms_per_step;                               /* its device time per step */
+  int candidates;                                   /* shapes timed */
+} sqdem_tune;
+/* Autotuner: times each candidate shape (search blocks per SM 1..occupancy x pass-1 blocks
+ * per SM 4/8/16/32) for `steps` timesteps on the scene itself, twice, and sets the fastest.
+ * The tuning steps are ordinary timesteps (shapes change no result): the scene advances by
+ * candidates x (2 x steps + 1) steps.  No counterpart in the reference. */
+sqdem_status sqdem_autotune(sqdem_ctx* ctx, int steps, sqdem_tune* out);
+
 /* Contact model (SQDEM_CONTACT_*); takes effect at the next step, existing contacts keep
  * their state.  sqdem_contact_model returns the current one (-1 for a NULL context). */
 sqdem_status sqdem_set_contact_model(sqdem_ctx* ctx, int model);

@@ -27,6 +27,10 @@ class SqdemError(RuntimeError):
         self.status = status
 
 
+class _Tune(C.Structure):
+    _fields_ = [("search", C.c_int), ("pass1", C.c_int), ("ms", C.c_double), ("n", C.c_int)]
+
+
 class _Config(C.Structure):
     _fields_ = [("device", C.c_int), ("precision", C.c_int), ("contacts_per_body", C.c_int), ("use_graph", C.c_int)]
 
@@ -110,6 +114,7 @@ def load_library(build_if_missing=True):
         "sqdem_contacts_static_queue": (i, [v]),
         "sqdem_set_contact_model": (i, [v, i]), "sqdem_contact_model": (i, [v]), "sqdem_num_materials": (i, [v]),
         "sqdem_set_material_moduli": (i, [v, i, dp, dp]), "sqdem_get_material_moduli": (i, [v, dp, dp]),
+        "sqdem_set_launch_shape": (i, [v, i, i]), "sqdem_autotune": (i, [v, i, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -132,7 +137,7 @@ def exported_symbols():
             "sqdem_batch_size", "sqdem_batch_scene", "sqdem_batch_step", "sqdem_batch_sync", "sqdem_batch_time_steps",
             "sqdem_batch_time_e2e", "sqdem_batch_launch_count", "sqdem_snapshot", "sqdem_restore",
             "sqdem_set_contact_model", "sqdem_contact_model", "sqdem_num_materials", "sqdem_set_material_moduli",
-            "sqdem_get_material_moduli"]
+            "sqdem_get_material_moduli", "sqdem_set_launch_shape", "sqdem_autotune"]
 
 
 def _dp(a):
@@ -227,6 +232,18 @@ class Engine:
 
     def set_lm_spread(self, on=True):
         self._check(self.lib.sqdem_set_lm_spread(self.h, 1 if on else 0))
+
+    def set_launch_shape(self, search_blocks_per_sm=0, pass1_blocks_per_sm=0):
+        """Launch shapes of the contact stage (0 keeps the default); results are unchanged."""
+        self._check(self.lib.sqdem_set_launch_shape(self.h, int(search_blocks_per_sm), int(pass1_blocks_per_sm)))
+
+    def autotune(self, steps=5):
+        """Time the candidate launch shapes on this scene and keep the fastest.  The tuning
+        steps are ordinary timesteps (launch shapes change no result): the scene advances."""
+        t = _Tune()
+        self._check(self.lib.sqdem_autotune(self.h, int(steps), C.byref(t)))
+        return {"search_blocks_per_sm": t.search, "pass1_blocks_per_sm": t.pass1, "ms_per_step": t.ms,
+                "candidates": t.n}
 
     CONTACT_MODELS = {"linear": 0, "hertz_mindlin": 1}
 

@@ -2950,6 +2950,7 @@ struct sqdem_ctx {
   int device = 0, precision = SQDEM_FP64, useGraph = 1, contactsPerBody = 16, maxCand = 64;
   int numSMs = 152;
   int lmBlocksPerSM = 4, lmBlocksPerSMmixed = 4, nmBlocksPerSM = 4;
+  int shapeSearch = 0, shapePass1 = 0;   // launch shapes set by the caller or the autotuner (0: defaults)
   cudaStream_t stream = nullptr;
   Dev d;
   bool haveBodies = false, haveMats = false, haveParams = false;
@@ -3020,16 +3021,22 @@ static void launchScan(sqdem_ctx* c, const int* in, int n, int* out, const int* 
 }
 
 // Resident blocks per SM of the search kernel the context launches.
-static int searchBlocksPerSM(const sqdem_ctx* c) {
+static int maxSearchBlocksPerSM(const sqdem_ctx* c) {
   if (c->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN) return c->nmBlocksPerSM;
   return c->precision == SQDEM_MIXED ? c->lmBlocksPerSMmixed : c->lmBlocksPerSM;
 }
+static int searchBlocksPerSM(const sqdem_ctx* c) {
+  const int mx = maxSearchBlocksPerSM(c);
+  return c->shapeSearch > 0 ? std::min(c->shapeSearch, mx) : mx;
+}
+static const int PASS1_BLOCKS_PER_SM = 16;   // grid-stride blocks of pass 1 per SM (default)
 
 // The contact stage on c->stream: pass 1, then the searches of the selected contact model
 // (and, for Hertz-Mindlin, the finish pass of the contacts found touching).
 static void launchContactStage(sqdem_ctx* c, const Dev& d, int grid) {
   cudaStream_t s = c->stream;
-  k_contacts_pre<<<std::min(nblk(d.Pcap, 128), c->numSMs * 16), 128, 0, s>>>(d);
+  const int p1 = c->shapePass1 > 0 ? c->shapePass1 : PASS1_BLOCKS_PER_SM;
+  k_contacts_pre<<<std::min(nblk(d.Pcap, 128), c->numSMs * p1), 128, 0, s>>>(d);
   if (c->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN) {
     k_contacts_nm<<<grid, LM_BS, 0, s>>>(d);
     k_contacts_nm_finish<<<std::min(nblk(d.Pcap, 128), c->numSMs * 8), 128, 0, s>>>(d);
@@ -3956,6 +3963,48 @@ sqdem_status sqdem_set_lm_spread(sqdem_ctx* c, int on) {
   if (!c) return SQDEM_ERR_ARG;
   c->lmSpread = on ? 1 : 0;
   if (c->haveBodies) { sqdem_status s = uploadParams(c); if (s) return s; CK(cudaStreamSynchronize(c->stream)); }
+  return SQDEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Launch shapes of the contact stage and their autotuner.  The shapes change no result (each
+// search is a per-contact computation taken from a shared queue; forces are gathered in table
+// order), only the time.
+sqdem_status sqdem_set_launch_shape(sqdem_ctx* c, int search_blocks_per_sm, int pass1_blocks_per_sm) {
+  if (!c || search_blocks_per_sm < 0 || pass1_blocks_per_sm < 0 || pass1_blocks_per_sm > 64) return SQDEM_ERR_ARG;
+  if (search_blocks_per_sm != c->shapeSearch || pass1_blocks_per_sm != c->shapePass1) {
+    c->shapeSearch = search_blocks_per_sm; c->shapePass1 = pass1_blocks_per_sm;
+    c->graphValid = false; c->epoch++;
+  }
+  return SQDEM_OK;
+}
+
+// Time every candidate shape on the scene itself: two rounds over the candidates, `steps`
+// timesteps each (CUDA events on the context stream), the minimum per candidate kept.  Since
+// shapes change no result these are ordinary timesteps: the scene advances by
+// candidates x (2 x steps + 1) steps, as it would with the default shape.
+sqdem_status sqdem_autotune(sqdem_ctx* c, int steps, sqdem_tune* out) {
+  if (!c || steps <= 0) return SQDEM_ERR_ARG;
+  if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "no bodies");
+  const int mx = maxSearchBlocksPerSM(c);
+  const int p1s[4] = {4, 8, 16, 32};
+  std::vector<double> t(4 * (size_t)mx, 1e300);
+  sqdem_status s;
+  for (int round = 0; round < 2; round++)
+    for (int sb = 1; sb <= mx; sb++)
+      for (int k = 0; k < 4; k++) {
+        if ((s = sqdem_set_launch_shape(c, sb, p1s[k]))) return s;
+        if (round == 0 && (s = sqdem_step(c, 1))) return s;   // graph capture outside the timing
+        double ms = 0;
+        if ((s = sqdem_time_steps(c, steps, &ms))) return s;
+        double& b = t[4 * (size_t)(sb - 1) + k];
+        b = std::min(b, ms);
+      }
+  size_t bi = 0;
+  for (size_t i = 1; i < t.size(); i++) if (t[i] < t[bi]) bi = i;
+  const int bs = (int)(bi / 4) + 1, bp = p1s[bi % 4];
+  if ((s = sqdem_set_launch_shape(c, bs, bp))) return s;
+  if (out) { out->search_blocks_per_sm = bs; out->pass1_blocks_per_sm = bp; out->ms_per_step = t[bi] / steps; out->candidates = (int)t.size(); }
   return SQDEM_OK;
 }
 

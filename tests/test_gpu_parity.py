@@ -327,3 +327,24 @@ def test_periodic_single_step_within_oracle_conditioning(gpu):
     dv = np.linalg.norm(r[:, 7:10] - x0[:, 7:10], axis=1)
     ev = np.linalg.norm(g[:, 7:10] - r[:, 7:10], axis=1) / np.where(dv > 0, dv, 1)
     assert np.median(ev) < 1e-9 and np.mean(ev < 1e-6) > 0.97
+
+
+@pytest.mark.gpu
+def test_autotuned_launch_shapes_change_nothing(gpu):
+    """The autotuner's steps are ordinary timesteps and the shape it picks changes no result."""
+    spec = dense_spec(seed=10, n=300)
+    a, b = engine_for(spec), engine_for(spec)
+    t = a.autotune(steps=2)
+    assert 1 <= t["search_blocks_per_sm"] and t["pass1_blocks_per_sm"] in (4, 8, 16, 32)
+    n_tuned = int(a.scalars()[0])
+    assert n_tuned == t["candidates"] * (2 * 2 + 1)
+    b.step(n_tuned)
+    a.step(20); b.step(20)
+    a.sync(); b.sync()
+    assert np.array_equal(a.body_state(), b.body_state())
+    assert np.array_equal(a.interactions(True), b.interactions(True))
+    for sb, p1 in ((1, 4), (2, 32)):
+        c = engine_for(spec)
+        c.set_launch_shape(sb, p1)
+        c.step(n_tuned + 20); c.sync()
+        assert np.array_equal(c.body_state(), b.body_state())

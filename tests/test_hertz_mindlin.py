@@ -253,3 +253,33 @@ def test_gpu_cooperative_evaluations_change_nothing(gpu):
     for k in ("lm_calls", "lm_iterations", "nan_forces"):
         assert ra[k] == rb[k], k
     assert ra["evals_fp64"] >= rb["evals_fp64"] > 0   # speculative points evaluated in spare slots
+
+
+@pytest.mark.gpu
+def test_gpu_periodic_cell_single_step(gpu):
+    """Periodic cell: the Hertz-Mindlin geometry uses unshifted positions (only precompute sees
+    shift2), as the reference; the GPU follows the oracle there too."""
+    spec = assemblies.hertz_mindlin(assemblies.periodic_cell(400, seed=4, solid_fraction=0.42, strain_rate=3.0))
+    orc = OracleScene.from_spec(spec, threads=1)
+    orc.step(10)
+    eng = engine_for(spec)
+    snapshot_into(eng, orc)
+    eng.put_cell(orc.cell())
+    eng.step(1); eng.sync(); orc.step(1)
+    assert np.array_equal(eng.cell(), orc.cell())
+    G, R = touching_common(eng.interactions(True), orc.interactions())
+    assert len(G) > 30
+    e = rel_force_errors(G, R)
+    assert np.median(e) < 1e-9 and np.mean(e < 1e-6) > 0.95
+
+
+@pytest.mark.gpu
+def test_gpu_precision_flag_does_not_change_the_hm_search(gpu):
+    """The Hertz-Mindlin search always runs in FP64: a context created with the mixed form
+    gives the same results bit for bit."""
+    spec = dense_hm(seed=9, n=300)
+    a, b = engine_for(spec), engine_for(spec, precision="mixed")
+    a.step(25); b.step(25)
+    a.sync(); b.sync()
+    assert np.array_equal(a.body_state(), b.body_state())
+    assert np.array_equal(a.interactions(True), b.interactions(True))
