@@ -348,3 +348,44 @@ def test_autotuned_launch_shapes_change_nothing(gpu):
         c.set_launch_shape(sb, p1)
         c.step(n_tuned + 20); c.sync()
         assert np.array_equal(c.body_state(), b.body_state())
+
+
+def _bed_statistics(spec, bodies, recs, slab=10e-3):
+    """Packing fraction of the bottom slab (Superquadrics::Initial volumes of the particles
+    whose centres lie in it, over the slab volume), coordination number (touching
+    particle-particle contacts per particle) and floor stress (normal force on the floor wall
+    over the box area)."""
+    from sudodem_gb300 import shape_props
+    p = spec.kind == 0
+    vol = np.array([shape_props(*s)[0] for s in spec.shape5[p]])
+    z = bodies[p, 2]
+    box = spec.info["box"]
+    phi = float(np.sum(vol[z < slab]) / (box * box * slab))
+    touch = recs[(recs[:, 4] > 0) & (recs[:, 0] > 5) & (recs[:, 2] == 1)]
+    coord = 2.0 * len(touch) / int(np.sum(p))
+    floor = abs(bodies[4, 18]) / (box * box)   # force z of the floor wall (body 4)
+    return np.array([phi, coord, floor])
+
+
+def test_long_run_statistics_over_five_seeds(gpu):
+    """Granular dynamics are chaotic, so long runs are compared statistically: the config-0
+    deposition (1,000 superellipsoids, 30,000 steps: the lower layers have landed and
+    packed) on the GPU and on the oracle for five
+    seeds; the mean over seeds of packing fraction, coordination number and floor stress
+    must agree within three standard errors of the per-seed differences plus 2%."""
+    import os
+    thr = max(1, min(16, os.cpu_count() or 1))
+    G, R = [], []
+    for seed in (31, 32, 33, 34, 35):
+        spec = assemblies.config0(seed=seed)
+        eng = engine_for(spec)
+        orc = OracleScene.from_spec(spec, threads=thr)
+        eng.step(30000); eng.sync(); orc.step(30000)
+        G.append(_bed_statistics(spec, eng.body_state(), eng.interactions(False)))
+        R.append(_bed_statistics(spec, orc.bodies(), orc.interactions()))
+    G, R = np.array(G), np.array(R)
+    d = G - R
+    se = d.std(axis=0, ddof=1) / np.sqrt(len(d))
+    print("gpu mean", G.mean(axis=0), "oracle mean", R.mean(axis=0), "diff", d.mean(axis=0), "se", se)
+    assert np.all(R.mean(axis=0) > 0)
+    assert np.all(np.abs(d.mean(axis=0)) <= 3 * se + 0.02 * np.abs(R.mean(axis=0)))
