@@ -124,6 +124,9 @@ class OracleScene:
         self.h = self.L.sqo_create()
         self.L.sqo_set_threads(self.h, threads)
 
+    def set_threads(self, n):
+        self.L.sqo_set_threads(self.h, int(n))
+
     def close(self):
         if self.h:
             self.L.sqo_destroy(self.h)
