@@ -2997,7 +2997,8 @@ static void freeAll(sqdem_ctx* c) {
   for (void* p : c->allocs) cudaFree(p);
   c->allocs.clear();
 }
-static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
+// blocks for n items (at least one: every kernel bounds its items, and a zero grid is a launch error)
+static inline int nblk(long n, int bs) { return std::max(1, (int)((n + bs - 1) / bs)); }
 
 static sqdem_status allocTable(sqdem_ctx* c, Table& t, int cap) {
   CK(dalloc(c, &t.owner, cap)); CK(dalloc(c, &t.partner, cap)); CK(dalloc(c, &t.flags, cap));
