@@ -58,6 +58,10 @@ def workload_spec(name, seed):
                                          eps_range=(0.3, 1.8))
     if name == "sq1k_config0":
         return assemblies.config0(seed=seed)
+    if name == "config3":
+        # 5,000 superellipsoids generated as in config 0, one material per body (the specimen of
+        # the differentiation window, before its deposition)
+        return assemblies.config3(seed=seed)
     if name in ("hm200k_dense", "hm20k_dense"):
         # Hertz-Mindlin contact model (SuperquadricsGeom2 Nelder-Mead geometry, HertzMindlinPhys,
         # SuperquadricsLaw2): superellipsoids with half-axes U[0.8,1.2] mm, eps U[0.5,1.5] on a
@@ -439,6 +443,150 @@ def run_ours(args):
         print(json.dumps(line))
 
 
+def config3_start(args):
+    """Start of the config-3 window on the GPU engine: the specimen deposited for
+    --deposit-steps steps, the lid lowered at 0.1 m/s until it has carried a force for five
+    checks in a row (100 steps apart), then given the compression velocity 0.05/s x its height."""
+    from sudodem_gb300 import Engine, assemblies
+    spec = assemblies.config3(seed=args.seed, n=args.particles)
+    eng = Engine(device=0)
+    eng.load(spec)
+    eng.step(args.deposit_steps)
+    b = eng.body_state()
+    part = spec.kind == 0
+    b[5, 2] = float(np.max(b[part, 2] + np.max(spec.shape5[part, 0:3], axis=1))) + 0.05e-3
+    b[5, 7:10] = [0.0, 0.0, -0.1]
+    eng.put_body_state(b)
+    held, k = 0, 0
+    while held < 5 and k < 2000:
+        eng.step(100)
+        k += 1
+        held = held + 1 if abs(eng.body_state()[5, 18]) > 1e-3 else 0
+    b = eng.body_state()
+    height = float(b[5, 2] - b[4, 2])
+    b[5, 7:10] = [0.0, 0.0, -0.05 * height]
+    recs = eng.interactions(include_potential=True)
+    eng.close()
+    return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_steps": 100 * k, "lid_height_m": height,
+                           "lid_velocity_m_s": -0.05 * height}
+
+
+# HBM bytes of one reverse step, each item once: per pair the taped state it reads (ids 8,
+# flag 4, depth 8, angle 16, normal 32, shear 32, phys 32, Fv 32, contact point 32, code 4),
+# its adjoints read and written (angle 16, normal 32, shear 32, twice), the contributions it
+# writes (8 x 32) and the parameter accumulators (2 x 32, read and written); per body its taped
+# state (5 x 32), shape/mass/eps (80) and adjoints (7 x 32, read and written twice).
+ADJ_BYTES_PER_PAIR = 8 + 4 + 8 + 16 + 32 + 32 + 32 + 32 + 32 + 4 + 2 * 80 + 256 + 4 * 32
+ADJ_BYTES_PER_BODY = 160 + 80 + 4 * 224
+
+
+def run_ours_adjoint(args):
+    """Config 3: gradient of the final lid force over a window of --window steps with respect
+    to per-particle friction and exponents and the stiffnesses, through the adjoint."""
+    rank, ws, dist = dist_setup()
+    from sudodem_gb300.adjoint import AdjointWindow, window_loss
+    spec, bodies, recs, start = config3_start(args)
+    n = spec.n_bodies
+    npart = spec.n_particles
+    wF = np.zeros((n, 3))
+    wF[5, 2] = 1.0
+    w = AdjointWindow(0)
+    w.load(spec, bodies, recs)
+    eps0 = spec.shape5[:, 3:5].copy()
+    mu0 = np.tan(spec.materials["frictionAngle"])
+    Kn0, Ks0 = spec.materials["Kn"].copy(), spec.materials["Ks"].copy()
+    # warm-up: a short window, forward and reverse
+    w.forward(min(args.window, 20), args.checkpoint, wF, None)
+    w.backward()
+    clocks = ClockSampler(0)
+    clocks.start()
+    loss, sig = w.forward(args.window, args.checkpoint, wF, None)
+    g = w.backward()
+    clk = clocks.stop()
+    rep = w.report()
+    ms = rep["forward_ms"] + rep["backward_ms"]
+    value = npart * args.window / (ms / 1e3)
+    # end to end: the torch autograd function from host parameters to host gradients
+    import torch
+    te = torch.tensor(eps0, dtype=torch.float64, requires_grad=True)
+    tm = torch.tensor(mu0, dtype=torch.float64, requires_grad=True)
+    tkn = torch.tensor(Kn0, dtype=torch.float64, requires_grad=True)
+    tks = torch.tensor(Ks0, dtype=torch.float64, requires_grad=True)
+    t0 = time.perf_counter()
+    L = window_loss(w, te, tm, tkn, tks, args.window, args.checkpoint, wF, None)
+    L.backward()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": npart * args.window / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (2 * n + 3 * n) * 8 / args.window,
+           "d2h_bytes_per_step": (2 * n + 3 * n) * 8 / args.window,
+           "note": "torch.autograd.Function: parameters from host tensors, loss and gradients back to host"}
+    # finite differences along seeded directions (GPU forward, branch signatures compared)
+    fd = []
+    rng = np.random.default_rng(args.seed)
+    part = (spec.kind == 0)[:, None]
+    for k in range(args.fd_dirs):
+        for name, h in (("eps", 3e-8), ("mu", 3e-5), ("Kn", 3e-5), ("Ks", 3e-5)):
+            dE = rng.normal(size=eps0.shape) * eps0 * part if name == "eps" else 0 * eps0
+            dmu = rng.normal(size=mu0.shape) * mu0 if name == "mu" else 0 * mu0
+            dKn = rng.normal(size=Kn0.shape) * Kn0 if name == "Kn" else 0 * Kn0
+            dKs = rng.normal(size=Ks0.shape) * Ks0 if name == "Ks" else 0 * Ks0
+            ad = float(np.sum(g["eps"] * dE) + np.sum(g["mu"] * dmu) + np.sum(g["Kn"] * dKn) + np.sum(g["Ks"] * dKs))
+            vals, sigs = [], []
+            for sgn in (1, -1):
+                w.set_materials(Kn0 + sgn * h * dKn, Ks0 + sgn * h * dKs, mu0 + sgn * h * dmu)
+                w.set_eps(eps0 + sgn * h * dE)
+                lv, sv = w.forward(args.window, args.checkpoint, wF, None)
+                vals.append(lv)
+                sigs.append(sv)
+            f = (vals[0] - vals[1]) / (2 * h)
+            fd.append({"param": name, "h": h, "adjoint": ad, "fd": f, "rel_err": abs(f - ad) / max(abs(ad), 1e-300),
+                       "same_branches": bool(sigs[0] == sigs[1] == sig)})
+    w.set_materials(Kn0, Ks0, mu0)
+    w.set_eps(eps0)
+    cpu = None
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from oracle import OracleScene
+        threads = os.cpu_count()
+        o = OracleScene.from_spec(spec, threads=threads)
+        o.set_bodies(bodies)
+        o.set_interactions(recs)
+        o.reset_phys()
+        o.set_frozen(True)
+        t0 = time.perf_counter()
+        nst = 0
+        while nst < args.window and time.perf_counter() - t0 < args.cpu_budget:
+            o.step(1)
+            nst += 1
+        el = time.perf_counter() - t0
+        cpu = {"value": npart * nst / el, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{nst} steps of the frozen-pair window (forward only) from the same start state; a "
+                         f"finite-difference gradient needs two such windows per parameter direction"}
+    peak, peak_kind = measured_peaks()
+    P = len(w.pairs())
+    alg = ADJ_BYTES_PER_PAIR * P + ADJ_BYTES_PER_BODY * n
+    step_s = rep["backward_ms"] / 1e3 / args.window
+    achieved = alg / step_s / 1e9
+    roofline = {"bound": "hbm", "kernel": "reverse step (k_bwd_integrate, k_bwd_contacts, k_bwd_gather, with the "
+                                          "segment recompute)", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": None, "algorithmic_bytes": alg,
+                "note": "bound by the FP64 issue rate of the dual-number replay of the narrowphase, not by bytes"}
+    launches = args.window * 2 + 1 + args.window * 5
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.window, "warmup": 1,
+            "ms_per_step": ms / args.window, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "config3", "particles": npart, "bodies": n, "pairs": P, "window_steps": args.window,
+                       "checkpoint_every": args.checkpoint, "parameters": {"eps": 2 * npart, "mu": n, "Kn": n, "Ks": n},
+                       "loss": "final lid normal force", "start": start,
+                       "what": "particle-steps/s of forward + reverse window (one gradient)",
+                       "l2": "state and tape larger than L2"},
+            "loss": loss, "forward_ms": rep["forward_ms"], "backward_ms": rep["backward_ms"],
+            "replay_mismatches": rep["replay_mismatches"], "grad_norms": {k: float(np.linalg.norm(v)) for k, v in g.items()},
+            "fd_check": fd, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": launches}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -455,11 +603,18 @@ def main():
                     help="keep the default launch shapes of the contact stage (no tuning steps)")
     ap.add_argument("--no-lm-spread", action="store_true",
                     help="one Levenberg-Marquardt evaluation point per lane and round (same results)")
+    ap.add_argument("--window", type=int, default=2000, help="config3: steps of the differentiated window")
+    ap.add_argument("--checkpoint", type=int, default=100, help="config3: steps between checkpoints")
+    ap.add_argument("--particles", type=int, default=5000, help="config3: particles")
+    ap.add_argument("--deposit-steps", type=int, default=30000, help="config3: deposition steps before the window")
+    ap.add_argument("--fd-dirs", type=int, default=0, help="config3: finite-difference directions per parameter kind")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "config3":
+        run_ours_adjoint(args)
     else:
         run_ours(args)
 

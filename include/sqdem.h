@@ -324,6 +324,60 @@ sqdem_status sqdem_batch_time_e2e(sqdem_batch* batch, int nsteps, const double* 
 /* Kernel launches of one batch step (all scenes). */
 long long sqdem_batch_launch_count(sqdem_batch* batch);
 
+/* ---------------------------------------------------------------------------------------
+ * Adjoint of a window of timesteps (no counterpart in the reference, which has no
+ * differentiation; the forward it differentiates is the linear contact model's step,
+ * Scene::moveToNextTimeStep core/Scene.cpp:70-138 with the engines of sqdem_step).
+ *
+ * A window starts from a scene state (bodies and interactions in the SQDEM_BODY_STRIDE /
+ * SQDEM_INTR_STRIDE layouts, e.g. from sqdem_get_body_state / sqdem_get_interactions) and
+ * keeps its potential-pair set: the collider does not run and the law's bound-separation
+ * erase (pkg/dem/Superquadrics.cpp:1203-1207) is not applied; contacts still open and close
+ * through the narrowphase and the depth gate.  Ip2 (Superquadrics.cpp:1086-1116) is applied
+ * afresh to every pair from the materials given.  Particles must be free, damped, aspherical
+ * superquadrics not flagged as spheres; walls move with their prescribed velocity; no
+ * periodic cell, no viscous contact damping.
+ *
+ * Parameters: per-body exponents eps1, eps2 (narrowphase shape; mass, inertia and r_max keep
+ * the values of the state), per-material Kn, Ks and friction coefficient mu = tan(angle).
+ * Loss = sum_b wF_b . F_b(last step) + wX_b . pos_b(end), F_b the body's contact force of
+ * the window's last step (for a wall, its normal-force component is the wall force).
+ * Gradients are those of the discrete map with every branch (Levenberg-Marquardt decisions,
+ * contact gates, Coulomb cap, damping signs) taken as in the forward run. */
+typedef struct sqdem_adj sqdem_adj;
+sqdem_status sqdem_adj_create(sqdem_adj** out, int device);
+void sqdem_adj_destroy(sqdem_adj* adj);
+const char* sqdem_adj_last_error(sqdem_adj* adj);
+/* Scene of the window: n bodies (kind, shape5 = rx ry rz eps1 eps2, wall axis/sense pairs,
+ * material ids, sphere flags, state37 rows) and npairs interaction records.  Wall-wall pairs
+ * are dropped, wall pairs ordered (wall, particle). */
+sqdem_status sqdem_adj_load(sqdem_adj* adj, int n, const int* kind, const double* shape5, const int* wall_axis_sense,
+                            const int* mat, const int* isSphere, const double* state37, long npairs,
+                            const double* intr57, double dt, const double* gravity3, double damping);
+/* Materials (at least as many as the bodies use): Kn, Ks, frictionAngle. */
+sqdem_status sqdem_adj_set_materials(sqdem_adj* adj, int nmat, const double* Kn, const double* Ks,
+                                     const double* frictionAngle);
+/* Exponents of every body (n x 2; walls ignored). */
+sqdem_status sqdem_adj_set_eps(sqdem_adj* adj, const double* eps2);
+/* Run the window: nsteps steps, state checkpointed every checkpoint_every steps.  wF3, wX3:
+ * n x 3 loss weights (NULL = 0).  Returns the loss and a 64-bit signature of every branch
+ * taken (equal signatures: the same branches). */
+sqdem_status sqdem_adj_forward(sqdem_adj* adj, int nsteps, int checkpoint_every, const double* wF3,
+                               const double* wX3, double* loss, unsigned long long* signature);
+/* Gradient of the last forward run's loss: dL/deps (n x 2), dL/dKn, dL/dKs, dL/dmu (per
+ * material).  Recomputes each segment from its checkpoint; SQDEM_ERR_NUMERIC if a replay did
+ * not reproduce its forward branch. */
+sqdem_status sqdem_adj_backward(sqdem_adj* adj, double* dL_deps, double* dL_dKn, double* dL_dKs, double* dL_dmu);
+/* State after the window: n x 16 (pos ori(w,x,y,z) vel angVel angMom). */
+sqdem_status sqdem_adj_get_state(sqdem_adj* adj, double* out16);
+long sqdem_adj_num_pairs(sqdem_adj* adj);
+/* Pairs after the window, 16 doubles each: id1 id2 hasGeom depth contactAngle2 normal3
+ * shearForce3, then the force on id1 in the last step (3) and whether it was applied. */
+sqdem_status sqdem_adj_get_pairs(sqdem_adj* adj, double* out16);
+/* replay mismatches, Disfunction evaluations and LM calls of the forward run, pairs replayed,
+ * forward ms, backward ms, steps, checkpoint interval */
+sqdem_status sqdem_adj_report(sqdem_adj* adj, double* out8);
+
 #ifdef __cplusplus
 }
 #endif

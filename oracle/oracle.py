@@ -62,6 +62,8 @@ def lib():
         "sqo_pair_geom2": (i, [v, i, i, i, dp, dp]),
         "sqo_curvatures": (None, [d, d, d, d, d, d, d, dp]),
         "sqo_hertz_mindlin": (None, [dp, dp, d, dp]),
+        "sqo_set_frozen": (None, [v, i]), "sqo_signature": (C.c_ulonglong, [v]), "sqo_reset_phys": (None, [v]),
+        "sqo_set_material": (None, [v, i, d, d, d]), "sqo_set_eps": (None, [v, i, d, d]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -277,6 +279,22 @@ class OracleScene:
                 "point2": out[10:13], "contactAngle": out[13:15], "curvatures1": out[15:17],
                 "curvatures2": out[17:19], "curvatureAngle": out[19], "alpha": out[20], "K": out[21], "E": out[22],
                 "curvatures_sum": out[23], "isSphere": bool(out[24]), "nm_evaluations": it}
+
+    def set_frozen(self, on=True):
+        """Frozen-pair window: no collider pass, no bound-separation erase; signature reset."""
+        self.L.sqo_set_frozen(self.h, 1 if on else 0)
+
+    def signature(self):
+        return int(self.L.sqo_signature(self.h))
+
+    def reset_phys(self):
+        self.L.sqo_reset_phys(self.h)
+
+    def set_material(self, m, Kn, Ks, frictionAngle):
+        self.L.sqo_set_material(self.h, int(m), float(Kn), float(Ks), float(frictionAngle))
+
+    def set_eps(self, body, e1, e2):
+        self.L.sqo_set_eps(self.h, int(body), float(e1), float(e2))
 
     def set_quiet(self, on=True):
         self.L.sqo_set_quiet(self.h, 1 if on else 0)

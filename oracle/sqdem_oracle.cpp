@@ -228,6 +228,7 @@ struct Interaction {
   bool geomExists;      // functorCache.geomExists
   Geom g; Phys p;
   long iterBorn; long linIx; int cellDist[3];
+  bool sliding;         // the law capped the shear force at this step (Coulomb branch)
 };
 
 // InsertionSortCollider::Bounds (InsertionSortCollider.hpp:90-109)
@@ -237,7 +238,7 @@ struct Bounds {
   bool operator>(const Bounds& b) const { if (id == b.id && coord == b.coord) return !isMin; return coord > b.coord; }
 };
 
-struct Stats { long lmCalls, lmIters, disCalls, restarts, nanNormals; long hist[16]; long nanForces; };
+struct Stats { long lmCalls, lmIters, disCalls, restarts, nanNormals; long hist[16]; long nanForces; unsigned long long sig; };
 
 
 struct Scene {
@@ -273,6 +274,11 @@ struct Scene {
   void (*midHook)(void*) = nullptr; void* midHookArg = nullptr;
   // NewtonIntegrator::quiet_system_flag (NewtonIntegrator.hpp:73, .cpp:246-250,299)
   bool quietSystem = false;
+  // Window with a frozen pair set (the adjoint's forward map): the collider does not run and
+  // the law's bound-separation erase is skipped.  sig sums a hash of every branch taken
+  // (contact state, force, Coulomb cap, Disfunction evaluations per pair; damping signs per body).
+  bool frozenPairs = false;
+  unsigned long long sig = 0;
   // CompressionEngine (pkg/dem/Compression.hpp:39-252), run between InteractionLoop and Newton
   struct Servo* servo = nullptr;
   long stopAtIter = -1;   // Scene::stopAtIter as the engine requests it
@@ -828,13 +834,9 @@ static bool ig2WallSq(Scene& S, Interaction* I, const Body& w, const Body& b, co
 }
 
 // Ip2_SuperquadricsMat_SuperquadricsMat_SuperquadricsPhys::go (Superquadrics.cpp:1086-1116)
-static void ip2(Scene& S, Interaction* I) {
-  if (I->hasPhys) return;
+static void ip2Coeffs(Scene& S, Interaction* I, Phys& p) {
   const Mat& m1 = S.mats[S.bodies[I->id1].mat];
   const Mat& m2 = S.mats[S.bodies[I->id2].mat];
-  Phys& p = I->p;
-  std::memset(&p, 0, sizeof(Phys));
-  I->hasPhys = true;
   if (I->id1 > 5) {
     Real fa = std::min(m1.frictionAngle, m2.frictionAngle);
     p.tanphi = std::tan(fa);
@@ -847,6 +849,13 @@ static void ip2(Scene& S, Interaction* I) {
   }
   p.betan = std::max(m1.betan, m2.betan);
   p.betas = std::max(m1.betas, m2.betas);
+}
+static void ip2(Scene& S, Interaction* I) {
+  if (I->hasPhys) return;
+  Phys& p = I->p;
+  std::memset(&p, 0, sizeof(Phys));
+  I->hasPhys = true;
+  ip2Coeffs(S, I, p);
 }
 
 // SuperquadricsGeom::rotate (Superquadrics.cpp:1053-1080)
@@ -869,8 +878,9 @@ static bool law(Scene& S, Interaction* I, V3* F, V3* T) {
     ab_min = ab_min + sh;
     ab_max = ab_max + sh;
   }
-  if (A.bmin[0] >= ab_max[0] || ab_min[0] >= A.bmax[0] || A.bmin[1] >= ab_max[1] || ab_min[1] >= A.bmax[1] ||
-      A.bmin[2] >= ab_max[2] || ab_min[2] >= A.bmax[2]) {
+  I->sliding = false;
+  if (!S.frozenPairs && (A.bmin[0] >= ab_max[0] || ab_min[0] >= A.bmax[0] || A.bmin[1] >= ab_max[1] || ab_min[1] >= A.bmax[1] ||
+      A.bmin[2] >= ab_max[2] || ab_min[2] >= A.bmax[2])) {
     ph.normalForce = V3(); ph.shearForce = V3();
     requestErase(I);
     return false;
@@ -898,6 +908,7 @@ static bool law(Scene& S, Interaction* I, V3* F, V3* T) {
   shearForce1 = shearForce1 - ph.ks * g.shearInc;
   Real maxFs = sqnorm(normalForce) * std::pow(ph.tanphi, 2);
   if (sqnorm(shearForce1) > maxFs) {
+    I->sliding = true;
     Real ratio = std::sqrt(maxFs) / norm(shearForce1);
     shearForce1 = shearForce1 * ratio;
   } else if (useDamping) {
@@ -1256,6 +1267,14 @@ static bool law2(Scene& S, Interaction* I, V3* F, V3* T, Stats& st) {
   return true;
 }
 
+// hash of one item's branches at one step (the signature of a frozen-pair window)
+static inline unsigned long long branchHash(unsigned long long item, long step, unsigned long long bits) {
+  unsigned long long z = ((item + 1) * 0x9E3779B97F4A7C15ull) ^ ((unsigned long long)(step + 1) << 40) ^ (bits * 0xC2B2AE3D27D4EB4Full);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
 // InteractionLoop::action (pkg/common/InteractionLoop.cpp:23-149)
 static void interactionLoop(Scene& S) {
   const long size = (long)S.lin.size();
@@ -1290,15 +1309,22 @@ static void interactionLoop(Scene& S) {
       if (!law2(S, I, S.fbuf[tn].data(), S.tbuf[tn].data(), S.tstats[tn])) requestErase(I);
       continue;
     }
+    const long dc0 = S.tstats[tn].disCalls;
     if (b1.kind == KIND_WALL) ig2WallSq(S, I, b1, b2, shift2);
     else ig2SqSq(S, I, b1, b2, shift2, S.tstats[tn]);
     ip2(S, I);
     if (!law(S, I, S.fbuf[tn].data(), S.tbuf[tn].data())) requestErase(I);
+    if (S.frozenPairs) {
+      // the decisions at which the map jumps: the Levenberg-Marquardt path (Disfunction calls);
+      // the contact gate and the Coulomb cap are continuous and not recorded
+      S.tstats[tn].sig += branchHash(pairKey(I->id1, I->id2), S.iter, (unsigned long long)(S.tstats[tn].disCalls - dc0));
+    }
   }
   for (int t = 0; t < nt; t++) {
     S.stats.lmCalls += S.tstats[t].lmCalls; S.stats.lmIters += S.tstats[t].lmIters;
     S.stats.disCalls += S.tstats[t].disCalls; S.stats.restarts += S.tstats[t].restarts;
     S.stats.nanNormals += S.tstats[t].nanNormals;
+    S.sig += S.tstats[t].sig;
     if (S.tstats[t].nanForces) S.stopAtIter = S.iter + 1;
     S.stats.nanForces += S.tstats[t].nanForces;
     for (int k = 0; k < 16; k++) S.stats.hist[k] += S.tstats[t].hist[k];
@@ -1387,10 +1413,12 @@ static void newtonAction(Scene& S) {
     S.maxVelocitySq = sqnorm(S.prevCellSize - S.cellSize) / std::pow(dt, 2);
   else S.maxVelocitySq = 0;
   std::vector<Real> thrMax(S.nThreads, 0.0);
+  std::vector<unsigned long long> thrSig(S.nThreads, 0ull);
 #pragma omp parallel for num_threads(S.nThreads)
   for (long id = 0; id < nb; id++) {
     Body& b = S.bodies[id];
     V3 f = S.force[id], m = S.torque[id];
+    unsigned signBits = 0;
     const bool useAspherical = (S.exactAsphericalRot && b.aspherical && b.blockedDOFs != DOF_ALL);
     const bool isSphere = (b.kind == KIND_SQ) && b.sq.isSphere;
     const V3 fluctVel = periodic ? b.vel - mul(prevVelGrad, b.pos) : b.vel;
@@ -1399,7 +1427,12 @@ static void newtonAction(Scene& S) {
       if (b.blockedDOFs == 0) linAccel = V3(f[0] / b.mass + S.gravity[0], f[1] / b.mass + S.gravity[1], f[2] / b.mass + S.gravity[2]);
       else for (int i = 0; i < 3; i++) if (!(b.blockedDOFs & (1u << i))) linAccel[i] += f[i] / b.mass + S.gravity[i];
       if (b.isDamped)  // cundallDamp2nd (:23-25)
-        for (int i = 0; i < 3; i++) linAccel[i] *= 1 - S.damping * Sign(linAccel[i] * (fluctVel[i] + 0.5 * dt * linAccel[i]));
+        for (int i = 0; i < 3; i++) {
+          const Real w = fluctVel[i] + 0.5 * dt * linAccel[i];
+          const Real sg = Sign(linAccel[i] * w);
+          if (linAccel[i] != 0) signBits |= (w > 0 ? 1u : (w < 0 ? 2u : 3u)) << (2 * i);
+          linAccel[i] *= 1 - S.damping * sg;
+        }
       if (periodic && homoDeform) linAccel = linAccel + mul(prevVelGrad, b.vel);
       b.vel = b.vel + dt * linAccel;
       if (!useAspherical) {
@@ -1419,7 +1452,11 @@ static void newtonAction(Scene& S) {
             for (int i = 0; i < 3; i++) angAccel[i] *= 1 - S.damping * Sign(angAccel[i] * (b.angVel[i] + 0.5 * dt * angAccel[i]));
             b.angVel = b.angVel + dt * angAccel;
           } else {  // cundallDamp1st on the torque (:19-21)
-            for (int i = 0; i < 3; i++) m[i] *= 1 - S.damping * Sign(m[i] * b.angVel[i]);
+            for (int i = 0; i < 3; i++) {
+              const Real sg = Sign(m[i] * b.angVel[i]);
+              if (m[i] != 0) signBits |= (b.angVel[i] > 0 ? 1u : (b.angVel[i] < 0 ? 2u : 3u)) << (2 * (i + 3));
+              m[i] *= 1 - S.damping * sg;
+            }
           }
         }
       }
@@ -1436,6 +1473,7 @@ static void newtonAction(Scene& S) {
       if (periodic && homoDeform) b.vel = b.vel + mul(dVelGrad, b.pos);  // leapfrogTranslate (:306-317)
       b.pos = b.pos + b.vel * dt;
     }
+    if (S.frozenPairs && b.kind == KIND_SQ) thrSig[threadNum()] += branchHash(id, S.iter, signBits | 4096u);
     // saveMaximaDisplacement (:72-85)
     if (b.hasBound) {
       V3 disp = b.pos - b.refPos;
@@ -1447,6 +1485,7 @@ static void newtonAction(Scene& S) {
   }
   if (S.quietSystem) S.quietSystem = false;
   for (Real t : thrMax) S.maxVelocitySq = std::max(S.maxVelocitySq, t);
+  for (unsigned long long t : thrSig) S.sig += t;
   if (periodic) { S.prevCellSize = S.cellSize; S.prevVelGrad = S.velGrad; }
 }
 
@@ -1714,7 +1753,7 @@ static void svAction(Scene& S, Servo& C) {            // action_cubic, Compressi
 static void step(Scene& S) {
   S.lastStepCollided = false;
   if (S.isPeriodic) cellIntegrate(S);
-  if (colliderIsActivated(S)) { colliderAction(S); S.lastStepCollided = true; }
+  if (!S.frozenPairs && colliderIsActivated(S)) { colliderAction(S); S.lastStepCollided = true; }
   interactionLoop(S);
   if (S.midHook) S.midHook(S.midHookArg);
   if (S.servo) svAction(S, *S.servo);
@@ -1738,6 +1777,27 @@ void sqo_destroy(void* h) {
   delete S;
 }
 void sqo_set_threads(void* h, int n) { ((Scene*)h)->nThreads = n > 0 ? n : 1; }
+
+// Frozen-pair window (the forward map the adjoint differentiates): on = no collider pass and
+// no bound-separation erase from now on; the branch signature restarts at 0.
+void sqo_set_frozen(void* h, int on) { Scene* S = (Scene*)h; S->frozenPairs = on != 0; S->sig = 0; }
+unsigned long long sqo_signature(void* h) { return ((Scene*)h)->sig; }
+// Recompute the Ip2 coefficients (kn, ks, tan(phi), betas) of every interaction that has a
+// phys from the current materials, keeping its force history (the start of an adjoint window).
+void sqo_reset_phys(void* h) {
+  Scene* S = (Scene*)h;
+  for (Interaction* I : S->lin)
+    if (I->hasPhys) ip2Coeffs(*S, I, I->p);
+}
+void sqo_set_material(void* h, int m, double Kn, double Ks, double frictionAngle) {
+  Mat& M = ((Scene*)h)->mats[m];
+  M.Kn = Kn; M.Ks = Ks; M.frictionAngle = frictionAngle;
+}
+// Exponents of one body's shape (mass, inertia and r_max keep their values).
+void sqo_set_eps(void* h, int body, double e1, double e2) {
+  SQ& q = ((Scene*)h)->bodies[body].sq;
+  q.eps1 = e1; q.eps2 = e2;
+}
 
 int sqo_add_material(void* h, double Kn, double Ks, double frictionAngle, double betan, double betas, double density) {
   Scene* S = (Scene*)h;

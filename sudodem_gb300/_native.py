@@ -115,6 +115,13 @@ def load_library(build_if_missing=True):
         "sqdem_set_contact_model": (i, [v, i]), "sqdem_contact_model": (i, [v]), "sqdem_num_materials": (i, [v]),
         "sqdem_set_material_moduli": (i, [v, i, dp, dp]), "sqdem_get_material_moduli": (i, [v, dp, dp]),
         "sqdem_set_launch_shape": (i, [v, i, i]), "sqdem_autotune": (i, [v, i, C.c_void_p]),
+        "sqdem_adj_create": (i, [P(v), i]), "sqdem_adj_destroy": (None, [v]),
+        "sqdem_adj_last_error": (C.c_char_p, [v]),
+        "sqdem_adj_load": (i, [v, i, ip, dp, ip, ip, ip, dp, l, dp, d, dp, d]),
+        "sqdem_adj_set_materials": (i, [v, i, dp, dp, dp]), "sqdem_adj_set_eps": (i, [v, dp]),
+        "sqdem_adj_forward": (i, [v, i, i, dp, dp, dp, P(C.c_ulonglong)]),
+        "sqdem_adj_backward": (i, [v, dp, dp, dp, dp]), "sqdem_adj_get_state": (i, [v, dp]),
+        "sqdem_adj_num_pairs": (l, [v]), "sqdem_adj_get_pairs": (i, [v, dp]), "sqdem_adj_report": (i, [v, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -137,7 +144,10 @@ def exported_symbols():
             "sqdem_batch_size", "sqdem_batch_scene", "sqdem_batch_step", "sqdem_batch_sync", "sqdem_batch_time_steps",
             "sqdem_batch_time_e2e", "sqdem_batch_launch_count", "sqdem_snapshot", "sqdem_restore",
             "sqdem_set_contact_model", "sqdem_contact_model", "sqdem_num_materials", "sqdem_set_material_moduli",
-            "sqdem_get_material_moduli", "sqdem_set_launch_shape", "sqdem_autotune"]
+            "sqdem_get_material_moduli", "sqdem_set_launch_shape", "sqdem_autotune",
+            "sqdem_adj_create", "sqdem_adj_destroy", "sqdem_adj_last_error", "sqdem_adj_load",
+            "sqdem_adj_set_materials", "sqdem_adj_set_eps", "sqdem_adj_forward", "sqdem_adj_backward",
+            "sqdem_adj_get_state", "sqdem_adj_num_pairs", "sqdem_adj_get_pairs", "sqdem_adj_report"]
 
 
 def _dp(a):

@@ -160,6 +160,30 @@ def config0(seed=0, n=1000):
     return walled_lattice(n, seed=seed, box=20e-3, per_side=7)
 
 
+def per_body_materials(spec, friction=None):
+    """Give every body its own copy of material 0 (so that friction, Kn, Ks can differ per
+    particle, as the adjoint's per-particle parameters do); friction: per-body coefficients
+    (tan of the friction angle) or None to keep material 0's."""
+    nb = spec.n_bodies
+    m0 = spec.materials
+    spec.materials = {k: np.full(nb, float(v[0])) for k, v in m0.items()}
+    if friction is not None:
+        spec.materials["frictionAngle"] = np.arctan(np.asarray(friction, dtype=np.float64))
+    spec.mat = np.arange(nb, dtype=np.int32)
+    return spec
+
+
+def config3(seed=0, n=5000):
+    """Differentiation specimen: n superellipsoids generated as in config 0 (half-axes U[0.8,1.2]
+    mm, eps U[0.5,1.5], uniform random orientations, jittered 2.6 mm lattice, kn=1e5 N/m,
+    ks/kn=0.5, density 2650, damping 0.3, dt = 0.5 critical) in a 43.8 mm square walled box
+    (16 x 16 particles per layer, 20 layers), one material per body with friction 0.5 (the
+    per-particle friction parameters).  The deposition and the lid placement that precede the
+    compression window are run by the caller (bench.py's config3 workload)."""
+    spec = walled_lattice(n, seed=seed, box=43.8e-3, per_side=16)
+    return per_body_materials(spec)
+
+
 def deposition_box(n, seed=0, eps_range=(0.3, 1.8), r_range=(0.8e-3, 1.2e-3), log_radius=False, spacing=2.6e-3):
     """Large walled deposition scene: a square box sized for ~n^(1/3)^2 particles per layer."""
     per_side = max(7, int(round(n ** (1.0 / 3.0) * 1.6)))

@@ -1,8 +1,10 @@
 """Build of the in-tree native libraries.
 
 ``build()`` compiles ``csrc/*.cu`` into ``sudodem_gb300/libsqdem_gpu.so`` for sm_103a with
-nvcc.  The FP64 translation unit is built with ``--fmad=false`` so that products and sums
-keep the rounding sequence of the reference's x86-64 build (no fused multiply-add).
+nvcc, the two translation units in parallel.  Both are built with ``--fmad=false`` so that
+products and sums keep the rounding sequence of the reference's x86-64 build (no fused
+multiply-add), and so that the adjoint's dual-number replay takes the branches of its
+forward run.
 """
 import os
 import shutil
@@ -43,12 +45,12 @@ def build(force=False, verbose=False):
     objs = []
     tmp = os.path.join(HERE, "_obj")
     os.makedirs(tmp, exist_ok=True)
-    units = [("sqdem_engine.cu", ["--fmad=false"])]
+    units = [("sqdem_engine.cu", ["--fmad=false"]), ("sqdem_adjoint.cu", ["--fmad=false"])]
     procs = []
     for src, extra in units:
         obj = os.path.join(tmp, src.replace(".cu", ".o"))
         cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
-               "-Xcompiler", "-Wno-deprecated-declarations",
+               "-Xcompiler", "-Wno-deprecated-declarations", "-diag-suppress", "1444",
                *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)

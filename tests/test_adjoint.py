@@ -1,0 +1,208 @@
+"""Adjoint of a frozen-pair window (sqdem_adj_*) against central finite differences.
+
+The reference for the finite differences is the oracle run as the same window (collider off,
+no bound-separation erase, Ip2 coefficients refreshed from the perturbed materials with the
+force history kept).  A finite difference is only a valid check when the +h and -h runs take
+the same branches as the base run (Levenberg-Marquardt decisions, contact gates, Coulomb cap,
+damping signs): both engines return a signature of their branches and the comparison uses the
+directions whose three signatures agree.  Steps: h = 3e-5 (relative) for friction and
+stiffness, whose losses are smooth but carry rounding noise of ~1e-11 relative, and h = 3e-8
+for the exponents, where larger steps change the number of Levenberg-Marquardt iterations of
+some pair.  Tolerance: 1e-5 relative on the directional derivative.
+"""
+import numpy as np
+import pytest
+
+from adjoint_scene import compressed_specimen, lid_weights, oracle_window, params_of
+
+NSTEPS = 60
+TOL = 1e-5
+H_SMOOTH, H_EPS = 3e-5, 3e-8
+
+
+@pytest.fixture(scope="module")
+def scene():
+    return compressed_specimen()
+
+
+def _dirs(rng, spec, eps, mu, Kn, Ks):
+    n = spec.n_bodies
+    part = (spec.kind == 0)[:, None]
+    dE = rng.normal(size=eps.shape) * eps * part
+    return [("eps", (dE, 0 * mu, 0 * Kn, 0 * Ks), H_EPS),
+            ("mu", (0 * eps, rng.normal(size=mu.shape) * mu, 0 * Kn, 0 * Ks), H_SMOOTH),
+            ("Kn", (0 * eps, 0 * mu, rng.normal(size=Kn.shape) * Kn, 0 * Ks), H_SMOOTH),
+            ("Ks", (0 * eps, 0 * mu, 0 * Kn, rng.normal(size=Ks.shape) * Ks), H_SMOOTH)][: 4 if n else 0]
+
+
+def _ad(gr, d):
+    dE, dmu, dKn, dKs = d
+    return float(np.sum(gr["eps"] * dE) + np.sum(gr["mu"] * dmu) + np.sum(gr["Kn"] * dKn) + np.sum(gr["Ks"] * dKs))
+
+
+# ---------------------------------------------------------------------------- CPU (oracle)
+def test_oracle_frozen_window_keeps_pair_set(scene):
+    import oracle as O
+    spec, bodies, recs = scene
+    o = O.OracleScene.from_spec(spec)
+    o.set_bodies(bodies)
+    o.set_interactions(recs)
+    runs0 = o.scalars()[7]
+    o.set_frozen(True)
+    o.step(150)
+    after = o.interactions()
+    assert o.scalars()[7] == runs0                      # no collider pass
+    key = lambda r: (min(r[0], r[1]), max(r[0], r[1]))  # noqa: E731
+    assert sorted(map(key, after[:, 0:2].tolist())) == sorted(map(key, recs[:, 0:2].tolist()))
+
+
+def test_oracle_reset_phys_refreshes_coefficients_and_keeps_history(scene):
+    import oracle as O
+    spec, bodies, recs = scene
+    o = O.OracleScene.from_spec(spec)
+    o.set_bodies(bodies)
+    o.set_interactions(recs)
+    for m in range(spec.n_bodies):
+        o.set_material(m, 2e5, 1e5, np.arctan(0.25))
+    o.reset_phys()
+    r = o.interactions()
+    real = r[:, 2] != 0
+    assert np.any(real)
+    assert np.all(r[real, 23] == 2e5) and np.all(r[real, 24] == 1e5)
+    assert np.allclose(r[real, 25], 0.25, rtol=1e-15)
+    assert np.array_equal(r[:, 29:32], recs[:, 29:32])   # shear springs kept
+
+
+def test_oracle_window_is_differentiable_along_friction(scene):
+    """The oracle's window loss is smooth along friction: two step sizes with unchanged
+    branches give the same central difference."""
+    spec, bodies, recs = scene
+    eps, mu, Kn, Ks = params_of(spec)
+    wF, wX = lid_weights(spec.n_bodies), np.zeros((spec.n_bodies, 3))
+    L0, s0, _ = oracle_window(spec, bodies, recs, eps, mu, Kn, Ks, NSTEPS, wF, wX)
+    assert L0 != 0
+    rng = np.random.default_rng(4)
+    agreed = 0
+    for trial in range(4):
+        dmu = rng.normal(size=mu.shape) * mu
+        fds = []
+        for h in (H_SMOOTH, H_SMOOTH / 3):
+            Lp, sp, _ = oracle_window(spec, bodies, recs, eps, mu + h * dmu, Kn, Ks, NSTEPS, wF, wX)
+            Lm, sm, _ = oracle_window(spec, bodies, recs, eps, mu - h * dmu, Kn, Ks, NSTEPS, wF, wX)
+            fds.append((Lp - Lm) / (2 * h) if sp == sm == s0 else None)
+        if None in fds:
+            continue
+        assert abs(fds[0] - fds[1]) <= 1e-5 * abs(fds[0])
+        agreed += 1
+    assert agreed >= 2
+
+
+# ---------------------------------------------------------------------------- GPU
+@pytest.fixture(scope="module")
+def window(scene):
+    from sudodem_gb300.adjoint import AdjointWindow
+    spec, bodies, recs = scene
+    w = AdjointWindow(0)
+    w.load(spec, bodies, recs)
+    yield w
+    w.close()
+
+
+def _gpu_loss(w, spec, eps, mu, Kn, Ks, wF, wX, nsteps=NSTEPS, every=25):
+    w.set_materials(Kn, Ks, mu)
+    w.set_eps(eps)
+    return w.forward(nsteps, every, wF, wX)
+
+
+@pytest.mark.gpu
+def test_adjoint_forward_matches_oracle(scene, window):
+    spec, bodies, recs = scene
+    eps, mu, Kn, Ks = params_of(spec)
+    n = spec.n_bodies
+    wF, wX = lid_weights(n), np.zeros((n, 3))
+    for nsteps in (1, 20):
+        L, _ = _gpu_loss(window, spec, eps, mu, Kn, Ks, wF, wX, nsteps, 10)
+        Lo, _, ob = oracle_window(spec, bodies, recs, eps, mu, Kn, Ks, nsteps, wF, wX)
+        st = window.state()
+        assert abs(L - Lo) <= 1e-9 * abs(Lo)
+        assert np.max(np.abs(st[:, 0:3] - ob[:, 0:3])) <= 1e-12
+        assert np.max(np.abs(st[:, 3:7] - ob[:, 3:7])) <= 1e-10
+        assert np.max(np.abs(st[:, 7:10] - ob[:, 7:10])) <= 1e-9 * max(1.0, np.max(np.abs(ob[:, 7:10])))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("reference", ["gpu", "oracle"])
+def test_adjoint_gradient_matches_central_differences(scene, window, reference):
+    spec, bodies, recs = scene
+    eps, mu, Kn, Ks = params_of(spec)
+    n = spec.n_bodies
+    wF, wX = lid_weights(n), np.zeros((n, 3))
+    L0, sg0 = _gpu_loss(window, spec, eps, mu, Kn, Ks, wF, wX)
+    gr = window.backward()
+    assert window.report()["replay_mismatches"] == 0
+    assert L0 != 0
+    if reference == "oracle":
+        L0o, sg0, _ = oracle_window(spec, bodies, recs, eps, mu, Kn, Ks, NSTEPS, wF, wX)
+        assert abs(L0o - L0) <= 1e-8 * abs(L0)
+    rng = np.random.default_rng(11)
+    checked = {}
+    for trial in range(4):
+        for name, d, h in _dirs(rng, spec, eps, mu, Kn, Ks):
+            dE, dmu, dKn, dKs = d
+            vals, sigs = [], []
+            for s in (1, -1):
+                args = (eps + s * h * dE, mu + s * h * dmu, Kn + s * h * dKn, Ks + s * h * dKs)
+                if reference == "gpu":
+                    l, sg = _gpu_loss(window, spec, *args, wF, wX)
+                else:
+                    l, sg, _ = oracle_window(spec, bodies, recs, *args, NSTEPS, wF, wX)
+                vals.append(l)
+                sigs.append(sg)
+            if not (sigs[0] == sigs[1] == sg0):
+                continue
+            fd = (vals[0] - vals[1]) / (2 * h)
+            ad = _ad(gr, d)
+            assert abs(fd - ad) <= TOL * abs(ad), (name, trial, fd, ad)
+            checked[name] = checked.get(name, 0) + 1
+    assert all(checked.get(k, 0) >= 2 for k in ("eps", "mu", "Kn", "Ks")), checked
+
+
+@pytest.mark.gpu
+def test_adjoint_checkpoint_interval_changes_nothing(scene, window):
+    spec, bodies, recs = scene
+    eps, mu, Kn, Ks = params_of(spec)
+    n = spec.n_bodies
+    wF = lid_weights(n)
+    wX = np.random.default_rng(2).normal(size=(n, 3)) * (spec.kind == 0)[:, None]
+    res = []
+    for every in (1, 7, 60, NSTEPS):
+        L, sg = _gpu_loss(window, spec, eps, mu, Kn, Ks, wF, wX, NSTEPS, every)
+        g = window.backward()
+        res.append((L, sg, g))
+    for L, sg, g in res[1:]:
+        assert L == res[0][0] and sg == res[0][1]
+        for k in g:
+            assert np.array_equal(g[k], res[0][2][k]), k
+
+
+@pytest.mark.gpu
+def test_window_loss_torch_autograd(scene, window):
+    torch = pytest.importorskip("torch")
+    from sudodem_gb300.adjoint import window_loss
+    spec, bodies, recs = scene
+    eps, mu, Kn, Ks = params_of(spec)
+    n = spec.n_bodies
+    wF, wX = lid_weights(n), np.zeros((n, 3))
+    te = torch.tensor(eps, dtype=torch.float64, requires_grad=True)
+    tm = torch.tensor(mu, dtype=torch.float64, requires_grad=True)
+    tkn = torch.tensor(Kn, dtype=torch.float64, requires_grad=True)
+    tks = torch.tensor(Ks, dtype=torch.float64, requires_grad=True)
+    loss = window_loss(window, te, tm, tkn, tks, NSTEPS, 25, wF, wX)
+    (2.0 * loss).backward()
+    L, _ = _gpu_loss(window, spec, eps, mu, Kn, Ks, wF, wX)
+    g = window.backward()
+    assert float(loss) == L
+    assert np.array_equal(te.grad.numpy(), 2.0 * g["eps"])
+    assert np.array_equal(tm.grad.numpy(), 2.0 * g["mu"])
+    assert np.array_equal(tkn.grad.numpy(), 2.0 * g["Kn"])
+    assert np.array_equal(tks.grad.numpy(), 2.0 * g["Ks"])
