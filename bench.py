@@ -445,7 +445,8 @@ def run_ours(args):
 
 def config3_start(args):
     """Start of the config-3 window on the GPU engine: the specimen deposited for
-    --deposit-steps steps, the lid lowered at 0.1 m/s until it has carried a force for five
+    --deposit-steps steps, the lid placed 0.05 mm above the highest particle's centre plus its
+    largest half-axis and lowered at 0.05 m/s until its force has stayed above 0.01 N for ten
     checks in a row (100 steps apart), then given the compression velocity 0.05/s x its height."""
     from sudodem_gb300 import Engine, assemblies
     spec = assemblies.config3(seed=args.seed, n=args.particles)
@@ -455,13 +456,13 @@ def config3_start(args):
     b = eng.body_state()
     part = spec.kind == 0
     b[5, 2] = float(np.max(b[part, 2] + np.max(spec.shape5[part, 0:3], axis=1))) + 0.05e-3
-    b[5, 7:10] = [0.0, 0.0, -0.1]
+    b[5, 7:10] = [0.0, 0.0, -0.05]
     eng.put_body_state(b)
     held, k = 0, 0
-    while held < 5 and k < 2000:
+    while held < 10 and k < 3000:
         eng.step(100)
         k += 1
-        held = held + 1 if abs(eng.body_state()[5, 18]) > 1e-3 else 0
+        held = held + 1 if abs(eng.body_state()[5, 18]) > 1e-2 else 0
     b = eng.body_state()
     height = float(b[5, 2] - b[4, 2])
     b[5, 7:10] = [0.0, 0.0, -0.05 * height]
@@ -562,7 +563,7 @@ def run_ours_adjoint(args):
                "sample": f"{nst} steps of the frozen-pair window (forward only) from the same start state; a "
                          f"finite-difference gradient needs two such windows per parameter direction"}
     peak, peak_kind = measured_peaks()
-    P = len(w.pairs())
+    P = w.num_pairs()
     alg = ADJ_BYTES_PER_PAIR * P + ADJ_BYTES_PER_BODY * n
     step_s = rep["backward_ms"] / 1e3 / args.window
     achieved = alg / step_s / 1e9
@@ -606,7 +607,7 @@ def main():
     ap.add_argument("--window", type=int, default=2000, help="config3: steps of the differentiated window")
     ap.add_argument("--checkpoint", type=int, default=100, help="config3: steps between checkpoints")
     ap.add_argument("--particles", type=int, default=5000, help="config3: particles")
-    ap.add_argument("--deposit-steps", type=int, default=30000, help="config3: deposition steps before the window")
+    ap.add_argument("--deposit-steps", type=int, default=60000, help="config3: deposition steps before the window")
     ap.add_argument("--fd-dirs", type=int, default=0, help="config3: finite-difference directions per parameter kind")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -116,6 +116,14 @@ class AdjointWindow:
         self._check(self.lib.sqdem_adj_get_state(self.h, _dp(out)))
         return out
 
+    def set_replay(self, grouped=True):
+        """Reverse-step kernel for the pairs: replays split over lane groups (default) or one
+        thread per pair; the gradients are bitwise the same."""
+        self._check(self.lib.sqdem_adj_set_replay(self.h, 1 if grouped else 0))
+
+    def num_pairs(self):
+        return int(self.lib.sqdem_adj_num_pairs(self.h))
+
     def pairs(self):
         m = self.lib.sqdem_adj_num_pairs(self.h)
         out = np.zeros((max(m, 1), 16))

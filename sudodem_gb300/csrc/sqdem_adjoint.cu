@@ -458,54 +458,56 @@ SQA_HD void loadPair(const Consts& C, const State& S, int c, PairVals& p) {
   p.nPrev = xyz(S.normal[c]); p.sPrev = xyz(S.shear[c]);
 }
 
-// tangent seeding: slot k of the current pass (none for the double instantiation)
+// tangent seeding: input k is tangent component k - base of this pass (none for double)
 template <class T> struct Seeder;
-template <> struct Seeder<double> { static SQA_HD double s(double x, int) { return x; } };
-template <> struct Seeder<DT> { static SQA_HD DT s(double x, int k) { return seed<NT>(x, k); } };
+template <> struct Seeder<double> { static SQA_HD double s(double x, int, int) { return x; } };
+template <int N> struct Seeder<Dual<N>> { static SQA_HD Dual<N> s(double x, int k, int base) { return seed<N>(x, k - base); } };
 
 // Geometry of a pair.  Replay slots: 0-2 position of id2, 3-6 orientation of id1, 7-10
 // orientation of id2, 11-12 eps of id1, 13-14 eps of id2, 15-16 the stored contact angles.
 // The position of id1 carries no tangent: the SQ-SQ outputs other than the contact point are
 // invariant under a common translation, which gives their derivatives with respect to it.
-template <class T> SQA_HD void pairGeom(const PairVals& p, Geom<T>& g) {
+template <class T> SQA_HD void pairGeom(const PairVals& p, Geom<T>& g, int base = 0) {
   typedef Seeder<T> Sd;
-  const V3<T> X2 = mk<T>(Sd::s(p.x2.x, 0), Sd::s(p.x2.y, 1), Sd::s(p.x2.z, 2));
+  const V3<T> X2 = mk<T>(Sd::s(p.x2.x, 0, base), Sd::s(p.x2.y, 1, base), Sd::s(p.x2.z, 2, base));
   T q2[4];
-  for (int k = 0; k < 4; k++) q2[k] = Sd::s(p.q2[k], 7 + k);
+  for (int k = 0; k < 4; k++) q2[k] = Sd::s(p.q2[k], 7 + k, base);
   Shape<T> B;
-  shapeInit(B, p.shp2, Sd::s(p.e2.x, 13), Sd::s(p.e2.y, 14), q2, X2);
+  shapeInit(B, p.shp2, Sd::s(p.e2.x, 13, base), Sd::s(p.e2.y, 14, base), q2, X2);
   if (p.i1.x == 1) {
     const double wallc = p.i1.y == 0 ? p.x1.x : (p.i1.y == 1 ? p.x1.y : p.x1.z);
     geomWallSq(g, p.isNew, p.prevDepth, p.i1.y, (double)p.i1.z, wallc, B);
   } else {
     T q1[4];
-    for (int k = 0; k < 4; k++) q1[k] = Sd::s(p.q1[k], 3 + k);
+    for (int k = 0; k < 4; k++) q1[k] = Sd::s(p.q1[k], 3 + k, base);
     Shape<T> A;
-    shapeInit(A, p.shp1, Sd::s(p.e1.x, 11), Sd::s(p.e1.y, 12), q1, lift<T>(p.x1));
-    const T angIn[2] = {Sd::s(p.ang[0], 15), Sd::s(p.ang[1], 16)};
+    shapeInit(A, p.shp1, Sd::s(p.e1.x, 11, base), Sd::s(p.e1.y, 12, base), q1, lift<T>(p.x1));
+    const T angIn[2] = {Sd::s(p.ang[0], 15, base), Sd::s(p.ang[1], 16, base)};
     geomSqSq(g, p.isNew, p.prevDepth, angIn, A, B);
   }
 }
 
-// Law inputs, 34 of them, in replay chunk `chunk` (slots 17*chunk .. 17*chunk+16):
+// Law inputs, 34 of them, in replay chunk `chunk` (inputs 17*chunk .. 17*chunk+16, from
+// tangent component `base` of the pass on):
 // 0 depth, 1-3 normal, 4-6 contact point, 7-9 x1, 10-12 x2, 13-15 v1, 16-18 w1, 19-21 v2,
 // 22-24 w2, 25-27 previous normal, 28-30 previous shear force, 31 kn, 32 ks, 33 tan(phi).
 static const int NLAW = 34;
-template <class T> SQA_HD T lawSeed(double x, int i, int chunk) { return Seeder<T>::s(x, i - NT * chunk); }
-template <class T> SQA_HD V3<T> lawSeed3(const V3<double>& v, int i, int chunk) {
-  return mk<T>(lawSeed<T>(v.x, i, chunk), lawSeed<T>(v.y, i + 1, chunk), lawSeed<T>(v.z, i + 2, chunk));
+template <class T> SQA_HD T lawSeed(double x, int i, int c0) { return Seeder<T>::s(x, i, c0); }
+template <class T> SQA_HD V3<T> lawSeed3(const V3<double>& v, int i, int c0) {
+  return mk<T>(lawSeed<T>(v.x, i, c0), lawSeed<T>(v.y, i + 1, c0), lawSeed<T>(v.z, i + 2, c0));
 }
 template <class T>
 SQA_HD void lawInputs(const PairVals& p, double depth, const V3<double>& normal, const V3<double>& cp, int chunk,
-                      LawIn<T>& in) {
-  in.depth = lawSeed<T>(depth, 0, chunk);
-  in.normal = lawSeed3<T>(normal, 1, chunk);
-  in.cp = lawSeed3<T>(cp, 4, chunk);
-  in.x1 = lawSeed3<T>(p.x1, 7, chunk); in.x2 = lawSeed3<T>(p.x2, 10, chunk);
-  in.v1 = lawSeed3<T>(p.v1, 13, chunk); in.w1 = lawSeed3<T>(p.w1, 16, chunk);
-  in.v2 = lawSeed3<T>(p.v2, 19, chunk); in.w2 = lawSeed3<T>(p.w2, 22, chunk);
-  in.nPrev = lawSeed3<T>(p.nPrev, 25, chunk); in.sPrev = lawSeed3<T>(p.sPrev, 28, chunk);
-  in.kn = lawSeed<T>(p.ph.x, 31, chunk); in.ks = lawSeed<T>(p.ph.y, 32, chunk); in.tanphi = lawSeed<T>(p.ph.z, 33, chunk);
+                      LawIn<T>& in, int base = 0) {
+  const int c0 = NT * chunk + base;
+  in.depth = lawSeed<T>(depth, 0, c0);
+  in.normal = lawSeed3<T>(normal, 1, c0);
+  in.cp = lawSeed3<T>(cp, 4, c0);
+  in.x1 = lawSeed3<T>(p.x1, 7, c0); in.x2 = lawSeed3<T>(p.x2, 10, c0);
+  in.v1 = lawSeed3<T>(p.v1, 13, c0); in.w1 = lawSeed3<T>(p.w1, 16, c0);
+  in.v2 = lawSeed3<T>(p.v2, 19, c0); in.w2 = lawSeed3<T>(p.w2, 22, c0);
+  in.nPrev = lawSeed3<T>(p.nPrev, 25, c0); in.sPrev = lawSeed3<T>(p.sPrev, 28, c0);
+  in.kn = lawSeed<T>(p.ph.x, 31, c0); in.ks = lawSeed<T>(p.ph.y, 32, c0); in.tanphi = lawSeed<T>(p.ph.z, 33, c0);
 }
 
 SQA_HD unsigned long long mix64(unsigned long long z) {
@@ -711,71 +713,66 @@ __global__ void __launch_bounds__(128) k_bwd_integrate(Consts C, State S, StepOu
 // contact angles, normal and shear force through lAng/lN/lS), and leave the adjoints of the
 // pair's inputs: its stored history (in lAng/lN/lS), its bodies' state (in con) and the
 // parameters (accumulated in accEps/accPhys).
-SQA_HD double dotd(const V3<double>& l, const V3<DT>& v, int j) {
+template <int N> SQA_HD double dotd(const V3<double>& l, const V3<Dual<N>>& v, int j) {
   return l.x * v.x.d[j] + l.y * v.y.d[j] + l.z * v.z.d[j];
 }
-SQA_HD void bwdContact(const Consts& C, const State& S, const StepOut& O, const Adj& A, int c) {
+struct PairAdjIn {
   PairVals p;
-  loadPair(C, S, c, p);
+  bool pre, force, needed;
+  int angMode;
+  V3<double> lFv, lT1, lT2, lnOut, lsOut;
+  double2 la2;
+};
+SQA_HD void pairAdjIn(const Consts& C, const State& S, const StepOut& O, const Adj& A, int c, PairAdjIn& q) {
+  loadPair(C, S, c, q.p);
   const int code = O.code[c];
-  const bool pre = (code & CO_PRE) != 0, force = (code & CO_FORCE) != 0;
-  const int angMode = (code & CO_ANG) ? 1 : ((code & CO_ANG0) ? 2 : 0);
-  const V3<double> lFv = xyz(A.lF[p.id.x]) - xyz(A.lF[p.id.y]);
-  const V3<double> lT1 = xyz(A.lT[p.id.x]), lT2 = xyz(A.lT[p.id.y]);
-  const double2 la2 = A.lAng[c];
-  const V3<double> lnOut = xyz(A.lN[c]), lsOut = xyz(A.lS[c]);
+  q.pre = (code & CO_PRE) != 0;
+  q.force = (code & CO_FORCE) != 0;
+  q.angMode = (code & CO_ANG) ? 1 : ((code & CO_ANG0) ? 2 : 0);
+  q.lFv = xyz(A.lF[q.p.id.x]) - xyz(A.lF[q.p.id.y]);
+  q.lT1 = xyz(A.lT[q.p.id.x]);
+  q.lT2 = xyz(A.lT[q.p.id.y]);
+  q.la2 = A.lAng[c];
+  q.lnOut = xyz(A.lN[c]);
+  q.lsOut = xyz(A.lS[c]);
+  // A pair without a force whose new contact angles nothing downstream depends on (zero
+  // adjoint) contributes nothing: its replay is skipped.
+  q.needed = q.pre || (q.angMode == 1 && (q.la2.x != 0 || q.la2.y != 0));
+}
+// Contraction of one law input's tangent (component j of the replay) with the adjoints of the
+// law's outputs.
+template <int N> SQA_HD double lawContract(const PairAdjIn& q, const LawOut<Dual<N>>& out, int j) {
+  return dotd(q.lFv, out.Fv, j) + dotd(q.lT1, out.T1, j) + dotd(q.lT2, out.T2, j) + dotd(q.lsOut, out.s, j);
+}
+// Contraction of one geometry input's tangent with the adjoints of the geometry's outputs
+// (depth, normal, contact point from the law; stored normal and angles from the next step).
+template <int N> SQA_HD double geomContract(const PairAdjIn& q, const Geom<Dual<N>>& gd, const double* lin, int j) {
+  double s = 0;
+  if (q.pre) {
+    const V3<double> lnormal = q.lnOut + mk<double>(lin[1], lin[2], lin[3]);
+    s += lin[0] * gd.depth.d[j] + dotd(lnormal, gd.normal, j) + dotd(mk<double>(lin[4], lin[5], lin[6]), gd.cp, j);
+  }
+  if (q.angMode == 1) s += q.la2.x * gd.ang[0].d[j] + q.la2.y * gd.ang[1].d[j];
+  return s;
+}
+// The pair's outputs of the reverse step from lin (dL/d law inputs, zero without a force) and
+// gs (contracted geometry tangents, zero without a replay).
+SQA_HD void assemblePair(const Adj& A, int c, const PairAdjIn& q, const double* lin, const double* gs) {
   V3<double> lx1 = zero3<double>(), lx2 = zero3<double>(), lv1 = zero3<double>(), lw1 = zero3<double>();
-  V3<double> lv2 = zero3<double>(), lw2 = zero3<double>(), lnPrev = zero3<double>(), lsPrev = zero3<double>();
+  V3<double> lv2 = zero3<double>(), lw2 = zero3<double>(), lsPrev = zero3<double>();
+  V3<double> lnPrev = (!q.pre && !q.p.isNew) ? q.lnOut : zero3<double>();   // passes through unchanged
   double lq1[4] = {0, 0, 0, 0}, lq2[4] = {0, 0, 0, 0}, leps[4] = {0, 0, 0, 0}, lphys[3] = {0, 0, 0};
-  double langIn[2] = {angMode == 0 ? la2.x : 0.0, angMode == 0 ? la2.y : 0.0};
-  if (!pre && !p.isNew) lnPrev = lnOut;   // the stored normal passes through unchanged
-  if (pre || angMode == 1) {
-    SQA_CNT(&C.cnt[A_REPLAYED], 1);
-    Geom<DT> gd;
-    pairGeom<DT>(p, gd);
-    if (gd.precomputed != pre || (gd.angMode == 1) != (angMode == 1)) SQA_CNT(&C.cnt[A_MISMATCH], 1);
-    double ldepth = 0;
-    V3<double> lnormal = zero3<double>(), lcp = zero3<double>();
-    if (pre) {
-      lnormal = lnOut;
-      if (force) {
-        const double depth = gd.depth.v;
-        const V3<double> nv = mk<double>(gd.normal.x.v, gd.normal.y.v, gd.normal.z.v);
-        const V3<double> cpv = mk<double>(gd.cp.x.v, gd.cp.y.v, gd.cp.z.v);
-        double lin[2 * NT];
-        for (int chunk = 0; chunk < 2; chunk++) {
-          LawIn<DT> in;
-          lawInputs<DT>(p, depth, nv, cpv, chunk, in);
-          LawOut<DT> out;
-          const bool ran = law(in, gd.isShearNew, C.dt, out);
-          if (!ran) { SQA_CNT(&C.cnt[A_MISMATCH], 1); for (int j = 0; j < NT; j++) lin[chunk * NT + j] = 0; continue; }
-          if (chunk == 0) {
-            const double4 F4 = O.Fv[c];
-            if (F4.x != out.Fv.x.v || F4.y != out.Fv.y.v || F4.z != out.Fv.z.v) SQA_CNT(&C.cnt[A_MISMATCH], 1);
-          }
-          for (int j = 0; j < NT; j++)
-            lin[chunk * NT + j] = dotd(lFv, out.Fv, j) + dotd(lT1, out.T1, j) + dotd(lT2, out.T2, j) + dotd(lsOut, out.s, j);
-        }
-        ldepth = lin[0];
-        lnormal = lnormal + mk<double>(lin[1], lin[2], lin[3]);
-        lcp = mk<double>(lin[4], lin[5], lin[6]);
-        lx1 = mk<double>(lin[7], lin[8], lin[9]); lx2 = mk<double>(lin[10], lin[11], lin[12]);
-        lv1 = mk<double>(lin[13], lin[14], lin[15]); lw1 = mk<double>(lin[16], lin[17], lin[18]);
-        lv2 = mk<double>(lin[19], lin[20], lin[21]); lw2 = mk<double>(lin[22], lin[23], lin[24]);
-        lnPrev = mk<double>(lin[25], lin[26], lin[27]); lsPrev = mk<double>(lin[28], lin[29], lin[30]);
-        lphys[0] = lin[31]; lphys[1] = lin[32]; lphys[2] = lin[33];
-      }
-    }
-    // contract the geometry's tangents
-    double gs[NT];
-    for (int j = 0; j < NT; j++) {
-      double s = 0;
-      if (pre) s += ldepth * gd.depth.d[j] + dotd(lnormal, gd.normal, j) + dotd(lcp, gd.cp, j);
-      if (angMode == 1) s += la2.x * gd.ang[0].d[j] + la2.y * gd.ang[1].d[j];
-      gs[j] = s;
-    }
+  double langIn[2] = {q.angMode == 0 ? q.la2.x : 0.0, q.angMode == 0 ? q.la2.y : 0.0};
+  if (q.force) {
+    lx1 = mk<double>(lin[7], lin[8], lin[9]); lx2 = mk<double>(lin[10], lin[11], lin[12]);
+    lv1 = mk<double>(lin[13], lin[14], lin[15]); lw1 = mk<double>(lin[16], lin[17], lin[18]);
+    lv2 = mk<double>(lin[19], lin[20], lin[21]); lw2 = mk<double>(lin[22], lin[23], lin[24]);
+    lnPrev = mk<double>(lin[25], lin[26], lin[27]); lsPrev = mk<double>(lin[28], lin[29], lin[30]);
+    lphys[0] = lin[31]; lphys[1] = lin[32]; lphys[2] = lin[33];
+  }
+  if (q.needed) {
     lx2 = lx2 + mk<double>(gs[0], gs[1], gs[2]);
-    if (p.i1.x != 1) lx1 = lx1 + lcp - mk<double>(gs[0], gs[1], gs[2]);
+    if (q.p.i1.x != 1) lx1 = lx1 + mk<double>(lin[4], lin[5], lin[6]) - mk<double>(gs[0], gs[1], gs[2]);
     for (int k = 0; k < 4; k++) { lq1[k] = gs[3 + k]; lq2[k] = gs[7 + k]; leps[k] = gs[11 + k]; }
     langIn[0] += gs[15]; langIn[1] += gs[16];
   }
@@ -789,9 +786,103 @@ SQA_HD void bwdContact(const Consts& C, const State& S, const StepOut& O, const 
   A.accEps[c] = make_double4(ae.x + leps[0], ae.y + leps[1], ae.z + leps[2], ae.w + leps[3]);
   A.accPhys[c] = make_double4(ap.x + lphys[0], ap.y + lphys[1], ap.z + lphys[2], 0);
 }
+// the replay's branches against the forward run's (counted, reported by the backward call)
+template <int N> SQA_HD void checkReplay(const Consts& C, const StepOut& O, int c, const PairAdjIn& q,
+                                         const Geom<Dual<N>>& gd) {
+  if (gd.precomputed != q.pre || (gd.angMode == 1) != (q.angMode == 1)) SQA_CNT(&C.cnt[A_MISMATCH], 1);
+}
+template <int N> SQA_HD void checkLaw(const Consts& C, const StepOut& O, int c, bool ran, const LawOut<Dual<N>>& out) {
+  if (!ran) { SQA_CNT(&C.cnt[A_MISMATCH], 1); return; }
+  const double4 F4 = O.Fv[c];
+  if (F4.x != out.Fv.x.v || F4.y != out.Fv.y.v || F4.z != out.Fv.z.v) SQA_CNT(&C.cnt[A_MISMATCH], 1);
+}
+
+// One thread per pair, all 17 geometry tangents and two chunks of 17 law tangents per thread.
+SQA_HD void bwdContact(const Consts& C, const State& S, const StepOut& O, const Adj& A, int c) {
+  PairAdjIn q;
+  pairAdjIn(C, S, O, A, c, q);
+  double lin[2 * NT], gs[NT];
+  for (int j = 0; j < 2 * NT; j++) lin[j] = 0;
+  for (int j = 0; j < NT; j++) gs[j] = 0;
+  if (q.needed) {
+    SQA_CNT(&C.cnt[A_REPLAYED], 1);
+    Geom<DT> gd;
+    pairGeom<DT>(q.p, gd);
+    checkReplay(C, O, c, q, gd);
+    if (q.pre && q.force) {
+      const V3<double> nv = mk<double>(gd.normal.x.v, gd.normal.y.v, gd.normal.z.v);
+      const V3<double> cpv = mk<double>(gd.cp.x.v, gd.cp.y.v, gd.cp.z.v);
+      for (int chunk = 0; chunk < 2; chunk++) {
+        LawIn<DT> in;
+        lawInputs<DT>(q.p, gd.depth.v, nv, cpv, chunk, in);
+        LawOut<DT> out;
+        const bool ran = law(in, gd.isShearNew, C.dt, out);
+        if (chunk == 0 || !ran) checkLaw(C, O, c, ran, out);
+        if (ran)
+          for (int j = 0; j < NT; j++) lin[chunk * NT + j] = lawContract(q, out, j);
+      }
+    }
+    for (int j = 0; j < NT; j++) gs[j] = geomContract(q, gd, lin, j);
+  }
+  assemblePair(A, c, q, lin, gs);
+}
 __global__ void __launch_bounds__(64) k_bwd_contacts(Consts C, State S, StepOut O, Adj A) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c < C.P) bwdContact(C, S, O, A, c);
+}
+
+// The same reverse step of a pair split over a group of GL lanes, lane l carrying the tangent
+// components TG*l .. TG*l+TG-1 of every replay (Dual<TG> values stay in registers, and the
+// longest Levenberg-Marquardt replay of a step costs about a forward evaluation per step of
+// its path instead of seventeen tangents' worth).  Every tangent component is computed by the
+// same operations as in k_bwd_contacts, so the results are bitwise the same.
+static const int TG = 3, GL = 6, GPW = 32 / GL;   // five groups per warp (lanes 30 and 31 idle)
+static const int GRP_WARPS = 4;
+__global__ void __launch_bounds__(32 * GRP_WARPS) k_bwd_contacts_grp(Consts C, State S, StepOut O, Adj A) {
+  __shared__ double shLin[GRP_WARPS * GPW][2 * NT];
+  __shared__ double shGs[GRP_WARPS * GPW][NT];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gw = lane / GL, l = lane - gw * GL;
+  const bool laneOn = gw < GPW;
+  const int slot = warp * GPW + (laneOn ? gw : 0);
+  const int c = (blockIdx.x * GRP_WARPS + warp) * GPW + gw;
+  const bool active = laneOn && c < C.P;
+  const int base = TG * l;
+  PairAdjIn q;
+  Geom<Dual<TG>> gd;
+  if (active) {
+    pairAdjIn(C, S, O, A, c, q);
+    for (int j = 0; j < TG; j++) {
+      const int k = base + j;
+      if (k < NT) { shLin[slot][k] = 0; shLin[slot][NT + k] = 0; }
+    }
+    if (q.needed) {
+      if (l == 0) SQA_CNT(&C.cnt[A_REPLAYED], 1);
+      pairGeom<Dual<TG>>(q.p, gd, base);
+      if (l == 0) checkReplay(C, O, c, q, gd);
+      if (q.pre && q.force) {
+        const V3<double> nv = mk<double>(gd.normal.x.v, gd.normal.y.v, gd.normal.z.v);
+        const V3<double> cpv = mk<double>(gd.cp.x.v, gd.cp.y.v, gd.cp.z.v);
+        for (int chunk = 0; chunk < 2; chunk++) {
+          LawIn<Dual<TG>> in;
+          lawInputs<Dual<TG>>(q.p, gd.depth.v, nv, cpv, chunk, in, base);
+          LawOut<Dual<TG>> out;
+          const bool ran = law(in, gd.isShearNew, C.dt, out);
+          if (l == 0 && (chunk == 0 || !ran)) checkLaw(C, O, c, ran, out);
+          if (ran)
+            for (int j = 0; j < TG; j++)
+              if (base + j < NT) shLin[slot][chunk * NT + base + j] = lawContract(q, out, j);
+        }
+      }
+    }
+  }
+  __syncwarp();
+  if (active) {
+    for (int j = 0; j < TG; j++)
+      if (base + j < NT) shGs[slot][base + j] = q.needed ? geomContract(q, gd, shLin[slot], j) : 0.0;
+  }
+  __syncwarp();
+  if (active && l == 0) assemblePair(A, c, q, shLin[slot], shGs[slot]);
 }
 
 // Reverse step, (3) each body adds its pairs' contributions, in list order.
@@ -869,6 +960,8 @@ struct sqdem_adj {
   StateLayout L;
   char* init = nullptr;   // state at the start of the window
   char* work = nullptr;
+  char* fin = nullptr;        // state after the last forward window (kept through the reverse pass)
+  double4* finFv = nullptr;   // forces of that window's last step
   std::vector<char*> ckpt;
   // tape of one segment
   int tapeCap = 0;
@@ -884,6 +977,7 @@ struct sqdem_adj {
   // the last forward window
   int nsteps = 0, every = 0;
   bool haveForward = false;
+  bool replayGrouped = true;   // pair replays split over lane groups (k_bwd_contacts_grp)
   double loss = 0;
   unsigned long long counters[A_NCOUNT] = {};
   double msForward = 0, msBackward = 0;
@@ -910,7 +1004,7 @@ static void afreeAll(sqdem_adj* a) {
   for (void* p : a->allocs) cudaFree(p);
   a->allocs.clear();
   a->ckpt.clear(); a->tapeState.clear();
-  a->init = a->work = nullptr; a->tapeCap = 0;
+  a->init = a->work = a->fin = nullptr; a->finFv = nullptr; a->tapeCap = 0;
 }
 
 static Consts consts(sqdem_adj* a) {
@@ -1074,7 +1168,8 @@ sqdem_status sqdem_adj_load(sqdem_adj* a, int n, const int* kind, const double* 
   ACUDA(aalloc(a, &a->binfo, n)); ACUDA(aalloc(a, &a->idsD, P)); ACUDA(aalloc(a, &a->phys, P));
   ACUDA(aalloc(a, &a->bStart, n + 1)); ACUDA(aalloc(a, &a->bList, 2 * (size_t)P));
   ACUDA(aalloc(a, &a->cnt, A_NCOUNT));
-  ACUDA(aalloc(a, &a->init, a->L.bytes)); ACUDA(aalloc(a, &a->work, a->L.bytes));
+  ACUDA(aalloc(a, &a->init, a->L.bytes)); ACUDA(aalloc(a, &a->work, a->L.bytes)); ACUDA(aalloc(a, &a->fin, a->L.bytes));
+  ACUDA(aalloc(a, &a->finFv, P));
   ACUDA(aalloc(a, &a->lPos, n)); ACUDA(aalloc(a, &a->lOri, n)); ACUDA(aalloc(a, &a->lVel, n));
   ACUDA(aalloc(a, &a->lW, n)); ACUDA(aalloc(a, &a->lL, n)); ACUDA(aalloc(a, &a->lF, n)); ACUDA(aalloc(a, &a->lT, n));
   ACUDA(aalloc(a, &a->lAng, P)); ACUDA(aalloc(a, &a->lN, P)); ACUDA(aalloc(a, &a->lS, P));
@@ -1175,6 +1270,8 @@ sqdem_status sqdem_adj_forward(sqdem_adj* a, int nsteps, int checkpoint_every, c
   }
   k_loss<<<1, 256, 0, a->st>>>(consts(a), S, O, a->wF, a->wX, a->lossD);
   ACUDA(cudaGetLastError());
+  ACUDA(cudaMemcpyAsync(a->fin, a->work, a->L.bytes, cudaMemcpyDeviceToDevice, a->st));
+  if (a->P) ACUDA(cudaMemcpyAsync(a->finFv, O.Fv, a->P * sizeof(double4), cudaMemcpyDeviceToDevice, a->st));
   ACUDA(cudaEventRecord(e1, a->st));
   ACUDA(cudaMemcpyAsync(&a->loss, a->lossD, sizeof(double), cudaMemcpyDeviceToHost, a->st));
   ACUDA(cudaMemcpyAsync(a->counters, a->cnt, A_NCOUNT * sizeof(unsigned long long), cudaMemcpyDeviceToHost, a->st));
@@ -1224,7 +1321,10 @@ sqdem_status sqdem_adj_backward(sqdem_adj* a, double* dL_deps, double* dL_dKn, d
       const State S = a->L.view(a->tapeState[t - t0]);
       const StepOut O = tapeOut(a, t - t0);
       k_bwd_integrate<<<nblk(n, 128), 128, 0, a->st>>>(C, S, O, A, t == nsteps - 1 ? 1 : 0);
-      if (P) k_bwd_contacts<<<nblk(P, 64), 64, 0, a->st>>>(C, S, O, A);
+      if (P && a->replayGrouped)
+        k_bwd_contacts_grp<<<nblk(P, GRP_WARPS * GPW), 32 * GRP_WARPS, 0, a->st>>>(C, S, O, A);
+      else if (P)
+        k_bwd_contacts<<<nblk(P, 64), 64, 0, a->st>>>(C, S, O, A);
       k_bwd_gather<<<nblk(n, 128), 128, 0, a->st>>>(C, A);
     }
     ACUDA(cudaGetLastError());
@@ -1275,7 +1375,7 @@ sqdem_status sqdem_adj_get_state(sqdem_adj* a, double* out16) {
   if (!a->haveForward) return afail(a, SQDEM_ERR_STATE, "no forward run");
   ACUDA(cudaSetDevice(a->device));
   std::vector<char> hs(a->L.bytes);
-  ACUDA(cudaMemcpyAsync(hs.data(), a->work, a->L.bytes, cudaMemcpyDeviceToHost, a->st));
+  ACUDA(cudaMemcpyAsync(hs.data(), a->fin, a->L.bytes, cudaMemcpyDeviceToHost, a->st));
   ACUDA(cudaStreamSynchronize(a->st));
   const State v = a->L.view(hs.data());
   for (int i = 0; i < a->nb; i++) {
@@ -1289,6 +1389,12 @@ sqdem_status sqdem_adj_get_state(sqdem_adj* a, double* out16) {
 
 long sqdem_adj_num_pairs(sqdem_adj* a) { return a ? a->P : 0; }
 
+sqdem_status sqdem_adj_set_replay(sqdem_adj* a, int grouped) {
+  if (!a) return SQDEM_ERR_ARG;
+  a->replayGrouped = grouped != 0;
+  return SQDEM_OK;
+}
+
 // per pair after the forward window: id1 id2 hasGeom depth angle2 normal3 shearForce3 | force on id1 (3) of the
 // last step, applied (1/0)  -> 16 doubles
 sqdem_status sqdem_adj_get_pairs(sqdem_adj* a, double* out16) {
@@ -1297,8 +1403,8 @@ sqdem_status sqdem_adj_get_pairs(sqdem_adj* a, double* out16) {
   ACUDA(cudaSetDevice(a->device));
   std::vector<char> hs(a->L.bytes);
   std::vector<double4> fv(a->P);
-  ACUDA(cudaMemcpyAsync(hs.data(), a->work, a->L.bytes, cudaMemcpyDeviceToHost, a->st));
-  if (a->P) ACUDA(cudaMemcpyAsync(fv.data(), a->tapeFv, a->P * sizeof(double4), cudaMemcpyDeviceToHost, a->st));
+  ACUDA(cudaMemcpyAsync(hs.data(), a->fin, a->L.bytes, cudaMemcpyDeviceToHost, a->st));
+  if (a->P) ACUDA(cudaMemcpyAsync(fv.data(), a->finFv, a->P * sizeof(double4), cudaMemcpyDeviceToHost, a->st));
   ACUDA(cudaStreamSynchronize(a->st));
   const State v = a->L.view(hs.data());
   for (int c = 0; c < a->P; c++) {

@@ -177,12 +177,32 @@ def test_adjoint_checkpoint_interval_changes_nothing(scene, window):
     res = []
     for every in (1, 7, 60, NSTEPS):
         L, sg = _gpu_loss(window, spec, eps, mu, Kn, Ks, wF, wX, NSTEPS, every)
+        st = window.state()
         g = window.backward()
+        assert np.array_equal(window.state(), st)   # the reverse pass leaves the window's result readable
         res.append((L, sg, g))
     for L, sg, g in res[1:]:
         assert L == res[0][0] and sg == res[0][1]
         for k in g:
             assert np.array_equal(g[k], res[0][2][k]), k
+
+
+@pytest.mark.gpu
+def test_grouped_and_single_thread_replays_agree_bitwise(scene, window):
+    spec, bodies, recs = scene
+    eps, mu, Kn, Ks = params_of(spec)
+    n = spec.n_bodies
+    wF = lid_weights(n)
+    wX = np.random.default_rng(3).normal(size=(n, 3)) * (spec.kind == 0)[:, None]
+    res = []
+    for grouped in (True, False):
+        window.set_replay(grouped)
+        _gpu_loss(window, spec, eps, mu, Kn, Ks, wF, wX)
+        res.append(window.backward())
+        assert window.report()["replay_mismatches"] == 0
+    window.set_replay(True)
+    for k in res[0]:
+        assert np.array_equal(res[0][k], res[1][k]), k
 
 
 @pytest.mark.gpu
@@ -201,8 +221,40 @@ def test_window_loss_torch_autograd(scene, window):
     (2.0 * loss).backward()
     L, _ = _gpu_loss(window, spec, eps, mu, Kn, Ks, wF, wX)
     g = window.backward()
-    assert float(loss) == L
+    assert float(loss.detach()) == L
     assert np.array_equal(te.grad.numpy(), 2.0 * g["eps"])
     assert np.array_equal(tm.grad.numpy(), 2.0 * g["mu"])
     assert np.array_equal(tkn.grad.numpy(), 2.0 * g["Kn"])
     assert np.array_equal(tks.grad.numpy(), 2.0 * g["Ks"])
+
+
+@pytest.mark.gpu
+def test_adjoint_window_from_engine_records(scene):
+    """A window started from the GPU engine's own records (after ten ordinary engine steps)
+    follows the oracle's window from the same records."""
+    from sudodem_gb300 import Engine
+    from sudodem_gb300.adjoint import AdjointWindow
+    spec, bodies, recs = scene
+    import oracle as O
+    orc = O.OracleScene.from_spec(spec)
+    orc.set_bodies(bodies)
+    orc.set_interactions(recs)
+    eng = Engine(device=0)
+    eng.load(spec)
+    eng.put_body_state(orc.bodies())
+    eng.put_interactions(orc.interactions())
+    eng.put_scalars(orc.scalars())
+    eng.step(10)
+    eng.sync()
+    st, er = eng.body_state(), eng.interactions(include_potential=True)
+    eng.close()
+    w = AdjointWindow(0)
+    w.load(spec, st, er)
+    eps, mu, Kn, Ks = params_of(spec)
+    n = spec.n_bodies
+    wF, wX = lid_weights(n), np.zeros((n, 3))
+    L, _ = w.forward(20, 5, wF, wX)
+    Lo, _, ob = oracle_window(spec, st, er, eps, mu, Kn, Ks, 20, wF, wX)
+    assert np.max(np.abs(w.state()[:, 0:3] - ob[:, 0:3])) <= 1e-12
+    assert abs(L - Lo) <= 1e-9 * abs(Lo)
+    w.close()
