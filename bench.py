@@ -446,8 +446,9 @@ def run_ours(args):
 def config3_start(args):
     """Start of the config-3 window on the GPU engine: the specimen deposited for
     --deposit-steps steps, the lid placed 0.05 mm above the highest particle's centre plus its
-    largest half-axis and lowered at 0.05 m/s until its force has stayed above 0.01 N for ten
-    checks in a row (100 steps apart), then given the compression velocity 0.05/s x its height."""
+    largest half-axis and lowered at 0.05 m/s until its force has stayed above 0.5 N (about twice
+    the bed's weight) for ten checks in a row (100 steps apart), then given the compression
+    velocity 0.05/s x its height."""
     from sudodem_gb300 import Engine, assemblies
     spec = assemblies.config3(seed=args.seed, n=args.particles)
     eng = Engine(device=0)
@@ -462,14 +463,16 @@ def config3_start(args):
     while held < 10 and k < 3000:
         eng.step(100)
         k += 1
-        held = held + 1 if abs(eng.body_state()[5, 18]) > 1e-2 else 0
+        held = held + 1 if abs(eng.body_state()[5, 18]) > 0.5 else 0
     b = eng.body_state()
     height = float(b[5, 2] - b[4, 2])
     b[5, 7:10] = [0.0, 0.0, -0.05 * height]
     recs = eng.interactions(include_potential=True)
     eng.close()
+    lid = recs[(recs[:, 0] == 5) | (recs[:, 1] == 5)]
     return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_steps": 100 * k, "lid_height_m": height,
-                           "lid_velocity_m_s": -0.05 * height}
+                           "lid_velocity_m_s": -0.05 * height, "lid_force_n": float(b[5, 18]),
+                           "lid_pairs": int(len(lid)), "lid_pairs_touching": int(np.sum(lid[:, 4] > 0))}
 
 
 # HBM bytes of one reverse step, each item once: per pair the taped state it reads (ids 8,
@@ -496,9 +499,18 @@ def run_ours_adjoint(args):
     eps0 = spec.shape5[:, 3:5].copy()
     mu0 = np.tan(spec.materials["frictionAngle"])
     Kn0, Ks0 = spec.materials["Kn"].copy(), spec.materials["Ks"].copy()
-    # warm-up: a short window, forward and reverse
-    w.forward(min(args.window, 20), args.checkpoint, wF, None)
-    w.backward()
+    # warm-up, and the shape of the pairs' reverse-step kernel timed on a short window (every
+    # shape gives bitwise the same gradients): the fastest is kept
+    loss1, _ = w.forward(1, 1, wF, None)
+    shapes = {}
+    nt = min(args.window, 50)
+    for shape in (1, 2, 3, 0):
+        w.set_replay(shape)
+        w.forward(nt, min(args.checkpoint, nt), wF, None)
+        w.backward()
+        shapes[AdjointWindow.REPLAY_SHAPES[shape]] = w.report()["backward_ms"] / nt
+    best = min(shapes, key=shapes.get)
+    w.set_replay([k for k, v in AdjointWindow.REPLAY_SHAPES.items() if v == best][0])
     clocks = ClockSampler(0)
     clocks.start()
     loss, sig = w.forward(args.window, args.checkpoint, wF, None)
@@ -578,9 +590,10 @@ def run_ours_adjoint(args):
             "config": {"workload": "config3", "particles": npart, "bodies": n, "pairs": P, "window_steps": args.window,
                        "checkpoint_every": args.checkpoint, "parameters": {"eps": 2 * npart, "mu": n, "Kn": n, "Ks": n},
                        "loss": "final lid normal force", "start": start,
+                       "replay_shape": best, "replay_ms_per_step_by_shape": shapes,
                        "what": "particle-steps/s of forward + reverse window (one gradient)",
                        "l2": "state and tape larger than L2"},
-            "loss": loss, "forward_ms": rep["forward_ms"], "backward_ms": rep["backward_ms"],
+            "loss": loss, "loss_after_one_step": loss1, "forward_ms": rep["forward_ms"], "backward_ms": rep["backward_ms"],
             "replay_mismatches": rep["replay_mismatches"], "grad_norms": {k: float(np.linalg.norm(v)) for k, v in g.items()},
             "fd_check": fd, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": launches}

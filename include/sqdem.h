@@ -374,10 +374,11 @@ long sqdem_adj_num_pairs(sqdem_adj* adj);
 /* Pairs after the window, 16 doubles each: id1 id2 hasGeom depth contactAngle2 normal3
  * shearForce3, then the force on id1 in the last step (3) and whether it was applied. */
 sqdem_status sqdem_adj_get_pairs(sqdem_adj* adj, double* out16);
-/* Reverse-step kernel for the pairs: grouped = 1 (default) splits each pair's dual-number
- * replay over six lanes with three tangent components each; 0 runs it on one thread with all
- * seventeen.  Both give bitwise the same gradients. */
-sqdem_status sqdem_adj_set_replay(sqdem_adj* adj, int grouped);
+/* Shape of the pairs' reverse-step kernel, which replays each pair's narrowphase and law in
+ * dual numbers: 0 one thread per pair with all seventeen tangent components, 1 (default) three
+ * lanes with six each, 2 two lanes with nine, 3 six lanes with three.  Every shape gives
+ * bitwise the same gradients. */
+sqdem_status sqdem_adj_set_replay(sqdem_adj* adj, int shape);
 /* replay mismatches, Disfunction evaluations and LM calls of the forward run, pairs replayed,
  * forward ms, backward ms, steps, checkpoint interval */
 sqdem_status sqdem_adj_report(sqdem_adj* adj, double* out8);

@@ -116,10 +116,12 @@ class AdjointWindow:
         self._check(self.lib.sqdem_adj_get_state(self.h, _dp(out)))
         return out
 
-    def set_replay(self, grouped=True):
-        """Reverse-step kernel for the pairs: replays split over lane groups (default) or one
-        thread per pair; the gradients are bitwise the same."""
-        self._check(self.lib.sqdem_adj_set_replay(self.h, 1 if grouped else 0))
+    REPLAY_SHAPES = {0: "1 lane x 17 tangents", 1: "3 lanes x 6", 2: "2 lanes x 9", 3: "6 lanes x 3"}
+
+    def set_replay(self, shape=1):
+        """Shape of the pairs' reverse-step kernel (REPLAY_SHAPES); the gradients are bitwise the
+        same for every shape."""
+        self._check(self.lib.sqdem_adj_set_replay(self.h, int(shape)))
 
     def num_pairs(self):
         return int(self.lib.sqdem_adj_num_pairs(self.h))

@@ -832,13 +832,15 @@ __global__ void __launch_bounds__(64) k_bwd_contacts(Consts C, State S, StepOut 
 }
 
 // The same reverse step of a pair split over a group of GL lanes, lane l carrying the tangent
-// components TG*l .. TG*l+TG-1 of every replay (Dual<TG> values stay in registers, and the
-// longest Levenberg-Marquardt replay of a step costs about a forward evaluation per step of
-// its path instead of seventeen tangents' worth).  Every tangent component is computed by the
-// same operations as in k_bwd_contacts, so the results are bitwise the same.
-static const int TG = 3, GL = 6, GPW = 32 / GL;   // five groups per warp (lanes 30 and 31 idle)
+// components TG*l .. TG*l+TG-1 of every replay (TG*GL >= 17).  Each lane repeats the primal
+// evaluations (GL-fold work) but carries fewer tangents, so the longest Levenberg-Marquardt
+// replay of a step is shorter and the Dual<TG> values stay in registers.  Every tangent
+// component is computed by the same operations as in k_bwd_contacts, so the results are
+// bitwise the same for every shape.
 static const int GRP_WARPS = 4;
+template <int TG, int GL>
 __global__ void __launch_bounds__(32 * GRP_WARPS) k_bwd_contacts_grp(Consts C, State S, StepOut O, Adj A) {
+  constexpr int GPW = 32 / GL;
   __shared__ double shLin[GRP_WARPS * GPW][2 * NT];
   __shared__ double shGs[GRP_WARPS * GPW][NT];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -977,7 +979,7 @@ struct sqdem_adj {
   // the last forward window
   int nsteps = 0, every = 0;
   bool haveForward = false;
-  bool replayGrouped = true;   // pair replays split over lane groups (k_bwd_contacts_grp)
+  int replay = 1;   // reverse-step kernel of the pairs: 0 one thread per pair, 1.. lane-group shapes
   double loss = 0;
   unsigned long long counters[A_NCOUNT] = {};
   double msForward = 0, msBackward = 0;
@@ -1057,6 +1059,18 @@ static sqdem_status ensureTape(sqdem_adj* a, int K) {
   ACUDA(aalloc(a, &a->tapeCode, (size_t)K * a->P));
   a->tapeCap = K;
   return SQDEM_OK;
+}
+
+// shapes of the pairs' reverse step: 0 one thread (17 tangents), 1: 3 lanes x 6, 2: 2 lanes x 9,
+// 3: 6 lanes x 3
+static void launchReplay(sqdem_adj* a, const Consts& C, const State& S, const StepOut& O, const Adj& A) {
+  const int P = a->P, bs = 32 * GRP_WARPS;
+  switch (a->replay) {
+    case 0: k_bwd_contacts<<<nblk(P, 64), 64, 0, a->st>>>(C, S, O, A); break;
+    case 2: k_bwd_contacts_grp<9, 2><<<nblk(P, GRP_WARPS * 16), bs, 0, a->st>>>(C, S, O, A); break;
+    case 3: k_bwd_contacts_grp<3, 6><<<nblk(P, GRP_WARPS * 5), bs, 0, a->st>>>(C, S, O, A); break;
+    default: k_bwd_contacts_grp<6, 3><<<nblk(P, GRP_WARPS * 10), bs, 0, a->st>>>(C, S, O, A); break;
+  }
 }
 
 static void launchStep(sqdem_adj* a, const State& S, const StepOut& O, int step) {
@@ -1321,10 +1335,7 @@ sqdem_status sqdem_adj_backward(sqdem_adj* a, double* dL_deps, double* dL_dKn, d
       const State S = a->L.view(a->tapeState[t - t0]);
       const StepOut O = tapeOut(a, t - t0);
       k_bwd_integrate<<<nblk(n, 128), 128, 0, a->st>>>(C, S, O, A, t == nsteps - 1 ? 1 : 0);
-      if (P && a->replayGrouped)
-        k_bwd_contacts_grp<<<nblk(P, GRP_WARPS * GPW), 32 * GRP_WARPS, 0, a->st>>>(C, S, O, A);
-      else if (P)
-        k_bwd_contacts<<<nblk(P, 64), 64, 0, a->st>>>(C, S, O, A);
+      if (P) launchReplay(a, C, S, O, A);
       k_bwd_gather<<<nblk(n, 128), 128, 0, a->st>>>(C, A);
     }
     ACUDA(cudaGetLastError());
@@ -1389,9 +1400,9 @@ sqdem_status sqdem_adj_get_state(sqdem_adj* a, double* out16) {
 
 long sqdem_adj_num_pairs(sqdem_adj* a) { return a ? a->P : 0; }
 
-sqdem_status sqdem_adj_set_replay(sqdem_adj* a, int grouped) {
-  if (!a) return SQDEM_ERR_ARG;
-  a->replayGrouped = grouped != 0;
+sqdem_status sqdem_adj_set_replay(sqdem_adj* a, int shape) {
+  if (!a || shape < 0 || shape > 3) return SQDEM_ERR_ARG;
+  a->replay = shape;
   return SQDEM_OK;
 }
 

@@ -188,21 +188,22 @@ def test_adjoint_checkpoint_interval_changes_nothing(scene, window):
 
 
 @pytest.mark.gpu
-def test_grouped_and_single_thread_replays_agree_bitwise(scene, window):
+def test_replay_shapes_agree_bitwise(scene, window):
     spec, bodies, recs = scene
     eps, mu, Kn, Ks = params_of(spec)
     n = spec.n_bodies
     wF = lid_weights(n)
     wX = np.random.default_rng(3).normal(size=(n, 3)) * (spec.kind == 0)[:, None]
     res = []
-    for grouped in (True, False):
-        window.set_replay(grouped)
+    for shape in (0, 1, 2, 3):
+        window.set_replay(shape)
         _gpu_loss(window, spec, eps, mu, Kn, Ks, wF, wX)
         res.append(window.backward())
         assert window.report()["replay_mismatches"] == 0
-    window.set_replay(True)
-    for k in res[0]:
-        assert np.array_equal(res[0][k], res[1][k]), k
+    window.set_replay(1)
+    for r in res[1:]:
+        for k in r:
+            assert np.array_equal(res[0][k], r[k]), k
 
 
 @pytest.mark.gpu
