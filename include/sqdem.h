@@ -374,6 +374,10 @@ long sqdem_adj_num_pairs(sqdem_adj* adj);
 /* Pairs after the window, 16 doubles each: id1 id2 hasGeom depth contactAngle2 normal3
  * shearForce3, then the force on id1 in the last step (3) and whether it was applied. */
 sqdem_status sqdem_adj_get_pairs(sqdem_adj* adj, double* out16);
+/* Forward kernel of the pairs: cooperative = 1 (default) shares each Disfunction evaluation
+ * among six lanes (the independent pow calls of each level on separate lanes), 0 runs the
+ * pair on one thread.  Both give bitwise the same results. */
+sqdem_status sqdem_adj_set_forward(sqdem_adj* adj, int cooperative);
 /* Shape of the pairs' reverse-step kernel, which replays each pair's narrowphase and law in
  * dual numbers: 0 one thread per pair with all seventeen tangent components, 1 (default) three
  * lanes with six each, 2 two lanes with nine, 3 six lanes with three.  Every shape gives

@@ -123,6 +123,11 @@ class AdjointWindow:
         same for every shape."""
         self._check(self.lib.sqdem_adj_set_replay(self.h, int(shape)))
 
+    def set_forward(self, cooperative=True):
+        """Forward kernel of the pairs: six lanes share each evaluation (default) or one thread
+        per pair; the results are bitwise the same."""
+        self._check(self.lib.sqdem_adj_set_forward(self.h, 1 if cooperative else 0))
+
     def num_pairs(self):
         return int(self.lib.sqdem_adj_num_pairs(self.h))
 

@@ -147,6 +147,7 @@ __device__ __forceinline__ void nmStart(NMState& M, double a0, double a1, double
   M.p[1][0] += del;
   M.p[2][1] += del;
   M.nfunc = 0; M.touching = true; M.st = NM_V0;
+  M.ilo = 0; M.ihi = 0; M.inhi = 0; M.si = 0;   // set by the ranking after the first simplex
   M.q0 = M.p[0][0]; M.q1 = M.p[0][1];
 }
 __device__ __forceinline__ bool nmReturn(NMState& M) {
@@ -257,7 +258,9 @@ __device__ __forceinline__ double2 nmTryPoint(const double ps[2], const double p
 __device__ __forceinline__ int nmPlan(const NMState& M, double2* q, int S) {
   int n = 0;
   q[n++] = make_double2(M.q0, M.q1);
-  if (M.st == NM_V0 || M.st == NM_V1) {
+  if (M.st == NM_V0 || M.st == NM_V1 || M.st == NM_V2) {
+    // vertices of the first simplex still to be evaluated; after the third the next point
+    // depends on the ranking, which is not known yet
     for (int v = M.st + 1; v < 3 && n < S; v++) q[n++] = make_double2(M.p[v][0], M.p[v][1]);
     return n;
   }

@@ -150,6 +150,77 @@ __host__ __device__ __noinline__ void disfunction(const Shape<T>& A, const Shape
   center = 0.5 * (p1 + p2);
   if (val(dot(contact, d)) > 0) stop_flag = true;
 }
+// The Disfunction evaluation lmder2 calls: in sequence on one thread (every instantiation),
+// or by a group of six lanes of a warp (CoopEval, forward kernel only).
+struct SeqEval {
+  template <class T>
+  SQA_HD void operator()(const Shape<T>& A, const Shape<T>& B, const T& pa0, const T& pa1, V3<T>& center, V3<T>& p1,
+                         V3<T>& p2, bool& stop_flag) const {
+    disfunction(A, B, pa0, pa1, center, p1, p2, stop_flag);
+  }
+};
+
+// Disfunction by six lanes: lanes g0..g0+2 compute body A's support point, g0+3..g0+5 body
+// B's, each triple running the independent pow calls of one level of Normal2Phi + getSurface
+// on separate lanes (Y X W | t u v | Z | pc1 w), so that the dependency chain of one evaluation
+// is 4 pow + 2 atan2 + 4 sincos instead of 18 pow + 4 atan2 + 6 sincos.  Every value is the
+// result of the same operation on the same operands as in disfunction: bitwise the same.
+struct CoopEval {
+  unsigned mask;   // the group's six lanes
+  int g0, sub;     // first lane of the group, this lane's place in it
+#ifdef __CUDA_ARCH__
+  __device__ double pick(double v, int src) const { return __shfl_sync(mask, v, src); }
+  __device__ V3<double> support(const Shape<double>& s, const V3<double>& n, int part, int l0) const {
+    double b, e;
+    if (part == 0) { b = fabs(s.ry * n.y); e = s.i1; }
+    else if (part == 1) { b = fabs(s.rx * n.x); e = s.i1; }
+    else { b = fabs(s.rx * n.x); e = s.i2; }
+    const double r1 = pow(b, e);
+    const double Y = pick(r1, l0), X = pick(r1, l0 + 1), W = pick(r1, l0 + 2);
+    const double ph0 = atan2(tsgn(n.y) * Y, tsgn(n.x) * X);
+    double s0, c0;
+    sincos(ph0, &s0, &c0);
+    if (part == 0) { b = fabs(c0); e = s.a1; }
+    else if (part == 1) { b = fabs(c0); e = s.e1; }
+    else { b = fabs(s0); e = s.e1; }
+    const double r2 = pow(b, e);
+    const double t = pick(r2, l0), u = pick(r2, l0 + 1), v = pick(r2, l0 + 2);
+    const double Z = pow(fabs(s.rz * n.z * t), s.i2);
+    const double ph1 = atan2(tsgn(n.z) * Z, W);
+    double s1, c1;
+    sincos(ph1, &s1, &c1);
+    if (part == 1) { b = fabs(s1); e = s.e2; } else { b = fabs(c1); e = s.e2; }
+    const double r3 = pow(b, e);
+    const double pc1 = pick(r3, l0), w = pick(r3, l0 + 1);
+    V3<double> r;
+    r.x = tsgn(c0) * s.rx * u * pc1;
+    r.y = tsgn(s0) * s.ry * v * pc1;
+    r.z = tsgn(s1) * s.rz * w;
+    return r;
+  }
+#endif
+  SQA_HD void operator()(const Shape<double>& A, const Shape<double>& B, const double& pa0, const double& pa1,
+                         V3<double>& center, V3<double>& p1, V3<double>& p2, bool& stop_flag) const {
+#ifdef __CUDA_ARCH__
+    double sa0, ca0, sa1, ca1;
+    sincos(pa0, &sa0, &ca0);
+    sincos(pa1, &sa1, &ca1);
+    const V3<double> contact = mk<double>(ca0 * ca1, sa0 * ca1, sa1);
+    const int body = sub / 3, part = sub - 3 * body;
+    const Shape<double>& Sh = body ? B : A;
+    const V3<double> n = body ? (-1.0) * mulL(B.R, contact) : mulL(A.R, contact);
+    const V3<double> pt = mulG(Sh.R, support(Sh, n, part, g0 + 3 * body)) + Sh.pos;
+    p1 = mk<double>(pick(pt.x, g0), pick(pt.y, g0), pick(pt.z, g0));
+    p2 = mk<double>(pick(pt.x, g0 + 3), pick(pt.y, g0 + 3), pick(pt.z, g0 + 3));
+    const V3<double> d = p2 - p1;
+    center = 0.5 * (p1 + p2);
+    if (dot(contact, d) > 0) stop_flag = true;
+#else
+    disfunction(A, B, pa0, pa1, center, p1, p2, stop_flag);
+#endif
+  }
+};
+
 template <class T> SQA_HD void centerLine(const V3<T>& pos1, const V3<T>& pos2, T para[2]) {
   const V3<T> d0 = pos2 - pos1;
   para[0] = tatan2(d0.y, d0.x);
@@ -162,7 +233,8 @@ template <class T> struct LMOut { V3<T> p1, p2, center, contact; bool touching; 
 // lmder2 with opts {1, 1e-15, 1e-3, 1e-20}, itmax 50 (Superquadrics_Ig2.cpp:1057-1354).  The
 // Jacobian's re-evaluation at the current point (JacfunctionApp, :1033-1054) is not repeated:
 // its values equal the ones stored for that point and are overwritten by the two probes.
-template <class T> __host__ __device__ __noinline__ void lmder2(const Shape<T>& A, const Shape<T>& B, T p[2], LMOut<T>& o) {
+template <class T, class E = SeqEval>
+__host__ __device__ __noinline__ void lmder2(const Shape<T>& A, const Shape<T>& B, T p[2], LMOut<T>& o, const E& ev = E()) {
   const double ONE_THIRD = 0.3333333333333334;
   o.touching = true; o.evals = 1;
   bool stop_flag = false;
@@ -171,7 +243,7 @@ template <class T> __host__ __device__ __noinline__ void lmder2(const Shape<T>& 
   int nu = 2, stop = 0, k;
   V3<T> P1, P2, C;
   o.contact = zero3<T>();
-  disfunction(A, B, p[0], p[1], C, P1, P2, stop_flag);
+  ev(A, B, p[0], p[1], C, P1, P2, stop_flag);
   V3<T> pf = P2 - P1;
   T pfL2 = nrm(pf);
   if (!isfinite(val(pfL2))) stop = 7;
@@ -184,9 +256,9 @@ template <class T> __host__ __device__ __noinline__ void lmder2(const Shape<T>& 
     o.contact = mk<T>(c0 * c1, s0 * c1, s1);
     const double angle = val(dot(pf, o.contact)) / (val(nrm(pf)) * val(nrm(o.contact)));
     if (fabs(angle) > 0.95) { stop = 8; break; }
-    disfunction(A, B, p[0] + Dp0, p[1], C, P1, P2, stop_flag);
+    ev(A, B, p[0] + Dp0, p[1], C, P1, P2, stop_flag);
     const V3<T> f1 = P2 - P1;
-    disfunction(A, B, p[0], p[1] + Dp1, C, P1, P2, stop_flag);
+    ev(A, B, p[0], p[1] + Dp1, C, P1, P2, stop_flag);
     const V3<T> f2 = P2 - P1;
     o.evals += 2;
     const T J00 = (f1.x - pf.x) / Dp0, J10 = (f1.y - pf.y) / Dp0, J20 = (f1.z - pf.z) / Dp0;
@@ -211,7 +283,7 @@ template <class T> __host__ __device__ __noinline__ void lmder2(const Shape<T>& 
       if (DpL2 < 1e-5) { stop = 2; break; }
       const T q0 = p[0] + Dp0, q1 = p[1] + Dp1;
       if (DpL2 >= (val(pL2) + 1e-3) / (1e-12 * 1e-12)) { stop = 4; break; }
-      disfunction(A, B, q0, q1, C, P1, P2, stop_flag);
+      ev(A, B, q0, q1, C, P1, P2, stop_flag);
       o.evals++;
       const V3<T> pDp_f = P2 - P1;
       const T pDp_fL2 = nrm(pDp_f);
@@ -249,8 +321,9 @@ template <class T> struct Geom {
 
 // Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go (Superquadrics_Ig2.cpp:1880-2317),
 // non-sphere bodies, no periodic shift.
-template <class T>
-__host__ __device__ __noinline__ void geomSqSq(Geom<T>& g, bool isNew, double prevDepth, const T angIn[2], const Shape<T>& A, const Shape<T>& B) {
+template <class T, class E = SeqEval>
+__host__ __device__ __noinline__ void geomSqSq(Geom<T>& g, bool isNew, double prevDepth, const T angIn[2], const Shape<T>& A,
+                                               const Shape<T>& B, const E& ev = E()) {
   g.precomputed = false; g.evals = 0; g.calls = 0;
   T para[2];
   if (isNew) { g.isShearNew = true; centerLine(A.pos, B.pos, para); }
@@ -260,18 +333,18 @@ __host__ __device__ __noinline__ void geomSqSq(Geom<T>& g, bool isNew, double pr
   const double r_sum = A.rmax + B.rmax;
   if (val(nrm(A.pos - B.pos)) > r_sum) { g.isShearNew = true; return; }
   LMOut<T> o;
-  lmder2(A, B, para, o);
+  lmder2(A, B, para, o, ev);
   g.evals += o.evals; g.calls++;
   if ((isnan(val(para[0])) || isnan(val(para[1])) || 7 == o.stop) && o.touching) {
     centerLine(A.pos, B.pos, para);
-    lmder2(A, B, para, o);
+    lmder2(A, B, para, o, ev);
     g.evals += o.evals; g.calls++;
   }
   T pDepth = dot(o.p1 - o.p2, o.contact);
   if (o.touching && 10.0 * val(nrm(o.p2 - o.p1)) > A.rmax) {
     if (!isInside(A, vval(o.p2 - A.pos)) || !isInside(B, vval(o.p1 - B.pos))) {
       centerLine(A.pos, B.pos, para);
-      lmder2(A, B, para, o);
+      lmder2(A, B, para, o, ev);
       g.evals += o.evals; g.calls++;
       pDepth = dot(o.p1 - o.p2, o.contact);
     }
@@ -467,7 +540,7 @@ template <int N> struct Seeder<Dual<N>> { static SQA_HD Dual<N> s(double x, int 
 // orientation of id2, 11-12 eps of id1, 13-14 eps of id2, 15-16 the stored contact angles.
 // The position of id1 carries no tangent: the SQ-SQ outputs other than the contact point are
 // invariant under a common translation, which gives their derivatives with respect to it.
-template <class T> SQA_HD void pairGeom(const PairVals& p, Geom<T>& g, int base = 0) {
+template <class T, class E = SeqEval> SQA_HD void pairGeom(const PairVals& p, Geom<T>& g, int base = 0, const E& ev = E()) {
   typedef Seeder<T> Sd;
   const V3<T> X2 = mk<T>(Sd::s(p.x2.x, 0, base), Sd::s(p.x2.y, 1, base), Sd::s(p.x2.z, 2, base));
   T q2[4];
@@ -483,7 +556,7 @@ template <class T> SQA_HD void pairGeom(const PairVals& p, Geom<T>& g, int base 
     Shape<T> A;
     shapeInit(A, p.shp1, Sd::s(p.e1.x, 11, base), Sd::s(p.e1.y, 12, base), q1, lift<T>(p.x1));
     const T angIn[2] = {Sd::s(p.ang[0], 15, base), Sd::s(p.ang[1], 16, base)};
-    geomSqSq(g, p.isNew, p.prevDepth, angIn, A, B);
+    geomSqSq(g, p.isNew, p.prevDepth, angIn, A, B, ev);
   }
 }
 
@@ -491,7 +564,6 @@ template <class T> SQA_HD void pairGeom(const PairVals& p, Geom<T>& g, int base 
 // tangent component `base` of the pass on):
 // 0 depth, 1-3 normal, 4-6 contact point, 7-9 x1, 10-12 x2, 13-15 v1, 16-18 w1, 19-21 v2,
 // 22-24 w2, 25-27 previous normal, 28-30 previous shear force, 31 kn, 32 ks, 33 tan(phi).
-static const int NLAW = 34;
 template <class T> SQA_HD T lawSeed(double x, int i, int c0) { return Seeder<T>::s(x, i, c0); }
 template <class T> SQA_HD V3<T> lawSeed3(const V3<double>& v, int i, int c0) {
   return mk<T>(lawSeed<T>(v.x, i, c0), lawSeed<T>(v.y, i + 1, c0), lawSeed<T>(v.z, i + 2, c0));
@@ -521,11 +593,14 @@ SQA_HD unsigned long long branchHash(int item, int step, unsigned long long bits
 }
 
 // forward step of one pair (double)
-SQA_HD void fwdContact(const Consts& C, const State& S, const StepOut& O, int step, int c) {
+template <class E = SeqEval>
+SQA_HD void fwdContact(const Consts& C, const State& S, const StepOut& O, int step, int c, const E& ev = E(),
+                       bool writer = true) {
   PairVals p;
   loadPair(C, S, c, p);
   Geom<double> g;
-  pairGeom<double>(p, g);
+  pairGeom<double>(p, g, 0, ev);
+  if (!writer) return;
   int code = (g.precomputed ? CO_PRE : 0) | (p.isNew ? CO_NEW : 0) | (g.isShearNew ? CO_SHNEW : 0);
   if (g.angMode == 1) { code |= CO_ANG; S.angle[c] = make_double2(g.ang[0], g.ang[1]); }
   else if (g.angMode == 2) { code |= CO_ANG0; S.angle[c] = make_double2(0, 0); }
@@ -556,6 +631,20 @@ SQA_HD void fwdContact(const Consts& C, const State& S, const StepOut& O, int st
 __global__ void __launch_bounds__(128) k_fwd_contacts(Consts C, State S, StepOut O, int step) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c < C.P) fwdContact(C, S, O, step, c);
+}
+// The same with six lanes per pair (five pairs per warp, lanes 30 and 31 idle): each
+// Disfunction evaluation is shared by the group (CoopEval); the group's first lane writes.
+static const int COOP_WARPS = 4;
+__global__ void __launch_bounds__(32 * COOP_WARPS) k_fwd_contacts_coop(Consts C, State S, StepOut O, int step) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gw = lane / 6, sub = lane - 6 * gw;
+  const int c = (blockIdx.x * COOP_WARPS + warp) * 5 + gw;
+  if (gw >= 5 || c >= C.P) return;
+  CoopEval ev;
+  ev.mask = 0x3Fu << (6 * gw);
+  ev.g0 = 6 * gw;
+  ev.sub = sub;
+  fwdContact(C, S, O, step, c, ev, sub == 0);
 }
 
 // ForceContainer sum of one body over its pairs, in list order (NewtonIntegrator's view)
@@ -980,6 +1069,7 @@ struct sqdem_adj {
   int nsteps = 0, every = 0;
   bool haveForward = false;
   int replay = 1;   // reverse-step kernel of the pairs: 0 one thread per pair, 1.. lane-group shapes
+  bool coopForward = true;   // forward pairs on six-lane groups (k_fwd_contacts_coop)
   double loss = 0;
   unsigned long long counters[A_NCOUNT] = {};
   double msForward = 0, msBackward = 0;
@@ -1075,7 +1165,10 @@ static void launchReplay(sqdem_adj* a, const Consts& C, const State& S, const St
 
 static void launchStep(sqdem_adj* a, const State& S, const StepOut& O, int step) {
   const Consts C = consts(a);
-  k_fwd_contacts<<<nblk(a->P, 128), 128, 0, a->st>>>(C, S, O, step);
+  if (a->coopForward)
+    k_fwd_contacts_coop<<<nblk(a->P, COOP_WARPS * 5), 32 * COOP_WARPS, 0, a->st>>>(C, S, O, step);
+  else
+    k_fwd_contacts<<<nblk(a->P, 128), 128, 0, a->st>>>(C, S, O, step);
   k_fwd_integrate<<<nblk(a->nb, 128), 128, 0, a->st>>>(C, S, O, step);
 }
 
@@ -1399,6 +1492,13 @@ sqdem_status sqdem_adj_get_state(sqdem_adj* a, double* out16) {
 }
 
 long sqdem_adj_num_pairs(sqdem_adj* a) { return a ? a->P : 0; }
+
+sqdem_status sqdem_adj_set_forward(sqdem_adj* a, int cooperative) {
+  if (!a) return SQDEM_ERR_ARG;
+  a->coopForward = cooperative != 0;
+  a->haveForward = false;
+  return SQDEM_OK;
+}
 
 sqdem_status sqdem_adj_set_replay(sqdem_adj* a, int shape) {
   if (!a || shape < 0 || shape > 3) return SQDEM_ERR_ARG;

@@ -207,6 +207,28 @@ def test_replay_shapes_agree_bitwise(scene, window):
 
 
 @pytest.mark.gpu
+def test_cooperative_forward_is_bitwise_the_single_thread_one(scene, window):
+    spec, bodies, recs = scene
+    eps, mu, Kn, Ks = params_of(spec)
+    n = spec.n_bodies
+    wF = lid_weights(n)
+    wX = np.random.default_rng(5).normal(size=(n, 3)) * (spec.kind == 0)[:, None]
+    res = []
+    for coop in (True, False):
+        window.set_forward(coop)
+        L, sg = _gpu_loss(window, spec, eps, mu, Kn, Ks, wF, wX)
+        st = window.state()
+        g = window.backward()
+        assert window.report()["replay_mismatches"] == 0
+        res.append((L, sg, st, g))
+    window.set_forward(True)
+    (L0, s0, st0, g0), (L1, s1, st1, g1) = res
+    assert L0 == L1 and s0 == s1 and np.array_equal(st0, st1)
+    for k in g0:
+        assert np.array_equal(g0[k], g1[k]), k
+
+
+@pytest.mark.gpu
 def test_window_loss_torch_autograd(scene, window):
     torch = pytest.importorskip("torch")
     from sudodem_gb300.adjoint import window_loss
