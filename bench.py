@@ -447,8 +447,9 @@ def config3_start(args):
     """Start of the config-3 window on the GPU engine: the specimen deposited for
     --deposit-steps steps, the lid placed 0.05 mm above the highest particle's centre plus its
     largest half-axis and lowered at 0.05 m/s until its force has stayed above 0.5 N (about twice
-    the bed's weight) for ten checks in a row (100 steps apart), then given the compression
-    velocity 0.05/s x its height."""
+    the bed's weight) for ten checks in a row (100 steps apart); then every velocity is zeroed
+    (NewtonIntegrator.quiet_system_flag), the lid given the compression velocity 0.05/s x its
+    height, and the bed relaxed under it for --relax-steps steps."""
     from sudodem_gb300 import Engine, assemblies
     spec = assemblies.config3(seed=args.seed, n=args.particles)
     eng = Engine(device=0)
@@ -460,17 +461,26 @@ def config3_start(args):
     b[5, 7:10] = [0.0, 0.0, -0.05]
     eng.put_body_state(b)
     held, k = 0, 0
-    while held < 10 and k < 3000:
+    while held < 10 and k < 1000:
         eng.step(100)
         k += 1
         held = held + 1 if abs(eng.body_state()[5, 18]) > 0.5 else 0
     b = eng.body_state()
     height = float(b[5, 2] - b[4, 2])
     b[5, 7:10] = [0.0, 0.0, -0.05 * height]
+    eng.put_body_state(b)
+    eng.set_quiet(True)      # zeroes the lid's velocity too (every body's)
+    eng.step(1)
+    b = eng.body_state()
+    b[5, 7:10] = [0.0, 0.0, -0.05 * height]
+    eng.put_body_state(b)
+    eng.step(args.relax_steps)
+    b = eng.body_state()
     recs = eng.interactions(include_potential=True)
     eng.close()
     lid = recs[(recs[:, 0] == 5) | (recs[:, 1] == 5)]
-    return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_steps": 100 * k, "lid_height_m": height,
+    return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_steps": 100 * k, "relax_steps": args.relax_steps,
+                           "lid_height_m": height,
                            "lid_velocity_m_s": -0.05 * height, "lid_force_n": float(b[5, 18]),
                            "lid_pairs": int(len(lid)), "lid_pairs_touching": int(np.sum(lid[:, 4] > 0))}
 
@@ -622,6 +632,7 @@ def main():
     ap.add_argument("--particles", type=int, default=5000, help="config3: particles")
     ap.add_argument("--deposit-steps", type=int, default=60000, help="config3: deposition steps before the window")
     ap.add_argument("--fd-dirs", type=int, default=0, help="config3: finite-difference directions per parameter kind")
+    ap.add_argument("--relax-steps", type=int, default=3000, help="config3: steps of the bed under the slow lid before the window")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

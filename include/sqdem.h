@@ -379,9 +379,9 @@ sqdem_status sqdem_adj_get_pairs(sqdem_adj* adj, double* out16);
  * pair on one thread.  Both give bitwise the same results. */
 sqdem_status sqdem_adj_set_forward(sqdem_adj* adj, int cooperative);
 /* Shape of the pairs' reverse-step kernel, which replays each pair's narrowphase and law in
- * dual numbers: 0 one thread per pair with all seventeen tangent components, 1 (default) three
- * lanes with six each, 2 two lanes with nine, 3 six lanes with three.  Every shape gives
- * bitwise the same gradients. */
+ * dual numbers: 0 one thread per pair with all seventeen tangent components, 1 three lanes with
+ * six each, 2 two lanes with nine, 3 (default) six lanes with three.  Every shape gives bitwise
+ * the same gradients. */
 sqdem_status sqdem_adj_set_replay(sqdem_adj* adj, int shape);
 /* replay mismatches, Disfunction evaluations and LM calls of the forward run, pairs replayed,
  * forward ms, backward ms, steps, checkpoint interval */

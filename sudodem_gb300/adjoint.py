@@ -118,7 +118,7 @@ class AdjointWindow:
 
     REPLAY_SHAPES = {0: "1 lane x 17 tangents", 1: "3 lanes x 6", 2: "2 lanes x 9", 3: "6 lanes x 3"}
 
-    def set_replay(self, shape=1):
+    def set_replay(self, shape=3):
         """Shape of the pairs' reverse-step kernel (REPLAY_SHAPES); the gradients are bitwise the
         same for every shape."""
         self._check(self.lib.sqdem_adj_set_replay(self.h, int(shape)))

@@ -1068,7 +1068,7 @@ struct sqdem_adj {
   // the last forward window
   int nsteps = 0, every = 0;
   bool haveForward = false;
-  int replay = 1;   // reverse-step kernel of the pairs: 0 one thread per pair, 1.. lane-group shapes
+  int replay = 3;   // reverse-step kernel of the pairs: 0 one thread per pair, 1.. lane-group shapes
   bool coopForward = true;   // forward pairs on six-lane groups (k_fwd_contacts_coop)
   double loss = 0;
   unsigned long long counters[A_NCOUNT] = {};
@@ -1158,8 +1158,8 @@ static void launchReplay(sqdem_adj* a, const Consts& C, const State& S, const St
   switch (a->replay) {
     case 0: k_bwd_contacts<<<nblk(P, 64), 64, 0, a->st>>>(C, S, O, A); break;
     case 2: k_bwd_contacts_grp<9, 2><<<nblk(P, GRP_WARPS * 16), bs, 0, a->st>>>(C, S, O, A); break;
-    case 3: k_bwd_contacts_grp<3, 6><<<nblk(P, GRP_WARPS * 5), bs, 0, a->st>>>(C, S, O, A); break;
-    default: k_bwd_contacts_grp<6, 3><<<nblk(P, GRP_WARPS * 10), bs, 0, a->st>>>(C, S, O, A); break;
+    case 1: k_bwd_contacts_grp<6, 3><<<nblk(P, GRP_WARPS * 10), bs, 0, a->st>>>(C, S, O, A); break;
+    default: k_bwd_contacts_grp<3, 6><<<nblk(P, GRP_WARPS * 5), bs, 0, a->st>>>(C, S, O, A); break;
   }
 }
 
