@@ -448,8 +448,10 @@ def config3_start(args):
     --deposit-steps steps, the lid placed 0.05 mm above the highest particle's centre plus its
     largest half-axis and lowered at 0.05 m/s until its force has stayed above 0.5 N (about twice
     the bed's weight) for ten checks in a row (100 steps apart); then every velocity is zeroed
-    (NewtonIntegrator.quiet_system_flag), the lid given the compression velocity 0.05/s x its
-    height, and the bed relaxed under it for --relax-steps steps."""
+    (NewtonIntegrator.quiet_system_flag), the bed relaxed for --relax-steps steps under the lid
+    moving at the compression velocity 0.05/s x its height, and the lid kept moving at that
+    velocity until its force has stayed above 0.05 N for five checks in a row (the relaxed bed
+    settles below the lid: the window starts from a lid in quasi-static contact)."""
     from sudodem_gb300 import Engine, assemblies
     spec = assemblies.config3(seed=args.seed, n=args.particles)
     eng = Engine(device=0)
@@ -475,11 +477,17 @@ def config3_start(args):
     b[5, 7:10] = [0.0, 0.0, -0.05 * height]
     eng.put_body_state(b)
     eng.step(args.relax_steps)
+    held, k2 = 0, 0
+    while held < 5 and k2 < 400:
+        eng.step(100)
+        k2 += 1
+        held = held + 1 if abs(eng.body_state()[5, 18]) > 0.05 else 0
     b = eng.body_state()
     recs = eng.interactions(include_potential=True)
     eng.close()
     lid = recs[(recs[:, 0] == 5) | (recs[:, 1] == 5)]
     return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_steps": 100 * k, "relax_steps": args.relax_steps,
+                           "reload_steps": 100 * k2,
                            "lid_height_m": height,
                            "lid_velocity_m_s": -0.05 * height, "lid_force_n": float(b[5, 18]),
                            "lid_pairs": int(len(lid)), "lid_pairs_touching": int(np.sum(lid[:, 4] > 0))}
