@@ -478,7 +478,7 @@ def config3_start(args):
     eng.put_body_state(b)
     eng.step(args.relax_steps)
     held, k2 = 0, 0
-    while held < 5 and k2 < 400:
+    while held < 5 and k2 < args.reload_max:
         eng.step(100)
         k2 += 1
         held = held + 1 if abs(eng.body_state()[5, 18]) > 0.05 else 0
@@ -512,6 +512,10 @@ def run_ours_adjoint(args):
     npart = spec.n_particles
     wF = np.zeros((n, 3))
     wF[5, 2] = 1.0
+    wX = None
+    if args.loss_heights:   # plus the particles' mean final height
+        wX = np.zeros((n, 3))
+        wX[spec.kind == 0, 2] = 1.0 / npart
     w = AdjointWindow(0)
     w.load(spec, bodies, recs)
     eps0 = spec.shape5[:, 3:5].copy()
@@ -519,19 +523,19 @@ def run_ours_adjoint(args):
     Kn0, Ks0 = spec.materials["Kn"].copy(), spec.materials["Ks"].copy()
     # warm-up, and the shape of the pairs' reverse-step kernel timed on a short window (every
     # shape gives bitwise the same gradients): the fastest is kept
-    loss1, _ = w.forward(1, 1, wF, None)
+    loss1, _ = w.forward(1, 1, wF, wX)
     shapes = {}
     nt = min(args.window, 50)
     for shape in (1, 2, 3, 0):
         w.set_replay(shape)
-        w.forward(nt, min(args.checkpoint, nt), wF, None)
+        w.forward(nt, min(args.checkpoint, nt), wF, wX)
         w.backward()
         shapes[AdjointWindow.REPLAY_SHAPES[shape]] = w.report()["backward_ms"] / nt
     best = min(shapes, key=shapes.get)
     w.set_replay([k for k, v in AdjointWindow.REPLAY_SHAPES.items() if v == best][0])
     clocks = ClockSampler(0)
     clocks.start()
-    loss, sig = w.forward(args.window, args.checkpoint, wF, None)
+    loss, sig = w.forward(args.window, args.checkpoint, wF, wX)
     g = w.backward()
     clk = clocks.stop()
     rep = w.report()
@@ -544,7 +548,7 @@ def run_ours_adjoint(args):
     tkn = torch.tensor(Kn0, dtype=torch.float64, requires_grad=True)
     tks = torch.tensor(Ks0, dtype=torch.float64, requires_grad=True)
     t0 = time.perf_counter()
-    L = window_loss(w, te, tm, tkn, tks, args.window, args.checkpoint, wF, None)
+    L = window_loss(w, te, tm, tkn, tks, args.window, args.checkpoint, wF, wX)
     L.backward()
     e2e_s = time.perf_counter() - t0
     e2e = {"value": npart * args.window / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (2 * n + 3 * n) * 8 / args.window,
@@ -565,7 +569,7 @@ def run_ours_adjoint(args):
             for sgn in (1, -1):
                 w.set_materials(Kn0 + sgn * h * dKn, Ks0 + sgn * h * dKs, mu0 + sgn * h * dmu)
                 w.set_eps(eps0 + sgn * h * dE)
-                lv, sv = w.forward(args.window, args.checkpoint, wF, None)
+                lv, sv = w.forward(args.window, args.checkpoint, wF, wX)
                 vals.append(lv)
                 sigs.append(sv)
             f = (vals[0] - vals[1]) / (2 * h)
@@ -607,7 +611,8 @@ def run_ours_adjoint(args):
             "dtype": "f64", "data": "synthetic",
             "config": {"workload": "config3", "particles": npart, "bodies": n, "pairs": P, "window_steps": args.window,
                        "checkpoint_every": args.checkpoint, "parameters": {"eps": 2 * npart, "mu": n, "Kn": n, "Ks": n},
-                       "loss": "final lid normal force", "start": start,
+                       "loss": "final lid normal force" + (" + mean final particle height" if args.loss_heights else ""),
+                       "start": start,
                        "replay_shape": best, "replay_ms_per_step_by_shape": shapes,
                        "what": "particle-steps/s of forward + reverse window (one gradient)",
                        "l2": "state and tape larger than L2"},
@@ -640,6 +645,9 @@ def main():
     ap.add_argument("--particles", type=int, default=5000, help="config3: particles")
     ap.add_argument("--deposit-steps", type=int, default=60000, help="config3: deposition steps before the window")
     ap.add_argument("--fd-dirs", type=int, default=0, help="config3: finite-difference directions per parameter kind")
+    ap.add_argument("--reload-max", type=int, default=400,
+                    help="config3: at most this many 100-step checks while the lid reloads after the relaxation")
+    ap.add_argument("--loss-heights", action="store_true", help="config3: add the particles' mean final height to the loss")
     ap.add_argument("--relax-steps", type=int, default=3000, help="config3: steps of the bed under the slow lid before the window")
     args = ap.parse_args()
     if args.warmup < 3:
