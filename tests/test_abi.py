@@ -45,3 +45,17 @@ def test_engine_without_gpu_fails_loudly():
         pytest.skip("a GPU is present")
     with pytest.raises(_native.SqdemError):
         _native.Engine(device=0)
+
+
+def test_adjoint_without_gpu_fails_loudly():
+    import pytest
+    try:
+        import torch
+        has = torch.cuda.is_available()
+    except Exception:
+        has = False
+    if has:
+        pytest.skip("a GPU is present")
+    from sudodem_gb300.adjoint import AdjointWindow
+    with pytest.raises(_native.SqdemError):
+        AdjointWindow(0)
