@@ -463,7 +463,7 @@ def config3_start(args):
     b[5, 7:10] = [0.0, 0.0, -0.05]
     eng.put_body_state(b)
     held, k = 0, 0
-    while held < 10 and k < 1000:
+    while held < 10 and k < args.approach_max:
         eng.step(100)
         k += 1
         held = held + 1 if abs(eng.body_state()[5, 18]) > 0.5 else 0
@@ -645,6 +645,8 @@ def main():
     ap.add_argument("--particles", type=int, default=5000, help="config3: particles")
     ap.add_argument("--deposit-steps", type=int, default=60000, help="config3: deposition steps before the window")
     ap.add_argument("--fd-dirs", type=int, default=0, help="config3: finite-difference directions per parameter kind")
+    ap.add_argument("--approach-max", type=int, default=1000,
+                    help="config3: at most this many 100-step checks while the lid is lowered onto the bed")
     ap.add_argument("--reload-max", type=int, default=400,
                     help="config3: at most this many 100-step checks while the lid reloads after the relaxation")
     ap.add_argument("--loss-heights", action="store_true", help="config3: add the particles' mean final height to the loss")
