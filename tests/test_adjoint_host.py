@@ -1,0 +1,134 @@
+"""The adjoint's arithmetic on the host, against the oracle's frozen-pair window (no GPU).
+
+`tests/adjoint_host.cu` builds the __host__ __device__ functions that the CUDA kernels of
+`sqdem_adjoint.cu` run (geometry, law and integrator templates on double and on dual numbers,
+the per-pair and per-body reverse steps) for the host and runs a whole window with them.  With
+the host's libm on both sides the forward equals the oracle's bit for bit, and the reverse pass
+is checked against central differences of the oracle, as the GPU tests check the kernels.  Test
+infrastructure only: the package never loads this build.
+"""
+import ctypes as C
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from adjoint_scene import compressed_specimen, lid_weights, oracle_window, params_of
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libadjoint_host.so")
+SOURCES = [os.path.join(HERE, "adjoint_host.cu"), os.path.join(ROOT, "sudodem_gb300", "csrc", "sqdem_adjoint.cu"),
+           os.path.join(ROOT, "sudodem_gb300", "csrc", "sq_dual.cuh"), os.path.join(ROOT, "include", "sqdem.h")]
+NSTEPS = 60
+TOL = 1e-5
+
+
+def _nvcc():
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    return None
+
+
+@pytest.fixture(scope="module")
+def host():
+    nvcc = _nvcc()
+    if nvcc is None:
+        pytest.skip("nvcc is needed to build the host copy of the adjoint's functions")
+    if not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in SOURCES):
+        os.makedirs(BUILD, exist_ok=True)
+        cmd = [nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "--fmad=false",
+               "-diag-suppress", "1444", "-Xcompiler", "-Wno-deprecated-declarations", "-shared",
+               "-gencode", "arch=compute_103a,code=sm_103a", "-o", LIB + ".tmp", SOURCES[0]]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+        assert r.returncode == 0, r.stdout.decode(errors="replace")
+        os.replace(LIB + ".tmp", LIB)
+    lib = C.CDLL(LIB)
+    lib.adjh_run.restype = C.c_double
+    dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
+    lib.adjh_run.argtypes = [C.c_int, ip, dp, ip, ip, dp, C.c_long, dp, C.c_double, dp, C.c_double, C.c_int, dp, dp,
+                             dp, dp, C.c_int, dp, dp, dp, dp, dp, dp, dp, C.POINTER(C.c_ulonglong),
+                             C.POINTER(C.c_longlong)]
+    return lib
+
+
+def _run(lib, spec, bodies, recs, eps, mu, Kn, Ks, nsteps, wF, wX):
+    """(loss, signature, replay mismatches, gradients, final state) of the host window."""
+    n = spec.n_bodies
+    nm = len(Kn)
+
+    def d(a):
+        return np.ascontiguousarray(a, dtype=np.float64)
+
+    def i(a):
+        return np.ascontiguousarray(a, dtype=np.int32)
+
+    arrs = dict(kind=i(spec.kind), shape5=d(spec.shape5), was=i(spec.wall_axis_sense), mat=i(spec.mat),
+                st=d(bodies), recs=d(recs), g=d(spec.params["gravity"]), Kn=d(Kn), Ks=d(Ks), fa=d(np.arctan(mu)),
+                eps=d(eps), wF=d(wF), wX=d(wX))
+    gE, gKn, gKs, gMu, fin = np.zeros((n, 2)), np.zeros(nm), np.zeros(nm), np.zeros(nm), np.zeros((n, 16))
+    sig, mism = C.c_ulonglong(), C.c_longlong()
+    P = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    Q = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))  # noqa: E731
+    L = lib.adjh_run(n, Q(arrs["kind"]), P(arrs["shape5"]), Q(arrs["was"]), Q(arrs["mat"]), P(arrs["st"]),
+                     len(recs), P(arrs["recs"]), float(spec.params["dt"]), P(arrs["g"]),
+                     float(spec.params["damping"]), nm, P(arrs["Kn"]), P(arrs["Ks"]), P(arrs["fa"]), P(arrs["eps"]),
+                     int(nsteps), P(arrs["wF"]), P(arrs["wX"]), P(gE), P(gKn), P(gKs), P(gMu), P(fin), C.byref(sig),
+                     C.byref(mism))
+    return L, sig.value, mism.value, {"eps": gE, "Kn": gKn, "Ks": gKs, "mu": gMu}, fin
+
+
+@pytest.fixture(scope="module")
+def scene():
+    return compressed_specimen()
+
+
+def test_host_forward_is_the_oracles_bit_for_bit(host, scene):
+    spec, bodies, recs = scene
+    eps, mu, Kn, Ks = params_of(spec)
+    n = spec.n_bodies
+    wF, wX = lid_weights(n), np.zeros((n, 3))
+    for nsteps in (1, NSTEPS):
+        L, _, _, _, fin = _run(host, spec, bodies, recs, eps, mu, Kn, Ks, nsteps, wF, wX)
+        Lo, _, ob = oracle_window(spec, bodies, recs, eps, mu, Kn, Ks, nsteps, wF, wX)
+        assert L != 0
+        assert np.array_equal(fin[:, 0:3], ob[:, 0:3])
+        assert np.array_equal(fin[:, 7:10], ob[:, 7:10])
+        assert L == Lo
+
+
+def test_host_reverse_pass_matches_oracle_central_differences(host, scene):
+    spec, bodies, recs = scene
+    eps, mu, Kn, Ks = params_of(spec)
+    n = spec.n_bodies
+    wF, wX = lid_weights(n), np.zeros((n, 3))
+    L0, _, mism, gr, _ = _run(host, spec, bodies, recs, eps, mu, Kn, Ks, NSTEPS, wF, wX)
+    assert mism == 0
+    _, s0, _ = oracle_window(spec, bodies, recs, eps, mu, Kn, Ks, NSTEPS, wF, wX)
+    rng = np.random.default_rng(11)
+    part = (spec.kind == 0)[:, None]
+    checked = {}
+    for trial in range(4):
+        dirs = [("eps", (rng.normal(size=eps.shape) * eps * part, 0 * mu, 0 * Kn, 0 * Ks), 3e-8),
+                ("mu", (0 * eps, rng.normal(size=mu.shape) * mu, 0 * Kn, 0 * Ks), 3e-5),
+                ("Kn", (0 * eps, 0 * mu, rng.normal(size=Kn.shape) * Kn, 0 * Ks), 3e-5),
+                ("Ks", (0 * eps, 0 * mu, 0 * Kn, rng.normal(size=Ks.shape) * Ks), 3e-5)]
+        for name, (dE, dmu, dKn, dKs), h in dirs:
+            vals, sigs = [], []
+            for s in (1, -1):
+                Ls, ss, _ = oracle_window(spec, bodies, recs, eps + s * h * dE, mu + s * h * dmu, Kn + s * h * dKn,
+                                          Ks + s * h * dKs, NSTEPS, wF, wX)
+                vals.append(Ls)
+                sigs.append(ss)
+            if not (sigs[0] == sigs[1] == s0):
+                continue
+            fd = (vals[0] - vals[1]) / (2 * h)
+            ad = float(np.sum(gr["eps"] * dE) + np.sum(gr["mu"] * dmu) + np.sum(gr["Kn"] * dKn) +
+                       np.sum(gr["Ks"] * dKs))
+            assert abs(fd - ad) <= TOL * abs(ad), (name, trial, fd, ad)
+            checked[name] = checked.get(name, 0) + 1
+    assert all(checked.get(k, 0) >= 2 for k in ("eps", "mu", "Kn", "Ks")), checked
