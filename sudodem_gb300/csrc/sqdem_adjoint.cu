@@ -9,20 +9,22 @@
 // depth gate.  Ip2 is applied afresh to every pair at the start of the window, so the contact
 // stiffness and friction are functions of the current material parameters.
 //
-// Forward: one thread per pair runs the narrowphase (Levenberg-Marquardt restated one
+// Forward: a group of six lanes per pair runs the narrowphase (Levenberg-Marquardt restated one
 // evaluation after another, lmder2 Superquadrics_Ig2.cpp:1057-1354, with its restart rules
-// :2013-2053), precompute (Superquadrics.cpp:1030-1050) and the law (:1209-1361); one thread
-// per body gathers forces in a fixed order and integrates (NewtonIntegrator.cpp:99-304,
-// 391-429).  The state is checkpointed every `checkpoint_every` steps.
+// :2013-2053; each evaluation shared by the group), precompute (Superquadrics.cpp:1030-1050)
+// and the law (:1209-1361); one thread per body gathers forces in a fixed order and integrates
+// (NewtonIntegrator.cpp:99-304, 391-429).  The state is checkpointed every `checkpoint_every`
+// steps.
 //
 // Reverse: per segment between checkpoints (last first), the segment is recomputed from its
 // checkpoint with every step's state kept on a device tape, then the steps are reversed one by
 // one: (1) per body, the adjoint of the integrator (translation by hand, rotation by replaying
-// the leapfrog in dual numbers); (2) per pair, the geometry and the law replayed in dual numbers
-// from the taped state (the same double operations, hence the same branches: LM decisions,
-// contact gates, Coulomb cap, damping signs, taken as they were), contracted with the incoming
-// adjoints; (3) per body, a fixed-order gather of the pairs' contributions.  Parameter
-// adjoints accumulate per pair and are mapped to bodies and materials at the end.
+// the leapfrog in dual numbers); (2) per pair, on a group of lanes that share its tangent
+// components, the geometry and the law replayed in dual numbers from the taped state (the same
+// double operations, hence the same branches: LM decisions, contact gates, Coulomb cap, damping
+// signs, taken as they were), contracted with the incoming adjoints; (3) per body, a
+// fixed-order gather of the pairs' contributions.  Parameter adjoints accumulate per pair and
+// are mapped to bodies and materials at the end.
 //
 // Parameters: per-body exponents eps1, eps2 (the narrowphase shape; mass, inertia and r_max
 // keep the values the bodies were built with), per-material Kn, Ks and friction coefficient

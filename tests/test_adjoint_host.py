@@ -112,7 +112,7 @@ def test_host_reverse_pass_matches_oracle_central_differences(host, scene):
     rng = np.random.default_rng(11)
     part = (spec.kind == 0)[:, None]
     checked = {}
-    for trial in range(4):
+    for trial in range(5):   # 20 seeded directions, five per parameter kind
         dirs = [("eps", (rng.normal(size=eps.shape) * eps * part, 0 * mu, 0 * Kn, 0 * Ks), 3e-8),
                 ("mu", (0 * eps, rng.normal(size=mu.shape) * mu, 0 * Kn, 0 * Ks), 3e-5),
                 ("Kn", (0 * eps, 0 * mu, rng.normal(size=Kn.shape) * Kn, 0 * Ks), 3e-5),
@@ -131,4 +131,4 @@ def test_host_reverse_pass_matches_oracle_central_differences(host, scene):
                        np.sum(gr["Ks"] * dKs))
             assert abs(fd - ad) <= TOL * abs(ad), (name, trial, fd, ad)
             checked[name] = checked.get(name, 0) + 1
-    assert all(checked.get(k, 0) >= 2 for k in ("eps", "mu", "Kn", "Ks")), checked
+    assert all(checked.get(k, 0) >= 3 for k in ("eps", "mu", "Kn", "Ks")), checked
