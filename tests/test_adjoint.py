@@ -26,13 +26,13 @@ def scene():
 
 
 def _dirs(rng, spec, eps, mu, Kn, Ks):
-    n = spec.n_bodies
+    """One seeded direction per parameter kind with its finite-difference step."""
     part = (spec.kind == 0)[:, None]
     dE = rng.normal(size=eps.shape) * eps * part
     return [("eps", (dE, 0 * mu, 0 * Kn, 0 * Ks), H_EPS),
             ("mu", (0 * eps, rng.normal(size=mu.shape) * mu, 0 * Kn, 0 * Ks), H_SMOOTH),
             ("Kn", (0 * eps, 0 * mu, rng.normal(size=Kn.shape) * Kn, 0 * Ks), H_SMOOTH),
-            ("Ks", (0 * eps, 0 * mu, 0 * Kn, rng.normal(size=Ks.shape) * Ks), H_SMOOTH)][: 4 if n else 0]
+            ("Ks", (0 * eps, 0 * mu, 0 * Kn, rng.normal(size=Ks.shape) * Ks), H_SMOOTH)]
 
 
 def _ad(gr, d):
