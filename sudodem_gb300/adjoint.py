@@ -21,6 +21,21 @@ from . import _native
 from ._native import BODY_STRIDE, INTR_STRIDE, SqdemError, _dp, _ip, load_library
 
 
+def check_window_spec(spec):
+    """Raise ValueError for a scene the adjoint window does not model: a periodic cell, viscous
+    contact damping (betan/betas), the Hertz-Mindlin contact model, particles flagged as
+    spheres."""
+    if spec.info.get("periodic"):
+        raise ValueError("the adjoint window has no periodic cell")
+    if spec.info.get("contact_model", "linear") != "linear":
+        raise ValueError("the adjoint window differentiates the linear contact model only")
+    m = spec.materials
+    if np.any(np.asarray(m["betan"]) > 1e-5) or np.any(np.asarray(m["betas"]) > 1e-5):
+        raise ValueError("the adjoint window has no viscous contact damping (betan, betas must be 0)")
+    if np.any((np.asarray(spec.kind) == 0) & (np.asarray(spec.isSphere) != 0)):
+        raise ValueError("the adjoint window supports superquadrics not flagged as spheres")
+
+
 class AdjointWindow:
     """One scene's window on one GPU (no CPU fallback: raises without a device)."""
 
@@ -54,6 +69,7 @@ class AdjointWindow:
         """Window start: the bodies of ``spec`` (a SceneSpec) in ``state`` (n x 37, default the
         spec's), the interaction records ``interactions`` (m x 57, default none), the spec's
         dt, gravity and damping, its materials and exponents."""
+        check_window_spec(spec)
         n = spec.n_bodies
         st = np.ascontiguousarray(spec.state if state is None else state, dtype=np.float64).reshape(n, BODY_STRIDE)
         recs = np.zeros((0, INTR_STRIDE)) if interactions is None else interactions
@@ -205,5 +221,5 @@ def tan_friction(spec):
     return np.array([math.tan(a) for a in spec.materials["frictionAngle"]])
 
 
-__all__ = ["AdjointWindow", "window_loss", "wall_force_weights", "tan_friction"]
+__all__ = ["AdjointWindow", "check_window_spec", "window_loss", "wall_force_weights", "tan_friction"]
 _ = _native

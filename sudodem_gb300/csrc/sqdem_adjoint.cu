@@ -1236,6 +1236,8 @@ sqdem_status sqdem_adj_load(sqdem_adj* a, int n, const int* kind, const double* 
     const double* o = intr57 + (size_t)r * SQDEM_INTR_STRIDE;
     int i1 = (int)o[0], i2 = (int)o[1];
     if (i1 < 0 || i2 < 0 || i1 >= n || i2 >= n || i1 == i2) return afail(a, SQDEM_ERR_ARG, "pair with a bad body id");
+    if (o[44] != 0 || o[45] != 0 || o[46] != 0)
+      return afail(a, SQDEM_ERR_ARG, "pair across a periodic cell boundary: the adjoint window has no periodic cell");
     if (kind[i1] == SQDEM_WALL && kind[i2] == SQDEM_WALL) continue;
     if (kind[i1] == SQDEM_SUPERQUADRIC && kind[i2] == SQDEM_WALL) std::swap(i1, i2);
     a->ids.push_back(make_int2(i1, i2));

@@ -97,6 +97,29 @@ def test_oracle_window_is_differentiable_along_friction(scene):
     assert agreed >= 2
 
 
+def test_window_spec_checks_reject_unmodelled_scenes(scene):
+    import copy
+    from sudodem_gb300 import assemblies
+    from sudodem_gb300.adjoint import check_window_spec
+    spec = scene[0]
+    check_window_spec(spec)
+    bad = copy.deepcopy(spec)
+    bad.info["periodic"] = True
+    with pytest.raises(ValueError):
+        check_window_spec(bad)
+    bad = copy.deepcopy(spec)
+    bad.materials["betan"] = np.full(len(bad.materials["betan"]), 0.1)
+    with pytest.raises(ValueError):
+        check_window_spec(bad)
+    with pytest.raises(ValueError):
+        check_window_spec(assemblies.hertz_mindlin(assemblies.walled_lattice(8, seed=1)))
+    bad = copy.deepcopy(spec)
+    bad.isSphere = bad.isSphere.copy()
+    bad.isSphere[6] = 1
+    with pytest.raises(ValueError):
+        check_window_spec(bad)
+
+
 # ---------------------------------------------------------------------------- GPU
 @pytest.fixture(scope="module")
 def window(scene):
