@@ -241,11 +241,14 @@ sqdem_status sqdem_time_contacts(sqdem_ctx* ctx, int nrep, double* ms);
  * sqdem_time_contacts without its timing) that allocates nothing: its work queue is a fixed
  * static device array of SQDEM_STATIC_QUEUE_MAX ints (4 MiB per GPU, held until exit) instead
  * of a buffer owned by the context.  For callers that cannot call cudaMalloc at that point
- * (inside a stream capture, under a host framework that forbids raw allocations after
- * start-up).  Rejects tables larger than the array with SQDEM_ERR_CAPACITY.  The first call on
- * a device looks up the array's address (cudaGetSymbolAddress); make it before any stream
+ * (host frameworks that own device memory through their own pool and forbid raw allocations
+ * after start-up, loops that must not block in the allocator).  Rejects, with
+ * SQDEM_ERR_CAPACITY, a context whose contact-table capacity (contacts_per_body x particles)
+ * exceeds the array; the check reads only that host-side capacity.  The first call on a device
+ * looks up the array's address (cudaGetSymbolAddress) and keeps it; make it before any stream
  * capture.  Calls share the array, so calls that overlap on the GPU race.  Asynchronous on the
- * context stream.  No counterpart in the reference. */
+ * context stream, ordered after the work already queued there.  No counterpart in the
+ * reference. */
 #define SQDEM_STATIC_QUEUE_MAX (1 << 20)
 sqdem_status sqdem_contacts_static_queue(sqdem_ctx* ctx);
 

@@ -36,6 +36,7 @@
 #include <string>
 #include <algorithm>
 #include <limits>
+#include <mutex>
 #include "sq_device.cuh"
 #include "sq_hm.cuh"
 #include "../../include/sqdem.h"
@@ -3887,30 +3888,37 @@ sqdem_status sqdem_put_cell(sqdem_ctx* c, const double* o) {
 // ---------------------------------------------------------------------------
 // Contact stage without allocation.
 //
-// Some callers cannot call cudaMalloc at the point where they advance the contacts: code
-// running while a CUDA stream is being captured into a graph (allocation is not allowed
-// there), host frameworks that own all device memory through their own pool and forbid raw
-// allocations after start-up, or real-time loops that must not block in the allocator.  For
-// them this entry point runs one pass of the contact stage (pre-pass, Levenberg-Marquardt
-// kernel, contact physics and law) on the context's state with its work queue (scratch) in
+// Some callers cannot call cudaMalloc at the point where they advance the contacts: host
+// frameworks that own all device memory through their own pool and forbid raw allocations
+// after start-up, or real-time loops that must not block in the allocator.  For them this
+// entry point runs one pass of the contact stage (pre-pass, Levenberg-Marquardt kernel,
+// contact physics and law) on the context's state with its work queue (scratch) in
 // g_static_lm_queue instead of a buffer owned by the context.  It calls no cudaMalloc,
 // cudaFree or allocating library routine.
 //
 // Limits and rules:
-//  * at most SQDEM_STATIC_QUEUE_MAX (1,048,576) contact-table entries; larger tables are
-//    rejected with SQDEM_ERR_CAPACITY before anything is launched;
+//  * the context's contact table may hold at most SQDEM_STATIC_QUEUE_MAX (1,048,576)
+//    entries: a context created with a larger table capacity (contacts_per_body x particles)
+//    is rejected with SQDEM_ERR_CAPACITY before anything is launched.  The check reads only
+//    that host-side capacity, never the current table size on the device, so it cannot pass
+//    on a stale size while earlier work is still queued on the context stream; the queue
+//    never holds more entries than the table;
 //  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current); make that first call before any
-//    stream capture;
+//    cudaGetSymbolAddress (with that device current) and keeps it for later calls; make that
+//    first call before any stream capture.  A device reset (cudaDeviceReset) invalidates the
+//    kept address: do not use the library across one;
 //  * all calls share the one array, which keeps the last call's contents; nothing in it needs
 //    to start at zero (the queue counters live in the context and are reset by the call), but
 //    calls that overlap on the GPU (other streams or contexts at the same time) race on it;
-//  * the launches are asynchronous on the context stream, like sqdem_step.
+//  * the launches are asynchronous on the context stream, like sqdem_step, and ordered after
+//    the work already queued there.
+static std::mutex g_static_queue_mutex;
 static int* g_static_queue_addr[128];
 static bool g_static_queue_ready[128];
 
 static sqdem_status staticQueueAddress(sqdem_ctx* c, int** out) {
   if (c->device < 0 || c->device >= 128) return fail(c, SQDEM_ERR_ARG, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_static_queue_mutex);
   if (!g_static_queue_ready[c->device]) {
     CK(cudaSetDevice(c->device));
     int* ptr = nullptr;
@@ -3925,12 +3933,11 @@ static sqdem_status staticQueueAddress(sqdem_ctx* c, int** out) {
 sqdem_status sqdem_contacts_static_queue(sqdem_ctx* c) {
   if (!c) return SQDEM_ERR_ARG;
   if (!c->haveBodies) return fail(c, SQDEM_ERR_STATE, "bodies must be set before the contact stage");
+  if (c->d.Pcap > SQDEM_STATIC_QUEUE_MAX)
+    return fail(c, SQDEM_ERR_CAPACITY, "contact table capacity is " + std::to_string(c->d.Pcap) +
+                " entries; sqdem_contacts_static_queue handles at most " + std::to_string(SQDEM_STATIC_QUEUE_MAX) +
+                " (create the context with fewer contacts per body or fewer particles)");
   CK(cudaSetDevice(c->device));
-  int P = 0;
-  CK(cudaMemcpy(&P, (char*)c->d.S + offsetof(SceneState, P), sizeof(int), cudaMemcpyDeviceToHost));
-  if (P > SQDEM_STATIC_QUEUE_MAX)
-    return fail(c, SQDEM_ERR_CAPACITY, "contact table has " + std::to_string(P) +
-                " entries; sqdem_contacts_static_queue handles at most " + std::to_string(SQDEM_STATIC_QUEUE_MAX));
   int* queue = nullptr;
   sqdem_status st = staticQueueAddress(c, &queue);
   if (st) return st;

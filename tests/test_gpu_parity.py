@@ -299,7 +299,8 @@ def test_periodic_first_steps_pair_set_celldist_bitexact(gpu):
         assert np.array_equal(e2.body_state()[:, 22:33], orc.bodies()[:, 22:33])
         G, R = by_pair(e2.interactions(True)), by_pair(orc.interactions())
         # the GPU holds every image-overlapping pair; the oracle's circular insertion sort may
-        # transiently miss one, so compare on the oracle's pairs
+        # transiently miss one (a bound that wrapped down and moved back below the cell size is
+        # not compared with the other body's wrapped bound), so compare on the oracle's pairs
         missing = set(R) - set(G)
         assert not missing, [(k, R[k][2], R[k][4], R[k][44:47]) for k in missing]
         assert all(np.array_equal(G[k][44:47], R[k][44:47]) for k in R)
