@@ -44,6 +44,8 @@ def lib():
         "sqo_stats": (None, [v, C.POINTER(l)]), "sqo_max_velocity_sq": (d, [v]),
         "sqo_get_bodies": (None, [v, dp]), "sqo_set_bodies": (None, [v, dp]),
         "sqo_get_interactions": (None, [v, dp]), "sqo_set_interactions": (None, [v, l, dp]),
+        "sqo_get_margins": (None, [v, dp]),
+        "sqo_disfunction": (None, [dp, dp, dp, dp, dp, dp, d, d, dp, dp]),
         "sqo_get_scalars": (None, [v, dp]), "sqo_set_scalars": (None, [v, dp]),
         "sqo_rebuild_sorted_bounds": (None, [v]),
         "sqo_pair_geom": (i, [v, i, i, i, dp, dp]),
@@ -109,6 +111,17 @@ def hertz_mindlin(c1, c2, theta):
     out = np.zeros(4)
     lib().sqo_hertz_mindlin(_dp(a), _dp(b), float(theta), _dp(out))
     return tuple(out)
+
+
+def disfunction(shapeA, qA, posA, shapeB, qB, posB, pa0, pa1, margins=False):
+    """One FP64 Disfunction evaluation between two free superellipsoids: (p1, p2, stop_flag[,
+    margins])."""
+    out = np.zeros(7)
+    m = np.zeros(10)
+    a = [np.ascontiguousarray(x, dtype=np.float64) for x in (shapeA, qA, posA, shapeB, qB, posB)]
+    lib().sqo_disfunction(*[_dp(x) for x in a], float(pa0), float(pa1), _dp(out), _dp(m) if margins else None)
+    r = (out[0:3], out[3:6], bool(out[6]))
+    return r + (m,) if margins else r
 
 
 def normal2phi(shape5, n):
@@ -223,6 +236,17 @@ class OracleScene:
         out = np.zeros((max(n, 1), INTR_STRIDE))
         if n:
             self.L.sqo_get_interactions(self.h, _dp(out))
+        return out[:n]
+
+    def margins(self):
+        """Decision margins of the last step, one row per interaction (order of interactions()):
+        |c.(p2-p1)| (m), ||cos|-0.95|, |Dp-1e-5|/1e-5, |dF| (m), |J^T f - 1e-15|/1e-15, restart
+        distance, isInside distance, |depth| (m), smallest ill-conditioned trig value,
+        evaluations."""
+        n = self.L.sqo_num_interactions(self.h)
+        out = np.zeros((max(n, 1), 10))
+        if n:
+            self.L.sqo_get_margins(self.h, _dp(out))
         return out[:n]
 
     def set_interactions(self, recs):

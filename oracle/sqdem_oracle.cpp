@@ -174,12 +174,34 @@ static inline V3 sqSurface(const SQ& s, Real ph0, Real ph1) {
   r[2] = Sign(std::sin(ph1)) * s.rz * std::pow(std::fabs(std::sin(ph1)), s.eps2);
   return r;
 }
+// Margins of the decisions one pair's narrowphase and law took this step (minimum over every
+// evaluation / check of the pair):
+//  [0] |c.(p2-p1)| (m) of every Disfunction evaluation (stop_flag: c.d > 0)
+//  [1] ||cos| - 0.95| of every angle check (lmder2 stop 8)
+//  [2] |‖Dp‖ - 1e-5| / 1e-5 of every damped step (lmder2 stop 2)
+//  [3] |dF| (m) of every trial (accepted iff dF/dL > 0)
+//  [4] |‖J^T f‖inf - 1e-15| / 1e-15 (lmder2 stop 1)
+//  [5] |10 ‖p2-p1‖ - r_max| / r_max and [6] |isInside value - 1| of the restart rule
+//  [7] |PenetrationDepth - 1e-18| (m) at the law's contact gate
+//  [8] smallest |cos| of a surface angle next to an odd multiple of pi/2, or |sin| next to pi,
+//      in any evaluation (FP64 rounds the angle to ~1e-16 there: the support point's own
+//      rounding error grows as that value shrinks)
+//  [9] number of Disfunction evaluations
+static thread_local double* g_marg = nullptr;
+static inline void margMin(int k, double v) {
+  if (g_marg) { v = std::fabs(v); if (!(v >= g_marg[k])) g_marg[k] = v; }
+}
+
 // Superquadrics.cpp:269-307 (surface angles of the point whose outward normal is n, local frame)
 static inline void sqNormal2Phi(const SQ& s, const V3& n, Real& ph0, Real& ph1) {
   ph0 = std::atan2(Sign(n[1]) * std::pow(std::fabs(s.ry * n[1]), 1 / (2. - s.eps1)),
                    Sign(n[0]) * std::pow(std::fabs(s.rx * n[0]), 1 / (2. - s.eps1)));
   ph1 = std::atan2(Sign(n[2]) * std::pow(std::fabs(s.rz * n[2] * std::pow(std::fabs(std::cos(ph0)), 2. - s.eps1)), 1 / (2. - s.eps2)),
                    std::pow(std::fabs(s.rx * n[0]), 1 / (2. - s.eps2)));
+  if (g_marg) {
+    margMin(8, std::cos(ph0)); margMin(8, std::cos(ph1));
+    if (std::fabs(ph0) > 1.5707963267948966) margMin(8, std::sin(ph0));
+  }
 }
 // Superquadrics.cpp:258-266 (local, unnormalised outward normal at angles phi)
 static inline V3 sqNormal(const SQ& s, Real ph0, Real ph1) {
@@ -229,7 +251,12 @@ struct Interaction {
   Geom g; Phys p;
   long iterBorn; long linIx; int cellDist[3];
   bool sliding;         // the law capped the shear force at this step (Coulomb branch)
+  // Distance of this step's decisions from their thresholds (test instrumentation: lets a
+  // parity test tell contacts at a branch boundary, or evaluated where FP64 itself is
+  // ill-conditioned, from the rest).  Filled by the narrowphase and the law; see Margins.
+  double marg[10];
 };
+
 
 // InsertionSortCollider::Bounds (InsertionSortCollider.hpp:90-109)
 struct Bounds {
@@ -595,6 +622,7 @@ static inline void disfunction(const PairCtx& c, Real pa0, Real pa1, V3& center,
   V3 d = p2 - p1;
   center = 0.5 * (p1 + p2);
   if (dot(contact, d) > 0) stop_flag = true;
+  if (g_marg) { margMin(0, dot(contact, d)); g_marg[9] += 1; }
 }
 // JacfunctionApp (Superquadrics_Ig2.cpp:1033-1054): forward differences with step paraDelta
 static inline void jacApp(const PairCtx& c, Real pa0, Real pa1, const Real Dp[2], V3& center, V3& p1, V3& p2,
@@ -639,6 +667,7 @@ static void lmder2(const PairCtx& c, Real p[2], int itmax, V3& p1, V3& p2, V3& c
       contact[1] = std::sin(p[0]) * std::cos(p[1]);
       contact[2] = std::sin(p[1]);
       Real angle = dot(p_f, contact) / (norm(p_f) * norm(contact));
+      margMin(1, std::fabs(angle) - 0.95);
       if (std::fabs(angle) > 0.95) { stop = 8; break; }
     }
     Real J[3][2];
@@ -652,6 +681,7 @@ static void lmder2(const PairCtx& c, Real p[2], int itmax, V3& p1, V3& p2, V3& c
     jacTf[1] = J[0][1] * (-1.0 * p_f[0]) + (J[1][1] * (-1.0 * p_f[1]) + J[2][1] * (-1.0 * p_f[2]));
     jacTf_inf = (std::fabs(jacTf[0]) > std::fabs(jacTf[1]) ? std::fabs(jacTf[0]) : std::fabs(jacTf[1]));
     p_L2 = std::sqrt(p[0] * p[0] + p[1] * p[1]);
+    margMin(4, (jacTf_inf - eps1) / eps1);
     if (jacTf_inf <= eps1) { Dp_L2 = 0.0; stop = 1; break; }
     if (k == 0) {
       tmp = (jtj[0][0] > jtj[1][1] ? jtj[0][0] : jtj[1][1]);
@@ -665,6 +695,7 @@ static void lmder2(const PairCtx& c, Real p[2], int itmax, V3& p1, V3& p2, V3& c
       Dp[0] = (jacTf[0] * jtj[1][1] - jacTf[1] * jtj[0][1]) / n_a;
       Dp[1] = (jacTf[1] * jtj[0][0] - jacTf[0] * jtj[0][1]) / n_a;
       Dp_L2 = std::sqrt(Dp[0] * Dp[0] + Dp[1] * Dp[1]);
+      margMin(2, (Dp_L2 - 1e-5) / 1e-5);
       if (Dp_L2 < 1e-5) { stop = 2; break; }
       pDp[0] = p[0] + Dp[0]; pDp[1] = p[1] + Dp[1];
       if (Dp_L2 >= (p_L2 + eps2) / (EPSILON * EPSILON)) { stop = 4; break; }
@@ -674,6 +705,7 @@ static void lmder2(const PairCtx& c, Real p[2], int itmax, V3& p1, V3& p2, V3& c
       if (!std::isfinite(pDp_fL2)) { stop = 7; break; }
       dL = Dp[0] * (mu * Dp[0] + jacTf[0]) + Dp[1] * (mu * Dp[1] + jacTf[1]);
       dF = p_fL2 - pDp_fL2;
+      margMin(3, dF);
       tmp = dF / dL;
       if (tmp > 0.0) {
         tmp = 1.0 - std::pow(2 * tmp - 1., 3.);
@@ -769,6 +801,14 @@ static bool ig2SqSq(Scene& S, Interaction* I, const Body& b1, const Body& b2, co
       }
     }
     pDepth = dot(p1 - p2, contactNormal);
+    if (touching && g_marg) {
+      margMin(5, (10.0 * norm(p2 - p1) - A->r_max) / A->r_max);
+      if (10.0 * norm(p2 - p1) > A->r_max) {
+        V3 q = mul(A->loc, p2 - position1);
+        margMin(6, std::pow(std::pow(std::fabs(q[0] / A->rx), 2.0 / A->eps1) + std::pow(std::fabs(q[1] / A->ry), 2.0 / A->eps1),
+                            A->eps1 / A->eps2) + std::pow(std::fabs(q[2] / A->rz), 2.0 / A->eps2) - 1);
+      }
+    }
     if (touching) {
       if (10.0 * norm(p2 - p1) > A->r_max) {
         if (!(sqIsInside(*A, p2 - position1)) || !(sqIsInside(*B, p1 - position2))) {
@@ -885,6 +925,7 @@ static bool law(Scene& S, Interaction* I, V3* F, V3* T) {
     requestErase(I);
     return false;
   }
+  margMin(7, g.PenetrationDepth - 1E-18);
   if (!(g.PenetrationDepth > 1E-18)) { ph.normalForce = V3(); ph.shearForce = V3(); return true; }
   V3 normalForce = g.normal * g.PenetrationDepth * ph.kn;
   V3 shearForce1;
@@ -1310,10 +1351,14 @@ static void interactionLoop(Scene& S) {
       continue;
     }
     const long dc0 = S.tstats[tn].disCalls;
+    for (int k = 0; k < 9; k++) I->marg[k] = INFINITY;
+    I->marg[9] = 0;
+    g_marg = I->marg;
     if (b1.kind == KIND_WALL) ig2WallSq(S, I, b1, b2, shift2);
     else ig2SqSq(S, I, b1, b2, shift2, S.tstats[tn]);
     ip2(S, I);
     if (!law(S, I, S.fbuf[tn].data(), S.tbuf[tn].data())) requestErase(I);
+    g_marg = nullptr;
     if (S.frozenPairs) {
       // the decisions at which the map jumps: the Levenberg-Marquardt path (Disfunction calls);
       // the contact gate and the Coulomb cap are continuous and not recorded
@@ -1839,6 +1884,38 @@ int sqo_add_sq(void* h, double rx, double ry, double rz, double e1, double e2, i
   return (int)S->bodies.size() - 1;
 }
 
+// One Disfunction evaluation (Superquadrics_Ig2.cpp:622-687) between two free superellipsoids
+// given by shape (rx, ry, rz, eps1, eps2), orientation (w, x, y, z; normalised as
+// Superquadrics::setOrientation does) and centre; out = p1 (3), p2 (3), stop flag.  Also the
+// margins of Margins [0] and [8] when margOut is non-null (10 values).
+void sqo_disfunction(const double* shapeA5, const double* qA, const double* posA, const double* shapeB5,
+                     const double* qB, const double* posB, double pa0, double pa1, double* out, double* margOut) {
+  SQ sq[2];
+  const double* sh[2] = {shapeA5, shapeB5};
+  const double* qq[2] = {qA, qB};
+  for (int k = 0; k < 2; k++) {
+    std::memset(&sq[k], 0, sizeof(SQ));
+    sq[k].rx = sh[k][0]; sq[k].ry = sh[k][1]; sq[k].rz = sh[k][2]; sq[k].eps1 = sh[k][3]; sq[k].eps2 = sh[k][4];
+    sqInitial(sq[k]);
+    Quat o{qq[k][0], qq[k][1], qq[k][2], qq[k][3]};
+    qnormalize(o);
+    sq[k].loc = toRot(conj(o)); sq[k].glob = toRot(o);
+  }
+  long calls = 0;
+  PairCtx c{&sq[0], &sq[1], V3(posA[0], posA[1], posA[2]), V3(posB[0], posB[1], posB[2]), &calls};
+  double marg[10];
+  for (int k = 0; k < 9; k++) marg[k] = INFINITY;
+  marg[9] = 0;
+  if (margOut) g_marg = marg;
+  V3 center, p1, p2;
+  bool stop = false;
+  disfunction(c, pa0, pa1, center, p1, p2, stop);
+  g_marg = nullptr;
+  for (int k = 0; k < 3; k++) { out[k] = p1[k]; out[3 + k] = p2[k]; }
+  out[6] = stop ? 1 : 0;
+  if (margOut) for (int k = 0; k < 10; k++) margOut[k] = marg[k];
+}
+
 void sqo_set_params(void* h, double dt, const double* gravity, double damping, double verletDist, int targetInterv,
                     double minSweepDistFactor, int sortAxis) {
   Scene* S = (Scene*)h;
@@ -1960,6 +2037,13 @@ void sqo_get_interactions(void* h, double* out) {
     o[47] = g.curvatures1[0]; o[48] = g.curvatures1[1]; o[49] = g.curvatures2[0]; o[50] = g.curvatures2[1];
     o[51] = g.curvatureAngle; o[52] = g.alpha; o[53] = g.K; o[54] = g.E; o[55] = g.curvatures_sum; o[56] = g.isSphere ? 1 : 0;
   }
+}
+// Decision margins of the last step (Margins above), one row of 10 per interaction in the
+// order of sqo_get_interactions.
+void sqo_get_margins(void* h, double* out) {
+  Scene* S = (Scene*)h;
+  for (size_t i = 0; i < S->lin.size(); i++)
+    for (int k = 0; k < 10; k++) out[i * 10 + k] = S->lin[i]->marg[k];
 }
 // Replace the whole interaction container by the given records (same layout); the
 // functor cache is rebuilt as the InteractionLoop would have left it.

@@ -9,9 +9,7 @@ import os
 import numpy as np
 
 from . import build as _build
-
-BODY_STRIDE = 37
-INTR_STRIDE = 57
+from .shapes import BODY_STRIDE, INTR_STRIDE  # noqa: F401
 NSCALARS = 9
 
 SQDEM_SUPERQUADRIC = 0

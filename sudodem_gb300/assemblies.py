@@ -15,9 +15,9 @@ import math
 
 import numpy as np
 
-from . import _native
+from .shapes import BODY_STRIDE, shape_props
 
-BODY_STRIDE = _native.BODY_STRIDE
+_shape_props = shape_props
 
 
 @dataclass
@@ -69,7 +69,7 @@ def _add_wall(b, pos, axis, sense, mat=0):
 
 
 def _add_sq(b, rxyz, eps, q, pos, density, mat=0, isSphere=0, props_cache=None):
-    props = _native.shape_props(rxyz[0], rxyz[1], rxyz[2], eps[0], eps[1])
+    props = np.asarray(_shape_props(rxyz[0], rxyz[1], rxyz[2], eps[0], eps[1]))
     st = np.zeros(BODY_STRIDE)
     st[0:3] = pos
     st[3:7] = q
@@ -97,12 +97,22 @@ def default_material(kn=1e5, ks_over_kn=0.5, friction=0.5, density=2650.0):
             "betas": [0.0], "density": [density]}
 
 
-def critical_dt(spec, factor=0.5):
-    """dt = factor * sqrt(m_min / kn).  The reference has no superquadric critical-dt routine
-    (GlobalStiffnessTimeStepper handles ScGeom only)."""
-    m = spec.state[spec.kind == 0, 33]
-    kn = float(np.max(spec.materials["Kn"]))
-    return factor * math.sqrt(float(np.min(m)) / kn)
+def critical_dt(spec, factor=0.5, k=None):
+    """dt = factor * min over particles of min(sqrt(m / k), sqrt(I_min / (k r_max^2))), k = the
+    largest Kn.  The reference has no superquadric critical-dt routine (GlobalStiffnessTimeStepper
+    handles ScGeom only).  The rotational term is the period scale of a particle turning about its
+    axis of least inertia against a contact spring at its bounding radius: for elongated or
+    pointed superellipsoids (eps near 2, aspect ratios up to 1.5) it is 2-5 times shorter than the
+    translational sqrt(m / k), and a step above it lets those particles spin up without bound in
+    dense packings (the kinetic energy grows until the packing becomes a hot gas)."""
+    part = spec.kind == 0
+    m = spec.state[part, 33]
+    inertia = np.min(spec.state[part, 34:37], axis=1)
+    rmax = np.array([shape_props(*s)[4] for s in spec.shape5[part]])
+    kk = float(np.max(spec.materials["Kn"])) if k is None else float(k)
+    trans = float(np.min(np.sqrt(m / kk)))
+    rot = float(np.min(np.sqrt(inertia / (kk * rmax ** 2))))
+    return factor * min(trans, rot)
 
 
 def walled_lattice(n_particles, seed=0, r_range=(0.8e-3, 1.2e-3), eps_range=(0.5, 1.5), spacing=2.6e-3,
@@ -217,7 +227,7 @@ def periodic_cell(n_particles, seed=0, solid_fraction=0.3, r_range=(0.8e-3, 1.2e
     r = rng.uniform(r_range[0], r_range[1], size=(n_particles, 3))
     eps = rng.uniform(eps_range[0], eps_range[1], size=(n_particles, 2))
     q = random_quaternions(rng, n_particles)
-    vol = np.array([_native.shape_props(*r[p], *eps[p])[0] for p in range(n_particles)])
+    vol = np.array([_shape_props(*r[p], *eps[p])[0] for p in range(n_particles)])
     L = (vol.sum() / solid_fraction) ** (1.0 / 3.0)
     m = int(math.ceil(n_particles ** (1.0 / 3.0)))
     spacing = L / m
@@ -371,7 +381,8 @@ def hertz_mindlin(spec, G=2e8, nu=0.3, dt_factor=0.5, overlap=0.05):
     {G, nu}, Ip2_SuperquadricsMat2_SuperquadricsMat2_HertzMindlinPhys, SuperquadricsLaw2).
     Walls (ids 0-5) keep the linear Kn, Ks of their material, as Ip2 gives them.  dt is
     dt_factor * sqrt(m_min / k), k the larger of the wall Kn and the Hertz normal stiffness
-    8/3 Gab sqrt(depth R) of the smallest particle pair at the given relative overlap."""
+    8/3 Gab sqrt(depth R) of the smallest particle pair at the given relative overlap (with the
+    rotational term of critical_dt)."""
     m = dict(spec.materials)
     nm = len(m["Kn"])
     m["G"] = np.full(nm, float(G))
@@ -386,6 +397,5 @@ def hertz_mindlin(spec, G=2e8, nu=0.3, dt_factor=0.5, overlap=0.05):
     r_eff = 0.5 * rmin
     k_hm = 8.0 / 3.0 * gab * math.sqrt(overlap * rmin * r_eff)
     k = max(k_hm, float(np.max(m["Kn"])))
-    mmin = float(np.min(spec.state[sq, 33]))
-    out.params["dt"] = dt_factor * math.sqrt(mmin / k)
+    out.params["dt"] = critical_dt(spec, dt_factor, k=k)
     return out

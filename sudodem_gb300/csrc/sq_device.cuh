@@ -12,7 +12,7 @@
 namespace sqdem {
 
 struct D3 { double x, y, z; };
-__device__ __forceinline__ D3 d3(double a, double b, double c) { D3 r; r.x = a; r.y = b; r.z = c; return r; }
+__host__ __device__ __forceinline__ D3 d3(double a, double b, double c) { D3 r; r.x = a; r.y = b; r.z = c; return r; }
 __device__ __forceinline__ D3 operator+(D3 a, D3 b) { return d3(a.x + b.x, a.y + b.y, a.z + b.z); }
 __device__ __forceinline__ D3 operator-(D3 a, D3 b) { return d3(a.x - b.x, a.y - b.y, a.z - b.z); }
 __device__ __forceinline__ D3 operator-(D3 a) { return d3(-a.x, -a.y, -a.z); }
@@ -39,7 +39,7 @@ __device__ __forceinline__ double fmin_ref(double a, double b) { return (b < a) 
 // R^T = conj(q).toRotationMatrix() (rot_mat2local) on the shape; both are bit-identical
 // to what is built here from the same quaternion, so only R is kept.
 struct Rot { double m[9]; };
-__device__ __forceinline__ Rot quatToRot(double w, double x, double y, double z) {
+__host__ __device__ __forceinline__ Rot quatToRot(double w, double x, double y, double z) {
   const double tx = 2.0 * x, ty = 2.0 * y, tz = 2.0 * z;
   const double twx = tx * w, twy = ty * w, twz = tz * w;
   const double txx = tx * x, txy = ty * x, txz = tz * x;
@@ -71,7 +71,7 @@ struct SqShape {
   Rot R;
   D3 pos;
 };
-__device__ __forceinline__ void shapeInit(SqShape& s, double rx, double ry, double rz, double e1, double e2,
+__host__ __device__ __forceinline__ void shapeInit(SqShape& s, double rx, double ry, double rz, double e1, double e2,
                                           double rmax) {
   s.rx = rx; s.ry = ry; s.rz = rz; s.e1 = e1; s.e2 = e2; s.rmax = rmax;
   s.a1 = 2. - e1; s.a2 = 2. - e2;

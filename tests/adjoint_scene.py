@@ -10,8 +10,8 @@ import oracle as O
 from sudodem_gb300 import assemblies
 
 
-def compressed_specimen(n=27, seed=2, relax=20000, v_lid=0.1, mu_range=(0.3, 0.7)):
-    """(spec, bodies, interactions): n superellipsoids deposited for `relax` steps in an 8.2 mm
+def compressed_specimen(n=27, seed=2, relax_time=0.067, v_lid=0.1, mu_range=(0.3, 0.7)):
+    """(spec, bodies, interactions): n superellipsoids deposited for `relax_time` seconds in an 8.2 mm
     box, then a lid moving down at v_lid (m/s) until it has carried a force for 200 steps in a
     row; per-body materials with friction coefficients uniform in mu_range."""
     spec = assemblies.walled_lattice(n, seed=seed, spacing=2.6e-3, per_side=3, box=8.2e-3, lid_height=0.2)
@@ -26,14 +26,14 @@ def compressed_specimen(n=27, seed=2, relax=20000, v_lid=0.1, mu_range=(0.3, 0.7
     b = o.bodies()
     b[6:, 2] -= 0.7e-3
     o.set_bodies(b)
-    o.step(relax)
+    o.step(int(round(relax_time / spec.params["dt"])))
     b = o.bodies()
     part = spec.kind == 0
     b[5, 2] = np.max(b[part, 2] + np.max(spec.shape5[part, 0:3], axis=1)) + 0.05e-3
     b[5, 7:10] = [0.0, 0.0, -v_lid]
     o.set_bodies(b)
     held = 0
-    for _ in range(3000):
+    for _ in range(int(round(0.1 / (10 * spec.params["dt"])))):   # at most 0.1 s of lid travel
         o.step(10)
         held = held + 1 if abs(o.bodies()[5, 18]) > 1e-3 else 0
         if held == 20:

@@ -5,7 +5,7 @@ import re
 import numpy as np
 
 import oracle as O
-from sudodem_gb300 import _native, build
+from sudodem_gb300 import _native, build, shapes
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -31,7 +31,19 @@ def test_shape_props_host_helper_matches_oracle_bitwise():
         s = [*rng.uniform(0.5e-3, 2e-3, 3), *rng.uniform(0.2, 1.8, 2)]
         a = _native.shape_props(*s)
         b = O.shape_props(*s)
+        c = np.asarray(shapes.shape_props(*s))
         assert np.array_equal(a, b)
+        assert np.array_equal(a, c)
+
+
+def test_building_inputs_loads_no_native_library():
+    """Scene generation (the inputs of every benchmark arm) must not map libsqdem_gpu.so."""
+    import subprocess
+    import sys
+    code = ("import sudodem_gb300.assemblies as a; a.periodic_cell(50, seed=1); a.walled_lattice(40, seed=2); "
+            "import sys; print(any(n.endswith('libsqdem_gpu.so') for n in open('/proc/self/maps').read().split()))")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, check=True)
+    assert out.stdout.strip() == "False", out.stdout + out.stderr
 
 
 def test_engine_without_gpu_fails_loudly():

@@ -23,7 +23,13 @@ ID1, ID2, REAL, KN, FN, FS, CD = 0, 1, 2, 23, slice(26, 29), slice(29, 32), slic
 
 
 def specimen(n=120, seed=3, **kw):
+    # These tests check the engine's bookkeeping (gains, clamps, iteration schedules) over a few
+    # hundred steps whose schedules were written for dt = 0.5 sqrt(m_min / kn), the translational
+    # step without the rotational term of critical_dt; over so few steps the rotational
+    # instability that term prevents does not develop.
     spec = assemblies.cubic_specimen(n, seed=seed, **kw)
+    part = spec.kind == 0
+    spec.params["dt"] = 0.5 * float(np.sqrt(np.min(spec.state[part, 33]) / np.max(spec.materials["Kn"])))
     return spec, OracleScene.from_spec(spec, threads=2)
 
 
@@ -50,14 +56,15 @@ def test_first_run_gains_are_alpha_area_over_wall_stiffness():
     got = [st["gain_x"], st["gain_x1"], st["gain_y"], st["gain_y1"], st["gain_z"], st["gain_z1"]]
     for g, w in zip(got, want):
         assert g == pytest.approx(w, rel=1e-12) or (math.isinf(g) and math.isinf(w))
-    vols = [assemblies._native.shape_props(*spec.shape5[k])[0] for k in range(6, len(spec.kind))]
+    vols = [assemblies.shape_props(*spec.shape5[k])[0] for k in range(6, len(spec.kind))]
     assert st["particlesVolume"] == pytest.approx(sum(vols), rel=1e-14)
 
 
 def test_consolidation_moves_walls_inward_toward_the_goal():
     spec, o = specimen(n=150, seed=5)
     o.set_servo(servo_config(goalx=1e5, goaly=1e5, goalz=1e5, max_vel=1.0, iterate_num_max=20))
-    o.step(400)
+    nsteps = 400
+    o.step(nsteps)
     st = state_dict(o.servo_state())
     b = o.bodies()
     box = spec.info["box"]
@@ -65,7 +72,7 @@ def test_consolidation_moves_walls_inward_toward_the_goal():
     assert st["width"] < box[0] and st["height"] < box[2]
     assert st["wsxx"] > 0 and st["wsyy"] > 0 and st["wszz"] > 0
     # each wall moved at most max_vel*dt per step
-    assert b[0, 0] <= 400 * 1.0 * spec.params["dt"] * (1 + 1e-12)
+    assert b[0, 0] <= nsteps * 1.0 * spec.params["dt"] * (1 + 1e-12)
 
 
 def test_wall_step_is_gain_times_stress_error_clamped():
