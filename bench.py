@@ -31,15 +31,30 @@ BYTES_PER_BODY = 216
 BYTES_PER_PAIR = 108 + 148
 
 
+TILE = os.path.join(ROOT, "tests", "golden", "config1_tile.npz")
+DEFAULT_WORKLOAD = "config1_dense"
+# force-error bar of the mixed form (per touching contact, relative error of normal + shear force
+# after one step from identical states, against the FP64 oracle)
+MIXED_TOL, MIXED_FRAC = 1e-6, 0.999
+
+
 def workload_spec(name, seed):
     from sudodem_gb300 import assemblies
+    if name == "config1_dense":
+        # the dense end of config 1: 200,000 superellipsoids (half-axes U[0.8,1.2] mm, eps U[0.3,1.8])
+        # in a periodic cell at 100 kPa mean stress (5^3 copies of a 1,600-particle cell the oracle
+        # compressed under config 1's isotropic loading), still under velGrad = -1/s I
+        return assemblies.config1_dense(TILE, tiles=5)
+    if name.startswith("config1_dense_t"):
+        return assemblies.config1_dense(TILE, tiles=int(name[15:]))
     if name == "sq200k_walled":
         # 200,000 superellipsoids with the size distribution of the plain-vs-mixed config
         # (half-axes U[0.8,1.2] mm, eps1/eps2 U[0.3,1.8]) deposited in a walled box.
         return assemblies.deposition_box(200_000, seed=seed, eps_range=(0.3, 1.8))
-    if name == "config1":
-        # 200,000 superellipsoids, half-axes U[0.8,1.2] mm, eps U[0.3,1.8], periodic cell at
-        # solid fraction 0.3 under isotropic strain-controlled compression (velGrad = -1/s I)
+    if name in ("config1", "config1_loose"):
+        # the start of config 1: 200,000 superellipsoids, half-axes U[0.8,1.2] mm, eps U[0.3,1.8],
+        # jittered lattice in a periodic cell at solid fraction 0.3 under isotropic
+        # strain-controlled compression (velGrad = -1/s I)
         return assemblies.config1(seed=seed)
     if name.startswith("config1_n"):
         return assemblies.periodic_cell(int(name[9:]), seed=seed)
@@ -273,7 +288,7 @@ def run_reference(args):
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": n, "warmup": args.warmup,
             "ms_per_step": 1e3 * el / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": args.workload, "particles": spec.n_particles, "precision": "fp64"},
+            "config": workload_config(args.workload, spec),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{n} timesteps of the full workload (time budget {budget:.0f} s)"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -289,7 +304,8 @@ def run_ours_batch(args):
     sizes = [sp.n_particles for sp in specs]
     mine = rank_share(sizes, rank, ws)
     my_specs = [specs[i] for i in mine]
-    b = Batch(len(my_specs), device=0, precision=args.precision, contacts_per_body=args.contacts_per_body)
+    precision = "fp64" if args.precision == "both" else args.precision
+    b = Batch(len(my_specs), device=0, precision=precision, contacts_per_body=args.contacts_per_body)
     for e in b.scenes:
         e.set_lm_spread(not args.no_lm_spread)
     b.load(my_specs, servo=servo)
@@ -340,10 +356,10 @@ def run_ours_batch(args):
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "strong",
-                "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+                "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "f32+f64",
                 "data": "synthetic",
                 "config": {"workload": args.workload, "specimens": len(specs), "particles": total_particles,
-                           "particles_rank0": npart, "table_entries_rank0": nentries, "precision": args.precision,
+                           "particles_rank0": npart, "table_entries_rank0": nentries, "precision": precision,
                            "parallelism": "specimens sharded across ranks (balanced particle counts)",
                            "engine": "CompressionEngine shear phase, lateral walls at 100 kPa",
                            "l2": f"inputs larger than L2: {nentries} table entries x >= 256 B on rank 0"},
@@ -352,29 +368,54 @@ def run_ours_batch(args):
         print(json.dumps(line))
 
 
-def run_ours(args):
-    if args.workload.startswith("config2"):
-        return run_ours_batch(args)
-    rank, ws, dist = dist_setup()
+def workload_config(name, spec):
+    """The workload's description, the same dict in both arms (nothing measured in it)."""
+    cfg = {"workload": name, "particles": spec.n_particles, "bodies": spec.n_bodies,
+           "contact_model": spec.info.get("contact_model", "linear"), "parallelism": "replicas",
+           "periodic": bool(spec.info.get("periodic", False)),
+           "l2": f"inputs larger than L2: {spec.n_bodies} bodies x 256 B of state + a contact table of "
+                 f"~6-12 entries per particle x 256 B, well above 129 MB"}
+    if name == "config1_dense":
+        cfg["state"] = (f"periodic cell of 5^3 copies of a 1,600-particle cell compressed to "
+                        f"{spec.info['tile_mean_stress'] / 1e3:.0f} kPa mean stress (solid fraction "
+                        f"{spec.info['tile_solid_fraction']:.3f}), under config 1's velGrad = -1/s I")
+    return cfg
+
+
+def pipe_flops_per_eval():
+    """FP32 and FP64 flops of one Disfunction evaluation (double-float and FP64 forms), from the
+    committed ncu summary of the pipe-peak kernels (2 x FMA + ADD + MUL instructions per thread,
+    per evaluation)."""
+    p = os.path.join(ROOT, "profiles", "pipe_peaks_flops.md")
+    out = {}
+    if os.path.exists(p):
+        for ln in open(p):
+            for key in ("fp32_flops_per_ff_eval", "fp64_flops_per_fp64_eval", "fp64_flops_per_ff_eval"):
+                if ln.startswith(key + ":"):
+                    out[key] = float(ln.split(":")[1])
+    return out
+
+
+def measure_form(spec, precision, args, rank, ws, dist):
+    """Throughput of one precision form on the workload: CUDA-graph timesteps timed with CUDA
+    events on the engine stream (max over ranks), per-stage and search-kernel device times from
+    eager steps, and the end-to-end figure through the C ABI with pinned host buffers."""
     from sudodem_gb300 import Engine
-    spec = workload_spec(args.workload, args.seed + rank)
-    eng = Engine(device=0, precision=args.precision, contacts_per_body=args.contacts_per_body)
+    eng = Engine(device=0, precision=precision, contacts_per_body=args.contacts_per_body)
     eng.set_lm_spread(not args.no_lm_spread)
     eng.load(spec)
-    npart = spec.n_particles
     tune = None
     if not args.no_autotune:
-        # launch shapes of the contact stage picked on a second copy of the scene (shapes
-        # change no result; the measured scene runs exactly the steps it runs untuned)
-        tuner = Engine(device=0, precision=args.precision, contacts_per_body=args.contacts_per_body)
+        # launch shapes of the contact stage picked on a second copy of the scene (shapes change
+        # no result; the measured scene runs exactly the steps it runs untuned)
+        tuner = Engine(device=0, precision=precision, contacts_per_body=args.contacts_per_body)
         tuner.set_lm_spread(not args.no_lm_spread)
         tuner.load(spec)
         tune = tuner.autotune(steps=3)
-        del tuner
+        tuner.close()
         eng.set_launch_shape(tune["search_blocks_per_sm"], tune["pass1_blocks_per_sm"])
     eng.step(args.warmup)
     eng.sync()
-    # timed region: K graph-replayed timesteps, CUDA events on the engine stream
     l0 = eng.launch_count()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
     if dist:
@@ -385,36 +426,23 @@ def run_ours(args):
     clk = clocks.stop()
     launches = eng.launch_count() - l0
     if spec.info.get("contact_model") == "hertz_mindlin" and rep["nan_forces"]:
-        # SuperquadricsLaw2 stops the run after a NaN force (later steps do nothing)
         raise SystemExit("the run stopped on a NaN contact force: timing invalid")
     if dist:
         import torch
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = ws * npart * args.steps / (ms / 1e3)
+    npart = spec.n_particles
     nentries = len(eng.interactions(True))
-    # per-stage device times from eager launches (events on the engine stream)
+    # eager steps: per-stage and search-kernel device times, evaluations per step
     eng.set_use_graph(False)
     k2 = 3
     eng.step(k2)
     st = eng.stage_times()
-    eng.sync()
+    srch = eng.search_times()
+    rep2 = eng.sync()
     eng.set_use_graph(True)
-    contacts_ms = st[1] / k2
-    peak, peak_kind = measured_peaks()
-    alg_bytes = BYTES_PER_BODY * spec.n_bodies + BYTES_PER_PAIR * nentries
-    achieved = alg_bytes / (contacts_ms / 1e3) / 1e9
-    tpp = profiled_traffic_per_pair()
-    roofline = {"bound": "hbm", "kernel": "k_contacts", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": (tpp * nentries) if tpp else None,
-                "algorithmic_bytes": alg_bytes, "launch_ms": contacts_ms,
-                "stage_ms_per_step": {"collider": st[0] / k2, "contacts": st[1] / k2, "integrate": st[2] / k2},
-                "note": ("FP64-issue bound on GB300 (transcendental-heavy " +
-                         ("Nelder-Mead" if spec.info.get("contact_model") == "hertz_mindlin" else "LM") +
-                         " narrowphase); HBM fraction stated for the contact kernel")}
-    # end to end through the C ABI with pinned host buffers
+    # end to end through the C ABI with pinned host buffers (kinematics in and out every step)
     import torch
     kin = eng.kinematics()
     hin = torch.empty((spec.n_bodies, 16), dtype=torch.float64, pin_memory=True)
@@ -422,25 +450,124 @@ def run_ours(args):
     hin.numpy()[:] = kin
     e2e_steps = max(3, min(args.steps, 20))
     ems = eng.time_e2e(e2e_steps, hin.data_ptr(), hout.data_ptr())
-    e2e = {"value": npart * e2e_steps / (ems / 1e3) * ws, "unit": UNIT,
-           "h2d_bytes_per_step": 128 * spec.n_bodies, "d2h_bytes_per_step": 128 * spec.n_bodies}
-    cpu = None
+    return {"engine": eng, "value": ws * npart * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+            "e2e": {"value": ws * npart * e2e_steps / (ems / 1e3), "unit": UNIT,
+                    "h2d_bytes_per_step": 128 * spec.n_bodies, "d2h_bytes_per_step": 128 * spec.n_bodies},
+            "stage_ms_per_step": {"collider": st[0] / k2, "contacts": st[1] / k2, "integrate": st[2] / k2},
+            "search_kernel_ms": srch[0] / k2, "fallback_kernel_ms": srch[1] / k2,
+            "evals_per_step": {"double_float": rep2["evals_fp32"] / k2, "fp64": rep2["evals_fp64"] / k2},
+            "fallback_searches_per_step": rep2["fallback_fp64"] / k2,
+            "table_entries": nentries, "launches": launches, "launch_shape": tune, "clocks": clk, "report": rep}
+
+
+def force_errors(spec, state, precisions, threads):
+    """One step of the oracle and of a fresh engine per precision form from the same state
+    (bodies, interactions, scalars, cell): per touching contact, the relative error of the
+    normal + shear force against the oracle (the checker of the cpu_baseline leg)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import OracleScene
+    from sudodem_gb300 import Engine
+    bodies, recs, scal, cell = state
+    o = OracleScene.from_spec(spec, threads=threads)
+    o.set_bodies(bodies)
+    o.set_interactions(recs)
+    o.set_scalars(scal)
+    if cell is not None:
+        o.put_cell(cell)
+    o.rebuild_sorted_bounds()
+    o.step(1)
+    R = {(int(r[0]), int(r[1])): r for r in o.interactions() if r[4] > 0 and r[2] == 1}
+    out = {}
+    for prec in precisions:
+        e = Engine(device=0, precision=prec)
+        e.load(spec)
+        e.put_body_state(bodies)
+        e.put_interactions(recs)
+        e.put_scalars(scal)
+        if cell is not None:
+            e.put_cell(cell)
+        e.step(1)
+        rep = e.sync()
+        G = {(int(r[0]), int(r[1])): r for r in e.interactions(True)}
+        keys = [k for k in R if k in G]
+        g = np.array([G[k][26:29] + G[k][29:32] for k in keys])
+        r = np.array([R[k][26:29] + R[k][29:32] for k in keys])
+        den = np.linalg.norm(r, axis=1)
+        err = np.linalg.norm(g - r, axis=1) / np.where(den > 0, den, 1)
+        q = lambda p: float(np.quantile(err, p))
+        out[prec] = {"touching": len(err), "median": q(0.5), "p99": q(0.99), "p999": q(0.999), "max": float(err.max()),
+                     "frac_le_1e-6": float(np.mean(err <= 1e-6)), "frac_le_1e-10": float(np.mean(err <= 1e-10)),
+                     "searches_deferred_to_fp64": int(rep["fallback_fp64"])}
+        e.close()
+    o.close()
+    return out
+
+
+def run_ours(args):
+    if args.workload.startswith("config2"):
+        return run_ours_batch(args)
+    rank, ws, dist = dist_setup()
+    from sudodem_gb300 import _native
+    spec = workload_spec(args.workload, args.seed + rank)
+    npart = spec.n_particles
+    forms = ("fp64", "mixed") if args.precision == "both" else (args.precision,)
+    res = {p: measure_form(spec, p, args, rank, ws, dist) for p in forms}
+    peaks = _native.pipe_peaks(0)
+    flops = pipe_flops_per_eval()
+    # the roofline of each form's dominant kernel (the search kernel): issue-bound on the pipe
+    # its evaluations run on (FP64 for k_contacts_lm; FP32 for the double-float
+    # k_contacts_lm_ff), against this GPU's measured FMA peak of that pipe
+    for p, r in res.items():
+        ev = r["evals_per_step"]["double_float" if p == "mixed" else "fp64"]
+        kms = r["search_kernel_ms"]
+        pipe = "fp32" if p == "mixed" else "fp64"
+        fpe = flops.get("fp32_flops_per_ff_eval" if p == "mixed" else "fp64_flops_per_fp64_eval")
+        peak = peaks["fp32_tflops" if p == "mixed" else "fp64_tflops"]
+        peak_eval = peaks["disfunction_ff_geval_s" if p == "mixed" else "disfunction_fp64_geval_s"] * 1e9
+        rate = ev / (kms / 1e3) if kms > 0 else 0.0
+        achieved = rate * fpe / 1e12 if fpe else None
+        r["roofline"] = {"bound": pipe, "kernel": "k_contacts_lm_ff" if p == "mixed" else "k_contacts_lm",
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if achieved is not None else None,
+                         "peak_source": "measured on this GPU by sqdem_pipe_peaks (FMA loop of that pipe)",
+                         "traffic": None, "launch_ms": kms, "evaluations_per_launch": ev,
+                         "flops_per_evaluation": fpe,
+                         "evaluation_rate": rate, "peak_evaluation_rate": peak_eval,
+                         "evaluation_rate_frac": rate / peak_eval if peak_eval else None,
+                         "note": "Disfunction evaluations of the Levenberg-Marquardt searches dominate; flops per "
+                                 "evaluation counted by ncu on the pipe-peak kernel that does nothing else"}
+    cpu, ferr = None, None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(spec, budget_s=args.cpu_budget)
+        # force errors of each form against the oracle, one step from the state the FP64 engine
+        # reached (the checker runs in this leg)
+        e = res[forms[0]]["engine"]
+        state = (e.body_state(), e.interactions(True), e.scalars(), e.cell() if spec.info.get("periodic") else None)
+        ferr = force_errors(spec, state, forms, os.cpu_count())
+    head = forms[0]
+    if "mixed" in res and ferr and ferr["mixed"]["frac_le_1e-6"] >= MIXED_FRAC:
+        head = "mixed"
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-                "data": "synthetic",
-                "config": {"workload": args.workload, "particles": npart, "bodies": spec.n_bodies,
-                           "table_entries": nentries, "precision": args.precision, "parallelism": "replicas",
-                           "contact_model": spec.info.get("contact_model", "linear"),
-                           "launch_shape": tune,
-                           "lm_spread": not args.no_lm_spread,
-                           "l2": f"inputs larger than L2: contact table {nentries} entries x >= 256 B"},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
-                "report": rep}
+        h = res[head]
+        line = {"metric": METRIC, "value": h["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": h["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32+f64" if head == "mixed" else "f64", "data": "synthetic",
+                "config": workload_config(args.workload, spec),
+                "headline_form": head,
+                "headline_rule": (f"mixed when at least {MIXED_FRAC:.1%} of touching contacts are within "
+                                  f"{MIXED_TOL:g} relative force error of the FP64 oracle in this run, else fp64"),
+                "roofline": h["roofline"], "cpu_baseline": cpu, "e2e": h["e2e"], "clocks": h["clocks"],
+                "gpu_launches": h["launches"],
+                "forms": {p: {k: v for k, v in r.items() if k not in ("engine", "report", "clocks")}
+                          for p, r in res.items()},
+                "force_error": ferr,
+                "peaks": peaks,
+                "report": h["report"]}
+        if "mixed" in res and "fp64" in res:
+            line["mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
         print(json.dumps(line))
+    for r in res.values():
+        r["engine"].close()
 
 
 def config3_start(args):
@@ -630,8 +757,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config1")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
+    ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"],
+                    help="single-scene workloads: time one form or both (default; the headline is the mixed form "
+                         "when it meets its force-error bar in this run)")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--contacts-per-body", type=int, default=16)
     ap.add_argument("--cpu-budget", type=float, default=20.0)

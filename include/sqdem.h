@@ -102,10 +102,12 @@ typedef struct {
   long long overflow;         /* contact-table or candidate-buffer overflows */
   long long collider_runs;    /* collider passes executed */
   long long steps;            /* timesteps executed */
-  long long evals_fp32;       /* Disfunction evaluations in FP32 (mixed form) */
+  long long evals_fp32;       /* Disfunction evaluations on the FP32 pipes (double-float, mixed form) */
   long long evals_fp64;       /* Disfunction evaluations in FP64 */
-  long long lm_rounds_max;    /* longest contact, in evaluation rounds of the FP64 LM kernel
+  long long lm_rounds_max;    /* longest contact, in evaluation rounds of the LM kernel
                                  (the critical path of the contact stage), max over steps */
+  long long fallback_fp64;    /* mixed form: searches deferred to the FP64 kernel (a decision
+                                 inside its rounding band, or an evaluation it does not reproduce) */
 } sqdem_report;
 
 /* Record layouts shared with the CPU oracle (doubles per record). */
@@ -208,6 +210,13 @@ sqdem_status sqdem_set_record_full(sqdem_ctx* ctx, int on);
  * bit for bit; only the time of the longest searches changes. */
 sqdem_status sqdem_set_lm_spread(sqdem_ctx* ctx, int on);
 
+/* Device time (ms, summed over the steps of the last sqdem_step call made with use_graph = 0,
+ * CUDA events on the context stream) of the contact search kernel (k_contacts_lm, or the mixed
+ * form's double-float k_contacts_lm_ff) and of the mixed form's FP64 fallback kernel (0 for the
+ * FP64 form).  Linear contact model only (0, 0 otherwise).  No counterpart in the reference
+ * (per-kernel timing of what the reference times per engine with timing.stats). */
+sqdem_status sqdem_search_times(sqdem_ctx* ctx, double* out2);
+
 /* Per-stage device time of the last sqdem_step call in milliseconds (cudaEvent pairs on the
  * context stream; only when the context was created with use_graph == 0):
  * out[0] collider gate+passes, out[1] contacts (narrowphase+law), out[2] integrator+reductions. */
@@ -251,6 +260,13 @@ sqdem_status sqdem_time_contacts(sqdem_ctx* ctx, int nrep, double* ms);
  * reference. */
 #define SQDEM_STATIC_QUEUE_MAX (1 << 20)
 sqdem_status sqdem_contacts_static_queue(sqdem_ctx* ctx);
+
+/* Pipe peaks of the GPU `device`, measured by kernels of known instruction mix (no counterpart
+ * in the reference; the denominators of the contact stage's roofline): out[0] FP64 FMA TFLOP/s,
+ * out[1] FP32 FMA TFLOP/s, out[2] FP64 Disfunction evaluations per second (1e9/s) and out[3]
+ * double-float Disfunction evaluations per second (1e9/s), every lane of a full grid evaluating
+ * independent points.  Allocates 64 bytes of device memory for the duration of the call. */
+sqdem_status sqdem_pipe_peaks(int device, double* out4);
 
 /* Superquadrics::Initial (pkg/dem/Superquadrics.cpp:47-93): volume, geometric inertia (3),
  * bounding radius r_max, for unit density.  Host-only helper. */

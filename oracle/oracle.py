@@ -46,6 +46,8 @@ def lib():
         "sqo_get_interactions": (None, [v, dp]), "sqo_set_interactions": (None, [v, l, dp]),
         "sqo_get_margins": (None, [v, dp]),
         "sqo_disfunction": (None, [dp, dp, dp, dp, dp, dp, d, d, dp, dp]),
+        "sqo_lmder2": (None, [dp, dp, dp, dp, dp, dp, dp, dp]),
+        "sqo_set_periodic_fix": (None, [v, i]),
         "sqo_get_scalars": (None, [v, dp]), "sqo_set_scalars": (None, [v, dp]),
         "sqo_rebuild_sorted_bounds": (None, [v]),
         "sqo_pair_geom": (i, [v, i, i, i, dp, dp]),
@@ -122,6 +124,16 @@ def disfunction(shapeA, qA, posA, shapeB, qB, posB, pa0, pa1, margins=False):
     lib().sqo_disfunction(*[_dp(x) for x in a], float(pa0), float(pa1), _dp(out), _dp(m) if margins else None)
     r = (out[0:3], out[3:6], bool(out[6]))
     return r + (m,) if margins else r
+
+
+def lmder2(shapeA, qA, posA, shapeB, qB, posB, p0):
+    """One lmder2 call: dict of the final angles, p1, p2, contact, touching, iterations, stop
+    code and Disfunction evaluations."""
+    out = np.zeros(15)
+    a = [np.ascontiguousarray(x, dtype=np.float64) for x in (shapeA, qA, posA, shapeB, qB, posB, p0)]
+    lib().sqo_lmder2(*[_dp(x) for x in a], _dp(out))
+    return {"p": out[0:2], "p1": out[2:5], "p2": out[5:8], "contact": out[8:11], "touching": bool(out[11]),
+            "iters": int(out[12]), "stop": int(out[13]), "evals": int(out[14])}
 
 
 def normal2phi(shape5, n):
@@ -319,6 +331,11 @@ class OracleScene:
 
     def set_eps(self, body, e1, e2):
         self.L.sqo_set_eps(self.h, int(body), float(e1), float(e2))
+
+    def set_periodic_fix(self, on=True):
+        """Fixture option (not the reference's behaviour): torque arm and relative velocity of
+        contacts across the periodic boundary taken with the image shift."""
+        self.L.sqo_set_periodic_fix(self.h, 1 if on else 0)
 
     def set_quiet(self, on=True):
         self.L.sqo_set_quiet(self.h, 1 if on else 0)

@@ -305,6 +305,13 @@ struct Scene {
   // the law's bound-separation erase is skipped.  sig sums a hash of every branch taken
   // (contact state, force, Coulomb cap, Disfunction evaluations per pair; damping signs per body).
   bool frozenPairs = false;
+  // Test-fixture option, off by default (the reference's behaviour): in a periodic cell, the
+  // reference applies the torque of a contact across the boundary to body 2 at its unshifted
+  // position (Superquadrics.cpp:1356, FIXME at :1550) and leaves the image's field velocity
+  // velGrad*shift2 out of the relative velocity (:1042-1045); both make such contacts spin
+  // particles up.  periodicFix applies both with shift2, so that a periodic packing generated by
+  // the oracle has sound dynamics.
+  bool periodicFix = false;
   unsigned long long sig = 0;
   // CompressionEngine (pkg/dem/Compression.hpp:39-252), run between InteractionLoop and Newton
   struct Servo* servo = nullptr;
@@ -728,7 +735,8 @@ static void lmder2(const PairCtx& c, Real p[2], int itmax, V3& p1, V3& p2, V3& c
 }
 
 // Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::precompute (Superquadrics.cpp:1030-1050)
-static void precompute(Geom& g, const Body& b1, const Body& b2, Real dt, const V3& currentNormal, bool isNew, const V3& shift2) {
+static void precompute(Geom& g, const Body& b1, const Body& b2, Real dt, const V3& currentNormal, bool isNew, const V3& shift2,
+                       const V3& shiftVel = V3()) {
   if (!isNew) {
     g.orthonormal_axis = cross(g.normal, currentNormal);
     Real angle = dt * 0.5 * dot(currentNormal, b1.angVel + b2.angVel);
@@ -737,7 +745,7 @@ static void precompute(Geom& g, const Body& b1, const Body& b2, Real dt, const V
   g.normal = currentNormal;
   V3 c1x = g.contactPoint - b1.pos;
   V3 c2x = (g.contactPoint - b2.pos) - shift2;
-  V3 relVel = (b2.vel + cross(b2.angVel, c2x)) - (b1.vel + cross(b1.angVel, c1x));
+  V3 relVel = ((b2.vel + shiftVel) + cross(b2.angVel, c2x)) - (b1.vel + cross(b1.angVel, c1x));
   g.relativeVn = dot(g.normal, relVel) * g.normal;
   g.relativeVs = relVel - g.relativeVn;
   g.shearInc = g.relativeVs * dt;
@@ -830,7 +838,7 @@ static bool ig2SqSq(Scene& S, Interaction* I, const Body& b1, const Body& b2, co
     g.PenetrationDepth = pDepth;
     normalize(contactNormal);
   }
-  precompute(g, b1, b2, S.dt, contactNormal, g.isShearNew, shift2);
+  precompute(g, b1, b2, S.dt, contactNormal, g.isShearNew, shift2, S.periodicFix ? mul(S.velGrad, shift2) : V3());
   g.normal = contactNormal;
   g.contactAngle[0] = para[0]; g.contactAngle[1] = para[1];
   return true;
@@ -868,7 +876,7 @@ static bool ig2WallSq(Scene& S, Interaction* I, const Body& w, const Body& b, co
     g.contactPoint = 0.5 * (point2 + p1);
     g.PenetrationDepth = norm(d);
   }
-  precompute(g, w, b, S.dt, normal, g.isShearNew, shift2);
+  precompute(g, w, b, S.dt, normal, g.isShearNew, shift2, S.periodicFix ? mul(S.velGrad, shift2) : V3());
   g.normal = normal;
   return true;
 }
@@ -960,7 +968,7 @@ static bool law(Scene& S, Interaction* I, V3* F, V3* T) {
   F[I->id1] = F[I->id1] + Fv;
   F[I->id2] = F[I->id2] + (-Fv);
   T[I->id1] = T[I->id1] + (-cross(A.pos - g.contactPoint, Fv));
-  T[I->id2] = T[I->id2] + cross(B.pos - g.contactPoint, Fv);
+  T[I->id2] = T[I->id2] + cross((S.periodicFix && S.isPeriodic ? B.pos + cellShift(S, I->cellDist) : B.pos) - g.contactPoint, Fv);
   ph.normalForce = normalForce;
   ph.shearForce = shearForce1;
   return true;
@@ -1211,7 +1219,7 @@ static bool ig2SqSq2(Scene& S, Interaction* I, const Body& b1, const Body& b2, c
     g.curvatureAngle = angle;
     hertzMindlin(g, c1, c2, angle);
   }
-  precompute(g, b1, b2, S.dt, contactNormal, g.isShearNew, shift2);
+  precompute(g, b1, b2, S.dt, contactNormal, g.isShearNew, shift2, S.periodicFix ? mul(S.velGrad, shift2) : V3());
   g.normal = contactNormal;
   g.contactAngle[0] = para[0]; g.contactAngle[1] = para[1];
   return true;
@@ -1915,6 +1923,36 @@ void sqo_disfunction(const double* shapeA5, const double* qA, const double* posA
   out[6] = stop ? 1 : 0;
   if (margOut) for (int k = 0; k < 10; k++) margOut[k] = marg[k];
 }
+
+// One lmder2 call (Superquadrics_Ig2.cpp:1057-1354, itmax 50) between two free superellipsoids
+// (as sqo_disfunction) from the angles p0 (2).  out: angles (2), p1 (3), p2 (3), contact (3),
+// touching, iterations, stop code, Disfunction evaluations.
+void sqo_lmder2(const double* shapeA5, const double* qA, const double* posA, const double* shapeB5, const double* qB,
+                const double* posB, const double* p0, double* out) {
+  SQ sq[2];
+  const double* sh[2] = {shapeA5, shapeB5};
+  const double* qq[2] = {qA, qB};
+  for (int k = 0; k < 2; k++) {
+    std::memset(&sq[k], 0, sizeof(SQ));
+    sq[k].rx = sh[k][0]; sq[k].ry = sh[k][1]; sq[k].rz = sh[k][2]; sq[k].eps1 = sh[k][3]; sq[k].eps2 = sh[k][4];
+    sqInitial(sq[k]);
+    Quat o{qq[k][0], qq[k][1], qq[k][2], qq[k][3]};
+    qnormalize(o);
+    sq[k].loc = toRot(conj(o)); sq[k].glob = toRot(o);
+  }
+  long calls = 0;
+  PairCtx c{&sq[0], &sq[1], V3(posA[0], posA[1], posA[2]), V3(posB[0], posB[1], posB[2]), &calls};
+  Real p[2] = {p0[0], p0[1]};
+  V3 p1, p2, center, contact;
+  bool touching = true;
+  LMInfo info;
+  lmder2(c, p, 50, p1, p2, center, touching, contact, info);
+  out[0] = p[0]; out[1] = p[1];
+  for (int k = 0; k < 3; k++) { out[2 + k] = p1[k]; out[5 + k] = p2[k]; out[8 + k] = contact[k]; }
+  out[11] = touching ? 1 : 0; out[12] = info.iters; out[13] = info.stop; out[14] = (double)calls;
+}
+
+void sqo_set_periodic_fix(void* h, int on) { ((Scene*)h)->periodicFix = on != 0; }
 
 void sqo_set_params(void* h, double dt, const double* gravity, double damping, double verletDist, int targetInterv,
                     double minSweepDistFactor, int sortAxis) {

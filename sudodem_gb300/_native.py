@@ -44,7 +44,7 @@ class _Params(C.Structure):
 class _Report(C.Structure):
     _fields_ = [(n, C.c_longlong) for n in ("nan_normals", "nan_forces", "lm_calls", "lm_iterations", "lm_maxiter",
                                              "overflow", "collider_runs", "steps", "evals_fp32", "evals_fp64",
-                                             "lm_rounds_max")]
+                                             "lm_rounds_max", "fallback_fp64")]
 
 
 _LIB = None
@@ -110,6 +110,8 @@ def load_library(build_if_missing=True):
         "sqdem_get_cell": (i, [v, dp]),
         "sqdem_put_cell": (i, [v, dp]),
         "sqdem_contacts_static_queue": (i, [v]),
+        "sqdem_pipe_peaks": (i, [i, dp]),
+        "sqdem_search_times": (i, [v, dp]),
         "sqdem_set_contact_model": (i, [v, i]), "sqdem_contact_model": (i, [v]), "sqdem_num_materials": (i, [v]),
         "sqdem_set_material_moduli": (i, [v, i, dp, dp]), "sqdem_get_material_moduli": (i, [v, dp, dp]),
         "sqdem_set_launch_shape": (i, [v, i, i]), "sqdem_autotune": (i, [v, i, C.c_void_p]),
@@ -137,7 +139,7 @@ def exported_symbols():
             "sqdem_put_interactions", "sqdem_get_scalars", "sqdem_put_scalars", "sqdem_stage_times",
             "sqdem_shape_props", "sqdem_launch_count", "sqdem_set_record_full", "sqdem_time_steps",
             "sqdem_time_e2e", "sqdem_time_contacts", "sqdem_set_use_graph", "sqdem_set_lm_spread", "sqdem_set_periodic",
-            "sqdem_set_velgrad", "sqdem_get_cell", "sqdem_put_cell", "sqdem_contacts_static_queue",
+            "sqdem_set_velgrad", "sqdem_get_cell", "sqdem_put_cell", "sqdem_contacts_static_queue", "sqdem_pipe_peaks", "sqdem_search_times",
             "sqdem_set_servo", "sqdem_get_servo", "sqdem_put_servo", "sqdem_set_quiet", "sqdem_unbalanced_force",
             "sqdem_get_stress", "sqdem_batch_create", "sqdem_batch_destroy", "sqdem_batch_last_error",
             "sqdem_batch_size", "sqdem_batch_scene", "sqdem_batch_step", "sqdem_batch_sync", "sqdem_batch_time_steps",
@@ -156,6 +158,18 @@ def _dp(a):
 
 def _ip(a):
     return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def pipe_peaks(device=0):
+    """Measured pipe peaks of the GPU: FP64 and FP32 FMA TFLOP/s and the FP64 and double-float
+    Disfunction evaluation rates (1e9/s) of a saturated grid (sqdem_pipe_peaks)."""
+    lib = load_library()
+    out = np.zeros(4)
+    st = lib.sqdem_pipe_peaks(int(device), _dp(out))
+    if st:
+        raise SqdemError(st, "sqdem_pipe_peaks failed")
+    return {"fp64_tflops": out[0], "fp32_tflops": out[1], "disfunction_fp64_geval_s": out[2],
+            "disfunction_ff_geval_s": out[3]}
 
 
 def shape_props(rx, ry, rz, eps1, eps2):
@@ -342,6 +356,12 @@ class Engine:
     def stage_times(self):
         out = np.zeros(3)
         self._check(self.lib.sqdem_stage_times(self.h, _dp(out)))
+        return out
+
+    def search_times(self):
+        """(search kernel ms, FP64 fallback kernel ms) summed over the last eager step() call."""
+        out = np.zeros(2)
+        self._check(self.lib.sqdem_search_times(self.h, _dp(out)))
         return out
 
     def time_steps(self, n):

@@ -257,6 +257,46 @@ def config1(seed=0, n=200_000):
     return periodic_cell(n, seed=seed)
 
 
+def config1_dense(tile_path, tiles=5, strain_rate=1.0):
+    """The dense end of config 1: a periodic cell of ``tiles``^3 copies (5: 200,000 particles) of a
+    1,600-particle periodic cell of config 1's particles (half-axes U[0.8,1.2] mm, eps U[0.3,1.8])
+    compressed isotropically to 100 kPa mean stress (the fixture tests/golden/config1_tile.npz,
+    made by tests/golden/make_config1_tile.py), under config 1's loading velGrad =
+    -strain_rate I.  Each copy keeps the tile's positions, orientations and velocities (plus the
+    affine field velGrad * shift of its place in the larger cell, as a periodic image moves); the
+    contact history is not kept (the first steps rebuild the contact angles, the shear springs
+    restart from zero)."""
+    t = np.load(tile_path)
+    shape5, st16, cell = t["shape5"], t["state"], t["cell"]
+    h = np.array(cell[0:9]).reshape(3, 3)
+    if np.count_nonzero(h - np.diag(np.diag(h))):
+        raise ValueError("the tile's cell must be orthogonal")
+    Lt = np.diag(h)
+    velGrad = -strain_rate * np.eye(3)
+    b = _builder()
+    density = 2650.0
+    n = len(shape5)
+    for iz in range(tiles):
+        for iy in range(tiles):
+            for ix in range(tiles):
+                shift = np.array([ix, iy, iz]) * Lt
+                for p in range(n):
+                    _add_sq(b, shape5[p, 0:3], shape5[p, 3:5], st16[p, 3:7], st16[p, 0:3] + shift, density)
+                    row = b["state"][-1]
+                    row[7:10] = st16[p, 7:10] + velGrad @ shift
+                    row[10:16] = st16[p, 10:16]
+    mats = default_material(kn=1e5, friction=0.5, density=density)
+    params = {"dt": 1.0, "gravity": (0.0, 0.0, 0.0), "damping": 0.3, "verletDist": 0.2e-3, "targetInterv": 50,
+              "minSweepDistFactor": 0.1, "sortAxis": 0, "isSuperquadrics": 1, "exactAsphericalRot": 1}
+    hSize = np.diag(Lt * tiles).reshape(9)
+    spec = _finish(b, mats, params, {"periodic": True, "hSize": hSize, "velGrad": velGrad.reshape(9),
+                                     "cell_side": float(Lt[0] * tiles), "tiles": tiles,
+                                     "tile_mean_stress": float(t["mean_stress"]),
+                                     "tile_solid_fraction": float(t["solid_fraction"])})
+    spec.params["dt"] = critical_dt(spec, 0.5)
+    return spec
+
+
 def cubic_specimen(n_particles, seed=0, friction=0.5, eps_range=(0.4, 1.6), r_range=(0.8e-3, 1.2e-3),
                    spacing=2.6e-3, jitter=0.1e-3, kn=1e5, damping=0.3, verletDist=0.2e-3, dt_factor=0.5,
                    wall_gap=0.2e-3):

@@ -1,7 +1,7 @@
 """Build of the in-tree native libraries.
 
 ``build()`` compiles ``csrc/*.cu`` into ``sudodem_gb300/libsqdem_gpu.so`` for sm_103a with
-nvcc, the two translation units in parallel.  Both are built with ``--fmad=false`` so that
+nvcc, the translation units in parallel.  Both are built with ``--fmad=false`` so that
 products and sums keep the rounding sequence of the reference's x86-64 build (no fused
 multiply-add), and so that the adjoint's dual-number replay takes the branches of its
 forward run.
@@ -45,7 +45,8 @@ def build(force=False, verbose=False):
     objs = []
     tmp = os.path.join(HERE, "_obj")
     os.makedirs(tmp, exist_ok=True)
-    units = [("sqdem_engine.cu", ["--fmad=false"]), ("sqdem_adjoint.cu", ["--fmad=false"])]
+    units = [("sqdem_engine.cu", ["--fmad=false"]), ("sqdem_adjoint.cu", ["--fmad=false"]),
+             ("sqdem_peaks.cu", ["--fmad=false"])]
     procs = []
     for src, extra in units:
         obj = os.path.join(tmp, src.replace(".cu", ".o"))

@@ -242,6 +242,14 @@ FFH ff ffDiv(ff a, ff b) {
   return ffAddF(fastTwoSum(q1, q2), q3);
 }
 
+// sqrt(a) for a >= 0: the float root and one correction from the exact remainder.
+FFH ff ffSqrt(ff a) {
+  if (!(a.hi > 0.f)) return mkff(a.hi == 0.f ? 0.f : NAN, 0.f);
+  const float s = sqrtf(a.hi);
+  const ff r = ffSub(a, twoProd(s, s));
+  return fastTwoSum(s, r.hi / (2.f * s));
+}
+
 // log2 of a positive double-float whose high part is a normal float.
 FFH ff ffLog2(ff x) {
   int e = ((ffBits(x.hi) >> 23) & 0xff) - 127;   // x.hi in [2^e, 2^(e+1))
@@ -286,9 +294,8 @@ FFH ff ffExp2(ff x) {
   return mkff(p.hi * s1 * s2, 0.f);
 }
 
-// sin and cos of a double angle |a| < 6000; returns false (NaN, larger angles) otherwise.
-FFH bool ffSinCos(double a, ff& s, ff& c) {
-  const ff x = ffFromD(a);
+// sin and cos of a double-float angle |x| < 6000; returns false (NaN, larger angles) otherwise.
+FFH bool ffSinCos(ff x, ff& s, ff& c) {
   if (!(fabsf(x.hi) < 6000.f)) { s = c = mkff(NAN, 0.f); return false; }
   const float k = rintf(x.hi * 0.636619772f);
   // r = x - k pi/2 (k P1 and k P2 exact: 12 trailing zero bits; x.hi - k P1 exact)
@@ -317,6 +324,7 @@ FFH bool ffSinCos(double a, ff& s, ff& c) {
   }
   return true;
 }
+FFH bool ffSinCos(double a, ff& s, ff& c) { return ffSinCos(ffFromD(a), s, c); }
 
 // ---------------------------------------------------------------------------
 // Disfunction in double-float, in the frame of body A translated to A's centre.
@@ -324,6 +332,7 @@ struct FFShape {
   ff rx, ry, rz;
   ff e1, e2, a1, i1, i2;   // eps1, eps2, 2 - eps1, 1/(2 - eps1), 1/(2 - eps2): the FP64 values
   ff R[9];                 // rotation matrix (local -> global), row-major
+  float rmax, pad;         // bounding radius (float) and padding to 9 float4
 };
 struct FFPair { FFShape A, B; ff pB[3]; };   // pB: centre of B (with its periodic shift) - centre of A
 
@@ -331,6 +340,7 @@ FFH void ffShapeInit(FFShape& f, const SqShape& s) {
   f.rx = ffFromD(s.rx); f.ry = ffFromD(s.ry); f.rz = ffFromD(s.rz);
   f.e1 = ffFromD(s.e1); f.e2 = ffFromD(s.e2); f.a1 = ffFromD(s.a1); f.i1 = ffFromD(s.i1); f.i2 = ffFromD(s.i2);
   for (int k = 0; k < 9; k++) f.R[k] = ffFromD(s.R.m[k]);
+  f.rmax = (float)s.rmax; f.pad = 0.f;
 }
 FFH void ffPairInit(FFPair& P, const SqShape& A, const SqShape& B) {
   ffShapeInit(P.A, A);
@@ -435,13 +445,11 @@ struct FFEval {
   ff c[3], p1[3], p2[3], d[3], sep;
   bool ill;
 };
-FFH void ffDisfunction(const FFPair& P, double pa0, double pa1, FFEval& r) {
+FFH void ffDisfunction(const FFShape& A, const FFShape& B, const ff pB[3], ff pa0, ff pa1, FFEval& r) {
   ff s0, c0, s1, c1;
   const bool ok0 = ffSinCos(pa0, s0, c0), ok1 = ffSinCos(pa1, s1, c1);
   r.ill = !(ok0 && ok1);
   r.c[0] = ffMul(c0, c1); r.c[1] = ffMul(s0, c1); r.c[2] = s1;
-  const FFShape& A = P.A;
-  const FFShape& B = P.B;
   ff q[3];
   // A: local normal R_A^T c
   ffSupport(A, ffDot3(A.R[0], A.R[3], A.R[6], r.c[0], r.c[1], r.c[2]),
@@ -453,10 +461,13 @@ FFH void ffDisfunction(const FFPair& P, double pa0, double pa1, FFEval& r) {
             ffNeg(ffDot3(B.R[1], B.R[4], B.R[7], r.c[0], r.c[1], r.c[2])),
             ffNeg(ffDot3(B.R[2], B.R[5], B.R[8], r.c[0], r.c[1], r.c[2])), q, r.ill);
   for (int i = 0; i < 3; i++)
-    r.p2[i] = ffAdd(ffDot3(B.R[3 * i], B.R[3 * i + 1], B.R[3 * i + 2], q[0], q[1], q[2]), P.pB[i]);
+    r.p2[i] = ffAdd(ffDot3(B.R[3 * i], B.R[3 * i + 1], B.R[3 * i + 2], q[0], q[1], q[2]), pB[i]);
   for (int i = 0; i < 3; i++) r.d[i] = ffSub(r.p2[i], r.p1[i]);
   r.sep = ffDot3(r.c[0], r.c[1], r.c[2], r.d[0], r.d[1], r.d[2]);
   if (!(fabsf(r.sep.hi) < INFINITY)) r.ill = true;   // non-finite: the FP64 path decides
+}
+FFH void ffDisfunction(const FFPair& P, double pa0, double pa1, FFEval& r) {
+  ffDisfunction(P.A, P.B, P.pB, ffFromD(pa0), ffFromD(pa1), r);
 }
 
 }  // namespace sqdem

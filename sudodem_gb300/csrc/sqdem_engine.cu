@@ -39,6 +39,8 @@
 #include <mutex>
 #include "sq_device.cuh"
 #include "sq_hm.cuh"
+#include "sq_ff.cuh"
+#include "sq_lmff.cuh"
 #include "../../include/sqdem.h"
 
 // Work queue of the contact stage for sqdem_contacts_static_queue: a fixed device array so
@@ -67,7 +69,8 @@ struct Params {
   int contactModel;   // SQDEM_CONTACT_LINEAR or SQDEM_CONTACT_HERTZ_MINDLIN
 };
 
-enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_EVAL32, E_EVAL64, E_ROUNDS_MAX, E_NUM };
+enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_EVAL32, E_EVAL64, E_ROUNDS_MAX,
+       E_FALLBACK, E_NUM };
 
 // CompressionEngine (pkg/dem/Compression.hpp:39-252), cubic specimen: configuration and state.
 struct ServoDev {
@@ -95,6 +98,7 @@ struct SceneState {
   int runCollider, initSort, newtonRan, maxDispCode;
   int P, Pnew, nWW, overflowRun;
   int lmCount, lmHead;
+  int fbCount, fbHead;   // searches the mixed form deferred to the FP64 kernel
   int nmFin;   // Hertz-Mindlin searches that ended touching, for the finish pass
   int nmShort; // Hertz-Mindlin searches queued from the back of the queue (expected short)
   int numReinit; long long colliderRuns;
@@ -142,6 +146,8 @@ struct Dev {
   int* wCount; int* wList; int* wBlk;
   int2* ww;
   int* lmQueue; int qCap;   // work queue of the contact searches and its capacity
+  int* fbQueue;             // mixed form: searches deferred to the FP64 kernel (capacity Pcap)
+  FFShape* bodyFF;          // mixed form: double-float shape and rotation of each body, this step
   // grid
   int* bodyCell; int* cellCount; int* cellStart; int* cellFill; int* cellBodies;
   float4* cellBox;   // per cell slot: bound centre (xyz) and, in the next entry, half extents (xyz)
@@ -270,7 +276,7 @@ __global__ void k_scan_apply(const int* __restrict__ in, int n, const int* __res
 __global__ void k_gate(Dev d) {
   SceneState& S = *d.S;
   S.skip = (S.haltAt >= 0 && S.iter >= S.haltAt) ? 1 : 0;
-  if (S.skip) { S.runCollider = 0; S.lmCount = 0; S.lmHead = 0; S.nmFin = 0; S.nmShort = 0; return; }
+  if (S.skip) { S.runCollider = 0; S.lmCount = 0; S.lmHead = 0; S.fbCount = 0; S.fbHead = 0; S.nmFin = 0; S.nmShort = 0; return; }
   if (S.newtonRan) {
     const double code = S.maxDispCode == 2 ? 2.0 : (S.maxDispCode == 1 ? 0.5 : 0.0);
     S.maxVelocitySq = fmax_ref(S.cellTerm, code);
@@ -299,7 +305,7 @@ __global__ void k_gate(Dev d) {
     else run = 0;
   }
   S.runCollider = run;
-  S.lmCount = 0; S.lmHead = 0; S.nmFin = 0; S.nmShort = 0;
+  S.lmCount = 0; S.lmHead = 0; S.fbCount = 0; S.fbHead = 0; S.nmFin = 0; S.nmShort = 0;
   if (run) {
     int init = 0;
     if (S.doSort) { init = 1; S.doSort = 0; }
@@ -1743,12 +1749,14 @@ __device__ __forceinline__ void allocSlots(bool in, unsigned rounds, int budget,
 // warp, each point is evaluated by a group of six lanes (coopEval), which shortens each
 // round as well.  Results are those of the one-point rounds: an evaluation depends only on
 // its point and the two shapes.
-__global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
+__global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d, int fallback) {
   __shared__ SqShape shA[LM_BS], shB[LM_BS];
   __shared__ double2 slotQ[LM_BS];
   __shared__ int slotOwner[LM_BS];
   const SceneState& S = *d.S;
-  const int count = S.lmCount;
+  const int count = fallback ? S.fbCount : S.lmCount;
+  const int* queue = fallback ? d.fbQueue : d.lmQueue;
+  int* head = fallback ? &d.S->fbHead : &d.S->lmHead;
   const int lane = threadIdx.x & 31;
   const int wbase = threadIdx.x & ~31;
   const bool spread = d.prm->lmSpread != 0;
@@ -1762,7 +1770,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
     if (idle) {
       const int leader = __ffs(idle) - 1;
       int base = 0;
-      if (lane == leader) base = atomicAdd(&d.S->lmHead, __popc(idle));
+      if (lane == leader) base = atomicAdd(head, __popc(idle));
       base = __shfl_sync(0xffffffffu, base, leader);
       if (!active && !exhausted) {
         const int idx = base + __popc(idle & ((1u << lane) - 1));
@@ -1770,7 +1778,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d) {
           // start a contact: Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go up to lmder2
           SqShape& A = shA[threadIdx.x];
           SqShape& B = shB[threadIdx.x];
-          L.e = d.lmQueue[idx];
+          L.e = queue[idx];
           const unsigned fl = d.A.flags[L.e];
           int id1, id2;
           entryIds(d, L.e, fl, id1, id2);
@@ -2092,158 +2100,121 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_nm(Dev d) {
 }
 
 // ---------------------------------------------------------------------------
-// Mixed form of pass 2.  The Levenberg-Marquardt rules of lmder2 run first with FP32
-// Disfunction evaluations in the frame of body A; the same FP64 state machine as the plain
-// form then continues from the FP32 solution (warm start), with its evaluations capped at
-// MIX_EVAL64 so that non-converging searches cannot serialise the warp on the FP64 pipe.
-// A pair the FP32 search shows to be separated by more than MIX_SEP_MARGIN of the summed
-// bounding radii along some direction is separated in exact arithmetic (separating axis of
-// two convex bodies), so it is finished without FP64 work.
-static const int MIX_EVAL64 = 12;
-static const float MIX_SEP_MARGIN = 1e-4f;
-// Smallest forward-difference step of the FP32 search: FP32 evaluations resolve ~1e-7 of
-// the particle size, so steps much below 1e-4 rad give a noise-dominated Jacobian.
-static const float MIX_FD_MIN = 3e-4f;
-__device__ __forceinline__ float fdStep(float dp) { return fabsf(dp) >= MIX_FD_MIN ? dp : (dp < 0 ? -MIX_FD_MIN : MIX_FD_MIN); }
+// Mixed form of pass 2: the searches of lmder2 (Superquadrics_Ig2.cpp:1057-1354) in
+// double-float arithmetic on the FP32 pipes (sq_ff.cuh), Disfunction included, with the same
+// lockstep lanes, work queue and spare-lane evaluation as the FP64 kernel.  GB300 issues FP64 at
+// 1/64 of its FP32 rate: a double-float evaluation costs ~1/12 of the FP64 one, and the search's
+// own arithmetic (Jacobian, normal equations, damping, step control) in double-float costs a
+// few percent of its evaluations instead of more than they do.
+//
+// Every decision of lmder2 and of the geometry functor is taken on double-float values only
+// when its margin exceeds the difference double-float and FP64 rounding can make: the stop flag
+// c.(p2-p1) > 0 and the trial acceptance dF > 0 outside E = 4e-13 of the summed bounding radii
+// (~1e-15 m; both arithmetics round these to ~1e-17 m), the 0.95 cosine test outside
+// 1e-12 + 4E/|f|, the |Dp| < 1e-5 and |J^T f|inf <= 1e-15 tests outside 1e-5 relative, the
+// restart rule's distance and isInside tests outside 1e-9, the law's contact gate outside E.
+// A search that meets a decision inside its band, or an evaluation the double-float routines
+// do not reproduce (ill: exactly axis-aligned normals, non-finite values), is deferred whole:
+// the lane drops it without writing anything and appends it to the fallback queue, which the
+// FP64 kernel (k_contacts_lm on that queue) then runs from the same inputs.  The starting
+// angles (table or centre line, FP64), the contact points, depth, normal, precompute, Ip2 and
+// the law stay FP64.
 
-struct LMLaneF {
-  int st, k, stop, nu;
-  bool stopFlag, moved;
-  float sepMax;
-  float p0, p1, q0, q1, mu, Dp0, Dp1, pfL2, pL2, j00, j01, j11, diag0, diag1, jt0, jt1;
-  F3 pf, f1, P1, P2;
-};
+// Double-float shape of each body for this step (the mixed form's searches load it instead of
+// converting per contact).
+__global__ void k_body_ff(Dev d) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= d.N) return;
+  FFShape f;
+  const int4 info = d.info[b];
+  if (info.x == KIND_SQ) {
+    SqShape s;
+    const double4 a = d.shpA[b], e = d.shpB[b], o = d.ori[b];
+    shapeInit(s, a.x, a.y, a.z, e.x, e.y, a.w);
+    s.R = quatToRot(o.x, o.y, o.z, o.w);
+    ffShapeInit(f, s);
+  } else {
+    memset(&f, 0, sizeof(f));
+  }
+  d.bodyFF[b] = f;
+}
 
-__device__ __forceinline__ void lmfStart(LMLaneF& L, float p0, float p1) {
-  L.stopFlag = false; L.moved = false; L.stop = 0; L.sepMax = -INFINITY;
-  L.p0 = p0; L.p1 = p1; L.q0 = p0; L.q1 = p1; L.st = ST_INIT;
+// Superquadrics::isInside value (Superquadrics.cpp:103-108) of point p relative to the centre
+__device__ __forceinline__ double insideValue(const SqShape& s, D3 p) {
+  p = mulL(s.R, p);
+  return pow(pow(fabs(p.x / s.rx), 2.0 / s.e1) + pow(fabs(p.y / s.ry), 2.0 / s.e1), s.e1 / s.e2) +
+         pow(fabs(p.z / s.rz), 2.0 / s.e2);
 }
-__device__ __forceinline__ bool lmfOuter(LMLaneF& L) {
-  if (!(L.k < 50 && !L.stop)) { if (L.k >= 50) L.stop = 3; return false; }
-  if (L.pfL2 <= 1e-20f) { L.stop = 6; return false; }
-  if (L.stopFlag) { L.stop = 9; return false; }
-  float s0, c0, s1, c1;
-  sincosf(L.p0, &s0, &c0);
-  sincosf(L.p1, &s1, &c1);
-  const F3 c = f3(c0 * c1, s0 * c1, s1);
-  const float angle = dotf(L.pf, c) / (nrmf(L.pf) * nrmf(c));
-  if (fabsf(angle) > 0.95f) { L.stop = 8; return false; }
-  L.Dp0 = fdStep(L.Dp0); L.Dp1 = fdStep(L.Dp1);
-  L.q0 = L.p0 + L.Dp0; L.q1 = L.p1; L.st = ST_PROBE0;
-  return true;
+__device__ __forceinline__ void shapeFromGlobal(SqShape& s, const Dev& d, int b) {
+  const double4 a = d.shpA[b], e = d.shpB[b], o = d.ori[b];
+  shapeInit(s, a.x, a.y, a.z, e.x, e.y, a.w);
+  s.R = quatToRot(o.x, o.y, o.z, o.w);
 }
-__device__ __forceinline__ bool lmfInner(LMLaneF& L) {
-  L.j00 += L.mu;
-  L.j11 += L.mu;
-  const float n_a = L.j00 * L.j11 - L.j01 * L.j01;
-  L.Dp0 = (L.jt0 * L.j11 - L.jt1 * L.j01) / n_a;
-  L.Dp1 = (L.jt1 * L.j00 - L.jt0 * L.j01) / n_a;
-  const float Dp_L2 = sqrtf(L.Dp0 * L.Dp0 + L.Dp1 * L.Dp1);
-  if (Dp_L2 < 1e-5f) { L.stop = 2; L.k++; return lmfOuter(L); }
-  L.q0 = L.p0 + L.Dp0; L.q1 = L.p1 + L.Dp1;
-  if (Dp_L2 >= (L.pL2 + 1e-3f) * 1e24f) { L.stop = 4; L.k++; return lmfOuter(L); }
-  L.st = ST_TRIAL;
-  return true;
-}
-__device__ __forceinline__ bool lmfConsume(LMLaneF& L) {
-  const F3 f = f3(L.P2.x - L.P1.x, L.P2.y - L.P1.y, L.P2.z - L.P1.z);
-  switch (L.st) {
-    case ST_INIT:
-      L.pf = f; L.pfL2 = nrmf(f);
-      L.stop = isfinite(L.pfL2) ? 0 : 7;
-      L.k = 0; L.mu = 0; L.nu = 2; L.Dp0 = 1e-7f; L.Dp1 = 1e-7f;
-      return lmfOuter(L);
-    case ST_PROBE0:
-      L.f1 = f;
-      L.q0 = L.p0; L.q1 = L.p1 + L.Dp1; L.st = ST_PROBE1;
-      return true;
-    case ST_PROBE1: {
-      const F3 f0 = L.pf;
-      const float J00 = (L.f1.x - f0.x) / L.Dp0, J10 = (L.f1.y - f0.y) / L.Dp0, J20 = (L.f1.z - f0.z) / L.Dp0;
-      const float J01 = (f.x - f0.x) / L.Dp1, J11 = (f.y - f0.y) / L.Dp1, J21 = (f.z - f0.z) / L.Dp1;
-      L.j00 = J00 * J00 + (J10 * J10 + J20 * J20);
-      L.j01 = J00 * J01 + (J10 * J11 + J20 * J21);
-      L.j11 = J01 * J01 + (J11 * J11 + J21 * J21);
-      L.jt0 = -(J00 * f0.x + (J10 * f0.y + J20 * f0.z));
-      L.jt1 = -(J01 * f0.x + (J11 * f0.y + J21 * f0.z));
-      const float jinf = fmaxf(fabsf(L.jt0), fabsf(L.jt1));
-      L.pL2 = sqrtf(L.p0 * L.p0 + L.p1 * L.p1);
-      if (jinf <= 1e-15f) { L.stop = 1; return false; }
-      if (L.k == 0) L.mu = fmaxf(L.j00, L.j11);
-      L.diag0 = L.j00; L.diag1 = L.j11;
-      return lmfInner(L);
-    }
-    default: {
-      const float fl2 = nrmf(f);
-      if (!isfinite(fl2)) { L.stop = 7; L.k++; return lmfOuter(L); }
-      const float dL = L.Dp0 * (L.mu * L.Dp0 + L.jt0) + L.Dp1 * (L.mu * L.Dp1 + L.jt1);
-      float tmp = (L.pfL2 - fl2) / dL;
-      if (tmp > 0.0f) {
-        const float t = 2 * tmp - 1.f;
-        tmp = 1.0f - t * t * t;
-        L.mu = L.mu * fmaxf(tmp, 0.33333334f);
-        L.nu = 2;
-        L.p0 = L.q0; L.p1 = L.q1;
-        L.pf = f; L.pfL2 = fl2;
-        L.moved = true;
-        L.k++;
-        return lmfOuter(L);
+
+// One lmder2 call ended: the restart rules of Superquadrics_Ig2.cpp:2013-2053 (as lmCallEnd).
+// Returns LMF_MORE when a restarted call begins, LMF_END when the contact's geometry is final,
+// LMF_DEFER when a restart decision falls inside its band.
+__device__ __forceinline__ int lmfCallEnd(const Dev& d, LMF& L, int id1, int id2, D3 shift2, const FFPair* P) {
+  for (;;) {
+    L.calls++; L.iters += L.k; L.maxit += (L.stop == 3);
+    bool restart = false;
+    if (L.phase == 0) L.phase = 1;   // no NaN/stop-7 restart: non-finite evaluations were deferred
+    if (L.phase == 1) {
+      L.phase = 3;
+      if (L.touching) {
+        ff dd[3];
+        for (int i = 0; i < 3; i++) dd[i] = ffSub(L.P2[i], L.P1[i]);
+        const float dist = sqrtf(ffDot3(dd[0], dd[1], dd[2], dd[0], dd[1], dd[2]).hi);
+        const float rmaxA = P->A.rmax;
+        const float x = 10.f * dist / rmaxA - 1.f;
+        if (!(fabsf(x) >= 1e-6f)) return LMF_DEFER;
+        if (x > 0.f) {
+          SqShape A, B;
+          shapeFromGlobal(A, d, id1);
+          shapeFromGlobal(B, d, id2);
+          const D3 p2a = d3(ffToD(L.P2[0]), ffToD(L.P2[1]), ffToD(L.P2[2]));
+          const D3 pb = d3(ffToD(P->pB[0]), ffToD(P->pB[1]), ffToD(P->pB[2]));
+          const D3 p1b = d3(ffToD(L.P1[0]), ffToD(L.P1[1]), ffToD(L.P1[2])) - pb;
+          const double va = insideValue(A, p2a), vb = insideValue(B, p1b);
+          if (!(fabs(va - 1.0) >= 1e-9) || !(fabs(vb - 1.0) >= 1e-9)) return LMF_DEFER;
+          if (!(1 > va) || !(1 > vb)) { L.phase = 2; restart = true; }
+        }
       }
-      L.mu *= L.nu;
-      const int nu2 = (int)((unsigned)L.nu << 1);
-      if (nu2 <= L.nu) { L.stop = 5; L.k++; return lmfOuter(L); }
-      L.nu = nu2;
-      L.j00 = L.diag0; L.j11 = L.diag1;
-      return lmfInner(L);
+    } else L.phase = 3;
+    if (!restart) return LMF_END;
+    if (!L.fromCenter) {
+      double para[2];
+      const D3 pa = xyz(d.pos[id1]);
+      centerLine(pa, xyz(d.pos[id2]) + shift2, para);
+      L.p0 = ffFromD(para[0]); L.p1 = ffFromD(para[1]);
+      L.fromCenter = true;
+      lmfStartSolve(L);
+      return LMF_MORE;
     }
+    // the restarted call would repeat the one that just ended (same start, same state): its
+    // outcome is the one at hand; counted as run
   }
 }
 
-union ShapePair {
-  struct { SqShape A, B; } d;
-  struct { SqShapeF A, B; } f;
-};
-
-__device__ __forceinline__ void buildShapes64(ShapePair& sp, const Dev& d, int id1, int id2, D3 shift2) {
-  const double4 o1 = d.ori[id1], o2 = d.ori[id2];
-  const double4 a1 = d.shpA[id1], a2 = d.shpA[id2], e1 = d.shpB[id1], e2 = d.shpB[id2];
-  shapeInit(sp.d.A, a1.x, a1.y, a1.z, e1.x, e1.y, a1.w); sp.d.A.R = quatToRot(o1.x, o1.y, o1.z, o1.w); sp.d.A.pos = xyz(d.pos[id1]);
-  shapeInit(sp.d.B, a2.x, a2.y, a2.z, e2.x, e2.y, a2.w); sp.d.B.R = quatToRot(o2.x, o2.y, o2.z, o2.w);
-  sp.d.B.pos = xyz(d.pos[id2]) + shift2;
-}
-__device__ __forceinline__ void buildShapes32(ShapePair& sp, const Dev& d, int id1, int id2, D3 shift2) {
-  const double4 o1 = d.ori[id1], o2 = d.ori[id2];
-  const double4 a1 = d.shpA[id1], a2 = d.shpA[id2], e1 = d.shpB[id1], e2 = d.shpB[id2];
-  const D3 rel = (xyz(d.pos[id2]) + shift2) - xyz(d.pos[id1]);
-  shapeInitF(sp.f.A, a1.x, a1.y, a1.z, e1.x, e1.y, quatToRot(o1.x, o1.y, o1.z, o1.w), d3(0, 0, 0));
-  shapeInitF(sp.f.B, a2.x, a2.y, a2.z, e2.x, e2.y, quatToRot(o2.x, o2.y, o2.z, o2.w), rel);
-}
-
-// Pass 2, mixed form.  Each round, the lanes whose search is in its FP32 phase take one FP32
-// evaluation each; then the searches in their FP64 phase share the warp's 32 lanes for FP64
-// evaluations (FP32-phase and idle lanes help: an FP64 warp instruction costs the same
-// whatever the number of lanes taking part), planned and consumed as in k_contacts_lm.
-// A restart from the centre line that would repeat a call which also started there is
-// counted, not run (same computation, same outcome).
-__global__ void __launch_bounds__(LM_BS) k_contacts_lm_mixed(Dev d) {
-  __shared__ ShapePair shp[LM_BS];
-  __shared__ double2 slotQ[LM_BS];
+// Pass 2, mixed form (see the section comment).  Rounds of one double-float evaluation per
+// lane; once the queue is drained, the lanes without a contact evaluate the points the running
+// searches of their warp ask for next (lmfPlan), as in k_contacts_lm.
+__global__ void __launch_bounds__(LM_BS) k_contacts_lm_ff(Dev d) {
+  __shared__ FFPair shp[LM_BS];
+  __shared__ float4 slotQ[LM_BS];
   __shared__ int slotOwner[LM_BS];
-  ShapePair& SP = shp[threadIdx.x];
   const SceneState& S = *d.S;
   const int count = S.lmCount;
-  const double dt = d.prm->dt;
   const int lane = threadIdx.x & 31;
   const int wbase = threadIdx.x & ~31;
   const bool spread = d.prm->lmSpread != 0;
   Counters cnt = {0, 0, 0, 0, 0};
-  unsigned long long ev32 = 0, ev64 = 0;
-  LMLane L;
-  LMLaneF F;
-  bool active = false, exhausted = false, fp32 = true;
-  int id1 = 0, id2 = 0, budget = 0;
-  double rsum = 0;
+  unsigned long long ev32 = 0, deferred = 0;
+  unsigned roundsMax = 0;
+  LMF L;
+  int id1 = 0, id2 = 0;
   D3 shift2 = d3(0, 0, 0);
+  bool active = false, exhausted = false;
   while (true) {
     const unsigned idle = __ballot_sync(0xffffffffu, !active && !exhausted);
     if (idle) {
@@ -2258,171 +2229,118 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_mixed(Dev d) {
           const unsigned fl = d.A.flags[L.e];
           entryIds(d, L.e, fl, id1, id2);
           shift2 = cellShift(S, d.A.cd[L.e]);
-          rsum = d.shpA[id1].w + d.shpA[id2].w;
+          FFPair& P = shp[threadIdx.x];
+          P.A = d.bodyFF[id1];
+          P.B = d.bodyFF[id2];
+          const D3 pa = xyz(d.pos[id1]), pb = xyz(d.pos[id2]) + shift2;
+          P.pB[0] = ffFromD(pb.x - pa.x); P.pB[1] = ffFromD(pb.y - pa.y); P.pB[2] = ffFromD(pb.z - pa.z);
+          L.E = 4e-13f * (P.A.rmax + P.B.rmax);
           L.isNew = !(fl & F_GEOM);
-          if (L.isNew) {
-            double para[2];
-            centerLine(xyz(d.pos[id1]), xyz(d.pos[id2]) + shift2, para);
-            L.p0 = para[0]; L.p1 = para[1];
-          } else { const double2 an = d.A.angle[L.e]; L.p0 = an.x; L.p1 = an.y; }
-          L.contact = d3(0, 0, 0); L.P1 = d3(0, 0, 0); L.P2 = d3(0, 0, 0); L.C = d3(0, 0, 0);
-          L.phase = 0; L.calls = 0; L.iters = 0; L.maxit = 0; L.touching = true;
-          L.fromCenter = L.isNew; L.rounds = 0;
-          buildShapes32(SP, d, id1, id2, shift2);
-          lmfStart(F, (float)L.p0, (float)L.p1);
-          fp32 = true;
+          if (L.isNew) { double para[2]; centerLine(pa, pb, para); L.p0 = ffFromD(para[0]); L.p1 = ffFromD(para[1]); }
+          else { const double2 an = d.A.angle[L.e]; L.p0 = ffFromD(an.x); L.p1 = ffFromD(an.y); }
+          L.fromCenter = L.isNew;
+          L.phase = 0; L.calls = 0; L.iters = 0; L.maxit = 0; L.rounds = 0;
+          lmfStartSolve(L);
           active = true;
         } else exhausted = true;
       }
     }
-    if (!__any_sync(0xffffffffu, active)) break;
-    bool fin = false;
-    if (active && fp32) {
-      float sep;
-      disfunctionF(SP.f.A, SP.f.B, F.q0, F.q1, F.P1, F.P2, sep);
-      ev32++;
-      if (sep > 0) { F.stopFlag = true; F.sepMax = fmaxf(F.sepMax, sep); }
-      if (!lmfConsume(F)) {
-        L.iters += F.k;
-        if (F.stop == 9 && F.sepMax > MIX_SEP_MARGIN * (float)rsum) {
-          // separated: finish as the reference does for a non-touching pair
-          L.touching = false; L.p0 = F.p0; L.p1 = F.p1; L.calls++;
-          fin = true;
-        } else {
-          buildShapes64(SP, d, id1, id2, shift2);
-          // continue in FP64 from the FP32 solution, or from the exact FP64 start if the
-          // FP32 search accepted no step
-          if (F.moved) { L.p0 = (double)F.p0; L.p1 = (double)F.p1; }
-          lmStartSolve(L);
-          budget = MIX_EVAL64;
-          fp32 = false;
-        }
-      }
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!act) break;
+    const int nA = __popc(act);
+    const bool drained = spread && __any_sync(0xffffffffu, exhausted);
+    int spc, base, jmax;
+    allocSlots(active, L.rounds, drained ? 32 : nA, spc, base, jmax);
+    slotOwner[threadIdx.x] = -1;
+    __syncwarp();
+    if (active) lmfPlan(L, &slotQ[wbase + base], &slotOwner[wbase + base], spc, lane);
+    __syncwarp();
+    FFEval v;
+    const int own = slotOwner[threadIdx.x];
+    {
+      // lanes without a slot evaluate the warp's first slot (whose owner always exists) so that
+      // every lane computes on valid inputs
+      const int slot = own >= 0 ? threadIdx.x : wbase;
+      const int src = wbase + slotOwner[slot];
+      const float4 q = slotQ[slot];
+      ffDisfunction(shp[src].A, shp[src].B, shp[src].pB, mkff(q.x, q.y), mkff(q.z, q.w), v);
+      if (own >= 0) ev32++;
     }
-    // FP64 round
-    const bool in64 = active && !fp32 && !fin;
-    const unsigned act64 = __ballot_sync(0xffffffffu, in64);
-    if (act64) {
-      const int nA = __popc(act64);
-      const bool coop = spread && nA <= COOP_POINTS;
-      int spc, base, jmax;
-      allocSlots(in64, L.rounds, spread ? (coop ? COOP_POINTS : 32) : nA, spc, base, jmax);
-      slotOwner[threadIdx.x] = -1;
-      __syncwarp();
-      if (in64) { L.rounds++; lmPlan(L, &slotQ[wbase + base], &slotOwner[wbase + base], spc, lane); }
-      __syncwarp();
-      D3 P1 = d3(0, 0, 0), P2 = d3(0, 0, 0);
-      bool flag = false;
-      if (coop) {
-        // group g of six lanes evaluates slot g; lanes 30-31 and groups without a point
-        // mirror slot 0 (its owner always exists) so that every lane computes on valid inputs
-        const int graw = lane / COOP_LANES;
-        const int grp = graw < COOP_POINTS ? graw : 0;
-        const int sub = graw < COOP_POINTS ? lane - grp * COOP_LANES : lane - COOP_POINTS * COOP_LANES;
-        const int o = slotOwner[wbase + grp];
-        const bool has = graw < COOP_POINTS && o >= 0;
-        const int slot = has ? grp : 0;
-        const int src = wbase + slotOwner[wbase + slot];
-        const double2 q = slotQ[wbase + slot];
-        coopEval(shp[src].d.A, shp[src].d.B, q.x, q.y, grp * COOP_LANES, sub, P1, P2, flag);
-        if (has && sub == 0) ev64++;
-      } else {
-        const int own = slotOwner[threadIdx.x];
-        if (own >= 0) {
-          const double2 q = slotQ[threadIdx.x];
-          D3 C;
-          disfunction(shp[wbase + own].d.A, shp[wbase + own].d.B, q.x, q.y, C, P1, P2, flag);
-          ev64++;
-        }
+    if (active) L.rounds++;
+    for (int j = 0; j < jmax; j++) {
+      const int si = base + j;
+      const bool mine = j < spc;
+      const int src = mine ? si : lane;
+      FFEval w;
+#define SHF(x) __shfl_sync(0xffffffffu, (x), src)
+      for (int i = 0; i < 3; i++) {
+        w.c[i] = mkff(SHF(v.c[i].hi), SHF(v.c[i].lo)); w.p1[i] = mkff(SHF(v.p1[i].hi), SHF(v.p1[i].lo));
+        w.p2[i] = mkff(SHF(v.p2[i].hi), SHF(v.p2[i].lo)); w.d[i] = mkff(SHF(v.d[i].hi), SHF(v.d[i].lo));
       }
-      __syncwarp();
-      bool mine64 = in64;
-      for (int j = 0; j < jmax; j++) {
-        const int si = base + j;
-        const bool mine = mine64 && j < spc;
-        const int src = mine ? (coop ? si * COOP_LANES : si) : lane;
-        const double x1 = __shfl_sync(0xffffffffu, P1.x, src), y1 = __shfl_sync(0xffffffffu, P1.y, src),
-                     z1 = __shfl_sync(0xffffffffu, P1.z, src);
-        const double x2 = __shfl_sync(0xffffffffu, P2.x, src), y2 = __shfl_sync(0xffffffffu, P2.y, src),
-                     z2 = __shfl_sync(0xffffffffu, P2.z, src);
-        const bool f = __shfl_sync(0xffffffffu, (int)flag, src) != 0;
-        if (mine && slotOwner[wbase + si] == lane && sameBits(slotQ[wbase + si], L.q0, L.q1)) {
-          L.P1 = d3(x1, y1, z1);
-          L.P2 = d3(x2, y2, z2);
-          L.C = 0.5 * (L.P1 + L.P2);
-          if (f) L.stopFlag = true;
-          bool more = lmConsume(L);
-          if (more && --budget <= 0) { L.stop = 3; more = false; }
-          if (!more) {
-            mine64 = false;   // this call ended: the rest of the round's slots are stale
-            for (;;) {
-              L.calls++; L.iters += L.k; L.maxit += (L.stop == 3);
-              bool restart = false;
-              if (L.phase == 0) {
-                L.phase = 1;
-                if ((isnan(L.p0) || isnan(L.p1) || 7 == L.stop) && L.touching) restart = true;
-              }
-              if (!restart && L.phase == 1) {
-                L.phase = 3;
-                if (L.touching && 10.0 * nrm(L.P2 - L.P1) > SP.d.A.rmax &&
-                    (!isInside(SP.d.A, L.P2 - SP.d.A.pos) || !isInside(SP.d.B, L.P1 - SP.d.B.pos))) {
-                  L.phase = 2; restart = true;
-                }
-              } else if (!restart) L.phase = 3;
-              if (!restart) { fin = true; break; }
-              if (!L.fromCenter) {
-                double para[2];
-                centerLine(SP.d.A.pos, SP.d.B.pos, para);
-                L.p0 = para[0]; L.p1 = para[1];
-                L.fromCenter = true;
-                fp32 = true;   // FP32 shapes are rebuilt after the round (helpers may still read these)
-                break;
-              }
-              // the restarted search (FP32 then FP64 from the centre line) would repeat the
-              // one that just ended: count it and go on with its outcome
-              L.iters += F.k;
-            }
+      w.sep = mkff(SHF(v.sep.hi), SHF(v.sep.lo));
+      w.ill = SHF((int)v.ill) != 0;
+#undef SHF
+      if (mine && active && slotOwner[wbase + si] == lane && sameFF(slotQ[wbase + si], L.q0, L.q1)) {
+        int r = lmfConsume(L, w);
+        if (r == LMF_END) r = lmfCallEnd(d, L, id1, id2, shift2, &shp[threadIdx.x]);
+        if (r == LMF_END) {
+          // end of Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go (FP64), then Ip2 + law
+          const int e = L.e;
+          const unsigned fl = d.A.flags[e];
+          const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
+          GeomOut g;
+          g.lmCalls = L.calls; g.lmIters = L.iters; g.lmStop = 0; g.nanNormal = false;
+          g.isShearNew = L.isNew ? true : (d.A.depth[e] <= 0);
+          g.cp = L.isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
+          g.ang0 = ffToD(L.p0); g.ang1 = ffToD(L.p1); g.angSet = true;
+          bool ok = true;
+          if (!L.touching) {
+            g.precomputed = false; g.depth = 0; g.isShearNew = true;
+          } else {
+            const D3 P1 = b1.pos + d3(ffToD(L.P1[0]), ffToD(L.P1[1]), ffToD(L.P1[2]));
+            const D3 P2 = b1.pos + d3(ffToD(L.P2[0]), ffToD(L.P2[1]), ffToD(L.P2[2]));
+            const D3 contact = d3(ffToD(L.c[0]), ffToD(L.c[1]), ffToD(L.c[2]));
+            const double pDepth = dot(P1 - P2, contact);
+            if (!(fabs(pDepth - 1e-18) >= (double)L.E)) ok = false;   // the law's contact gate
+            g.p1 = P1; g.p2 = P2;
+            g.cp = 0.5 * (P1 + P2);
+            g.depth = pDepth;
+            D3 cn = contact;
+            normalize(cn);
+            const D3 oldNormal = L.isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
+            g.precomputed = true;
+            precomputeD(g, oldNormal, b1, b2, d.prm->dt, cn, g.isShearNew, shift2);
+            g.normal = cn;
           }
+          if (ok) {
+            cnt.lmCalls += L.calls; cnt.lmIters += L.iters; cnt.lmMax += L.maxit;
+            finishEntry(d, e, fl, L.isNew, id1, b1, b2, g, cnt);
+          } else r = LMF_DEFER;
+        }
+        if (r == LMF_DEFER) {
+          const int k = atomicAdd(&d.S->fbCount, 1);
+          d.fbQueue[k] = L.e;
+          deferred++;
+        }
+        if (r != LMF_MORE) {
+          active = false;
+          roundsMax = max(roundsMax, L.rounds);
         }
       }
-      __syncwarp();
-      if (in64 && fp32) {  // restart: FP32 search from the centre line
-        buildShapes32(SP, d, id1, id2, shift2);
-        lmfStart(F, (float)L.p0, (float)L.p1);
-      }
     }
-    if (fin) {
-      // end of the geometry functor, then Ip2 + law
-      const int e = L.e;
-      const unsigned fl = d.A.flags[e];
-      const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
-      GeomOut g;
-      g.lmCalls = L.calls; g.lmIters = L.iters; g.lmStop = 0; g.nanNormal = false;
-      g.isShearNew = L.isNew ? true : (d.A.depth[e] <= 0);
-      g.cp = L.isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
-      g.ang0 = L.p0; g.ang1 = L.p1; g.angSet = true;
-      if (!L.touching) {
-        g.precomputed = false; g.depth = 0; g.isShearNew = true;
-      } else {
-        g.p1 = L.P1; g.p2 = L.P2;
-        if (isnan(L.contact.x)) g.nanNormal = true;
-        g.cp = L.C;
-        g.depth = dot(L.P1 - L.P2, L.contact);
-        D3 cn = L.contact;
-        normalize(cn);
-        const D3 oldNormal = L.isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
-        g.precomputed = true;
-        precomputeD(g, oldNormal, b1, b2, dt, cn, g.isShearNew, shift2);
-        g.normal = cn;
-      }
-      cnt.lmCalls += L.calls; cnt.lmIters += L.iters; cnt.lmMax += L.maxit;
-      finishEntry(d, e, fl, L.isNew, id1, b1, b2, g, cnt);
-      active = false;
-    }
+    __syncwarp();
   }
   flushCounters(d, cnt);
-  for (int o = 16; o > 0; o >>= 1) { ev32 += __shfl_down_sync(0xffffffffu, ev32, o); ev64 += __shfl_down_sync(0xffffffffu, ev64, o); }
-  if (lane == 0) { atomicAdd(&d.S->err[E_EVAL32], ev32); atomicAdd(&d.S->err[E_EVAL64], ev64); }
+  for (int o = 16; o > 0; o >>= 1) {
+    ev32 += __shfl_down_sync(0xffffffffu, ev32, o);
+    deferred += __shfl_down_sync(0xffffffffu, deferred, o);
+    roundsMax = max(roundsMax, __shfl_down_sync(0xffffffffu, roundsMax, o));
+  }
+  if (lane == 0) {
+    atomicAdd(&d.S->err[E_EVAL32], ev32);
+    atomicAdd(&d.S->err[E_FALLBACK], deferred);
+    atomicMax(&d.S->err[E_ROUNDS_MAX], (unsigned long long)roundsMax);
+  }
 }
 
 // contribution of table entry e to body b (b is id1 when asId1)
@@ -2905,7 +2823,9 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d) {
   (void)S;
 }
 
-__global__ void k_reset_queue(Dev d) { d.S->lmCount = 0; d.S->lmHead = 0; d.S->nmFin = 0; d.S->nmShort = 0; }
+__global__ void k_reset_queue(Dev d) {
+  d.S->lmCount = 0; d.S->lmHead = 0; d.S->fbCount = 0; d.S->fbHead = 0; d.S->nmFin = 0; d.S->nmShort = 0;
+}
 
 // Start of NewtonIntegrator::action (NewtonIntegrator.cpp:107-117): pending velGrad, the
 // cell-size-change velocity that seeds maxVelocitySq, and the gradients the body update uses.
@@ -2969,8 +2889,10 @@ struct sqdem_ctx {
   int nMats = 0;
   std::vector<double4> hostMats; std::vector<double2> hostMatsB, hostMatsE;
   long long launches = 0, launchesPerStep = 0;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   float stageMs[3] = {0, 0, 0};
+  float searchMs[2] = {0, 0};   // eager steps: search kernel, then the mixed form's FP64 fallback kernel
+  bool timingSearch = false;
 };
 
 static sqdem_status fail(sqdem_ctx* c, sqdem_status s, const std::string& m) {
@@ -3044,9 +2966,21 @@ static void launchContactStage(sqdem_ctx* c, const Dev& d, int grid) {
     k_contacts_nm_finish<<<std::min(nblk(d.Pcap, 128), c->numSMs * 8), 128, 0, s>>>(d);
     c->launches += 3;
   } else {
-    if (c->precision == SQDEM_MIXED) k_contacts_lm_mixed<<<grid, LM_BS, 0, s>>>(d);
-    else k_contacts_lm<<<grid, LM_BS, 0, s>>>(d);
-    c->launches += 2;
+    if (c->precision == SQDEM_MIXED) {
+      // double-float searches, then the FP64 kernel on the searches they deferred
+      k_body_ff<<<nblk(d.N, 256), 256, 0, s>>>(d);
+      if (c->timingSearch) cudaEventRecord(c->ev[4], s);
+      k_contacts_lm_ff<<<grid, LM_BS, 0, s>>>(d);
+      if (c->timingSearch) cudaEventRecord(c->ev[5], s);
+      k_contacts_lm<<<grid, LM_BS, 0, s>>>(d, 1);
+      if (c->timingSearch) cudaEventRecord(c->ev[6], s);
+      c->launches += 4;
+    } else {
+      if (c->timingSearch) cudaEventRecord(c->ev[4], s);
+      k_contacts_lm<<<grid, LM_BS, 0, s>>>(d, 0);
+      if (c->timingSearch) { cudaEventRecord(c->ev[5], s); cudaEventRecord(c->ev[6], s); }
+      c->launches += 2;
+    }
   }
 }
 
@@ -3207,12 +3141,12 @@ sqdem_status sqdem_create(sqdem_ctx** out, const sqdem_config* cfg) {
     int nb = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_contacts_lm, LM_BS, 0));
     c->lmBlocksPerSM = nb > 0 ? nb : 1;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_contacts_lm_mixed, LM_BS, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_contacts_lm_ff, LM_BS, 0));
     c->lmBlocksPerSMmixed = nb > 0 ? nb : 1;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_contacts_nm, LM_BS, 0));
     c->nmBlocksPerSM = nb > 0 ? nb : 1;
   }
-  for (int i = 0; i < 4; i++) CK(cudaEventCreate(&c->ev[i]));
+  for (int i = 0; i < 7; i++) CK(cudaEventCreate(&c->ev[i]));
   std::memset(&c->d, 0, sizeof(Dev));
   std::memset(&c->params, 0, sizeof(c->params));
   c->params.dt = 1e-5; c->params.damping = 0.2; c->params.verletDist = -0.5; c->params.targetInterv = 50;
@@ -3353,6 +3287,8 @@ sqdem_status sqdem_set_bodies(sqdem_ctx* c, int n, const int* kind, const double
   c->servoOn = false;
   CK(dalloc(c, &d.ww, std::max(d.W * d.W, 1)));
   CK(dalloc(c, &d.lmQueue, d.Pcap));
+  CK(dalloc(c, &d.fbQueue, d.Pcap));
+  CK(dalloc(c, &d.bodyFF, d.N));
   d.qCap = d.Pcap;
   CK(dalloc(c, &d.bodyCell, n)); CK(dalloc(c, &d.cellCount, d.Gmax + 1)); CK(dalloc(c, &d.cellStart, d.Gmax + 1));
   CK(dalloc(c, &d.cellFill, d.Gmax + 1)); CK(dalloc(c, &d.cellBodies, n)); CK(dalloc(c, &d.cellBox, 2 * (size_t)n));
@@ -3423,7 +3359,8 @@ sqdem_status sqdem_step(sqdem_ctx* c, int nsteps) {
     for (int i = 0; i < nsteps; i++) CK(cudaGraphLaunch(c->exec, c->stream));
     c->launches += c->launchesPerStep * nsteps;
   } else {
-    float acc[3] = {0, 0, 0};
+    float acc[5] = {0, 0, 0, 0, 0};
+    c->timingSearch = c->contactModel != SQDEM_CONTACT_HERTZ_MINDLIN;
     for (int i = 0; i < nsteps; i++) {
       enqueueStep(c, true);
       CK(cudaEventSynchronize(c->ev[3]));
@@ -3431,8 +3368,14 @@ sqdem_status sqdem_step(sqdem_ctx* c, int nsteps) {
       cudaEventElapsedTime(&t, c->ev[0], c->ev[1]); acc[0] += t;
       cudaEventElapsedTime(&t, c->ev[1], c->ev[2]); acc[1] += t;
       cudaEventElapsedTime(&t, c->ev[2], c->ev[3]); acc[2] += t;
+      if (c->timingSearch) {
+        cudaEventElapsedTime(&t, c->ev[4], c->ev[5]); acc[3] += t;
+        cudaEventElapsedTime(&t, c->ev[5], c->ev[6]); acc[4] += t;
+      }
     }
+    c->timingSearch = false;
     for (int k = 0; k < 3; k++) c->stageMs[k] = acc[k];
+    c->searchMs[0] = acc[3]; c->searchMs[1] = acc[4];
   }
   CK(cudaGetLastError());
   return SQDEM_OK;
@@ -3454,6 +3397,7 @@ sqdem_status sqdem_sync(sqdem_ctx* c, sqdem_report* r) {
     r->collider_runs = (long long)e[E_COLLIDER_RUNS]; r->steps = (long long)e[E_STEPS];
     r->evals_fp32 = (long long)e[E_EVAL32]; r->evals_fp64 = (long long)e[E_EVAL64];
     r->lm_rounds_max = (long long)e[E_ROUNDS_MAX];
+    r->fallback_fp64 = (long long)e[E_FALLBACK];
   }
   if (e[E_OVERFLOW]) return fail(c, SQDEM_ERR_CAPACITY, "contact table or candidate buffer overflow; increase contacts_per_body");
   return SQDEM_OK;
@@ -3739,6 +3683,12 @@ sqdem_status sqdem_put_scalars(sqdem_ctx* c, const double* o) {
   S.bbInit = o[8] != 0;
   CK(cudaMemcpyAsync(c->d.S, &S, sizeof(S), cudaMemcpyHostToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_search_times(sqdem_ctx* c, double* out2) {
+  if (!c || !out2) return SQDEM_ERR_ARG;
+  out2[0] = c->searchMs[0]; out2[1] = c->searchMs[1];
   return SQDEM_OK;
 }
 

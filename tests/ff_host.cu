@@ -3,18 +3,24 @@
 // sq_ff.cuh's routines are __host__ __device__ and use only IEEE float operations and fmaf, so
 // this host build computes what the kernels compute, bit for bit; the CPU tests compare it with
 // the oracle's FP64 Disfunction.  Nothing here is loaded by the package.
-#include "../sudodem_gb300/csrc/sq_ff.cuh"
+#include "../sudodem_gb300/csrc/sq_lmff.cuh"
 #include <cmath>
 
 using namespace sqdem;
 
-static void hostShape(SqShape& s, const double* shape5, const double* q, const double* pos) {
+// renorm: normalise the quaternion as Superquadrics::setOrientation does (a body being created);
+// 0: use it as stored (a body's current orientation, as the engines do)
+static void hostShape(SqShape& s, const double* shape5, const double* q, const double* pos, int renorm = 1) {
   double w = q[0], x = q[1], y = q[2], z = q[3];
-  // Eigen's normalize (Superquadrics::setOrientation): squaredNorm = (x^2 + y^2) + (z^2 + w^2)
-  const double n = std::sqrt((x * x + y * y) + (z * z + w * w));
-  w /= n; x /= n; y /= n; z /= n;
+  if (renorm) {
+    // Eigen's normalize: squaredNorm = (x^2 + y^2) + (z^2 + w^2)
+    const double n = std::sqrt((x * x + y * y) + (z * z + w * w));
+    w /= n; x /= n; y /= n; z /= n;
+  }
+  // r_max of Superquadrics::Initial (Superquadrics.cpp:47-93)
   double rmax = shape5[0] > shape5[1] ? shape5[0] : shape5[1];
   rmax = rmax > shape5[2] ? rmax : shape5[2];
+  if (shape5[3] < 1.0 || shape5[4] < 1.0) rmax *= std::pow(2.0, 0.5);
   shapeInit(s, shape5[0], shape5[1], shape5[2], shape5[3], shape5[4], rmax);
   s.R = quatToRot(w, x, y, z);
   s.pos = d3(pos[0], pos[1], pos[2]);
@@ -48,4 +54,32 @@ extern "C" void ffh_elem(int op, const double* x, long n, double* out) {
       default: ffSinCos(x[i], s, c); out[i] = ffToD(c); break;
     }
   }
+}
+
+// One lmder2 call with the double-float state machine of the mixed form, from angles p0 (2).
+// out: angles (2), p1 (3), p2 (3) relative to A's centre, contact (3), touching, iterations,
+// stop code, evaluations, outcome (1 ended, 2 deferred to FP64).
+extern "C" void ffh_lmder2(const double* shapeA5, const double* qA, const double* posA, const double* shapeB5,
+                           const double* qB, const double* posB, const double* p0, double* out, int renorm) {
+  SqShape A, B;
+  hostShape(A, shapeA5, qA, posA, renorm);
+  hostShape(B, shapeB5, qB, posB, renorm);
+  FFPair P;
+  ffPairInit(P, A, B);
+  LMF L;
+  L.p0 = ffFromD(p0[0]); L.p1 = ffFromD(p0[1]);
+  L.E = 4e-13f * (P.A.rmax + P.B.rmax);
+  L.touching = true;
+  for (int i = 0; i < 3; i++) L.c[i] = L.P1[i] = L.P2[i] = mkff(0.f, 0.f);
+  lmfStartSolve(L);
+  int r = LMF_MORE, evals = 0;
+  while (r == LMF_MORE && evals < 100000) {
+    FFEval v;
+    ffDisfunction(P.A, P.B, P.pB, L.q0, L.q1, v);
+    evals++;
+    r = lmfConsume(L, v);
+  }
+  out[0] = ffToD(L.p0); out[1] = ffToD(L.p1);
+  for (int i = 0; i < 3; i++) { out[2 + i] = ffToD(L.P1[i]); out[5 + i] = ffToD(L.P2[i]); out[8 + i] = ffToD(L.c[i]); }
+  out[11] = L.touching ? 1 : 0; out[12] = L.k; out[13] = L.stop; out[14] = evals; out[15] = r;
 }

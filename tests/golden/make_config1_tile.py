@@ -10,7 +10,12 @@ not that of a jammed packing).  The CPU oracle compresses it isotropically (stra
 velGrad = -rate I) at 3/s through the gas phase until a contact network carries 1 kPa, then at
 config 1's 1/s until the mean stress of Shop::getStress (pkg/dem/Shop_02.cpp:350-376) has
 reached 100 kPa at two checks 500 steps apart.  The time step is assemblies.critical_dt's
-(0.5 x the smaller of the translational and rotational critical steps).  Saved: the
+(0.5 x the smaller of the translational and rotational critical steps).  The oracle runs with
+its periodicFix option: the reference applies the torque of a contact across the periodic
+boundary to body 2 at its unshifted position and leaves the image's field velocity out of the
+relative velocity, which spins particles up without bound (angular velocities of 1e11 rad/s in
+this compression); the fixture is a packing with sound dynamics, the workload then runs the
+reference's own semantics.  Saved: the
 particles' shapes and kinematic state and the cell; the contact history is not saved (the
 workload's warm-up steps rebuild the contact angles, and the shear springs restart from zero).
 
@@ -47,6 +52,7 @@ def main():
     spec = assemblies.periodic_cell(N_TILE, seed=SEED, solid_fraction=phi0, eps_range=(0.3, 1.8), strain_rate=3.0)
     print(f"start: solid fraction {phi0:.4f}, lattice spacing {spacing * 1e3:.3f} mm", flush=True)
     o = OracleScene.from_spec(spec, threads=threads)
+    o.set_periodic_fix(True)
     held = 0
     slow = False
     t0 = time.time()

@@ -21,8 +21,19 @@ from sudodem_gb300.servo import STATE_NAMES, servo_config, state_dict  # noqa: E
 pytestmark = pytest.mark.gpu
 
 
+
+def _specimen(n, seed, **kw):
+    # The schedules of these tests (iterations at which the walls carry force, stop tests) were
+    # written for dt = 0.5 sqrt(m_min / kn), the translational step without the rotational term of
+    # assemblies.critical_dt; over a few hundred steps the instability that term prevents does
+    # not develop.  Both engines of a comparison run the same spec.
+    spec = assemblies.cubic_specimen(n, seed=seed, **kw)
+    part = spec.kind == 0
+    spec.params["dt"] = 0.5 * float(np.sqrt(np.min(spec.state[part, 33]) / np.max(spec.materials["Kn"])))
+    return spec
+
 def shared_state(cfg, n=150, seed=5, steps=250):
-    spec = assemblies.cubic_specimen(n, seed=seed)
+    spec = _specimen(n, seed=seed)
     o = OracleScene.from_spec(spec, threads=4)
     o.set_servo(cfg)
     o.step(steps)
@@ -83,7 +94,7 @@ def test_shop_reductions_match_oracle(gpu):
 def test_stop_at_iter_halts_and_resumes(gpu):
     cfg = servo_config(goalx=1e5, goaly=1e5, goalz=1e5, max_vel=1.0, solve_num_max=150,
                        f_threshold=1e9, fmin_threshold=1e9, unbf_tol=1e9)
-    spec = assemblies.cubic_specimen(100, seed=4)
+    spec = _specimen(100, seed=4)
     e = Engine(device=0)
     e.load(spec)
     e.set_servo(cfg)
@@ -106,7 +117,7 @@ def test_stop_at_iter_halts_and_resumes(gpu):
 
 
 def test_quiet_flag(gpu):
-    spec = assemblies.cubic_specimen(80, seed=2)
+    spec = _specimen(80, seed=2)
     e = Engine(device=0)
     e.load(spec)
     e.step(20)
@@ -123,7 +134,7 @@ def test_quiet_flag(gpu):
 def test_graph_equals_eager_with_servo(gpu):
     cfg = servo_config(goalx=1e5, goaly=1e5, goalz=1e5, max_vel=1.0, iterate_num_max=10, solve_num_max=50,
                        echo_interval=25, savedata_interval=12)
-    spec = assemblies.cubic_specimen(120, seed=9)
+    spec = _specimen(120, seed=9)
     a, b = Engine(device=0, use_graph=True), Engine(device=0, use_graph=False)
     for x in (a, b):
         x.load(spec)
