@@ -107,7 +107,10 @@ typedef struct {
   long long lm_rounds_max;    /* longest contact, in evaluation rounds of the LM kernel
                                  (the critical path of the contact stage), max over steps */
   long long fallback_fp64;    /* mixed form: searches deferred to the FP64 kernel (a decision
-                                 inside its rounding band, or an evaluation it does not reproduce) */
+                                 inside its rounding band, itmax reached, or an evaluation it does
+                                 not reproduce) */
+  long long lm_rounds_max_ff; /* mixed form: longest search in rounds of the double-float kernel
+                                 (lm_rounds_max: of the FP64 kernel) */
 } sqdem_report;
 
 /* Record layouts shared with the CPU oracle (doubles per record). */

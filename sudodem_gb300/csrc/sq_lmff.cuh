@@ -17,6 +17,7 @@ struct LMF {
   ff pf[3], f1[3], c[3], P1[3], P2[3];
   float E;
   unsigned calls, iters, maxit, rounds;
+  float pad;   // 73 words: an odd stride, so the lanes' states in shared memory fall in distinct banks
 };
 enum { LMF_MORE = 0, LMF_END = 1, LMF_DEFER = 2 };
 

@@ -59,6 +59,12 @@ enum : unsigned {
   F_OWNER_ID1 = 8u,   // the row owner is Interaction::id1 (else the partner is)
   F_FORCE = 16u,      // the law applied a force this step
 };
+// Bits 20-23 of an entry's flags: bit length of the Levenberg-Marquardt iterations its search
+// took at the last step (0 when no search ran).  The pre-pass queues new contacts and searches
+// that took at least 4 iterations first, so that the longest searches start first.
+static const unsigned F_ITERS_SHIFT = 20, F_ITERS_MASK = 15u << 20;
+static const unsigned LONG_ITERS_BUCKET = 3;   // iterations >= 4
+__device__ __forceinline__ unsigned itersBucket(int iters) { return iters > 0 ? min(15u, 32u - __clz((unsigned)iters)) : 0u; }
 enum { KIND_SQ = 0, KIND_WALL = 1 };
 static const unsigned DOF_ALL = 63u;
 
@@ -70,7 +76,7 @@ struct Params {
 };
 
 enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_EVAL32, E_EVAL64, E_ROUNDS_MAX,
-       E_FALLBACK, E_NUM };
+       E_FALLBACK, E_ROUNDS_MAX_FF, E_NUM };
 
 // CompressionEngine (pkg/dem/Compression.hpp:39-252), cubic specimen: configuration and state.
 struct ServoDev {
@@ -100,7 +106,7 @@ struct SceneState {
   int lmCount, lmHead;
   int fbCount, fbHead;   // searches the mixed form deferred to the FP64 kernel
   int nmFin;   // Hertz-Mindlin searches that ended touching, for the finish pass
-  int nmShort; // Hertz-Mindlin searches queued from the back of the queue (expected short)
+  int nmShort; // searches queued from the back of the queue (expected short)
   int numReinit; long long colliderRuns;
   unsigned long long bbLo[3], bbHi[3];   // order-preserving encodings of the bbox of particle bound centres
   double org[3]; double h; int dim[3]; int nCells;
@@ -1251,6 +1257,7 @@ __device__ void finishEntry(const Dev& d, int e, unsigned fl, bool isNew, int id
     d.A.shear[e] = dd4(shearForce1, 0);
     fl |= F_FORCE;
   }
+  fl = (fl & ~F_ITERS_MASK) | (itersBucket(g.lmCalls > 0 ? g.lmIters : 0) << F_ITERS_SHIFT);
   d.A.flags[e] = fl;
 }
 
@@ -1411,10 +1418,13 @@ __global__ void __launch_bounds__(128, 3) k_contacts_pre(Dev d) {
         if (done) finishEntry(d, e, fl, isNew, id1, b1, b2, g, cnt);
         else {
           queue = true;
-          // Nelder-Mead searches expected short (a contact touching at the previous step: the
-          // warm start usually converges on its first simplex) go to the back of the queue, so
-          // that the long ones (new or re-touching contacts) start first
-          shortq = d.prm->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN && !isNew && prevDepth > 0;
+          // searches expected short go to the back of the queue, so that the long ones start
+          // first: Nelder-Mead searches of a contact touching at the previous step (the warm start
+          // usually converges on its first simplex), Levenberg-Marquardt searches of an existing
+          // contact that took fewer than 4 iterations at the last step
+          shortq = d.prm->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN
+                       ? (!isNew && prevDepth > 0)
+                       : (!isNew && ((fl & F_ITERS_MASK) >> F_ITERS_SHIFT) < LONG_ITERS_BUCKET);
         }
       }
     }
@@ -1460,6 +1470,16 @@ struct LMLane {
 };
 
 static const int LM_BS = 128;
+
+// x^3 for the damping update of lmder2 (pow(2*tmp - 1., 3.), Superquadrics_Ig2.cpp:1299): x^2
+// split exactly into h + l with a fused multiply-add, then h x + l x with one rounding — the
+// correctly rounded cube except in cases of measure ~2^-50, where it is off by one ulp, as a
+// general-purpose pow may be.  Four FMA-class operations instead of a general FP64 pow.
+__device__ __forceinline__ double cube(double x) {
+  const double h = x * x;
+  const double l = fma(x, x, -h);
+  return fma(h, x, l * x);
+}
 
 __device__ __forceinline__ void lmStartSolve(LMLane& L) {
   L.touching = true; L.stopFlag = false; L.stop = 0;
@@ -1531,7 +1551,7 @@ __device__ __forceinline__ bool lmConsume(LMLane& L) {
       const double dF = L.pfL2 - pDp_fL2;
       double tmp = dF / dL;
       if (tmp > 0.0) {
-        tmp = 1.0 - pow(2 * tmp - 1., 3.);
+        tmp = 1.0 - cube(2 * tmp - 1.);
         L.mu = L.mu * ((tmp >= 0.3333333333333334) ? tmp : 0.3333333333333334);
         L.nu = 2;
         L.p0 = L.q0; L.p1 = L.q1;
@@ -1754,8 +1774,10 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d, int fallback) {
   __shared__ double2 slotQ[LM_BS];
   __shared__ int slotOwner[LM_BS];
   const SceneState& S = *d.S;
-  const int count = fallback ? S.fbCount : S.lmCount;
+  const int nFront = fallback ? S.fbCount : S.lmCount;   // long searches first, then the short ones
+  const int count = fallback ? S.fbCount : S.lmCount + S.nmShort;
   const int* queue = fallback ? d.fbQueue : d.lmQueue;
+  const int qBack = fallback ? 0 : d.qCap - 1;
   int* head = fallback ? &d.S->fbHead : &d.S->lmHead;
   const int lane = threadIdx.x & 31;
   const int wbase = threadIdx.x & ~31;
@@ -1778,7 +1800,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d, int fallback) {
           // start a contact: Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go up to lmder2
           SqShape& A = shA[threadIdx.x];
           SqShape& B = shB[threadIdx.x];
-          L.e = queue[idx];
+          L.e = idx < nFront ? queue[idx] : queue[qBack - (idx - nFront)];
           const unsigned fl = d.A.flags[L.e];
           int id1, id2;
           entryIds(d, L.e, fl, id1, id2);
@@ -2154,7 +2176,7 @@ __device__ __forceinline__ void shapeFromGlobal(SqShape& s, const Dev& d, int b)
 // One lmder2 call ended: the restart rules of Superquadrics_Ig2.cpp:2013-2053 (as lmCallEnd).
 // Returns LMF_MORE when a restarted call begins, LMF_END when the contact's geometry is final,
 // LMF_DEFER when a restart decision falls inside its band.
-__device__ __forceinline__ int lmfCallEnd(const Dev& d, LMF& L, int id1, int id2, D3 shift2, const FFPair* P) {
+__device__ __forceinline__ int lmfCallEnd(const Dev& d, LMF& L, int id1, int id2, D3 pB) {
   for (;;) {
     L.calls++; L.iters += L.k; L.maxit += (L.stop == 3);
     bool restart = false;
@@ -2165,7 +2187,7 @@ __device__ __forceinline__ int lmfCallEnd(const Dev& d, LMF& L, int id1, int id2
         ff dd[3];
         for (int i = 0; i < 3; i++) dd[i] = ffSub(L.P2[i], L.P1[i]);
         const float dist = sqrtf(ffDot3(dd[0], dd[1], dd[2], dd[0], dd[1], dd[2]).hi);
-        const float rmaxA = P->A.rmax;
+        const float rmaxA = d.bodyFF[id1].rmax;
         const float x = 10.f * dist / rmaxA - 1.f;
         if (!(fabsf(x) >= 1e-6f)) return LMF_DEFER;
         if (x > 0.f) {
@@ -2173,8 +2195,7 @@ __device__ __forceinline__ int lmfCallEnd(const Dev& d, LMF& L, int id1, int id2
           shapeFromGlobal(A, d, id1);
           shapeFromGlobal(B, d, id2);
           const D3 p2a = d3(ffToD(L.P2[0]), ffToD(L.P2[1]), ffToD(L.P2[2]));
-          const D3 pb = d3(ffToD(P->pB[0]), ffToD(P->pB[1]), ffToD(P->pB[2]));
-          const D3 p1b = d3(ffToD(L.P1[0]), ffToD(L.P1[1]), ffToD(L.P1[2])) - pb;
+          const D3 p1b = d3(ffToD(L.P1[0]), ffToD(L.P1[1]), ffToD(L.P1[2])) - pB;
           const double va = insideValue(A, p2a), vb = insideValue(B, p1b);
           if (!(fabs(va - 1.0) >= 1e-9) || !(fabs(vb - 1.0) >= 1e-9)) return LMF_DEFER;
           if (!(1 > va) || !(1 > vb)) { L.phase = 2; restart = true; }
@@ -2184,8 +2205,7 @@ __device__ __forceinline__ int lmfCallEnd(const Dev& d, LMF& L, int id1, int id2
     if (!restart) return LMF_END;
     if (!L.fromCenter) {
       double para[2];
-      const D3 pa = xyz(d.pos[id1]);
-      centerLine(pa, xyz(d.pos[id2]) + shift2, para);
+      centerLine(xyz(d.pos[id1]), xyz(d.pos[id2]) + cellShift(*d.S, d.A.cd[L.e]), para);
       L.p0 = ffFromD(para[0]); L.p1 = ffFromD(para[1]);
       L.fromCenter = true;
       lmfStartSolve(L);
@@ -2198,22 +2218,28 @@ __device__ __forceinline__ int lmfCallEnd(const Dev& d, LMF& L, int id1, int id2
 
 // Pass 2, mixed form (see the section comment).  Rounds of one double-float evaluation per
 // lane; once the queue is drained, the lanes without a contact evaluate the points the running
-// searches of their warp ask for next (lmfPlan), as in k_contacts_lm.
+// searches of their warp ask for next (lmfPlan), as in k_contacts_lm.  Each lane's search state
+// and each round's evaluation results live in shared memory and the bodies' double-float shapes
+// are read from bodyFF, so that the registers serve the evaluation (more resident warps hide
+// the latency of its dependent FP32 chains).  A finished search's geometry goes to a compact
+// list in the merge buffer (table B); k_contacts_lm_ff_finish completes it in FP64.
+static const int FFEV_WORDS = 27;   // c, p1, p2, d (ff, 3 each), sep (ff), ill
 __global__ void __launch_bounds__(LM_BS) k_contacts_lm_ff(Dev d) {
-  __shared__ FFPair shp[LM_BS];
+  __shared__ LMF sL[LM_BS];
+  __shared__ float sEv[FFEV_WORDS][LM_BS];
+  __shared__ int sId[2][LM_BS];
+  __shared__ float sPB[6][LM_BS];
   __shared__ float4 slotQ[LM_BS];
   __shared__ int slotOwner[LM_BS];
   const SceneState& S = *d.S;
-  const int count = S.lmCount;
-  const int lane = threadIdx.x & 31;
-  const int wbase = threadIdx.x & ~31;
+  const int nFront = S.lmCount, count = S.lmCount + S.nmShort;   // long searches first
+  const int t = threadIdx.x;
+  const int lane = t & 31;
+  const int wbase = t & ~31;
   const bool spread = d.prm->lmSpread != 0;
-  Counters cnt = {0, 0, 0, 0, 0};
   unsigned long long ev32 = 0, deferred = 0;
   unsigned roundsMax = 0;
-  LMF L;
-  int id1 = 0, id2 = 0;
-  D3 shift2 = d3(0, 0, 0);
+  LMF& L = sL[t];
   bool active = false, exhausted = false;
   while (true) {
     const unsigned idle = __ballot_sync(0xffffffffu, !active && !exhausted);
@@ -2225,19 +2251,20 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_ff(Dev d) {
       if (!active && !exhausted) {
         const int idx = base + __popc(idle & ((1u << lane) - 1));
         if (idx < count) {
-          L.e = d.lmQueue[idx];
-          const unsigned fl = d.A.flags[L.e];
-          entryIds(d, L.e, fl, id1, id2);
-          shift2 = cellShift(S, d.A.cd[L.e]);
-          FFPair& P = shp[threadIdx.x];
-          P.A = d.bodyFF[id1];
-          P.B = d.bodyFF[id2];
+          const int e = idx < nFront ? d.lmQueue[idx] : d.lmQueue[d.qCap - 1 - (idx - nFront)];
+          const unsigned fl = d.A.flags[e];
+          int id1, id2;
+          entryIds(d, e, fl, id1, id2);
+          const D3 shift2 = cellShift(S, d.A.cd[e]);
           const D3 pa = xyz(d.pos[id1]), pb = xyz(d.pos[id2]) + shift2;
-          P.pB[0] = ffFromD(pb.x - pa.x); P.pB[1] = ffFromD(pb.y - pa.y); P.pB[2] = ffFromD(pb.z - pa.z);
-          L.E = 4e-13f * (P.A.rmax + P.B.rmax);
+          sId[0][t] = id1; sId[1][t] = id2;
+          const ff px = ffFromD(pb.x - pa.x), py = ffFromD(pb.y - pa.y), pz = ffFromD(pb.z - pa.z);
+          sPB[0][t] = px.hi; sPB[1][t] = px.lo; sPB[2][t] = py.hi; sPB[3][t] = py.lo; sPB[4][t] = pz.hi; sPB[5][t] = pz.lo;
+          L.e = e;
+          L.E = 4e-13f * (d.bodyFF[id1].rmax + d.bodyFF[id2].rmax);
           L.isNew = !(fl & F_GEOM);
           if (L.isNew) { double para[2]; centerLine(pa, pb, para); L.p0 = ffFromD(para[0]); L.p1 = ffFromD(para[1]); }
-          else { const double2 an = d.A.angle[L.e]; L.p0 = ffFromD(an.x); L.p1 = ffFromD(an.y); }
+          else { const double2 an = d.A.angle[e]; L.p0 = ffFromD(an.x); L.p1 = ffFromD(an.y); }
           L.fromCenter = L.isNew;
           L.phase = 0; L.calls = 0; L.iters = 0; L.maxit = 0; L.rounds = 0;
           lmfStartSolve(L);
@@ -2250,74 +2277,60 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_ff(Dev d) {
     const int nA = __popc(act);
     const bool drained = spread && __any_sync(0xffffffffu, exhausted);
     int spc, base, jmax;
-    allocSlots(active, L.rounds, drained ? 32 : nA, spc, base, jmax);
-    slotOwner[threadIdx.x] = -1;
+    allocSlots(active, active ? L.rounds : 0u, drained ? 32 : nA, spc, base, jmax);
+    slotOwner[t] = -1;
     __syncwarp();
     if (active) lmfPlan(L, &slotQ[wbase + base], &slotOwner[wbase + base], spc, lane);
     __syncwarp();
-    FFEval v;
-    const int own = slotOwner[threadIdx.x];
     {
       // lanes without a slot evaluate the warp's first slot (whose owner always exists) so that
       // every lane computes on valid inputs
-      const int slot = own >= 0 ? threadIdx.x : wbase;
+      const int own = slotOwner[t];
+      const int slot = own >= 0 ? t : wbase;
       const int src = wbase + slotOwner[slot];
       const float4 q = slotQ[slot];
-      ffDisfunction(shp[src].A, shp[src].B, shp[src].pB, mkff(q.x, q.y), mkff(q.z, q.w), v);
+      const ff pB[3] = {mkff(sPB[0][src], sPB[1][src]), mkff(sPB[2][src], sPB[3][src]), mkff(sPB[4][src], sPB[5][src])};
+      FFEval v;
+      ffDisfunction(d.bodyFF[sId[0][src]], d.bodyFF[sId[1][src]], pB, mkff(q.x, q.y), mkff(q.z, q.w), v);
+      for (int i = 0; i < 3; i++) {
+        sEv[2 * i][t] = v.c[i].hi; sEv[2 * i + 1][t] = v.c[i].lo;
+        sEv[6 + 2 * i][t] = v.p1[i].hi; sEv[7 + 2 * i][t] = v.p1[i].lo;
+        sEv[12 + 2 * i][t] = v.p2[i].hi; sEv[13 + 2 * i][t] = v.p2[i].lo;
+        sEv[18 + 2 * i][t] = v.d[i].hi; sEv[19 + 2 * i][t] = v.d[i].lo;
+      }
+      sEv[24][t] = v.sep.hi; sEv[25][t] = v.sep.lo; sEv[26][t] = v.ill ? 1.f : 0.f;
       if (own >= 0) ev32++;
     }
-    if (active) L.rounds++;
-    for (int j = 0; j < jmax; j++) {
-      const int si = base + j;
-      const bool mine = j < spc;
-      const int src = mine ? si : lane;
-      FFEval w;
-#define SHF(x) __shfl_sync(0xffffffffu, (x), src)
-      for (int i = 0; i < 3; i++) {
-        w.c[i] = mkff(SHF(v.c[i].hi), SHF(v.c[i].lo)); w.p1[i] = mkff(SHF(v.p1[i].hi), SHF(v.p1[i].lo));
-        w.p2[i] = mkff(SHF(v.p2[i].hi), SHF(v.p2[i].lo)); w.d[i] = mkff(SHF(v.d[i].hi), SHF(v.d[i].lo));
-      }
-      w.sep = mkff(SHF(v.sep.hi), SHF(v.sep.lo));
-      w.ill = SHF((int)v.ill) != 0;
-#undef SHF
-      if (mine && active && slotOwner[wbase + si] == lane && sameFF(slotQ[wbase + si], L.q0, L.q1)) {
-        int r = lmfConsume(L, w);
-        if (r == LMF_END) r = lmfCallEnd(d, L, id1, id2, shift2, &shp[threadIdx.x]);
-        if (r == LMF_END) {
-          // end of Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go (FP64), then Ip2 + law
-          const int e = L.e;
-          const unsigned fl = d.A.flags[e];
-          const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
-          GeomOut g;
-          g.lmCalls = L.calls; g.lmIters = L.iters; g.lmStop = 0; g.nanNormal = false;
-          g.isShearNew = L.isNew ? true : (d.A.depth[e] <= 0);
-          g.cp = L.isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
-          g.ang0 = ffToD(L.p0); g.ang1 = ffToD(L.p1); g.angSet = true;
-          bool ok = true;
-          if (!L.touching) {
-            g.precomputed = false; g.depth = 0; g.isShearNew = true;
-          } else {
-            const D3 P1 = b1.pos + d3(ffToD(L.P1[0]), ffToD(L.P1[1]), ffToD(L.P1[2]));
-            const D3 P2 = b1.pos + d3(ffToD(L.P2[0]), ffToD(L.P2[1]), ffToD(L.P2[2]));
-            const D3 contact = d3(ffToD(L.c[0]), ffToD(L.c[1]), ffToD(L.c[2]));
-            const double pDepth = dot(P1 - P2, contact);
-            if (!(fabs(pDepth - 1e-18) >= (double)L.E)) ok = false;   // the law's contact gate
-            g.p1 = P1; g.p2 = P2;
-            g.cp = 0.5 * (P1 + P2);
-            g.depth = pDepth;
-            D3 cn = contact;
-            normalize(cn);
-            const D3 oldNormal = L.isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
-            g.precomputed = true;
-            precomputeD(g, oldNormal, b1, b2, d.prm->dt, cn, g.isShearNew, shift2);
-            g.normal = cn;
-          }
-          if (ok) {
-            cnt.lmCalls += L.calls; cnt.lmIters += L.iters; cnt.lmMax += L.maxit;
-            finishEntry(d, e, fl, L.isNew, id1, b1, b2, g, cnt);
-          } else r = LMF_DEFER;
+    __syncwarp();
+    if (active) {
+      L.rounds++;
+      for (int j = 0; j < spc; j++) {
+        const int si = wbase + base + j;
+        if (!(slotOwner[si] == lane && sameFF(slotQ[si], L.q0, L.q1))) continue;
+        FFEval w;
+        for (int i = 0; i < 3; i++) {
+          w.c[i] = mkff(sEv[2 * i][si], sEv[2 * i + 1][si]);
+          w.p1[i] = mkff(sEv[6 + 2 * i][si], sEv[7 + 2 * i][si]);
+          w.p2[i] = mkff(sEv[12 + 2 * i][si], sEv[13 + 2 * i][si]);
+          w.d[i] = mkff(sEv[18 + 2 * i][si], sEv[19 + 2 * i][si]);
         }
-        if (r == LMF_DEFER) {
+        w.sep = mkff(sEv[24][si], sEv[25][si]);
+        w.ill = sEv[26][si] != 0.f;
+        int r = lmfConsume(L, w);
+        if (r == LMF_END) r = lmfCallEnd(d, L, sId[0][t], sId[1][t],
+                                         d3(ffToD(mkff(sPB[0][t], sPB[1][t])), ffToD(mkff(sPB[2][t], sPB[3][t])),
+                                            ffToD(mkff(sPB[4][t], sPB[5][t]))));
+        if (r == LMF_END) {
+          // the search's geometry to the finish list (merge buffer), completed in FP64 by
+          // k_contacts_lm_ff_finish
+          const int i = atomicAdd(&d.S->nmFin, 1);
+          d.B.owner[i] = L.e;
+          d.B.angle[i] = make_double2(ffToD(L.p0), ffToD(L.p1));
+          d.B.p1[i] = make_double4(ffToD(L.P1[0]), ffToD(L.P1[1]), ffToD(L.P1[2]), 0);
+          d.B.p2[i] = make_double4(ffToD(L.P2[0]), ffToD(L.P2[1]), ffToD(L.P2[2]), 0);
+          d.B.normal[i] = make_double4(ffToD(L.c[0]), ffToD(L.c[1]), ffToD(L.c[2]), 0);
+          d.B.cd[i] = make_int4((int)L.calls, (int)L.iters, (int)L.maxit, L.touching ? 1 : 0);
+        } else if (r == LMF_DEFER) {
           const int k = atomicAdd(&d.S->fbCount, 1);
           d.fbQueue[k] = L.e;
           deferred++;
@@ -2325,12 +2338,12 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_ff(Dev d) {
         if (r != LMF_MORE) {
           active = false;
           roundsMax = max(roundsMax, L.rounds);
+          break;   // the rest of this round's slots were planned for the call that ended
         }
       }
     }
     __syncwarp();
   }
-  flushCounters(d, cnt);
   for (int o = 16; o > 0; o >>= 1) {
     ev32 += __shfl_down_sync(0xffffffffu, ev32, o);
     deferred += __shfl_down_sync(0xffffffffu, deferred, o);
@@ -2339,8 +2352,67 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_ff(Dev d) {
   if (lane == 0) {
     atomicAdd(&d.S->err[E_EVAL32], ev32);
     atomicAdd(&d.S->err[E_FALLBACK], deferred);
-    atomicMax(&d.S->err[E_ROUNDS_MAX], (unsigned long long)roundsMax);
+    atomicMax(&d.S->err[E_ROUNDS_MAX_FF], (unsigned long long)roundsMax);
   }
+}
+
+// The end of Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go (Superquadrics_Ig2.cpp:
+// 2054-2095) in FP64 for the searches k_contacts_lm_ff finished, one thread per search: the
+// contact points in the global frame, the depth (deferred to the FP64 kernel when inside the
+// band of the law's contact gate), normal, precompute, then Ip2 and the law.
+__global__ void __launch_bounds__(128) k_contacts_lm_ff_finish(Dev d) {
+  const SceneState& S = *d.S;
+  if (S.skip) return;
+  const int n = S.nmFin;
+  const double dt = d.prm->dt;
+  Counters cnt = {0, 0, 0, 0, 0};
+  unsigned long long deferred = 0;
+  for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+    const int i = i0 + threadIdx.x;
+    if (i >= n) continue;
+    const int e = d.B.owner[i];
+    const int4 info = d.B.cd[i];
+    const unsigned fl = d.A.flags[e];
+    int id1, id2;
+    entryIds(d, e, fl, id1, id2);
+    const BodyView b1 = loadBody(d, id1), b2 = loadBody(d, id2);
+    const bool isNew = !(fl & F_GEOM);
+    GeomOut g;
+    g.lmCalls = info.x; g.lmIters = info.y; g.lmStop = 0; g.nanNormal = false;
+    g.isShearNew = isNew ? true : (d.A.depth[e] <= 0);
+    g.cp = isNew ? d3(0, 0, 0) : xyz(d.A.cp[e]);
+    const double2 an = d.B.angle[i];
+    g.ang0 = an.x; g.ang1 = an.y; g.angSet = true;
+    bool ok = true;
+    if (!info.w) {
+      g.precomputed = false; g.depth = 0; g.isShearNew = true;
+    } else {
+      const D3 P1 = b1.pos + xyz(d.B.p1[i]), P2 = b1.pos + xyz(d.B.p2[i]);
+      const D3 contact = xyz(d.B.normal[i]);
+      const double pDepth = dot(P1 - P2, contact);
+      const double E = 4e-13 * (b1.shpA.w + b2.shpA.w);
+      if (!(fabs(pDepth - 1e-18) >= E)) ok = false;   // the law's contact gate inside its band
+      g.p1 = P1; g.p2 = P2;
+      g.cp = 0.5 * (P1 + P2);
+      g.depth = pDepth;
+      D3 cn = contact;
+      normalize(cn);
+      const D3 oldNormal = isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
+      g.precomputed = true;
+      precomputeD(g, oldNormal, b1, b2, dt, cn, g.isShearNew, cellShift(S, d.A.cd[e]));
+      g.normal = cn;
+    }
+    if (ok) {
+      cnt.lmCalls += info.x; cnt.lmIters += info.y; cnt.lmMax += info.z;
+      finishEntry(d, e, fl, isNew, id1, b1, b2, g, cnt);
+    } else {
+      const int k = atomicAdd(&d.S->fbCount, 1);
+      d.fbQueue[k] = e;
+      deferred++;
+    }
+  }
+  flushCounters(d, cnt);
+  if (deferred) atomicAdd(&d.S->err[E_FALLBACK], deferred);
 }
 
 // contribution of table entry e to body b (b is id1 when asId1)
@@ -2972,9 +3044,10 @@ static void launchContactStage(sqdem_ctx* c, const Dev& d, int grid) {
       if (c->timingSearch) cudaEventRecord(c->ev[4], s);
       k_contacts_lm_ff<<<grid, LM_BS, 0, s>>>(d);
       if (c->timingSearch) cudaEventRecord(c->ev[5], s);
+      k_contacts_lm_ff_finish<<<std::min(nblk(d.Pcap, 128), c->numSMs * 8), 128, 0, s>>>(d);
       k_contacts_lm<<<grid, LM_BS, 0, s>>>(d, 1);
       if (c->timingSearch) cudaEventRecord(c->ev[6], s);
-      c->launches += 4;
+      c->launches += 5;
     } else {
       if (c->timingSearch) cudaEventRecord(c->ev[4], s);
       k_contacts_lm<<<grid, LM_BS, 0, s>>>(d, 0);
@@ -3398,6 +3471,7 @@ sqdem_status sqdem_sync(sqdem_ctx* c, sqdem_report* r) {
     r->evals_fp32 = (long long)e[E_EVAL32]; r->evals_fp64 = (long long)e[E_EVAL64];
     r->lm_rounds_max = (long long)e[E_ROUNDS_MAX];
     r->fallback_fp64 = (long long)e[E_FALLBACK];
+    r->lm_rounds_max_ff = (long long)e[E_ROUNDS_MAX_FF];
   }
   if (e[E_OVERFLOW]) return fail(c, SQDEM_ERR_CAPACITY, "contact table or candidate buffer overflow; increase contacts_per_body");
   return SQDEM_OK;
@@ -4455,6 +4529,7 @@ sqdem_status sqdem_batch_sync(sqdem_batch* B, sqdem_report* total) {
       total->lm_iterations += r.lm_iterations; total->lm_maxiter += r.lm_maxiter; total->overflow += r.overflow;
       total->collider_runs += r.collider_runs; total->steps += r.steps; total->evals_fp32 += r.evals_fp32;
       total->evals_fp64 += r.evals_fp64; total->lm_rounds_max = std::max(total->lm_rounds_max, r.lm_rounds_max);
+      total->fallback_fp64 += r.fallback_fp64; total->lm_rounds_max_ff = std::max(total->lm_rounds_max_ff, r.lm_rounds_max_ff);
     }
   }
   return first;

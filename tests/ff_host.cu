@@ -83,3 +83,28 @@ extern "C" void ffh_lmder2(const double* shapeA5, const double* qA, const double
   for (int i = 0; i < 3; i++) { out[2 + i] = ffToD(L.P1[i]); out[5 + i] = ffToD(L.P2[i]); out[8 + i] = ffToD(L.c[i]); }
   out[11] = L.touching ? 1 : 0; out[12] = L.k; out[13] = L.stop; out[14] = evals; out[15] = r;
 }
+
+// The same evaluation as tests/ff_device_probe.cu's kernel, on the host: in 26 doubles per case
+// (shapeA5, qA4 used as given, posA3, shapeB5, qB4, posB3, pa0, pa1), out 14 doubles.
+extern "C" void ffh_disfunction_raw(const double* in, long n, double* out) {
+  for (long i = 0; i < n; i++) {
+    const double* v = in + 26 * i;
+    SqShape A, B;
+    double ra = v[0] > v[1] ? v[0] : v[1]; ra = ra > v[2] ? ra : v[2];
+    double rb = v[12] > v[13] ? v[12] : v[13]; rb = rb > v[14] ? rb : v[14];
+    shapeInit(A, v[0], v[1], v[2], v[3], v[4], ra);
+    A.R = quatToRot(v[5], v[6], v[7], v[8]);
+    A.pos = d3(v[9], v[10], v[11]);
+    shapeInit(B, v[12], v[13], v[14], v[15], v[16], rb);
+    B.R = quatToRot(v[17], v[18], v[19], v[20]);
+    B.pos = d3(v[21], v[22], v[23]);
+    FFPair P;
+    ffPairInit(P, A, B);
+    FFEval r;
+    ffDisfunction(P, v[24], v[25], r);
+    double* o = out + 14 * i;
+    for (int k = 0; k < 3; k++) { o[k] = ffToD(r.p1[k]); o[3 + k] = ffToD(r.p2[k]); o[6 + k] = ffToD(r.d[k]); o[11 + k] = ffToD(r.c[k]); }
+    o[9] = ffToD(r.sep);
+    o[10] = r.ill ? 1 : 0;
+  }
+}
