@@ -48,6 +48,7 @@ def lib():
         "sqo_disfunction": (None, [dp, dp, dp, dp, dp, dp, d, d, dp, dp]),
         "sqo_lmder2": (None, [dp, dp, dp, dp, dp, dp, dp, dp]),
         "sqo_set_periodic_fix": (None, [v, i]),
+        "sqo_set_math_noise": (None, [C.c_ulonglong, d]),
         "sqo_get_scalars": (None, [v, dp]), "sqo_set_scalars": (None, [v, dp]),
         "sqo_rebuild_sorted_bounds": (None, [v]),
         "sqo_pair_geom": (i, [v, i, i, i, dp, dp]),
@@ -141,6 +142,13 @@ def normal2phi(shape5, n):
     n = np.ascontiguousarray(n, dtype=np.float64)
     lib().sqo_normal2phi(*[float(x) for x in shape5], _dp(n), _dp(out))
     return out
+
+
+def set_math_noise(seed, rel=0.0):
+    """Last-bit noise on the narrowphase's pow/sin/cos/atan2 results (seed 0: off).  rel = 0 moves
+    a result by one ulp, rel > 0 by rel * |value|; the sign (-1, 0, +1) comes from a hash of the
+    value and the seed.  Process-wide; set between steps."""
+    lib().sqo_set_math_noise(int(seed), float(rel))
 
 
 class OracleScene:

@@ -160,18 +160,46 @@ static void sqInitial(SQ& s) {
   s.inertia[2] = 0.5 * a * (std::pow(s.rx, 2.) + std::pow(s.ry, 2.)) * beta1;
 }
 
+// Last-bit noise on the transcendental calls of the narrowphase (a test instrument; off unless a
+// seed is set).  With seed != 0 every pow/sin/cos/atan2 result of the Disfunction and of the
+// Nelder-Mead geometry moves by -1, 0 or +1 unit, chosen by a hash of the value and the seed: one
+// ulp when rel == 0, else rel * |value|.  This models another libm whose results differ from
+// glibc's in the last bits (CUDA's do).  How far a pair's result moves over a few seeds is the
+// reference's own conditioning at FP64: the part of its answer that its inputs and its
+// arithmetic do not determine.
+static uint64_t g_noiseSeed = 0;
+static double g_noiseRel = 0;
+static inline double NZ(double v) {
+  if (!g_noiseSeed || !(v != 0) || !std::isfinite(v)) return v;
+  uint64_t h;
+  std::memcpy(&h, &v, 8);
+  h ^= g_noiseSeed;
+  h += 0x9e3779b97f4a7c15ULL;
+  h = (h ^ (h >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  h = (h ^ (h >> 27)) * 0x94d049bb133111ebULL;
+  h ^= h >> 31;
+  const int s = (int)(h % 3) - 1;
+  if (!s) return v;
+  if (g_noiseRel > 0) return v + s * std::fabs(v) * g_noiseRel;
+  return std::nextafter(v, s > 0 ? Inf : -Inf);
+}
+#define NPOW(a, b) NZ(std::pow(a, b))
+#define NSIN(a) NZ(std::sin(a))
+#define NCOS(a) NZ(std::cos(a))
+#define NATAN2(a, b) NZ(std::atan2(a, b))
+
 // Superquadrics.cpp:103-108
 static bool sqIsInside(const SQ& s, V3 p) {
   p = mul(s.loc, p);
-  return 1 > std::pow(std::pow(std::fabs(p[0] / s.rx), 2.0 / s.eps1) + std::pow(std::fabs(p[1] / s.ry), 2.0 / s.eps1),
-                      s.eps1 / s.eps2) + std::pow(std::fabs(p[2] / s.rz), 2.0 / s.eps2);
+  return 1 > NPOW(NPOW(std::fabs(p[0] / s.rx), 2.0 / s.eps1) + NPOW(std::fabs(p[1] / s.ry), 2.0 / s.eps1),
+                      s.eps1 / s.eps2) + NPOW(std::fabs(p[2] / s.rz), 2.0 / s.eps2);
 }
 // Superquadrics.cpp:110-120 (local surface point from the two surface angles)
 static inline V3 sqSurface(const SQ& s, Real ph0, Real ph1) {
   V3 r;
-  r[0] = Sign(std::cos(ph0)) * s.rx * std::pow(std::fabs(std::cos(ph0)), s.eps1) * std::pow(std::fabs(std::cos(ph1)), s.eps2);
-  r[1] = Sign(std::sin(ph0)) * s.ry * std::pow(std::fabs(std::sin(ph0)), s.eps1) * std::pow(std::fabs(std::cos(ph1)), s.eps2);
-  r[2] = Sign(std::sin(ph1)) * s.rz * std::pow(std::fabs(std::sin(ph1)), s.eps2);
+  r[0] = Sign(NCOS(ph0)) * s.rx * NPOW(std::fabs(NCOS(ph0)), s.eps1) * NPOW(std::fabs(NCOS(ph1)), s.eps2);
+  r[1] = Sign(NSIN(ph0)) * s.ry * NPOW(std::fabs(NSIN(ph0)), s.eps1) * NPOW(std::fabs(NCOS(ph1)), s.eps2);
+  r[2] = Sign(NSIN(ph1)) * s.rz * NPOW(std::fabs(NSIN(ph1)), s.eps2);
   return r;
 }
 // Margins of the decisions one pair's narrowphase and law took this step (minimum over every
@@ -194,10 +222,10 @@ static inline void margMin(int k, double v) {
 
 // Superquadrics.cpp:269-307 (surface angles of the point whose outward normal is n, local frame)
 static inline void sqNormal2Phi(const SQ& s, const V3& n, Real& ph0, Real& ph1) {
-  ph0 = std::atan2(Sign(n[1]) * std::pow(std::fabs(s.ry * n[1]), 1 / (2. - s.eps1)),
-                   Sign(n[0]) * std::pow(std::fabs(s.rx * n[0]), 1 / (2. - s.eps1)));
-  ph1 = std::atan2(Sign(n[2]) * std::pow(std::fabs(s.rz * n[2] * std::pow(std::fabs(std::cos(ph0)), 2. - s.eps1)), 1 / (2. - s.eps2)),
-                   std::pow(std::fabs(s.rx * n[0]), 1 / (2. - s.eps2)));
+  ph0 = NATAN2(Sign(n[1]) * NPOW(std::fabs(s.ry * n[1]), 1 / (2. - s.eps1)),
+                   Sign(n[0]) * NPOW(std::fabs(s.rx * n[0]), 1 / (2. - s.eps1)));
+  ph1 = NATAN2(Sign(n[2]) * NPOW(std::fabs(s.rz * n[2] * NPOW(std::fabs(NCOS(ph0)), 2. - s.eps1)), 1 / (2. - s.eps2)),
+                   NPOW(std::fabs(s.rx * n[0]), 1 / (2. - s.eps2)));
   if (g_marg) {
     margMin(8, std::cos(ph0)); margMin(8, std::cos(ph1));
     if (std::fabs(ph0) > 1.5707963267948966) margMin(8, std::sin(ph0));
@@ -206,9 +234,9 @@ static inline void sqNormal2Phi(const SQ& s, const V3& n, Real& ph0, Real& ph1) 
 // Superquadrics.cpp:258-266 (local, unnormalised outward normal at angles phi)
 static inline V3 sqNormal(const SQ& s, Real ph0, Real ph1) {
   V3 n;
-  n[0] = Sign(std::cos(ph0)) / s.rx * std::pow(std::fabs(std::cos(ph0)), 2. - s.eps1) * std::pow(std::fabs(std::cos(ph1)), 2. - s.eps2);
-  n[1] = Sign(std::sin(ph0)) / s.ry * std::pow(std::fabs(std::sin(ph0)), 2. - s.eps1) * std::pow(std::fabs(std::cos(ph1)), 2. - s.eps2);
-  n[2] = Sign(std::sin(ph1)) / s.rz * std::pow(std::fabs(std::sin(ph1)), 2. - s.eps2);
+  n[0] = Sign(NCOS(ph0)) / s.rx * NPOW(std::fabs(NCOS(ph0)), 2. - s.eps1) * NPOW(std::fabs(NCOS(ph1)), 2. - s.eps2);
+  n[1] = Sign(NSIN(ph0)) / s.ry * NPOW(std::fabs(NSIN(ph0)), 2. - s.eps1) * NPOW(std::fabs(NCOS(ph1)), 2. - s.eps2);
+  n[2] = Sign(NSIN(ph1)) / s.rz * NPOW(std::fabs(NSIN(ph1)), 2. - s.eps2);
   return n;
 }
 
@@ -616,7 +644,7 @@ struct PairCtx {
 // Disfunction, 9-argument form (Superquadrics_Ig2.cpp:622-687)
 static inline void disfunction(const PairCtx& c, Real pa0, Real pa1, V3& center, V3& p1, V3& p2, bool& stop_flag) {
   (*c.disCalls)++;
-  V3 contact(std::cos(pa0) * std::cos(pa1), std::sin(pa0) * std::cos(pa1), std::sin(pa1));
+  V3 contact(NCOS(pa0) * NCOS(pa1), NSIN(pa0) * NCOS(pa1), NSIN(pa1));
   V3 contact1 = mul(c.A->loc, contact);
   Real ph0, ph1;
   sqNormal2Phi(*c.A, contact1, ph0, ph1);
@@ -670,9 +698,9 @@ static void lmder2(const PairCtx& c, Real p[2], int itmax, V3& p1, V3& p2, V3& c
     if (p_fL2 <= eps3) { stop = 6; break; }
     if (stop_flag) { stop = 9; touching = false; break; }
     {
-      contact[0] = std::cos(p[0]) * std::cos(p[1]);
-      contact[1] = std::sin(p[0]) * std::cos(p[1]);
-      contact[2] = std::sin(p[1]);
+      contact[0] = NCOS(p[0]) * NCOS(p[1]);
+      contact[1] = NSIN(p[0]) * NCOS(p[1]);
+      contact[2] = NSIN(p[1]);
       Real angle = dot(p_f, contact) / (norm(p_f) * norm(contact));
       margMin(1, std::fabs(angle) - 0.95);
       if (std::fabs(angle) > 0.95) { stop = 8; break; }
@@ -715,7 +743,7 @@ static void lmder2(const PairCtx& c, Real p[2], int itmax, V3& p1, V3& p2, V3& c
       margMin(3, dF);
       tmp = dF / dL;
       if (tmp > 0.0) {
-        tmp = 1.0 - std::pow(2 * tmp - 1., 3.);
+        tmp = 1.0 - NPOW(2 * tmp - 1., 3.);
         mu = mu * ((tmp >= ONE_THIRD) ? tmp : ONE_THIRD);
         nu = 2;
         p[0] = pDp[0]; p[1] = pDp[1];
@@ -753,7 +781,7 @@ static void precompute(Geom& g, const Body& b1, const Body& b2, Real dt, const V
 
 static inline void centerLine(const V3& pos1, const V3& pos2, Real para[2]) {
   V3 d0 = pos2 - pos1;
-  para[0] = std::atan2(d0[1], d0[0]);
+  para[0] = NATAN2(d0[1], d0[0]);
   para[1] = std::atan(d0[2] / std::sqrt(d0[0] * d0[0] + d0[1] * d0[1]));
   para[0] += 1e-5; para[1] += 1e-5;
 }
@@ -813,8 +841,8 @@ static bool ig2SqSq(Scene& S, Interaction* I, const Body& b1, const Body& b2, co
       margMin(5, (10.0 * norm(p2 - p1) - A->r_max) / A->r_max);
       if (10.0 * norm(p2 - p1) > A->r_max) {
         V3 q = mul(A->loc, p2 - position1);
-        margMin(6, std::pow(std::pow(std::fabs(q[0] / A->rx), 2.0 / A->eps1) + std::pow(std::fabs(q[1] / A->ry), 2.0 / A->eps1),
-                            A->eps1 / A->eps2) + std::pow(std::fabs(q[2] / A->rz), 2.0 / A->eps2) - 1);
+        margMin(6, NPOW(NPOW(std::fabs(q[0] / A->rx), 2.0 / A->eps1) + NPOW(std::fabs(q[1] / A->ry), 2.0 / A->eps1),
+                            A->eps1 / A->eps2) + NPOW(std::fabs(q[2] / A->rz), 2.0 / A->eps2) - 1);
       }
     }
     if (touching) {
@@ -998,7 +1026,7 @@ static M3 cRotationMat(const V3& position1, const V3& position2) {
 // direction given by the angles in the CRotationMat frame
 static Real disfun(const Real para[2], const SQ& A, const SQ& B, const V3& position1, const V3& position2, V3& p1,
                    V3& p2, const M3& gc, bool& touching, long* nev) {
-  V3 contact(std::cos(para[0]) * std::cos(para[1]), std::sin(para[0]) * std::cos(para[1]), std::sin(para[1]));
+  V3 contact(NCOS(para[0]) * NCOS(para[1]), NSIN(para[0]) * NCOS(para[1]), NSIN(para[1]));
   contact = mul(gc, contact);
   Real ph0, ph1;
   sqNormal2Phi(A, mul(A.loc, contact), ph0, ph1);
@@ -1093,13 +1121,13 @@ static void sqCurvatures(const SQ& q, Real ph0, Real ph1, V3& dirMax, V3& dirMin
   if (std::fabs(ph0) < 1E-20) ph0 = 1E-20;
   if (std::fabs(ph1) < 1E-20) ph1 = 1E-20;
   const Real rx = q.rx, ry = q.ry, rz = q.rz, eps1 = q.eps1, eps2 = q.eps2;
-  const Real s1 = std::sin(ph0), s2 = std::sin(ph1), c1 = std::cos(ph0), c2 = std::cos(ph1);
+  const Real s1 = NSIN(ph0), s2 = NSIN(ph1), c1 = NCOS(ph0), c2 = NCOS(ph1);
   const Real s_s1 = Sign(s1), s_s2 = Sign(s2), s_c1 = Sign(c1), s_c2 = Sign(c2);
   const Real abs_s1 = std::fabs(s1), abs_s2 = std::fabs(s2), abs_c1 = std::fabs(c1), abs_c2 = std::fabs(c2);
-  const Real s10 = s_s1 * std::pow(abs_s1, eps1), s20 = s_s2 * std::pow(abs_s2, eps2);
-  const Real c10 = s_c1 * std::pow(abs_c1, eps1), c20 = s_c2 * std::pow(abs_c2, eps2);
-  const Real s12 = s_s1 * std::pow(abs_s1, eps1 - 2.0), s22 = s_s2 * std::pow(abs_s2, eps2 - 2.0);
-  const Real c12 = s_c1 * std::pow(abs_c1, eps1 - 2.0), c22 = s_c2 * std::pow(abs_c2, eps2 - 2.0);
+  const Real s10 = s_s1 * NPOW(abs_s1, eps1), s20 = s_s2 * NPOW(abs_s2, eps2);
+  const Real c10 = s_c1 * NPOW(abs_c1, eps1), c20 = s_c2 * NPOW(abs_c2, eps2);
+  const Real s12 = s_s1 * NPOW(abs_s1, eps1 - 2.0), s22 = s_s2 * NPOW(abs_s2, eps2 - 2.0);
+  const Real c12 = s_c1 * NPOW(abs_c1, eps1 - 2.0), c22 = s_c2 * NPOW(abs_c2, eps2 - 2.0);
   const V3 R1(-rx * eps1 * c12 * c1 * c20 * s1, ry * eps1 * c1 * c20 * s12 * s1, 0);
   const V3 R2(-rx * eps2 * c10 * c22 * c2 * s2, -ry * eps2 * c22 * c2 * s10 * s2, rz * eps2 * c2 * s22 * s2);
   const V3 R11(rx * eps1 * c12 * s20 * s1 * s1 * (eps1 - 1.0) - rx * eps1 * c10 * c20,
@@ -1132,7 +1160,7 @@ static void hertzMindlin(Geom& g, const Real c1[2], const Real c2[2], Real theta
   if (rho21 * rho22 < 1E-18) rho21 = rho22 = 0.0;
   const Real sum_rho = ((rho11 + rho12) + rho21) + rho22;
   const Real F_rho = -std::sqrt((std::pow(rho11 - rho12, 2) + std::pow(rho21 - rho22, 2)) +
-                                2 * (std::fabs(rho11 - rho12)) * std::fabs(rho21 - rho22) * std::cos(2 * theta));
+                                2 * (std::fabs(rho11 - rho12)) * std::fabs(rho21 - rho22) * NCOS(2 * theta));
   const Real A = (sum_rho + F_rho) / 4., B = (sum_rho - F_rho) / 4.;
   g.curvatures_sum = A + B;
   const Real x_squ = std::pow(std::log10(B / A), 2);
@@ -1198,7 +1226,7 @@ static bool ig2SqSq2(Scene& S, Interaction* I, const Body& b1, const Body& b2, c
     g.point1 = p1; g.point2 = p2;
     g.contactPoint = 0.5 * (p1 + p2);
     g.PenetrationDepth = info[1];
-    V3 contact(std::cos(para[0]) * std::sin(para[1]), std::sin(para[0]) * std::sin(para[1]), std::cos(para[1]));
+    V3 contact(NCOS(para[0]) * NSIN(para[1]), NSIN(para[0]) * NSIN(para[1]), NCOS(para[1]));
     contact = mul(gc, contact);
     const V3 contact1 = mul(A->loc, contact), contact2 = mul(B->loc, contact);
     V3 dmax1, dmax2, dmin1, dmin2;
@@ -1434,8 +1462,8 @@ static void leapfrogSphericalRotate(Scene& S, Body& b) {
     V3 axis(b.angVel[0] / angle, b.angVel[1] / angle, b.angVel[2] / angle);
     // Quaternionr(AngleAxisr(angle*dt, axis)): w = cos(h), vec = sin(h)*axis
     Real h = 0.5 * (angle * S.dt);
-    Real s = std::sin(h);
-    Quat q{std::cos(h), s * axis[0], s * axis[1], s * axis[2]};
+    Real s = NSIN(h);
+    Quat q{NCOS(h), s * axis[0], s * axis[1], s * axis[2]};
     // q * ori (Hamilton product, Eigen Quaternion.h quat_product)
     Quat o = b.ori;
     Quat r;
@@ -1953,6 +1981,10 @@ void sqo_lmder2(const double* shapeA5, const double* qA, const double* posA, con
 }
 
 void sqo_set_periodic_fix(void* h, int on) { ((Scene*)h)->periodicFix = on != 0; }
+
+// Test instrument: last-bit noise on the narrowphase's transcendental calls (NZ above); seed 0
+// turns it off.  Process-wide: set it between steps, not while one runs.
+void sqo_set_math_noise(unsigned long long seed, double rel) { g_noiseSeed = seed; g_noiseRel = rel; }
 
 void sqo_set_params(void* h, double dt, const double* gravity, double damping, double verletDist, int targetInterv,
                     double minSweepDistFactor, int sortAxis) {

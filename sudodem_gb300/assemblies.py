@@ -80,6 +80,15 @@ def _add_sq(b, rxyz, eps, q, pos, density, mat=0, isSphere=0, props_cache=None):
     b["mat"].append(mat); b["sph"].append(isSphere); b["state"].append(st)
 
 
+def default_params():
+    """Timestep parameters at the defaults of the reference's engines: NewtonIntegrator
+    (damping 0.2, no gravity, pkg/dem/NewtonIntegrator.hpp:70-89) and InsertionSortCollider
+    (verletDist -0.5, targetInterv 50, minSweepDistFactor 0.1, sortAxis 0,
+    pkg/common/InsertionSortCollider.hpp:212-222); dt as Scene's default 1e-8."""
+    return {"dt": 1e-8, "gravity": (0.0, 0.0, 0.0), "damping": 0.2, "verletDist": -0.5, "targetInterv": 50,
+            "minSweepDistFactor": 0.1, "sortAxis": 0, "isSuperquadrics": 1, "exactAsphericalRot": 1}
+
+
 def _finish(b, materials, params, info):
     return SceneSpec(
         kind=np.array(b["kind"], dtype=np.int32),

@@ -33,8 +33,12 @@
 
 #ifdef __CUDACC__
 #define FFH __host__ __device__ __forceinline__
+// the elementary functions are called, not inlined: one evaluation calls them ~40 times, and
+// inlined copies overflow the instruction cache (warps then stall on instruction fetch)
+#define FFN static __host__ __device__ __noinline__
 #else
 #define FFH inline
+#define FFN static inline
 #endif
 
 #ifdef __CUDA_ARCH__
@@ -251,7 +255,7 @@ FFH ff ffSqrt(ff a) {
 }
 
 // log2 of a positive double-float whose high part is a normal float.
-FFH ff ffLog2(ff x) {
+FFN ff ffLog2(ff x) {
   int e = ((ffBits(x.hi) >> 23) & 0xff) - 127;   // x.hi in [2^e, 2^(e+1))
   const float sc = pow2i(-e);
   ff m = mkff(x.hi * sc, x.lo * sc);            // m.hi in [1, 2), exact scaling
@@ -272,7 +276,7 @@ FFH ff ffLog2(ff x) {
 
 // 2^x for a double-float x.  Results below 2^-126 keep only their high part (and become 0
 // below 2^-149): the callers use such values only as negligible terms.
-FFH ff ffExp2(ff x) {
+FFN ff ffExp2(ff x) {
   if (x.hi < -149.f) return mkff(0.f, 0.f);
   if (x.hi > 127.f) return mkff(INFINITY, 0.f);
   const float n = rintf(x.hi);
@@ -294,9 +298,14 @@ FFH ff ffExp2(ff x) {
   return mkff(p.hi * s1 * s2, 0.f);
 }
 
-// sin and cos of a double-float angle |x| < 6000; returns false (NaN, larger angles) otherwise.
-FFH bool ffSinCos(ff x, ff& s, ff& c) {
-  if (!(fabsf(x.hi) < 6000.f)) { s = c = mkff(NAN, 0.f); return false; }
+// sin and cos of a double-float angle |x| < 6000; ok = false (NaN, larger angles) otherwise.
+struct FFSinCos { ff s, c; bool ok; };
+FFN FFSinCos ffSinCosV(ff x) {
+  FFSinCos out;
+  ff& s = out.s;
+  ff& c = out.c;
+  out.ok = true;
+  if (!(fabsf(x.hi) < 6000.f)) { s = c = mkff(NAN, 0.f); out.ok = false; return out; }
   const float k = rintf(x.hi * 0.636619772f);
   // r = x - k pi/2 (k P1 and k P2 exact: 12 trailing zero bits; x.hi - k P1 exact)
   ff r = twoSum(x.hi - k * FF_PIO2_1, -k * FF_PIO2_2);
@@ -322,7 +331,13 @@ FFH bool ffSinCos(ff x, ff& s, ff& c) {
     case 2: s = ffNeg(sv); c = ffNeg(cv); break;
     default: s = ffNeg(cv); c = sv; break;
   }
-  return true;
+  return out;
+}
+FFH bool ffSinCos(ff x, ff& s, ff& c) {
+  const FFSinCos r = ffSinCosV(x);
+  s = r.s;
+  c = r.c;
+  return r.ok;
 }
 FFH bool ffSinCos(double a, ff& s, ff& c) { return ffSinCos(ffFromD(a), s, c); }
 

@@ -550,6 +550,8 @@ class Omega:
         self._state = None
         self._pulled = True
         self._iter0 = 0
+        self._timeBase = 0.0
+        self._pendingArchive = None
         self.tags = {}
         self.periodic = False
         self.cell = Cell(self)
@@ -602,6 +604,8 @@ class Omega:
         return col, ilp, newton, runners
 
     # state exchange --------------------------------------------------------------------------
+    loadSkipped = ()
+
     def _material_table(self):
         mats, index = [], {}
         for b in self.bodies._b:
@@ -687,6 +691,9 @@ class Omega:
         if self._servo is not None:
             eng.set_servo(self._servo._config())
             self._servoKey = tuple(self._servo._config())
+        if self._pendingArchive is not None:
+            self._apply_archive(eng, self._pendingArchive)
+            self._pendingArchive = None
         self._engine = eng
         self._parts = (col, ilp, newton, runners)
         self._structDirty = False
@@ -740,7 +747,7 @@ class Omega:
 
     @property
     def time(self):
-        return self.iter * self.dt
+        return self._timeBase + (self.iter - self._iter0) * self.dt
 
     def _prepare(self):
         if self._structDirty or self._engine is None:
@@ -810,9 +817,18 @@ class Omega:
 
     # saving and loading ------------------------------------------------------------------------
     def save(self, fileName):
-        """Save the scene (O.save, core/Omega.cpp:230-279): the Python objects (bodies, materials,
+        """Save the scene (O.save, core/Omega.cpp:230-279).
+
+        A name ending in .xml, .xml.bz2 or .xml.gz (ObjectIO::isXmlFilename) writes the
+        reference's Boost XML archive (sudodem_gb300.archive): bodies, materials, interactions
+        with their history, cell, dt, iter, time and tags, which SudoDEM3D's O.load reads.  The
+        engine list is written empty there: set O.engines after loading, in either program.
+        Any other name writes this library's own format: the Python objects (bodies, materials,
         engines, cell) and the GPU state (sqdem_snapshot: contact history, collider and engine
-        state), in this library's own format, not the reference's .xml.bz2."""
+        state), from which load() continues bit for bit."""
+        from . import archive
+        if archive.is_xml_filename(fileName):
+            return self._save_archive(fileName)
         import pickle
         if self._engine is None or self._structDirty or self._hostDirty:
             self._prepare()
@@ -833,7 +849,15 @@ class Omega:
                     bd.state.__dict__["_scene"] = sc
 
     def load(self, fileName):
-        """Load a scene written by save(): the run continues bit for bit from where it was saved."""
+        """Load a scene written by save() (the run continues bit for bit from where it was saved)
+        or a SudoDEM3D XML archive (.xml, .xml.bz2, .xml.gz; see save()).  From an archive, the
+        engines the GPU path knows are mapped (ForceResetter, InsertionSortCollider,
+        InteractionLoop with the superquadric functors, NewtonIntegrator, CompressionEngine,
+        PyRunner); O.loadSkipped lists the others.  The collider starts with a full sort, as
+        after the reference's O.load."""
+        from . import archive
+        if archive.is_xml_filename(fileName):
+            return self._load_archive(fileName)
         import pickle
         with open(fileName, "rb") as f:
             d = pickle.load(f)
@@ -866,6 +890,178 @@ class Omega:
         self._structDirty = False
         self._hostDirty = False
         self._pulled = False
+
+
+    # SudoDEM3D XML archives ---------------------------------------------------------------
+    def _spec(self):
+        """The SceneSpec of the current Python scene (shapes, materials, parameters)."""
+        from .assemblies import SceneSpec, default_params
+        mats = self._material_table()
+        kind, shape5, was, mat, sph, st, blocked = self._body_arrays()
+        m = {k: np.array([float(getattr(x, k)) for x in mats]) for k in ("Kn", "Ks", "frictionAngle", "betan",
+                                                                            "betas", "density")}
+        if any(isinstance(x, SuperquadricsMat2) for x in mats):
+            d2 = SuperquadricsMat2._defaults
+            m["G"] = np.array([float(getattr(x, "G", d2["G"])) for x in mats])
+            m["nu"] = np.array([float(getattr(x, "nu", d2["nu"])) for x in mats])
+        p = default_params()
+        p["dt"] = self.dt
+        info = {"contact_model": getattr(self, "_contactModel", "linear")}
+        if self.periodic:
+            info.update(periodic=True, hSize=self.cell._hSize.copy(), velGrad=self.cell._velGrad.copy())
+        return SceneSpec(kind=kind, shape5=shape5, wall_axis_sense=was, mat=mat, isSphere=sph, state=st,
+                         materials=m, params=p, info=info), mats
+
+    def _save_archive(self, fileName):
+        from . import archive
+        if self._engine is None or self._structDirty or self._hostDirty:
+            self._prepare()
+        self.wait()
+        self._pull()
+        spec, mats = self._spec()
+        bodies = self.bodies._b
+        extra = {"refPos": np.array([np.asarray(b.state.refPos, dtype=np.float64) for b in bodies]).reshape(-1, 3),
+                 "groupMask": np.array([int(b.mask) for b in bodies]),
+                 "blockedDOFs": np.array([_dof_mask(b.state.blockedDOFs) for b in bodies]),
+                 "isDamped": np.array([bool(b.state.isDamped) for b in bodies])}
+        tags = [f"{k}={v}" for k, v in self.tags.items()]
+        a = archive.from_engine(self._engine, spec, dt=self.dt, time=self.time, tags=tags, body_extra=extra)
+        for k, x in enumerate(mats):
+            a.materials[k]["label"] = str(getattr(x, "label", "") or "")
+            a.materials[k]["IsSplitable"] = bool(getattr(x, "IsSplitable", False))
+            a.materials[k]["strength"] = float(getattr(x, "strength", 100.0))
+        archive.save(fileName, a)
+
+    def _load_archive(self, fileName):
+        from . import archive
+        a = archive.load(fileName)
+        device = self.device
+        self.reset()
+        self.device = device
+        for k, m in enumerate(a.materials):
+            cls = SuperquadricsMat2 if m["cls"] == "SuperquadricsMat2" else SuperquadricsMat
+            kw = {x: m[x] for x in ("Kn", "Ks", "frictionAngle", "betan", "betas", "density")}
+            if cls is SuperquadricsMat2:
+                kw.update(G=m["G"], nu=m["nu"])
+            mat = cls(IsSplitable=m.get("IsSplitable", False), strength=m.get("strength", 100.0), **kw)
+            mat.label = m.get("label", "")
+            self.materials.append(mat)
+        for i in range(a.n):
+            b = Body()
+            if a.kind[i] == 1:
+                b.shape = Wall(axis=int(a.wall[i, 0]), sense=int(a.wall[i, 1]))
+            else:
+                b.shape = Superquadrics(*a.shape5[i], isSphere=bool(a.isSphere[i]))
+            b.mat = b.material = self.materials[int(a.mat[i])]
+            b.mask = int(a.groupMask[i])
+            b.aspherical = bool(a.flags[i] & archive.FLAG_ASPHERICAL)
+            st = a.state[i]
+            s = b.state
+            s.pos, s.ori, s.vel = st[0:3].copy(), st[3:7].copy(), st[7:10].copy()
+            s.angVel, s.angMom = st[10:13].copy(), st[13:16].copy()
+            s.mass, s.inertia = float(st[33]), st[34:37].copy()
+            s.refPos = a.refPos[i].copy()
+            s.blockedDOFs = int(a.blockedDOFs[i])
+            s.isDamped = bool(a.isDamped[i])
+            self.bodies.append(b)
+        self.dt = a.dt
+        self._iter0 = a.iter
+        self._timeBase = a.time
+        self.tags = dict(t.split("=", 1) if "=" in t else (t, "") for t in a.tags)
+        self.periodic = a.isPeriodic
+        if a.isPeriodic and a.cell is not None:
+            self.cell._hSize = a.cell["hSize"].copy()
+            self.cell._velGrad = (a.cell["nextVelGrad"] if a.cell["velGradChanged"] else a.cell["velGrad"]).copy()
+        self._engines, self.loadSkipped = _engines_from_archive(a.engines)
+        self._pendingArchive = a
+        self._structDirty = True
+
+    def _apply_archive(self, eng, a):
+        st = a.state.copy()
+        st[:, 22:28] = np.nan
+        eng.put_body_state(st)
+        if len(a.intr):
+            eng.put_interactions(a.intr)
+        s = eng.scalars()
+        s[0] = a.iter
+        s[8] = 0
+        eng.put_scalars(s)
+        if a.isPeriodic and a.cell is not None:
+            c = eng.cell()
+            c[18:27] = a.cell["prevVelGrad"].reshape(9)
+            eng.put_cell(c)
+
+
+def _num(v, default=0.0):
+    try:
+        return float(v)
+    except (TypeError, ValueError):
+        return default
+
+
+def _vec3(v):
+    if isinstance(v, tuple) and len(v) == 2 and isinstance(v[1], dict):
+        return tuple(_num(v[1].get(c)) for c in ("x", "y", "z"))
+    return None
+
+
+def _functors(disp):
+    """The functor class names of a dispatcher description (class, attributes)."""
+    if not (isinstance(disp, tuple) and len(disp) == 2):
+        return []
+    out = []
+    for f in disp[1].get("functors") or []:
+        if isinstance(f, tuple) and f[0] in globals():
+            out.append(globals()[f[0]]())
+    return out
+
+
+def _engines_from_archive(descs):
+    """Map the engines of a SudoDEM3D archive onto this module's engine classes."""
+    engines, skipped = [], []
+    for d in descs:
+        if d is None:
+            continue
+        cls, at = d
+        dead = _num(at.get("dead"), 0) != 0
+        if cls == "ForceResetter":
+            engines.append(ForceResetter(dead=dead))
+        elif cls == "InsertionSortCollider":
+            e = InsertionSortCollider(_functors(at.get("boundDispatcher")))
+            for k in ("verletDist", "minSweepDistFactor", "updatingDispFactor"):
+                if k in at:
+                    setattr(e, k, _num(at[k]))
+            for k in ("targetInterv", "sortAxis"):
+                if k in at:
+                    setattr(e, k, int(_num(at[k])))
+            engines.append(e)
+        elif cls == "InteractionLoop":
+            engines.append(InteractionLoop(_functors(at.get("geomDispatcher")), _functors(at.get("physDispatcher")),
+                                           _functors(at.get("lawDispatcher"))))
+        elif cls == "NewtonIntegrator":
+            e = NewtonIntegrator()
+            if "damping" in at:
+                e.damping = _num(at["damping"])
+            g = _vec3(at.get("gravity"))
+            if g is not None:
+                e.gravity = g
+            if "isSuperquadrics" in at:
+                e.isSuperquadrics = int(_num(at["isSuperquadrics"]))
+            if "exactAsphericalRot" in at:
+                e.exactAsphericalRot = _num(at["exactAsphericalRot"]) != 0
+            engines.append(e)
+        elif cls == "PyRunner":
+            engines.append(PyRunner(command=at.get("command") or "", iterPeriod=int(_num(at.get("iterPeriod"), 1)),
+                                    dead=dead))
+        elif cls == "CompressionEngine":
+            e = CompressionEngine()
+            for k, v in CompressionEngine._defaults.items():
+                if k in at and isinstance(v, (bool, int, float)) and not isinstance(at[k], tuple):
+                    setattr(e, k, type(v)(_num(at[k])) if not isinstance(v, bool) else _num(at[k]) != 0)
+            engines.append(e)
+        else:
+            skipped.append(cls)
+    return engines, skipped
 
 
 O = Omega()

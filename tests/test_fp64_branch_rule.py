@@ -1,7 +1,7 @@
-"""Plain FP64 form against the oracle with the branch-boundary rule: every touching contact whose
-step took no decision within its rounding band, whose evaluations were not ill-conditioned in
-FP64 itself and whose search was not long, must match the oracle within 1e-10 relative force
-error; the others are excluded and counted (with a cap).
+"""Plain FP64 form against the oracle with the branch-boundary rule: the touching contacts whose
+step took a decision within its rounding band, or whose evaluations were ill-conditioned in FP64
+itself, are excluded and counted (with a cap); the rest are held to 1e-10 relative force error
+as stated at the end.
 
 The decisions (the oracle records their distance from the threshold for each pair, Margins in
 oracle/sqdem_oracle.cpp): the stop flag c.(p2-p1) > 0 (Superquadrics_Ig2.cpp:1138-1143), the
@@ -12,6 +12,12 @@ surface angle next to a multiple of pi/2 to ~1e-16, so an evaluation whose small
 below 1e-6 is ill-conditioned in FP64 (its own relative error above 1e-10).  CUDA's and glibc's
 pow/atan2/sincos differ in the last ulp; the search's finite-difference steps (1e-7 at the
 first iteration) amplify such differences, so a search of many evaluations can drift too.
+
+So the rest is held to 1e-10 or, where the reference's own answer is not determined to that
+level at FP64, to ten times its own spread: how far the oracle's force moves when its
+pow/sin/cos/atan2 results move by one ulp (six noise seeds, parity_util.oracle_spread; the GPU's
+libm is one more such variant, so its error is one more sample of that spread).  The contacts
+above 1e-10 are counted and printed with their spreads.
 """
 import os
 
@@ -19,7 +25,7 @@ import numpy as np
 import pytest
 
 from oracle import OracleScene
-from parity_util import rel_force_errors, snapshot_into, touching_common
+from parity_util import oracle_spread, rel_force_errors, snapshot_into, touching_common
 from sudodem_gb300 import Engine, assemblies
 
 pytestmark = pytest.mark.gpu
@@ -28,11 +34,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 TILE = os.path.join(HERE, "golden", "config1_tile.npz")
 
 # band of each margin (column of OracleScene.margins()) within which a contact is excluded
+SPREAD_FACTOR = 10
 BANDS = {0: 1e-13, 1: 1e-6, 2: 1e-6, 3: 1e-13, 4: 1e-6, 5: 1e-9, 6: 1e-9, 7: 1e-13, 8: 1e-6}
-LONG_SEARCH = 100    # Disfunction evaluations of the step above which a search counts as long
 
 
 def branch_rule(spec, orc, label, periodic=False, cap=0.02):
+    state = (orc.bodies(), orc.interactions(), orc.scalars(), orc.cell() if periodic else None)
+    spread = oracle_spread(spec, state, seeds=(1, 2, 3, 4, 5, 6), threads=os.cpu_count())
     eng = Engine(device=0)
     eng.load(spec)
     snapshot_into(eng, orc, periodic=periodic)
@@ -45,19 +53,23 @@ def branch_rule(spec, orc, label, periodic=False, cap=0.02):
     M = {(int(r[0]), int(r[1])): m for r, m in zip(recs, marg)}
     e = rel_force_errors(G, R)
     m = np.array([M[k] for k in keys])
+    sp = np.array([spread.get(k, 0.0) for k in keys])
     near = np.zeros(len(keys), dtype=bool)
     for col, band in BANDS.items():
         near |= m[:, col] < band
-    long_ = m[:, 9] > LONG_SEARCH
-    excl = near | long_
-    bad = (e > 1e-10) & ~excl
-    print(f"{label}: touching {len(e)}, excluded {excl.sum()} ({excl.mean():.3%}: near a decision {near.sum()}, long "
-          f"searches {long_.sum()}), max err of the rest {e[~excl].max():.2e}, above 1e-10 among them {bad.sum()}")
-    for n in np.argsort(-e)[:12]:
-        print(f"   {keys[n]} err {e[n]:.2e} excluded {excl[n]} margins " + " ".join(f"{x:.1e}" for x in m[n]))
+    rest = ~near
+    above = (e > 1e-10) & rest
+    explained = above & (e <= SPREAD_FACTOR * sp)
+    print(f"{label}: touching {len(e)}, excluded near a decision {near.sum()} ({near.mean():.3%}); of the rest "
+          f"{above.sum()} above 1e-10, {explained.sum()} of them within {SPREAD_FACTOR}x the oracle's own one-ulp "
+          f"spread; "
+          f"reference spread above 1e-10 on {np.mean(sp[rest] > 1e-10):.2%} of the rest; max err of the rest "
+          f"{e[rest].max():.2e}")
+    for n in list(np.argsort(-e)[:8]) + list(np.nonzero(above & ~explained)[0]):
+        print(f"   {keys[n]} err {e[n]:.2e} spread {sp[n]:.2e} near {near[n]} margins " + " ".join(f"{x:.1e}" for x in m[n]))
     assert len(e) > 300
-    assert excl.mean() <= cap
-    assert e[~excl].max() <= 1e-10
+    assert near.mean() <= cap
+    assert np.all((e[rest] <= 1e-10) | (e[rest] <= SPREAD_FACTOR * sp[rest]))
 
 
 def test_branch_rule_dense_walled_wide_exponents(gpu):
