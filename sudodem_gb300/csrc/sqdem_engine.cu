@@ -64,6 +64,7 @@ enum : unsigned {
 // that took at least 4 iterations first, so that the longest searches start first.
 static const unsigned F_ITERS_SHIFT = 20, F_ITERS_MASK = 15u << 20;
 static const unsigned LONG_ITERS_BUCKET = 3;   // iterations >= 4
+static const unsigned VLONG_ITERS_BUCKET = 6;  // iterations >= 32: the searches that bound the kernel
 __device__ __forceinline__ unsigned itersBucket(int iters) { return iters > 0 ? min(15u, 32u - __clz((unsigned)iters)) : 0u; }
 enum { KIND_SQ = 0, KIND_WALL = 1 };
 static const unsigned DOF_ALL = 63u;
@@ -1425,6 +1426,17 @@ __global__ void __launch_bounds__(128, 3) k_contacts_pre(Dev d) {
           shortq = d.prm->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN
                        ? (!isNew && prevDepth > 0)
                        : (!isNew && ((fl & F_ITERS_MASK) >> F_ITERS_SHIFT) < LONG_ITERS_BUCKET);
+          // Levenberg-Marquardt searches that took 32 or more iterations at the last step go to
+          // the long-search queue (fbQueue): the FP64 kernel spreads them over its warps, at
+          // most LONG_PER_WARP per warp, and gives them the spare evaluation slots, so that the
+          // chains of dependent evaluations that bound the stage advance an iteration per round;
+          // the mixed form runs them in FP64 (a double-float search that long would be deferred)
+          if (d.prm->contactModel != SQDEM_CONTACT_HERTZ_MINDLIN && !isNew &&
+              ((fl & F_ITERS_MASK) >> F_ITERS_SHIFT) >= VLONG_ITERS_BUCKET) {
+            queue = false;
+            const int k = atomicAdd(&d.S->fbCount, 1);
+            d.fbQueue[k] = e;
+          }
         }
       }
     }
@@ -1467,6 +1479,7 @@ struct LMLane {
   double j00, j01, j11, diag0, diag1, jt0, jt1;
   D3 pf, f1, contact, P1, P2, C;
   unsigned calls, iters, maxit, rounds;
+  bool isLong;   // taken from the long-search queue: first claim on the spare slots
 };
 
 static const int LM_BS = 128;
@@ -1693,6 +1706,10 @@ __device__ __forceinline__ bool lmCallEnd(const Dev& d, LMLane& L, const SqShape
 // first lane, sub the lane's place in it.  (Four-lane groups, eight points per round, were
 // measured slower: one more pow on the chain.)
 static const int COOP_LANES = 6, COOP_POINTS = 5;
+// FP64 search kernel: searches a warp holds while its queues have work, long-queue searches
+// per warp, and the spare slots one search may take in a round (trial, two probes, the next
+// trials after rejections)
+static const int MAIN_CAP = 24, LONG_PER_WARP = 2, MAX_EXTRA = 4;
 __device__ __forceinline__ void coopEval(const SqShape& A, const SqShape& B, double q0, double q1, int g0, int sub,
                                          D3& p1, D3& p2, bool& flag, const Rot* G = nullptr, double* dist = nullptr) {
   const unsigned FULL = 0xffffffffu;
@@ -1734,28 +1751,30 @@ __device__ __forceinline__ void coopEval(const SqShape& A, const SqShape& B, dou
 }
 
 // Slot allocation of one evaluation round: every searching lane (in) gets one slot, the rest
-// of the budget goes evenly to all, the remainder to the searches that have run the most
-// rounds.  Returns the lane's slot count (spc) and first slot (base), and the round's
-// largest slot count (jmax) for the uniform consume pass.
-__device__ __forceinline__ void allocSlots(bool in, unsigned rounds, int budget, int& spc, int& base, int& jmax) {
+// of the budget goes evenly to all, the remainder to the searches of highest priority (prio:
+// the long-search flag above the rounds run so far, the likeliest to bound the kernel), at
+// most maxExtra more each.  Returns the lane's slot count (spc) and first slot (base), and the
+// round's largest slot count (jmax) for the uniform consume pass.
+__device__ __forceinline__ void allocSlots(bool in, unsigned prio, int budget, int maxExtra, int& spc, int& base,
+                                           int& jmax) {
   const int lane = threadIdx.x & 31;
   const unsigned act = __ballot_sync(0xffffffffu, in);
   const int nA = __popc(act);
   const int share = budget / nA, extra = budget - share * nA;
-  const unsigned prio = in ? rounds : 0u;
+  if (!in) prio = 0u;
   int before = 0;
   for (int o = 0; o < 32; o++) {
     const unsigned po = __shfl_sync(0xffffffffu, prio, o);
     if ((act >> o) & 1u) before += (po > prio || (po == prio && o < lane)) ? 1 : 0;
   }
-  spc = in ? share + (before < extra ? 1 : 0) : 0;
+  spc = in ? share + max(0, min(maxExtra, extra - before * maxExtra)) : 0;
   base = spc;
   for (int o = 1; o < 32; o <<= 1) {
     const int y = __shfl_up_sync(0xffffffffu, base, o);
     if (lane >= o) base += y;
   }
   base -= spc;
-  jmax = share + (extra > 0 ? 1 : 0);
+  jmax = share + min(maxExtra, extra);
 }
 
 // Pass 2, FP64.  Rounds of one Disfunction evaluation per lane.  While the queue has work,
@@ -1774,63 +1793,98 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d, int fallback) {
   __shared__ double2 slotQ[LM_BS];
   __shared__ int slotOwner[LM_BS];
   const SceneState& S = *d.S;
-  const int nFront = fallback ? S.fbCount : S.lmCount;   // long searches first, then the short ones
-  const int count = fallback ? S.fbCount : S.lmCount + S.nmShort;
-  const int* queue = fallback ? d.fbQueue : d.lmQueue;
-  const int qBack = fallback ? 0 : d.qCap - 1;
-  int* head = fallback ? &d.S->fbHead : &d.S->lmHead;
+  // the main queue (lmQueue: long searches first, then the short ones from its back) and the
+  // long-search queue (fbQueue: searches of 32+ iterations at the last step, and in the mixed
+  // form's second pass the double-float searches deferred to FP64, fallback = 1)
+  const int nFront = S.lmCount, count = S.lmCount + S.nmShort;
+  const int nLongQ = S.fbCount;
   const int lane = threadIdx.x & 31;
   const int wbase = threadIdx.x & ~31;
   const bool spread = d.prm->lmSpread != 0;
+  // searches a warp holds: in the main pass at most LONG_PER_WARP from the long queue and
+  // MAIN_CAP in all while the main queue has work (the slots left go to the longest searches);
+  // in the second pass of the mixed form as many as spread the queue over all warps, at most
+  // COOP_POINTS
+  const int warps = gridDim.x * (LM_BS / 32);
+  const int cap = !spread ? 32 : fallback ? min(COOP_POINTS, max(1, (nLongQ + warps - 1) / warps)) : MAIN_CAP;
   Counters cnt = {0, 0, 0, 0, 0};
   unsigned long long ev64 = 0;
   unsigned roundsMax = 0;
   LMLane L;
-  bool active = false, exhausted = false;
+  L.isLong = false;
+  bool active = false;
+  bool mainDone = fallback != 0, longDone = false;   // warp-uniform: the queues this warp found empty
+  auto start = [&](int e) {
+    // start a contact: Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go up to lmder2
+    SqShape& A = shA[threadIdx.x];
+    SqShape& B = shB[threadIdx.x];
+    L.e = e;
+    const unsigned fl = d.A.flags[L.e];
+    int id1, id2;
+    entryIds(d, L.e, fl, id1, id2);
+    const double4 o1 = d.ori[id1], o2 = d.ori[id2];
+    const double4 a1 = d.shpA[id1], a2 = d.shpA[id2], e1 = d.shpB[id1], e2 = d.shpB[id2];
+    shapeInit(A, a1.x, a1.y, a1.z, e1.x, e1.y, a1.w); A.R = quatToRot(o1.x, o1.y, o1.z, o1.w); A.pos = xyz(d.pos[id1]);
+    shapeInit(B, a2.x, a2.y, a2.z, e2.x, e2.y, a2.w); B.R = quatToRot(o2.x, o2.y, o2.z, o2.w);
+    B.pos = xyz(d.pos[id2]) + cellShift(S, d.A.cd[L.e]);
+    L.isNew = !(fl & F_GEOM);
+    if (L.isNew) { double para[2]; centerLine(A.pos, B.pos, para); L.p0 = para[0]; L.p1 = para[1]; }
+    else { const double2 an = d.A.angle[L.e]; L.p0 = an.x; L.p1 = an.y; }
+    L.fromCenter = L.isNew;
+    L.contact = d3(0, 0, 0); L.P1 = d3(0, 0, 0); L.P2 = d3(0, 0, 0); L.C = d3(0, 0, 0);
+    L.phase = 0; L.calls = 0; L.iters = 0; L.maxit = 0; L.rounds = 0;
+    lmStartSolve(L);
+    active = true;
+  };
   while (true) {
-    const unsigned idle = __ballot_sync(0xffffffffu, !active && !exhausted);
-    if (idle) {
-      const int leader = __ffs(idle) - 1;
-      int base = 0;
-      if (lane == leader) base = atomicAdd(head, __popc(idle));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (!active && !exhausted) {
-        const int idx = base + __popc(idle & ((1u << lane) - 1));
-        if (idx < count) {
-          // start a contact: Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go up to lmder2
-          SqShape& A = shA[threadIdx.x];
-          SqShape& B = shB[threadIdx.x];
-          L.e = idx < nFront ? queue[idx] : queue[qBack - (idx - nFront)];
-          const unsigned fl = d.A.flags[L.e];
-          int id1, id2;
-          entryIds(d, L.e, fl, id1, id2);
-          const double4 o1 = d.ori[id1], o2 = d.ori[id2];
-          const double4 a1 = d.shpA[id1], a2 = d.shpA[id2], e1 = d.shpB[id1], e2 = d.shpB[id2];
-          shapeInit(A, a1.x, a1.y, a1.z, e1.x, e1.y, a1.w); A.R = quatToRot(o1.x, o1.y, o1.z, o1.w); A.pos = xyz(d.pos[id1]);
-          shapeInit(B, a2.x, a2.y, a2.z, e2.x, e2.y, a2.w); B.R = quatToRot(o2.x, o2.y, o2.z, o2.w);
-          B.pos = xyz(d.pos[id2]) + cellShift(S, d.A.cd[L.e]);
-          L.isNew = !(fl & F_GEOM);
-          if (L.isNew) { double para[2]; centerLine(A.pos, B.pos, para); L.p0 = para[0]; L.p1 = para[1]; }
-          else { const double2 an = d.A.angle[L.e]; L.p0 = an.x; L.p1 = an.y; }
-          L.fromCenter = L.isNew;
-          L.contact = d3(0, 0, 0); L.P1 = d3(0, 0, 0); L.P2 = d3(0, 0, 0); L.C = d3(0, 0, 0);
-          L.phase = 0; L.calls = 0; L.iters = 0; L.maxit = 0; L.rounds = 0;
-          lmStartSolve(L);
-          active = true;
-        } else exhausted = true;
+    // take work: idle lanes claim entries with one atomic per warp and queue, up to the caps
+    const unsigned below = (1u << lane) - 1;
+    if (!longDone) {
+      const unsigned idle = __ballot_sync(0xffffffffu, !active);
+      const int nAct = 32 - __popc(idle);
+      const int held = __popc(__ballot_sync(0xffffffffu, active && L.isLong));
+      const int perWarp = (fallback || !spread) ? cap : LONG_PER_WARP;
+      const int want = min(__popc(idle), min(perWarp - held, cap - nAct));
+      if (want > 0) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&d.S->fbHead, want);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const int r = __popc(idle & below);
+        if (!active && r < want && base + r < nLongQ) { start(d.fbQueue[base + r]); L.isLong = true; }
+        if (base + want >= nLongQ) longDone = true;
+      }
+    }
+    if (!mainDone) {
+      const unsigned idle = __ballot_sync(0xffffffffu, !active);
+      const int room = cap - (32 - __popc(idle));
+      const int want = min(__popc(idle), room);
+      if (want > 0) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&d.S->lmHead, want);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const int r = __popc(idle & below);
+        if (!active && r < want) {
+          const int idx = base + r;
+          if (idx < count) { start(idx < nFront ? d.lmQueue[idx] : d.lmQueue[d.qCap - 1 - (idx - nFront)]); L.isLong = false; }
+        }
+        if (base + want >= count) mainDone = true;
       }
     }
     const unsigned act = __ballot_sync(0xffffffffu, active);
-    if (!act) break;
-    // Points per running search: 1 while the queue has work.  Once it is drained, the warp's
-    // evaluation slots (five groups of six lanes, coopEval, while at most COOP_POINTS
-    // searches run, else 32 single lanes) are shared out evenly, the remainder going to the
-    // searches that have run the most rounds, the likeliest to bound the kernel.
+    if (!act && mainDone && longDone) break;
+    if (!act) continue;
+    // Points per running search: 1 while the queues have work and the warp holds 32 searches.
+    // Otherwise the warp's evaluation slots (five groups of six lanes, coopEval, while at most
+    // COOP_POINTS searches run, else 32 single lanes) are shared out: one each, the rest to the
+    // long searches first, then to those that have run the most rounds.
     const int nA = __popc(act);
-    const bool drained = spread && __any_sync(0xffffffffu, exhausted);
-    const bool coop = drained && nA <= COOP_POINTS;
+    const bool drained = spread && mainDone && longDone;
+    const bool capped = spread && !drained && cap < 32;
+    const bool coop = (drained || capped) && nA <= COOP_POINTS;
+    const unsigned prio = (L.isLong ? 0x80000000u : 0u) | min(L.rounds, 0x7fffffffu);
     int spc, base, jmax;
-    allocSlots(active, L.rounds, drained ? (coop ? COOP_POINTS : 32) : nA, spc, base, jmax);
+    allocSlots(active, prio, (drained || capped) ? (coop ? COOP_POINTS : 32) : nA, drained ? 1 : MAX_EXTRA, spc, base,
+               jmax);
     slotOwner[threadIdx.x] = -1;
     __syncwarp();
     if (active) lmPlan(L, &slotQ[wbase + base], &slotOwner[wbase + base], spc, lane);
@@ -2047,7 +2101,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_nm(Dev d) {
     const bool drained = spread && __any_sync(0xffffffffu, exhausted);
     const bool coop = drained && nA <= COOP_POINTS;
     int spc, base, jmax;
-    allocSlots(active, L.rounds, drained ? (coop ? COOP_POINTS : 32) : nA, spc, base, jmax);
+    allocSlots(active, L.rounds, drained ? (coop ? COOP_POINTS : 32) : nA, 1, spc, base, jmax);
     slotOwner[threadIdx.x] = -1;
     __syncwarp();
     if (active) {
@@ -2277,7 +2331,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_ff(Dev d) {
     const int nA = __popc(act);
     const bool drained = spread && __any_sync(0xffffffffu, exhausted);
     int spc, base, jmax;
-    allocSlots(active, active ? L.rounds : 0u, drained ? 32 : nA, spc, base, jmax);
+    allocSlots(active, active ? L.rounds : 0u, drained ? 32 : nA, 1, spc, base, jmax);
     slotOwner[t] = -1;
     __syncwarp();
     if (active) lmfPlan(L, &slotQ[wbase + base], &slotOwner[wbase + base], spc, lane);
