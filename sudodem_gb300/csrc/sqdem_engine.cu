@@ -1709,7 +1709,7 @@ static const int COOP_LANES = 6, COOP_POINTS = 5;
 // FP64 search kernel: searches a warp holds while its queues have work, long-queue searches
 // per warp, and the spare slots one search may take in a round (trial, two probes, the next
 // trials after rejections)
-static const int MAIN_CAP = 24, LONG_PER_WARP = 2, MAX_EXTRA = 4;
+static const int MAIN_CAP = 24, LONG_PER_WARP = 2, MAX_EXTRA = 4;   // MAIN_CAP: double-float kernel
 __device__ __forceinline__ void coopEval(const SqShape& A, const SqShape& B, double q0, double q1, int g0, int sub,
                                          D3& p1, D3& p2, bool& flag, const Rot* G = nullptr, double* dist = nullptr) {
   const unsigned FULL = 0xffffffffu;
@@ -1788,7 +1788,12 @@ __device__ __forceinline__ void allocSlots(bool in, unsigned prio, int budget, i
 // warp, each point is evaluated by a group of six lanes (coopEval), which shortens each
 // round as well.  Results are those of the one-point rounds: an evaluation depends only on
 // its point and the two shapes.
-__global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d, int fallback) {
+// Two builds: MINB = 1 keeps every lane's state in registers (222, two blocks per SM); MINB =
+// 3 caps registers at 168 for three blocks per SM (more warps to hide FP64 latency, at the cost
+// of a few hundred bytes of spills per thread).  The launch shape (search blocks per SM)
+// selects one; the autotuner times both.
+template <int MINB>
+__global__ void __launch_bounds__(LM_BS, MINB) k_contacts_lm(Dev d, int fallback) {
   __shared__ SqShape shA[LM_BS], shB[LM_BS];
   __shared__ double2 slotQ[LM_BS];
   __shared__ int slotOwner[LM_BS];
@@ -1801,12 +1806,12 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d, int fallback) {
   const int lane = threadIdx.x & 31;
   const int wbase = threadIdx.x & ~31;
   const bool spread = d.prm->lmSpread != 0;
-  // searches a warp holds: in the main pass at most LONG_PER_WARP from the long queue and
-  // MAIN_CAP in all while the main queue has work (the slots left go to the longest searches);
-  // in the second pass of the mixed form as many as spread the queue over all warps, at most
-  // COOP_POINTS
+  // searches a warp holds: in the main pass at most LONG_PER_WARP from the long queue, and in
+  // all 32 less MAX_EXTRA per long search held while the main queue has work (those slots go
+  // to the long searches); in the second pass of the mixed form as many as spread the queue
+  // over all warps, at most COOP_POINTS
   const int warps = gridDim.x * (LM_BS / 32);
-  const int cap = !spread ? 32 : fallback ? min(COOP_POINTS, max(1, (nLongQ + warps - 1) / warps)) : MAIN_CAP;
+  const int cap = !spread ? 32 : fallback ? min(COOP_POINTS, max(1, (nLongQ + warps - 1) / warps)) : 32;
   Counters cnt = {0, 0, 0, 0, 0};
   unsigned long long ev64 = 0;
   unsigned roundsMax = 0;
@@ -1856,7 +1861,8 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d, int fallback) {
     }
     if (!mainDone) {
       const unsigned idle = __ballot_sync(0xffffffffu, !active);
-      const int room = cap - (32 - __popc(idle));
+      const int held = spread ? __popc(__ballot_sync(0xffffffffu, active && L.isLong)) : 0;
+      const int room = cap - MAX_EXTRA * held - (32 - __popc(idle));
       const int want = min(__popc(idle), room);
       if (want > 0) {
         int base = 0;
@@ -1879,7 +1885,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm(Dev d, int fallback) {
     // long searches first, then to those that have run the most rounds.
     const int nA = __popc(act);
     const bool drained = spread && mainDone && longDone;
-    const bool capped = spread && !drained && cap < 32;
+    const bool capped = spread && !drained && (cap < 32 || __any_sync(0xffffffffu, active && L.isLong));
     const bool coop = (drained || capped) && nA <= COOP_POINTS;
     const unsigned prio = (L.isLong ? 0x80000000u : 0u) | min(L.rounds, 0x7fffffffu);
     int spc, base, jmax;
@@ -2294,16 +2300,21 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_ff(Dev d) {
   unsigned long long ev32 = 0, deferred = 0;
   unsigned roundsMax = 0;
   LMF& L = sL[t];
-  bool active = false, exhausted = false;
+  // searches a warp holds while the queue has work (the slots left go to the searches that
+  // have run the most rounds, as in k_contacts_lm)
+  const int cap = spread ? MAIN_CAP : 32;
+  bool active = false, done = false;   // done: warp-uniform, the queue is empty
   while (true) {
-    const unsigned idle = __ballot_sync(0xffffffffu, !active && !exhausted);
-    if (idle) {
-      const int leader = __ffs(idle) - 1;
+    const unsigned idleAll = __ballot_sync(0xffffffffu, !active);
+    const int want = done ? 0 : min(__popc(idleAll), cap - (32 - __popc(idleAll)));
+    if (want > 0) {
       int base = 0;
-      if (lane == leader) base = atomicAdd(&d.S->lmHead, __popc(idle));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (!active && !exhausted) {
-        const int idx = base + __popc(idle & ((1u << lane) - 1));
+      if (lane == 0) base = atomicAdd(&d.S->lmHead, want);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      const int r = __popc(idleAll & ((1u << lane) - 1));
+      if (base + want >= count) done = true;
+      if (!active && r < want) {
+        const int idx = base + r;
         if (idx < count) {
           const int e = idx < nFront ? d.lmQueue[idx] : d.lmQueue[d.qCap - 1 - (idx - nFront)];
           const unsigned fl = d.A.flags[e];
@@ -2323,15 +2334,20 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_ff(Dev d) {
           L.phase = 0; L.calls = 0; L.iters = 0; L.maxit = 0; L.rounds = 0;
           lmfStartSolve(L);
           active = true;
-        } else exhausted = true;
+        }
       }
     }
     const unsigned act = __ballot_sync(0xffffffffu, active);
-    if (!act) break;
+    if (!act) {
+      if (done) break;
+      continue;
+    }
     const int nA = __popc(act);
-    const bool drained = spread && __any_sync(0xffffffffu, exhausted);
+    const bool drained = spread && done;
+    const bool capped = spread && !done;
     int spc, base, jmax;
-    allocSlots(active, active ? L.rounds : 0u, drained ? 32 : nA, 1, spc, base, jmax);
+    allocSlots(active, active ? L.rounds : 0u, (drained || capped) ? 32 : nA, drained ? 1 : MAX_EXTRA, spc, base,
+               jmax);
     slotOwner[t] = -1;
     __syncwarp();
     if (active) lmfPlan(L, &slotQ[wbase + base], &slotOwner[wbase + base], spc, lane);
@@ -3081,6 +3097,13 @@ static int searchBlocksPerSM(const sqdem_ctx* c) {
 }
 static const int PASS1_BLOCKS_PER_SM = 16;   // grid-stride blocks of pass 1 per SM (default)
 
+// the FP64 search kernel build for a grid of `grid` blocks: the three-blocks-per-SM build when
+// the grid asks for more than two blocks per SM
+static void launchLmFP64(const sqdem_ctx* c, int grid, cudaStream_t s, const Dev& d, int fallback) {
+  if (grid > 2 * c->numSMs) k_contacts_lm<3><<<grid, LM_BS, 0, s>>>(d, fallback);
+  else k_contacts_lm<1><<<grid, LM_BS, 0, s>>>(d, fallback);
+}
+
 // The contact stage on c->stream: pass 1, then the searches of the selected contact model
 // (and, for Hertz-Mindlin, the finish pass of the contacts found touching).
 static void launchContactStage(sqdem_ctx* c, const Dev& d, int grid) {
@@ -3099,12 +3122,12 @@ static void launchContactStage(sqdem_ctx* c, const Dev& d, int grid) {
       k_contacts_lm_ff<<<grid, LM_BS, 0, s>>>(d);
       if (c->timingSearch) cudaEventRecord(c->ev[5], s);
       k_contacts_lm_ff_finish<<<std::min(nblk(d.Pcap, 128), c->numSMs * 8), 128, 0, s>>>(d);
-      k_contacts_lm<<<grid, LM_BS, 0, s>>>(d, 1);
+      launchLmFP64(c, grid, s, d, 1);
       if (c->timingSearch) cudaEventRecord(c->ev[6], s);
       c->launches += 5;
     } else {
       if (c->timingSearch) cudaEventRecord(c->ev[4], s);
-      k_contacts_lm<<<grid, LM_BS, 0, s>>>(d, 0);
+      launchLmFP64(c, grid, s, d, 0);
       if (c->timingSearch) { cudaEventRecord(c->ev[5], s); cudaEventRecord(c->ev[6], s); }
       c->launches += 2;
     }
@@ -3266,7 +3289,7 @@ sqdem_status sqdem_create(sqdem_ctx** out, const sqdem_config* cfg) {
   CK(cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, c->device));
   {
     int nb = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_contacts_lm, LM_BS, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_contacts_lm<3>, LM_BS, 0));
     c->lmBlocksPerSM = nb > 0 ? nb : 1;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_contacts_lm_ff, LM_BS, 0));
     c->lmBlocksPerSMmixed = nb > 0 ? nb : 1;
