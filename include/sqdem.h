@@ -213,6 +213,15 @@ sqdem_status sqdem_set_record_full(sqdem_ctx* ctx, int on);
  * bit for bit; only the time of the longest searches changes. */
 sqdem_status sqdem_set_lm_spread(sqdem_ctx* ctx, int on);
 
+/* Periodic-boundary correction, off by default (the reference's behaviour).  For a contact
+ * with the image of body 2 (cellDist != 0) the reference applies body 2's torque about its
+ * unshifted position (pkg/dem/Superquadrics.cpp:1356, its own FIXME at :1550) and leaves the
+ * image's field velocity velGrad*shift2 out of the relative velocity (:1042-1045); under
+ * compression these spin boundary particles up without bound.  on = 1 takes the torque arm
+ * from the image and adds velGrad*shift2 (both models' geometry, the linear law's torque).
+ * No counterpart in the reference. */
+sqdem_status sqdem_set_periodic_fix(sqdem_ctx* ctx, int on);
+
 /* Device time (ms, summed over the steps of the last sqdem_step call made with use_graph = 0,
  * CUDA events on the context stream) of the contact search kernel (k_contacts_lm, or the mixed
  * form's double-float k_contacts_lm_ff) and of the mixed form's FP64 fallback kernel (0 for the

@@ -94,7 +94,7 @@ def load_library(build_if_missing=True):
         "sqdem_time_e2e": (i, [v, i, v, v, dp]),
         "sqdem_time_contacts": (i, [v, i, dp]),
         "sqdem_set_use_graph": (i, [v, i]),
-        "sqdem_set_lm_spread": (i, [v, i]),
+        "sqdem_set_lm_spread": (i, [v, i]), "sqdem_set_periodic_fix": (i, [v, i]),
         "sqdem_set_servo": (i, [v, dp]), "sqdem_get_servo": (i, [v, dp]), "sqdem_put_servo": (i, [v, dp]),
         "sqdem_set_quiet": (i, [v, i]), "sqdem_unbalanced_force": (i, [v, i, dp]),
         "sqdem_get_stress": (i, [v, C.c_double, dp]),
@@ -138,7 +138,7 @@ def exported_symbols():
             "sqdem_get_kinematics", "sqdem_put_kinematics", "sqdem_num_interactions", "sqdem_get_interactions",
             "sqdem_put_interactions", "sqdem_get_scalars", "sqdem_put_scalars", "sqdem_stage_times",
             "sqdem_shape_props", "sqdem_launch_count", "sqdem_set_record_full", "sqdem_time_steps",
-            "sqdem_time_e2e", "sqdem_time_contacts", "sqdem_set_use_graph", "sqdem_set_lm_spread", "sqdem_set_periodic",
+            "sqdem_time_e2e", "sqdem_time_contacts", "sqdem_set_use_graph", "sqdem_set_lm_spread", "sqdem_set_periodic_fix", "sqdem_set_periodic",
             "sqdem_set_velgrad", "sqdem_get_cell", "sqdem_put_cell", "sqdem_contacts_static_queue", "sqdem_pipe_peaks", "sqdem_search_times",
             "sqdem_set_servo", "sqdem_get_servo", "sqdem_put_servo", "sqdem_set_quiet", "sqdem_unbalanced_force",
             "sqdem_get_stress", "sqdem_batch_create", "sqdem_batch_destroy", "sqdem_batch_last_error",
@@ -256,6 +256,11 @@ class Engine:
 
     def set_lm_spread(self, on=True):
         self._check(self.lib.sqdem_set_lm_spread(self.h, 1 if on else 0))
+
+    def set_periodic_fix(self, on=True):
+        """Periodic-boundary correction (off by default, the reference's behaviour): see
+        sqdem_set_periodic_fix in include/sqdem.h."""
+        self._check(self.lib.sqdem_set_periodic_fix(self.h, 1 if on else 0))
 
     def set_launch_shape(self, search_blocks_per_sm=0, pass1_blocks_per_sm=0):
         """Launch shapes of the contact stage (0 keeps the default); results are unchanged."""

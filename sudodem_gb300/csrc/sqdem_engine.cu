@@ -74,6 +74,7 @@ struct Params {
   int targetInterv, sortAxis, isSuperquadrics, exactAsphericalRot, recordFull;
   int lmSpread;   // idle lanes evaluate the points running searches ask for next
   int contactModel;   // SQDEM_CONTACT_LINEAR or SQDEM_CONTACT_HERTZ_MINDLIN
+  int periodicFix;    // sqdem_set_periodic_fix: torque arm and relative velocity of image contacts
 };
 
 enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_EVAL32, E_EVAL64, E_ROUNDS_MAX,
@@ -105,7 +106,8 @@ struct SceneState {
   int runCollider, initSort, newtonRan, maxDispCode;
   int P, Pnew, nWW, overflowRun;
   int lmCount, lmHead;
-  int fbCount, fbHead;   // searches the mixed form deferred to the FP64 kernel
+  int vlCount, vlHead;   // long-search queue: fbQueue[0, vlCount), filled by pass 1
+  int fbCount, fbHead;   // searches the mixed form deferred to FP64: fbQueue[vlCount, vlCount + fbCount)
   int nmFin;   // Hertz-Mindlin searches that ended touching, for the finish pass
   int nmShort; // searches queued from the back of the queue (expected short)
   int numReinit; long long colliderRuns;
@@ -186,6 +188,15 @@ __device__ __forceinline__ D3 m3v(const double* M, D3 v) {
 __device__ __forceinline__ D3 cellShift(const SceneState& S, int4 cd) {
   if (!S.periodic) return d3(0, 0, 0);
   return m3v(S.hSize, d3((double)cd.x, (double)cd.y, (double)cd.z));
+}
+// The image's field velocity velGrad * shift2 that the reference leaves out of the relative
+// velocity of a contact across the periodic boundary (Superquadrics.cpp:1042-1045); added only
+// with the periodic-boundary correction on (sqdem_set_periodic_fix), zero otherwise.
+__device__ __forceinline__ D3 shiftVelOf(const SceneState& S, const Params& P, D3 shift2) {
+  if (!P.periodicFix || !S.periodic) return d3(0, 0, 0);
+  const double* v = S.velGrad;
+  return d3(v[0] * shift2.x + (v[1] * shift2.y + v[2] * shift2.z), v[3] * shift2.x + (v[4] * shift2.y + v[5] * shift2.z),
+            v[6] * shift2.x + (v[7] * shift2.y + v[8] * shift2.z));
 }
 // InsertionSortCollider::cellWrap / cellWrapRel (InsertionSortCollider.cpp:404-414)
 __device__ __forceinline__ double cellWrapD(double x, double x0, double x1, int& period) {
@@ -283,7 +294,7 @@ __global__ void k_scan_apply(const int* __restrict__ in, int n, const int* __res
 __global__ void k_gate(Dev d) {
   SceneState& S = *d.S;
   S.skip = (S.haltAt >= 0 && S.iter >= S.haltAt) ? 1 : 0;
-  if (S.skip) { S.runCollider = 0; S.lmCount = 0; S.lmHead = 0; S.fbCount = 0; S.fbHead = 0; S.nmFin = 0; S.nmShort = 0; return; }
+  if (S.skip) { S.runCollider = 0; S.lmCount = 0; S.lmHead = 0; S.fbCount = 0; S.fbHead = 0; S.vlCount = 0; S.vlHead = 0; S.nmFin = 0; S.nmShort = 0; return; }
   if (S.newtonRan) {
     const double code = S.maxDispCode == 2 ? 2.0 : (S.maxDispCode == 1 ? 0.5 : 0.0);
     S.maxVelocitySq = fmax_ref(S.cellTerm, code);
@@ -312,7 +323,7 @@ __global__ void k_gate(Dev d) {
     else run = 0;
   }
   S.runCollider = run;
-  S.lmCount = 0; S.lmHead = 0; S.fbCount = 0; S.fbHead = 0; S.nmFin = 0; S.nmShort = 0;
+  S.lmCount = 0; S.lmHead = 0; S.fbCount = 0; S.fbHead = 0; S.vlCount = 0; S.vlHead = 0; S.nmFin = 0; S.nmShort = 0;
   if (run) {
     int init = 0;
     if (S.doSort) { init = 1; S.doSort = 0; }
@@ -941,7 +952,7 @@ struct GeomOut {
 
 // SuperquadricsGeom::precompute (Superquadrics.cpp:1030-1050)
 __device__ __forceinline__ void precomputeD(GeomOut& g, const D3& oldNormal, const BodyView& b1, const BodyView& b2,
-                                            double dt, D3 currentNormal, bool isNew, D3 shift2) {
+                                            double dt, D3 currentNormal, bool isNew, D3 shift2, D3 shiftVel) {
   if (!isNew) {
     g.ortho = cross(oldNormal, currentNormal);
     double angle = dt * 0.5 * dot(currentNormal, b1.angVel + b2.angVel);
@@ -950,7 +961,8 @@ __device__ __forceinline__ void precomputeD(GeomOut& g, const D3& oldNormal, con
   g.normal = currentNormal;
   D3 c1x = g.cp - b1.pos;
   D3 c2x = (g.cp - b2.pos) - shift2;
-  D3 relVel = (b2.vel + cross(b2.angVel, c2x)) - (b1.vel + cross(b1.angVel, c1x));
+  // shiftVel is zero unless the periodic-boundary correction is on (sqdem_set_periodic_fix)
+  D3 relVel = ((b2.vel + shiftVel) + cross(b2.angVel, c2x)) - (b1.vel + cross(b1.angVel, c1x));
   g.relVn = dot(g.normal, relVel) * g.normal;
   g.relVs = relVel - g.relVn;
   g.shearInc = g.relVs * dt;
@@ -966,7 +978,7 @@ __device__ __forceinline__ void makeShape(SqShape& s, const BodyView& b) {
 // Levenberg-Marquardt search: both bodies flagged as spheres (Superquadrics_Ig2.cpp:1950-1970)
 // and centres farther apart than the bounding radii (:1973-1979).
 __device__ void geomSqSqSimple(GeomOut& g, bool isNew, double prevDepth, D3 oldNormal, D3 oldCp,
-                               const BodyView& b1, const BodyView& b2, double dt, D3 shift2) {
+                               const BodyView& b1, const BodyView& b2, double dt, D3 shift2, D3 shiftVel) {
   g.precomputed = false; g.angSet = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 0; g.nanNormal = false; g.hm = 0;
   g.cp = oldCp;
   const D3 position1 = b1.pos, position2 = b2.pos + shift2;
@@ -987,7 +999,7 @@ __device__ void geomSqSqSimple(GeomOut& g, bool isNew, double prevDepth, D3 oldN
   g.cp = 0.5 * (p1 + p2);
   g.depth = depth;
   g.precomputed = true;
-  precomputeD(g, oldNormal, b1, b2, dt, contactNormal, g.isShearNew, shift2);
+  precomputeD(g, oldNormal, b1, b2, dt, contactNormal, g.isShearNew, shift2, shiftVel);
   g.normal = contactNormal;
   if (isNew) { g.ang0 = para[0]; g.ang1 = para[1]; g.angSet = true; }
 }
@@ -1026,7 +1038,7 @@ __device__ void geomWallSq(GeomOut& g, bool isNew, double prevDepth, D3 oldNorma
     g.depth = nrm(dd);
   }
   g.precomputed = true;
-  precomputeD(g, oldNormal, w, b, dt, normal, g.isShearNew, d3(0, 0, 0));
+  precomputeD(g, oldNormal, w, b, dt, normal, g.isShearNew, d3(0, 0, 0), d3(0, 0, 0));
   g.normal = normal;
 }
 
@@ -1035,7 +1047,7 @@ __device__ void geomWallSq(GeomOut& g, bool isNew, double prevDepth, D3 oldNorma
 // the bounding radii.  The reference uses the unshifted positions here (only precompute
 // sees shift2).
 __device__ void geomSqSq2Simple(GeomOut& g, bool isNew, double prevDepth, D3 oldNormal, D3 oldCp,
-                                const BodyView& b1, const BodyView& b2, double dt, D3 shift2) {
+                                const BodyView& b1, const BodyView& b2, double dt, D3 shift2, D3 shiftVel) {
   g.precomputed = false; g.angSet = false; g.lmIters = 0; g.lmStop = 0; g.lmCalls = 0; g.nanNormal = false; g.hm = 0;
   g.cp = oldCp;
   g.isShearNew = isNew ? true : (prevDepth <= 0);
@@ -1056,7 +1068,7 @@ __device__ void geomSqSq2Simple(GeomOut& g, bool isNew, double prevDepth, D3 old
   g.depth = depth;
   g.hm = 1; g.hEll.sum = r_sum / (rmaxA * rmaxB);
   g.precomputed = true;
-  precomputeD(g, oldNormal, b1, b2, dt, contactNormal, g.isShearNew, shift2);
+  precomputeD(g, oldNormal, b1, b2, dt, contactNormal, g.isShearNew, shift2, shiftVel);
   g.normal = contactNormal;
   g.ang0 = 0; g.ang1 = 0; g.angSet = true;
 }
@@ -1391,7 +1403,7 @@ __global__ void __launch_bounds__(128, 3) k_contacts_pre(Dev d) {
         else if (d.prm->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN) {
           const bool sph = (b1.info.z != 0) && (b2.info.z != 0);
           if (sph || nrm(b1.pos - b2.pos) > b1.shpA.w + b2.shpA.w) {
-            geomSqSq2Simple(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt, shift2);
+            geomSqSq2Simple(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt, shift2, shiftVelOf(S, *d.prm, shift2));
           } else {
             const double2 an = isNew ? make_double2(0, 0) : d.A.angle[e];
             const int nev = screenSeparatedNM(b1, b2, an.x, an.y, isNew ? 0.1 : 0.001);
@@ -1414,7 +1426,7 @@ __global__ void __launch_bounds__(128, 3) k_contacts_pre(Dev d) {
               g.ang0 = para[0]; g.ang1 = para[1]; g.angSet = true;
               cnt.lmCalls++;
             } else done = false;
-          } else geomSqSqSimple(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt, shift2);
+          } else geomSqSqSimple(g, isNew, prevDepth, oldNormal, oldCp, b1, b2, dt, shift2, shiftVelOf(S, *d.prm, shift2));
         }
         if (done) finishEntry(d, e, fl, isNew, id1, b1, b2, g, cnt);
         else {
@@ -1434,7 +1446,7 @@ __global__ void __launch_bounds__(128, 3) k_contacts_pre(Dev d) {
           if (d.prm->contactModel != SQDEM_CONTACT_HERTZ_MINDLIN && !isNew &&
               ((fl & F_ITERS_MASK) >> F_ITERS_SHIFT) >= VLONG_ITERS_BUCKET) {
             queue = false;
-            const int k = atomicAdd(&d.S->fbCount, 1);
+            const int k = atomicAdd(&d.S->vlCount, 1);
             d.fbQueue[k] = e;
           }
         }
@@ -1688,7 +1700,8 @@ __device__ __forceinline__ bool lmCallEnd(const Dev& d, LMLane& L, const SqShape
     normalize(cn);
     const D3 oldNormal = L.isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
     g.precomputed = true;
-    precomputeD(g, oldNormal, b1, b2, d.prm->dt, cn, g.isShearNew, cellShift(S, d.A.cd[e]));
+    precomputeD(g, oldNormal, b1, b2, d.prm->dt, cn, g.isShearNew, cellShift(S, d.A.cd[e]),
+                shiftVelOf(S, *d.prm, cellShift(S, d.A.cd[e])));
     g.normal = cn;
   }
   cnt.lmCalls += L.calls; cnt.lmIters += L.iters; cnt.lmMax += L.maxit;
@@ -1709,7 +1722,7 @@ static const int COOP_LANES = 6, COOP_POINTS = 5;
 // FP64 search kernel: searches a warp holds while its queues have work, long-queue searches
 // per warp, and the spare slots one search may take in a round (trial, two probes, the next
 // trials after rejections)
-static const int MAIN_CAP = 24, LONG_PER_WARP = 2, MAX_EXTRA = 4;   // MAIN_CAP: double-float kernel
+static const int LONG_PER_WARP = 2, MAX_EXTRA = 4;
 __device__ __forceinline__ void coopEval(const SqShape& A, const SqShape& B, double q0, double q1, int g0, int sub,
                                          D3& p1, D3& p2, bool& flag, const Rot* G = nullptr, double* dist = nullptr) {
   const unsigned FULL = 0xffffffffu;
@@ -1792,17 +1805,24 @@ __device__ __forceinline__ void allocSlots(bool in, unsigned prio, int budget, i
 // 3 caps registers at 168 for three blocks per SM (more warps to hide FP64 latency, at the cost
 // of a few hundred bytes of spills per thread).  The launch shape (search blocks per SM)
 // selects one; the autotuner times both.
+// mode: LM_FP64 the FP64 form (main queue and long-search queue); LM_LONG the mixed form's
+// long-search queue alone (run beside the double-float kernel); LM_DEFERRED the searches the
+// double-float kernels deferred to FP64.
+enum { LM_FP64 = 0, LM_LONG = 1, LM_DEFERRED = 2 };
 template <int MINB>
-__global__ void __launch_bounds__(LM_BS, MINB) k_contacts_lm(Dev d, int fallback) {
+__global__ void __launch_bounds__(LM_BS, MINB) k_contacts_lm(Dev d, int mode) {
   __shared__ SqShape shA[LM_BS], shB[LM_BS];
   __shared__ double2 slotQ[LM_BS];
   __shared__ int slotOwner[LM_BS];
   const SceneState& S = *d.S;
   // the main queue (lmQueue: long searches first, then the short ones from its back) and the
-  // long-search queue (fbQueue: searches of 32+ iterations at the last step, and in the mixed
-  // form's second pass the double-float searches deferred to FP64, fallback = 1)
+  // long-search queue in fbQueue: the searches of 32+ iterations at the last step
+  // ([0, vlCount)), or the deferred searches ([vlCount, vlCount + fbCount))
+  const int fallback = mode != LM_FP64;   // no main queue: the long-search queue alone
   const int nFront = S.lmCount, count = S.lmCount + S.nmShort;
-  const int nLongQ = S.fbCount;
+  const int longBase = mode == LM_DEFERRED ? S.vlCount : 0;
+  const int nLongQ = mode == LM_DEFERRED ? S.fbCount : S.vlCount;
+  int* longHead = mode == LM_DEFERRED ? &d.S->fbHead : &d.S->vlHead;
   const int lane = threadIdx.x & 31;
   const int wbase = threadIdx.x & ~31;
   const bool spread = d.prm->lmSpread != 0;
@@ -1852,10 +1872,10 @@ __global__ void __launch_bounds__(LM_BS, MINB) k_contacts_lm(Dev d, int fallback
       const int want = min(__popc(idle), min(perWarp - held, cap - nAct));
       if (want > 0) {
         int base = 0;
-        if (lane == 0) base = atomicAdd(&d.S->fbHead, want);
+        if (lane == 0) base = atomicAdd(longHead, want);
         base = __shfl_sync(0xffffffffu, base, 0);
         const int r = __popc(idle & below);
-        if (!active && r < want && base + r < nLongQ) { start(d.fbQueue[base + r]); L.isLong = true; }
+        if (!active && r < want && base + r < nLongQ) { start(d.fbQueue[longBase + base + r]); L.isLong = true; }
         if (base + want >= nLongQ) longDone = true;
       }
     }
@@ -2044,7 +2064,8 @@ __global__ void __launch_bounds__(128) k_contacts_nm_finish(Dev d) {
       g.hEll = hertzMindlin(c1, c2, angle);
       const D3 oldNormal = isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
       g.precomputed = true;
-      precomputeD(g, oldNormal, b1, b2, d.prm->dt, contactNormal, g.isShearNew, cellShift(S, d.A.cd[e]));
+      precomputeD(g, oldNormal, b1, b2, d.prm->dt, contactNormal, g.isShearNew, cellShift(S, d.A.cd[e]),
+                  shiftVelOf(S, *d.prm, cellShift(S, d.A.cd[e])));
       g.normal = contactNormal;
       cnt.lmCalls += 1; cnt.lmIters += nfunc; cnt.lmMax += (nfunc >= NM_NMAX);
       finishEntry(d, e, fl, isNew, id1, b1, b2, g, cnt);
@@ -2300,9 +2321,10 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_ff(Dev d) {
   unsigned long long ev32 = 0, deferred = 0;
   unsigned roundsMax = 0;
   LMF& L = sL[t];
-  // searches a warp holds while the queue has work (the slots left go to the searches that
-  // have run the most rounds, as in k_contacts_lm)
-  const int cap = spread ? MAIN_CAP : 32;
+  // a warp holds 32 searches while the queue has work (capping it to leave spare slots for the
+  // longest searches, as the FP64 kernel does for its long-search queue, was measured slower
+  // here: the double-float rounds are short and the bulk throughput dominates)
+  const int cap = 32;
   bool active = false, done = false;   // done: warp-uniform, the queue is empty
   while (true) {
     const unsigned idleAll = __ballot_sync(0xffffffffu, !active);
@@ -2344,10 +2366,8 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_ff(Dev d) {
     }
     const int nA = __popc(act);
     const bool drained = spread && done;
-    const bool capped = spread && !done;
     int spc, base, jmax;
-    allocSlots(active, active ? L.rounds : 0u, (drained || capped) ? 32 : nA, drained ? 1 : MAX_EXTRA, spc, base,
-               jmax);
+    allocSlots(active, active ? L.rounds : 0u, drained ? 32 : nA, 1, spc, base, jmax);
     slotOwner[t] = -1;
     __syncwarp();
     if (active) lmfPlan(L, &slotQ[wbase + base], &slotOwner[wbase + base], spc, lane);
@@ -2402,7 +2422,7 @@ __global__ void __launch_bounds__(LM_BS) k_contacts_lm_ff(Dev d) {
           d.B.cd[i] = make_int4((int)L.calls, (int)L.iters, (int)L.maxit, L.touching ? 1 : 0);
         } else if (r == LMF_DEFER) {
           const int k = atomicAdd(&d.S->fbCount, 1);
-          d.fbQueue[k] = L.e;
+          d.fbQueue[d.S->vlCount + k] = L.e;
           deferred++;
         }
         if (r != LMF_MORE) {
@@ -2469,7 +2489,8 @@ __global__ void __launch_bounds__(128) k_contacts_lm_ff_finish(Dev d) {
       normalize(cn);
       const D3 oldNormal = isNew ? d3(0, 0, 0) : xyz(d.A.normal[e]);
       g.precomputed = true;
-      precomputeD(g, oldNormal, b1, b2, dt, cn, g.isShearNew, cellShift(S, d.A.cd[e]));
+      precomputeD(g, oldNormal, b1, b2, dt, cn, g.isShearNew, cellShift(S, d.A.cd[e]),
+                  shiftVelOf(S, *d.prm, cellShift(S, d.A.cd[e])));
       g.normal = cn;
     }
     if (ok) {
@@ -2477,7 +2498,7 @@ __global__ void __launch_bounds__(128) k_contacts_lm_ff_finish(Dev d) {
       finishEntry(d, e, fl, isNew, id1, b1, b2, g, cnt);
     } else {
       const int k = atomicAdd(&d.S->fbCount, 1);
-      d.fbQueue[k] = e;
+      d.fbQueue[d.S->vlCount + k] = e;
       deferred++;
     }
   }
@@ -2489,6 +2510,9 @@ __global__ void __launch_bounds__(128) k_contacts_lm_ff_finish(Dev d) {
 __device__ __forceinline__ void addContribution(const Dev& d, int e, bool asId1, D3 pos, D3& f, D3& t) {
   const D3 F = xyz(d.A.F[e]);
   const D3 cp = xyz(d.A.cp[e]);
+  // the reference takes body 2's torque arm from its unshifted position (Superquadrics.cpp:1356,
+  // FIXME at :1550); the periodic-boundary correction takes it from the image body 2 touches
+  if (!asId1 && d.prm->periodicFix && d.S->periodic) pos = pos + cellShift(*d.S, d.A.cd[e]);
   if (asId1) { f = f + F; t = t + (-cross(pos - cp, F)); }
   else { f = f + (-F); t = t + cross(pos - cp, F); }
 }
@@ -2966,7 +2990,8 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d) {
 }
 
 __global__ void k_reset_queue(Dev d) {
-  d.S->lmCount = 0; d.S->lmHead = 0; d.S->fbCount = 0; d.S->fbHead = 0; d.S->nmFin = 0; d.S->nmShort = 0;
+  d.S->lmCount = 0; d.S->lmHead = 0; d.S->fbCount = 0; d.S->fbHead = 0; d.S->vlCount = 0; d.S->vlHead = 0;
+  d.S->nmFin = 0; d.S->nmShort = 0;
 }
 
 // Start of NewtonIntegrator::action (NewtonIntegrator.cpp:107-117): pending velGrad, the
@@ -3024,6 +3049,7 @@ struct sqdem_ctx {
   sqdem_params params;
   int recordFull = 0;
   int lmSpread = 1;
+  int periodicFix = 0;   // sqdem_set_periodic_fix
   int contactModel = SQDEM_CONTACT_LINEAR;
   bool servoOn = false;
   std::vector<int> kind, wallIds, matIds, isSphere, axisSense;
@@ -3032,6 +3058,8 @@ struct sqdem_ctx {
   std::vector<double4> hostMats; std::vector<double2> hostMatsB, hostMatsE;
   long long launches = 0, launchesPerStep = 0;
   cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t stream2 = nullptr;                       // mixed form: the long-search branch
+  cudaEvent_t evFork = nullptr, evJoin = nullptr;       // its fork and join (timing disabled)
   float stageMs[3] = {0, 0, 0};
   float searchMs[2] = {0, 0};   // eager steps: search kernel, then the mixed form's FP64 fallback kernel
   bool timingSearch = false;
@@ -3099,9 +3127,9 @@ static const int PASS1_BLOCKS_PER_SM = 16;   // grid-stride blocks of pass 1 per
 
 // the FP64 search kernel build for a grid of `grid` blocks: the three-blocks-per-SM build when
 // the grid asks for more than two blocks per SM
-static void launchLmFP64(const sqdem_ctx* c, int grid, cudaStream_t s, const Dev& d, int fallback) {
-  if (grid > 2 * c->numSMs) k_contacts_lm<3><<<grid, LM_BS, 0, s>>>(d, fallback);
-  else k_contacts_lm<1><<<grid, LM_BS, 0, s>>>(d, fallback);
+static void launchLmFP64(const sqdem_ctx* c, int grid, cudaStream_t s, const Dev& d, int mode) {
+  if (grid > 2 * c->numSMs) k_contacts_lm<3><<<grid, LM_BS, 0, s>>>(d, mode);
+  else k_contacts_lm<1><<<grid, LM_BS, 0, s>>>(d, mode);
 }
 
 // The contact stage on c->stream: pass 1, then the searches of the selected contact model
@@ -3116,18 +3144,25 @@ static void launchContactStage(sqdem_ctx* c, const Dev& d, int grid) {
     c->launches += 3;
   } else {
     if (c->precision == SQDEM_MIXED) {
-      // double-float searches, then the FP64 kernel on the searches they deferred
+      // the long-search queue in FP64 on a second stream, beside the double-float searches
+      // (FP64 and FP32 pipes; one block per SM next to the double-float kernel's), then the FP64
+      // kernel on the searches the double-float kernels deferred
+      cudaEventRecord(c->evFork, s);
+      cudaStreamWaitEvent(c->stream2, c->evFork, 0);
+      launchLmFP64(c, c->numSMs, c->stream2, d, LM_LONG);
+      cudaEventRecord(c->evJoin, c->stream2);
       k_body_ff<<<nblk(d.N, 256), 256, 0, s>>>(d);
       if (c->timingSearch) cudaEventRecord(c->ev[4], s);
       k_contacts_lm_ff<<<grid, LM_BS, 0, s>>>(d);
       if (c->timingSearch) cudaEventRecord(c->ev[5], s);
       k_contacts_lm_ff_finish<<<std::min(nblk(d.Pcap, 128), c->numSMs * 8), 128, 0, s>>>(d);
-      launchLmFP64(c, grid, s, d, 1);
+      cudaStreamWaitEvent(s, c->evJoin, 0);
+      launchLmFP64(c, grid, s, d, LM_DEFERRED);
       if (c->timingSearch) cudaEventRecord(c->ev[6], s);
-      c->launches += 5;
+      c->launches += 6;
     } else {
       if (c->timingSearch) cudaEventRecord(c->ev[4], s);
-      launchLmFP64(c, grid, s, d, 0);
+      launchLmFP64(c, grid, s, d, LM_FP64);
       if (c->timingSearch) { cudaEventRecord(c->ev[5], s); cudaEventRecord(c->ev[6], s); }
       c->launches += 2;
     }
@@ -3227,6 +3262,7 @@ static sqdem_status uploadParams(sqdem_ctx* c) {
   P.exactAsphericalRot = c->params.exactAsphericalRot; P.recordFull = c->recordFull;
   P.lmSpread = c->lmSpread;
   P.contactModel = c->contactModel;
+  P.periodicFix = c->periodicFix;
   P.h0 = hostH0(c);
   CK(cudaMemcpyAsync(c->d.prm, &P, sizeof(P), cudaMemcpyHostToDevice, c->stream));
   return SQDEM_OK;
@@ -3297,6 +3333,9 @@ sqdem_status sqdem_create(sqdem_ctx** out, const sqdem_config* cfg) {
     c->nmBlocksPerSM = nb > 0 ? nb : 1;
   }
   for (int i = 0; i < 7; i++) CK(cudaEventCreate(&c->ev[i]));
+  CK(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&c->evFork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&c->evJoin, cudaEventDisableTiming));
   std::memset(&c->d, 0, sizeof(Dev));
   std::memset(&c->params, 0, sizeof(c->params));
   c->params.dt = 1e-5; c->params.damping = 0.2; c->params.verletDist = -0.5; c->params.targetInterv = 50;
@@ -3309,8 +3348,12 @@ void sqdem_destroy(sqdem_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->stream2) cudaStreamSynchronize(c->stream2);
   freeAll(c);
-  for (int i = 0; i < 4; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  for (int i = 0; i < 7; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  if (c->evFork) cudaEventDestroy(c->evFork);
+  if (c->evJoin) cudaEventDestroy(c->evJoin);
+  if (c->stream2) cudaStreamDestroy(c->stream2);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -4064,6 +4107,14 @@ sqdem_status sqdem_set_use_graph(sqdem_ctx* c, int on) {
 sqdem_status sqdem_set_record_full(sqdem_ctx* c, int on) {
   if (!c) return SQDEM_ERR_ARG;
   c->recordFull = on ? 1 : 0;
+  if (c->haveBodies) { sqdem_status s = uploadParams(c); if (s) return s; CK(cudaStreamSynchronize(c->stream)); }
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_set_periodic_fix(sqdem_ctx* c, int on) {
+  if (!c) return SQDEM_ERR_ARG;
+  c->periodicFix = on ? 1 : 0;
+  c->graphValid = false;
   if (c->haveBodies) { sqdem_status s = uploadParams(c); if (s) return s; CK(cudaStreamSynchronize(c->stream)); }
   return SQDEM_OK;
 }

@@ -39,10 +39,12 @@ def oracle_state(orc, periodic=False):
     return (orc.bodies(), orc.interactions(), orc.scalars(), orc.cell() if periodic else None)
 
 
-def restore_oracle(spec, state, threads=1):
+def restore_oracle(spec, state, threads=1, periodic_fix=False):
     from oracle import OracleScene
     bodies, intr, sc, cell = state
     o = OracleScene.from_spec(spec, threads=threads)
+    if periodic_fix:
+        o.set_periodic_fix(True)
     o.set_bodies(bodies)
     o.set_interactions(intr)
     o.set_scalars(sc)
@@ -52,20 +54,20 @@ def restore_oracle(spec, state, threads=1):
     return o
 
 
-def oracle_spread(spec, state, seeds=(1, 2, 3), rel=0.0, threads=1):
+def oracle_spread(spec, state, seeds=(1, 2, 3), rel=0.0, threads=1, periodic_fix=False):
     """The reference's own conditioning, per touching pair: the largest relative change of the
     contact force (normal + shear) of the next step when the narrowphase's pow/sin/cos/atan2
     results move in their last bits (oracle.set_math_noise: one ulp for rel = 0, else rel times
     the value), over a few noise seeds.  Returns {pair: spread}."""
     import oracle
-    ref = restore_oracle(spec, state, threads)
+    ref = restore_oracle(spec, state, threads, periodic_fix)
     ref.step(1)
     R = by_pair(ref.interactions())
     out = {k: 0.0 for k, r in R.items() if r[4] > 0 and r[2] == 1}
     try:
         for s in seeds:
             oracle.set_math_noise(s, rel)
-            o = restore_oracle(spec, state, threads)
+            o = restore_oracle(spec, state, threads, periodic_fix)
             o.step(1)
             N = by_pair(o.interactions())
             for k in out:

@@ -1,0 +1,55 @@
+"""Config 2's servo-controlled specimen, the protocol of the long-run statistics
+(tests/test_long_run_stats.py, tests/golden/make_compression_stats.py).
+
+A closed cubic box of six walls around 500 superellipsoids on a 2.1 mm jittered lattice with the
+walls against the outer particles (assemblies.config2's specimen, eps U[0.4, 1.6], friction 0.5,
+kn = 1e5 N/m), run by config 2's CompressionEngine (pkg/dem/Compression.cpp:395-604): 100 kPa
+held on the lateral walls, the top and bottom walls driven in strain (the shear phase of
+action_cubic).  Recorded after STEPS steps: the axial and mean lateral wall stresses, the
+porosity of the box, the coordination number of the particles and the axial strain.
+"""
+import numpy as np
+
+from sudodem_gb300 import assemblies
+from sudodem_gb300.servo import servo_config, state_dict
+
+N = 500
+STEPS = 30_000
+CHUNK = 1000
+
+
+def spec_and_config(seed, n=N, kn=1e5):
+    spec = assemblies.cubic_specimen(n, seed=seed, friction=0.5, eps_range=(0.4, 1.6), spacing=2.1e-3, wall_gap=0.0,
+                                     kn=kn)
+    cfg = servo_config(z_servo=0, shearMode=1, goalx=1e5, goaly=1e5, goalz=0.05, max_vel=1.0, gain_alpha=0.5,
+                       ramp_interval=200, ramp_chunks=20, echo_interval=1000, savedata_interval=1000,
+                       target_strain=10.0)
+    return spec, cfg
+
+
+class Run:
+    def __init__(self, spec, engine, cfg):
+        self.spec, self.e = spec, engine
+        engine.set_servo(cfg)
+        self.steps = 0
+        self.done = False
+        self.result = None
+
+    def advance(self):
+        self.e.step(CHUNK)
+        self.steps += CHUNK
+
+    def check(self):
+        if self.steps < STEPS:
+            return False
+        self.done = True
+        st = state_dict(self.e.servo_state())
+        recs = self.e.interactions()
+        kind = self.spec.kind
+        touching = (recs[:, 2] != 0) & (recs[:, 4] > 0)
+        pp = touching & (kind[recs[:, 0].astype(int)] == 0) & (kind[recs[:, 1].astype(int)] == 0)
+        self.result = {"axial_stress": st["wszz"], "lateral_stress": 0.5 * (st["wsxx"] + st["wsyy"]),
+                       "porosity": 1.0 - st["particlesVolume"] / st["Current_boxVolume"],
+                       "coordination": 2.0 * float(np.sum(pp)) / self.spec.n_particles, "axial_strain": st["strain2"],
+                       "unbalanced_force": st["UnbalancedForce"]}
+        return True

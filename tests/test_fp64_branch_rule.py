@@ -38,11 +38,13 @@ SPREAD_FACTOR = 10
 BANDS = {0: 1e-13, 1: 1e-6, 2: 1e-6, 3: 1e-13, 4: 1e-6, 5: 1e-9, 6: 1e-9, 7: 1e-13, 8: 1e-6}
 
 
-def branch_rule(spec, orc, label, periodic=False, cap=0.02):
+def branch_rule(spec, orc, label, periodic=False, cap=0.02, periodic_fix=False):
     state = (orc.bodies(), orc.interactions(), orc.scalars(), orc.cell() if periodic else None)
-    spread = oracle_spread(spec, state, seeds=(1, 2, 3, 4, 5, 6), threads=os.cpu_count())
+    spread = oracle_spread(spec, state, seeds=(1, 2, 3, 4, 5, 6), threads=os.cpu_count(), periodic_fix=periodic_fix)
     eng = Engine(device=0)
     eng.load(spec)
+    if periodic_fix:
+        eng.set_periodic_fix(True)
     snapshot_into(eng, orc, periodic=periodic)
     eng.step(1)
     eng.sync()
@@ -70,6 +72,7 @@ def branch_rule(spec, orc, label, periodic=False, cap=0.02):
     assert len(e) > 300
     assert near.mean() <= cap
     assert np.all((e[rest] <= 1e-10) | (e[rest] <= SPREAD_FACTOR * sp[rest]))
+    return eng
 
 
 def test_branch_rule_dense_walled_wide_exponents(gpu):
@@ -93,3 +96,23 @@ def test_branch_rule_dense_periodic(gpu):
     orc = OracleScene.from_spec(spec, threads=os.cpu_count())
     orc.step(3)
     branch_rule(spec, orc, "periodic 1600 at 100 kPa", periodic=True)
+
+
+def test_branch_rule_dense_periodic_with_boundary_correction(gpu):
+    """The same rule with the periodic-boundary correction on in both engines
+    (sqdem_set_periodic_fix / the oracle's periodicFix): torque arm from the image body and
+    the image's field velocity in the relative velocity."""
+    if not os.path.exists(TILE):
+        pytest.skip("tests/golden/config1_tile.npz missing")
+    spec = assemblies.config1_dense(TILE, tiles=1)
+    orc = OracleScene.from_spec(spec, threads=os.cpu_count())
+    orc.set_periodic_fix(True)
+    orc.step(3)
+    eng = branch_rule(spec, orc, "periodic 1600 at 100 kPa, boundary correction", periodic=True, periodic_fix=True)
+    # body torques: the arm of a contact with an image is taken from the image (without the
+    # correction the arm of such a contact would be off by a cell size)
+    tg, to = eng.body_state()[:, 19:22], orc.bodies()[:, 19:22]
+    den = np.linalg.norm(to, axis=1)
+    rel = np.linalg.norm(tg - to, axis=1) / np.where(den > 0, den, 1)
+    print(f"torques: median rel err {np.median(rel):.2e}, above 1e-6 {np.mean(rel > 1e-6):.3%}, max {rel.max():.2e}")
+    assert np.median(rel) < 1e-10 and np.mean(rel > 1e-6) < 0.01
