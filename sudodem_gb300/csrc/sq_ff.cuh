@@ -403,7 +403,7 @@ FFH ff ffAtanSmall(ff r) {
 // reference's cosine or sine is small, that small value is the one the reference's FP64 rounding
 // gives (fp64RoundedOffset).  ill: a normal component below 1e-30 (exactly axis-aligned
 // directions, where the reference's sgn(0) = 0 conventions apply) or a non-finite value.
-FFH void ffSupport(const FFShape& s, ff nx, ff ny, ff nz, ff q[3], bool& ill) {
+FFH void ffSupportBody(const FFShape& s, ff nx, ff ny, ff nz, ff q[3], bool& ill) {
   ff ax = ffMul(s.rx, nx), ay = ffMul(s.ry, ny), az = ffMul(s.rz, nz);
   const float sx = ax.hi < 0.f ? -1.f : 1.f, sy = ay.hi < 0.f ? -1.f : 1.f, sz = az.hi < 0.f ? -1.f : 1.f;
   ax = ffAbs(ax); ay = ffAbs(ay); az = ffAbs(az);
@@ -452,6 +452,22 @@ FFH void ffSupport(const FFShape& s, ff nx, ff ny, ff nz, ff q[3], bool& ill) {
   q[0] = ffMulF(ffMul(s.rx, ffExp2(ffAdd(ffMul(s.e1, lc), ec1))), sc0);
   q[1] = ffMulF(ffMul(s.ry, ffExp2(ffAdd(ffMul(s.e1, ls), ec1))), ss0);
   q[2] = ffMulF(ffMul(s.rz, ffExp2(ffMul(s.e2, ls1))), sz);
+}
+
+struct FFSup { ff q0, q1, q2; bool ill; };
+FFN FFSup ffSupportV(const FFShape& s, ff nx, ff ny, ff nz) {
+  FFSup out;
+  out.ill = false;
+  ff q[3];
+  bool& ill = out.ill;
+  ffSupportBody(s, nx, ny, nz, q, ill);
+  out.q0 = q[0]; out.q1 = q[1]; out.q2 = q[2];
+  return out;
+}
+FFH void ffSupport(const FFShape& s, ff nx, ff ny, ff nz, ff q[3], bool& ill) {
+  const FFSup r = ffSupportV(s, nx, ny, nz);
+  q[0] = r.q0; q[1] = r.q1; q[2] = r.q2;
+  if (r.ill) ill = true;
 }
 
 // One evaluation: support points of A along c(pa) and of B along -c(pa), relative to A's

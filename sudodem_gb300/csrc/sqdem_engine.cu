@@ -1805,10 +1805,11 @@ __device__ __forceinline__ void allocSlots(bool in, unsigned prio, int budget, i
 // 3 caps registers at 168 for three blocks per SM (more warps to hide FP64 latency, at the cost
 // of a few hundred bytes of spills per thread).  The launch shape (search blocks per SM)
 // selects one; the autotuner times both.
-// mode: LM_FP64 the FP64 form (main queue and long-search queue); LM_LONG the mixed form's
-// long-search queue alone (run beside the double-float kernel); LM_DEFERRED the searches the
-// double-float kernels deferred to FP64.
-enum { LM_FP64 = 0, LM_LONG = 1, LM_DEFERRED = 2 };
+// mode: LM_FP64 the FP64 form (main queue and long-search queue); LM_DEFERRED the mixed form's
+// FP64 pass: its long-search queue and the searches the double-float kernels deferred.  (Running
+// the long-search queue on a second stream beside the double-float kernel was measured slower:
+// its blocks take the SM resources the double-float kernel's warps need.)
+enum { LM_FP64 = 0, LM_DEFERRED = 2 };
 template <int MINB>
 __global__ void __launch_bounds__(LM_BS, MINB) k_contacts_lm(Dev d, int mode) {
   __shared__ SqShape shA[LM_BS], shB[LM_BS];
@@ -1817,11 +1818,12 @@ __global__ void __launch_bounds__(LM_BS, MINB) k_contacts_lm(Dev d, int mode) {
   const SceneState& S = *d.S;
   // the main queue (lmQueue: long searches first, then the short ones from its back) and the
   // long-search queue in fbQueue: the searches of 32+ iterations at the last step
-  // ([0, vlCount)), or the deferred searches ([vlCount, vlCount + fbCount))
+  // ([0, vlCount)), in the mixed form's FP64 pass followed by the deferred searches
+  // ([vlCount, vlCount + fbCount))
   const int fallback = mode != LM_FP64;   // no main queue: the long-search queue alone
   const int nFront = S.lmCount, count = S.lmCount + S.nmShort;
-  const int longBase = mode == LM_DEFERRED ? S.vlCount : 0;
-  const int nLongQ = mode == LM_DEFERRED ? S.fbCount : S.vlCount;
+  const int longBase = 0;
+  const int nLongQ = mode == LM_DEFERRED ? S.vlCount + S.fbCount : S.vlCount;
   int* longHead = mode == LM_DEFERRED ? &d.S->fbHead : &d.S->vlHead;
   const int lane = threadIdx.x & 31;
   const int wbase = threadIdx.x & ~31;
@@ -2257,7 +2259,7 @@ __device__ __forceinline__ void shapeFromGlobal(SqShape& s, const Dev& d, int b)
 // One lmder2 call ended: the restart rules of Superquadrics_Ig2.cpp:2013-2053 (as lmCallEnd).
 // Returns LMF_MORE when a restarted call begins, LMF_END when the contact's geometry is final,
 // LMF_DEFER when a restart decision falls inside its band.
-__device__ __forceinline__ int lmfCallEnd(const Dev& d, LMF& L, int id1, int id2, D3 pB) {
+__device__ __noinline__ int lmfCallEnd(const Dev& d, LMF& L, int id1, int id2, D3 pB) {
   for (;;) {
     L.calls++; L.iters += L.k; L.maxit += (L.stop == 3);
     bool restart = false;
@@ -3058,8 +3060,6 @@ struct sqdem_ctx {
   std::vector<double4> hostMats; std::vector<double2> hostMatsB, hostMatsE;
   long long launches = 0, launchesPerStep = 0;
   cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-  cudaStream_t stream2 = nullptr;                       // mixed form: the long-search branch
-  cudaEvent_t evFork = nullptr, evJoin = nullptr;       // its fork and join (timing disabled)
   float stageMs[3] = {0, 0, 0};
   float searchMs[2] = {0, 0};   // eager steps: search kernel, then the mixed form's FP64 fallback kernel
   bool timingSearch = false;
@@ -3144,22 +3144,16 @@ static void launchContactStage(sqdem_ctx* c, const Dev& d, int grid) {
     c->launches += 3;
   } else {
     if (c->precision == SQDEM_MIXED) {
-      // the long-search queue in FP64 on a second stream, beside the double-float searches
-      // (FP64 and FP32 pipes; one block per SM next to the double-float kernel's), then the FP64
-      // kernel on the searches the double-float kernels deferred
-      cudaEventRecord(c->evFork, s);
-      cudaStreamWaitEvent(c->stream2, c->evFork, 0);
-      launchLmFP64(c, c->numSMs, c->stream2, d, LM_LONG);
-      cudaEventRecord(c->evJoin, c->stream2);
+      // double-float searches, then the FP64 kernel on the long-search queue and the searches
+      // the double-float kernels deferred
       k_body_ff<<<nblk(d.N, 256), 256, 0, s>>>(d);
       if (c->timingSearch) cudaEventRecord(c->ev[4], s);
       k_contacts_lm_ff<<<grid, LM_BS, 0, s>>>(d);
       if (c->timingSearch) cudaEventRecord(c->ev[5], s);
       k_contacts_lm_ff_finish<<<std::min(nblk(d.Pcap, 128), c->numSMs * 8), 128, 0, s>>>(d);
-      cudaStreamWaitEvent(s, c->evJoin, 0);
       launchLmFP64(c, grid, s, d, LM_DEFERRED);
       if (c->timingSearch) cudaEventRecord(c->ev[6], s);
-      c->launches += 6;
+      c->launches += 5;
     } else {
       if (c->timingSearch) cudaEventRecord(c->ev[4], s);
       launchLmFP64(c, grid, s, d, LM_FP64);
@@ -3333,9 +3327,6 @@ sqdem_status sqdem_create(sqdem_ctx** out, const sqdem_config* cfg) {
     c->nmBlocksPerSM = nb > 0 ? nb : 1;
   }
   for (int i = 0; i < 7; i++) CK(cudaEventCreate(&c->ev[i]));
-  CK(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
-  CK(cudaEventCreateWithFlags(&c->evFork, cudaEventDisableTiming));
-  CK(cudaEventCreateWithFlags(&c->evJoin, cudaEventDisableTiming));
   std::memset(&c->d, 0, sizeof(Dev));
   std::memset(&c->params, 0, sizeof(c->params));
   c->params.dt = 1e-5; c->params.damping = 0.2; c->params.verletDist = -0.5; c->params.targetInterv = 50;
@@ -3348,12 +3339,8 @@ void sqdem_destroy(sqdem_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  if (c->stream2) cudaStreamSynchronize(c->stream2);
   freeAll(c);
   for (int i = 0; i < 7; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
-  if (c->evFork) cudaEventDestroy(c->evFork);
-  if (c->evJoin) cudaEventDestroy(c->evJoin);
-  if (c->stream2) cudaStreamDestroy(c->stream2);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

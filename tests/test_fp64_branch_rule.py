@@ -111,8 +111,11 @@ def test_branch_rule_dense_periodic_with_boundary_correction(gpu):
     eng = branch_rule(spec, orc, "periodic 1600 at 100 kPa, boundary correction", periodic=True, periodic_fix=True)
     # body torques: the arm of a contact with an image is taken from the image (without the
     # correction the arm of such a contact would be off by a cell size)
+    # (relative to the larger of the body's torque and the median torque, so that bodies whose
+    # contact torques nearly cancel do not inflate it; without the correction about half of the
+    # bodies, those touching an image, would be off by order one)
     tg, to = eng.body_state()[:, 19:22], orc.bodies()[:, 19:22]
-    den = np.linalg.norm(to, axis=1)
-    rel = np.linalg.norm(tg - to, axis=1) / np.where(den > 0, den, 1)
+    den = np.maximum(np.linalg.norm(to, axis=1), np.median(np.linalg.norm(to, axis=1)))
+    rel = np.linalg.norm(tg - to, axis=1) / den
     print(f"torques: median rel err {np.median(rel):.2e}, above 1e-6 {np.mean(rel > 1e-6):.3%}, max {rel.max():.2e}")
-    assert np.median(rel) < 1e-10 and np.mean(rel > 1e-6) < 0.01
+    assert np.median(rel) < 1e-10 and np.mean(rel > 1e-6) < 0.03 and rel.max() < 1e-2
