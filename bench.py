@@ -461,6 +461,7 @@ def measure_form(spec, precision, args, rank, ws, dist):
             "search_kernel_ms": srch[0] / k2, "fallback_kernel_ms": srch[1] / k2,
             "evals_per_step": {"double_float": rep2["evals_fp32"] / k2, "fp64": rep2["evals_fp64"] / k2},
             "fallback_searches_per_step": rep2["fallback_fp64"] / k2,
+            "long_queue_searches_per_step": rep2["long_queue"] / k2,
             "table_entries": nentries, "launches": launches, "launch_shape": tune, "clocks": clk, "report": rep}
 
 

@@ -111,6 +111,8 @@ typedef struct {
                                  not reproduce) */
   long long lm_rounds_max_ff; /* mixed form: longest search in rounds of the double-float kernel
                                  (lm_rounds_max: of the FP64 kernel) */
+  long long long_queue;       /* searches of 32+ iterations at the previous step, queued for the
+                                 FP64 kernel's long-search handling (both forms) */
 } sqdem_report;
 
 /* Record layouts shared with the CPU oracle (doubles per record). */

@@ -44,7 +44,7 @@ class _Params(C.Structure):
 class _Report(C.Structure):
     _fields_ = [(n, C.c_longlong) for n in ("nan_normals", "nan_forces", "lm_calls", "lm_iterations", "lm_maxiter",
                                              "overflow", "collider_runs", "steps", "evals_fp32", "evals_fp64",
-                                             "lm_rounds_max", "fallback_fp64", "lm_rounds_max_ff")]
+                                             "lm_rounds_max", "fallback_fp64", "lm_rounds_max_ff", "long_queue")]
 
 
 _LIB = None

@@ -28,8 +28,10 @@ FFH void lmfStartSolve(LMF& L) {
   L.q0 = L.p0; L.q1 = L.p1; L.st = LMF_ST_INIT;
 }
 
-// top of lmder2's for-loop: loop condition, then the checks before the Jacobian
-FFH int lmfOuter(LMF& L) {
+// top of lmder2's for-loop: loop condition, then the checks before the Jacobian (a called
+// function, as lmfInner and the damped solve: inlined, their copies at every call site overflow
+// the instruction cache)
+FFN int lmfOuter(LMF& L) {
   // A search that reaches itmax (stop 3) is still moving after 50 iterations: along such a
   // path the difference between double-float and FP64 rounding, amplified by the 1e-7
   // finite-difference steps, compounds, so it is deferred to the FP64 path.
@@ -50,14 +52,21 @@ FFH int lmfOuter(LMF& L) {
   return LMF_MORE;
 }
 // the damped step (jtj + mu I) Dp = jt
-FFH void lmfSolve(ff j00, ff j01, ff j11, ff jt0, ff jt1, ff& Dp0, ff& Dp1, ff& dp2) {
+struct LMFStep { ff Dp0, Dp1, dp2; };
+FFN LMFStep lmfSolveV(ff j00, ff j01, ff j11, ff jt0, ff jt1) {
+  LMFStep r;
   const ff inv = ffDiv(mkff(1.f, 0.f), ffSub(ffMul(j00, j11), ffMul(j01, j01)));
-  Dp0 = ffMul(ffSub(ffMul(jt0, j11), ffMul(jt1, j01)), inv);
-  Dp1 = ffMul(ffSub(ffMul(jt1, j00), ffMul(jt0, j01)), inv);
-  dp2 = ffAdd(ffMul(Dp0, Dp0), ffMul(Dp1, Dp1));
+  r.Dp0 = ffMul(ffSub(ffMul(jt0, j11), ffMul(jt1, j01)), inv);
+  r.Dp1 = ffMul(ffSub(ffMul(jt1, j00), ffMul(jt0, j01)), inv);
+  r.dp2 = ffAdd(ffMul(r.Dp0, r.Dp0), ffMul(r.Dp1, r.Dp1));
+  return r;
+}
+FFH void lmfSolve(ff j00, ff j01, ff j11, ff jt0, ff jt1, ff& Dp0, ff& Dp1, ff& dp2) {
+  const LMFStep r = lmfSolveV(j00, j01, j11, jt0, jt1);
+  Dp0 = r.Dp0; Dp1 = r.Dp1; dp2 = r.dp2;
 }
 // top of the damping while-loop
-FFH int lmfInner(LMF& L) {
+FFN int lmfInner(LMF& L) {
   L.j00 = ffAdd(L.j00, L.mu);
   L.j11 = ffAdd(L.j11, L.mu);
   ff dp2;

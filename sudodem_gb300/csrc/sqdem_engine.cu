@@ -78,7 +78,7 @@ struct Params {
 };
 
 enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_EVAL32, E_EVAL64, E_ROUNDS_MAX,
-       E_FALLBACK, E_ROUNDS_MAX_FF, E_NUM };
+       E_FALLBACK, E_ROUNDS_MAX_FF, E_LONG_QUEUE, E_NUM };
 
 // CompressionEngine (pkg/dem/Compression.hpp:39-252), cubic specimen: configuration and state.
 struct ServoDev {
@@ -1448,6 +1448,7 @@ __global__ void __launch_bounds__(128, 3) k_contacts_pre(Dev d) {
             queue = false;
             const int k = atomicAdd(&d.S->vlCount, 1);
             d.fbQueue[k] = e;
+            atomicAdd(&d.S->err[E_LONG_QUEUE], 1ull);
           }
         }
       }
@@ -3151,7 +3152,10 @@ static void launchContactStage(sqdem_ctx* c, const Dev& d, int grid) {
       k_contacts_lm_ff<<<grid, LM_BS, 0, s>>>(d);
       if (c->timingSearch) cudaEventRecord(c->ev[5], s);
       k_contacts_lm_ff_finish<<<std::min(nblk(d.Pcap, 128), c->numSMs * 8), 128, 0, s>>>(d);
-      launchLmFP64(c, grid, s, d, LM_DEFERRED);
+      // one block per SM: one warp per scheduler, so that the FP64 pipe serves each warp's
+      // chain of dependent evaluations alone (these searches are long; more warps per
+      // scheduler lengthen every round of the longest one)
+      launchLmFP64(c, c->numSMs, s, d, LM_DEFERRED);
       if (c->timingSearch) cudaEventRecord(c->ev[6], s);
       c->launches += 5;
     } else {
@@ -3579,6 +3583,7 @@ sqdem_status sqdem_sync(sqdem_ctx* c, sqdem_report* r) {
     r->lm_rounds_max = (long long)e[E_ROUNDS_MAX];
     r->fallback_fp64 = (long long)e[E_FALLBACK];
     r->lm_rounds_max_ff = (long long)e[E_ROUNDS_MAX_FF];
+    r->long_queue = (long long)e[E_LONG_QUEUE];
   }
   if (e[E_OVERFLOW]) return fail(c, SQDEM_ERR_CAPACITY, "contact table or candidate buffer overflow; increase contacts_per_body");
   return SQDEM_OK;
@@ -4645,6 +4650,7 @@ sqdem_status sqdem_batch_sync(sqdem_batch* B, sqdem_report* total) {
       total->collider_runs += r.collider_runs; total->steps += r.steps; total->evals_fp32 += r.evals_fp32;
       total->evals_fp64 += r.evals_fp64; total->lm_rounds_max = std::max(total->lm_rounds_max, r.lm_rounds_max);
       total->fallback_fp64 += r.fallback_fp64; total->lm_rounds_max_ff = std::max(total->lm_rounds_max_ff, r.lm_rounds_max_ff);
+      total->long_queue += r.long_queue;
     }
   }
   return first;
