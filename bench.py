@@ -714,6 +714,15 @@ def run_ours_adjoint(args):
         shapes[AdjointWindow.REPLAY_SHAPES[shape]] = w.report()["backward_ms"] / nt
     best = min(shapes, key=shapes.get)
     w.set_replay([k for k, v in AdjointWindow.REPLAY_SHAPES.items() if v == best][0])
+    # resident blocks per SM of the grouped reverse kernel (the lanes' replayed state in L2 at 1)
+    blocks = {}
+    for nbk in (1, 2, 0):
+        w.set_replay_blocks(nbk)
+        w.forward(nt, min(args.checkpoint, nt), wF, wX)
+        w.backward()
+        blocks[nbk] = w.report()["backward_ms"] / nt
+    best_blocks = min(blocks, key=blocks.get)
+    w.set_replay_blocks(best_blocks)
     clocks = ClockSampler(0)
     clocks.start()
     loss, sig = w.forward(args.window, args.checkpoint, wF, wX)
@@ -735,12 +744,31 @@ def run_ours_adjoint(args):
     e2e = {"value": npart * args.window / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (2 * n + 3 * n) * 8 / args.window,
            "d2h_bytes_per_step": (2 * n + 3 * n) * 8 / args.window,
            "note": "torch.autograd.Function: parameters from host tensors, loss and gradients back to host"}
-    # finite differences along seeded directions (GPU forward, branch signatures compared)
+    # divergence of the window's trajectory: one particle moved by 1e-13 m at the start; the
+    # separation of the two runs' positions at the end, per step (the time over which a
+    # finite-difference check of the gradient can hold)
+    divergence = None
+    if args.fd_dirs:
+        base = w.state()
+        pb = bodies.copy()
+        ip = int(np.nonzero(spec.kind == 0)[0][npart // 2])
+        pb[ip, 0] += 1e-13
+        w.load(spec, pb, recs)
+        w.forward(args.window, args.checkpoint, wF, wX)
+        sep = float(np.max(np.abs(w.state()[:, 0:3] - base[:, 0:3])))
+        w.load(spec, bodies, recs)
+        w.forward(args.window, args.checkpoint, wF, wX)
+        divergence = {"perturbation_m": 1e-13, "max_separation_end_m": sep,
+                      "growth_per_step": math.log(max(sep, 1e-300) / 1e-13) / args.window}
+    # finite differences along seeded directions (GPU forward, central differences in FP64 at the
+    # relative step --fd-h, the directions cycling over the parameter kinds; a direction counts
+    # when the +h and -h runs took the base run's branches)
     fd = []
     rng = np.random.default_rng(args.seed)
     part = (spec.kind == 0)[:, None]
+    kinds = ("eps", "mu", "Kn", "Ks")
     for k in range(args.fd_dirs):
-        for name, h in (("eps", 3e-8), ("mu", 3e-5), ("Kn", 3e-5), ("Ks", 3e-5)):
+        for name, h in ((kinds[k % 4], args.fd_h),):
             dE = rng.normal(size=eps0.shape) * eps0 * part if name == "eps" else 0 * eps0
             dmu = rng.normal(size=mu0.shape) * mu0 if name == "mu" else 0 * mu0
             dKn = rng.normal(size=Kn0.shape) * Kn0 if name == "Kn" else 0 * Kn0
@@ -795,11 +823,18 @@ def run_ours_adjoint(args):
                        "loss": "final lid normal force" + (" + mean final particle height" if args.loss_heights else ""),
                        "start": start,
                        "replay_shape": best, "replay_ms_per_step_by_shape": shapes,
+                       "replay_blocks_per_sm": best_blocks,
+                       "replay_ms_per_step_by_blocks_per_sm": {str(k): v for k, v in blocks.items()},
                        "what": "particle-steps/s of forward + reverse window (one gradient)",
                        "l2": "state and tape larger than L2"},
             "loss": loss, "loss_after_one_step": loss1, "forward_ms": rep["forward_ms"], "backward_ms": rep["backward_ms"],
             "replay_mismatches": rep["replay_mismatches"], "grad_norms": {k: float(np.linalg.norm(v)) for k, v in g.items()},
-            "fd_check": fd, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "fd_check": fd,
+            "fd_summary": ({"directions": len(fd), "h_relative": args.fd_h,
+                            "same_branches": sum(x["same_branches"] for x in fd),
+                            "max_rel_err_same_branches": max([x["rel_err"] for x in fd if x["same_branches"]],
+                                                             default=None)} if fd else None),
+            "divergence": divergence, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": launches}
     if rank == 0:
         print(json.dumps(line))
@@ -826,8 +861,10 @@ def main():
     ap.add_argument("--window", type=int, default=2000, help="config3: steps of the differentiated window")
     ap.add_argument("--checkpoint", type=int, default=100, help="config3: steps between checkpoints")
     ap.add_argument("--particles", type=int, default=5000, help="config3: particles")
-    ap.add_argument("--deposit-steps", type=int, default=60000, help="config3: deposition steps before the window")
-    ap.add_argument("--fd-dirs", type=int, default=0, help="config3: finite-difference directions per parameter kind")
+    ap.add_argument("--deposit-steps", type=int, default=90000, help="config3: deposition steps before the window")
+    ap.add_argument("--fd-dirs", type=int, default=0,
+                    help="config3: finite-difference directions, cycling over eps, mu, Kn, Ks")
+    ap.add_argument("--fd-h", type=float, default=1e-6, help="config3: relative finite-difference step")
     ap.add_argument("--approach-max", type=int, default=1000,
                     help="config3: at most this many 100-step checks while the lid is lowered onto the bed")
     ap.add_argument("--reload-max", type=int, default=400,

@@ -416,6 +416,11 @@ sqdem_status sqdem_adj_set_forward(sqdem_adj* adj, int cooperative);
  * six each, 2 two lanes with nine, 3 (default) six lanes with three.  Every shape gives bitwise
  * the same gradients. */
 sqdem_status sqdem_adj_set_replay(sqdem_adj* adj, int shape);
+/* Resident blocks per SM of the grouped reverse-step kernels (grid-stride over the pairs;
+ * default 1): each lane keeps its replayed state in local memory (a few KB), and bounding the
+ * resident lanes keeps that state in L2 instead of DRAM.  0: one block per group of pairs.
+ * Gradients are bitwise the same for every value. */
+sqdem_status sqdem_adj_set_replay_blocks(sqdem_adj* adj, int blocks_per_sm);
 /* replay mismatches, Disfunction evaluations and LM calls of the forward run, pairs replayed,
  * forward ms, backward ms, steps, checkpoint interval */
 sqdem_status sqdem_adj_report(sqdem_adj* adj, double* out8);

@@ -139,6 +139,11 @@ class AdjointWindow:
         same for every shape."""
         self._check(self.lib.sqdem_adj_set_replay(self.h, int(shape)))
 
+    def set_replay_blocks(self, blocks_per_sm=1):
+        """Resident blocks per SM of the grouped reverse-step kernels (0: unbounded); the
+        gradients are bitwise the same for every value (see include/sqdem.h)."""
+        self._check(self.lib.sqdem_adj_set_replay_blocks(self.h, int(blocks_per_sm)))
+
     def set_forward(self, cooperative=True):
         """Forward kernel of the pairs: six lanes share each evaluation (default) or one thread
         per pair; the results are bitwise the same."""

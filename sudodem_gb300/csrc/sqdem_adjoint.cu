@@ -938,9 +938,12 @@ __global__ void __launch_bounds__(32 * GRP_WARPS) k_bwd_contacts_grp(Consts C, S
   const int gw = lane / GL, l = lane - gw * GL;
   const bool laneOn = gw < GPW;
   const int slot = warp * GPW + (laneOn ? gw : 0);
-  const int c = (blockIdx.x * GRP_WARPS + warp) * GPW + gw;
-  const bool active = laneOn && c < C.P;
   const int base = TG * l;
+  // grid-stride over the pairs: the launch sizes the grid so that the lanes' local memory (the
+  // replayed state, a few KB per lane) of the resident blocks stays in L2
+  for (int c0 = blockIdx.x * GRP_WARPS * GPW; c0 < C.P; c0 += gridDim.x * GRP_WARPS * GPW) {
+  const int c = c0 + warp * GPW + gw;
+  const bool active = laneOn && c < C.P;
   PairAdjIn q;
   Geom<Dual<TG>> gd;
   if (active) {
@@ -976,6 +979,8 @@ __global__ void __launch_bounds__(32 * GRP_WARPS) k_bwd_contacts_grp(Consts C, S
   }
   __syncwarp();
   if (active && l == 0) assemblePair(A, c, q, shLin[slot], shGs[slot]);
+  __syncwarp();
+  }
 }
 
 // Reverse step, (3) each body adds its pairs' contributions, in list order.
@@ -1071,6 +1076,8 @@ struct sqdem_adj {
   int nsteps = 0, every = 0;
   bool haveForward = false;
   int replay = 3;   // reverse-step kernel of the pairs: 0 one thread per pair, 1.. lane-group shapes
+  int replayBlocks = 1;   // grouped reverse kernels: resident blocks per SM (grid-stride); 0 = unbounded
+  int numSMs = 1;
   bool coopForward = true;   // forward pairs on six-lane groups (k_fwd_contacts_coop)
   double loss = 0;
   unsigned long long counters[A_NCOUNT] = {};
@@ -1157,11 +1164,17 @@ static sqdem_status ensureTape(sqdem_adj* a, int K) {
 // 3: 6 lanes x 3
 static void launchReplay(sqdem_adj* a, const Consts& C, const State& S, const StepOut& O, const Adj& A) {
   const int P = a->P, bs = 32 * GRP_WARPS;
+  // blocks of the grouped kernels: a->replayBlocks per SM (grid-stride), 0 = one block per
+  // group of pairs (as many resident as fit: their local memory spills past L2 to DRAM)
+  auto grid = [&](int perBlock) {
+    const int g = nblk(P, perBlock);
+    return a->replayBlocks > 0 ? std::min(g, a->numSMs * a->replayBlocks) : g;
+  };
   switch (a->replay) {
     case 0: k_bwd_contacts<<<nblk(P, 64), 64, 0, a->st>>>(C, S, O, A); break;
-    case 2: k_bwd_contacts_grp<9, 2><<<nblk(P, GRP_WARPS * 16), bs, 0, a->st>>>(C, S, O, A); break;
-    case 1: k_bwd_contacts_grp<6, 3><<<nblk(P, GRP_WARPS * 10), bs, 0, a->st>>>(C, S, O, A); break;
-    default: k_bwd_contacts_grp<3, 6><<<nblk(P, GRP_WARPS * 5), bs, 0, a->st>>>(C, S, O, A); break;
+    case 2: k_bwd_contacts_grp<9, 2><<<grid(GRP_WARPS * 16), bs, 0, a->st>>>(C, S, O, A); break;
+    case 1: k_bwd_contacts_grp<6, 3><<<grid(GRP_WARPS * 10), bs, 0, a->st>>>(C, S, O, A); break;
+    default: k_bwd_contacts_grp<3, 6><<<grid(GRP_WARPS * 5), bs, 0, a->st>>>(C, S, O, A); break;
   }
 }
 
@@ -1184,7 +1197,8 @@ sqdem_status sqdem_adj_create(sqdem_adj** out, int device) {
   if (device < 0 || device >= n) return SQDEM_ERR_ARG;
   sqdem_adj* a = new sqdem_adj();
   a->device = device;
-  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&a->st, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&a->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaDeviceGetAttribute(&a->numSMs, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
     delete a;
     return SQDEM_ERR_CUDA;
   }
@@ -1507,6 +1521,12 @@ sqdem_status sqdem_adj_set_forward(sqdem_adj* a, int cooperative) {
 sqdem_status sqdem_adj_set_replay(sqdem_adj* a, int shape) {
   if (!a || shape < 0 || shape > 3) return SQDEM_ERR_ARG;
   a->replay = shape;
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_adj_set_replay_blocks(sqdem_adj* a, int blocks_per_sm) {
+  if (!a || blocks_per_sm < 0) return SQDEM_ERR_ARG;
+  a->replayBlocks = blocks_per_sm;
   return SQDEM_OK;
 }
 

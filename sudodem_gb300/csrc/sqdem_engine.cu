@@ -75,6 +75,7 @@ struct Params {
   int lmSpread;   // idle lanes evaluate the points running searches ask for next
   int contactModel;   // SQDEM_CONTACT_LINEAR or SQDEM_CONTACT_HERTZ_MINDLIN
   int periodicFix;    // sqdem_set_periodic_fix: torque arm and relative velocity of image contacts
+  int vlongBucket;    // iteration bucket from which a search goes to the long-search queue
 };
 
 enum { E_NAN_NORMAL = 0, E_NAN_FORCE, E_LM_CALLS, E_LM_ITERS, E_LM_MAX, E_OVERFLOW, E_COLLIDER_RUNS, E_STEPS, E_EVAL32, E_EVAL64, E_ROUNDS_MAX,
@@ -1438,13 +1439,13 @@ __global__ void __launch_bounds__(128, 3) k_contacts_pre(Dev d) {
           shortq = d.prm->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN
                        ? (!isNew && prevDepth > 0)
                        : (!isNew && ((fl & F_ITERS_MASK) >> F_ITERS_SHIFT) < LONG_ITERS_BUCKET);
-          // Levenberg-Marquardt searches that took 32 or more iterations at the last step go to
+          // Levenberg-Marquardt searches that took 32 (mixed form: 64) or more iterations at the last step go to
           // the long-search queue (fbQueue): the FP64 kernel spreads them over its warps, at
           // most LONG_PER_WARP per warp, and gives them the spare evaluation slots, so that the
           // chains of dependent evaluations that bound the stage advance an iteration per round;
           // the mixed form runs them in FP64 (a double-float search that long would be deferred)
           if (d.prm->contactModel != SQDEM_CONTACT_HERTZ_MINDLIN && !isNew &&
-              ((fl & F_ITERS_MASK) >> F_ITERS_SHIFT) >= VLONG_ITERS_BUCKET) {
+              (int)((fl & F_ITERS_MASK) >> F_ITERS_SHIFT) >= d.prm->vlongBucket) {
             queue = false;
             const int k = atomicAdd(&d.S->vlCount, 1);
             d.fbQueue[k] = e;
@@ -3261,6 +3262,10 @@ static sqdem_status uploadParams(sqdem_ctx* c) {
   P.lmSpread = c->lmSpread;
   P.contactModel = c->contactModel;
   P.periodicFix = c->periodicFix;
+  // FP64 form: 32+ iterations; mixed form: 64+ (a double-float search of 32-49 iterations costs
+  // less than its FP64 run, and the fewer searches the FP64 pass holds per warp, the faster its
+  // longest chain)
+  P.vlongBucket = c->precision == SQDEM_MIXED ? (int)VLONG_ITERS_BUCKET + 1 : (int)VLONG_ITERS_BUCKET;
   P.h0 = hostH0(c);
   CK(cudaMemcpyAsync(c->d.prm, &P, sizeof(P), cudaMemcpyHostToDevice, c->stream));
   return SQDEM_OK;

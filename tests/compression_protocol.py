@@ -11,9 +11,12 @@ with the periodic-boundary correction on: with the reference's own torque arm an
 velocity at the boundary (Superquadrics.cpp:1042-1045,1356) boundary particles spin up without
 bound under compression, and the packing's statistics are then those of that instability.
 
-Recorded per run: the steps to 1 kPa and to 100 kPa, and at the end the solid fraction, the
+Recorded per run: the steps to 1 kPa and to 100 kPa, and at 100 kPa the solid fraction, the
 mean stress, the deviatoric stress (von Mises of sigma) and the coordination number (touching
-particle-particle contacts per particle, cf. py/utils.py:498).
+particle-particle contacts per particle, cf. py/utils.py:498); then the packing's bulk
+stiffness, the rise of the mean stress over a further volumetric strain of PROBE_STRAIN at the
+same rate divided by that strain, which scales with the contact stiffness (a 30% stiffer or
+stiffer-reporting contact law shows as a 30% higher value).
 """
 import numpy as np
 
@@ -24,6 +27,7 @@ CHUNK = 500
 GAS_RATE, SLOW_RATE = 10.0, 1.0
 P_SWITCH, P_TARGET = 1e3, 1e5
 MAX_STEPS = 600_000
+PROBE_STRAIN = 3e-3   # volumetric strain of the stiffness probe after 100 kPa
 
 
 def spec_for(seed, n=N, kn=1e5):
@@ -57,11 +61,7 @@ class Run:
         self.done = False
         self.at_switch = None
         self.result = None
-
-    def advance(self):
-        """Queue the next chunk (asynchronous on the GPU engine)."""
-        self.e.step(CHUNK)
-        self.steps += CHUNK
+        self.probe_steps = 0
 
     def check(self):
         """After a chunk: read the stress, switch rates, detect the end."""
@@ -71,9 +71,14 @@ class Run:
             self.e.set_velgrad((-SLOW_RATE * np.eye(3)).reshape(9))
             self.slow = True
             self.at_switch = self.steps
+        if self.result is not None:      # the stiffness probe has run
+            dt = self.spec.params["dt"]
+            eps_v = 3.0 * SLOW_RATE * self.probe_steps * dt
+            self.result["bulk_stiffness"] = float((p - self.result["mean_stress"]) / eps_v)
+            self.done = True
+            return True
         self.held = self.held + 1 if p >= P_TARGET else 0
         if self.held >= 2 or self.steps >= MAX_STEPS:
-            self.done = True
             L = self.e.cell()[0:9].reshape(3, 3)
             dev = s - np.eye(3) * np.trace(s) / 3.0
             self.result = {"steps_to_1kPa": self.at_switch, "steps_to_100kPa": self.steps,
@@ -81,4 +86,11 @@ class Run:
                            "deviatoric_stress": float(np.sqrt(1.5 * np.sum(dev * dev))),
                            "coordination": float(coordination(self.e.interactions(), self.spec.n_particles)),
                            "reached": bool(self.held >= 2)}
-        return self.done
+            self.probe_steps = int(np.ceil(PROBE_STRAIN / (3.0 * SLOW_RATE * self.spec.params["dt"])))
+        return False
+
+    def advance(self):
+        """Queue the next chunk (asynchronous on the GPU engine); after 100 kPa, the probe."""
+        n = self.probe_steps if self.result is not None else CHUNK
+        self.e.step(n)
+        self.steps += n

@@ -5,8 +5,9 @@ A closed cubic box of six walls around 500 superellipsoids on a 2.1 mm jittered 
 walls against the outer particles (assemblies.config2's specimen, eps U[0.4, 1.6], friction 0.5,
 kn = 1e5 N/m), run by config 2's CompressionEngine (pkg/dem/Compression.cpp:395-604): 100 kPa
 held on the lateral walls, the top and bottom walls driven in strain (the shear phase of
-action_cubic).  Recorded after STEPS steps: the axial and mean lateral wall stresses, the
-porosity of the box, the coordination number of the particles and the axial strain.
+action_cubic).  Recorded after DURATION seconds of simulated time (the number of steps follows
+from the specimen's time step): the axial and mean lateral wall stresses, the porosity of the
+box, the coordination number of the particles and the axial strain.
 """
 import numpy as np
 
@@ -14,7 +15,7 @@ from sudodem_gb300 import assemblies
 from sudodem_gb300.servo import servo_config, state_dict
 
 N = 500
-STEPS = 30_000
+DURATION = 0.035   # s of simulated time
 CHUNK = 1000
 
 
@@ -32,15 +33,17 @@ class Run:
         self.spec, self.e = spec, engine
         engine.set_servo(cfg)
         self.steps = 0
+        self.total = int(np.ceil(DURATION / spec.params["dt"]))
         self.done = False
         self.result = None
 
     def advance(self):
-        self.e.step(CHUNK)
-        self.steps += CHUNK
+        n = min(CHUNK, self.total - self.steps)
+        self.e.step(n)
+        self.steps += n
 
     def check(self):
-        if self.steps < STEPS:
+        if self.steps < self.total:
             return False
         self.done = True
         st = state_dict(self.e.servo_state())

@@ -2,7 +2,8 @@
 the GPU engine against the CPU oracle over five seeds each.
 
 The dynamics are chaotic, so the two engines are compared statistically: for each outcome
-(steps to 100 kPa, solid fraction, coordination number and deviatoric stress at 100 kPa) the
+(steps to 100 kPa, solid fraction, coordination number and deviatoric stress at 100 kPa, and the
+bulk stiffness of the packing there) the
 means over the seeds must agree within three standard errors of the difference plus 2%.  The
 oracle's runs are a committed fixture (tests/golden/compression_stats.json, written by
 tests/golden/make_compression_stats.py), together with runs of an oracle with a planted mistake
@@ -18,7 +19,7 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 STATS = os.path.join(HERE, "golden", "compression_stats.json")
 SEEDS = (1, 2, 3, 4, 5)
-METRICS = ("steps_to_100kPa", "solid_fraction", "coordination", "deviatoric_stress")
+METRICS = ("steps_to_100kPa", "solid_fraction", "coordination", "deviatoric_stress", "bulk_stiffness")
 REL_TOL = 0.02
 
 
@@ -32,10 +33,13 @@ def _load(prefix=""):
     return d
 
 
-def agree(a, b):
+SERVO_METRICS = ("axial_stress", "lateral_stress", "porosity", "coordination")
+
+
+def agree(a, b, metrics=METRICS):
     """Per metric: (ok, |mean difference|, allowed) for two lists of per-seed results."""
     out = {}
-    for m in METRICS:
+    for m in metrics:
         x = np.array([r[m] for r in a], dtype=float)
         y = np.array([r[m] for r in b], dtype=float)
         se = np.sqrt(x.var(ddof=1) / len(x) + y.var(ddof=1) / len(y))
@@ -81,4 +85,42 @@ def test_gpu_compression_statistics_match_oracle(gpu):
         g = np.mean([r[m] for r in gpu_runs])
         o = np.mean([r[m] for r in oracle_runs])
         print(f"{m}: gpu {g:.6g} oracle {o:.6g} |diff| {diff:.4g} allowed {allowed:.4g}")
+    assert all(ok for ok, _, _ in res.values())
+
+
+def test_servo_rule_detects_a_30_percent_stiffness_gap():
+    d = _load("servo_")
+    good = [d[f"servo_oracle/{s}"] for s in SEEDS]
+    bad = [d[f"servo_oracle_kn_x1.3/{s}"] for s in SEEDS]
+    res = agree(bad, good, SERVO_METRICS)
+    for m, (ok, diff, allowed) in res.items():
+        print(f"servo, kn x1.3 vs oracle: {m}: |diff| {diff:.4g}, allowed {allowed:.4g}, {'agree' if ok else 'DIFFER'}")
+    assert not all(ok for ok, _, _ in res.values())
+
+
+@pytest.mark.gpu
+def test_gpu_servo_statistics_match_oracle(gpu):
+    """Config 2's servo-controlled specimen (tests/servo_protocol.py), five seeds."""
+    import servo_protocol as SP
+    from sudodem_gb300 import Engine
+    d = _load("servo_")
+    oracle_runs = [d[f"servo_oracle/{s}"] for s in SEEDS]
+    runs = []
+    for s in SEEDS:
+        spec, cfg = SP.spec_and_config(s)
+        e = Engine(device=0)
+        e.load(spec)
+        runs.append(SP.Run(spec, e, cfg))
+    while not all(r.done for r in runs):
+        live = [r for r in runs if not r.done]
+        for r in live:
+            r.advance()
+        for r in live:
+            r.check()
+    gpu_runs = [r.result for r in runs]
+    res = agree(gpu_runs, oracle_runs, SERVO_METRICS)
+    for m, (ok, diff, allowed) in res.items():
+        g = np.mean([r[m] for r in gpu_runs])
+        o = np.mean([r[m] for r in oracle_runs])
+        print(f"servo {m}: gpu {g:.6g} oracle {o:.6g} |diff| {diff:.4g} allowed {allowed:.4g}")
     assert all(ok for ok, _, _ in res.values())
