@@ -192,16 +192,18 @@ def per_body_materials(spec, friction=None):
     return spec
 
 
-def config3(seed=0, n=5000, box=67.6e-3):
+def config3(seed=0, n=5000, spacing=3.45e-3, per_side=25):
     """Differentiation specimen: n superellipsoids generated as in config 0 (half-axes U[0.8,1.2]
-    mm, eps U[0.5,1.5], uniform random orientations, jittered 2.6 mm lattice, kn=1e5 N/m,
-    ks/kn=0.5, density 2650, damping 0.3, dt = 0.5 critical) in a square walled box wider than
-    config 0's: 67.6 mm, 25 x 25 particles per layer, 8 layers at 5,000 particles (a 20-layer
-    column in a narrow box keeps collapsing for ~45,000 steps and its surface outruns a slowly
-    loaded lid); one material per body with friction 0.5 (the per-particle friction
-    parameters).  The deposition and the lid placement that precede the compression window are
-    run by the caller (bench.py's config3 workload)."""
-    spec = walled_lattice(n, seed=seed, box=box)
+    mm, eps U[0.5,1.5], uniform random orientations, jittered lattice, kn=1e5 N/m, ks/kn=0.5,
+    density 2650, damping 0.3, dt = 0.5 critical) in a square walled box wider than config 0's:
+    25 x 25 particles per layer, 8 layers at 5,000 particles (a 20-layer column in a narrow box
+    keeps collapsing for ~45,000 steps and its surface outruns a slowly loaded lid), on a 3.45 mm
+    lattice (config 0's 2.6 mm lets two boxy particles, eps < 1 and bounding radius up to 1.7 mm,
+    overlap at the start, which launches some at up to 2 m/s, 0.2 m high); one material per body
+    with friction 0.5 (the per-particle friction parameters).  The deposition and the lid
+    placement that precede the compression window are run by the caller (bench.py's config3
+    workload)."""
+    spec = walled_lattice(n, seed=seed, box=(per_side + 1) * spacing, spacing=spacing)
     return per_body_materials(spec)
 
 

@@ -1439,7 +1439,7 @@ __global__ void __launch_bounds__(128, 3) k_contacts_pre(Dev d) {
           shortq = d.prm->contactModel == SQDEM_CONTACT_HERTZ_MINDLIN
                        ? (!isNew && prevDepth > 0)
                        : (!isNew && ((fl & F_ITERS_MASK) >> F_ITERS_SHIFT) < LONG_ITERS_BUCKET);
-          // Levenberg-Marquardt searches that took 32 (mixed form: 64) or more iterations at the last step go to
+          // Levenberg-Marquardt searches that took 32 or more iterations at the last step go to
           // the long-search queue (fbQueue): the FP64 kernel spreads them over its warps, at
           // most LONG_PER_WARP per warp, and gives them the spare evaluation slots, so that the
           // chains of dependent evaluations that bound the stage advance an iteration per round;
@@ -3262,10 +3262,9 @@ static sqdem_status uploadParams(sqdem_ctx* c) {
   P.lmSpread = c->lmSpread;
   P.contactModel = c->contactModel;
   P.periodicFix = c->periodicFix;
-  // FP64 form: 32+ iterations; mixed form: 64+ (a double-float search of 32-49 iterations costs
-  // less than its FP64 run, and the fewer searches the FP64 pass holds per warp, the faster its
-  // longest chain)
-  P.vlongBucket = c->precision == SQDEM_MIXED ? (int)VLONG_ITERS_BUCKET + 1 : (int)VLONG_ITERS_BUCKET;
+  // 32+ iterations in both forms (from 64 in the mixed form was measured no faster: the
+  // double-float kernel then deferred more searches past 50 iterations, run again in FP64)
+  P.vlongBucket = (int)VLONG_ITERS_BUCKET;
   P.h0 = hostH0(c);
   CK(cudaMemcpyAsync(c->d.prm, &P, sizeof(P), cudaMemcpyHostToDevice, c->stream));
   return SQDEM_OK;
