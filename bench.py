@@ -626,13 +626,13 @@ def run_ours(args):
 
 def config3_start(args):
     """Start of the config-3 window on the GPU engine: the specimen deposited for
-    --deposit-steps steps, the lid placed 0.05 mm above the highest particle's centre plus its
-    largest half-axis and lowered at 0.05 m/s until its force has stayed above 0.5 N (about twice
-    the bed's weight) for ten checks in a row (100 steps apart); then every velocity is zeroed
-    (NewtonIntegrator.quiet_system_flag), the bed relaxed for --relax-steps steps under the lid
-    moving at the compression velocity 0.05/s x its height, and the lid kept moving at that
-    velocity until its force has stayed above 0.05 N for five checks in a row (the relaxed bed
-    settles below the lid: the window starts from a lid in quasi-static contact)."""
+    --deposit-steps steps; the lid placed 0.05 mm above the highest particle's centre plus its
+    largest half-axis and lowered at 0.05 m/s until its force has stayed above 0.5 N (about
+    twice the bed's weight) for ten checks in a row (100 steps apart); every velocity zeroed
+    (NewtonIntegrator.quiet_system_flag); the lid lowered again at 0.01 m/s until its force has
+    stayed above 0.5 N for five checks; then the lid set to the window's compression velocity
+    (0.05/s x its height) and the bed relaxed for --relax-steps steps under it, so that the
+    window starts from a lid in quasi-static contact."""
     from sudodem_gb300 import Engine, assemblies
     spec = assemblies.config3(seed=args.seed, n=args.particles)
     eng = Engine(device=0)
@@ -643,33 +643,32 @@ def config3_start(args):
     b[5, 2] = float(np.max(b[part, 2] + np.max(spec.shape5[part, 0:3], axis=1))) + 0.05e-3
     b[5, 7:10] = [0.0, 0.0, -0.05]
     eng.put_body_state(b)
-    held, k = 0, 0
-    while held < 10 and k < args.approach_max:
-        eng.step(100)
-        k += 1
-        held = held + 1 if abs(eng.body_state()[5, 18]) > 0.5 else 0
+
+    def lower(need, cap):
+        held, k = 0, 0
+        while held < need and k < cap:
+            eng.step(100)
+            k += 1
+            held = held + 1 if abs(eng.body_state()[5, 18]) > 0.5 else 0
+        return k
+    k = lower(10, args.approach_max)
+    eng.set_quiet(True)      # zeroes every body's velocity, the lid's too
+    eng.step(1)
+    b = eng.body_state()
+    b[5, 7:10] = [0.0, 0.0, -0.01]
+    eng.put_body_state(b)
+    k2 = lower(5, args.reload_max)
     b = eng.body_state()
     height = float(b[5, 2] - b[4, 2])
     b[5, 7:10] = [0.0, 0.0, -0.05 * height]
     eng.put_body_state(b)
-    eng.set_quiet(True)      # zeroes the lid's velocity too (every body's)
-    eng.step(1)
-    b = eng.body_state()
-    b[5, 7:10] = [0.0, 0.0, -0.05 * height]
-    eng.put_body_state(b)
     eng.step(args.relax_steps)
-    held, k2 = 0, 0
-    while held < 5 and k2 < args.reload_max:
-        eng.step(100)
-        k2 += 1
-        held = held + 1 if abs(eng.body_state()[5, 18]) > 0.05 else 0
     b = eng.body_state()
     recs = eng.interactions(include_potential=True)
     eng.close()
     lid = recs[(recs[:, 0] == 5) | (recs[:, 1] == 5)]
-    return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_steps": 100 * k, "relax_steps": args.relax_steps,
-                           "reload_steps": 100 * k2,
-                           "lid_height_m": height,
+    return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_steps": 100 * k, "reload_steps": 100 * k2,
+                           "relax_steps": args.relax_steps, "lid_height_m": height,
                            "lid_velocity_m_s": -0.05 * height, "lid_force_n": float(b[5, 18]),
                            "lid_pairs": int(len(lid)), "lid_pairs_touching": int(np.sum(lid[:, 4] > 0))}
 
@@ -767,12 +766,22 @@ def run_ours_adjoint(args):
     rng = np.random.default_rng(args.seed)
     part = (spec.kind == 0)[:, None]
     kinds = ("eps", "mu", "Kn", "Ks")
+    # each direction perturbs the parameters of --fd-support particles drawn from those within
+    # 3 mm of the lid (those that carry its force; 0 = every body): a direction over every
+    # parameter changes some of the ~45k pairs' Levenberg-Marquardt paths at any usable step
+    top = bodies[5, 2]
+    near = np.nonzero((spec.kind == 0) & (bodies[:, 2] > top - 3e-3))[0]
     for k in range(args.fd_dirs):
         for name, h in ((kinds[k % 4], args.fd_h),):
-            dE = rng.normal(size=eps0.shape) * eps0 * part if name == "eps" else 0 * eps0
-            dmu = rng.normal(size=mu0.shape) * mu0 if name == "mu" else 0 * mu0
-            dKn = rng.normal(size=Kn0.shape) * Kn0 if name == "Kn" else 0 * Kn0
-            dKs = rng.normal(size=Ks0.shape) * Ks0 if name == "Ks" else 0 * Ks0
+            sel = np.zeros(n, bool)
+            if args.fd_support > 0 and len(near):
+                sel[rng.choice(near, size=min(args.fd_support, len(near)), replace=False)] = True
+            else:
+                sel[:] = True
+            dE = rng.normal(size=eps0.shape) * eps0 * part * sel[:, None] if name == "eps" else 0 * eps0
+            dmu = rng.normal(size=mu0.shape) * mu0 * sel if name == "mu" else 0 * mu0
+            dKn = rng.normal(size=Kn0.shape) * Kn0 * sel if name == "Kn" else 0 * Kn0
+            dKs = rng.normal(size=Ks0.shape) * Ks0 * sel if name == "Ks" else 0 * Ks0
             ad = float(np.sum(g["eps"] * dE) + np.sum(g["mu"] * dmu) + np.sum(g["Kn"] * dKn) + np.sum(g["Ks"] * dKs))
             vals, sigs = [], []
             for sgn in (1, -1):
@@ -830,7 +839,7 @@ def run_ours_adjoint(args):
             "loss": loss, "loss_after_one_step": loss1, "forward_ms": rep["forward_ms"], "backward_ms": rep["backward_ms"],
             "replay_mismatches": rep["replay_mismatches"], "grad_norms": {k: float(np.linalg.norm(v)) for k, v in g.items()},
             "fd_check": fd,
-            "fd_summary": ({"directions": len(fd), "h_relative": args.fd_h,
+            "fd_summary": ({"directions": len(fd), "h_relative": args.fd_h, "support_particles": args.fd_support,
                             "same_branches": sum(x["same_branches"] for x in fd),
                             "max_rel_err_same_branches": max([x["rel_err"] for x in fd if x["same_branches"]],
                                                              default=None)} if fd else None),
@@ -865,6 +874,8 @@ def main():
     ap.add_argument("--fd-dirs", type=int, default=0,
                     help="config3: finite-difference directions, cycling over eps, mu, Kn, Ks")
     ap.add_argument("--fd-h", type=float, default=1e-6, help="config3: relative finite-difference step")
+    ap.add_argument("--fd-support", type=int, default=20,
+                    help="config3: particles (near the lid) each direction perturbs; 0 = every body")
     ap.add_argument("--approach-max", type=int, default=1000,
                     help="config3: at most this many 100-step checks while the lid is lowered onto the bed")
     ap.add_argument("--reload-max", type=int, default=400,
