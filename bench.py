@@ -715,7 +715,7 @@ def run_ours_adjoint(args):
     w.set_replay([k for k, v in AdjointWindow.REPLAY_SHAPES.items() if v == best][0])
     # resident blocks per SM of the grouped reverse kernel (the lanes' replayed state in L2 at 1)
     blocks = {}
-    for nbk in (1, 2, 0):
+    for nbk in ((1, 2, 0) if args.replay_blocks < 0 else (args.replay_blocks,)):
         w.set_replay_blocks(nbk)
         w.forward(nt, min(args.checkpoint, nt), wF, wX)
         w.backward()
@@ -874,6 +874,8 @@ def main():
     ap.add_argument("--fd-dirs", type=int, default=0,
                     help="config3: finite-difference directions, cycling over eps, mu, Kn, Ks")
     ap.add_argument("--fd-h", type=float, default=1e-6, help="config3: relative finite-difference step")
+    ap.add_argument("--replay-blocks", type=int, default=-1,
+                    help="config3: resident blocks per SM of the reverse kernel (-1: time 1, 2, unbounded, keep the fastest)")
     ap.add_argument("--fd-support", type=int, default=20,
                     help="config3: particles (near the lid) each direction perturbs; 0 = every body")
     ap.add_argument("--approach-max", type=int, default=1000,
