@@ -628,11 +628,12 @@ def config3_start(args):
     """Start of the config-3 window on the GPU engine: the specimen deposited for
     --deposit-steps steps; the lid placed 0.05 mm above the highest particle's centre plus its
     largest half-axis and lowered at 0.05 m/s until its force has stayed above 0.5 N (about
-    twice the bed's weight) for ten checks in a row (100 steps apart); every velocity zeroed
-    (NewtonIntegrator.quiet_system_flag); the lid lowered again at 0.01 m/s until its force has
-    stayed above 0.5 N for five checks; then the lid set to the window's compression velocity
-    (0.05/s x its height) and the bed relaxed for --relax-steps steps under it, so that the
-    window starts from a lid in quasi-static contact."""
+    the bed's weight) for ten checks in a row (100 steps apart); every velocity zeroed
+    (NewtonIntegrator.quiet_system_flag); then the lid servo-controlled to the preload
+    --lid-force (every 20 steps its velocity set to 2e-3 m/s per N of force error, at most
+    0.01 m/s) until the force has stayed within 10% of the preload for 25 checks in a row; then
+    the lid set to the window's compression velocity (0.05/s x its height).  The window starts
+    from the quasi-static, preloaded bed."""
     from sudodem_gb300 import Engine, assemblies
     spec = assemblies.config3(seed=args.seed, n=args.particles)
     eng = Engine(device=0)
@@ -643,33 +644,35 @@ def config3_start(args):
     b[5, 2] = float(np.max(b[part, 2] + np.max(spec.shape5[part, 0:3], axis=1))) + 0.05e-3
     b[5, 7:10] = [0.0, 0.0, -0.05]
     eng.put_body_state(b)
-
-    def lower(need, cap):
-        held, k = 0, 0
-        while held < need and k < cap:
-            eng.step(100)
-            k += 1
-            held = held + 1 if abs(eng.body_state()[5, 18]) > 0.5 else 0
-        return k
-    k = lower(10, args.approach_max)
+    held, k = 0, 0
+    while held < 10 and k < args.approach_max:
+        eng.step(100)
+        k += 1
+        held = held + 1 if abs(eng.body_state()[5, 18]) > 0.5 else 0
     eng.set_quiet(True)      # zeroes every body's velocity, the lid's too
     eng.step(1)
-    b = eng.body_state()
-    b[5, 7:10] = [0.0, 0.0, -0.01]
-    eng.put_body_state(b)
-    k2 = lower(5, args.reload_max)
+    target, gain, vmax = args.lid_force, 2e-3, 0.01
+    held, k2 = 0, 0
+    while held < 25 and k2 < args.servo_max:
+        b = eng.body_state()
+        F = abs(b[5, 18])
+        held = held + 1 if abs(F - target) <= 0.1 * target else 0
+        b[5, 7:10] = [0.0, 0.0, -float(np.clip(gain * (target - F), -vmax, vmax))]
+        eng.put_body_state(b)
+        eng.step(20)
+        k2 += 1
     b = eng.body_state()
     height = float(b[5, 2] - b[4, 2])
+    force0 = float(abs(b[5, 18]))
     b[5, 7:10] = [0.0, 0.0, -0.05 * height]
     eng.put_body_state(b)
-    eng.step(args.relax_steps)
     b = eng.body_state()
     recs = eng.interactions(include_potential=True)
     eng.close()
     lid = recs[(recs[:, 0] == 5) | (recs[:, 1] == 5)]
-    return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_steps": 100 * k, "reload_steps": 100 * k2,
-                           "relax_steps": args.relax_steps, "lid_height_m": height,
-                           "lid_velocity_m_s": -0.05 * height, "lid_force_n": float(b[5, 18]),
+    return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_steps": 100 * k, "servo_steps": 20 * k2,
+                           "servo_converged": bool(held >= 25), "preload_n": target, "lid_height_m": height,
+                           "lid_velocity_m_s": -0.05 * height, "lid_force_n": force0,
                            "lid_pairs": int(len(lid)), "lid_pairs_touching": int(np.sum(lid[:, 4] > 0))}
 
 
@@ -706,7 +709,7 @@ def run_ours_adjoint(args):
     loss1, _ = w.forward(1, 1, wF, wX)
     shapes = {}
     nt = min(args.window, 50)
-    for shape in (1, 2, 3, 0):
+    for shape in ((1, 2, 3, 0) if args.replay_shape < 0 else (args.replay_shape,)):
         w.set_replay(shape)
         w.forward(nt, min(args.checkpoint, nt), wF, wX)
         w.backward()
@@ -746,53 +749,85 @@ def run_ours_adjoint(args):
     # divergence of the window's trajectory: one particle moved by 1e-13 m at the start; the
     # separation of the two runs' positions at the end, per step (the time over which a
     # finite-difference check of the gradient can hold)
+    # divergence of the trajectory: one particle moved by 1e-13 m at the start; the separation
+    # of the two runs' positions after the finite-difference window and after the whole window,
+    # per step (the e-folding time bounds the window over which a difference at a relative step
+    # of 1e-6 stays linear)
     divergence = None
+    fd, fd_summary = [], None
     if args.fd_dirs:
-        base = w.state()
+        fdw = min(args.fd_window, args.window)
+        base = {}
+        for nst in sorted({fdw, args.window}):
+            w.forward(nst, args.checkpoint, wF, wX)
+            base[nst] = w.state()
         pb = bodies.copy()
         ip = int(np.nonzero(spec.kind == 0)[0][npart // 2])
         pb[ip, 0] += 1e-13
         w.load(spec, pb, recs)
-        w.forward(args.window, args.checkpoint, wF, wX)
-        sep = float(np.max(np.abs(w.state()[:, 0:3] - base[:, 0:3])))
+        divergence = {"perturbation_m": 1e-13}
+        for nst in sorted(base):
+            w.forward(nst, args.checkpoint, wF, wX)
+            sep = float(np.max(np.abs(w.state()[:, 0:3] - base[nst][:, 0:3])))
+            divergence[f"after_{nst}_steps"] = {"max_separation_m": sep,
+                                                "growth_per_step": math.log(max(sep, 1e-300) / 1e-13) / nst}
         w.load(spec, bodies, recs)
-        w.forward(args.window, args.checkpoint, wF, wX)
-        divergence = {"perturbation_m": 1e-13, "max_separation_end_m": sep,
-                      "growth_per_step": math.log(max(sep, 1e-300) / 1e-13) / args.window}
-    # finite differences along seeded directions (GPU forward, central differences in FP64 at the
-    # relative step --fd-h, the directions cycling over the parameter kinds; a direction counts
-    # when the +h and -h runs took the base run's branches)
-    fd = []
-    rng = np.random.default_rng(args.seed)
-    part = (spec.kind == 0)[:, None]
-    kinds = ("eps", "mu", "Kn", "Ks")
-    # each direction perturbs the parameters of --fd-support particles drawn from those within
-    # 3 mm of the lid (those that carry its force; 0 = every body): a direction over every
-    # parameter changes some of the ~45k pairs' Levenberg-Marquardt paths at any usable step
-    top = bodies[5, 2]
-    near = np.nonzero((spec.kind == 0) & (bodies[:, 2] > top - 3e-3))[0]
-    for k in range(args.fd_dirs):
-        for name, h in ((kinds[k % 4], args.fd_h),):
-            sel = np.zeros(n, bool)
-            if args.fd_support > 0 and len(near):
-                sel[rng.choice(near, size=min(args.fd_support, len(near)), replace=False)] = True
-            else:
-                sel[:] = True
-            dE = rng.normal(size=eps0.shape) * eps0 * part * sel[:, None] if name == "eps" else 0 * eps0
-            dmu = rng.normal(size=mu0.shape) * mu0 * sel if name == "mu" else 0 * mu0
-            dKn = rng.normal(size=Kn0.shape) * Kn0 * sel if name == "Kn" else 0 * Kn0
-            dKs = rng.normal(size=Ks0.shape) * Ks0 * sel if name == "Ks" else 0 * Ks0
-            ad = float(np.sum(g["eps"] * dE) + np.sum(g["mu"] * dmu) + np.sum(g["Kn"] * dKn) + np.sum(g["Ks"] * dKs))
-            vals, sigs = [], []
-            for sgn in (1, -1):
-                w.set_materials(Kn0 + sgn * h * dKn, Ks0 + sgn * h * dKs, mu0 + sgn * h * dmu)
-                w.set_eps(eps0 + sgn * h * dE)
-                lv, sv = w.forward(args.window, args.checkpoint, wF, wX)
-                vals.append(lv)
-                sigs.append(sv)
-            f = (vals[0] - vals[1]) / (2 * h)
-            fd.append({"param": name, "h": h, "adjoint": ad, "fd": f, "rel_err": abs(f - ad) / max(abs(ad), 1e-300),
-                       "same_branches": bool(sigs[0] == sigs[1] == sig)})
+        # central differences over --fd-window steps along --fd-dirs seeded directions over every
+        # parameter (the kinds cycling eps, mu, Kn, Ks), at the relative step --fd-h, in FP64 on the
+        # GPU: (a) runs forced onto the base run's recorded branches (sqdem_adj_set_branches), the
+        # differences of the branch whose derivative the reverse pass computes; (b) the same runs
+        # evaluated naturally, which count when they took the base run's branches (signature)
+        w.set_branches(AdjointWindow.BRANCH_RECORD)
+        Lb, sigb = w.forward(fdw, args.checkpoint, wF, wX)
+        gb = w.backward()
+        decisions = w.branch_report()["decisions"]
+        w.set_branches(AdjointWindow.BRANCH_FORCE)
+        rng = np.random.default_rng(args.seed)
+        noise = 0.0   # rounding noise of the loss: runs perturbed by 1e-13, whose linear change is below it
+        for k in range(4):
+            d = rng.normal(size=mu0.shape) * mu0
+            w.set_materials(Kn0, Ks0, mu0 + 1e-13 * d)
+            ln, _ = w.forward(fdw, args.checkpoint, wF, wX)
+            noise = max(noise, abs(ln - Lb - 1e-13 * float(np.sum(gb["mu"] * d))))
+        part = (spec.kind == 0)[:, None]
+        kinds = ("eps", "mu", "Kn", "Ks")
+        h = args.fd_h
+        for k in range(args.fd_dirs):
+            name = kinds[k % 4]
+            dE = rng.normal(size=eps0.shape) * eps0 * part if name == "eps" else 0 * eps0
+            dmu = rng.normal(size=mu0.shape) * mu0 if name == "mu" else 0 * mu0
+            dKn = rng.normal(size=Kn0.shape) * Kn0 if name == "Kn" else 0 * Kn0
+            dKs = rng.normal(size=Ks0.shape) * Ks0 if name == "Ks" else 0 * Ks0
+            ad = float(np.sum(gb["eps"] * dE) + np.sum(gb["mu"] * dmu) + np.sum(gb["Kn"] * dKn) + np.sum(gb["Ks"] * dKs))
+            row = {"param": name, "h": h, "adjoint": ad}
+            for mode, tag in ((AdjointWindow.BRANCH_FORCE, "forced"), (AdjointWindow.BRANCH_NATURAL, "natural")):
+                w.set_branches(mode)
+                vals, sigs, dis = [], [], 0
+                for sgn in (1, -1):
+                    w.set_materials(Kn0 + sgn * h * dKn, Ks0 + sgn * h * dKs, mu0 + sgn * h * dmu)
+                    w.set_eps(eps0 + sgn * h * dE)
+                    lv, sv = w.forward(fdw, args.checkpoint, wF, wX)
+                    vals.append(lv)
+                    sigs.append(sv)
+                    dis += w.branch_report()["disagreements"] if mode == AdjointWindow.BRANCH_FORCE else 0
+                f = (vals[0] - vals[1]) / (2 * h)
+                row[tag] = {"fd": f, "rel_err": abs(f - ad) / max(abs(ad), 1e-300)}
+                if tag == "forced":
+                    row[tag]["decisions_forced_against_their_natural_outcome"] = dis
+                    row[tag]["noise_bound_rel"] = noise / h / max(abs(ad), 1e-300)
+                else:
+                    row[tag]["same_branches"] = bool(sigs[0] == sigs[1] == sigb)
+            fd.append(row)
+        w.set_branches(AdjointWindow.BRANCH_NATURAL)
+        forced_err = [x["forced"]["rel_err"] for x in fd]
+        fd_summary = {"directions": len(fd), "h_relative": h, "window_steps": fdw, "loss": Lb,
+                      "decisions_per_run": decisions, "loss_rounding_noise": noise,
+                      "forced_within_1e-5": int(sum(e <= 1e-5 for e in forced_err)),
+                      "forced_max_rel_err": max(forced_err),
+                      "forced_within_1e-5_or_noise": int(sum(x["forced"]["rel_err"] <= 1e-5 + 2 * x["forced"]["noise_bound_rel"]
+                                                             for x in fd)),
+                      "natural_same_branches": int(sum(x["natural"]["same_branches"] for x in fd)),
+                      "natural_within_1e-5": int(sum(x["natural"]["rel_err"] <= 1e-5 for x in fd))}
     w.set_materials(Kn0, Ks0, mu0)
     w.set_eps(eps0)
     cpu = None
@@ -838,11 +873,7 @@ def run_ours_adjoint(args):
                        "l2": "state and tape larger than L2"},
             "loss": loss, "loss_after_one_step": loss1, "forward_ms": rep["forward_ms"], "backward_ms": rep["backward_ms"],
             "replay_mismatches": rep["replay_mismatches"], "grad_norms": {k: float(np.linalg.norm(v)) for k, v in g.items()},
-            "fd_check": fd,
-            "fd_summary": ({"directions": len(fd), "h_relative": args.fd_h, "support_particles": args.fd_support,
-                            "same_branches": sum(x["same_branches"] for x in fd),
-                            "max_rel_err_same_branches": max([x["rel_err"] for x in fd if x["same_branches"]],
-                                                             default=None)} if fd else None),
+            "fd_check": fd, "fd_summary": fd_summary,
             "divergence": divergence, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": launches}
     if rank == 0:
@@ -874,16 +905,18 @@ def main():
     ap.add_argument("--fd-dirs", type=int, default=0,
                     help="config3: finite-difference directions, cycling over eps, mu, Kn, Ks")
     ap.add_argument("--fd-h", type=float, default=1e-6, help="config3: relative finite-difference step")
+    ap.add_argument("--replay-shape", type=int, default=-1,
+                    help="config3: shape of the reverse kernel (AdjointWindow.REPLAY_SHAPES; -1: time each, keep the fastest)")
     ap.add_argument("--replay-blocks", type=int, default=-1,
                     help="config3: resident blocks per SM of the reverse kernel (-1: time 1, 2, unbounded, keep the fastest)")
-    ap.add_argument("--fd-support", type=int, default=20,
-                    help="config3: particles (near the lid) each direction perturbs; 0 = every body")
+    ap.add_argument("--fd-window", type=int, default=200,
+                    help="config3: steps of the finite-difference check's window (at most --window)")
     ap.add_argument("--approach-max", type=int, default=1000,
                     help="config3: at most this many 100-step checks while the lid is lowered onto the bed")
-    ap.add_argument("--reload-max", type=int, default=400,
-                    help="config3: at most this many 100-step checks while the lid reloads after the relaxation")
+    ap.add_argument("--lid-force", type=float, default=1.0, help="config3: lid preload (N) at the window's start")
+    ap.add_argument("--servo-max", type=int, default=5000,
+                    help="config3: at most this many 20-step servo checks while the lid is brought to its preload")
     ap.add_argument("--loss-heights", action="store_true", help="config3: add the particles' mean final height to the loss")
-    ap.add_argument("--relax-steps", type=int, default=3000, help="config3: steps of the bed under the slow lid before the window")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

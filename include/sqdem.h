@@ -421,6 +421,19 @@ sqdem_status sqdem_adj_set_replay(sqdem_adj* adj, int shape);
  * resident lanes keeps that state in L2 instead of DRAM.  0: one block per group of pairs.
  * Gradients are bitwise the same for every value. */
 sqdem_status sqdem_adj_set_replay_blocks(sqdem_adj* adj, int blocks_per_sm);
+/* Branch tape of the forward runs: 0 (default) evaluates every decision; 1 records the outcome
+ * of every decision at which the step map jumps or kinks (the Levenberg-Marquardt path, the
+ * narrowphase restarts, the bounding-sphere and contact gates, the shear reset, the Coulomb
+ * cap, the local damping's signs) in each following forward run; 2 makes the following forward
+ * runs take the recorded outcomes (over at most as many steps as the recorded run), so that a
+ * run with perturbed parameters stays on the recorded branches and central differences are
+ * those of one smooth branch.  The reverse pass always evaluates its decisions: gradients are
+ * those of the recorded (natural) run.  SQDEM_ERR_STATE for 2 without a recording; a new scene
+ * drops the recording. */
+sqdem_status sqdem_adj_set_branches(sqdem_adj* adj, int mode);
+/* Of the last forward run: decisions taken, forced decisions whose natural outcome differed,
+ * decisions beyond the tape's 224 per pair and step (evaluated, not forced), steps recorded. */
+sqdem_status sqdem_adj_branch_report(sqdem_adj* adj, double* out4);
 /* replay mismatches, Disfunction evaluations and LM calls of the forward run, pairs replayed,
  * forward ms, backward ms, steps, checkpoint interval */
 sqdem_status sqdem_adj_report(sqdem_adj* adj, double* out8);

@@ -123,7 +123,8 @@ def load_library(build_if_missing=True):
         "sqdem_adj_backward": (i, [v, dp, dp, dp, dp]), "sqdem_adj_get_state": (i, [v, dp]),
         "sqdem_adj_num_pairs": (l, [v]), "sqdem_adj_get_pairs": (i, [v, dp]), "sqdem_adj_report": (i, [v, dp]),
         "sqdem_adj_set_replay": (i, [v, i]), "sqdem_adj_set_forward": (i, [v, i]),
-        "sqdem_adj_set_replay_blocks": (i, [v, i]),
+        "sqdem_adj_set_replay_blocks": (i, [v, i]), "sqdem_adj_set_branches": (i, [v, i]),
+        "sqdem_adj_branch_report": (i, [v, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -150,7 +151,8 @@ def exported_symbols():
             "sqdem_adj_create", "sqdem_adj_destroy", "sqdem_adj_last_error", "sqdem_adj_load",
             "sqdem_adj_set_materials", "sqdem_adj_set_eps", "sqdem_adj_forward", "sqdem_adj_backward",
             "sqdem_adj_get_state", "sqdem_adj_num_pairs", "sqdem_adj_get_pairs", "sqdem_adj_report",
-            "sqdem_adj_set_replay", "sqdem_adj_set_forward", "sqdem_adj_set_replay_blocks"]
+            "sqdem_adj_set_replay", "sqdem_adj_set_forward", "sqdem_adj_set_replay_blocks", "sqdem_adj_set_branches",
+            "sqdem_adj_branch_report"]
 
 
 def _dp(a):

@@ -144,6 +144,21 @@ class AdjointWindow:
         gradients are bitwise the same for every value (see include/sqdem.h)."""
         self._check(self.lib.sqdem_adj_set_replay_blocks(self.h, int(blocks_per_sm)))
 
+    BRANCH_NATURAL, BRANCH_RECORD, BRANCH_FORCE = 0, 1, 2
+
+    def set_branches(self, mode):
+        """Branch tape of the following forward runs: BRANCH_NATURAL evaluates every decision,
+        BRANCH_RECORD records their outcomes, BRANCH_FORCE takes the recorded outcomes (a run
+        with perturbed parameters then stays on the recorded branches; see include/sqdem.h)."""
+        self._check(self.lib.sqdem_adj_set_branches(self.h, int(mode)))
+
+    def branch_report(self):
+        """Of the last forward run: decisions taken, forced decisions whose natural outcome
+        differed, decisions beyond the tape (evaluated), steps recorded."""
+        out = np.zeros(4)
+        self._check(self.lib.sqdem_adj_branch_report(self.h, _dp(out)))
+        return dict(zip(("decisions", "disagreements", "unforced", "steps_recorded"), out.astype(np.int64).tolist()))
+
     def set_forward(self, cooperative=True):
         """Forward kernel of the pairs: six lanes share each evaluation (default) or one thread
         per pair; the results are bitwise the same."""

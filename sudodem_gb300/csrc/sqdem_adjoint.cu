@@ -232,11 +232,51 @@ template <class T> SQA_HD void centerLine(const V3<T>& pos1, const V3<T>& pos2, 
 
 template <class T> struct LMOut { V3<T> p1, p2, center, contact; bool touching; int iters, stop, evals; };
 
+// Branch tape.  The step map jumps or kinks where a decision changes: the Levenberg-Marquardt
+// path (its stopping tests, step acceptances and damping updates), the narrowphase's restarts,
+// the bounding-sphere and contact gates, the shear reset, the Coulomb cap and the sign of the
+// local damping.  A forward run can record the outcome of every such decision (a bit per
+// decision, per pair and step, in the order the pair's step takes them), and a later run can
+// take the recorded outcomes instead of evaluating them: a run with perturbed parameters then
+// follows the recorded branches, and its central differences are differences of one smooth
+// branch, the one whose derivative the reverse pass computes.  Each forced decision whose
+// natural outcome differs is counted.  The replay of the reverse pass evaluates its decisions
+// (NoBranch).
+enum { BR_OFF = 0, BR_RECORD = 1, BR_FORCE = 2 };
+static const int BR_WORDS = 8;   // per pair and step: the number of decisions, then 7 words of outcomes
+struct NoBranch {
+  SQA_HD bool operator()(bool v) { return v; }
+};
+struct BrCur {
+  unsigned* w;   // this pair's words of this step
+  int mode, n, dis;
+  unsigned acc;
+  bool writer;
+  SQA_HD bool operator()(bool v) {
+    if (mode == BR_OFF) return v;
+    const int k = n++;
+    if (k >= 32 * (BR_WORDS - 1)) return v;   // beyond the tape: evaluated (counted as unforced)
+    const int word = 1 + (k >> 5), bit = k & 31;
+    if (mode == BR_RECORD) {
+      acc |= (unsigned)v << bit;
+      if (bit == 31) {
+        if (writer) w[word] = acc;
+        acc = 0u;
+      }
+      return v;
+    }
+    if (bit == 0) acc = w[word];
+    const bool r = (acc >> bit) & 1u;
+    dis += r != v;
+    return r;
+  }
+};
+
 // lmder2 with opts {1, 1e-15, 1e-3, 1e-20}, itmax 50 (Superquadrics_Ig2.cpp:1057-1354).  The
 // Jacobian's re-evaluation at the current point (JacfunctionApp, :1033-1054) is not repeated:
 // its values equal the ones stored for that point and are overwritten by the two probes.
-template <class T, class E = SeqEval>
-__host__ __device__ __noinline__ void lmder2(const Shape<T>& A, const Shape<T>& B, T p[2], LMOut<T>& o, const E& ev = E()) {
+template <class T, class E, class BR>
+__host__ __device__ __noinline__ void lmder2(const Shape<T>& A, const Shape<T>& B, T p[2], LMOut<T>& o, const E& ev, BR& br) {
   const double ONE_THIRD = 0.3333333333333334;
   o.touching = true; o.evals = 1;
   bool stop_flag = false;
@@ -248,16 +288,16 @@ __host__ __device__ __noinline__ void lmder2(const Shape<T>& A, const Shape<T>& 
   ev(A, B, p[0], p[1], C, P1, P2, stop_flag);
   V3<T> pf = P2 - P1;
   T pfL2 = nrm(pf);
-  if (!isfinite(val(pfL2))) stop = 7;
+  if (br(!isfinite(val(pfL2)))) stop = 7;
   for (k = 0; k < 50 && !stop; ++k) {
-    if (val(pfL2) <= 1e-20) { stop = 6; break; }
-    if (stop_flag) { stop = 9; o.touching = false; break; }
+    if (br(val(pfL2) <= 1e-20)) { stop = 6; break; }
+    if (br(stop_flag)) { stop = 9; o.touching = false; break; }
     T s0, c0, s1, c1;
     tsincos(p[0], &s0, &c0);
     tsincos(p[1], &s1, &c1);
     o.contact = mk<T>(c0 * c1, s0 * c1, s1);
     const double angle = val(dot(pf, o.contact)) / (val(nrm(pf)) * val(nrm(o.contact)));
-    if (fabs(angle) > 0.95) { stop = 8; break; }
+    if (br(fabs(angle) > 0.95)) { stop = 8; break; }
     ev(A, B, p[0] + Dp0, p[1], C, P1, P2, stop_flag);
     const V3<T> f1 = P2 - P1;
     ev(A, B, p[0], p[1] + Dp1, C, P1, P2, stop_flag);
@@ -272,8 +312,8 @@ __host__ __device__ __noinline__ void lmder2(const Shape<T>& A, const Shape<T>& 
     jt1 = J01 * (-1.0 * pf.x) + (J11 * (-1.0 * pf.y) + J21 * (-1.0 * pf.z));
     const double jinf = (fabs(val(jt0)) > fabs(val(jt1)) ? fabs(val(jt0)) : fabs(val(jt1)));
     pL2 = tsqrt(p[0] * p[0] + p[1] * p[1]);
-    if (jinf <= 1e-15) { stop = 1; break; }
-    if (k == 0) mu = 1.0 * (val(j00) > val(j11) ? j00 : j11);
+    if (br(jinf <= 1e-15)) { stop = 1; break; }
+    if (k == 0) mu = 1.0 * (br(val(j00) > val(j11)) ? j00 : j11);
     diag0 = j00; diag1 = j11;
     for (;;) {
       j00 += mu;
@@ -282,20 +322,20 @@ __host__ __device__ __noinline__ void lmder2(const Shape<T>& A, const Shape<T>& 
       Dp0 = (jt0 * j11 - jt1 * j01) / n_a;
       Dp1 = (jt1 * j00 - jt0 * j01) / n_a;
       const double DpL2 = sqrt(val(Dp0) * val(Dp0) + val(Dp1) * val(Dp1));
-      if (DpL2 < 1e-5) { stop = 2; break; }
+      if (br(DpL2 < 1e-5)) { stop = 2; break; }
       const T q0 = p[0] + Dp0, q1 = p[1] + Dp1;
-      if (DpL2 >= (val(pL2) + 1e-3) / (1e-12 * 1e-12)) { stop = 4; break; }
+      if (br(DpL2 >= (val(pL2) + 1e-3) / (1e-12 * 1e-12))) { stop = 4; break; }
       ev(A, B, q0, q1, C, P1, P2, stop_flag);
       o.evals++;
       const V3<T> pDp_f = P2 - P1;
       const T pDp_fL2 = nrm(pDp_f);
-      if (!isfinite(val(pDp_fL2))) { stop = 7; break; }
+      if (br(!isfinite(val(pDp_fL2)))) { stop = 7; break; }
       const T dL = Dp0 * (mu * Dp0 + jt0) + Dp1 * (mu * Dp1 + jt1);
       const T dF = pfL2 - pDp_fL2;
       T tmp = dF / dL;
-      if (val(tmp) > 0.0) {
+      if (br(val(tmp) > 0.0)) {
         tmp = 1.0 - tpow(2 * tmp - 1., 3.);
-        mu = mu * ((val(tmp) >= ONE_THIRD) ? tmp : T(ONE_THIRD));
+        mu = mu * (br(val(tmp) >= ONE_THIRD) ? tmp : T(ONE_THIRD));
         nu = 2;
         p[0] = q0; p[1] = q1;
         pf = pDp_f; pfL2 = pDp_fL2;
@@ -323,30 +363,30 @@ template <class T> struct Geom {
 
 // Ig2_Superquadrics_Superquadrics_SuperquadricsGeom::go (Superquadrics_Ig2.cpp:1880-2317),
 // non-sphere bodies, no periodic shift.
-template <class T, class E = SeqEval>
+template <class T, class E, class BR>
 __host__ __device__ __noinline__ void geomSqSq(Geom<T>& g, bool isNew, double prevDepth, const T angIn[2], const Shape<T>& A,
-                                               const Shape<T>& B, const E& ev = E()) {
+                                               const Shape<T>& B, const E& ev, BR& br) {
   g.precomputed = false; g.evals = 0; g.calls = 0;
   T para[2];
   if (isNew) { g.isShearNew = true; centerLine(A.pos, B.pos, para); }
-  else { g.isShearNew = prevDepth <= 0; para[0] = angIn[0]; para[1] = angIn[1]; }
+  else { g.isShearNew = br(prevDepth <= 0); para[0] = angIn[0]; para[1] = angIn[1]; }
   g.angMode = isNew ? 2 : 0;
   g.depth = T(0.0);
   const double r_sum = A.rmax + B.rmax;
-  if (val(nrm(A.pos - B.pos)) > r_sum) { g.isShearNew = true; return; }
+  if (br(val(nrm(A.pos - B.pos)) > r_sum)) { g.isShearNew = true; return; }
   LMOut<T> o;
-  lmder2(A, B, para, o, ev);
+  lmder2(A, B, para, o, ev, br);
   g.evals += o.evals; g.calls++;
-  if ((isnan(val(para[0])) || isnan(val(para[1])) || 7 == o.stop) && o.touching) {
+  if (br((isnan(val(para[0])) || isnan(val(para[1])) || 7 == o.stop) && o.touching)) {
     centerLine(A.pos, B.pos, para);
-    lmder2(A, B, para, o, ev);
+    lmder2(A, B, para, o, ev, br);
     g.evals += o.evals; g.calls++;
   }
   T pDepth = dot(o.p1 - o.p2, o.contact);
-  if (o.touching && 10.0 * val(nrm(o.p2 - o.p1)) > A.rmax) {
-    if (!isInside(A, vval(o.p2 - A.pos)) || !isInside(B, vval(o.p1 - B.pos))) {
+  if (br(o.touching && 10.0 * val(nrm(o.p2 - o.p1)) > A.rmax)) {
+    if (br(!isInside(A, vval(o.p2 - A.pos)) || !isInside(B, vval(o.p1 - B.pos)))) {
       centerLine(A.pos, B.pos, para);
-      lmder2(A, B, para, o, ev);
+      lmder2(A, B, para, o, ev, br);
       g.evals += o.evals; g.calls++;
       pDepth = dot(o.p1 - o.p2, o.contact);
     }
@@ -362,10 +402,11 @@ __host__ __device__ __noinline__ void geomSqSq(Geom<T>& g, bool isNew, double pr
 }
 
 // Ig2_Wall_Superquadrics_SuperquadricsGeom::go (Superquadrics_Ig2.cpp:2522-2611), non-sphere
-template <class T>
-SQA_HD void geomWallSq(Geom<T>& g, bool isNew, double prevDepth, int PA, double sense, double wallc, const Shape<T>& B) {
+template <class T, class BR>
+SQA_HD void geomWallSq(Geom<T>& g, bool isNew, double prevDepth, int PA, double sense, double wallc, const Shape<T>& B,
+                       BR& br) {
   g.precomputed = false; g.evals = 1; g.calls = 0; g.angMode = isNew ? 2 : 0;
-  g.isShearNew = isNew ? true : (prevDepth <= 0);
+  g.isShearNew = isNew ? true : br(prevDepth <= 0);
   g.depth = T(0.0);
   V3<double> nd = mk<double>(0.0, 0.0, 0.0);
   if (PA == 0) nd.x = sense; else if (PA == 1) nd.y = sense; else nd.z = sense;
@@ -375,9 +416,11 @@ SQA_HD void geomWallSq(Geom<T>& g, bool isNew, double prevDepth, int PA, double 
   if (PA == 0) p1.x = T(wallc); else if (PA == 1) p1.y = T(wallc); else p1.z = T(wallc);
   const V3<T> dd = point2 - p1;
   const double ndot = PA == 0 ? nd.x * val(dd.x) : (PA == 1 ? nd.y * val(dd.y) : nd.z * val(dd.z));
-  if (ndot >= 0.0) { g.isShearNew = true; return; }
+  const bool apart = ndot >= 0.0;
+  if (br(apart)) { g.isShearNew = true; return; }
   g.cp = 0.5 * (point2 + p1);
-  g.depth = nrm(dd);
+  // |dd|, signed where a forced contact is apart (the depth's smooth continuation)
+  g.depth = apart ? -nrm(dd) : nrm(dd);
   g.normal = normal;
   g.precomputed = true;
 }
@@ -390,8 +433,8 @@ template <class T> struct LawIn {
   T depth; V3<T> normal, cp, x1, x2, v1, w1, v2, w2, nPrev, sPrev; T kn, ks, tanphi;
 };
 template <class T> struct LawOut { V3<T> Fv, T1, T2, s; bool sliding; };
-template <class T> SQA_HD bool law(const LawIn<T>& in, bool isShearNew, double dt, LawOut<T>& out) {
-  if (!(val(in.depth) > 1E-18)) return false;
+template <class T, class BR> SQA_HD bool law(const LawIn<T>& in, bool isShearNew, double dt, LawOut<T>& out, BR& br) {
+  if (!br(val(in.depth) > 1E-18)) return false;
   V3<T> ortho, twist;
   if (!isShearNew) {
     ortho = cross(in.nPrev, in.normal);
@@ -416,8 +459,10 @@ template <class T> SQA_HD bool law(const LawIn<T>& in, bool isShearNew, double d
   sf = sf - in.ks * shearInc;
   const T maxFs = sqn(normalForce) * (in.tanphi * in.tanphi);
   out.sliding = false;
-  if (val(sqn(sf)) > val(maxFs)) {
-    const T ratio = tsqrt(maxFs) / nrm(sf);
+  if (br(val(sqn(sf)) > val(maxFs))) {
+    // |Fn| tan(phi), signed where a forced contact has a negative depth (its smooth continuation)
+    const T cap = val(in.depth) < 0 ? -tsqrt(maxFs) : tsqrt(maxFs);
+    const T ratio = cap / nrm(sf);
     sf = sf * ratio;
     out.sliding = true;
   }
@@ -427,6 +472,10 @@ template <class T> SQA_HD bool law(const LawIn<T>& in, bool isShearNew, double d
   out.T2 = cross(in.x2 - in.cp, Fv);
   out.s = sf;
   return true;
+}
+template <class T> SQA_HD bool law(const LawIn<T>& in, bool isShearNew, double dt, LawOut<T>& out) {
+  NoBranch nb;
+  return law(in, isShearNew, dt, out, nb);
 }
 
 // NewtonIntegrator rotation of a superquadric: leapfrogAsphericalRotate with
@@ -471,7 +520,7 @@ SQA_HD void rotStep(const T q[4], const V3<T>& L, const V3<T>& M, double4 I, dou
 // Device data
 enum : int { CF_GEOM = 1 };                 // flag: Interaction::geom present
 enum : int { CO_PRE = 1, CO_FORCE = 2, CO_ANG = 4, CO_ANG0 = 8, CO_NEW = 16, CO_SHNEW = 32, CO_SLIDE = 64 };
-enum { A_MISMATCH = 0, A_EVALS, A_LMCALLS, A_REPLAYED, A_SIG, A_SIGB, A_NCOUNT };
+enum { A_MISMATCH = 0, A_EVALS, A_LMCALLS, A_REPLAYED, A_SIG, A_SIGB, A_BRDEC, A_BRDIS, A_BRUNF, A_NCOUNT };
 
 struct Consts {
   int nb, P;
@@ -484,6 +533,11 @@ struct Consts {
   const double4* phys;    // kn ks tanphi
   const int* bStart; const int* bList;   // per body: pair index * 2 + side (0: the body is id1)
   unsigned long long* cnt;
+  // branch tape of the forward run (BR_OFF in the reverse pass's recomputation): BR_WORDS words
+  // per pair and step, one word per body and step (the local damping's sign codes)
+  unsigned* brPair;
+  unsigned* brBody;
+  int brMode;
 };
 // state of the scene between steps
 struct State {
@@ -542,7 +596,7 @@ template <int N> struct Seeder<Dual<N>> { static SQA_HD Dual<N> s(double x, int 
 // orientation of id2, 11-12 eps of id1, 13-14 eps of id2, 15-16 the stored contact angles.
 // The position of id1 carries no tangent: the SQ-SQ outputs other than the contact point are
 // invariant under a common translation, which gives their derivatives with respect to it.
-template <class T, class E = SeqEval> SQA_HD void pairGeom(const PairVals& p, Geom<T>& g, int base = 0, const E& ev = E()) {
+template <class T, class E, class BR> SQA_HD void pairGeom(const PairVals& p, Geom<T>& g, int base, const E& ev, BR& br) {
   typedef Seeder<T> Sd;
   const V3<T> X2 = mk<T>(Sd::s(p.x2.x, 0, base), Sd::s(p.x2.y, 1, base), Sd::s(p.x2.z, 2, base));
   T q2[4];
@@ -551,15 +605,19 @@ template <class T, class E = SeqEval> SQA_HD void pairGeom(const PairVals& p, Ge
   shapeInit(B, p.shp2, Sd::s(p.e2.x, 13, base), Sd::s(p.e2.y, 14, base), q2, X2);
   if (p.i1.x == 1) {
     const double wallc = p.i1.y == 0 ? p.x1.x : (p.i1.y == 1 ? p.x1.y : p.x1.z);
-    geomWallSq(g, p.isNew, p.prevDepth, p.i1.y, (double)p.i1.z, wallc, B);
+    geomWallSq(g, p.isNew, p.prevDepth, p.i1.y, (double)p.i1.z, wallc, B, br);
   } else {
     T q1[4];
     for (int k = 0; k < 4; k++) q1[k] = Sd::s(p.q1[k], 3 + k, base);
     Shape<T> A;
     shapeInit(A, p.shp1, Sd::s(p.e1.x, 11, base), Sd::s(p.e1.y, 12, base), q1, lift<T>(p.x1));
     const T angIn[2] = {Sd::s(p.ang[0], 15, base), Sd::s(p.ang[1], 16, base)};
-    geomSqSq(g, p.isNew, p.prevDepth, angIn, A, B, ev);
+    geomSqSq(g, p.isNew, p.prevDepth, angIn, A, B, ev, br);
   }
+}
+template <class T, class E = SeqEval> SQA_HD void pairGeom(const PairVals& p, Geom<T>& g, int base = 0, const E& ev = E()) {
+  NoBranch nb;
+  pairGeom(p, g, base, ev, nb);
 }
 
 // Law inputs, 34 of them, in replay chunk `chunk` (inputs 17*chunk .. 17*chunk+16, from
@@ -601,7 +659,10 @@ SQA_HD void fwdContact(const Consts& C, const State& S, const StepOut& O, int st
   PairVals p;
   loadPair(C, S, c, p);
   Geom<double> g;
-  pairGeom<double>(p, g, 0, ev);
+  BrCur br;
+  br.mode = C.brMode; br.n = 0; br.dis = 0; br.acc = 0u; br.writer = writer;
+  br.w = C.brMode != BR_OFF ? C.brPair + ((size_t)step * C.P + c) * BR_WORDS : nullptr;
+  pairGeom<double>(p, g, 0, ev, br);
   if (!writer) return;
   int code = (g.precomputed ? CO_PRE : 0) | (p.isNew ? CO_NEW : 0) | (g.isShearNew ? CO_SHNEW : 0);
   if (g.angMode == 1) { code |= CO_ANG; S.angle[c] = make_double2(g.ang[0], g.ang[1]); }
@@ -612,7 +673,7 @@ SQA_HD void fwdContact(const Consts& C, const State& S, const StepOut& O, int st
     LawIn<double> in;
     lawInputs<double>(p, g.depth, g.normal, g.cp, 0, in);
     LawOut<double> out;
-    if (law(in, g.isShearNew, C.dt, out)) {
+    if (law(in, g.isShearNew, C.dt, out, br)) {
       code |= CO_FORCE | (out.sliding ? CO_SLIDE : 0);
       Fv = d4(out.Fv, 1.0);
       sOut = out.s;
@@ -629,6 +690,16 @@ SQA_HD void fwdContact(const Consts& C, const State& S, const StepOut& O, int st
   // the decisions at which the map jumps: the Levenberg-Marquardt path (evaluations, calls).
   // The contact gate and the Coulomb cap are continuous (kinks), so they are not recorded.
   SQA_CNT(&C.cnt[A_SIG], branchHash(c, step, (unsigned long long)g.evals | ((unsigned long long)g.calls << 20)));
+  if (br.mode != BR_OFF) {
+    const int cap = 32 * (BR_WORDS - 1);
+    if (br.mode == BR_RECORD) {
+      if ((br.n & 31) && br.n < cap) br.w[1 + (br.n >> 5)] = br.acc;
+      br.w[0] = (unsigned)br.n;
+    }
+    SQA_CNT(&C.cnt[A_BRDEC], br.n);
+    if (br.dis) SQA_CNT(&C.cnt[A_BRDIS], br.dis);
+    if (br.n > cap) SQA_CNT(&C.cnt[A_BRUNF], br.n - cap);
+  }
 }
 __global__ void __launch_bounds__(128) k_fwd_contacts(Consts C, State S, StepOut O, int step) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -687,6 +758,36 @@ SQA_HD unsigned long long velSignBits(const V3<double>& a, const V3<double>& v, 
          sgnBits(a.z, v.z + 0.5 * dt * a.z, 2) | sgnBits(m.x, w.x, 3) | sgnBits(m.y, w.y, 4) | sgnBits(m.z, w.z, 5) |
          (1ull << 12);
 }
+// The local damping on the branch tape: per component the sign of x w (2 bits: 1 positive, 2
+// negative, 0 zero), which selects the factor 1 - d sgn(x w); x (1 - d sgn(x w)) kinks where x
+// crosses 0 and jumps where w does.  Forced: the recorded factor where the natural one differs.
+SQA_HD unsigned dampCode(double x, double w) {
+  const double s = tsgn(x * w);
+  return s > 0 ? 1u : (s < 0 ? 2u : 0u);
+}
+SQA_HD void dampBranches(const Consts& C, int step, int b, const V3<double>& a0, const V3<double>& vel0,
+                         const V3<double>& m0, const V3<double>& angVel, Trans& t) {
+  const double dt = C.dt, d = C.damping;
+  const unsigned nat = dampCode(a0.x, vel0.x + 0.5 * dt * a0.x) | dampCode(a0.y, vel0.y + 0.5 * dt * a0.y) << 2 |
+                       dampCode(a0.z, vel0.z + 0.5 * dt * a0.z) << 4 | dampCode(m0.x, angVel.x) << 6 |
+                       dampCode(m0.y, angVel.y) << 8 | dampCode(m0.z, angVel.z) << 10;
+  unsigned* slot = C.brBody + (size_t)step * C.nb + b;
+  int dis = 0;
+  if (C.brMode == BR_RECORD) {
+    *slot = nat;
+  } else if (*slot != nat) {
+    const unsigned rec = *slot;
+    double* f[6] = {&t.s.x, &t.s.y, &t.s.z, &t.sr.x, &t.sr.y, &t.sr.z};
+    for (int k = 0; k < 6; k++) {
+      const unsigned r2 = (rec >> (2 * k)) & 3u;
+      if (r2 == ((nat >> (2 * k)) & 3u)) continue;
+      dis++;
+      *f[k] = 1 - d * (r2 == 1u ? 1.0 : (r2 == 2u ? -1.0 : 0.0));
+    }
+  }
+  SQA_CNT(&C.cnt[A_BRDEC], 6);
+  if (dis) SQA_CNT(&C.cnt[A_BRDIS], dis);
+}
 SQA_HD void fwdBody(const Consts& C, const State& S, const StepOut& O, int step, int b) {
   const double dt = C.dt;
   V3<double> pos = xyz(S.pos[b]);
@@ -700,8 +801,12 @@ SQA_HD void fwdBody(const Consts& C, const State& S, const StepOut& O, int step,
   gatherFT(C, O, b, pos, f, m);
   const V3<double> angVel = xyz(S.angVel[b]);
   const double4 mI = C.massI[b];
-  const Trans t = dampFactors(C, f, m, mI.x, vel, angVel, a);
+  Trans t = dampFactors(C, f, m, mI.x, vel, angVel, a);
   const V3<double> a0 = a, vel0 = vel, m0 = m;
+  // local damping x (1 - d sgn(x w)) is continuous where x crosses 0 and jumps where w does:
+  // the sign of w (v + dt a / 2, resp. the angular velocity) where x is not 0
+  const unsigned long long bits = velSignBits(a0, vel0, dt, m0, angVel);
+  if (C.brMode != BR_OFF) dampBranches(C, step, b, a0, vel0, m0, angVel, t);
   a.x *= t.s.x; a.y *= t.s.y; a.z *= t.s.z;
   vel = vel + dt * a;
   m.x *= t.sr.x; m.y *= t.sr.y; m.z *= t.sr.z;
@@ -713,9 +818,6 @@ SQA_HD void fwdBody(const Consts& C, const State& S, const StepOut& O, int step,
   S.pos[b] = d4(pos, 0);
   S.ori[b] = make_double4(qo[0], qo[1], qo[2], qo[3]);
   S.vel[b] = d4(vel, 0); S.angVel[b] = d4(wo, 0); S.angMom[b] = d4(Lo, 0);
-  // local damping x (1 - d sgn(x w)) is continuous where x crosses 0 and jumps where w does:
-  // record the sign of w (v + dt a / 2, resp. the angular velocity) where x is not 0
-  const unsigned long long bits = velSignBits(a0, vel0, dt, m0, angVel);
   SQA_CNT(&C.cnt[A_SIGB], branchHash(C.P + b, step, bits));
 }
 __global__ void __launch_bounds__(128) k_fwd_integrate(Consts C, State S, StepOut O, int step) {
@@ -1079,6 +1181,10 @@ struct sqdem_adj {
   int replayBlocks = 1;   // grouped reverse kernels: resident blocks per SM (grid-stride); 0 = unbounded
   int numSMs = 1;
   bool coopForward = true;   // forward pairs on six-lane groups (k_fwd_contacts_coop)
+  // branch tape (BR_OFF, BR_RECORD, BR_FORCE) and the steps it holds
+  int brMode = BR_OFF, brSteps = 0;
+  size_t brCap = 0;   // steps allocated
+  unsigned *brPair = nullptr, *brBody = nullptr;
   double loss = 0;
   unsigned long long counters[A_NCOUNT] = {};
   double msForward = 0, msBackward = 0;
@@ -1106,14 +1212,22 @@ static void afreeAll(sqdem_adj* a) {
   a->allocs.clear();
   a->ckpt.clear(); a->tapeState.clear();
   a->init = a->work = a->fin = nullptr; a->finFv = nullptr; a->tapeCap = 0;
+  a->brPair = a->brBody = nullptr; a->brCap = 0; a->brSteps = 0;
+}
+static void afree(sqdem_adj* a, void* p) {
+  if (!p) return;
+  auto it = std::find(a->allocs.begin(), a->allocs.end(), p);
+  if (it != a->allocs.end()) { cudaFree(p); a->allocs.erase(it); }
 }
 
-static Consts consts(sqdem_adj* a) {
+static Consts consts(sqdem_adj* a, bool branches = false) {
   Consts C;
   C.nb = a->nb; C.P = a->P; C.dt = a->dt; C.g[0] = a->g[0]; C.g[1] = a->g[1]; C.g[2] = a->g[2];
   C.damping = a->damping;
   C.shp = a->shp; C.eps = a->eps; C.massI = a->massI; C.binfo = a->binfo; C.ids = a->idsD; C.phys = a->phys;
   C.bStart = a->bStart; C.bList = a->bList; C.cnt = a->cnt;
+  C.brMode = branches ? a->brMode : BR_OFF;
+  C.brPair = a->brPair; C.brBody = a->brBody;
   return C;
 }
 static StepOut tapeOut(sqdem_adj* a, int slot) {
@@ -1178,8 +1292,8 @@ static void launchReplay(sqdem_adj* a, const Consts& C, const State& S, const St
   }
 }
 
-static void launchStep(sqdem_adj* a, const State& S, const StepOut& O, int step) {
-  const Consts C = consts(a);
+static void launchStep(sqdem_adj* a, const State& S, const StepOut& O, int step, bool branches = false) {
+  const Consts C = consts(a, branches);
   if (a->coopForward)
     k_fwd_contacts_coop<<<nblk(a->P, COOP_WARPS * 5), 32 * COOP_WARPS, 0, a->st>>>(C, S, O, step);
   else
@@ -1376,6 +1490,16 @@ sqdem_status sqdem_adj_forward(sqdem_adj* a, int nsteps, int checkpoint_every, c
   }
   sqdem_status s = ensureTape(a, 1);
   if (s != SQDEM_OK) return s;
+  if (a->brMode == BR_FORCE && nsteps > a->brSteps)
+    return afail(a, SQDEM_ERR_STATE, "forced branches: the recorded run has fewer steps than this one");
+  if (a->brMode == BR_RECORD && (size_t)nsteps > a->brCap) {
+    afree(a, a->brPair); afree(a, a->brBody);
+    a->brPair = nullptr; a->brBody = nullptr; a->brCap = 0; a->brSteps = 0;
+    ACUDA(aalloc(a, &a->brPair, (size_t)nsteps * a->P * BR_WORDS + 1));
+    ACUDA(aalloc(a, &a->brBody, (size_t)nsteps * a->nb));
+    a->brCap = nsteps;
+  }
+  if (a->brMode == BR_RECORD) a->brSteps = 0;
   std::vector<double4> hw(a->nb);
   for (int i = 0; i < a->nb; i++) hw[i] = wF3 ? make_double4(wF3[3 * i], wF3[3 * i + 1], wF3[3 * i + 2], 0) : make_double4(0, 0, 0, 0);
   ACUDA(cudaMemcpyAsync(a->wF, hw.data(), a->nb * sizeof(double4), cudaMemcpyHostToDevice, a->st));
@@ -1391,8 +1515,9 @@ sqdem_status sqdem_adj_forward(sqdem_adj* a, int nsteps, int checkpoint_every, c
   for (int t = 0; t < nsteps; t++) {
     if (t % checkpoint_every == 0)
       ACUDA(cudaMemcpyAsync(a->ckpt[t / checkpoint_every], a->work, a->L.bytes, cudaMemcpyDeviceToDevice, a->st));
-    launchStep(a, S, O, t);
+    launchStep(a, S, O, t, true);
   }
+  if (a->brMode == BR_RECORD) a->brSteps = nsteps;
   k_loss<<<1, 256, 0, a->st>>>(consts(a), S, O, a->wF, a->wX, a->lossD);
   ACUDA(cudaGetLastError());
   ACUDA(cudaMemcpyAsync(a->fin, a->work, a->L.bytes, cudaMemcpyDeviceToDevice, a->st));
@@ -1555,6 +1680,20 @@ sqdem_status sqdem_adj_get_pairs(sqdem_adj* a, double* out16) {
 
 // counters of the last runs: replay mismatches, Disfunction evaluations (forward), LM calls
 // (forward), pairs replayed (backward), forward ms, backward ms, steps, checkpoint interval
+sqdem_status sqdem_adj_set_branches(sqdem_adj* a, int mode) {
+  if (!a || mode < BR_OFF || mode > BR_FORCE) return SQDEM_ERR_ARG;
+  if (mode == BR_FORCE && a->brSteps == 0) return afail(a, SQDEM_ERR_STATE, "forced branches: no recorded run");
+  a->brMode = mode;
+  return SQDEM_OK;
+}
+
+sqdem_status sqdem_adj_branch_report(sqdem_adj* a, double* out4) {
+  if (!a || !out4) return SQDEM_ERR_ARG;
+  out4[0] = (double)a->counters[A_BRDEC]; out4[1] = (double)a->counters[A_BRDIS];
+  out4[2] = (double)a->counters[A_BRUNF]; out4[3] = (double)a->brSteps;
+  return SQDEM_OK;
+}
+
 sqdem_status sqdem_adj_report(sqdem_adj* a, double* out8) {
   if (!a || !out8) return SQDEM_ERR_ARG;
   out8[0] = (double)a->counters[A_MISMATCH]; out8[1] = (double)a->counters[A_EVALS];

@@ -15,6 +15,16 @@ extern "C" sqdem_status sqdem_shape_props(double rx, double ry, double rz, doubl
   out5[0] = out5[1] = out5[2] = out5[3] = 0; out5[4] = r;
   return SQDEM_OK;
 }
+// branch tape of the host window (sqdem_adj_set_branches' modes), kept between runs
+static int g_brMode = BR_OFF, g_brSteps = 0;
+static std::vector<unsigned> g_brPair, g_brBody;
+static double g_brReport[4] = {0, 0, 0, 0};
+extern "C" int adjh_set_branches(int mode) {
+  if (mode < BR_OFF || mode > BR_FORCE || (mode == BR_FORCE && g_brSteps == 0)) return 1;
+  g_brMode = mode;
+  return 0;
+}
+extern "C" void adjh_branch_report(double* out4) { for (int k = 0; k < 4; k++) out4[k] = g_brReport[k]; }
 extern "C" double adjh_run(int n, const int* kind, const double* shape5, const int* was, const int* mat,
                            const double* state37, long npairs, const double* intr57, double dt, const double* g3,
                            double damping, int nmat, const double* Kn, const double* Ks, const double* fa,
@@ -56,6 +66,13 @@ extern "C" double adjh_run(int n, const int* kind, const double* shape5, const i
   Consts C; C.nb = n; C.P = P; C.dt = dt; for (int k = 0; k < 3; k++) C.g[k] = g3[k]; C.damping = damping;
   C.shp = hShp.data(); C.eps = hEps.data(); C.massI = hMI.data(); C.binfo = hInfo.data(); C.ids = a->ids.data();
   C.phys = ph.data(); C.bStart = start.data(); C.bList = list.data(); C.cnt = cnt;
+  if (g_brMode == BR_FORCE && nsteps > g_brSteps) return NAN;
+  if (g_brMode == BR_RECORD) {
+    g_brPair.assign((size_t)nsteps * P * BR_WORDS + 1, 0u);
+    g_brBody.assign((size_t)nsteps * n, 0u);
+    g_brSteps = nsteps;
+  }
+  C.brMode = g_brMode; C.brPair = g_brPair.data(); C.brBody = g_brBody.data();
   StateLayout L; L.init(n, P);
   std::vector<std::vector<char>> st(nsteps + 1, std::vector<char>(L.bytes, 0));
   {
@@ -99,6 +116,9 @@ extern "C" double adjh_run(int n, const int* kind, const double* shape5, const i
     }
   }
   sigOut[0] = cnt[A_SIG] + cnt[A_SIGB];
+  g_brReport[0] = (double)cnt[A_BRDEC]; g_brReport[1] = (double)cnt[A_BRDIS]; g_brReport[2] = (double)cnt[A_BRUNF];
+  g_brReport[3] = g_brSteps;
+  C.brMode = BR_OFF;   // the reverse pass evaluates its decisions
   // backward
   std::vector<double4> lPos(wX), lOri(n), lVel(n), lW(n), lL(n), lF(n), lT(n), lN(P + 1), lS(P + 1), con(8 * (size_t)P + 8),
       accE(P + 1), accP(P + 1);

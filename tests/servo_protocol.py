@@ -7,7 +7,9 @@ kn = 1e5 N/m), run by config 2's CompressionEngine (pkg/dem/Compression.cpp:395-
 held on the lateral walls, the top and bottom walls driven in strain (the shear phase of
 action_cubic).  Recorded after DURATION seconds of simulated time (the number of steps follows
 from the specimen's time step): the axial and mean lateral wall stresses, the porosity of the
-box, the coordination number of the particles and the axial strain.
+box, the coordination number of the particles, the axial strain, and the mean penetration depth
+of the touching particle pairs averaged over the last AVG_CHUNKS chunks (at a given stress it
+scales as 1/kn: the contact stiffness's fingerprint).
 """
 import numpy as np
 
@@ -28,7 +30,20 @@ def spec_and_config(seed, n=N, kn=1e5):
     return spec, cfg
 
 
+AVG_CHUNKS = 10   # chunks at the end over which the mean penetration depth is averaged
+
+
+def _mean_depth(spec, recs):
+    kind = spec.kind
+    touching = (recs[:, 2] != 0) & (recs[:, 4] > 0)
+    pp = touching & (kind[recs[:, 0].astype(int)] == 0) & (kind[recs[:, 1].astype(int)] == 0)
+    return (float(np.mean(recs[pp, 4])) if np.any(pp) else 0.0), pp
+
+
 class Run:
+    """One specimen, advanced chunk by chunk (engine-agnostic: the oracle scene or the GPU engine,
+    both with step, set_servo, servo_state and interactions)."""
+
     def __init__(self, spec, engine, cfg):
         self.spec, self.e = spec, engine
         engine.set_servo(cfg)
@@ -36,6 +51,7 @@ class Run:
         self.total = int(np.ceil(DURATION / spec.params["dt"]))
         self.done = False
         self.result = None
+        self.depths = []
 
     def advance(self):
         n = min(CHUNK, self.total - self.steps)
@@ -43,16 +59,16 @@ class Run:
         self.steps += n
 
     def check(self):
+        if self.steps >= self.total - AVG_CHUNKS * CHUNK:
+            self.depths.append(_mean_depth(self.spec, self.e.interactions())[0])
         if self.steps < self.total:
             return False
         self.done = True
         st = state_dict(self.e.servo_state())
         recs = self.e.interactions()
-        kind = self.spec.kind
-        touching = (recs[:, 2] != 0) & (recs[:, 4] > 0)
-        pp = touching & (kind[recs[:, 0].astype(int)] == 0) & (kind[recs[:, 1].astype(int)] == 0)
+        _, pp = _mean_depth(self.spec, recs)
         self.result = {"axial_stress": st["wszz"], "lateral_stress": 0.5 * (st["wsxx"] + st["wsyy"]),
                        "porosity": 1.0 - st["particlesVolume"] / st["Current_boxVolume"],
                        "coordination": 2.0 * float(np.sum(pp)) / self.spec.n_particles, "axial_strain": st["strain2"],
-                       "unbalanced_force": st["UnbalancedForce"]}
+                       "unbalanced_force": st["UnbalancedForce"], "mean_depth": float(np.mean(self.depths))}
         return True

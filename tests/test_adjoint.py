@@ -191,6 +191,64 @@ def test_adjoint_gradient_matches_central_differences(scene, window, reference):
 
 
 @pytest.mark.gpu
+def test_forced_branches_central_differences_at_the_relative_step_1e_6(scene, window):
+    """The branch tape (sqdem_adj_set_branches) on the GPU: a forced run with the recorded
+    parameters is bitwise the recorded one, and central differences at the relative step 1e-6
+    of runs forced onto the recorded branches match the reverse pass along 20 seeded directions
+    within 1e-5 relative, or within the loss's measured rounding noise divided by h where the
+    directional derivative is too small for the difference to resolve it (at least 15 of 20
+    within 1e-5), while naturally evaluated runs leave the recorded branches in some of them."""
+    from sudodem_gb300.adjoint import AdjointWindow
+    spec, bodies, recs = scene
+    eps, mu, Kn, Ks = params_of(spec)
+    n = spec.n_bodies
+    wF, wX = lid_weights(n), np.zeros((n, 3))
+    w = window
+    h = 1e-6
+    try:
+        w.set_branches(AdjointWindow.BRANCH_RECORD)
+        L0, s0 = _gpu_loss(w, spec, eps, mu, Kn, Ks, wF, wX)
+        gr = w.backward()
+        rec = w.branch_report()
+        assert rec["decisions"] > 0 and rec["disagreements"] == 0 and rec["steps_recorded"] == NSTEPS
+        w.set_branches(AdjointWindow.BRANCH_FORCE)
+        L1, s1 = _gpu_loss(w, spec, eps, mu, Kn, Ks, wF, wX)
+        rep = w.branch_report()
+        assert L1 == L0 and s1 == s0 and rep["disagreements"] == 0 and rep["decisions"] == rec["decisions"]
+        rng = np.random.default_rng(7)
+        noise = 0.0
+        for k in range(4):
+            d = rng.normal(size=mu.shape) * mu
+            Ls, _ = _gpu_loss(w, spec, eps, mu + 1e-13 * d, Kn, Ks, wF, wX)
+            noise = max(noise, abs(Ls - L0 - 1e-13 * float(np.sum(gr["mu"] * d))))
+        part = (spec.kind == 0)[:, None]
+        within, left = 0, 0
+        for trial in range(5):
+            dirs = [("eps", (rng.normal(size=eps.shape) * eps * part, 0 * mu, 0 * Kn, 0 * Ks)),
+                    ("mu", (0 * eps, rng.normal(size=mu.shape) * mu, 0 * Kn, 0 * Ks)),
+                    ("Kn", (0 * eps, 0 * mu, rng.normal(size=Kn.shape) * Kn, 0 * Ks)),
+                    ("Ks", (0 * eps, 0 * mu, 0 * Kn, rng.normal(size=Ks.shape) * Ks))]
+            for name, d in dirs:
+                dE, dmu, dKn, dKs = d
+                vals, dis = [], 0
+                for sg in (1, -1):
+                    l, _ = _gpu_loss(w, spec, eps + sg * h * dE, mu + sg * h * dmu, Kn + sg * h * dKn,
+                                     Ks + sg * h * dKs, wF, wX)
+                    vals.append(l)
+                    dis += w.branch_report()["disagreements"]
+                left += dis > 0
+                fd = (vals[0] - vals[1]) / (2 * h)
+                ad = _ad(gr, d)
+                within += abs(fd - ad) <= TOL * abs(ad)
+                assert abs(fd - ad) <= TOL * abs(ad) + 2 * noise / h, (name, trial, fd, ad, dis, noise)
+        assert within >= 15 and left > 0, (within, left)
+    finally:
+        w.set_branches(AdjointWindow.BRANCH_NATURAL)
+        w.set_materials(Kn, Ks, mu)
+        w.set_eps(eps)
+
+
+@pytest.mark.gpu
 def test_adjoint_checkpoint_interval_changes_nothing(scene, window):
     spec, bodies, recs = scene
     eps, mu, Kn, Ks = params_of(spec)

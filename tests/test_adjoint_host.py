@@ -48,6 +48,10 @@ def host():
         assert r.returncode == 0, r.stdout.decode(errors="replace")
         os.replace(LIB + ".tmp", LIB)
     lib = C.CDLL(LIB)
+    lib.adjh_set_branches.restype = C.c_int
+    lib.adjh_set_branches.argtypes = [C.c_int]
+    lib.adjh_branch_report.restype = None
+    lib.adjh_branch_report.argtypes = [C.POINTER(C.c_double)]
     lib.adjh_run.restype = C.c_double
     dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
     lib.adjh_run.argtypes = [C.c_int, ip, dp, ip, ip, dp, C.c_long, dp, C.c_double, dp, C.c_double, C.c_int, dp, dp,
@@ -132,3 +136,68 @@ def test_host_reverse_pass_matches_oracle_central_differences(host, scene):
             assert abs(fd - ad) <= TOL * abs(ad), (name, trial, fd, ad)
             checked[name] = checked.get(name, 0) + 1
     assert all(checked.get(k, 0) >= 3 for k in ("eps", "mu", "Kn", "Ks")), checked
+
+
+def _branch_report(lib):
+    out = np.zeros(4)
+    lib.adjh_branch_report(out.ctypes.data_as(C.POINTER(C.c_double)))
+    return dict(zip(("decisions", "disagreements", "unforced", "steps"), out.astype(np.int64).tolist()))
+
+
+def test_host_forced_branches_central_differences_at_the_relative_step_1e_6(host, scene):
+    """Finite differences within the recorded branches (sqdem_adj_set_branches): the base run
+    records every decision, the +h and -h runs take the recorded outcomes.  At the relative step
+    1e-6 of the differentiation check the natural runs leave the base run's branches (a
+    Levenberg-Marquardt stopping test, a contact gate, a damping sign), the forced ones do not,
+    and their central differences match the reverse pass along 20 seeded directions within 1e-5
+    relative, or within the loss's rounding noise (measured from runs perturbed by 1e-13, at
+    which the linear change is below it) divided by h where the directional derivative is so
+    small that the noise dominates the difference; at least 15 of the 20 within 1e-5."""
+    spec, bodies, recs = scene
+    eps, mu, Kn, Ks = params_of(spec)
+    n = spec.n_bodies
+    wF, wX = lid_weights(n), np.zeros((n, 3))
+    assert host.adjh_set_branches(2) != 0            # nothing recorded yet
+    assert host.adjh_set_branches(1) == 0
+    L0, s0, mism, gr, _ = _run(host, spec, bodies, recs, eps, mu, Kn, Ks, NSTEPS, wF, wX)
+    rec = _branch_report(host)
+    assert mism == 0 and rec["decisions"] > 0 and rec["disagreements"] == 0 and rec["steps"] == NSTEPS
+    h = 1e-6
+    rng = np.random.default_rng(7)
+    part = (spec.kind == 0)[:, None]
+    natural_left, within, worst = 0, 0, 0.0
+    try:
+        assert host.adjh_set_branches(2) == 0
+        L1, s1, _, _, _ = _run(host, spec, bodies, recs, eps, mu, Kn, Ks, NSTEPS, wF, wX)
+        rep = _branch_report(host)
+        assert L1 == L0 and s1 == s0 and rep["disagreements"] == 0 and rep["decisions"] == rec["decisions"]
+        noise = 0.0
+        for k in range(4):
+            d = rng.normal(size=mu.shape) * mu
+            Ls, _, _, _, _ = _run(host, spec, bodies, recs, eps, mu + 1e-13 * d, Kn, Ks, NSTEPS, wF, wX)
+            noise = max(noise, abs(Ls - L0 - 1e-13 * float(np.sum(gr["mu"] * d))))
+        for trial in range(5):
+            dirs = [("eps", (rng.normal(size=eps.shape) * eps * part, 0 * mu, 0 * Kn, 0 * Ks)),
+                    ("mu", (0 * eps, rng.normal(size=mu.shape) * mu, 0 * Kn, 0 * Ks)),
+                    ("Kn", (0 * eps, 0 * mu, rng.normal(size=Kn.shape) * Kn, 0 * Ks)),
+                    ("Ks", (0 * eps, 0 * mu, 0 * Kn, rng.normal(size=Ks.shape) * Ks))]
+            for name, (dE, dmu, dKn, dKs) in dirs:
+                vals, dis = [], 0
+                for sgn in (1, -1):
+                    args = (eps + sgn * h * dE, mu + sgn * h * dmu, Kn + sgn * h * dKn, Ks + sgn * h * dKs)
+                    Ls, _, _, _, _ = _run(host, spec, bodies, recs, *args, NSTEPS, wF, wX)
+                    vals.append(Ls)
+                    dis += _branch_report(host)["disagreements"]
+                natural_left += dis > 0
+                fd = (vals[0] - vals[1]) / (2 * h)
+                ad = float(np.sum(gr["eps"] * dE) + np.sum(gr["mu"] * dmu) + np.sum(gr["Kn"] * dKn) +
+                           np.sum(gr["Ks"] * dKs))
+                err = abs(fd - ad)
+                worst = max(worst, err / abs(ad))
+                within += err <= TOL * abs(ad)
+                assert err <= TOL * abs(ad) + 2 * noise / h, (name, trial, fd, ad, dis, noise)
+    finally:
+        host.adjh_set_branches(0)
+    print(f"forced central differences at h=1e-6: {within}/20 within 1e-5 (worst {worst:.2e}, rounding noise of "
+          f"the loss {noise:.1e}); {natural_left}/20 directions left a recorded branch when evaluated naturally")
+    assert within >= 15 and natural_left > 0

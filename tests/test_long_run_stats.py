@@ -28,12 +28,13 @@ def _load(prefix=""):
         pytest.skip("tests/golden/compression_stats.json missing (tests/golden/make_compression_stats.py)")
     d = json.load(open(STATS))
     need = [f"{prefix}{lab}/{s}" for lab in ("oracle", "oracle_kn_x1.3") for s in SEEDS]
-    if not all(k in d for k in need):
+    metrics = SERVO_METRICS if prefix == "servo_" else METRICS
+    if not all(k in d and all(m in d[k] for m in metrics) for k in need):
         pytest.skip("tests/golden/compression_stats.json is incomplete (tests/golden/make_compression_stats.py)")
     return d
 
 
-SERVO_METRICS = ("axial_stress", "lateral_stress", "porosity", "coordination")
+SERVO_METRICS = ("axial_stress", "lateral_stress", "porosity", "coordination", "mean_depth")
 
 
 def agree(a, b, metrics=METRICS):
