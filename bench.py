@@ -630,8 +630,9 @@ def config3_start(args):
     largest half-axis and lowered at 0.05 m/s until its force has stayed above 0.5 N (about
     the bed's weight) for ten checks in a row (100 steps apart); every velocity zeroed
     (NewtonIntegrator.quiet_system_flag); then the lid servo-controlled to the preload
-    --lid-force (every 20 steps its velocity set to 2e-3 m/s per N of force error, at most
-    0.01 m/s) until the force has stayed within 10% of the preload for 25 checks in a row; then
+    --lid-force (every 20 steps its velocity set to 2e-3 m/s per N of error of the force averaged
+    over the last five checks, at most 2 mm/s either way) until that force has stayed within 10%
+    of the preload for 25 checks in a row; then
     the lid set to the window's compression velocity (0.05/s x its height).  The window starts
     from the quasi-static, preloaded bed."""
     from sudodem_gb300 import Engine, assemblies
@@ -651,11 +652,12 @@ def config3_start(args):
         held = held + 1 if abs(eng.body_state()[5, 18]) > 0.5 else 0
     eng.set_quiet(True)      # zeroes every body's velocity, the lid's too
     eng.step(1)
-    target, gain, vmax = args.lid_force, 2e-3, 0.01
-    held, k2 = 0, 0
+    target, gain, vmax = args.lid_force, 2e-3, 2e-3
+    held, k2, hist = 0, 0, []
     while held < 25 and k2 < args.servo_max:
         b = eng.body_state()
-        F = abs(b[5, 18])
+        hist = (hist + [abs(b[5, 18])])[-5:]
+        F = float(np.mean(hist))     # the lid force averaged over the last five checks
         held = held + 1 if abs(F - target) <= 0.1 * target else 0
         b[5, 7:10] = [0.0, 0.0, -float(np.clip(gain * (target - F), -vmax, vmax))]
         eng.put_body_state(b)
@@ -792,6 +794,23 @@ def run_ours_adjoint(args):
         part = (spec.kind == 0)[:, None]
         kinds = ("eps", "mu", "Kn", "Ks")
         h = args.fd_h
+        scan = sorted({h, *[float(x) for x in args.fd_scan.split(",") if x]}, reverse=True)
+
+        def central(mode, dE, dmu, dKn, dKs, hh):
+            w.set_branches(mode)
+            vals, sigs, dis, cross = [], [], 0, 0
+            for sgn in (1, -1):
+                w.set_materials(Kn0 + sgn * hh * dKn, Ks0 + sgn * hh * dKs, mu0 + sgn * hh * dmu)
+                w.set_eps(eps0 + sgn * hh * dE)
+                lv, sv = w.forward(fdw, args.checkpoint, wF, wX)
+                vals.append(lv)
+                sigs.append(sv)
+                if mode == AdjointWindow.BRANCH_FORCE:
+                    br = w.branch_report()
+                    dis += br["disagreements"]
+                    cross += br["surface_sign_changes"]
+            return (vals[0] - vals[1]) / (2 * hh), sigs, dis, cross
+
         for k in range(args.fd_dirs):
             name = kinds[k % 4]
             dE = rng.normal(size=eps0.shape) * eps0 * part if name == "eps" else 0 * eps0
@@ -799,33 +818,33 @@ def run_ours_adjoint(args):
             dKn = rng.normal(size=Kn0.shape) * Kn0 if name == "Kn" else 0 * Kn0
             dKs = rng.normal(size=Ks0.shape) * Ks0 if name == "Ks" else 0 * Ks0
             ad = float(np.sum(gb["eps"] * dE) + np.sum(gb["mu"] * dmu) + np.sum(gb["Kn"] * dKn) + np.sum(gb["Ks"] * dKs))
-            row = {"param": name, "h": h, "adjoint": ad}
-            for mode, tag in ((AdjointWindow.BRANCH_FORCE, "forced"), (AdjointWindow.BRANCH_NATURAL, "natural")):
-                w.set_branches(mode)
-                vals, sigs, dis = [], [], 0
-                for sgn in (1, -1):
-                    w.set_materials(Kn0 + sgn * h * dKn, Ks0 + sgn * h * dKs, mu0 + sgn * h * dmu)
-                    w.set_eps(eps0 + sgn * h * dE)
-                    lv, sv = w.forward(fdw, args.checkpoint, wF, wX)
-                    vals.append(lv)
-                    sigs.append(sv)
-                    dis += w.branch_report()["disagreements"] if mode == AdjointWindow.BRANCH_FORCE else 0
-                f = (vals[0] - vals[1]) / (2 * h)
-                row[tag] = {"fd": f, "rel_err": abs(f - ad) / max(abs(ad), 1e-300)}
-                if tag == "forced":
-                    row[tag]["decisions_forced_against_their_natural_outcome"] = dis
-                    row[tag]["noise_bound_rel"] = noise / h / max(abs(ad), 1e-300)
-                else:
-                    row[tag]["same_branches"] = bool(sigs[0] == sigs[1] == sigb)
+            row = {"param": name, "adjoint": ad, "forced": {}}
+            for hh in scan:
+                f, _, dis, cross = central(AdjointWindow.BRANCH_FORCE, dE, dmu, dKn, dKs, hh)
+                row["forced"][f"{hh:.0e}"] = {"fd": f, "rel_err": abs(f - ad) / max(abs(ad), 1e-300),
+                                              "decisions_forced_against_their_natural_outcome": dis,
+                                              "pair_steps_crossing_a_surface_singularity": cross,
+                                              "noise_bound_rel": noise / hh / max(abs(ad), 1e-300)}
+            best = min(row["forced"], key=lambda x: row["forced"][x]["rel_err"])
+            row["forced_best"] = {"h": float(best), "rel_err": row["forced"][best]["rel_err"]}
+            f, sigs, _, _ = central(AdjointWindow.BRANCH_NATURAL, dE, dmu, dKn, dKs, h)
+            row["natural"] = {"h": h, "fd": f, "rel_err": abs(f - ad) / max(abs(ad), 1e-300),
+                              "same_branches": bool(sigs[0] == sigs[1] == sigb)}
             fd.append(row)
         w.set_branches(AdjointWindow.BRANCH_NATURAL)
-        forced_err = [x["forced"]["rel_err"] for x in fd]
-        fd_summary = {"directions": len(fd), "h_relative": h, "window_steps": fdw, "loss": Lb,
+        at_h = [x["forced"][f"{h:.0e}"] for x in fd]
+        fd_summary = {"directions": len(fd), "h_relative": h, "h_scanned": scan, "window_steps": fdw, "loss": Lb,
                       "decisions_per_run": decisions, "loss_rounding_noise": noise,
-                      "forced_within_1e-5": int(sum(e <= 1e-5 for e in forced_err)),
-                      "forced_max_rel_err": max(forced_err),
-                      "forced_within_1e-5_or_noise": int(sum(x["forced"]["rel_err"] <= 1e-5 + 2 * x["forced"]["noise_bound_rel"]
-                                                             for x in fd)),
+                      "forced_within_1e-5_at_h": int(sum(x["rel_err"] <= 1e-5 for x in at_h)),
+                      "forced_max_rel_err_at_h": max(x["rel_err"] for x in at_h),
+                      "forced_within_1e-5_or_noise_at_h": int(sum(x["rel_err"] <= 1e-5 + 2 * x["noise_bound_rel"]
+                                                                  for x in at_h)),
+                      "forced_at_h_without_surface_crossing": int(sum(x["pair_steps_crossing_a_surface_singularity"] == 0
+                                                                      for x in at_h)),
+                      "forced_within_1e-5_at_h_without_surface_crossing": int(sum(
+                          x["rel_err"] <= 1e-5 for x in at_h if x["pair_steps_crossing_a_surface_singularity"] == 0)),
+                      "forced_within_1e-5_best_h": int(sum(x["forced_best"]["rel_err"] <= 1e-5 for x in fd)),
+                      "forced_max_rel_err_best_h": max(x["forced_best"]["rel_err"] for x in fd),
                       "natural_same_branches": int(sum(x["natural"]["same_branches"] for x in fd)),
                       "natural_within_1e-5": int(sum(x["natural"]["rel_err"] <= 1e-5 for x in fd))}
     w.set_materials(Kn0, Ks0, mu0)
@@ -909,6 +928,8 @@ def main():
                     help="config3: shape of the reverse kernel (AdjointWindow.REPLAY_SHAPES; -1: time each, keep the fastest)")
     ap.add_argument("--replay-blocks", type=int, default=-1,
                     help="config3: resident blocks per SM of the reverse kernel (-1: time 1, 2, unbounded, keep the fastest)")
+    ap.add_argument("--fd-scan", default="1e-4,1e-5,1e-7,1e-8",
+                    help="config3: further relative steps of the forced central differences (comma-separated)")
     ap.add_argument("--fd-window", type=int, default=200,
                     help="config3: steps of the finite-difference check's window (at most --window)")
     ap.add_argument("--approach-max", type=int, default=1000,

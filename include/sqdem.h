@@ -432,8 +432,11 @@ sqdem_status sqdem_adj_set_replay_blocks(sqdem_adj* adj, int blocks_per_sm);
  * drops the recording. */
 sqdem_status sqdem_adj_set_branches(sqdem_adj* adj, int mode);
 /* Of the last forward run: decisions taken, forced decisions whose natural outcome differed,
- * decisions beyond the tape's 224 per pair and step (evaluated, not forced), steps recorded. */
-sqdem_status sqdem_adj_branch_report(sqdem_adj* adj, double* out4);
+ * decisions beyond the tape's 224 per pair and step (evaluated, not forced), steps recorded,
+ * and (forced runs) pair steps whose surface evaluations saw other signs of the local
+ * directions' components than the recorded run: the superquadric's support point has no
+ * derivative where such a component crosses 0, so no branch can be forced there. */
+sqdem_status sqdem_adj_branch_report(sqdem_adj* adj, double* out5);
 /* replay mismatches, Disfunction evaluations and LM calls of the forward run, pairs replayed,
  * forward ms, backward ms, steps, checkpoint interval */
 sqdem_status sqdem_adj_report(sqdem_adj* adj, double* out8);

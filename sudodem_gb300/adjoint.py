@@ -154,10 +154,13 @@ class AdjointWindow:
 
     def branch_report(self):
         """Of the last forward run: decisions taken, forced decisions whose natural outcome
-        differed, decisions beyond the tape (evaluated), steps recorded."""
-        out = np.zeros(4)
+        differed, decisions beyond the tape (evaluated), steps recorded, and pair steps whose
+        surface evaluations saw other signs of the local directions than the recorded run (a
+        non-differentiable point of the superquadric surface crossed)."""
+        out = np.zeros(5)
         self._check(self.lib.sqdem_adj_branch_report(self.h, _dp(out)))
-        return dict(zip(("decisions", "disagreements", "unforced", "steps_recorded"), out.astype(np.int64).tolist()))
+        return dict(zip(("decisions", "disagreements", "unforced", "steps_recorded", "surface_sign_changes"),
+                        out.astype(np.int64).tolist()))
 
     def set_forward(self, cooperative=True):
         """Forward kernel of the pairs: six lanes share each evaluation (default) or one thread

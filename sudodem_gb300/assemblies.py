@@ -200,11 +200,17 @@ def config3(seed=0, n=5000, spacing=3.45e-3, per_side=25):
     keeps collapsing for ~45,000 steps and its surface outruns a slowly loaded lid), on a 3.45 mm
     lattice (config 0's 2.6 mm lets two boxy particles, eps < 1 and bounding radius up to 1.7 mm,
     overlap at the start, which launches some at up to 2 m/s, 0.2 m high); one material per body
-    with friction 0.5 (the per-particle friction parameters).  The deposition and the lid
-    placement that precede the compression window are run by the caller (bench.py's config3
-    workload)."""
+    (the per-particle friction parameters) with friction coefficients U[0.45, 0.55] around config
+    0's 0.5: Ip2 gives a pair the smaller of its two friction angles, and with equal values every
+    pair sits at the tie of that min, where the loss has no derivative with respect to one
+    particle's friction (the one-sided derivatives differ), so the friction gradient needs
+    distinct values.  Walls keep 0.5.  The deposition and the lid placement that precede the
+    compression window are run by the caller (bench.py's config3 workload)."""
     spec = walled_lattice(n, seed=seed, box=(per_side + 1) * spacing, spacing=spacing)
-    return per_body_materials(spec)
+    mu = np.full(spec.n_bodies, 0.5)
+    part = spec.kind == 0
+    mu[part] = np.random.default_rng(seed + 7).uniform(0.45, 0.55, int(np.sum(part)))
+    return per_body_materials(spec, friction=mu)
 
 
 def deposition_box(n, seed=0, eps_range=(0.3, 1.8), r_range=(0.8e-3, 1.2e-3), log_radius=False, spacing=2.6e-3):

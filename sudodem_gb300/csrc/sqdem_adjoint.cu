@@ -242,21 +242,57 @@ template <class T> struct LMOut { V3<T> p1, p2, center, contact; bool touching; 
 // branch, the one whose derivative the reverse pass computes.  Each forced decision whose
 // natural outcome differs is counted.  The replay of the reverse pass evaluates its decisions
 // (NoBranch).
+//
+// The superquadric surface itself is not smooth everywhere: its support point, a signed power
+// sgn(x)|x|^(1/(2-e)) of the local direction's components, has an infinite derivative where a
+// component crosses 0 (e < 1) and no continuation through it.  Those points are not forced;
+// the tape keeps a hash of the signs of the local direction's components at every surface
+// evaluation of the step (in the order evaluated), and a forced run counts the pair steps whose
+// hash differs: a central difference across such a point is not a derivative.
 enum { BR_OFF = 0, BR_RECORD = 1, BR_FORCE = 2 };
-static const int BR_WORDS = 8;   // per pair and step: the number of decisions, then 7 words of outcomes
+// per pair and step: the number of decisions, the surface-sign hash, then 7 words of outcomes
+static const int BR_WORDS = 9;
+static const int BR_BITS = 32 * (BR_WORDS - 2);
+SQA_HD unsigned sgn3(double x, double y, double z) {
+  return (x > 0 ? 1u : (x < 0 ? 2u : 0u)) | (y > 0 ? 4u : (y < 0 ? 8u : 0u)) | (z > 0 ? 16u : (z < 0 ? 32u : 0u));
+}
 struct NoBranch {
   SQA_HD bool operator()(bool v) { return v; }
+  template <class T> SQA_HD void surf(const Shape<T>&, const Shape<T>&, const T&, const T&) {}
+  template <class T> SQA_HD void surf1(const Shape<T>&, const V3<T>&) {}
 };
 struct BrCur {
   unsigned* w;   // this pair's words of this step
   int mode, n, dis;
-  unsigned acc;
+  unsigned acc, cusp;
   bool writer;
+  // signs of the surface evaluation's local directions: the contact direction of the angles
+  // (pa0, pa1) in A's and B's frames
+  template <class T> SQA_HD void surf(const Shape<T>& A, const Shape<T>& B, const T& pa0, const T& pa1) {
+    if (mode == BR_OFF) return;
+    double s0, c0, s1, c1;
+    tsincos(val(pa0), &s0, &c0);
+    tsincos(val(pa1), &s1, &c1);
+    const V3<double> d = mk<double>(c0 * c1, s0 * c1, s1);
+    Rot<double> R;
+    for (int k = 0; k < 9; k++) R.m[k] = val(A.R.m[k]);
+    const V3<double> la = mulL(R, d);
+    for (int k = 0; k < 9; k++) R.m[k] = val(B.R.m[k]);
+    const V3<double> lb = mulL(R, d);
+    cusp = cusp * 0x9E3779B1u + (sgn3(la.x, la.y, la.z) | sgn3(lb.x, lb.y, lb.z) << 6) + 1u;
+  }
+  template <class T> SQA_HD void surf1(const Shape<T>& B, const V3<T>& dir) {
+    if (mode == BR_OFF) return;
+    Rot<double> R;
+    for (int k = 0; k < 9; k++) R.m[k] = val(B.R.m[k]);
+    const V3<double> lb = mulL(R, vval(dir));
+    cusp = cusp * 0x9E3779B1u + sgn3(lb.x, lb.y, lb.z) + 1u;
+  }
   SQA_HD bool operator()(bool v) {
     if (mode == BR_OFF) return v;
     const int k = n++;
-    if (k >= 32 * (BR_WORDS - 1)) return v;   // beyond the tape: evaluated (counted as unforced)
-    const int word = 1 + (k >> 5), bit = k & 31;
+    if (k >= BR_BITS) return v;   // beyond the tape: evaluated (counted as unforced)
+    const int word = 2 + (k >> 5), bit = k & 31;
     if (mode == BR_RECORD) {
       acc |= (unsigned)v << bit;
       if (bit == 31) {
@@ -286,6 +322,7 @@ __host__ __device__ __noinline__ void lmder2(const Shape<T>& A, const Shape<T>& 
   V3<T> P1, P2, C;
   o.contact = zero3<T>();
   ev(A, B, p[0], p[1], C, P1, P2, stop_flag);
+  br.surf(A, B, p[0], p[1]);
   V3<T> pf = P2 - P1;
   T pfL2 = nrm(pf);
   if (br(!isfinite(val(pfL2)))) stop = 7;
@@ -299,8 +336,10 @@ __host__ __device__ __noinline__ void lmder2(const Shape<T>& A, const Shape<T>& 
     const double angle = val(dot(pf, o.contact)) / (val(nrm(pf)) * val(nrm(o.contact)));
     if (br(fabs(angle) > 0.95)) { stop = 8; break; }
     ev(A, B, p[0] + Dp0, p[1], C, P1, P2, stop_flag);
+    br.surf(A, B, p[0] + Dp0, p[1]);
     const V3<T> f1 = P2 - P1;
     ev(A, B, p[0], p[1] + Dp1, C, P1, P2, stop_flag);
+    br.surf(A, B, p[0], p[1] + Dp1);
     const V3<T> f2 = P2 - P1;
     o.evals += 2;
     const T J00 = (f1.x - pf.x) / Dp0, J10 = (f1.y - pf.y) / Dp0, J20 = (f1.z - pf.z) / Dp0;
@@ -326,6 +365,7 @@ __host__ __device__ __noinline__ void lmder2(const Shape<T>& A, const Shape<T>& 
       const T q0 = p[0] + Dp0, q1 = p[1] + Dp1;
       if (br(DpL2 >= (val(pL2) + 1e-3) / (1e-12 * 1e-12))) { stop = 4; break; }
       ev(A, B, q0, q1, C, P1, P2, stop_flag);
+      br.surf(A, B, q0, q1);
       o.evals++;
       const V3<T> pDp_f = P2 - P1;
       const T pDp_fL2 = nrm(pDp_f);
@@ -411,6 +451,7 @@ SQA_HD void geomWallSq(Geom<T>& g, bool isNew, double prevDepth, int PA, double 
   V3<double> nd = mk<double>(0.0, 0.0, 0.0);
   if (PA == 0) nd.x = sense; else if (PA == 1) nd.y = sense; else nd.z = sense;
   const V3<T> normal = lift<T>(nd);
+  br.surf1(B, normal);
   const V3<T> point2 = mulG(B.R, supportLocal(B, -mulL(B.R, normal))) + B.pos;
   V3<T> p1 = point2;
   if (PA == 0) p1.x = T(wallc); else if (PA == 1) p1.y = T(wallc); else p1.z = T(wallc);
@@ -520,7 +561,7 @@ SQA_HD void rotStep(const T q[4], const V3<T>& L, const V3<T>& M, double4 I, dou
 // Device data
 enum : int { CF_GEOM = 1 };                 // flag: Interaction::geom present
 enum : int { CO_PRE = 1, CO_FORCE = 2, CO_ANG = 4, CO_ANG0 = 8, CO_NEW = 16, CO_SHNEW = 32, CO_SLIDE = 64 };
-enum { A_MISMATCH = 0, A_EVALS, A_LMCALLS, A_REPLAYED, A_SIG, A_SIGB, A_BRDEC, A_BRDIS, A_BRUNF, A_NCOUNT };
+enum { A_MISMATCH = 0, A_EVALS, A_LMCALLS, A_REPLAYED, A_SIG, A_SIGB, A_BRDEC, A_BRDIS, A_BRUNF, A_BRCUSP, A_NCOUNT };
 
 struct Consts {
   int nb, P;
@@ -660,7 +701,7 @@ SQA_HD void fwdContact(const Consts& C, const State& S, const StepOut& O, int st
   loadPair(C, S, c, p);
   Geom<double> g;
   BrCur br;
-  br.mode = C.brMode; br.n = 0; br.dis = 0; br.acc = 0u; br.writer = writer;
+  br.mode = C.brMode; br.n = 0; br.dis = 0; br.acc = 0u; br.cusp = 0u; br.writer = writer;
   br.w = C.brMode != BR_OFF ? C.brPair + ((size_t)step * C.P + c) * BR_WORDS : nullptr;
   pairGeom<double>(p, g, 0, ev, br);
   if (!writer) return;
@@ -691,14 +732,16 @@ SQA_HD void fwdContact(const Consts& C, const State& S, const StepOut& O, int st
   // The contact gate and the Coulomb cap are continuous (kinks), so they are not recorded.
   SQA_CNT(&C.cnt[A_SIG], branchHash(c, step, (unsigned long long)g.evals | ((unsigned long long)g.calls << 20)));
   if (br.mode != BR_OFF) {
-    const int cap = 32 * (BR_WORDS - 1);
     if (br.mode == BR_RECORD) {
-      if ((br.n & 31) && br.n < cap) br.w[1 + (br.n >> 5)] = br.acc;
+      if ((br.n & 31) && br.n < BR_BITS) br.w[2 + (br.n >> 5)] = br.acc;
       br.w[0] = (unsigned)br.n;
+      br.w[1] = br.cusp;
+    } else if (br.w[1] != br.cusp) {
+      SQA_CNT(&C.cnt[A_BRCUSP], 1);
     }
     SQA_CNT(&C.cnt[A_BRDEC], br.n);
     if (br.dis) SQA_CNT(&C.cnt[A_BRDIS], br.dis);
-    if (br.n > cap) SQA_CNT(&C.cnt[A_BRUNF], br.n - cap);
+    if (br.n > BR_BITS) SQA_CNT(&C.cnt[A_BRUNF], br.n - BR_BITS);
   }
 }
 __global__ void __launch_bounds__(128) k_fwd_contacts(Consts C, State S, StepOut O, int step) {
@@ -1687,10 +1730,11 @@ sqdem_status sqdem_adj_set_branches(sqdem_adj* a, int mode) {
   return SQDEM_OK;
 }
 
-sqdem_status sqdem_adj_branch_report(sqdem_adj* a, double* out4) {
-  if (!a || !out4) return SQDEM_ERR_ARG;
-  out4[0] = (double)a->counters[A_BRDEC]; out4[1] = (double)a->counters[A_BRDIS];
-  out4[2] = (double)a->counters[A_BRUNF]; out4[3] = (double)a->brSteps;
+sqdem_status sqdem_adj_branch_report(sqdem_adj* a, double* out5) {
+  if (!a || !out5) return SQDEM_ERR_ARG;
+  out5[0] = (double)a->counters[A_BRDEC]; out5[1] = (double)a->counters[A_BRDIS];
+  out5[2] = (double)a->counters[A_BRUNF]; out5[3] = (double)a->brSteps;
+  out5[4] = (double)a->counters[A_BRCUSP];
   return SQDEM_OK;
 }
 

@@ -18,13 +18,13 @@ extern "C" sqdem_status sqdem_shape_props(double rx, double ry, double rz, doubl
 // branch tape of the host window (sqdem_adj_set_branches' modes), kept between runs
 static int g_brMode = BR_OFF, g_brSteps = 0;
 static std::vector<unsigned> g_brPair, g_brBody;
-static double g_brReport[4] = {0, 0, 0, 0};
+static double g_brReport[5] = {0, 0, 0, 0, 0};
 extern "C" int adjh_set_branches(int mode) {
   if (mode < BR_OFF || mode > BR_FORCE || (mode == BR_FORCE && g_brSteps == 0)) return 1;
   g_brMode = mode;
   return 0;
 }
-extern "C" void adjh_branch_report(double* out4) { for (int k = 0; k < 4; k++) out4[k] = g_brReport[k]; }
+extern "C" void adjh_branch_report(double* out5) { for (int k = 0; k < 5; k++) out5[k] = g_brReport[k]; }
 extern "C" double adjh_run(int n, const int* kind, const double* shape5, const int* was, const int* mat,
                            const double* state37, long npairs, const double* intr57, double dt, const double* g3,
                            double damping, int nmat, const double* Kn, const double* Ks, const double* fa,
@@ -117,7 +117,7 @@ extern "C" double adjh_run(int n, const int* kind, const double* shape5, const i
   }
   sigOut[0] = cnt[A_SIG] + cnt[A_SIGB];
   g_brReport[0] = (double)cnt[A_BRDEC]; g_brReport[1] = (double)cnt[A_BRDIS]; g_brReport[2] = (double)cnt[A_BRUNF];
-  g_brReport[3] = g_brSteps;
+  g_brReport[3] = g_brSteps; g_brReport[4] = (double)cnt[A_BRCUSP];
   C.brMode = BR_OFF;   // the reverse pass evaluates its decisions
   // backward
   std::vector<double4> lPos(wX), lOri(n), lVel(n), lW(n), lL(n), lF(n), lT(n), lN(P + 1), lS(P + 1), con(8 * (size_t)P + 8),

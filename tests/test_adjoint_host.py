@@ -139,9 +139,10 @@ def test_host_reverse_pass_matches_oracle_central_differences(host, scene):
 
 
 def _branch_report(lib):
-    out = np.zeros(4)
+    out = np.zeros(5)
     lib.adjh_branch_report(out.ctypes.data_as(C.POINTER(C.c_double)))
-    return dict(zip(("decisions", "disagreements", "unforced", "steps"), out.astype(np.int64).tolist()))
+    return dict(zip(("decisions", "disagreements", "unforced", "steps", "surface_sign_changes"),
+                    out.astype(np.int64).tolist()))
 
 
 def test_host_forced_branches_central_differences_at_the_relative_step_1e_6(host, scene):
