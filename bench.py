@@ -627,14 +627,14 @@ def run_ours(args):
 def config3_start(args):
     """Start of the config-3 window on the GPU engine: the specimen deposited for
     --deposit-steps steps; the lid placed 0.05 mm above the highest particle's centre plus its
-    largest half-axis and lowered at 0.05 m/s until its force has stayed above 0.5 N (about
-    the bed's weight) for ten checks in a row (100 steps apart); every velocity zeroed
-    (NewtonIntegrator.quiet_system_flag); then the lid servo-controlled to the preload
-    --lid-force (every 20 steps its velocity set to 2e-3 m/s per N of error of the force averaged
-    over the last five checks, at most 2 mm/s either way) until that force has stayed within 10%
-    of the preload for 25 checks in a row; then
-    the lid set to the window's compression velocity (0.05/s x its height).  The window starts
-    from the quasi-static, preloaded bed."""
+    largest half-axis, lowered at 0.1 m/s to its first contact (checked every 20 steps) and then
+    at 0.05 m/s until its force has stayed above 0.5 N (about the bed's weight) for ten checks
+    in a row (100 steps apart); every velocity zeroed (NewtonIntegrator.quiet_system_flag); then
+    the lid servo-controlled to the preload --lid-force (every 20 steps its velocity set to 5e-3
+    m/s per N of error of the force averaged over the last five checks, at most 3 mm/s either
+    way) until that force has stayed within 10% of the preload for 25 checks in a row (or
+    --servo-max checks); then the lid set to the window's compression velocity (0.05/s x its
+    height).  The window starts from the quasi-static, preloaded bed."""
     from sudodem_gb300 import Engine, assemblies
     spec = assemblies.config3(seed=args.seed, n=args.particles)
     eng = Engine(device=0)
@@ -643,6 +643,13 @@ def config3_start(args):
     b = eng.body_state()
     part = spec.kind == 0
     b[5, 2] = float(np.max(b[part, 2] + np.max(spec.shape5[part, 0:3], axis=1))) + 0.05e-3
+    b[5, 7:10] = [0.0, 0.0, -0.1]
+    eng.put_body_state(b)
+    k0 = 0
+    while k0 < 5 * args.approach_max and abs(eng.body_state()[5, 18]) == 0.0:   # to the first contact
+        eng.step(20)
+        k0 += 1
+    b = eng.body_state()
     b[5, 7:10] = [0.0, 0.0, -0.05]
     eng.put_body_state(b)
     held, k = 0, 0
@@ -652,7 +659,7 @@ def config3_start(args):
         held = held + 1 if abs(eng.body_state()[5, 18]) > 0.5 else 0
     eng.set_quiet(True)      # zeroes every body's velocity, the lid's too
     eng.step(1)
-    target, gain, vmax = args.lid_force, 2e-3, 2e-3
+    target, gain, vmax = args.lid_force, 5e-3, 3e-3
     held, k2, hist = 0, 0, []
     while held < 25 and k2 < args.servo_max:
         b = eng.body_state()
@@ -672,7 +679,8 @@ def config3_start(args):
     recs = eng.interactions(include_potential=True)
     eng.close()
     lid = recs[(recs[:, 0] == 5) | (recs[:, 1] == 5)]
-    return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_steps": 100 * k, "servo_steps": 20 * k2,
+    return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_fast_steps": 20 * k0, "lid_steps": 100 * k,
+                           "servo_steps": 20 * k2,
                            "servo_converged": bool(held >= 25), "preload_n": target, "lid_height_m": height,
                            "lid_velocity_m_s": -0.05 * height, "lid_force_n": force0,
                            "lid_pairs": int(len(lid)), "lid_pairs_touching": int(np.sum(lid[:, 4] > 0))}
@@ -934,7 +942,7 @@ def main():
                     help="config3: steps of the finite-difference check's window (at most --window)")
     ap.add_argument("--approach-max", type=int, default=1000,
                     help="config3: at most this many 100-step checks while the lid is lowered onto the bed")
-    ap.add_argument("--lid-force", type=float, default=1.0, help="config3: lid preload (N) at the window's start")
+    ap.add_argument("--lid-force", type=float, default=0.3, help="config3: lid preload (N) at the window's start")
     ap.add_argument("--servo-max", type=int, default=5000,
                     help="config3: at most this many 20-step servo checks while the lid is brought to its preload")
     ap.add_argument("--loss-heights", action="store_true", help="config3: add the particles' mean final height to the loss")
