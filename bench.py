@@ -627,14 +627,14 @@ def run_ours(args):
 def config3_start(args):
     """Start of the config-3 window on the GPU engine: the specimen deposited for
     --deposit-steps steps; the lid placed 0.05 mm above the highest particle's centre plus its
-    largest half-axis, lowered at 0.1 m/s to its first contact (checked every 20 steps) and then
-    at 0.05 m/s until its force has stayed above 0.5 N (about the bed's weight) for ten checks
-    in a row (100 steps apart); every velocity zeroed (NewtonIntegrator.quiet_system_flag); then
-    the lid servo-controlled to the preload --lid-force (every 20 steps its velocity set to 5e-3
-    m/s per N of error of the force averaged over the last five checks, at most 3 mm/s either
-    way) until that force has stayed within 10% of the preload for 25 checks in a row (or
-    --servo-max checks); then the lid set to the window's compression velocity (0.05/s x its
-    height).  The window starts from the quasi-static, preloaded bed."""
+    largest half-axis (above every particle: a particle behind a wall would read as deeply
+    penetrating it) and lowered at 0.1 m/s, sweeping any particle still in flight ahead of it,
+    until its force has stayed above 0.5 N (about the bed's weight) for three checks in a row
+    (20 steps apart); every velocity zeroed (NewtonIntegrator.quiet_system_flag); then the lid
+    set to the window's compression velocity (0.05/s x its height) and the compression run for
+    --precompress-steps steps.  The window is a slice of that ongoing quasi-static compression
+    (a lid held at a preload by a servo oscillated against the stiff top contacts, and a bed
+    left under a slow lid right after a fast approach kept moving away from it)."""
     from sudodem_gb300 import Engine, assemblies
     spec = assemblies.config3(seed=args.seed, n=args.particles)
     eng = Engine(device=0)
@@ -645,44 +645,29 @@ def config3_start(args):
     b[5, 2] = float(np.max(b[part, 2] + np.max(spec.shape5[part, 0:3], axis=1))) + 0.05e-3
     b[5, 7:10] = [0.0, 0.0, -0.1]
     eng.put_body_state(b)
-    k0 = 0
-    while k0 < 5 * args.approach_max and abs(eng.body_state()[5, 18]) == 0.0:   # to the first contact
-        eng.step(20)
-        k0 += 1
-    b = eng.body_state()
-    b[5, 7:10] = [0.0, 0.0, -0.05]
-    eng.put_body_state(b)
     held, k = 0, 0
-    while held < 10 and k < args.approach_max:
-        eng.step(100)
+    while held < 3 and k < args.approach_max:
+        eng.step(20)
         k += 1
         held = held + 1 if abs(eng.body_state()[5, 18]) > 0.5 else 0
     eng.set_quiet(True)      # zeroes every body's velocity, the lid's too
     eng.step(1)
-    target, gain, vmax = args.lid_force, 5e-3, 3e-3
-    held, k2, hist = 0, 0, []
-    while held < 25 and k2 < args.servo_max:
-        b = eng.body_state()
-        hist = (hist + [abs(b[5, 18])])[-5:]
-        F = float(np.mean(hist))     # the lid force averaged over the last five checks
-        held = held + 1 if abs(F - target) <= 0.1 * target else 0
-        b[5, 7:10] = [0.0, 0.0, -float(np.clip(gain * (target - F), -vmax, vmax))]
-        eng.put_body_state(b)
-        eng.step(20)
-        k2 += 1
     b = eng.body_state()
     height = float(b[5, 2] - b[4, 2])
-    force0 = float(abs(b[5, 18]))
     b[5, 7:10] = [0.0, 0.0, -0.05 * height]
     eng.put_body_state(b)
+    trace = []
+    for k2 in range(0, args.precompress_steps, 10000):
+        eng.step(min(10000, args.precompress_steps - k2))
+        trace.append(round(float(abs(eng.body_state()[5, 18])), 4))
     b = eng.body_state()
+    force0 = float(abs(b[5, 18]))
     recs = eng.interactions(include_potential=True)
     eng.close()
     lid = recs[(recs[:, 0] == 5) | (recs[:, 1] == 5)]
-    return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_fast_steps": 20 * k0, "lid_steps": 100 * k,
-                           "servo_steps": 20 * k2,
-                           "servo_converged": bool(held >= 25), "preload_n": target, "lid_height_m": height,
-                           "lid_velocity_m_s": -0.05 * height, "lid_force_n": force0,
+    return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_steps": 20 * k, "lid_reached": bool(held >= 3),
+                           "precompress_steps": args.precompress_steps, "lid_force_every_10000_steps_n": trace,
+                           "lid_height_m": height, "lid_velocity_m_s": -0.05 * height, "lid_force_n": force0,
                            "lid_pairs": int(len(lid)), "lid_pairs_touching": int(np.sum(lid[:, 4] > 0))}
 
 
@@ -802,7 +787,7 @@ def run_ours_adjoint(args):
         part = (spec.kind == 0)[:, None]
         kinds = ("eps", "mu", "Kn", "Ks")
         h = args.fd_h
-        scan = sorted({h, *[float(x) for x in args.fd_scan.split(",") if x]}, reverse=True)
+        scan = sorted({h, h / 2, *[float(x) for x in args.fd_scan.split(",") if x]}, reverse=True)
 
         def central(mode, dE, dmu, dKn, dKs, hh):
             w.set_branches(mode)
@@ -835,6 +820,10 @@ def run_ours_adjoint(args):
                                               "noise_bound_rel": noise / hh / max(abs(ad), 1e-300)}
             best = min(row["forced"], key=lambda x: row["forced"][x]["rel_err"])
             row["forced_best"] = {"h": float(best), "rel_err": row["forced"][best]["rel_err"]}
+            # Richardson extrapolation of the central differences at h and h/2 (their error is
+            # c h^2 on a smooth branch): (4 D(h/2) - D(h)) / 3
+            rich = (4 * row["forced"][f"{h / 2:.0e}"]["fd"] - row["forced"][f"{h:.0e}"]["fd"]) / 3
+            row["forced_richardson"] = {"h": h, "fd": rich, "rel_err": abs(rich - ad) / max(abs(ad), 1e-300)}
             f, sigs, _, _ = central(AdjointWindow.BRANCH_NATURAL, dE, dmu, dKn, dKs, h)
             row["natural"] = {"h": h, "fd": f, "rel_err": abs(f - ad) / max(abs(ad), 1e-300),
                               "same_branches": bool(sigs[0] == sigs[1] == sigb)}
@@ -851,6 +840,7 @@ def run_ours_adjoint(args):
                                                                       for x in at_h)),
                       "forced_within_1e-5_at_h_without_surface_crossing": int(sum(
                           x["rel_err"] <= 1e-5 for x in at_h if x["pair_steps_crossing_a_surface_singularity"] == 0)),
+                      "forced_richardson_within_1e-5": int(sum(x["forced_richardson"]["rel_err"] <= 1e-5 for x in fd)),
                       "forced_within_1e-5_best_h": int(sum(x["forced_best"]["rel_err"] <= 1e-5 for x in fd)),
                       "forced_max_rel_err_best_h": max(x["forced_best"]["rel_err"] for x in fd),
                       "natural_same_branches": int(sum(x["natural"]["same_branches"] for x in fd)),
@@ -940,11 +930,10 @@ def main():
                     help="config3: further relative steps of the forced central differences (comma-separated)")
     ap.add_argument("--fd-window", type=int, default=200,
                     help="config3: steps of the finite-difference check's window (at most --window)")
-    ap.add_argument("--approach-max", type=int, default=1000,
-                    help="config3: at most this many 100-step checks while the lid is lowered onto the bed")
-    ap.add_argument("--lid-force", type=float, default=0.3, help="config3: lid preload (N) at the window's start")
-    ap.add_argument("--servo-max", type=int, default=5000,
-                    help="config3: at most this many 20-step servo checks while the lid is brought to its preload")
+    ap.add_argument("--approach-max", type=int, default=20000,
+                    help="config3: at most this many 20-step checks while the lid is lowered onto the bed")
+    ap.add_argument("--precompress-steps", type=int, default=200000,
+                    help="config3: steps of the compression at 0.05/s before the window")
     ap.add_argument("--loss-heights", action="store_true", help="config3: add the particles' mean final height to the loss")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -593,6 +593,7 @@ struct Adj {
   double4* con;                                       // per pair: 8 double4 (x q v w of id1, then of id2)
   double4 *accEps, *accPhys;                          // per pair parameter adjoints (e1a e2a e1b e2b | kn ks tanphi)
   const double4 *wF, *wX;
+  const int* order;   // the reverse step's pair order (longest forward search first), or null
 };
 
 SQA_HD void loadQ(double4 o, double q[4]) { q[0] = o.x; q[1] = o.y; q[2] = o.z; q[3] = o.w; }
@@ -725,7 +726,8 @@ SQA_HD void fwdContact(const Consts& C, const State& S, const StepOut& O, int st
   S.flag[c] |= CF_GEOM;
   S.depth[c] = g.depth;
   S.shear[c] = d4(sOut, 0);
-  O.Fv[c] = Fv; O.cp[c] = cp; O.code[c] = code;
+  // bits 16-30: the step's Disfunction evaluations (the reverse step's cost, for its ordering)
+  O.Fv[c] = Fv; O.cp[c] = cp; O.code[c] = code | (g.evals < 0x7FFF ? g.evals : 0x7FFF) << 16;
   SQA_CNT(&C.cnt[A_EVALS], g.evals);
   SQA_CNT(&C.cnt[A_LMCALLS], g.calls);
   // the decisions at which the map jumps: the Levenberg-Marquardt path (evaluations, calls).
@@ -1087,8 +1089,9 @@ __global__ void __launch_bounds__(32 * GRP_WARPS) k_bwd_contacts_grp(Consts C, S
   // grid-stride over the pairs: the launch sizes the grid so that the lanes' local memory (the
   // replayed state, a few KB per lane) of the resident blocks stays in L2
   for (int c0 = blockIdx.x * GRP_WARPS * GPW; c0 < C.P; c0 += gridDim.x * GRP_WARPS * GPW) {
-  const int c = c0 + warp * GPW + gw;
-  const bool active = laneOn && c < C.P;
+  const int i = c0 + warp * GPW + gw;
+  const bool active = laneOn && i < C.P;
+  const int c = active && A.order ? A.order[i] : i;
   PairAdjIn q;
   Geom<Dual<TG>> gd;
   if (active) {
@@ -1146,6 +1149,43 @@ SQA_HD void bwdGather(const Consts& C, const Adj& A, int b) {
 __global__ void __launch_bounds__(128) k_bwd_gather(Consts C, Adj A) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b < C.nb) bwdGather(C, A, b);
+}
+
+// Order of a reverse step's pairs: a counting sort on the forward step's evaluation counts,
+// longest first, so that the longest replays start in the first wave and pairs of similar
+// length share a warp.  Each pair's reverse step writes only its own outputs, so the order
+// changes no result.  Buckets: 64 - min(63, evals / 4), i.e. bucket 1 holds 252+ evaluations.
+static const int ORD_BUCKETS = 64;
+SQA_HD int ordBucket(int code) {
+  const int ev = code >> 16;
+  return ORD_BUCKETS - 1 - (ev / 4 < ORD_BUCKETS - 1 ? ev / 4 : ORD_BUCKETS - 1);
+}
+__global__ void __launch_bounds__(256) k_order_count(int P, const int* code, int* cnt) {
+  __shared__ int sh[ORD_BUCKETS];
+  for (int k = threadIdx.x; k < ORD_BUCKETS; k += blockDim.x) sh[k] = 0;
+  __syncthreads();
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < P; c += gridDim.x * blockDim.x)
+    atomicAdd(&sh[ordBucket(code[c])], 1);
+  __syncthreads();
+  for (int k = threadIdx.x; k < ORD_BUCKETS; k += blockDim.x)
+    if (sh[k]) atomicAdd(&cnt[k], sh[k]);
+}
+// exclusive scan of the bucket counts into the write cursors (one warp pair of 64 threads)
+__global__ void __launch_bounds__(ORD_BUCKETS) k_order_scan(int* cnt) {
+  __shared__ int sh[ORD_BUCKETS];
+  const int t = threadIdx.x;
+  sh[t] = cnt[t];
+  __syncthreads();
+  if (t == 0) {
+    int run = 0;
+    for (int k = 0; k < ORD_BUCKETS; k++) { const int v = sh[k]; sh[k] = run; run += v; }
+  }
+  __syncthreads();
+  cnt[t] = sh[t];
+}
+__global__ void __launch_bounds__(256) k_order_scatter(int P, const int* code, int* cursor, int* order) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < P; c += gridDim.x * blockDim.x)
+    order[atomicAdd(&cursor[ordBucket(code[c])], 1)] = c;
 }
 
 }  // namespace sqadj
@@ -1217,6 +1257,7 @@ struct sqdem_adj {
   double4 *lN = nullptr, *lS = nullptr, *con = nullptr, *accEps = nullptr, *accPhys = nullptr;
   double4 *wF = nullptr, *wX = nullptr;
   double* lossD = nullptr;
+  int *order = nullptr, *orderCnt = nullptr;   // reverse-step pair order and its bucket counters
   // the last forward window
   int nsteps = 0, every = 0;
   bool haveForward = false;
@@ -1256,6 +1297,7 @@ static void afreeAll(sqdem_adj* a) {
   a->ckpt.clear(); a->tapeState.clear();
   a->init = a->work = a->fin = nullptr; a->finFv = nullptr; a->tapeCap = 0;
   a->brPair = a->brBody = nullptr; a->brCap = 0; a->brSteps = 0;
+  a->order = a->orderCnt = nullptr;
 }
 static void afree(sqdem_adj* a, void* p) {
   if (!p) return;
@@ -1283,6 +1325,7 @@ static Adj adjView(sqdem_adj* a) {
   A.lPos = a->lPos; A.lOri = a->lOri; A.lVel = a->lVel; A.lW = a->lW; A.lL = a->lL; A.lF = a->lF; A.lT = a->lT;
   A.lAng = a->lAng; A.lN = a->lN; A.lS = a->lS; A.con = a->con; A.accEps = a->accEps; A.accPhys = a->accPhys;
   A.wF = a->wF; A.wX = a->wX;
+  A.order = nullptr;
   return A;
 }
 static inline int nblk(int n, int bs) { return n > 0 ? (n + bs - 1) / bs : 1; }
@@ -1319,8 +1362,17 @@ static sqdem_status ensureTape(sqdem_adj* a, int K) {
 
 // shapes of the pairs' reverse step: 0 one thread (17 tangents), 1: 3 lanes x 6, 2: 2 lanes x 9,
 // 3: 6 lanes x 3
-static void launchReplay(sqdem_adj* a, const Consts& C, const State& S, const StepOut& O, const Adj& A) {
+static void launchReplay(sqdem_adj* a, const Consts& C, const State& S, const StepOut& O, const Adj& A0) {
   const int P = a->P, bs = 32 * GRP_WARPS;
+  Adj A = A0;
+  if (a->order && a->replay != 0 && P > 0) {
+    const int g = std::min(nblk(P, 256), 4 * a->numSMs);
+    cudaMemsetAsync(a->orderCnt, 0, ORD_BUCKETS * sizeof(int), a->st);
+    k_order_count<<<g, 256, 0, a->st>>>(P, O.code, a->orderCnt);
+    k_order_scan<<<1, ORD_BUCKETS, 0, a->st>>>(a->orderCnt);
+    k_order_scatter<<<g, 256, 0, a->st>>>(P, O.code, a->orderCnt, a->order);
+    A.order = a->order;
+  }
   // blocks of the grouped kernels: a->replayBlocks per SM (grid-stride), 0 = one block per
   // group of pairs (as many resident as fit: their local memory spills past L2 to DRAM)
   auto grid = [&](int perBlock) {
@@ -1457,6 +1509,7 @@ sqdem_status sqdem_adj_load(sqdem_adj* a, int n, const int* kind, const double* 
   ACUDA(aalloc(a, &a->lAng, P)); ACUDA(aalloc(a, &a->lN, P)); ACUDA(aalloc(a, &a->lS, P));
   ACUDA(aalloc(a, &a->con, 8 * (size_t)P)); ACUDA(aalloc(a, &a->accEps, P)); ACUDA(aalloc(a, &a->accPhys, P));
   ACUDA(aalloc(a, &a->wF, n)); ACUDA(aalloc(a, &a->wX, n)); ACUDA(aalloc(a, &a->lossD, 1));
+  ACUDA(aalloc(a, &a->order, (size_t)P + 1)); ACUDA(aalloc(a, &a->orderCnt, ORD_BUCKETS));
   ACUDA(cudaMemcpyAsync(a->shp, hShp.data(), n * sizeof(double4), cudaMemcpyHostToDevice, a->st));
   ACUDA(cudaMemcpyAsync(a->massI, hMI.data(), n * sizeof(double4), cudaMemcpyHostToDevice, a->st));
   ACUDA(cudaMemcpyAsync(a->eps, hEps.data(), n * sizeof(double2), cudaMemcpyHostToDevice, a->st));
