@@ -626,22 +626,30 @@ def run_ours(args):
 
 def config3_start(args):
     """Start of the config-3 window on the GPU engine: the specimen deposited for
-    --deposit-steps steps; the lid placed 0.05 mm above the highest particle's centre plus its
-    largest half-axis (above every particle: a particle behind a wall would read as deeply
-    penetrating it) and lowered at 0.1 m/s, sweeping any particle still in flight ahead of it,
-    until its force has stayed above 0.5 N (about the bed's weight) for three checks in a row
-    (20 steps apart); every velocity zeroed (NewtonIntegrator.quiet_system_flag); then the lid
-    set to the window's compression velocity (0.05/s x its height) and the compression run for
-    --precompress-steps steps.  The window is a slice of that ongoing quasi-static compression
-    (a lid held at a preload by a servo oscillated against the stiff top contacts, and a bed
-    left under a slow lid right after a fast approach kept moving away from it)."""
+    --deposit-steps steps and settled by --settle-rounds rounds of zeroed velocities
+    (NewtonIntegrator.quiet_system_flag) 2,000 steps apart (with no viscous contact damping the
+    collapsed column keeps bouncing at a few cm/s for hundreds of thousands of steps); the lid
+    placed 0.05 mm above the highest particle's centre plus its largest half-axis (above every
+    particle: a particle behind a wall would read as deeply penetrating it) and lowered at
+    0.1 m/s, sweeping any particle still in flight ahead of it, until its force has stayed above
+    0.5 N (about the bed's weight) for three checks in a row (20 steps apart); every velocity
+    zeroed; then the lid brought to the preload --lid-force by a one-sided servo (every 20 steps
+    it moves down at 5e-3 m/s per N of missing force, at most 1.5 mm/s, and stands still when the
+    force is reached, so that it never pulls away from the bed) until the force has stayed above
+    80% of the preload for 50 checks in a row (or --servo-max checks); then the lid set to the
+    window's compression velocity (0.05/s x its height) for --precompress-steps steps.  The
+    window is a slice of that ongoing compression."""
     from sudodem_gb300 import Engine, assemblies
     spec = assemblies.config3(seed=args.seed, n=args.particles)
     eng = Engine(device=0)
     eng.load(spec)
     eng.step(args.deposit_steps)
+    for _ in range(args.settle_rounds):
+        eng.set_quiet(True)
+        eng.step(2000)
     b = eng.body_state()
     part = spec.kind == 0
+    vp99 = float(np.percentile(np.linalg.norm(b[part, 7:10], axis=1), 99))
     b[5, 2] = float(np.max(b[part, 2] + np.max(spec.shape5[part, 0:3], axis=1))) + 0.05e-3
     b[5, 7:10] = [0.0, 0.0, -0.1]
     eng.put_body_state(b)
@@ -650,22 +658,35 @@ def config3_start(args):
         eng.step(20)
         k += 1
         held = held + 1 if abs(eng.body_state()[5, 18]) > 0.5 else 0
+    reached = held >= 3
     eng.set_quiet(True)      # zeroes every body's velocity, the lid's too
     eng.step(1)
+    target, gain, vmax = args.lid_force, 5e-3, 1.5e-3
+    held, k2 = 0, 0
+    while held < 50 and k2 < args.servo_max:
+        b = eng.body_state()
+        F = abs(b[5, 18])
+        held = held + 1 if F >= 0.8 * target else 0
+        b[5, 7:10] = [0.0, 0.0, -float(min(vmax, gain * max(0.0, target - F)))]
+        eng.put_body_state(b)
+        eng.step(20)
+        k2 += 1
     b = eng.body_state()
     height = float(b[5, 2] - b[4, 2])
     b[5, 7:10] = [0.0, 0.0, -0.05 * height]
     eng.put_body_state(b)
     trace = []
-    for k2 in range(0, args.precompress_steps, 10000):
-        eng.step(min(10000, args.precompress_steps - k2))
+    for k3 in range(0, args.precompress_steps, 10000):
+        eng.step(min(10000, args.precompress_steps - k3))
         trace.append(round(float(abs(eng.body_state()[5, 18])), 4))
     b = eng.body_state()
     force0 = float(abs(b[5, 18]))
     recs = eng.interactions(include_potential=True)
     eng.close()
     lid = recs[(recs[:, 0] == 5) | (recs[:, 1] == 5)]
-    return spec, b, recs, {"deposit_steps": args.deposit_steps, "lid_steps": 20 * k, "lid_reached": bool(held >= 3),
+    return spec, b, recs, {"deposit_steps": args.deposit_steps, "settle_rounds": args.settle_rounds,
+                           "particle_speed_p99_after_settling_m_s": vp99, "lid_steps": 20 * k, "lid_reached": bool(reached),
+                           "servo_steps": 20 * k2, "servo_held": bool(held >= 50), "preload_n": target,
                            "precompress_steps": args.precompress_steps, "lid_force_every_10000_steps_n": trace,
                            "lid_height_m": height, "lid_velocity_m_s": -0.05 * height, "lid_force_n": force0,
                            "lid_pairs": int(len(lid)), "lid_pairs_touching": int(np.sum(lid[:, 4] > 0))}
@@ -918,7 +939,7 @@ def main():
     ap.add_argument("--window", type=int, default=2000, help="config3: steps of the differentiated window")
     ap.add_argument("--checkpoint", type=int, default=100, help="config3: steps between checkpoints")
     ap.add_argument("--particles", type=int, default=5000, help="config3: particles")
-    ap.add_argument("--deposit-steps", type=int, default=90000, help="config3: deposition steps before the window")
+    ap.add_argument("--deposit-steps", type=int, default=200000, help="config3: deposition steps before the window")
     ap.add_argument("--fd-dirs", type=int, default=0,
                     help="config3: finite-difference directions, cycling over eps, mu, Kn, Ks")
     ap.add_argument("--fd-h", type=float, default=1e-6, help="config3: relative finite-difference step")
@@ -932,8 +953,13 @@ def main():
                     help="config3: steps of the finite-difference check's window (at most --window)")
     ap.add_argument("--approach-max", type=int, default=20000,
                     help="config3: at most this many 20-step checks while the lid is lowered onto the bed")
-    ap.add_argument("--precompress-steps", type=int, default=200000,
+    ap.add_argument("--precompress-steps", type=int, default=50000,
                     help="config3: steps of the compression at 0.05/s before the window")
+    ap.add_argument("--settle-rounds", type=int, default=10,
+                    help="config3: rounds of zeroed velocities, 2,000 steps apart, after the deposition")
+    ap.add_argument("--lid-force", type=float, default=0.5, help="config3: lid preload (N) before the compression")
+    ap.add_argument("--servo-max", type=int, default=10000,
+                    help="config3: at most this many 20-step checks while the lid is brought to its preload")
     ap.add_argument("--loss-heights", action="store_true", help="config3: add the particles' mean final height to the loss")
     args = ap.parse_args()
     if args.warmup < 3:
