@@ -725,7 +725,7 @@ def run_ours_adjoint(args):
     loss1, _ = w.forward(1, 1, wF, wX)
     shapes = {}
     nt = min(args.window, 50)
-    for shape in ((1, 2, 3, 0, 4, 5) if args.replay_shape < 0 else (args.replay_shape,)):
+    for shape in ((1, 2, 3, 0) if args.replay_shape < 0 else (args.replay_shape,)):
         w.set_replay(shape)
         w.forward(nt, min(args.checkpoint, nt), wF, wX)
         w.backward()

@@ -413,9 +413,8 @@ sqdem_status sqdem_adj_get_pairs(sqdem_adj* adj, double* out16);
 sqdem_status sqdem_adj_set_forward(sqdem_adj* adj, int cooperative);
 /* Shape of the pairs' reverse-step kernel, which replays each pair's narrowphase and law in
  * dual numbers: 0 one thread per pair with all seventeen tangent components, 1 three lanes with
- * six each, 2 two lanes with nine, 3 (default) six lanes with three; 4 and 5 are shapes 3 and 1
- * compiled for three resident blocks per SM (fewer registers, more local memory).  Every shape
- * gives bitwise the same gradients. */
+ * six each, 2 two lanes with nine, 3 (default) six lanes with three.  Every shape gives bitwise
+ * the same gradients. */
 sqdem_status sqdem_adj_set_replay(sqdem_adj* adj, int shape);
 /* Resident blocks per SM of the grouped reverse-step kernels (grid-stride over the pairs;
  * default 1): each lane keeps its replayed state in local memory (a few KB), and bounding the

@@ -132,8 +132,7 @@ class AdjointWindow:
         self._check(self.lib.sqdem_adj_get_state(self.h, _dp(out)))
         return out
 
-    REPLAY_SHAPES = {0: "1 lane x 17 tangents", 1: "3 lanes x 6", 2: "2 lanes x 9", 3: "6 lanes x 3",
-                     4: "6 lanes x 3, 3 blocks/SM", 5: "3 lanes x 6, 3 blocks/SM"}
+    REPLAY_SHAPES = {0: "1 lane x 17 tangents", 1: "3 lanes x 6", 2: "2 lanes x 9", 3: "6 lanes x 3"}
 
     def set_replay(self, shape=3):
         """Shape of the pairs' reverse-step kernel (REPLAY_SHAPES); the gradients are bitwise the

@@ -1076,8 +1076,8 @@ __global__ void __launch_bounds__(64) k_bwd_contacts(Consts C, State S, StepOut 
 // component is computed by the same operations as in k_bwd_contacts, so the results are
 // bitwise the same for every shape.
 static const int GRP_WARPS = 4;
-template <int TG, int GL, int MINB = 1>
-__global__ void __launch_bounds__(32 * GRP_WARPS, MINB) k_bwd_contacts_grp(Consts C, State S, StepOut O, Adj A) {
+template <int TG, int GL>
+__global__ void __launch_bounds__(32 * GRP_WARPS) k_bwd_contacts_grp(Consts C, State S, StepOut O, Adj A) {
   constexpr int GPW = 32 / GL;
   __shared__ double shLin[GRP_WARPS * GPW][2 * NT];
   __shared__ double shGs[GRP_WARPS * GPW][NT];
@@ -1383,9 +1383,6 @@ static void launchReplay(sqdem_adj* a, const Consts& C, const State& S, const St
     case 0: k_bwd_contacts<<<nblk(P, 64), 64, 0, a->st>>>(C, S, O, A); break;
     case 2: k_bwd_contacts_grp<9, 2><<<grid(GRP_WARPS * 16), bs, 0, a->st>>>(C, S, O, A); break;
     case 1: k_bwd_contacts_grp<6, 3><<<grid(GRP_WARPS * 10), bs, 0, a->st>>>(C, S, O, A); break;
-    // register-capped forms (3 blocks of 128 threads per SM: 168 registers, more local memory)
-    case 4: k_bwd_contacts_grp<3, 6, 3><<<grid(GRP_WARPS * 5), bs, 0, a->st>>>(C, S, O, A); break;
-    case 5: k_bwd_contacts_grp<6, 3, 3><<<grid(GRP_WARPS * 10), bs, 0, a->st>>>(C, S, O, A); break;
     default: k_bwd_contacts_grp<3, 6><<<grid(GRP_WARPS * 5), bs, 0, a->st>>>(C, S, O, A); break;
   }
 }
@@ -1743,7 +1740,7 @@ sqdem_status sqdem_adj_set_forward(sqdem_adj* a, int cooperative) {
 }
 
 sqdem_status sqdem_adj_set_replay(sqdem_adj* a, int shape) {
-  if (!a || shape < 0 || shape > 5) return SQDEM_ERR_ARG;
+  if (!a || shape < 0 || shape > 3) return SQDEM_ERR_ARG;
   a->replay = shape;
   return SQDEM_OK;
 }

@@ -276,7 +276,7 @@ def test_replay_shapes_agree_bitwise(scene, window):
     wF = lid_weights(n)
     wX = np.random.default_rng(3).normal(size=(n, 3)) * (spec.kind == 0)[:, None]
     res = []
-    for shape, blocks in ((0, 1), (1, 1), (2, 1), (3, 1), (3, 0), (3, 2), (1, 0), (4, 0), (5, 0), (4, 1)):
+    for shape, blocks in ((0, 1), (1, 1), (2, 1), (3, 1), (3, 0), (3, 2), (1, 0)):
         window.set_replay(shape)
         window.set_replay_blocks(blocks)   # resident blocks per SM of the grouped kernels
         _gpu_loss(window, spec, eps, mu, Kn, Ks, wF, wX)
