@@ -202,3 +202,33 @@ def test_host_forced_branches_central_differences_at_the_relative_step_1e_6(host
     print(f"forced central differences at h=1e-6: {within}/20 within 1e-5 (worst {worst:.2e}, rounding noise of "
           f"the loss {noise:.1e}); {natural_left}/20 directions left a recorded branch when evaluated naturally")
     assert within >= 15 and natural_left > 0
+
+
+def test_host_forced_differences_converge_as_h_squared(host, scene):
+    """On the recorded branch the map is smooth: the error of forced central differences along
+    an exponent direction falls as h^2 (the central difference's own truncation) while the
+    natural runs would have changed hundreds of decisions at the larger steps."""
+    spec, bodies, recs = scene
+    eps, mu, Kn, Ks = params_of(spec)
+    n = spec.n_bodies
+    wF, wX = lid_weights(n), np.zeros((n, 3))
+    try:
+        assert host.adjh_set_branches(1) == 0
+        _, _, _, gr, _ = _run(host, spec, bodies, recs, eps, mu, Kn, Ks, NSTEPS, wF, wX)
+        assert host.adjh_set_branches(2) == 0
+        dE = np.random.default_rng(7).normal(size=eps.shape) * eps * (spec.kind == 0)[:, None]
+        ad = float(np.sum(gr["eps"] * dE))
+        errs, dis = [], []
+        for h in (1e-4, 1e-5):
+            vals = []
+            for sgn in (1, -1):
+                Ls, _, _, _, _ = _run(host, spec, bodies, recs, eps + sgn * h * dE, mu, Kn, Ks, NSTEPS, wF, wX)
+                vals.append(Ls)
+                dis.append(_branch_report(host)["disagreements"])
+            errs.append(abs((vals[0] - vals[1]) / (2 * h) - ad) / abs(ad))
+    finally:
+        host.adjh_set_branches(0)
+    print(f"forced central differences along eps: rel. error {errs[0]:.2e} at h=1e-4, {errs[1]:.2e} at 1e-5; "
+          f"decisions forced against their natural outcome {dis}")
+    assert max(dis[:2]) > 100
+    assert 1e-2 / 3 <= errs[1] / errs[0] <= 3e-2
