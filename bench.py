@@ -157,15 +157,17 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic_per_pair():
-    """dram bytes per table entry of one k_contacts launch from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "k_contacts_periodic100k.txt")
-    if not os.path.exists(p):
-        return None
-    for ln in open(p):
-        if ln.startswith("dram_bytes_per_entry:"):
-            return float(ln.split(":")[1])
-    return None
+def profiled_search_traffic(workload):
+    """DRAM bytes (read + write) per launch of each form's search kernel, from the committed ncu
+    summary of that workload (one capture at full size); {} where none was captured."""
+    p = os.path.join(ROOT, "profiles", f"traffic_search_kernels_{workload}.md")
+    out = {}
+    if os.path.exists(p):
+        for ln in open(p):
+            if ln.startswith("dram_bytes_per_launch "):
+                form, v = ln.split()[1], ln.split()[2]
+                out[form] = float(v)
+    return out
 
 
 def cpu_baseline(spec, budget_s=20.0, threads=None):
@@ -565,6 +567,7 @@ def run_ours(args):
     res = {p: measure_form(spec, p, args, rank, ws, dist) for p in forms}
     peaks = _native.pipe_peaks(0)
     flops = pipe_flops_per_eval()
+    traffic = profiled_search_traffic(args.workload)
     # the roofline of each form's dominant kernel (the search kernel): issue-bound on the pipe
     # its evaluations run on (FP64 for k_contacts_lm; FP32 for the double-float
     # k_contacts_lm_ff), against this GPU's measured FMA peak of that pipe
@@ -581,7 +584,7 @@ def run_ours(args):
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if achieved is not None else None,
                          "peak_source": "measured on this GPU by sqdem_pipe_peaks (FMA loop of that pipe)",
-                         "traffic": None, "launch_ms": kms, "evaluations_per_launch": ev,
+                         "traffic": traffic.get(p), "launch_ms": kms, "evaluations_per_launch": ev,
                          "flops_per_evaluation": fpe,
                          "evaluation_rate": rate, "peak_evaluation_rate": peak_eval,
                          "evaluation_rate_frac": rate / peak_eval if peak_eval else None,
