@@ -4,7 +4,8 @@ specimen (tests/servo_protocol.py) for seeds 1-5, and for the same seeds with a 
 (contact stiffness kn x 1.3, so stresses at a given strain are 30% higher), which the
 statistics test must tell apart from the correct oracle.
 
-Run: python tests/golden/make_compression_stats.py [threads]   (a few hours on 8 cores)
+Run: python tests/golden/make_compression_stats.py [threads]   (about an hour on 8 cores; keys already
+present in the file are kept, so a partial run resumes)
 """
 import json
 import os
